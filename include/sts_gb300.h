@@ -1,0 +1,110 @@
+/*
+ * C ABI of the GB300 SIMPLE-TS time step (libsts_gb300.so).
+ *
+ * The reference solver (SIMPLE_TS_MPI.cpp) has no library interface: its seam
+ * is the process and the files in its working directory.  EnteredData.txt and
+ * the body files go in (SIMPLE_TS_MPI.cpp:5241-5561, Objects_for_Solving.h:306-412),
+ * the field dumps u/v/p/Temper/vol_inf_fb come out (SIMPLE_TS_MPI.cpp:5564-5731),
+ * and the time loop of main() (SIMPLE_TS_MPI.cpp:3230-4691) does the work.  The
+ * entry points below replace that loop and keep the file formats.
+ *
+ * Conventions: plain pointers and sizes; fields are double[Nx*Ny] with
+ * index i + j*Nx (x fastest), exactly the reference's layout.  Every call
+ * returns STS_OK (0) or a negative STS_ERR_* code; sts_last_error() gives the
+ * message of the last failure on the calling thread.  A context owns its
+ * device buffers and one CUDA stream; one context must not be used from two
+ * threads at once, different contexts are independent.  Host buffers are
+ * owned by the caller and only copied.
+ */
+#ifndef STS_GB300_H
+#define STS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define STS_OK 0
+#define STS_ERR_ARG (-1)       /* bad argument or unknown field name */
+#define STS_ERR_INPUT (-2)     /* missing or malformed case file */
+#define STS_ERR_CUDA (-3)      /* CUDA runtime error (no device, launch failure, ...) */
+#define STS_ERR_NONFINITE (-4) /* a residual went NaN/Inf during the steps just taken */
+
+typedef struct sts_ctx sts_ctx;
+
+typedef struct sts_options {
+  /* 1: the sweep loop runs exactly N_I_p_c sweeps (the shipped build, FIXED_NUMBER_OF_ITERATIONS_LOOP_3
+   *    defined, SIMPLE_TS_MPI.cpp:56 and :4099-4100);
+   * 0: it stops on MaxError_p_c / MaxError_T after at least 2 sweeps (SIMPLE_TS_MPI.cpp:4101-4106). */
+  int fixed_sweeps;
+  /* 1: run the steps as one CUDA graph with conditional nodes (no host round trip per sweep);
+   * 0: launch kernel by kernel from the host. */
+  int use_graph;
+  /* CUDA device ordinal. */
+  int device;
+  /* 1: sts_run_case writes dumps and logs into the case directory like the reference. */
+  int write_files;
+} sts_options;
+
+/* Fills *opt with the defaults (fixed_sweeps 1, use_graph 1, device 0, write_files 1). */
+void sts_default_options(sts_options* opt);
+
+/* Reads a case directory (EnteredData.txt, solve_*_b.txt, restart dumps when
+ * ToReadSolvedDataFromFile = 1) and prepares the device state up to the first
+ * time step.  Replaces main() up to the time loop, SIMPLE_TS_MPI.cpp:1796-3227. */
+int sts_open_case(const char* case_dir, const sts_options* opt, sts_ctx** out);
+
+/* Advances up to nsteps time steps (SIMPLE_TS_MPI.cpp:3230-4691 per step).  Stops
+ * early when the reference's continue rule ends the run (Nt reached or the
+ * steady-state stop MaxError_to_stop_program, SIMPLE_TS_MPI.cpp:4442-4449);
+ * *steps_done (optional) receives the count taken. */
+int sts_step(sts_ctx* ctx, int nsteps, int* steps_done);
+
+/* Copies a field to host memory.  Names: u v p T rho sqrt_T rho_u rho_v Fx Fy D_ux D_uy
+ * D_vx D_vy DTx DTy Gamma_xf Gamma_yf ScT1 apx apy bpx bpy u_pseudo v_pseudo d_p_c_12
+ * d_p_c_34 Tw_u Tw_v (Nx*Ny doubles); hx x_v (Nx); hy y_v (Ny). */
+int sts_get_field(sts_ctx* ctx, const char* name, double* host_out);
+
+/* Overwrites u, v, p or T from host memory (Nx*Ny doubles); rho and sqrt_T follow on the next step. */
+int sts_set_field(sts_ctx* ctx, const char* name, const double* host_in);
+
+/* Mesh size. */
+int sts_dims(sts_ctx* ctx, int* Nx, int* Ny);
+
+/* Statistics of the last step: [Iter, Iter_p_c, res_p first sweep, res_p last sweep,
+ * res_T first, res_T last, res_u, res_v, time] (the numbers of Tmp.txt, SIMPLE_TS_MPI.cpp:5887-5928). */
+int sts_stats(sts_ctx* ctx, double* out9);
+
+/* Jacobi sweeps taken by each of the last steps (oldest first, at most cap, at most 4096). */
+int sts_sweep_history(sts_ctx* ctx, unsigned int* out, int cap, int* n_out);
+
+/* Applies the output-time wall-temperature overwrite and writes u.bin v.bin p.bin
+ * Temper.bin vol_inf_fb.bin it_begin.txt into the case directory (WriteSolvedDataToFile,
+ * SIMPLE_TS_MPI.cpp:5564-5731). */
+int sts_write_outputs(sts_ctx* ctx);
+
+/* Whole drop-in run of a case directory: open, step until the run ends, with the
+ * periodic saves and logs of the reference (Tmp.txt, Iterations_in_loops.txt), and the
+ * final dumps.  Equivalent to running the serial reference binary in case_dir. */
+int sts_run_case(const char* case_dir, const sts_options* opt);
+
+/* Synchronises the context's stream (the steps are asynchronous otherwise). */
+int sts_sync(sts_ctx* ctx);
+
+/* Releases the device buffers. */
+void sts_destroy(sts_ctx* ctx);
+
+/* Message of the last failure on this thread ("" if none). */
+const char* sts_last_error(void);
+
+/* Host-only inspection of a case directory (no device use): dims, obstacle ids
+ * (vol_inf_fb, Nx*Ny), per-cell classes (Nx*Ny bytes: bits 0-1 u, 2-3 v, 4-5 p/T with
+ * 0 unsolved, 1 interior, 2 boundary; bit 6 fluid) and the mesh (hx, x_v: Nx; hy, y_v: Ny).
+ * Pass NULL for outputs not wanted; call once with all NULL to learn the dims. */
+int sts_inspect_case(const char* case_dir, int* Nx, int* Ny, unsigned int* vol_out, unsigned char* cls_out,
+                     double* hx_out, double* hy_out, double* xv_out, double* yv_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* STS_GB300_H */

@@ -1959,6 +1959,20 @@ int ora_get(ora_handle* h, const char* name, double* out) {
   return 0;
 }
 
+// The interior/boundary lists encoded one byte per cell: bits 0-1 u, 2-3 v, 4-5 p/T
+// (1 = interior list, 2 = boundary list), bit 6 fluid.
+int ora_get_class(ora_handle* h, unsigned char* out) {
+  Oracle& o = h->o;
+  for (uint c = 0; c < o.Na; c++) out[c] = o.vol[c] ? 0x40 : 0;
+  for (uint n : o.nch_u) out[n] |= 1;
+  for (uint n : o.bc_u) out[n] |= 2;
+  for (uint n : o.nch_v) out[n] |= 1 << 2;
+  for (uint n : o.bc_v) out[n] |= 2 << 2;
+  for (uint n : o.nch_o) out[n] |= 1 << 4;
+  for (uint n : o.bc_o) out[n] |= 2 << 4;
+  return 0;
+}
+
 int ora_get_mask(ora_handle* h, unsigned int* out) {
   std::memcpy(out, h->o.vol_inf_fb.data(), sizeof(unsigned int) * h->o.Na);
   return 0;

@@ -1,0 +1,961 @@
+// FP64 kernels of the SIMPLE-TS time step, bit-exact with the reference CPU solver.
+//
+// This translation unit is compiled with --fmad=false: every expression keeps the
+// reference's operand order and rounding (no fused multiply-add), and division and
+// sqrt are IEEE round-to-nearest, so each field matches the serial reference
+// solver bit for bit.  One thread owns one cell (i, j); a per-cell class byte
+// says which of the reference's two formula variants applies (interior list
+// "nch" or boundary list "bc", SIMPLE_TS_MPI.cpp:8581-9063).
+//
+// Kernels per outer iteration: assemble -> sweep x S -> correct -> face_rho ->
+// boundary -> flux_diff.  The sweep count S is decided on the device by the last
+// block of each sweep (SIMPLE_TS_MPI.cpp:4099-4107), which also drives the CUDA
+// graph's conditional WHILE node.
+#include <cuda_runtime.h>
+
+#include "sts_common.cuh"
+#include "sts_kernels.h"
+
+namespace sts {
+
+namespace {
+
+__device__ __forceinline__ double dmax0(double a, double b) { return a > b ? a : b; }
+__device__ __forceinline__ double upwind_rho(double r0, double r1, double v1) {
+  return (v1 == 0) ? (0.5 * (r0 + r1)) : ((v1 > 0) ? r0 : r1);
+}
+__device__ __forceinline__ double Li(double f1, double f2, double h1, double h2) {
+  return (f1 * h2 + f2 * h1) / (h1 + h2);
+}
+__device__ __forceinline__ double Hi(double f1, double f2, double h1, double h2) {
+  return (h1 + h2) * f1 * f2 / (h1 * f2 + h2 * f1);
+}
+__device__ __forceinline__ double as_d(unsigned long long b) { return __longlong_as_double((long long)b); }
+__device__ __forceinline__ unsigned long long as_b(double d) { return (unsigned long long)__double_as_longlong(d); }
+
+// Running maximum that ignores NaN exactly like "if (m < fabs(r)) m = fabs(r)".
+__device__ __forceinline__ double mx(double m, double x) { return (m < x) ? x : m; }
+
+// Block-wide max of two non-negative values, folded into global maxima by bit pattern
+// (for non-negative IEEE doubles the bit patterns order like the values).
+__device__ void block_max2(double a, double b, unsigned long long* ga, unsigned long long* gb, unsigned int* status) {
+  __shared__ double sa[32], sb[32];
+  const int lane = (threadIdx.x + threadIdx.y * blockDim.x) & 31;
+  const int warp = (threadIdx.x + threadIdx.y * blockDim.x) >> 5;
+  const int nw = (blockDim.x * blockDim.y + 31) >> 5;
+  if (!(a <= 1.7976931348623157e308) && a == a) atomicOr(status, 1u);  // +inf
+  if (a != a || b != b) atomicOr(status, 1u);                           // NaN
+  for (int o = 16; o > 0; o >>= 1) {
+    a = mx(a, __shfl_xor_sync(0xffffffffu, a, o));
+    b = mx(b, __shfl_xor_sync(0xffffffffu, b, o));
+  }
+  if (lane == 0) { sa[warp] = a; sb[warp] = b; }
+  __syncthreads();
+  if (warp == 0) {
+    a = lane < nw ? sa[lane] : 0.0;
+    b = lane < nw ? sb[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      a = mx(a, __shfl_xor_sync(0xffffffffu, a, o));
+      b = mx(b, __shfl_xor_sync(0xffffffffu, b, o));
+    }
+    if (lane == 0) {
+      if (a > 0) atomicMax(ga, as_b(a));
+      if (b > 0) atomicMax(gb, as_b(b));
+    }
+  }
+}
+
+// True for exactly one thread in the grid: the last thread (0,0) of the last block to finish.
+__device__ bool last_block(unsigned int* counter) {
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    __threadfence();
+    const unsigned int nb = gridDim.x * gridDim.y;
+    const unsigned int t = atomicAdd(counter, 1u);
+    last = (t == nb - 1);
+    if (last) *counter = 0;
+  }
+  __syncthreads();
+  return last && threadIdx.x == 0 && threadIdx.y == 0;
+}
+
+struct Cell {
+  int i, j, ij;
+  bool ok;
+};
+__device__ __forceinline__ Cell cell(const Geo& g) {
+  Cell c;
+  c.i = blockIdx.x * blockDim.x + threadIdx.x;
+  c.j = blockIdx.y * blockDim.y + threadIdx.y;
+  c.ok = c.i < g.Nx && c.j < g.Ny;
+  c.ij = c.i + c.j * g.Nx;
+  return c;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// start of a time step: *_pr copies and per-step counters (SIMPLE_TS_MPI.cpp:3233-3260)
+// ---------------------------------------------------------------------------
+__global__ void k_step_begin(Geo g, int counters, unsigned long long h_outer, int in_graph) {
+  Cell c = cell(g);
+  Ctl* ctl = g.ctl;
+  const unsigned cur = ctl->cur;
+  if (c.ok) {
+    g.u_pr[c.ij] = g.u[c.ij];
+    g.v_pr[c.ij] = g.v[c.ij];
+    g.p_pr[c.ij] = g.p[cur][c.ij];
+    g.T_pr[c.ij] = g.T[cur][c.ij];
+    g.rho_pr[c.ij] = g.rho[c.ij];
+  }
+  if (counters && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    if (in_graph) cudaGraphSetConditional((cudaGraphConditionalHandle)h_outer, 1);
+    for (unsigned k = 0; k < ctl->Iter && k < 64; k++) {
+      ctl->res_p[k] = 0; ctl->res_T[k] = 0; ctl->res_p0[k] = 0; ctl->res_T0[k] = 0; ctl->sweeps[k] = 0;
+    }
+    ctl->it += g.ht;
+    ctl->it_counter++;
+    ctl->Iter_pr2 = ctl->Iter_pr1;
+    ctl->Iter_pr1 = ctl->Iter;
+    ctl->Iter = 0;
+    ctl->continue_iter = 1;
+    ctl->step_sweeps = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// momentum coefficients (u: SIMPLE_TS_MPI.cpp:3269-3344 bc, :3478-3545 nch;
+// v: :3373-3450 bc, :3561-3630 nch) and the energy source ScT1 (:3655-3756)
+// ---------------------------------------------------------------------------
+__global__ void k_assemble(Geo g, unsigned long long h_sweep, int in_graph) {
+  Cell c = cell(g);
+  Ctl* ctl = g.ctl;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    ctl->Iter_p_c = 0;
+    ctl->pt_done = 0;
+    ctl->res_bits_p = 0;
+    ctl->res_bits_T = 0;
+    ctl->res_bits_u = 0;
+    ctl->res_bits_v = 0;
+    if (in_graph) cudaGraphSetConditional((cudaGraphConditionalHandle)h_sweep, 1);
+  }
+  if (!c.ok) return;
+  const uint8_t cl = g.cls[c.ij];
+  if (!(cl & 0x3F)) return;
+  const int i = c.i, j = c.j, Nx = g.Nx;
+  const Nb d = neighbours(i, j, g.Nx, g.Ny, g.bits & F_PERIODIC);
+  const double cT = ctl->cT, cPch = ctl->cPch, ht = g.ht;
+  const double* __restrict__ hx = g.hx;
+  const double* __restrict__ hy = g.hy;
+  const double* __restrict__ u = g.u;
+  const double* __restrict__ v = g.v;
+  const double* __restrict__ Fx = g.Fx;
+  const double* __restrict__ Fy = g.Fy;
+  const double* __restrict__ sT = g.sqrt_T;
+  const double* __restrict__ rho = g.rho;
+  const double* __restrict__ rho_pr = g.rho_pr;
+  auto B = [&](int k) -> double { return cls_fluid(g.cls[k]) ? 1.0 : 0.0; };
+  auto BB = [&](int k) -> bool { return cls_fluid(g.cls[k]); };
+
+  const int cu = cls_u(cl);
+  if (cu) {
+    const double F_xu1 = 0.5 * (Fx[d.i_1j] + Fx[d.ij]);
+    const double F_xu2 = 0.5 * (Fx[d.ij] + Fx[d.i1j]);
+    double Scu;
+    if (cu == CLS_BC) {
+      Scu = cT * (B(d.i1j) * u[d.i1j] * sT[d.ij] * hy[j] / (hx[i] * 3.0) +
+                  B(d.i_2j) * u[d.i_1j] * sT[d.i_1j] * hy[j] / (hx[d.i_1] * 3.0) +
+                  g.Gamma_yf[d.ij1] * (v[d.ij1] * B(d.ij1) - v[d.i_1j1] * B(d.i_1j1)) -
+                  g.Gamma_yf[d.ij] * (v[d.ij] * B(d.ij_1) - v[d.i_1j] * B(d.i_1j_1)) -
+                  sT[d.ij] * (v[d.ij1] * B(d.ij1) - v[d.ij] * B(d.ij_1)) * 2.0 / 3.0 +
+                  sT[d.i_1j] * (v[d.i_1j1] * B(d.i_1j1) - v[d.i_1j] * B(d.i_1j_1)) * 2.0 / 3.0);
+    } else {
+      Scu = cT * (u[d.i1j] * sT[d.ij] * hy[j] / (hx[i] * 3.0) + u[d.i_1j] * sT[d.i_1j] * hy[j] / (hx[d.i_1] * 3.0) +
+                  g.Gamma_yf[d.ij1] * (v[d.ij1] - v[d.i_1j1]) - g.Gamma_yf[d.ij] * (v[d.ij] - v[d.i_1j]) -
+                  sT[d.ij] * (v[d.ij1] - v[d.ij]) * 2.0 / 3.0 + sT[d.i_1j] * (v[d.i_1j1] - v[d.i_1j]) * 2.0 / 3.0);
+    }
+    const double Spu = -(g.D_ux[d.ij] + g.D_ux[d.i1j]) / 3.0;
+    const double au1 = dmax0(0, F_xu1) + g.D_ux[d.ij];
+    const double au2 = dmax0(0, -F_xu2) + g.D_ux[d.i1j];
+    const double au3 = 0.5 * (dmax0(0, Fy[d.i_1j]) + dmax0(0, Fy[d.ij])) + g.D_uy[d.ij];
+    const double au4 = 0.5 * (dmax0(0, -Fy[d.i_1j1]) + dmax0(0, -Fy[d.ij1])) + g.D_uy[d.ij1];
+    const double bu3 = (rho_pr[d.i_1j] * hx[d.i_1] + rho_pr[d.ij] * hx[i]) * g.u_pr[d.ij] * hy[j] * 0.5 / ht + Scu;
+    const double au0 = au1 + au2 + au3 + au4 + 0.5 * (-Fy[d.i_1j] - Fy[d.ij] + Fy[d.i_1j1] + Fy[d.ij1]) + F_xu2 - F_xu1 -
+                       Spu + (rho[d.i_1j] * hx[d.i_1] + rho[d.ij] * hx[i]) * hy[j] * 0.5 / ht;
+    double up;
+    if (cu == CLS_BC)
+      up = (au1 * B(d.i1j) * u[d.i_1j] + au2 * B(d.i_2j) * u[d.i1j] + au3 * u[d.ij_1] + au4 * u[d.ij1] + bu3) / au0;
+    else
+      up = (au1 * u[d.i_1j] + au2 * u[d.i1j] + au3 * u[d.ij_1] + au4 * u[d.ij1] + bu3) / au0;
+    const double dpc = cPch * hy[j] / au0;
+    const double hr = hy[j] * g.rho_u[d.ij];
+    g.u_pseudo[d.ij] = up;
+    g.d12[d.ij] = dpc;
+    g.apx[d.ij] = dpc * hr;
+    g.bpx[d.ij] = (cu == CLS_BC) ? B(d.i_1j) * B(d.ij) * hr * up : hr * up;
+  }
+
+  const int cv = cls_v(cl);
+  if (cv) {
+    const int jm = j - ((j - 1) >= 0 ? 1 : 0);
+    const int far = d.ij_1 - ((j - 2) >= 0 ? Nx : 0);
+    const double F_yv3 = 0.5 * (Fy[d.ij_1] + Fy[d.ij]);
+    const double F_yv4 = 0.5 * (Fy[d.ij] + Fy[d.ij1]);
+    double Scv;
+    if (cv == CLS_BC) {
+      Scv = cT * (B(d.ij1) * v[d.ij1] * sT[d.ij] * hx[i] / (hy[j] * 3.0) +
+                  B(far) * v[d.ij_1] * sT[d.ij_1] * hx[i] / (hy[jm] * 3.0) +
+                  g.Gamma_xf[d.i1j] * (u[d.i1j] * B(d.i1j) - u[d.i1j_1] * B(d.i1j_1)) -
+                  g.Gamma_xf[d.ij] * (u[d.ij] * B(d.i_1j) - u[d.ij_1] * B(d.i_1j_1)) -
+                  sT[d.ij] * (u[d.i1j] * B(d.i1j) - u[d.ij] * B(d.i_1j)) * 2.0 / 3.0 +
+                  sT[d.ij_1] * (u[d.i1j_1] * B(d.i1j_1) - u[d.ij_1] * B(d.i_1j_1)) * 2.0 / 3.0) -
+            g.c_Fr_v * (rho[d.ij_1] * hx[i] * 0.5 * hy[jm] + rho[d.ij] * hx[i] * 0.5 * hy[j]);
+    } else {
+      Scv = cT * (v[d.ij1] * sT[d.ij] * hx[i] / (hy[j] * 3.0) + v[d.ij_1] * sT[d.ij_1] * hx[i] / (hy[j - 1] * 3.0) +
+                  g.Gamma_xf[d.i1j] * (u[d.i1j] - u[d.i1j_1]) - g.Gamma_xf[d.ij] * (u[d.ij] - u[d.ij_1]) -
+                  sT[d.ij] * (u[d.i1j] - u[d.ij]) * 2.0 / 3.0 + sT[d.ij_1] * (u[d.i1j_1] - u[d.ij_1]) * 2.0 / 3.0) -
+            g.c_Fr_v * (rho[d.ij_1] * hx[i] * 0.5 * hy[j - 1] + rho[d.ij] * hx[i] * 0.5 * hy[j]);
+    }
+    const double Spv = -(g.D_vy[d.ij] + g.D_vy[d.ij1]) / 3.0;
+    const double av1 = 0.5 * (dmax0(0, Fx[d.ij]) + dmax0(0, Fx[d.ij_1])) + g.D_vx[d.ij];
+    const double av2 = 0.5 * (dmax0(0, -Fx[d.i1j]) + dmax0(0, -Fx[d.i1j_1])) + g.D_vx[d.i1j];
+    const double av3 = dmax0(0, F_yv3) + g.D_vy[d.ij];
+    const double av4 = dmax0(0, -F_yv4) + g.D_vy[d.ij1];
+    const double bv3 = (rho_pr[d.ij_1] * hy[j - 1] + rho_pr[d.ij] * hy[j]) * g.v_pr[d.ij] * hx[i] * 0.5 / ht + Scv;
+    const double av0 = av1 + av2 + av3 + av4 + 0.5 * (Fx[d.i1j] - Fx[d.ij] + Fx[d.i1j_1] - Fx[d.ij_1]) + F_yv4 - F_yv3 -
+                       Spv + (rho[d.ij_1] * hy[j - 1] + rho[d.ij] * hy[j]) * hx[i] * 0.5 / ht;
+    double vp;
+    if (cv == CLS_BC)
+      vp = (av1 * v[d.i_1j] + av2 * v[d.i1j] + av3 * B(far) * v[d.ij_1] + av4 * B(d.ij1) * v[d.ij1] + bv3) / av0;
+    else
+      vp = (av1 * v[d.i_1j] + av2 * v[d.i1j] + av3 * v[d.ij_1] + av4 * v[d.ij1] + bv3) / av0;
+    const double dpc = cPch * hx[i] / av0;
+    const double hr = hx[i] * g.rho_v[d.ij];
+    g.v_pseudo[d.ij] = vp;
+    g.d34[d.ij] = dpc;
+    g.apy[d.ij] = dpc * hr;
+    g.bpy[d.ij] = (cv == CLS_BC) ? B(d.ij - Nx) * B(d.ij) * hr * vp : hr * vp;
+  }
+
+  const int co = cls_o(cl);
+  if (co) {
+    const int jm = j - (0 < j ? 1 : 0), jp = j + (j < (Nx - 1) ? 1 : 0);  // j is compared with Nx here (:3677)
+    double dudx, dvdy, s0, s1, s2, s3;
+    if (co == CLS_BC) {
+      dudx = (B(d.i1j) * u[d.i1j] - B(d.i_1j) * u[d.ij]) / hx[i];
+      dvdy = (B(d.ij1) * v[d.ij1] - B(d.ij_1) * v[d.ij]) / hy[j];
+      s0 = ((u[d.ij] - u[d.ij_1]) / ((double)(BB(d.i_1j_1) && BB(d.ij_1)) * hy[jm] + hy[j])) +
+           ((v[d.ij] - v[d.i_1j]) / ((double)(BB(d.i_1j_1) && BB(d.i_1j)) * hx[d.i_1] + hx[i]));
+      s1 = ((u[d.i1j] - u[d.i1j_1]) / ((double)(BB(d.ij_1) && BB(d.i1j_1)) * hy[jm] + hy[j])) +
+           ((v[d.i1j] - v[d.ij]) / (hx[i] + (double)(BB(d.i1j_1) && BB(d.i1j)) * hx[d.i1]));
+      s2 = ((u[d.ij1] - u[d.ij]) / (hy[j] + (double)(BB(d.i_1j1) && BB(d.ij1)) * hy[jp])) +
+           ((v[d.ij1] - v[d.i_1j1]) / ((double)(BB(d.i_1j) && BB(d.i_1j1)) * hx[d.i_1] + hx[i]));
+      s3 = ((u[d.i1j1] - u[d.i1j]) / (hy[j] + (double)(BB(d.ij1) && BB(d.i1j1)) * hy[jp])) +
+           ((v[d.i1j1] - v[d.ij1]) / (hx[i] + (double)(BB(d.i1j) && BB(d.i1j1)) * hx[d.i1]));
+    } else {
+      dudx = (u[d.i1j] - u[d.ij]) / hx[i];
+      dvdy = (v[d.ij1] - v[d.ij]) / hy[j];
+      s0 = ((u[d.ij] - u[d.ij_1]) / (hy[jm] + hy[j])) + ((v[d.ij] - v[d.i_1j]) / (hx[d.i_1] + hx[i]));
+      s1 = ((u[d.i1j] - u[d.i1j_1]) / (hy[jm] + hy[j])) + ((v[d.i1j] - v[d.ij]) / (hx[i] + hx[d.i1]));
+      s2 = ((u[d.ij1] - u[d.ij]) / (hy[j] + hy[jp])) + ((v[d.ij1] - v[d.i_1j1]) / (hx[d.i_1] + hx[i]));
+      s3 = ((u[d.i1j1] - u[d.i1j]) / (hy[j] + hy[jp])) + ((v[d.i1j1] - v[d.ij1]) / (hx[i] + hx[d.i1]));
+    }
+    g.ScT1[d.ij] = ht * sT[d.ij] * g.cT2 * hx[i] * hy[j] *
+                       (2.0 * (dudx * dudx + dvdy * dvdy) + s0 * s0 + s1 * s1 + s2 * s2 + s3 * s3 -
+                        (dudx + dvdy) * (dudx + dvdy) * 2.0 / 3.0) +
+                   g.p_pr[d.ij] * hx[i] * hy[j];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// one coupled p-T Jacobi sweep with the EOS substitution (SIMPLE_TS_MPI.cpp:3786-4131).
+// Reads buffer `cur`, writes buffer `cur^1` for every cell (unsolved cells copy through,
+// which keeps both buffers identical there exactly as the reference's memcpy + swap do).
+// ---------------------------------------------------------------------------
+__global__ void k_sweep(Geo g, unsigned long long h_sweep, int in_graph) {
+  Ctl* ctl = g.ctl;
+  if (ctl->pt_done) return;  // the loop already stopped: launch is a no-op
+  Cell c = cell(g);
+  const unsigned cur = ctl->cur;
+  const double* __restrict__ P = g.p[cur];
+  const double* __restrict__ TT = g.T[cur];
+  double* __restrict__ pn = g.p[cur ^ 1];
+  double* __restrict__ Tn = g.T[cur ^ 1];
+  double rp = 0, rT = 0;
+  if (c.ok) {
+    const uint8_t cl = g.cls[c.ij];
+    const int co = cls_o(cl);
+    if (!co) {
+      pn[c.ij] = P[c.ij];
+      Tn[c.ij] = TT[c.ij];
+    } else {
+      const int i = c.i, j = c.j;
+      const Nb d = neighbours(i, j, g.Nx, g.Ny, g.bits & F_PERIODIC);
+      const double* __restrict__ Fx = g.Fx;
+      const double* __restrict__ Fy = g.Fy;
+      const double* __restrict__ hx = g.hx;
+      const double* __restrict__ hy = g.hy;
+      const double ht = g.ht;
+      const double aT1 = dmax0(0, Fx[d.ij]) + g.DTx[d.ij];
+      const double aT2 = dmax0(0, -Fx[d.i1j]) + g.DTx[d.i1j];
+      const double aT3 = dmax0(0, Fy[d.ij]) + g.DTy[d.ij];
+      const double aT4 = dmax0(0, -Fy[d.ij1]) + g.DTy[d.ij1];
+      const double divu = (g.u[d.i1j] - g.u[d.ij]) * hy[j] + (g.v[d.ij1] - g.v[d.ij]) * hx[i];
+      double Tnew;
+      if (co == CLS_BC) {
+        auto B = [&](int k) -> double { return cls_fluid(g.cls[k]) ? 1.0 : 0.0; };
+        auto NB = [&](int k) -> double { return cls_fluid(g.cls[k]) ? 0.0 : 1.0; };
+        Tnew = (ht * (aT1 * (B(d.i_1j) * TT[d.i_1j] + NB(d.i_1j) * g.Tw_u[d.ij]) +
+                      aT2 * (B(d.i1j) * TT[d.i1j] + NB(d.i1j) * g.Tw_u[d.i1j]) +
+                      aT3 * (B(d.ij_1) * TT[d.ij_1] + NB(d.ij_1) * g.Tw_v[d.ij]) +
+                      aT4 * (B(d.ij1) * TT[d.ij1] + NB(d.ij1) * g.Tw_v[d.ij1]) + (1.0 - g.gamma1) * P[d.ij] * divu) +
+                g.ScT1[d.ij]) /
+               (ht * (aT1 + aT2 + aT3 + aT4 + Fx[d.i1j] - Fx[d.ij] + Fy[d.ij1] - Fy[d.ij]) + hx[i] * hy[j] * g.rho[d.ij]);
+      } else {
+        Tnew = (ht * (aT1 * TT[d.i_1j] + aT2 * TT[d.i1j] + aT3 * TT[d.ij_1] + aT4 * TT[d.ij1] +
+                      (1.0 - g.gamma1) * P[d.ij] * divu) +
+                g.ScT1[d.ij]) /
+               (ht * (aT1 + aT2 + aT3 + aT4 + Fx[d.i1j] - Fx[d.ij] + Fy[d.ij1] - Fy[d.ij]) + hx[i] * hy[j] * g.rho[d.ij]);
+      }
+      const double* __restrict__ apx = g.apx;
+      const double* __restrict__ apy = g.apy;
+      double num = apx[d.ij] * P[d.i_1j] + apx[d.i1j] * P[d.i1j] + apy[d.ij] * P[d.ij_1] + apy[d.ij1] * P[d.ij1] +
+                   g.bpx[d.ij] - g.bpx[d.i1j] + g.bpy[d.ij] - g.bpy[d.ij1];
+      if (co == CLS_BC) {
+        const double gxb = ((g.bits & F_GIVEN_U_XB) && i == g.Nx_o0) ? 1.0 : 0.0;
+        const double gxe = ((g.bits & F_GIVEN_U_XE) && i == g.Nx_o1 - 1) ? 1.0 : 0.0;
+        num = num + gxb * Fx[d.ij] - gxe * Fx[d.i1j];
+      }
+      const double pnew = (ht * num + g.p_pr[d.ij] * hx[i] * hy[j] / (g.T_pr[d.ij])) /
+                          (ht * (apx[d.ij] + apx[d.i1j] + apy[d.ij] + apy[d.ij1]) + hx[i] * hy[j] / (Tnew));
+      Tn[c.ij] = Tnew;
+      pn[c.ij] = pnew;
+      rT = fabs(Tnew - TT[c.ij]);
+      rp = fabs(pnew - P[c.ij]);
+    }
+  }
+  block_max2(rp, rT, &ctl->res_bits_p, &ctl->res_bits_T, &ctl->status);
+  if (last_block(&ctl->block_count)) {
+    // the reference's loop control, evaluated once per sweep (SIMPLE_TS_MPI.cpp:4087-4107)
+    const unsigned I = ctl->Iter < 64 ? ctl->Iter : 63;
+    const double res_p = as_d(atomicExch(&ctl->res_bits_p, 0ull));
+    const double res_T = as_d(atomicExch(&ctl->res_bits_T, 0ull));
+    ctl->res_p[I] = res_p;
+    ctl->res_T[I] = res_T;
+    if (ctl->Iter_p_c == 0) {
+      ctl->res_p0[I] = res_p;
+      ctl->res_T0[I] = res_T;
+    }
+    const unsigned n = ++ctl->Iter_p_c;
+    bool cont;
+    if (g.bits & F_FIXED_SWEEPS)
+      cont = n < (unsigned)g.N_I_p_c;
+    else
+      cont = (n < 2) || ((n < (unsigned)g.N_I_p_c) && ((g.MaxError_p_c < res_p) || (g.MaxError_T < res_T)));
+    ctl->cur = cur ^ 1;
+    if (!cont) {
+      ctl->pt_done = 1;
+      ctl->sweeps[I] = n;
+      ctl->step_sweeps += n;
+    }
+    if (in_graph) cudaGraphSetConditional((cudaGraphConditionalHandle)h_sweep, cont ? 1 : 0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// velocity correction with L-inf residuals (SIMPLE_TS_MPI.cpp:4171-4305) and
+// sqrt(T), rho = p/T (:4323-4330)
+// ---------------------------------------------------------------------------
+__global__ void k_correct(Geo g) {
+  Cell c = cell(g);
+  Ctl* ctl = g.ctl;
+  const unsigned cur = ctl->cur;
+  const double* __restrict__ p = g.p[cur];
+  const double* __restrict__ T = g.T[cur];
+  double ru = 0, rv = 0;
+  if (c.ok) {
+    const uint8_t cl = g.cls[c.ij];
+    const int n = c.ij;
+    if (cls_u(cl)) {
+      const int w = (cls_u(cl) == CLS_BC && (g.bits & F_PERIODIC) && c.i == 0) ? n + g.Nx - 1 : n - 1;
+      const double t = g.u[n];
+      const double un = g.u_pseudo[n] - (p[n] - p[w]) * g.d12[n];
+      g.u[n] = un;
+      ru = fabs(un - t);
+    }
+    if (cls_v(cl)) {
+      const double t = g.v[n];
+      const double vn = g.v_pseudo[n] - (p[n] - p[n - g.Nx]) * g.d34[n];
+      g.v[n] = vn;
+      rv = fabs(vn - t);
+    }
+    g.sqrt_T[n] = sqrt(T[n]);
+    g.rho[n] = cls_fluid(cl) ? p[n] / T[n] : 0.0;
+  }
+  block_max2(ru, rv, &ctl->res_bits_u, &ctl->res_bits_v, &ctl->status);
+}
+
+// Solve_rho_in_middle_points (SIMPLE_TS_MPI.cpp:10382-10437)
+__global__ void k_face_rho(Geo g) {
+  Cell c = cell(g);
+  if (!c.ok) return;
+  const Nb d = neighbours(c.i, c.j, g.Nx, g.Ny, g.bits & F_PERIODIC);
+  const double* __restrict__ rho = g.rho;
+  const bool bw = cls_fluid(g.cls[d.i_1j]), bp = cls_fluid(g.cls[d.ij]), bs = cls_fluid(g.cls[d.ij_1]);
+  double ru, rv;
+  if (bw && bp) ru = upwind_rho(rho[d.i_1j], rho[d.ij], g.u[d.ij]);
+  else if (bw != bp) ru = bw ? rho[d.i_1j] : rho[d.ij];
+  else ru = 0.0;
+  if (bs && bp) rv = upwind_rho(rho[d.ij_1], rho[d.ij], g.v[d.ij]);
+  else if (bs != bp) rv = bs ? rho[d.ij_1] : rho[d.ij];
+  else rv = 0.0;
+  g.rho_u[d.ij] = ru;
+  g.rho_v[d.ij] = rv;
+}
+
+// SolveFluxes (SIMPLE_TS_MPI.cpp:10440-10454) and SolveDiffisionTerms (:10457-10618)
+__global__ void k_flux_diff(Geo g) {
+  Cell c = cell(g);
+  if (!c.ok) return;
+  const int i = c.i, j = c.j;
+  const Nb d = neighbours(i, j, g.Nx, g.Ny, g.bits & F_PERIODIC);
+  const double* __restrict__ hx = g.hx;
+  const double* __restrict__ hy = g.hy;
+  const double* __restrict__ sT = g.sqrt_T;
+  const double* __restrict__ Tw_u = g.Tw_u;
+  const double* __restrict__ Tw_v = g.Tw_v;
+  const double cT = g.ctl->cT, cT1 = g.cT1;
+  g.Fx[d.ij] = hy[j] * g.rho_u[d.ij] * g.u[d.ij];
+  g.Fy[d.ij] = hx[i] * g.rho_v[d.ij] * g.v[d.ij];
+  const bool b_ws = cls_fluid(g.cls[d.i_1j_1]), b_s = cls_fluid(g.cls[d.ij_1]), b_w = cls_fluid(g.cls[d.i_1j]),
+             b_p = cls_fluid(g.cls[d.ij]);
+  const int jm = j - (0 < j ? 1 : 0);
+  double Gy = g.Gamma_yf[d.ij], Gx = g.Gamma_xf[d.ij];
+  if (b_ws && b_s && b_w && b_p) {
+    Gy = 0.5 * (Li(sT[d.i_1j_1], sT[d.i_1j], hy[jm], hy[j]) + Li(sT[d.ij_1], sT[d.ij], hy[jm], hy[j]));
+  } else if (b_ws || b_s || b_w || b_p) {
+    Gy = 0.5 * ((double)(b_ws && b_w) * Li(sT[d.i_1j_1], sT[d.i_1j], hy[jm], hy[j]) +
+                (double)(b_ws != b_w) * sqrt(Tw_v[d.i_1j]) +
+                (double)(b_s && b_p) * Li(sT[d.ij_1], sT[d.ij], hy[jm], hy[j]) + (double)(b_s != b_p) * sqrt(Tw_v[d.ij]) +
+                (double)((!(b_ws && b_w)) || (!(b_s && b_p))) * Li(sqrt(Tw_u[d.ij_1]), sqrt(Tw_u[d.ij]), hy[jm], hy[j]));
+  }
+  g.Gamma_yf[d.ij] = Gy;
+  g.D_ux[d.ij] = cT * sT[d.i_1j] * (hy[j] / hx[d.i_1]);
+  if ((b_p && b_w) || (b_s && b_ws))
+    g.D_uy[d.ij] = cT * Gy * ((hx[i] + hx[d.i_1]) / ((double)(b_p * b_w) * hy[j] + (double)(b_s * b_ws) * hy[jm]));
+  else
+    g.D_uy[d.ij] = 0;
+  if (b_ws && b_s && b_w && b_p) {
+    Gx = 0.5 * (Li(sT[d.i_1j_1], sT[d.ij_1], hx[d.i_1], hx[i]) + Li(sT[d.i_1j], sT[d.ij], hx[d.i_1], hx[i]));
+  } else if (b_ws || b_s || b_w || b_p) {
+    Gx = 0.5 * ((double)(b_ws && b_s) * Li(sT[d.i_1j_1], sT[d.ij_1], hx[d.i_1], hx[i]) +
+                (double)(b_ws != b_s) * sqrt(Tw_u[d.ij_1]) +
+                (double)(b_w && b_p) * Li(sT[d.i_1j], sT[d.ij], hx[d.i_1], hx[i]) + (double)(b_w != b_p) * sqrt(Tw_u[d.ij]) +
+                (double)((!(b_ws && b_s)) || (!(b_w && b_p))) * Li(sqrt(Tw_v[d.i_1j]), sqrt(Tw_v[d.ij]), hx[d.i_1], hx[i]));
+  }
+  g.Gamma_xf[d.ij] = Gx;
+  if ((b_p && b_s) || (b_w && b_ws))
+    g.D_vx[d.ij] = cT * Gx * ((hy[j] + hy[jm]) / ((double)(b_p * b_s) * hx[i] + (double)(b_w * b_ws) * hx[d.i_1]));
+  else
+    g.D_vx[d.ij] = 0;
+  g.D_vy[d.ij] = cT * sT[d.ij_1] * (hx[i] / hy[jm]);
+  if (b_p || b_w)
+    g.DTx[d.ij] = cT1 * (hy[j] / (0.5 * ((double)b_p * hx[i] + (double)b_w * hx[d.i_1]))) *
+                  ((double)((!b_p) || (!b_w)) * sqrt(Tw_u[d.ij]) +
+                   (double)(b_p * b_w) * Hi(sT[d.i_1j], sT[d.ij], hx[d.i_1], hx[i]));
+  else
+    g.DTx[d.ij] = 0;
+  if (b_p || b_s)
+    g.DTy[d.ij] = cT1 * (hx[i] / (0.5 * ((double)b_p * hy[j] + (double)b_s * hy[jm]))) *
+                  ((double)((!b_p) || (!b_s)) * sqrt(Tw_v[d.ij]) +
+                   (double)(b_p * b_s) * Hi(sT[d.ij_1], sT[d.ij], hy[jm], hy[j]));
+  else
+    g.DTy[d.ij] = 0;
+}
+
+// ApplyBodiesConditionsToVariables on the device (SIMPLE_TS_MPI.cpp:6470-6584): a face takes the
+// velocity of the body it belongs to, or of the body on its low side; body cells take p, T and rho = 0.
+__global__ void k_apply_bodies(Geo g) {
+  Cell c = cell(g);
+  if (!c.ok) return;
+  const unsigned cur = g.ctl->cur;
+  const int i = c.i, j = c.j, n = c.ij;
+  const uint32_t id = g.vol_id[n];
+  const uint32_t idw = (i > 0) ? g.vol_id[n - 1] : 0u;
+  const uint32_t ids = (j > 0) ? g.vol_id[n - g.Nx] : 0u;
+  if (id >= 1) g.u[n] = g.bodies[id - 1].u;
+  else if (idw >= 1) g.u[n] = g.bodies[idw - 1].u;
+  if (id >= 1) g.v[n] = g.bodies[id - 1].v;
+  else if (ids >= 1) g.v[n] = g.bodies[ids - 1].v;
+  if (id >= 1) {
+    g.p[cur][n] = g.bodies[id - 1].p;
+    g.T[cur][n] = g.bodies[id - 1].T;
+    g.rho[n] = cls_fluid(g.cls[n]) ? g.p[cur][n] / g.T[cur][n] : 0.0;
+  }
+}
+
+// sqrt(T) and rho over all cells (SIMPLE_TS_MPI.cpp:2995-3001, :3020-3032)
+__global__ void k_sqrt_rho(Geo g, int do_rho) {
+  Cell c = cell(g);
+  if (!c.ok) return;
+  const unsigned cur = g.ctl->cur;
+  const double T = g.T[cur][c.ij];
+  g.sqrt_T[c.ij] = sqrt(T);
+  if (do_rho) g.rho[c.ij] = cls_fluid(g.cls[c.ij]) ? g.p[cur][c.ij] / T : 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Boundary work of one outer iteration, in the reference's order, in a single CTA
+// (the lists are O(perimeter)).  `phases` selects the parts (PH_* in sts_kernels.h).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_boundary(Geo g, unsigned phases, unsigned long long h_outer, int in_graph) {
+  Ctl* ctl = g.ctl;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int Nx = g.Nx, Ny = g.Ny;
+  const bool per = g.bits & F_PERIODIC;
+  double* __restrict__ u = g.u;
+  double* __restrict__ v = g.v;
+  const unsigned cur = ctl->cur;
+  double* __restrict__ p = g.p[cur];
+  double* __restrict__ T = g.T[cur];
+  auto fl = [&](int k) { return cls_fluid(g.cls[k]); };
+  const uint64_t bits = g.bits;
+
+  if (phases & PH_CONTROL) {
+    // SIMPLE_TS_MPI.cpp:4347-4361 (coefficients) and :4406-4450 (loop control)
+    if (tid == 0) {
+      const int TypeND = g.TypeND;
+      if (TypeND == 1 || TypeND == 2) {
+        ctl->cT = (1.0 / g.Re) * (ctl->u_given_xb_in_it * ctl->p_BC_xb / g.T_BC_xb);
+        ctl->cPch = (TypeND == 1) ? 0.5 : ctl->u_given_xb_in_it * ctl->u_given_xb_in_it / (g.gamma1 * g.Ma * g.Ma);
+      }
+      const double ru = as_d(ctl->res_bits_u), rv = as_d(ctl->res_bits_v);
+      ctl->res_u = ru;
+      ctl->res_v = rv;
+      const unsigned It = ++ctl->Iter;
+      if (It == 1) {
+        ctl->res_u0 = ru;
+        ctl->res_v0 = rv;
+      }
+      const unsigned I = (It - 1) < 64 ? It - 1 : 63;
+      const double rpI = ctl->res_p[I], rTI = ctl->res_T[I];
+      const bool ci = (It < (unsigned)g.N_I) &&
+                      (g.MaxError_Velocities < ru || g.MaxError_Velocities < rv || g.MaxError_p_c < rpI || g.MaxError_T < rTI);
+      const double stop = g.MaxError_to_stop_program;
+      const bool cs = ((double)ctl->it_counter < g.Nt) &&
+                      ((!(It <= 1 && ctl->Iter_p_c <= 2)) || stop < ru || stop < rv || stop < ctl->res_p0[I] ||
+                       stop < ctl->res_T0[I]);
+      ctl->continue_iter = ci;
+      ctl->continue_step = cs;
+      if (in_graph) cudaGraphSetConditional((cudaGraphConditionalHandle)h_outer, ci ? 1 : 0);
+    }
+  }
+  __syncthreads();
+
+  // BoundaryConditions_Velocities_SlipBC_u (SIMPLE_TS_MPI.cpp:7098-7213); every entry performs
+  // only the writes that survive in the reference's sequential order (host-side analysis).
+  if (phases & PH_SLIP_U) {
+    const bool kl = bits & F_KN_LOCAL;
+    for (int k = tid; k < g.n_slip_u; k += nt) {
+      const int node = g.slip_u[k];
+      const uint8_t fin = g.slip_u_fin[k];
+      const int j = node / Nx, i = node - j * Nx;
+      const Nb d = neighbours(i, j, Nx, Ny, per);
+      const Body& Bd = g.bodies[g.vol_id[d.ij] - 1];
+      const double FK = Bd.F_slip * g.Kn;
+      if (g.vol_id[d.ij_1] == 0) {
+        const int jm = j - (0 < j ? 1 : 0);
+        const double a_ij = kl ? FK / (g.rho_u[d.ij_1] * 0.5 * g.hy[jm]) : FK / (0.5 * g.hy[jm]);
+        const double a_i1j = kl ? FK / (g.rho_u[d.i1j_1] * 0.5 * g.hy[jm]) : FK / (0.5 * g.hy[jm]);
+        if ((fin & 1) && fl(d.i_1j_1)) u[d.ij] = (u[d.ij_1] * a_ij + Bd.u) / (1.0 + a_ij);
+        if ((fin & 2) && fl(d.i1j_1)) u[d.i1j] = (u[d.i1j_1] * a_i1j + Bd.u) / (1.0 + a_i1j);
+      } else {
+        const int jp = j + (j < (Ny - 1) ? 1 : 0);
+        const double a_ij = kl ? FK / (g.rho_u[d.ij1] * 0.5 * g.hy[jp]) : FK / (0.5 * g.hy[jp]);
+        const double a_i1j = kl ? FK / (g.rho_u[d.i1j1] * 0.5 * g.hy[jp]) : FK / (0.5 * g.hy[jp]);
+        if ((fin & 1) && fl(d.i_1j1)) u[d.ij] = (u[d.ij1] * a_ij + Bd.u) / (1.0 + a_ij);
+        if ((fin & 2) && fl(d.i1j1)) u[d.i1j] = (u[d.i1j1] * a_i1j + Bd.u) / (1.0 + a_i1j);
+      }
+    }
+  }
+  __syncthreads();
+
+  // BoundaryConditions_Velocities_SlipBC_v (SIMPLE_TS_MPI.cpp:7216-7331)
+  if (phases & PH_SLIP_V) {
+    const bool kl = bits & F_KN_LOCAL;
+    for (int k = tid; k < g.n_slip_v; k += nt) {
+      const int node = g.slip_v[k];
+      const uint8_t fin = g.slip_v_fin[k];
+      const int j = node / Nx, i = node - j * Nx;
+      const Nb d = neighbours(i, j, Nx, Ny, per);
+      const Body& Bd = g.bodies[g.vol_id[d.ij] - 1];
+      const double FK = Bd.F_slip * g.Kn;
+      if (g.vol_id[d.i_1j] == 0) {
+        const double a_ij = kl ? FK / (g.rho_v[d.i_1j] * 0.5 * g.hx[d.i_1]) : FK / (0.5 * g.hx[d.i_1]);
+        const double a_ij1 = kl ? FK / (g.rho_v[d.i_1j1] * 0.5 * g.hx[d.i_1]) : FK / (0.5 * g.hx[d.i_1]);
+        if ((fin & 1) && fl(d.i_1j_1)) v[d.ij] = (v[d.i_1j] * a_ij + Bd.v) / (1.0 + a_ij);
+        if ((fin & 2) && fl(d.i_1j1)) v[d.ij1] = (v[d.i_1j1] * a_ij1 + Bd.v) / (1.0 + a_ij1);
+      } else {
+        const double a_ij = kl ? FK / (g.rho_v[d.i1j] * 0.5 * g.hx[d.i1]) : FK / (0.5 * g.hx[d.i1]);
+        const double a_ij1 = kl ? FK / (g.rho_v[d.i1j1] * 0.5 * g.hx[d.i1]) : FK / (0.5 * g.hx[d.i1]);
+        if ((fin & 1) && fl(d.i1j_1)) v[d.ij] = (v[d.i1j] * a_ij + Bd.v) / (1.0 + a_ij);
+        if ((fin & 2) && fl(d.i1j1)) v[d.ij1] = (v[d.i1j1] * a_ij1 + Bd.v) / (1.0 + a_ij1);
+      }
+    }
+  }
+  __syncthreads();
+
+  // BoundaryConditions_Velocities (SIMPLE_TS_MPI.cpp:6790-7096), each loop a phase
+  if ((phases & PH_VEL) && !per) {
+    if (bits & F_DVDX0_XB) {
+      for (int k = tid; k < Ny * g.Nx_v0; k += nt) {
+        const int j = k / g.Nx_v0, i = k - j * g.Nx_v0, n = g.Nx_v0 + j * Nx;
+        if (fl(n)) v[i + j * Nx] = v[n];
+      }
+      __syncthreads();
+    }
+    if (bits & F_DVDX0_XE) {
+      const int w = Nx - g.Nx_v1;
+      for (int k = tid; k < Ny * w; k += nt) {
+        const int j = k / w, i = g.Nx_v1 + (k - j * w), n = g.Nx_v1 - 1 + j * Nx;
+        if (fl(n)) v[i + j * Nx] = v[n];
+      }
+      __syncthreads();
+    }
+    if (bits & F_DVDY0_YB) {
+      for (int k = tid; k < Nx * g.Ny_v0; k += nt) {
+        const int jj = k / Nx, i = k - jj * Nx, n = i + g.Ny_v0 * Nx;
+        if (fl(n)) v[i + jj * Nx] = v[n];
+      }
+      __syncthreads();
+    }
+    if (bits & F_DVDY0_YE) {
+      const int w = Ny - g.Ny_v1;
+      for (int k = tid; k < Nx * w; k += nt) {
+        const int jj = k / Nx, i = k - jj * Nx, n = i + (g.Ny_v1 - 1) * Nx;
+        if (fl(n)) v[i + (g.Ny_v1 + jj) * Nx] = v[n];
+      }
+      __syncthreads();
+    }
+    if (bits & F_DUDX0_XB) {
+      for (int k = tid; k < Ny * g.Nx_u0; k += nt) {
+        const int j = k / g.Nx_u0, i = k - j * g.Nx_u0, n = g.Nx_u0 + j * Nx;
+        if (fl(n)) u[i + j * Nx] = u[n];
+      }
+      __syncthreads();
+    }
+    if (bits & F_DURHODX0_XB) {
+      for (int j = tid; j < Ny; j += nt) {
+        const int n = g.Nx_u0 - 1 + j * Nx;
+        if (fl(n)) u[n] = (g.rho_u[n + 1] * u[n + 1]) / g.rho_u[n];
+      }
+      __syncthreads();
+    }
+    if (bits & F_DRHODT0_XB) {
+      const int i = g.Nx_u0 - 1;
+      for (int j = tid; j < Ny; j += nt) {
+        const int n = i + j * Nx;
+        // the reference reads one row past the array for a fluid cell in the top row; skipped here
+        if (fl(n) && n + Nx < g.Na)
+          u[n] = ((g.rho[n] - g.rho_pr[n]) * g.hx[i] * g.hy[j] / g.ht +
+                  (g.rho_v[n + Nx] * v[n + Nx] - g.rho_v[n] * v[n]) * g.hx[i] + g.rho_u[n + 1] * u[n + 1] * g.hy[j]) /
+                 (g.rho_u[n] * g.hy[j]);
+      }
+      __syncthreads();
+    }
+    if (bits & F_DUDX0_XE) {
+      const int w = Nx - g.Nx_u1;
+      for (int k = tid; k < Ny * w; k += nt) {
+        const int j = k / w, i = g.Nx_u1 + (k - j * w), n = g.Nx_u1 - 1 + j * Nx;
+        if (fl(n)) u[i + j * Nx] = u[n];
+      }
+      __syncthreads();
+    }
+    if (bits & F_DURHODX0_XE) {
+      for (int j = tid; j < Ny; j += nt) {
+        const int n = g.Nx_u1 - 1 + j * Nx;
+        if (fl(n)) u[n + 1] = (g.rho_u[n] * u[n]) / g.rho_u[n + 1];
+      }
+      __syncthreads();
+    }
+    if (bits & F_DRHODT0_XE) {
+      const int i = g.Nx_u1 - 1;
+      for (int j = tid; j < Ny; j += nt) {
+        const int n = i + j * Nx;
+        if (fl(n) && n + Nx < g.Na)
+          u[n + 1] = (-(g.rho[n] - g.rho_pr[n]) * g.hx[i] * g.hy[j] / g.ht -
+                      (g.rho_v[n + Nx] * v[n + Nx] - g.rho_v[n] * v[n]) * g.hx[i] + g.rho_u[n] * u[n] * g.hy[j]) /
+                     (g.rho_u[n + 1] * g.hy[j]);
+      }
+      __syncthreads();
+    }
+    if (bits & F_U_MINMOUT_XE) {  // the reference keeps the last row's rho_u for Min and Mout
+      const double Min = g.rho_u[g.Nx_u0 + (Ny - 1) * Nx], Mout = g.rho_u[g.Nx_u1 + (Ny - 1) * Nx];
+      __syncthreads();
+      for (int j = tid; j < Ny; j += nt) {
+        const int n = g.Nx_u1 - 1 + j * Nx;
+        u[n + 1] = u[n] * Min / Mout;
+      }
+      __syncthreads();
+    }
+    if (bits & F_DUDY0_YB) {
+      for (int k = tid; k < Nx * g.Ny_u0; k += nt) {
+        const int jj = k / Nx, i = k - jj * Nx, n = i + g.Ny_u0 * Nx;
+        if (fl(n)) u[i + jj * Nx] = u[n];
+      }
+      __syncthreads();
+    }
+    if (bits & F_DUDY0_YE) {
+      const int w = Ny - g.Ny_u1;
+      for (int k = tid; k < Nx * w; k += nt) {
+        const int jj = k / Nx, i = k - jj * Nx, n = i + (g.Ny_u1 - 1) * Nx;
+        if (fl(n)) u[i + (g.Ny_u1 + jj) * Nx] = u[n];
+      }
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+
+  // BoundaryConditions_Pressure_begin_iteration_for_it (SIMPLE_TS_MPI.cpp:7430-7647)
+  if ((phases & PH_PBEGIN) && !per) {
+    __shared__ int ratio_side;  // 0: nothing, 1: inlet columns, 2: outlet columns
+    if (tid == 0) {
+      ratio_side = 0;
+      const int i = g.Nx_u0;
+      double umax = u[0];
+      for (int j = 0; j < Ny; j++) {
+        const int n = i + j * Nx;
+        if (fl(n)) umax = (umax > u[n]) ? umax : u[n];
+      }
+      double mean = 0, hin = 0;
+      for (int j = 0; j < Ny; j++) {
+        const int n = i + j * Nx;
+        if (fl(n)) { mean += u[n] * g.hy[j]; hin += g.hy[j]; }
+      }
+      mean = mean / hin;
+      ctl->u_in_max = umax;
+      ctl->u_in_mean = mean;
+      if (bits & F_GIVEN_REKN) ctl->u_given_xb = g.Re * g.Kn * sqrt(15.0 * 3.14159265358979323846 / 128.0);
+      const double ug = ctl->u_given_xb;
+      if (g.p_corr_method == 0) {
+        ctl->u_given_xb_in_it = ug;
+        if (bits & F_GIVEN_U_XB) {
+          const int ii = g.Nx_o0;
+          const int jj = (int)(((double)g.Ny_o1 - 1.0) - (double)g.Ny_o0);
+          ctl->p_BC_xb = p[ii + jj * Nx];
+        }
+      } else if (g.p_corr_method == 1) {
+        ctl->u_given_xb_in_it = umax;
+      } else if (g.p_corr_method == 2) {
+        ctl->u_given_xb_in_it = mean;
+      }
+      if ((bits & F_PRESSURE_BC) && (bits & F_RATIO_CORRECT)) {
+        double pc = ctl->p_correction;
+        if (bits & F_P_CORR_AUTO) {
+          const double r = sqrt(ctl->res_u * ctl->res_u + ctl->res_v * ctl->res_v);
+          double t;
+          if (ctl->Iter_pr1 <= ctl->Iter_pr2 && ctl->Iter_pr1 < (unsigned)(g.N_I - 1)) t = pc * (1.0 + r);
+          else t = pc * (1.0 - r);
+          if (t < g.p_correction_min) t = g.p_correction_min;
+          else if (g.p_correction_max < t) t = g.p_correction_max;
+          pc = t;
+          ctl->p_correction = pc;
+        }
+        const double ui = ctl->u_given_xb_in_it;
+        const bool cxb = bits & F_CORRECT_P_XB;
+        if (ui < (ug * (1.0 - g.u_given_xb_error))) {
+          if (cxb) ctl->p_BC_xb = ctl->p_BC_xb * (1.0 + pc * (ug - ui) * (ug - ui));
+          else {
+            const double t = ctl->p_BC_xe * (1.0 - pc * (ug - ui) * (ug - ui));
+            ctl->p_BC_xe = (t < 0.0) ? 0.0 : t;
+          }
+        } else if ((ug * (1.0 + g.u_given_xb_error)) < ui) {
+          if (cxb) {
+            const double t = ctl->p_BC_xb * (1.0 - pc * (ug - ui) * (ug - ui));
+            ctl->p_BC_xb = (t > ctl->p_BC_xe) ? t : ctl->p_BC_xe;
+          } else {
+            const double t = ctl->p_BC_xb * (1.0 + pc * (ug - ui) * (ug - ui));
+            ctl->p_BC_xe = (t > ctl->p_BC_xb) ? ctl->p_BC_xb : t;
+          }
+        }
+        ratio_side = cxb ? 1 : 2;
+      }
+    }
+    __syncthreads();
+    if (ratio_side == 1) {
+      const double pb = ctl->p_BC_xb, rb = ctl->p_BC_xb / g.T_BC_xb;
+      for (int k = tid; k < Ny * g.Nx_o0; k += nt) {
+        const int j = k / g.Nx_o0, i = k - j * g.Nx_o0, n = i + j * Nx;
+        if (fl(n)) { p[n] = pb; g.rho[n] = rb; }
+      }
+    } else if (ratio_side == 2) {
+      const double pe = ctl->p_BC_xe, re = ctl->p_BC_xe / g.T_BC_xe;
+      const int w = Nx - g.Nx_o1;
+      for (int k = tid; k < Ny * w; k += nt) {
+        const int j = k / w, i = g.Nx_o1 + (k - j * w), n = i + j * Nx;
+        if (fl(n)) { p[n] = pe; g.rho[n] = re; }
+      }
+    }
+  }
+  __syncthreads();
+
+  // inlet/outlet pressure and temperature before the time loop (SIMPLE_TS_MPI.cpp:2942-2979)
+  if ((phases & PH_PINIT) && (bits & F_PRESSURE_BC)) {
+    for (int k = tid; k < Ny * Nx; k += nt) {
+      const int j = k / Nx, i = k - j * Nx;
+      if (!fl(k)) continue;
+      if (i < g.Nx_o0) { p[k] = ctl->p_BC_xb; T[k] = g.T_BC_xb; }
+      else if (i >= g.Nx_o1) { p[k] = ctl->p_BC_xe; T[k] = g.T_BC_xe; }
+    }
+  }
+  __syncthreads();
+
+  // BoundaryConditions_Temperature_TemperatureJumpBC (SIMPLE_TS_MPI.cpp:7744-8045)
+  if (phases & (PH_TJUMP | PH_TJUMP_WRITE)) {
+    const bool kl = bits & F_KN_LOCAL;
+    for (int k = tid; k < g.n_tjump; k += nt) {
+      const int node = g.tjump[k];
+      const uint8_t fin = g.tjump_fin[k];
+      const int j = node / Nx, i = node - j * Nx;
+      const Nb d = neighbours(i, j, Nx, Ny, per);
+      const int nb[4] = {d.i_1j, d.i1j, d.ij_1, d.ij1};
+      const int dst[4] = {d.ij, d.i1j, d.ij, d.ij1};
+      for (int q = 0; q < 4; q++) {
+        if (fl(nb[q]) || !(fin & (1 << q))) continue;
+        const Body& Bd = g.bodies[g.vol_id[nb[q]] - 1];
+        double* out = (q < 2) ? g.Tw_u : g.Tw_v;
+        double val;
+        if (Bd.jump) {
+          const double FK = kl ? (Bd.F_jump * g.Kn) / g.rho[d.ij] : Bd.F_jump * g.Kn;
+          const double a = FK / (0.5 * ((q < 2) ? g.hx[i] : g.hy[j]));
+          val = (a * T[d.ij] + Bd.T) / (1.0 + a);
+        } else if (Bd.dTdn0 != 0) {
+          val = T[d.ij];
+        } else {
+          val = Bd.T;
+        }
+        out[dst[q]] = val;
+      }
+    }
+  }
+  __syncthreads();
+
+  // BoundaryConditions_Temperature_TemperatureJumpBC_WriteToMassiveToWriteDataToFile (:8048-8099)
+  if (phases & PH_TJUMP_WRITE) {
+    for (int k = tid; k < g.n_tjump; k += nt) {
+      const int node = g.tjump[k];
+      const uint8_t fin = g.tjump_wr_fin[k];
+      const int j = node / Nx, i = node - j * Nx;
+      const Nb d = neighbours(i, j, Nx, Ny, per);
+      if ((fin & 1) && !fl(d.i_1j)) T[d.i_1j] = g.Tw_u[d.ij];
+      if ((fin & 2) && !fl(d.i1j)) T[d.i1j] = g.Tw_u[d.i1j];
+      if ((fin & 4) && !fl(d.ij_1)) T[d.ij_1] = g.Tw_v[d.ij];
+      if ((fin & 8) && !fl(d.ij1)) T[d.ij1] = g.Tw_v[d.ij1];
+    }
+  }
+  __syncthreads();
+
+  // BoundaryConditions_Temperature (SIMPLE_TS_MPI.cpp:7650-7741)
+  if ((phases & PH_TEMP) && !per) {
+    if (bits & F_DTDX0_XB) {
+      for (int k = tid; k < Ny * g.Nx_o0; k += nt) {
+        const int j = k / g.Nx_o0, i = k - j * g.Nx_o0, n = g.Nx_o0 + j * Nx;
+        if (fl(n)) T[i + j * Nx] = T[n];
+      }
+      __syncthreads();
+    }
+    if (bits & F_DTDX0_XE) {
+      const int w = Nx - g.Nx_o1;
+      for (int k = tid; k < Ny * w; k += nt) {
+        const int j = k / w, i = g.Nx_o1 + (k - j * w), n = g.Nx_o1 - 1 + j * Nx;
+        if (fl(n)) T[i + j * Nx] = T[n];
+      }
+      __syncthreads();
+    }
+    if (bits & F_DTDY0_YB) {
+      for (int k = tid; k < Nx * g.Ny_o0; k += nt) {
+        const int jj = k / Nx, i = k - jj * Nx, n = i + g.Ny_o0 * Nx;
+        if (fl(n)) T[i + jj * Nx] = T[n];
+      }
+      __syncthreads();
+    }
+    if (bits & F_DTDY0_YE) {
+      const int w = Ny - g.Ny_o1;
+      for (int k = tid; k < Nx * w; k += nt) {
+        const int jj = k / Nx, i = k - jj * Nx, n = i + (g.Ny_o1 - 1) * Nx;
+        if (fl(n)) T[i + (g.Ny_o1 + jj) * Nx] = T[n];
+      }
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+
+  // BoundaryConditions_Pressure (SIMPLE_TS_MPI.cpp:7335-7428)
+  if ((phases & PH_PRES) && !per) {
+    if (bits & F_DPDX0_XB) {
+      for (int k = tid; k < Ny * g.Nx_o0; k += nt) {
+        const int j = k / g.Nx_o0, i = k - j * g.Nx_o0, n = g.Nx_o0 + j * Nx;
+        if (fl(n)) p[i + j * Nx] = p[n];
+      }
+      __syncthreads();
+    }
+    if (bits & F_DPDX0_XE) {
+      const int w = Nx - g.Nx_o1;
+      for (int k = tid; k < Ny * w; k += nt) {
+        const int j = k / w, i = g.Nx_o1 + (k - j * w), n = g.Nx_o1 - 1 + j * Nx;
+        if (fl(n)) p[i + j * Nx] = p[n];
+      }
+      __syncthreads();
+    }
+    if (bits & F_DPDY0_YB) {
+      for (int k = tid; k < Nx * g.Ny_o0; k += nt) {
+        const int jj = k / Nx, i = k - jj * Nx, n = i + g.Ny_o0 * Nx;
+        if (fl(n)) p[i + jj * Nx] = p[n];
+      }
+      __syncthreads();
+    }
+    if (bits & F_DPDY0_YE) {
+      const int w = Ny - g.Ny_o1;
+      for (int k = tid; k < Nx * w; k += nt) {
+        const int jj = k / Nx, i = k - jj * Nx, n = i + (g.Ny_o1 - 1) * Nx;
+        if (fl(n)) p[i + (g.Ny_o1 + jj) * Nx] = p[n];
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// End of a time step: time-dependent inflow (SIMPLE_TS_MPI.cpp:8102-8144), per-step
+// record and the multi-step loop condition.
+__global__ void k_step_end(Geo g, unsigned long long h_step, int in_graph) {
+  Ctl* ctl = g.ctl;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int Nx = g.Nx, Ny = g.Ny;
+  if ((g.bits & F_U_BY_TIME) && !(g.bits & F_PERIODIC)) {
+    const double it = ctl->it;
+    double ug;
+    if (it <= g.t_BC_b) ug = g.u_BC_xb_t_BC_b;
+    else if (g.t_BC_b < it && it <= g.t_BC_e)
+      ug = ((g.u_BC_xb_t_BC_e - g.u_BC_xb_t_BC_b) / (g.t_BC_e - g.t_BC_b)) * (it - g.t_BC_b) + g.u_BC_xb_t_BC_b;
+    else ug = g.u_BC_xb_t_BC_e;
+    for (int k = tid; k < Ny * g.Nx_u0; k += nt) {
+      const int j = k / g.Nx_u0, i = k - j * g.Nx_u0, n = i + j * Nx;
+      if (cls_fluid(g.cls[n])) g.u[n] = ug;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      ctl->u_gas_nd = ug;
+      ctl->u_given_xb = ug;
+    }
+  }
+  if (tid == 0) {
+    ctl->hist_sweeps[ctl->hist_n % 4096u] = ctl->step_sweeps;
+    ctl->hist_n++;
+    if (ctl->steps_left > 0) ctl->steps_left--;
+    if (in_graph)
+      cudaGraphSetConditional((cudaGraphConditionalHandle)h_step, (ctl->steps_left > 0 && ctl->continue_step) ? 1 : 0);
+  }
+}
+
+}  // namespace sts

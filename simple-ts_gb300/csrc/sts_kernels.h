@@ -1,0 +1,35 @@
+// Kernel declarations of the GB300 SIMPLE-TS step (FP64, bit-exact variant in sts_exact.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "sts_common.cuh"
+
+namespace sts {
+
+// Phases of k_boundary, run in this order when selected.
+enum : unsigned {
+  PH_CONTROL = 1u << 0,      // loop control after the velocity correction (SIMPLE_TS_MPI.cpp:4406-4450)
+  PH_SLIP_U = 1u << 1,       // SIMPLE_TS_MPI.cpp:7098-7213
+  PH_SLIP_V = 1u << 2,       // SIMPLE_TS_MPI.cpp:7216-7331
+  PH_VEL = 1u << 3,          // SIMPLE_TS_MPI.cpp:6790-7096
+  PH_PBEGIN = 1u << 4,       // SIMPLE_TS_MPI.cpp:7430-7647
+  PH_TJUMP = 1u << 5,        // SIMPLE_TS_MPI.cpp:7744-8045
+  PH_TJUMP_WRITE = 1u << 6,  // SIMPLE_TS_MPI.cpp:8048-8099 (output-time overwrite of wall temperatures)
+  PH_TEMP = 1u << 7,         // SIMPLE_TS_MPI.cpp:7650-7741
+  PH_PRES = 1u << 8,         // SIMPLE_TS_MPI.cpp:7335-7428
+  PH_PINIT = 1u << 9,        // SIMPLE_TS_MPI.cpp:2942-2979 (set-up only)
+  PH_ALL_STEP = PH_CONTROL | PH_SLIP_U | PH_SLIP_V | PH_VEL | PH_PBEGIN | PH_TJUMP | PH_TEMP | PH_PRES,
+};
+
+__global__ void k_step_begin(Geo g, int counters, unsigned long long h_outer, int in_graph);
+__global__ void k_apply_bodies(Geo g);
+__global__ void k_assemble(Geo g, unsigned long long h_sweep, int in_graph);
+__global__ void k_sweep(Geo g, unsigned long long h_sweep, int in_graph);
+__global__ void k_correct(Geo g);
+__global__ void k_face_rho(Geo g);
+__global__ void k_flux_diff(Geo g);
+__global__ void k_sqrt_rho(Geo g, int do_rho);
+__global__ void k_boundary(Geo g, unsigned phases, unsigned long long h_outer, int in_graph);
+__global__ void k_step_end(Geo g, unsigned long long h_step, int in_graph);
+
+}  // namespace sts

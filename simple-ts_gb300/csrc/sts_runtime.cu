@@ -1,0 +1,684 @@
+// Device context, set-up sequence, step orchestration (CUDA graph with
+// conditional WHILE nodes) and the C ABI of libsts_gb300.so.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <ctime>
+#include <fstream>
+#include <memory>
+#include <tuple>
+#include <algorithm>
+#include <iomanip>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "sts_common.cuh"
+#include "sts_host.h"
+#include "sts_kernels.h"
+#include "../../include/sts_gb300.h"
+
+using namespace sts;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CU(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(STS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));    \
+  } while (0)
+
+}  // namespace
+
+struct sts_ctx {
+  Case hc;
+  Geo g{};
+  Ctl* d_ctl = nullptr;
+  Ctl* h_ctl = nullptr;  // pinned mirror
+  cudaStream_t s = nullptr;
+  sts_options opt{};
+  std::vector<void*> allocs;
+  dim3 grid, block;
+  bool finished = false;
+  // graph
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  unsigned long long h_step = 0, h_outer = 0, h_sweep = 0;
+  std::chrono::steady_clock::time_point t0;
+  bool tmp_fresh = true, iter_fresh = true;
+
+  ~sts_ctx() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (void* p : allocs) cudaFree(p);
+    if (h_ctl) cudaFreeHost(h_ctl);
+    if (s) cudaStreamDestroy(s);
+  }
+
+  template <class T>
+  int alloc(T** p, size_t n) {
+    void* q = nullptr;
+    CU(cudaMalloc(&q, sizeof(T) * (n ? n : 1)));
+    CU(cudaMemsetAsync(q, 0, sizeof(T) * (n ? n : 1), s));
+    allocs.push_back(q);
+    *p = (T*)q;
+    return STS_OK;
+  }
+  template <class T>
+  int upload(T* dst, const std::vector<T>& src) {
+    if (!src.empty()) CU(cudaMemcpyAsync(dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice, s));
+    return STS_OK;
+  }
+  int read_ctl() {
+    CU(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    return STS_OK;
+  }
+  int check() {
+    CU(cudaGetLastError());
+    return STS_OK;
+  }
+  // launches
+  void boundary(unsigned ph) { k_boundary<<<1, 1024, 0, s>>>(g, ph, 0, 0); }
+  int build_graph();
+  int step_host(int n, int* done);
+  int step_graph(int n, int* done);
+  int write_outputs();
+  int write_logs();
+};
+
+namespace {
+
+// Adds a kernel node; the argument values are copied into the node.
+template <class... P, class... A>
+int add_kernel(cudaGraphNode_t* node, cudaGraph_t graph, const std::vector<cudaGraphNode_t>& deps, void (*f)(P...),
+               dim3 grid, dim3 block, A... args) {
+  std::tuple<P...> vals(args...);
+  void* argv[sizeof...(P)];
+  std::apply([&](auto&... x) {
+    int k = 0;
+    ((argv[k++] = (void*)&x), ...);
+  }, vals);
+  cudaKernelNodeParams p{};
+  p.func = (void*)f;
+  p.gridDim = grid;
+  p.blockDim = block;
+  p.sharedMemBytes = 0;
+  p.kernelParams = argv;
+  CU(cudaGraphAddKernelNode(node, graph, deps.data(), deps.size(), &p));
+  return STS_OK;
+}
+
+int add_while(cudaGraphNode_t* node, cudaGraph_t graph, const std::vector<cudaGraphNode_t>& deps,
+              cudaGraphConditionalHandle h, cudaGraph_t* body) {
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  CU(cudaGraphAddNode(node, graph, deps.data(), nullptr, deps.size(), &cp));
+  *body = cp.conditional.phGraph_out[0];
+  return STS_OK;
+}
+
+}  // namespace
+
+// The whole multi-step loop as one graph:
+//   WHILE(step) { step_begin -> WHILE(outer) { assemble -> WHILE(sweep){sweep} -> correct ->
+//                 face_rho -> boundary -> flux_diff } -> step_end }
+// Every decision (sweep count, outer iterations, end of run) is taken on the device.
+int sts_ctx::build_graph() {
+  CU(cudaGraphCreate(&graph, 0));
+  cudaGraphConditionalHandle hs;
+  CU(cudaGraphConditionalHandleCreate(&hs, graph, 1, cudaGraphCondAssignDefault));
+  cudaGraphNode_t n_step;
+  cudaGraph_t b_step;
+  if (int r = add_while(&n_step, graph, {}, hs, &b_step)) return r;
+  cudaGraphConditionalHandle ho;
+  CU(cudaGraphConditionalHandleCreate(&ho, b_step, 1, cudaGraphCondAssignDefault));
+  cudaGraphNode_t n_begin, n_outer, n_end;
+  if (int r = add_kernel(&n_begin, b_step, {}, k_step_begin, grid, block, g, 1, (unsigned long long)ho, 1)) return r;
+  cudaGraph_t b_outer;
+  if (int r = add_while(&n_outer, b_step, {n_begin}, ho, &b_outer)) return r;
+  if (int r = add_kernel(&n_end, b_step, {n_outer}, k_step_end, dim3(1), dim3(1024), g, (unsigned long long)hs, 1))
+    return r;
+  cudaGraphConditionalHandle hw;
+  CU(cudaGraphConditionalHandleCreate(&hw, b_outer, 1, cudaGraphCondAssignDefault));
+  cudaGraphNode_t n_asm, n_sw, n_cor, n_rho, n_bnd, n_fd;
+  if (int r = add_kernel(&n_asm, b_outer, {}, k_assemble, grid, block, g, (unsigned long long)hw, 1)) return r;
+  cudaGraph_t b_sweep;
+  if (int r = add_while(&n_sw, b_outer, {n_asm}, hw, &b_sweep)) return r;
+  cudaGraphNode_t n_one;
+  if (int r = add_kernel(&n_one, b_sweep, {}, k_sweep, grid, block, g, (unsigned long long)hw, 1)) return r;
+  if (int r = add_kernel(&n_cor, b_outer, {n_sw}, k_correct, grid, block, g)) return r;
+  if (int r = add_kernel(&n_rho, b_outer, {n_cor}, k_face_rho, grid, block, g)) return r;
+  if (int r = add_kernel(&n_bnd, b_outer, {n_rho}, k_boundary, dim3(1), dim3(1024), g, (unsigned)PH_ALL_STEP,
+                         (unsigned long long)ho, 1))
+    return r;
+  if (int r = add_kernel(&n_fd, b_outer, {n_bnd}, k_flux_diff, grid, block, g)) return r;
+  CU(cudaGraphInstantiate(&exec, graph, 0));
+  h_step = hs;
+  h_outer = ho;
+  h_sweep = hw;
+  return STS_OK;
+}
+
+int sts_ctx::step_graph(int n, int* done) {
+  if (!exec)
+    if (int r = build_graph()) return r;
+  const unsigned before = h_ctl->it_counter;
+  unsigned left = (unsigned)n;
+  CU(cudaMemcpyAsync(&d_ctl->steps_left, &left, sizeof(unsigned), cudaMemcpyHostToDevice, s));
+  CU(cudaGraphLaunch(exec, s));
+  if (int r = read_ctl()) return r;
+  *done = (int)(h_ctl->it_counter - before);
+  return STS_OK;
+}
+
+// Kernel-by-kernel variant: the device still decides every sweep; the host only
+// checks after each batch of sweep launches whether the loop has stopped.
+int sts_ctx::step_host(int n, int* done) {
+  const bool fixed = hc.bits & F_FIXED_SWEEPS;
+  const int NI = (int)hc.cfg.n("N_I"), Npc = (int)hc.cfg.n("N_I_p_c");
+  int k = 0;
+  for (; k < n; k++) {
+    k_step_begin<<<grid, block, 0, s>>>(g, 1, 0, 0);
+    for (int outer = 0; outer < NI; outer++) {
+      k_assemble<<<grid, block, 0, s>>>(g, 0, 0);
+      if (fixed) {
+        for (int q = 0; q < Npc; q++) k_sweep<<<grid, block, 0, s>>>(g, 0, 0);
+      } else {
+        int launched = 0;
+        for (;;) {
+          const int batch = 4;
+          for (int q = 0; q < batch && launched < Npc; q++, launched++) k_sweep<<<grid, block, 0, s>>>(g, 0, 0);
+          if (int r = read_ctl()) return r;
+          if (h_ctl->pt_done || launched >= Npc) break;
+        }
+      }
+      k_correct<<<grid, block, 0, s>>>(g);
+      k_face_rho<<<grid, block, 0, s>>>(g);
+      k_boundary<<<1, 1024, 0, s>>>(g, PH_ALL_STEP, 0, 0);
+      k_flux_diff<<<grid, block, 0, s>>>(g);
+      if (NI > 1) {
+        if (int r = read_ctl()) return r;
+        if (!h_ctl->continue_iter) break;
+      }
+    }
+    k_step_end<<<1, 1024, 0, s>>>(g, 0, 0);
+    if (int r = check()) return r;
+    if (int r = read_ctl()) return r;
+    if (!h_ctl->continue_step) {
+      k++;
+      break;
+    }
+  }
+  *done = k;
+  return STS_OK;
+}
+
+namespace {
+
+void write_bin(const std::string& f, const void* a, size_t bytes) {
+  FILE* fp = std::fopen(f.c_str(), "wb");
+  if (!fp) return;
+  std::fwrite(a, 1, bytes, fp);
+  std::fclose(fp);
+}
+
+template <class T>
+void write_txt(const std::string& f, const T* a, int n) {
+  std::ofstream o(f.c_str());
+  for (int k = 0; k < n; k++) o << std::setiosflags(std::ios::scientific) << std::setprecision(15) << a[k] << "\n";
+}
+
+std::string num(double x) {
+  std::ostringstream o;
+  o << x;
+  return o.str();
+}
+
+}  // namespace
+
+// WriteSolvedDataToFile (SIMPLE_TS_MPI.cpp:5564-5731): the wall-temperature overwrite is a
+// side effect on the state, then the dumps, it_begin.txt and EnteredData.txt.
+int sts_ctx::write_outputs() {
+  boundary(PH_TJUMP | PH_TJUMP_WRITE);
+  if (int r = check()) return r;
+  if (!opt.write_files) return STS_OK;
+  const int Na = hc.Na;
+  std::vector<double> buf(Na);
+  if (int r = read_ctl()) return r;
+  const unsigned cur = h_ctl->cur;
+  const double* src[4] = {g.u, g.v, g.p[cur], g.T[cur]};
+  const char* names[4] = {"u", "v", "p", "Temper"};
+  const bool bin = hc.cfg.b("ToWriteSolvedDataToBinaryFile");
+  const bool newf = hc.cfg.b("ToWriteSolvedDataToNewFiles");
+  const std::string its = num(h_ctl->it);
+  for (int k = 0; k < 4; k++) {
+    CU(cudaMemcpy(buf.data(), src[k], sizeof(double) * Na, cudaMemcpyDeviceToHost));
+    const std::string base = hc.dir + "/" + names[k];
+    if (bin) {
+      write_bin(base + ".bin", buf.data(), sizeof(double) * Na);
+      if (newf) write_bin(base + "." + its + ".bin", buf.data(), sizeof(double) * Na);
+    } else {
+      write_txt(base + ".txt", buf.data(), Na);
+      if (newf) write_txt(base + "." + its + ".txt", buf.data(), Na);
+    }
+  }
+  if (bin) {
+    write_bin(hc.dir + "/vol_inf_fb.bin", hc.vol_file.data(), sizeof(uint32_t) * Na);
+    if (newf) write_bin(hc.dir + "/vol_inf_fb." + its + ".bin", hc.vol_file.data(), sizeof(uint32_t) * Na);
+  } else {
+    write_txt(hc.dir + "/vol_inf_fb.txt", hc.vol_file.data(), Na);
+  }
+  std::ofstream itf((hc.dir + "/it_begin.txt").c_str());
+  itf << h_ctl->it << std::endl;
+  write_config(hc.dir + "/EnteredData.txt", hc.cfg);
+  return STS_OK;
+}
+
+// WriteTempDataToFile and WriteIterationsInLoopsToFile (SIMPLE_TS_MPI.cpp:5838-6006).
+int sts_ctx::write_logs() {
+  if (!opt.write_files) return STS_OK;
+  if (int r = read_ctl()) return r;
+  const Ctl& c = *h_ctl;
+  {
+    std::ofstream o;
+    if (tmp_fresh && !hc.restart) o.open((hc.dir + "/Tmp.txt").c_str());
+    else o.open((hc.dir + "/Tmp.txt").c_str(), std::ios::out | std::ios::app);
+    o << "it = " << c.it << "\tit_counter = " << c.it_counter << "\tIter = " << c.Iter << "\tIter_p_c = " << c.Iter_p_c
+      << "\tIter_T = " << (unsigned)hc.cfg.n("N_I_T") << std::endl;
+    unsigned sum = 0;
+    for (unsigned k = 0; k < c.Iter && k < 64; k++) {
+      o << "\t" << k << "\t" << c.sweeps[k] << std::setiosflags(std::ios::scientific) << std::setprecision(15) << "\t"
+        << c.res_p0[k] << "\t" << c.res_p[k] << "\t" << c.res_T0[k] << "\t" << c.res_T[k] << std::endl;
+      sum += c.sweeps[k];
+    }
+    o << "\t\t" << sum << std::endl;
+    o << std::setiosflags(std::ios::scientific) << std::setprecision(15) << "\t" << c.res_u0 << "\t" << c.res_u
+      << std::endl
+      << "\t" << c.res_v0 << "\t" << c.res_v << std::endl;
+    tmp_fresh = false;
+  }
+  {
+    std::ofstream o;
+    if (iter_fresh) {
+      if (hc.restart) o.open((hc.dir + "/Iterations_in_loops.txt").c_str(), std::ios::out | std::ios::app);
+      else {
+        o.open((hc.dir + "/Iterations_in_loops.txt").c_str());
+        o << "it" << "\tit_counter" << "\tIter" << "\tsum_max_Iter_p_c" << std::endl;
+      }
+    } else {
+      o.open((hc.dir + "/Iterations_in_loops.txt").c_str(), std::ios::out | std::ios::app);
+    }
+    unsigned sum = 0;
+    for (unsigned k = 0; k < c.Iter && k < 64; k++) sum += c.sweeps[k];
+    o << c.it << "\t" << c.it_counter << "\t\t" << c.Iter << "\t" << sum << std::endl;
+    iter_fresh = false;
+  }
+  return STS_OK;
+}
+
+namespace {
+
+int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
+  if (!dir || !out) return fail(STS_ERR_ARG, "null argument");
+  sts_options opt;
+  sts_default_options(&opt);
+  if (opt_in) opt = *opt_in;
+  std::unique_ptr<sts_ctx> c(new sts_ctx);
+  c->opt = opt;
+  c->t0 = std::chrono::steady_clock::now();
+  std::string err;
+  if (!load_case(dir, opt.fixed_sweeps != 0, c->hc, err)) return fail(STS_ERR_INPUT, err);
+  Case& h = c->hc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(STS_ERR_CUDA, "no CUDA device");
+  if (opt.device < 0 || opt.device >= ndev) return fail(STS_ERR_ARG, "bad device ordinal");
+  CU(cudaSetDevice(opt.device));
+  CU(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking));
+  CU(cudaMallocHost(&c->h_ctl, sizeof(Ctl)));
+  std::memset(c->h_ctl, 0, sizeof(Ctl));
+  const int Na = h.Na;
+  Geo& g = c->g;
+  g.Nx = h.Nx;
+  g.Ny = h.Ny;
+  g.Na = Na;
+  g.bits = h.bits;
+  g.Nx_u0 = h.Nx_u[0]; g.Nx_u1 = h.Nx_u[1]; g.Ny_u0 = h.Ny_u[0]; g.Ny_u1 = h.Ny_u[1];
+  g.Nx_v0 = h.Nx_v[0]; g.Nx_v1 = h.Nx_v[1]; g.Ny_v0 = h.Ny_v[0]; g.Ny_v1 = h.Ny_v[1];
+  g.Nx_o0 = h.Nx_o[0]; g.Nx_o1 = h.Nx_o[1]; g.Ny_o0 = h.Ny_o[0]; g.Ny_o1 = h.Ny_o[1];
+  const Config& cf = h.cfg;
+  g.ht = cf.d("ht");
+  g.gamma1 = cf.d("gamma1");
+  g.Kn = cf.d("Kn");
+  g.cT1 = h.cT1;
+  g.cT2 = h.cT2;
+  g.c_Fr_v = h.c_Fr_v;
+  g.Re = cf.d("Re");
+  g.Ma = cf.d("Ma");
+  g.T_BC_xb = cf.d("T_BC_xb");
+  g.T_BC_xe = cf.d("T_BC_xe");
+  g.u_given_xb_error = cf.d("u_given_xb_error");
+  g.p_correction_min = cf.d("p_correction_min");
+  g.p_correction_max = cf.d("p_correction_max");
+  g.MaxError_Velocities = cf.d("MaxError_Velocities");
+  g.MaxError_p_c = cf.d("MaxError_p_c");
+  g.MaxError_T = cf.d("MaxError_T");
+  g.MaxError_to_stop_program = cf.d("MaxError_to_stop_program");
+  g.Nt = cf.d("Nt");
+  g.t_BC_b = cf.d("t_BC_b");
+  g.t_BC_e = cf.d("t_BC_e");
+  g.u_BC_xb_t_BC_b = cf.d("u_BC_xb_t_BC_b");
+  g.u_BC_xb_t_BC_e = cf.d("u_BC_xb_t_BC_e");
+  g.TypeND = (int)cf.n("TypeOfNonDimensiolization");
+  g.N_I = (int)cf.n("N_I");
+  g.N_I_p_c = (int)cf.n("N_I_p_c");
+  g.p_corr_method = (int)cf.n("p_BC_xb_correction_method");
+
+  // static data
+  double *hx, *hy;
+  uint8_t* cls;
+  uint32_t* vid;
+  Body* bodies;
+  int *su, *sv, *tj;
+  uint8_t *suf, *svf, *tjf, *tjw;
+  if (int r = c->alloc(&hx, h.Nx)) return r;
+  if (int r = c->alloc(&hy, h.Ny)) return r;
+  if (int r = c->alloc(&cls, Na)) return r;
+  if (int r = c->alloc(&vid, Na)) return r;
+  if (int r = c->alloc(&bodies, h.bodies.size())) return r;
+  if (int r = c->alloc(&su, h.slip_u.size())) return r;
+  if (int r = c->alloc(&sv, h.slip_v.size())) return r;
+  if (int r = c->alloc(&tj, h.tjump.size())) return r;
+  if (int r = c->alloc(&suf, h.slip_u.size())) return r;
+  if (int r = c->alloc(&svf, h.slip_v.size())) return r;
+  if (int r = c->alloc(&tjf, h.tjump.size())) return r;
+  if (int r = c->alloc(&tjw, h.tjump.size())) return r;
+  std::vector<Body> bv;
+  for (const HostBody& b : h.bodies) bv.push_back(b.dev);
+  if (int r = c->upload(hx, h.hx)) return r;
+  if (int r = c->upload(hy, h.hy)) return r;
+  if (int r = c->upload(cls, h.cls)) return r;
+  if (int r = c->upload(vid, h.vol_file)) return r;
+  if (int r = c->upload(bodies, bv)) return r;
+  if (int r = c->upload(su, h.slip_u)) return r;
+  if (int r = c->upload(sv, h.slip_v)) return r;
+  if (int r = c->upload(tj, h.tjump)) return r;
+  if (int r = c->upload(suf, h.slip_u_fin)) return r;
+  if (int r = c->upload(svf, h.slip_v_fin)) return r;
+  if (int r = c->upload(tjf, h.tjump_fin)) return r;
+  if (int r = c->upload(tjw, h.tjump_wr_fin)) return r;
+  g.hx = hx; g.hy = hy; g.cls = cls; g.vol_id = vid; g.bodies = bodies;
+  g.slip_u = su; g.slip_v = sv; g.tjump = tj;
+  g.slip_u_fin = suf; g.slip_v_fin = svf; g.tjump_fin = tjf; g.tjump_wr_fin = tjw;
+  g.n_slip_u = (int)h.slip_u.size();
+  g.n_slip_v = (int)h.slip_v.size();
+  g.n_tjump = (int)h.tjump.size();
+
+  // fields
+  double** fields[] = {&g.u, &g.v, &g.u_pr, &g.v_pr, &g.p[0], &g.p[1], &g.T[0], &g.T[1], &g.p_pr, &g.T_pr, &g.rho,
+                       &g.rho_pr, &g.sqrt_T, &g.rho_u, &g.rho_v, &g.Fx, &g.Fy, &g.D_ux, &g.D_uy, &g.D_vx, &g.D_vy,
+                       &g.DTx, &g.DTy, &g.Gamma_xf, &g.Gamma_yf, &g.u_pseudo, &g.v_pseudo, &g.d12, &g.d34, &g.apx,
+                       &g.apy, &g.bpx, &g.bpy, &g.ScT1, &g.Tw_u, &g.Tw_v};
+  for (double** f : fields)
+    if (int r = c->alloc(f, Na)) return r;
+  if (int r = c->alloc(&c->d_ctl, 1)) return r;
+  g.ctl = c->d_ctl;
+  if (int r = c->upload(g.u, h.u)) return r;
+  if (int r = c->upload(g.v, h.v)) return r;
+  if (int r = c->upload(g.p[0], h.p)) return r;
+  if (int r = c->upload(g.p[1], h.p)) return r;
+  if (int r = c->upload(g.T[0], h.T)) return r;
+  if (int r = c->upload(g.T[1], h.T)) return r;
+  if (int r = c->upload(g.rho, h.rho)) return r;
+
+  // control block
+  Ctl& ct = *c->h_ctl;
+  ct.cT = h.cT;
+  ct.cPch = h.cPch;
+  ct.p_BC_xb = h.p_BC_xb;
+  ct.p_BC_xe = h.p_BC_xe;
+  ct.u_given_xb = h.u_given_xb;
+  ct.u_given_xb_in_it = h.u_given_xb_in_it;
+  ct.p_correction = cf.d("p_correction");
+  ct.u_gas_nd = cf.d("u_gas_nd");
+  ct.it = h.restart ? h.it_begin : 0.0;
+  ct.continue_step = 1;
+  CU(cudaMemcpyAsync(c->d_ctl, c->h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, c->s));
+
+  c->block = dim3(32, 8);
+  c->grid = dim3((h.Nx + 31) / 32, (h.Ny + 7) / 8);
+  const dim3 G = c->grid, B = c->block;
+  cudaStream_t s = c->s;
+
+  // the rest of main() before the time loop (SIMPLE_TS_MPI.cpp:2833-3227), on the device
+  if (!h.restart) {
+    k_step_begin<<<G, B, 0, s>>>(g, 0, 0, 0);  // *_pr copies
+    k_face_rho<<<G, B, 0, s>>>(g);
+    c->boundary(PH_VEL);
+    k_step_begin<<<G, B, 0, s>>>(g, 0, 0, 0);
+    k_face_rho<<<G, B, 0, s>>>(g);
+    if (int r = c->write_outputs()) return r;  // the set-up save (SIMPLE_TS_MPI.cpp:2863)
+  }
+  for (double* f : {g.d12, g.d34, g.apx, g.apy, g.bpx, g.bpy, g.Gamma_yf, g.Gamma_xf, g.Fx, g.Fy, g.u_pseudo,
+                    g.v_pseudo, g.D_ux, g.D_uy, g.D_vx, g.D_vy, g.DTx, g.DTy, g.ScT1, g.rho_u, g.rho_v})
+    CU(cudaMemsetAsync(f, 0, sizeof(double) * Na, s));
+  if (!h.restart) c->boundary(PH_PINIT);
+  if (cf.b("ToContinueFromInterpolation")) {
+    k_apply_bodies<<<G, B, 0, s>>>(g);
+    c->boundary(PH_SLIP_U | PH_SLIP_V | PH_TJUMP | PH_TJUMP_WRITE);
+  }
+  k_sqrt_rho<<<G, B, 0, s>>>(g, 1);
+  k_face_rho<<<G, B, 0, s>>>(g);
+  k_step_begin<<<G, B, 0, s>>>(g, 0, 0, 0);
+  k_sqrt_rho<<<G, B, 0, s>>>(g, 0);
+  k_face_rho<<<G, B, 0, s>>>(g);
+  c->boundary(PH_SLIP_U | PH_SLIP_V | PH_VEL | PH_PBEGIN | PH_TJUMP | PH_TEMP | PH_PRES);
+  k_flux_diff<<<G, B, 0, s>>>(g);
+  if (int r = c->check()) return r;
+  if (int r = c->read_ctl()) return r;
+  *out = c.release();
+  return STS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void sts_default_options(sts_options* opt) {
+  if (!opt) return;
+  opt->fixed_sweeps = 1;
+  opt->use_graph = 1;
+  opt->device = 0;
+  opt->write_files = 1;
+}
+
+int sts_open_case(const char* case_dir, const sts_options* opt, sts_ctx** out) {
+  g_err.clear();
+  if (out) *out = nullptr;
+  sts_options o;
+  sts_default_options(&o);
+  if (opt) o = *opt;
+  o.write_files = opt ? opt->write_files : 0;
+  return open_impl(case_dir, &o, out);
+}
+
+int sts_step(sts_ctx* ctx, int nsteps, int* steps_done) {
+  if (!ctx || nsteps < 0) return fail(STS_ERR_ARG, "bad argument");
+  int done = 0;
+  if (!ctx->finished && nsteps > 0) {
+    CU(cudaSetDevice(ctx->opt.device));
+    const unsigned status_before = ctx->h_ctl->status;
+    int r = ctx->opt.use_graph ? ctx->step_graph(nsteps, &done) : ctx->step_host(nsteps, &done);
+    if (r) return r;
+    if (!ctx->h_ctl->continue_step) ctx->finished = true;
+    if (ctx->h_ctl->status & ~status_before & 1u) {
+      if (steps_done) *steps_done = done;
+      return fail(STS_ERR_NONFINITE, "a residual became NaN or Inf");
+    }
+  }
+  if (steps_done) *steps_done = done;
+  return STS_OK;
+}
+
+int sts_get_field(sts_ctx* ctx, const char* name, double* out) {
+  if (!ctx || !name || !out) return fail(STS_ERR_ARG, "null argument");
+  CU(cudaSetDevice(ctx->opt.device));
+  if (int r = ctx->read_ctl()) return r;
+  const Geo& g = ctx->g;
+  const std::string n(name);
+  const unsigned cur = ctx->h_ctl->cur;
+  const double* src = nullptr;
+  if (n == "hx") { std::memcpy(out, ctx->hc.hx.data(), sizeof(double) * g.Nx); return STS_OK; }
+  if (n == "hy") { std::memcpy(out, ctx->hc.hy.data(), sizeof(double) * g.Ny); return STS_OK; }
+  if (n == "x_v") { std::memcpy(out, ctx->hc.x_v.data(), sizeof(double) * g.Nx); return STS_OK; }
+  if (n == "y_v") { std::memcpy(out, ctx->hc.y_v.data(), sizeof(double) * g.Ny); return STS_OK; }
+  struct { const char* k; const double* p; } tab[] = {
+      {"u", g.u}, {"v", g.v}, {"p", g.p[cur]}, {"T", g.T[cur]}, {"rho", g.rho}, {"sqrt_T", g.sqrt_T},
+      {"rho_u", g.rho_u}, {"rho_v", g.rho_v}, {"Fx", g.Fx}, {"Fy", g.Fy}, {"D_ux", g.D_ux}, {"D_uy", g.D_uy},
+      {"D_vx", g.D_vx}, {"D_vy", g.D_vy}, {"DTx", g.DTx}, {"DTy", g.DTy}, {"Gamma_xf", g.Gamma_xf},
+      {"Gamma_yf", g.Gamma_yf}, {"ScT1", g.ScT1}, {"apx", g.apx}, {"apy", g.apy}, {"bpx", g.bpx}, {"bpy", g.bpy},
+      {"u_pseudo", g.u_pseudo}, {"v_pseudo", g.v_pseudo}, {"d_p_c_12", g.d12}, {"d_p_c_34", g.d34},
+      {"Tw_u", g.Tw_u}, {"Tw_v", g.Tw_v}};
+  for (auto& t : tab)
+    if (n == t.k) src = t.p;
+  if (!src) return fail(STS_ERR_ARG, "unknown field " + n);
+  CU(cudaMemcpyAsync(out, src, sizeof(double) * g.Na, cudaMemcpyDeviceToHost, ctx->s));
+  CU(cudaStreamSynchronize(ctx->s));
+  return STS_OK;
+}
+
+int sts_set_field(sts_ctx* ctx, const char* name, const double* in) {
+  if (!ctx || !name || !in) return fail(STS_ERR_ARG, "null argument");
+  CU(cudaSetDevice(ctx->opt.device));
+  if (int r = ctx->read_ctl()) return r;
+  const Geo& g = ctx->g;
+  const std::string n(name);
+  const unsigned cur = ctx->h_ctl->cur;
+  double* dst = nullptr;
+  if (n == "u") dst = g.u;
+  else if (n == "v") dst = g.v;
+  else if (n == "p") dst = g.p[cur];
+  else if (n == "T") dst = g.T[cur];
+  if (!dst) return fail(STS_ERR_ARG, "field cannot be set: " + n);
+  CU(cudaMemcpyAsync(dst, in, sizeof(double) * g.Na, cudaMemcpyHostToDevice, ctx->s));
+  CU(cudaStreamSynchronize(ctx->s));
+  return STS_OK;
+}
+
+int sts_dims(sts_ctx* ctx, int* Nx, int* Ny) {
+  if (!ctx) return fail(STS_ERR_ARG, "null context");
+  if (Nx) *Nx = ctx->g.Nx;
+  if (Ny) *Ny = ctx->g.Ny;
+  return STS_OK;
+}
+
+int sts_stats(sts_ctx* ctx, double* out) {
+  if (!ctx || !out) return fail(STS_ERR_ARG, "null argument");
+  if (int r = ctx->read_ctl()) return r;
+  const Ctl& c = *ctx->h_ctl;
+  const unsigned I = c.Iter ? (c.Iter - 1 < 64 ? c.Iter - 1 : 63) : 0;
+  out[0] = c.Iter; out[1] = c.Iter_p_c; out[2] = c.res_p0[I]; out[3] = c.res_p[I]; out[4] = c.res_T0[I];
+  out[5] = c.res_T[I]; out[6] = c.res_u; out[7] = c.res_v; out[8] = c.it;
+  return STS_OK;
+}
+
+int sts_sweep_history(sts_ctx* ctx, unsigned int* out, int cap, int* n_out) {
+  if (!ctx || !out || cap < 0) return fail(STS_ERR_ARG, "bad argument");
+  if (int r = ctx->read_ctl()) return r;
+  const Ctl& c = *ctx->h_ctl;
+  const unsigned avail = c.hist_n < 4096u ? c.hist_n : 4096u;
+  const unsigned n = (unsigned)cap < avail ? (unsigned)cap : avail;
+  for (unsigned k = 0; k < n; k++) out[k] = c.hist_sweeps[(c.hist_n - n + k) % 4096u];
+  if (n_out) *n_out = (int)n;
+  return STS_OK;
+}
+
+int sts_write_outputs(sts_ctx* ctx) {
+  if (!ctx) return fail(STS_ERR_ARG, "null context");
+  CU(cudaSetDevice(ctx->opt.device));
+  const int w = ctx->opt.write_files;
+  ctx->opt.write_files = 1;
+  const int r = ctx->write_outputs();
+  ctx->opt.write_files = w;
+  return r;
+}
+
+int sts_run_case(const char* case_dir, const sts_options* opt) {
+  sts_options o;
+  sts_default_options(&o);
+  if (opt) o = *opt;
+  sts_ctx* ctx = nullptr;
+  g_err.clear();
+  if (int r = open_impl(case_dir, &o, &ctx)) return r;
+  std::unique_ptr<sts_ctx> guard(ctx);
+  const Config& cf = ctx->hc.cfg;
+  const long save_every = cf.n("Nt_save_solved_data") > 0 ? cf.n("Nt_save_solved_data") : 1;
+  const long log_every = cf.n("Nt_save_temp_data") > 0 ? cf.n("Nt_save_temp_data") : 1;
+  long save_c = 0, log_c = 0;
+  while (!ctx->finished) {
+    const long chunk = std::min(save_every - save_c, log_every - log_c);
+    int done = 0;
+    const int r = sts_step(ctx, (int)chunk, &done);
+    if (r && r != STS_ERR_NONFINITE) return r;
+    save_c += done;
+    log_c += done;
+    if (save_c >= save_every) {
+      if (int q = ctx->write_outputs()) return q;
+      save_c = 0;
+    }
+    if (log_c >= log_every) {
+      if (int q = ctx->write_logs()) return q;
+      log_c = 0;
+    }
+    if (done == 0) break;
+  }
+  // after the loop (SIMPLE_TS_MPI.cpp:4695-4714)
+  const double hours = std::chrono::duration<double>(std::chrono::steady_clock::now() - ctx->t0).count() / 3600.0;
+  ctx->hc.cfg.set("max_time_for_solve", hours);
+  if (int q = ctx->write_outputs()) return q;
+  if (int q = ctx->write_logs()) return q;
+  return STS_OK;
+}
+
+int sts_sync(sts_ctx* ctx) {
+  if (!ctx) return fail(STS_ERR_ARG, "null context");
+  CU(cudaStreamSynchronize(ctx->s));
+  return STS_OK;
+}
+
+void sts_destroy(sts_ctx* ctx) { delete ctx; }
+
+const char* sts_last_error(void) { return g_err.c_str(); }
+
+int sts_inspect_case(const char* case_dir, int* Nx, int* Ny, unsigned int* vol_out, unsigned char* cls_out,
+                     double* hx_out, double* hy_out, double* xv_out, double* yv_out) {
+  if (!case_dir) return fail(STS_ERR_ARG, "null argument");
+  Case h;
+  std::string err;
+  if (!load_case(case_dir, true, h, err)) return fail(STS_ERR_INPUT, err);
+  if (Nx) *Nx = h.Nx;
+  if (Ny) *Ny = h.Ny;
+  if (vol_out) std::memcpy(vol_out, h.vol_id.data(), sizeof(unsigned) * h.Na);
+  if (cls_out) std::memcpy(cls_out, h.cls.data(), h.Na);
+  if (hx_out) std::memcpy(hx_out, h.hx.data(), sizeof(double) * h.Nx);
+  if (hy_out) std::memcpy(hy_out, h.hy.data(), sizeof(double) * h.Ny);
+  if (xv_out) std::memcpy(xv_out, h.x_v.data(), sizeof(double) * h.Nx);
+  if (yv_out) std::memcpy(yv_out, h.y_v.data(), sizeof(double) * h.Ny);
+  return STS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,182 @@
+"""Python binding of libsts_gb300.so (ctypes over the C ABI in include/sts_gb300.h).
+
+The library is the product; this module only loads it and converts arrays.  It
+fails loudly when the library has not been built: there is no Python or CPU
+fallback for the time step.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libsts_gb300.so")
+EXE_PATH = os.path.join(HERE, "_build", "simple_ts_gb300")
+
+STS_OK = 0
+STS_ERR_ARG = -1
+STS_ERR_INPUT = -2
+STS_ERR_CUDA = -3
+STS_ERR_NONFINITE = -4
+
+# every symbol include/sts_gb300.h declares
+EXPORTS = [
+    "sts_default_options", "sts_open_case", "sts_step", "sts_get_field", "sts_set_field", "sts_dims",
+    "sts_stats", "sts_sweep_history", "sts_write_outputs", "sts_run_case", "sts_sync", "sts_destroy",
+    "sts_last_error", "sts_inspect_case",
+]
+
+FIELDS = ["u", "v", "p", "T", "rho", "sqrt_T", "rho_u", "rho_v", "Fx", "Fy", "D_ux", "D_uy", "D_vx", "D_vy",
+          "DTx", "DTy", "Gamma_xf", "Gamma_yf", "ScT1", "apx", "apy", "bpx", "bpy", "u_pseudo", "v_pseudo",
+          "d_p_c_12", "d_p_c_34", "Tw_u", "Tw_v"]
+
+
+class Options(C.Structure):
+    _fields_ = [("fixed_sweeps", C.c_int), ("use_graph", C.c_int), ("device", C.c_int), ("write_files", C.c_int)]
+
+
+class StsError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"sts error {code}: {msg}")
+        self.code = code
+
+
+_lib: Optional[C.CDLL] = None
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} is missing: build it with simple-ts_gb300/build.py (no fallback exists)")
+    lib = C.CDLL(path)
+    P = C.c_void_p
+    dp = C.POINTER(C.c_double)
+    lib.sts_default_options.argtypes = [C.POINTER(Options)]
+    lib.sts_default_options.restype = None
+    lib.sts_open_case.argtypes = [C.c_char_p, C.POINTER(Options), C.POINTER(P)]
+    lib.sts_step.argtypes = [P, C.c_int, C.POINTER(C.c_int)]
+    lib.sts_get_field.argtypes = [P, C.c_char_p, dp]
+    lib.sts_set_field.argtypes = [P, C.c_char_p, dp]
+    lib.sts_dims.argtypes = [P, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    lib.sts_stats.argtypes = [P, dp]
+    lib.sts_sweep_history.argtypes = [P, C.POINTER(C.c_uint), C.c_int, C.POINTER(C.c_int)]
+    lib.sts_write_outputs.argtypes = [P]
+    lib.sts_run_case.argtypes = [C.c_char_p, C.POINTER(Options)]
+    lib.sts_sync.argtypes = [P]
+    lib.sts_destroy.argtypes = [P]
+    lib.sts_destroy.restype = None
+    lib.sts_last_error.argtypes = []
+    lib.sts_last_error.restype = C.c_char_p
+    lib.sts_inspect_case.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_uint),
+                                     C.POINTER(C.c_ubyte), dp, dp, dp, dp]
+    _lib = lib
+    return lib
+
+
+def _check(code: int):
+    if code != STS_OK:
+        raise StsError(code, load().sts_last_error().decode())
+
+
+def options(fixed_sweeps=True, use_graph=True, device=0, write_files=False) -> Options:
+    o = Options()
+    load().sts_default_options(C.byref(o))
+    o.fixed_sweeps = int(fixed_sweeps)
+    o.use_graph = int(use_graph)
+    o.device = int(device)
+    o.write_files = int(write_files)
+    return o
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Solver:
+    """One case on one GPU: the reference's solve loop behind the C ABI."""
+
+    def __init__(self, case_dir: str, fixed_sweeps=True, use_graph=True, device=0):
+        lib = load()
+        self._h = C.c_void_p()
+        _check(lib.sts_open_case(case_dir.encode(), C.byref(options(fixed_sweeps, use_graph, device, False)),
+                                 C.byref(self._h)))
+        nx, ny = C.c_int(), C.c_int()
+        _check(lib.sts_dims(self._h, C.byref(nx), C.byref(ny)))
+        self.Nx, self.Ny = nx.value, ny.value
+
+    def step(self, n: int = 1, allow_nonfinite: bool = False) -> int:
+        done = C.c_int()
+        r = load().sts_step(self._h, int(n), C.byref(done))
+        if r == STS_ERR_NONFINITE and allow_nonfinite:
+            return done.value
+        _check(r)
+        return done.value
+
+    def field(self, name: str) -> np.ndarray:
+        n = self.Nx if name in ("hx", "x_v") else self.Ny if name in ("hy", "y_v") else self.Nx * self.Ny
+        out = np.empty(n, dtype=np.float64)
+        _check(load().sts_get_field(self._h, name.encode(), _dptr(out)))
+        return out if n != self.Nx * self.Ny else out.reshape(self.Ny, self.Nx)
+
+    def set_field(self, name: str, a: np.ndarray):
+        a = np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+        _check(load().sts_set_field(self._h, name.encode(), _dptr(a)))
+
+    def stats(self) -> np.ndarray:
+        out = np.zeros(9)
+        _check(load().sts_stats(self._h, _dptr(out)))
+        return out
+
+    def sweep_history(self, cap: int = 4096) -> np.ndarray:
+        out = np.zeros(cap, dtype=np.uint32)
+        n = C.c_int()
+        _check(load().sts_sweep_history(self._h, out.ctypes.data_as(C.POINTER(C.c_uint)), cap, C.byref(n)))
+        return out[: n.value]
+
+    def write_outputs(self):
+        _check(load().sts_write_outputs(self._h))
+
+    def sync(self):
+        _check(load().sts_sync(self._h))
+
+    def close(self):
+        if self._h:
+            load().sts_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def run_case(case_dir: str, fixed_sweeps=True, use_graph=True, device=0, write_files=True):
+    """The drop-in run: same effect as the reference binary in case_dir."""
+    _check(load().sts_run_case(case_dir.encode(), C.byref(options(fixed_sweeps, use_graph, device, write_files))))
+
+
+def inspect_case(case_dir: str) -> dict:
+    """Host-only set-up results (no GPU needed): mask, per-cell classes and mesh."""
+    lib = load()
+    nx, ny = C.c_int(), C.c_int()
+    _check(lib.sts_inspect_case(case_dir.encode(), C.byref(nx), C.byref(ny), None, None, None, None, None, None))
+    Nx, Ny = nx.value, ny.value
+    vol = np.empty(Nx * Ny, dtype=np.uint32)
+    cls = np.empty(Nx * Ny, dtype=np.uint8)
+    hx, hy, xv, yv = np.empty(Nx), np.empty(Ny), np.empty(Nx), np.empty(Ny)
+    _check(lib.sts_inspect_case(case_dir.encode(), C.byref(nx), C.byref(ny),
+                                vol.ctypes.data_as(C.POINTER(C.c_uint)), cls.ctypes.data_as(C.POINTER(C.c_ubyte)),
+                                _dptr(hx), _dptr(hy), _dptr(xv), _dptr(yv)))
+    return dict(Nx=Nx, Ny=Ny, vol=vol.reshape(Ny, Nx), cls=cls.reshape(Ny, Nx), hx=hx, hy=hy, x_v=xv, y_v=yv)

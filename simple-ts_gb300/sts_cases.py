@@ -458,3 +458,22 @@ def config_case(which: str, scale: float = 1.0, Nt: Optional[int] = None,
         return channel_case("channel_2048", s(2048), s(256), 0.5, 0.003, 1.25e-4,
                             Nt if Nt is not None else 1000, tol=tol)
     raise KeyError(which)
+
+
+def shipped_example(steps: int = 5) -> Case:
+    """The example input distributed with the reference: a pressure-driven channel
+    (p 3 -> 1, Kn 0.05) between two reservoirs on a 282x63 polynomial mesh.  The
+    EnteredData defaults above are its values; the two wall polygons are restated here."""
+    e: Dict[str, object] = {name: default for name, _, default in ENTERED_DATA}
+    e.update(Nt=steps, Nt_save_solved_data=steps, Nt_save_temp_data=1)
+    common = dict(p_body=0.0, T_body=1.0, slip=1, F_slip=1.1466, w_slip=0.0, jump=0, F_jump=2.1904, dTdn0=0.0)
+    low = Polygon(vertices=[(-100000.001, -0.99991), (0.000001, -0.99991), (0.000001, 0.00001), (10.00001, 0.00001),
+                            (10.00001, -0.99991), (100000.001, -0.99991), (100000.001, -100000.001),
+                            (-100000.001, -100000.001)],
+                  inside1=(100.01, -2000.1), inside2=(150.01, -2000.111), **common)
+    high = Polygon(vertices=[(-100000.001, 100000.001), (1000000.001, 100000.001), (1000000.001, 2.00001),
+                             (10.00001, 2.00001), (10.00001, 1.00001), (0.000001, 1.00001), (0.000001, 2.00001),
+                             (-100000.001, 2.000001)],
+                   inside1=(100.01, 2000.1), inside2=(150.01, 2000.111), **common)
+    return Case(name="shipped_example", entered=e, polygons=[low, high],
+                description="example input of the reference (282x63, Pressure_BC, Kn 0.05)")

@@ -1,0 +1,116 @@
+"""GB300 library against the reference (golden dumps) and the CPU oracle: bit-exact FP64."""
+import hashlib
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+import sts_cases as sc
+from conftest import golden_case
+
+pytestmark = pytest.mark.gpu
+
+NAMES = ["channel_ma0.1_80x8_resid", "channel_ma0.1_80x8_fixed", "channel_ma2.43_60x12_resid",
+         "rayleigh_benard_32x16_resid", "channel_circle_120x12_resid", "channel_ma0.1_400x40_resid_5steps",
+         "shipped_example_5steps"]
+
+ALL_FIELDS = ["u", "v", "p", "T", "rho", "sqrt_T", "rho_u", "rho_v", "Fx", "Fy", "D_ux", "D_uy", "D_vx", "D_vy",
+              "DTx", "DTy", "Gamma_xf", "Gamma_yf", "ScT1", "apx", "apy", "bpx", "bpy", "u_pseudo", "v_pseudo",
+              "d_p_c_12", "d_p_c_34", "Tw_u", "Tw_v"]
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("use_graph", [True, False], ids=["graph", "launches"])
+@pytest.mark.parametrize("name", NAMES)
+def test_dropin_run_matches_reference_dumps(name, use_graph, lib_built, golden_records):
+    """The drop-in run writes the same dumps and logs as the reference binary, byte for byte."""
+    import sts
+    rec = golden_records[name]
+    case, fixed = golden_case(name)
+    case.entered["Nt_save_temp_data"] = 1
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        sts.run_case(d, fixed_sweeps=fixed, use_graph=use_graph)
+        for f in ("u", "v", "p", "Temper", "vol_inf_fb"):
+            assert sha(sc.read_field(d, f, rec["Nx"], rec["Ny"])) == rec["sha256_" + f], f
+        lines = open(os.path.join(d, "Iterations_in_loops.txt")).read().split("\n")
+        assert [int(l.split()[-1]) for l in lines if l.strip() and not l.startswith("it")] == rec["sweeps"]
+        assert open(os.path.join(d, "Tmp.txt")).read() == rec["tmp_txt"]
+
+
+@pytest.mark.parametrize("name", ["channel_ma2.43_60x12_resid", "rayleigh_benard_32x16_resid",
+                                  "channel_circle_120x12_resid", "shipped_example_5steps"])
+def test_every_array_matches_oracle_step_by_step(name, lib_built, oracle_built):
+    import ora
+    import sts
+    case, fixed = golden_case(name)
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        o = ora.Oracle(d, fixed_sweeps=fixed)
+        g = sts.Solver(d, fixed_sweeps=fixed)
+        for f in ALL_FIELDS:  # after set-up
+            np.testing.assert_array_equal(g.field(f), o.field(f), err_msg=f"setup {f}")
+        for k in range(4):
+            assert g.step(1) == o.step(1) == 1
+            for f in ALL_FIELDS:
+                np.testing.assert_array_equal(g.field(f), o.field(f), err_msg=f"step {k + 1} {f}")
+            np.testing.assert_array_equal(g.stats(), o.stats())
+        g.close()
+
+
+def test_graph_and_launch_modes_agree(lib_built):
+    import sts
+    case = sc.channel_case("c", 100, 10, 0.3, 0.002, 1e-3, 40)
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        a = sts.Solver(d, fixed_sweeps=False, use_graph=True)
+        b = sts.Solver(d, fixed_sweeps=False, use_graph=False)
+        assert a.step(17) == b.step(17) == 17
+        for f in ("u", "v", "p", "T", "rho"):
+            np.testing.assert_array_equal(a.field(f), b.field(f))
+        np.testing.assert_array_equal(a.sweep_history(), b.sweep_history())
+
+
+def test_run_stops_at_Nt(lib_built):
+    import sts
+    case = sc.channel_case("c", 40, 6, 0.3, 0.002, 1e-3, 7)
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        s = sts.Solver(d, fixed_sweeps=False)
+        assert s.step(5) == 5
+        assert s.step(5) == 2  # Nt = 7 ends the run (SIMPLE_TS_MPI.cpp:4442)
+        assert s.step(5) == 0
+
+
+def test_full_size_channel_matches_oracle(lib_built, oracle_built):
+    """The 400x40 channel with the square, 60 steps at the 1e-8 residual tolerance."""
+    import ora
+    import sts
+    case = sc.config_case("channel_ma0.1", Nt=60)
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        o = ora.Oracle(d, fixed_sweeps=False)
+        g = sts.Solver(d, fixed_sweeps=False)
+        assert g.step(60) == o.step(60) == 60
+        for f in ("u", "v", "p", "T", "rho"):
+            np.testing.assert_array_equal(g.field(f), o.field(f), err_msg=f)
+        np.testing.assert_array_equal(g.sweep_history(), o.sweeps())
+
+
+def test_nonfinite_residual_is_reported(lib_built):
+    import sts
+    case = sc.channel_case("c", 40, 6, 0.3, 0.002, 1e-3, 10)
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        s = sts.Solver(d, fixed_sweeps=False)
+        s.step(1)
+        T = s.field("T")
+        T[3, 10] = np.nan
+        s.set_field("T", T)
+        with pytest.raises(sts.StsError) as e:
+            s.step(1)
+        assert e.value.code == sts.STS_ERR_NONFINITE

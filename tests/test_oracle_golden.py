@@ -1,0 +1,55 @@
+"""The CPU oracle against the golden dumps of the reference solver (tests/golden)."""
+import hashlib
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+import sts_cases as sc
+from conftest import GOLDEN, golden_case
+
+NAMES = ["channel_ma0.1_80x8_resid", "channel_ma0.1_80x8_fixed", "channel_ma2.43_60x12_resid",
+         "rayleigh_benard_32x16_resid", "channel_circle_120x12_resid", "channel_ma0.1_400x40_resid_5steps",
+         "shipped_example_5steps"]
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_matches_reference_dumps(name, oracle_built, golden_records):
+    import ora
+    rec = golden_records[name]
+    case, fixed = golden_case(name)
+    case.entered["Nt_save_temp_data"] = 1
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        ora.run_cli(d, fixed_sweeps=fixed)
+        for f in ("u", "v", "p", "Temper", "vol_inf_fb"):
+            a = sc.read_field(d, f, rec["Nx"], rec["Ny"])
+            assert sha(a) == rec["sha256_" + f], f
+        if rec["arrays"]:
+            g = np.load(os.path.join(GOLDEN, name + ".npz"))
+            for f in ("u", "v", "p", "Temper"):
+                np.testing.assert_array_equal(sc.read_field(d, f, rec["Nx"], rec["Ny"]), g[f])
+        assert open(os.path.join(d, "Tmp.txt")).read() == rec["tmp_txt"]
+        lines = open(os.path.join(d, "Iterations_in_loops.txt")).read().split("\n")
+        sweeps = [int(l.split()[-1]) for l in lines if l.strip() and not l.startswith("it")]
+        assert sweeps == rec["sweeps"]
+
+
+def test_oracle_library_matches_cli(oracle_built, golden_records):
+    """The in-process oracle (used on the GPU machine) steps exactly like its CLI."""
+    import ora
+    rec = golden_records["channel_ma2.43_60x12_resid"]
+    case, fixed = golden_case(rec["name"])
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        o = ora.Oracle(d, fixed_sweeps=fixed)
+        assert o.step(10 ** 6) == rec["steps"]
+        o.finish()
+        assert list(o.sweeps()) == rec["sweeps"]
+        assert sha(o.field("u")) == rec["sha256_u"]
+        assert sha(o.field("p")) == rec["sha256_p"]
