@@ -1,0 +1,304 @@
+"""Benchmark of the GB300 SIMPLE-TS time step (one JSON line on rank 0).
+
+Workload: the supersonic channel with a confined square (1200x120 fluid cells,
+Mach 2.43, Kn 0.00283, dt 2.5e-4), p-T Jacobi sweeps iterated to the 1e-8 update
+residual every step, FP64.  A "step" is one time step of the solver.  Inputs are
+synthetic case files generated by sts_cases.py (no dataset is involved).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+With N > 1 (torchrun, one rank per GPU) every rank advances its own copy of the
+case: the path shards by independent cases, there is no collective on the data
+path, scaling is weak.  The timed region of every rank is bracketed by a barrier
+and a device synchronisation; the slowest rank's time is reported.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [os.path.join(ROOT, "simple-ts_gb300"), os.path.join(ROOT, "oracle")]
+
+METRIC = "cell-steps/s at fixed residual: learned warm-start vs plain Jacobi; % HBM peak"
+UNIT = "cell-steps/s"
+WORKLOAD = "channel_ma2.43"
+L2_BYTES = 129 * 2 ** 20
+
+# algorithmic bytes per cell and launch of each kernel (stated in the design doc): arrays the
+# kernel must read once and write once for one cell, 8 bytes each, plus the 1-byte class
+BYTES_PER_CELL = {
+    "sweep": 32,          # read p, T of the iterate, write p, T
+    "assemble": 27 * 8 + 1,
+    "flux_diff": 15 * 8 + 1,
+    "correct": 10 * 8 + 1,
+    "face_rho": 5 * 8 + 1,
+    "step_begin": 10 * 8,
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--profile-target", type=int, default=0,
+                    help="only run this many steps kernel by kernel (a small target for ncu), then exit")
+    return ap.parse_args()
+
+
+def profile_target(args):
+    """A short, plain run of the workload (launch by launch) for an external profiler."""
+    import sts
+    import build as stsbuild
+    stsbuild.build()
+    _, d = make_case(args.workload)
+    s = sts.Solver(d, fixed_sweeps=False, use_graph=False)
+    s.step(args.profile_target)
+    s.sync()
+    print(f"profile target: {args.workload}, {args.profile_target} steps, sweeps {list(s.sweep_history())}")
+    s.close()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d["hbm_gbs"], "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def make_case(workload):
+    import sts_cases as sc
+    case = sc.config_case(workload, Nt=10 ** 7)
+    d = tempfile.mkdtemp(prefix="sts_bench_")
+    case.write(d)
+    return case, d
+
+
+def cpu_baseline(case_dir, seconds, start_steps=0):
+    """The oracle (serial C++ restatement of the reference) on this host: bounded sample."""
+    import ora
+    from build_oracle import build_oracle
+    build_oracle()
+    o = ora.Oracle(case_dir, fixed_sweeps=False)
+    if start_steps:
+        o.step(start_steps)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.step(1)
+        n += 1
+        dt = time.perf_counter() - t0
+        if (dt >= seconds and n >= 2) or n >= 10000:
+            break
+    cells = o.Nx * o.Ny
+    return {"value": cells * n / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{n} time steps (steps {start_steps + 1}-{start_steps + n}) of the same case, serial oracle"}
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    case, d = make_case(args.workload)
+    import ora
+    from build_oracle import build_oracle
+    build_oracle()
+    o = ora.Oracle(d, fixed_sweeps=False)
+    o.step(args.warmup)
+    t0 = time.perf_counter()
+    n = o.step(args.steps)
+    dt = time.perf_counter() - t0
+    cells = o.Nx * o.Ny
+    v = cells * n / dt
+    cfg = config(case, o.Nx, o.Ny)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": n, "warmup": args.warmup, "ms_per_step": dt / n * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": f"{n} time steps after {args.warmup} warm-up steps, serial oracle "
+                                       "(the reference solver is serial without MPI)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config(case, Nx, Ny):
+    e = case.entered
+    return {"workload": case.name + f" {Nx - 3}x{Ny - 3} fluid cells, square obstacle, slip/jump walls",
+            "Nx": Nx, "Ny": Ny, "cells_per_step": Nx * Ny, "mach": 2.43, "Kn": e["Kn"], "dt": e["ht"],
+            "residual_tolerance": e["MaxError_p_c"], "method": "plain Jacobi (p-T), FP64 bit-exact with the reference",
+            "l2": "flushed before every timed step (256 MiB write); working set 42 MB < L2"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    if args.profile_target:
+        return profile_target(args)
+    rank, world, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import sts
+    import build as stsbuild
+    stsbuild.build()
+    case, d = make_case(args.workload)
+    s = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local)
+    Na = s.Nx * s.Ny
+    flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # warm-up
+    for _ in range(max(args.warmup, 3)):
+        s.step(1)
+    s.sync()
+    h0 = len(s.sweep_history())
+    # timed region: K steps, each after an L2 flush, device time from events on the library stream
+    barrier()
+    total_ms, done = 0.0, 0
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            n, ms = s.step_timed(1)
+            total_ms += ms
+            done += n
+    barrier()
+    t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    total_ms = float(t.item())
+    sweeps = s.sweep_history()[-done:] if done else []
+    # kernels per step with one outer iteration: step_begin, assemble, S sweeps, correct,
+    # face_rho, boundary, flux_diff, step_end
+    launches = int(sum(7 + int(x) for x in sweeps))
+    value = Na * done * world / (total_ms / 1e3)
+
+    # e2e through the C ABI with host buffers: per step the state u, v, p, T goes host->device
+    # from pinned memory, one step runs, and the new state comes back device->host.
+    pins = {f: torch.empty(Na, dtype=torch.float64).pin_memory() for f in ("u", "v", "p", "T")}
+    for f, b in pins.items():
+        s.get_field_ptr(f, b.data_ptr())
+    barrier()
+    e2e_steps = max(1, min(args.steps, 20))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for f, b in pins.items():
+            s.set_field_ptr(f, b.data_ptr())
+        s.step(1)
+        for f, b in pins.items():
+            s.get_field_ptr(f, b.data_ptr())
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": Na * e2e_steps * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 4 * Na * 8,
+           "d2h_bytes_per_step": 4 * Na * 8}
+
+    # per-kernel device time over a few more real steps (the roofline's dominant kernel)
+    pn, kms, kcnt = s.profile(max(3, min(args.steps, 10)))
+    dom = max(kms, key=lambda k: kms[k])
+    peak, peak_kind = peaks()
+    avg_s = kms[dom] / 1e3 / max(kcnt[dom], 1)
+    bpc = BYTES_PER_CELL.get(dom, 0)
+    achieved = bpc * Na / avg_s / 1e9 if bpc else None
+    roof = {"bound": "hbm", "kernel": "k_" + dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None, "traffic": None,
+            "peak_source": peak_kind, "bytes_per_cell": bpc, "avg_launch_us": avg_s * 1e6,
+            "kernel_share": {k: round(v / sum(kms.values()), 4) for k, v in kms.items()}}
+
+    if rank == 0:
+        cpu = cpu_baseline(d, args.cpu_seconds, start_steps=0)
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": done,
+                "warmup": max(args.warmup, 3), "ms_per_step": total_ms / max(done, 1), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": config(case, s.Nx, s.Ny), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+                "clocks": clk.summary(), "gpu_launches": launches,
+                "sweeps_per_step": {"mean": float(sum(sweeps) / max(len(sweeps), 1)),
+                                    "max": int(max(sweeps)) if len(sweeps) else 0}}
+        print(json.dumps(line), flush=True)
+    s.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -59,6 +59,16 @@ int sts_open_case(const char* case_dir, const sts_options* opt, sts_ctx** out);
  * *steps_done (optional) receives the count taken. */
 int sts_step(sts_ctx* ctx, int nsteps, int* steps_done);
 
+/* sts_step with a CUDA event pair on the context's stream around the work;
+ * *device_ms receives the elapsed device time. */
+int sts_step_timed(sts_ctx* ctx, int nsteps, int* steps_done, double* device_ms);
+
+/* Runs up to nsteps steps kernel by kernel with an event pair around every launch and
+ * returns per-kernel device time and launch counts, indexed 0 step_begin, 1 assemble,
+ * 2 sweep, 3 correct, 4 face_rho, 5 boundary, 6 flux_diff, 7 step_end (8 entries each).
+ * The steps are real: the state advances exactly as with sts_step. */
+int sts_profile_steps(sts_ctx* ctx, int nsteps, double* kernel_ms, int* kernel_launches, int* steps_done);
+
 /* Copies a field to host memory.  Names: u v p T rho sqrt_T rho_u rho_v Fx Fy D_ux D_uy
  * D_vx D_vy DTx DTy Gamma_xf Gamma_yf ScT1 apx apy bpx bpy u_pseudo v_pseudo d_p_c_12
  * d_p_c_34 Tw_u Tw_v (Nx*Ny doubles); hx x_v (Nx); hy y_v (Ny). */

@@ -184,6 +184,7 @@ struct Oracle {
   bool write_files = true;
   bool fixed_sweeps = true;      // FIXED_NUMBER_OF_ITERATIONS_LOOP_3 (SIMPLE_TS_MPI.cpp:56)
   bool check_wallclock = false;  // honour max_time_for_solve (CLI only)
+  bool apply_saves = false;      // periodic WriteSolvedDataToFile inside step() (CLI only)
   bool finished = false;
   std::string err;
 
@@ -1848,7 +1849,7 @@ void Oracle::step() {
   bc_function_of_time();
   Nt_save_solved_data_counter++;
   if (Nt_save_solved_data_counter >= Nt_save_solved_data) {
-    write_solved();
+    if (apply_saves) write_solved();
     Nt_save_solved_data_counter = 0;
   }
   Nt_save_DragCoefficient_counter++;
@@ -2008,6 +2009,7 @@ int main(int argc, char** argv) {
   ora_handle* h = ora_open(dir, fixed, 1);
   if (!h) return 2;
   h->o.check_wallclock = true;
+  h->o.apply_saves = true;
   while (!h->o.finished) ora_step(h, 1 << 20);
   ora_finish(h);
   ora_close(h);

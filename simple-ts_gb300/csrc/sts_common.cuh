@@ -123,6 +123,7 @@ struct Geo {
   double *u, *v, *u_pr, *v_pr, *p[2], *T[2], *p_pr, *T_pr, *rho, *rho_pr, *sqrt_T, *rho_u, *rho_v;
   double *Fx, *Fy, *D_ux, *D_uy, *D_vx, *D_vy, *DTx, *DTy, *Gamma_xf, *Gamma_yf;
   double *u_pseudo, *v_pseudo, *d12, *d34, *apx, *apy, *bpx, *bpy, *ScT1, *Tw_u, *Tw_v;
+  double* inv[8];  // loop-invariant parts of the sweep, written by the first sweep of an outer iteration
   Ctl* ctl;
 };
 

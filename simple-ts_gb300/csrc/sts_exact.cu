@@ -33,6 +33,8 @@ __device__ __forceinline__ double Hi(double f1, double f2, double h1, double h2)
 __device__ __forceinline__ double as_d(unsigned long long b) { return __longlong_as_double((long long)b); }
 __device__ __forceinline__ unsigned long long as_b(double d) { return (unsigned long long)__double_as_longlong(d); }
 
+constexpr int kMaxColumn = 1024;  // rows staged in shared memory by the inflow-column reductions
+
 // Running maximum that ignores NaN exactly like "if (m < fabs(r)) m = fabs(r)".
 __device__ __forceinline__ double mx(double m, double x) { return (m < x) ? x : m; }
 
@@ -273,68 +275,118 @@ __global__ void k_assemble(Geo g, unsigned long long h_sweep, int in_graph) {
 // Reads buffer `cur`, writes buffer `cur^1` for every cell (unsolved cells copy through,
 // which keeps both buffers identical there exactly as the reference's memcpy + swap do).
 // ---------------------------------------------------------------------------
-__global__ void k_sweep(Geo g, unsigned long long h_sweep, int in_graph) {
+// The first sweep of an outer iteration evaluates the reference expressions in full and
+// stores their loop-invariant parts (identical operations, so identical bits); later sweeps
+// reuse them and keep the reference's order for every term that involves the iterate.
+// Invariants: a_k = aT_k, or aT_k * T_wall for a wall neighbour (the bc form multiplies the
+// wall temperature by aT_k and adds exact zeros), divu, the T denominator, the p_pr/T_pr
+// term and ht * (sum of the p coefficients).
+template <bool FIRST>
+__device__ __forceinline__ void sweep_cell(const Geo& g, const Cell& c, const double* __restrict__ P,
+                                           const double* __restrict__ TT, double* __restrict__ pn,
+                                           double* __restrict__ Tn, double& rp, double& rT) {
+  const uint8_t cl = g.cls[c.ij];
+  const int co = cls_o(cl);
+  if (!co) {
+    pn[c.ij] = P[c.ij];
+    Tn[c.ij] = TT[c.ij];
+    return;
+  }
+  const int i = c.i, j = c.j;
+  const Nb d = neighbours(i, j, g.Nx, g.Ny, g.bits & F_PERIODIC);
+  const double* __restrict__ Fx = g.Fx;
+  const double* __restrict__ Fy = g.Fy;
+  const double* __restrict__ hx = g.hx;
+  const double* __restrict__ hy = g.hy;
+  const double* __restrict__ apx = g.apx;
+  const double* __restrict__ apy = g.apy;
+  const double ht = g.ht;
+  const int ij = d.ij;
+  double Tnew, pnew;
+  if (FIRST) {
+    const double aT1 = dmax0(0, Fx[d.ij]) + g.DTx[d.ij];
+    const double aT2 = dmax0(0, -Fx[d.i1j]) + g.DTx[d.i1j];
+    const double aT3 = dmax0(0, Fy[d.ij]) + g.DTy[d.ij];
+    const double aT4 = dmax0(0, -Fy[d.ij1]) + g.DTy[d.ij1];
+    const double divu = (g.u[d.i1j] - g.u[d.ij]) * hy[j] + (g.v[d.ij1] - g.v[d.ij]) * hx[i];
+    const double denT =
+        ht * (aT1 + aT2 + aT3 + aT4 + Fx[d.i1j] - Fx[d.ij] + Fy[d.ij1] - Fy[d.ij]) + hx[i] * hy[j] * g.rho[d.ij];
+    double w1 = aT1, w2 = aT2, w3 = aT3, w4 = aT4;
+    if (co == CLS_BC) {
+      auto B = [&](int k) -> double { return cls_fluid(g.cls[k]) ? 1.0 : 0.0; };
+      auto NB = [&](int k) -> double { return cls_fluid(g.cls[k]) ? 0.0 : 1.0; };
+      Tnew = (ht * (aT1 * (B(d.i_1j) * TT[d.i_1j] + NB(d.i_1j) * g.Tw_u[d.ij]) +
+                    aT2 * (B(d.i1j) * TT[d.i1j] + NB(d.i1j) * g.Tw_u[d.i1j]) +
+                    aT3 * (B(d.ij_1) * TT[d.ij_1] + NB(d.ij_1) * g.Tw_v[d.ij]) +
+                    aT4 * (B(d.ij1) * TT[d.ij1] + NB(d.ij1) * g.Tw_v[d.ij1]) + (1.0 - g.gamma1) * P[d.ij] * divu) +
+              g.ScT1[d.ij]) /
+             denT;
+      if (!cls_fluid(g.cls[d.i_1j])) w1 = aT1 * g.Tw_u[d.ij];
+      if (!cls_fluid(g.cls[d.i1j])) w2 = aT2 * g.Tw_u[d.i1j];
+      if (!cls_fluid(g.cls[d.ij_1])) w3 = aT3 * g.Tw_v[d.ij];
+      if (!cls_fluid(g.cls[d.ij1])) w4 = aT4 * g.Tw_v[d.ij1];
+    } else {
+      Tnew = (ht * (aT1 * TT[d.i_1j] + aT2 * TT[d.i1j] + aT3 * TT[d.ij_1] + aT4 * TT[d.ij1] +
+                    (1.0 - g.gamma1) * P[d.ij] * divu) +
+              g.ScT1[d.ij]) /
+             denT;
+    }
+    const double pc = g.p_pr[d.ij] * hx[i] * hy[j] / (g.T_pr[d.ij]);
+    const double sa = ht * (apx[d.ij] + apx[d.i1j] + apy[d.ij] + apy[d.ij1]);
+    g.inv[0][ij] = w1;
+    g.inv[1][ij] = w2;
+    g.inv[2][ij] = w3;
+    g.inv[3][ij] = w4;
+    g.inv[4][ij] = divu;
+    g.inv[5][ij] = denT;
+    g.inv[6][ij] = pc;
+    g.inv[7][ij] = sa;
+    double num = apx[d.ij] * P[d.i_1j] + apx[d.i1j] * P[d.i1j] + apy[d.ij] * P[d.ij_1] + apy[d.ij1] * P[d.ij1] +
+                 g.bpx[d.ij] - g.bpx[d.i1j] + g.bpy[d.ij] - g.bpy[d.ij1];
+    if (co == CLS_BC) {
+      const double gxb = ((g.bits & F_GIVEN_U_XB) && i == g.Nx_o0) ? 1.0 : 0.0;
+      const double gxe = ((g.bits & F_GIVEN_U_XE) && i == g.Nx_o1 - 1) ? 1.0 : 0.0;
+      num = num + gxb * Fx[d.ij] - gxe * Fx[d.i1j];
+    }
+    pnew = (ht * num + pc) / (sa + hx[i] * hy[j] / (Tnew));
+  } else {
+    const double w1 = g.inv[0][ij], w2 = g.inv[1][ij], w3 = g.inv[2][ij], w4 = g.inv[3][ij];
+    double t1, t2, t3, t4;
+    if (co == CLS_BC) {
+      t1 = cls_fluid(g.cls[d.i_1j]) ? w1 * TT[d.i_1j] : w1;
+      t2 = cls_fluid(g.cls[d.i1j]) ? w2 * TT[d.i1j] : w2;
+      t3 = cls_fluid(g.cls[d.ij_1]) ? w3 * TT[d.ij_1] : w3;
+      t4 = cls_fluid(g.cls[d.ij1]) ? w4 * TT[d.ij1] : w4;
+    } else {
+      t1 = w1 * TT[d.i_1j];
+      t2 = w2 * TT[d.i1j];
+      t3 = w3 * TT[d.ij_1];
+      t4 = w4 * TT[d.ij1];
+    }
+    Tnew = (ht * (t1 + t2 + t3 + t4 + (1.0 - g.gamma1) * P[d.ij] * g.inv[4][ij]) + g.ScT1[d.ij]) / g.inv[5][ij];
+    double num = apx[d.ij] * P[d.i_1j] + apx[d.i1j] * P[d.i1j] + apy[d.ij] * P[d.ij_1] + apy[d.ij1] * P[d.ij1] +
+                 g.bpx[d.ij] - g.bpx[d.i1j] + g.bpy[d.ij] - g.bpy[d.ij1];
+    if (co == CLS_BC) {
+      const double gxb = ((g.bits & F_GIVEN_U_XB) && i == g.Nx_o0) ? 1.0 : 0.0;
+      const double gxe = ((g.bits & F_GIVEN_U_XE) && i == g.Nx_o1 - 1) ? 1.0 : 0.0;
+      num = num + gxb * Fx[d.ij] - gxe * Fx[d.i1j];
+    }
+    pnew = (ht * num + g.inv[6][ij]) / (g.inv[7][ij] + hx[i] * hy[j] / (Tnew));
+  }
+  Tn[ij] = Tnew;
+  pn[ij] = pnew;
+  rT = fabs(Tnew - TT[ij]);
+  rp = fabs(pnew - P[ij]);
+}
+
+template <bool FIRST>
+__device__ __forceinline__ void sweep_body(const Geo& g, unsigned long long h_sweep, int in_graph) {
   Ctl* ctl = g.ctl;
   if (ctl->pt_done) return;  // the loop already stopped: launch is a no-op
   Cell c = cell(g);
   const unsigned cur = ctl->cur;
-  const double* __restrict__ P = g.p[cur];
-  const double* __restrict__ TT = g.T[cur];
-  double* __restrict__ pn = g.p[cur ^ 1];
-  double* __restrict__ Tn = g.T[cur ^ 1];
   double rp = 0, rT = 0;
-  if (c.ok) {
-    const uint8_t cl = g.cls[c.ij];
-    const int co = cls_o(cl);
-    if (!co) {
-      pn[c.ij] = P[c.ij];
-      Tn[c.ij] = TT[c.ij];
-    } else {
-      const int i = c.i, j = c.j;
-      const Nb d = neighbours(i, j, g.Nx, g.Ny, g.bits & F_PERIODIC);
-      const double* __restrict__ Fx = g.Fx;
-      const double* __restrict__ Fy = g.Fy;
-      const double* __restrict__ hx = g.hx;
-      const double* __restrict__ hy = g.hy;
-      const double ht = g.ht;
-      const double aT1 = dmax0(0, Fx[d.ij]) + g.DTx[d.ij];
-      const double aT2 = dmax0(0, -Fx[d.i1j]) + g.DTx[d.i1j];
-      const double aT3 = dmax0(0, Fy[d.ij]) + g.DTy[d.ij];
-      const double aT4 = dmax0(0, -Fy[d.ij1]) + g.DTy[d.ij1];
-      const double divu = (g.u[d.i1j] - g.u[d.ij]) * hy[j] + (g.v[d.ij1] - g.v[d.ij]) * hx[i];
-      double Tnew;
-      if (co == CLS_BC) {
-        auto B = [&](int k) -> double { return cls_fluid(g.cls[k]) ? 1.0 : 0.0; };
-        auto NB = [&](int k) -> double { return cls_fluid(g.cls[k]) ? 0.0 : 1.0; };
-        Tnew = (ht * (aT1 * (B(d.i_1j) * TT[d.i_1j] + NB(d.i_1j) * g.Tw_u[d.ij]) +
-                      aT2 * (B(d.i1j) * TT[d.i1j] + NB(d.i1j) * g.Tw_u[d.i1j]) +
-                      aT3 * (B(d.ij_1) * TT[d.ij_1] + NB(d.ij_1) * g.Tw_v[d.ij]) +
-                      aT4 * (B(d.ij1) * TT[d.ij1] + NB(d.ij1) * g.Tw_v[d.ij1]) + (1.0 - g.gamma1) * P[d.ij] * divu) +
-                g.ScT1[d.ij]) /
-               (ht * (aT1 + aT2 + aT3 + aT4 + Fx[d.i1j] - Fx[d.ij] + Fy[d.ij1] - Fy[d.ij]) + hx[i] * hy[j] * g.rho[d.ij]);
-      } else {
-        Tnew = (ht * (aT1 * TT[d.i_1j] + aT2 * TT[d.i1j] + aT3 * TT[d.ij_1] + aT4 * TT[d.ij1] +
-                      (1.0 - g.gamma1) * P[d.ij] * divu) +
-                g.ScT1[d.ij]) /
-               (ht * (aT1 + aT2 + aT3 + aT4 + Fx[d.i1j] - Fx[d.ij] + Fy[d.ij1] - Fy[d.ij]) + hx[i] * hy[j] * g.rho[d.ij]);
-      }
-      const double* __restrict__ apx = g.apx;
-      const double* __restrict__ apy = g.apy;
-      double num = apx[d.ij] * P[d.i_1j] + apx[d.i1j] * P[d.i1j] + apy[d.ij] * P[d.ij_1] + apy[d.ij1] * P[d.ij1] +
-                   g.bpx[d.ij] - g.bpx[d.i1j] + g.bpy[d.ij] - g.bpy[d.ij1];
-      if (co == CLS_BC) {
-        const double gxb = ((g.bits & F_GIVEN_U_XB) && i == g.Nx_o0) ? 1.0 : 0.0;
-        const double gxe = ((g.bits & F_GIVEN_U_XE) && i == g.Nx_o1 - 1) ? 1.0 : 0.0;
-        num = num + gxb * Fx[d.ij] - gxe * Fx[d.i1j];
-      }
-      const double pnew = (ht * num + g.p_pr[d.ij] * hx[i] * hy[j] / (g.T_pr[d.ij])) /
-                          (ht * (apx[d.ij] + apx[d.i1j] + apy[d.ij] + apy[d.ij1]) + hx[i] * hy[j] / (Tnew));
-      Tn[c.ij] = Tnew;
-      pn[c.ij] = pnew;
-      rT = fabs(Tnew - TT[c.ij]);
-      rp = fabs(pnew - P[c.ij]);
-    }
-  }
+  if (c.ok) sweep_cell<FIRST>(g, c, g.p[cur], g.T[cur], g.p[cur ^ 1], g.T[cur ^ 1], rp, rT);
   block_max2(rp, rT, &ctl->res_bits_p, &ctl->res_bits_T, &ctl->status);
   if (last_block(&ctl->block_count)) {
     // the reference's loop control, evaluated once per sweep (SIMPLE_TS_MPI.cpp:4087-4107)
@@ -362,6 +414,9 @@ __global__ void k_sweep(Geo g, unsigned long long h_sweep, int in_graph) {
     if (in_graph) cudaGraphSetConditional((cudaGraphConditionalHandle)h_sweep, cont ? 1 : 0);
   }
 }
+
+__global__ void k_sweep_first(Geo g, unsigned long long h_sweep, int in_graph) { sweep_body<true>(g, h_sweep, in_graph); }
+__global__ void k_sweep(Geo g, unsigned long long h_sweep, int in_graph) { sweep_body<false>(g, h_sweep, in_graph); }
 
 // ---------------------------------------------------------------------------
 // velocity correction with L-inf residuals (SIMPLE_TS_MPI.cpp:4171-4305) and
@@ -720,22 +775,38 @@ __global__ void __launch_bounds__(1024) k_boundary(Geo g, unsigned phases, unsig
   // BoundaryConditions_Pressure_begin_iteration_for_it (SIMPLE_TS_MPI.cpp:7430-7647)
   if ((phases & PH_PBEGIN) && !per) {
     __shared__ int ratio_side;  // 0: nothing, 1: inlet columns, 2: outlet columns
+    // the inflow column is staged in shared memory by all threads; thread 0 then folds it
+    // in the reference's order (the mean is an ordered sum)
+    // (the column maximum and mean only feed correction methods 1 and 2)
+    __shared__ double col_u[kMaxColumn], col_h[kMaxColumn];
+    const bool need_col = (g.p_corr_method == 1 || g.p_corr_method == 2);
+    const bool staged = need_col && Ny <= kMaxColumn;
+    if (staged) {
+      for (int j = tid; j < Ny; j += nt) {
+        const int n = g.Nx_u0 + j * Nx;
+        col_u[j] = u[n];
+        col_h[j] = fl(n) ? g.hy[j] : -1.0;  // negative height marks a body cell
+      }
+    }
+    __syncthreads();
     if (tid == 0) {
       ratio_side = 0;
-      const int i = g.Nx_u0;
-      double umax = u[0];
-      for (int j = 0; j < Ny; j++) {
-        const int n = i + j * Nx;
-        if (fl(n)) umax = (umax > u[n]) ? umax : u[n];
+      if (need_col) {
+        const int i = g.Nx_u0;
+        double umax = u[0], mean = 0, hin = 0;
+        for (int j = 0; j < Ny; j++) {
+          const bool f = staged ? col_h[j] >= 0 : fl(i + j * Nx);
+          if (!f) continue;
+          const double uj = staged ? col_u[j] : u[i + j * Nx];
+          const double hj = staged ? col_h[j] : g.hy[j];
+          umax = (umax > uj) ? umax : uj;
+          mean += uj * hj;
+          hin += hj;
+        }
+        ctl->u_in_max = umax;
+        ctl->u_in_mean = mean / hin;
       }
-      double mean = 0, hin = 0;
-      for (int j = 0; j < Ny; j++) {
-        const int n = i + j * Nx;
-        if (fl(n)) { mean += u[n] * g.hy[j]; hin += g.hy[j]; }
-      }
-      mean = mean / hin;
-      ctl->u_in_max = umax;
-      ctl->u_in_mean = mean;
+      const double umax = ctl->u_in_max, mean = ctl->u_in_mean;
       if (bits & F_GIVEN_REKN) ctl->u_given_xb = g.Re * g.Kn * sqrt(15.0 * 3.14159265358979323846 / 128.0);
       const double ug = ctl->u_given_xb;
       if (g.p_corr_method == 0) {

@@ -24,6 +24,7 @@ enum : unsigned {
 __global__ void k_step_begin(Geo g, int counters, unsigned long long h_outer, int in_graph);
 __global__ void k_apply_bodies(Geo g);
 __global__ void k_assemble(Geo g, unsigned long long h_sweep, int in_graph);
+__global__ void k_sweep_first(Geo g, unsigned long long h_sweep, int in_graph);
 __global__ void k_sweep(Geo g, unsigned long long h_sweep, int in_graph);
 __global__ void k_correct(Geo g);
 __global__ void k_face_rho(Geo g);

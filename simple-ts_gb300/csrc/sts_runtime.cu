@@ -95,7 +95,8 @@ struct sts_ctx {
   int step_host(int n, int* done);
   int step_graph(int n, int* done);
   int write_outputs();
-  int write_logs();
+  int write_logs(bool iterations = true);
+  int profile(int n, double* ms, int* cnt, int* done);
 };
 
 namespace {
@@ -157,8 +158,10 @@ int sts_ctx::build_graph() {
   CU(cudaGraphConditionalHandleCreate(&hw, b_outer, 1, cudaGraphCondAssignDefault));
   cudaGraphNode_t n_asm, n_sw, n_cor, n_rho, n_bnd, n_fd;
   if (int r = add_kernel(&n_asm, b_outer, {}, k_assemble, grid, block, g, (unsigned long long)hw, 1)) return r;
+  cudaGraphNode_t n_first;
+  if (int r = add_kernel(&n_first, b_outer, {n_asm}, k_sweep_first, grid, block, g, (unsigned long long)hw, 1)) return r;
   cudaGraph_t b_sweep;
-  if (int r = add_while(&n_sw, b_outer, {n_asm}, hw, &b_sweep)) return r;
+  if (int r = add_while(&n_sw, b_outer, {n_first}, hw, &b_sweep)) return r;
   cudaGraphNode_t n_one;
   if (int r = add_kernel(&n_one, b_sweep, {}, k_sweep, grid, block, g, (unsigned long long)hw, 1)) return r;
   if (int r = add_kernel(&n_cor, b_outer, {n_sw}, k_correct, grid, block, g)) return r;
@@ -196,10 +199,11 @@ int sts_ctx::step_host(int n, int* done) {
     k_step_begin<<<grid, block, 0, s>>>(g, 1, 0, 0);
     for (int outer = 0; outer < NI; outer++) {
       k_assemble<<<grid, block, 0, s>>>(g, 0, 0);
+      k_sweep_first<<<grid, block, 0, s>>>(g, 0, 0);
       if (fixed) {
-        for (int q = 0; q < Npc; q++) k_sweep<<<grid, block, 0, s>>>(g, 0, 0);
+        for (int q = 1; q < Npc; q++) k_sweep<<<grid, block, 0, s>>>(g, 0, 0);
       } else {
-        int launched = 0;
+        int launched = 1;
         for (;;) {
           const int batch = 4;
           for (int q = 0; q < batch && launched < Npc; q++, launched++) k_sweep<<<grid, block, 0, s>>>(g, 0, 0);
@@ -224,6 +228,64 @@ int sts_ctx::step_host(int n, int* done) {
       break;
     }
   }
+  *done = k;
+  return STS_OK;
+}
+
+// The launch loop with a CUDA event pair around every kernel: per-kernel device time.
+// kinds: 0 step_begin, 1 assemble, 2 sweep, 3 correct, 4 face_rho, 5 boundary, 6 flux_diff, 7 step_end
+int sts_ctx::profile(int n, double* ms, int* cnt, int* done) {
+  const bool fixed = hc.bits & F_FIXED_SWEEPS;
+  const int NI = (int)hc.cfg.n("N_I"), Npc = (int)hc.cfg.n("N_I_p_c");
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> kind;
+  auto mark = [&](int k) {
+    cudaEvent_t a;
+    cudaEventCreate(&a);
+    cudaEventRecord(a, s);
+    ev.push_back(a);
+    kind.push_back(k);
+  };
+  for (int q = 0; q < 8; q++) { ms[q] = 0; cnt[q] = 0; }
+  int k = 0;
+  for (; k < n; k++) {
+    mark(-1); k_step_begin<<<grid, block, 0, s>>>(g, 1, 0, 0); mark(0);
+    for (int outer = 0; outer < NI; outer++) {
+      mark(-1); k_assemble<<<grid, block, 0, s>>>(g, 0, 0); mark(1);
+      // the sweep count of this outer iteration is only known afterwards: launch one at a time
+      for (int q = 0; q < Npc; q++) {
+        mark(-1);
+        if (q == 0) k_sweep_first<<<grid, block, 0, s>>>(g, 0, 0);
+        else k_sweep<<<grid, block, 0, s>>>(g, 0, 0);
+        mark(2);
+        if (!fixed) {
+          if (int r = read_ctl()) return r;
+          if (h_ctl->pt_done) break;
+        }
+      }
+      mark(-1); k_correct<<<grid, block, 0, s>>>(g); mark(3);
+      mark(-1); k_face_rho<<<grid, block, 0, s>>>(g); mark(4);
+      mark(-1); k_boundary<<<1, 1024, 0, s>>>(g, PH_ALL_STEP, 0, 0); mark(5);
+      mark(-1); k_flux_diff<<<grid, block, 0, s>>>(g); mark(6);
+      if (NI > 1) {
+        if (int r = read_ctl()) return r;
+        if (!h_ctl->continue_iter) break;
+      }
+    }
+    mark(-1); k_step_end<<<1, 1024, 0, s>>>(g, 0, 0); mark(7);
+    if (int r = check()) return r;
+    if (int r = read_ctl()) return r;
+    if (!h_ctl->continue_step) { k++; break; }
+  }
+  CU(cudaStreamSynchronize(s));
+  for (size_t q = 1; q < ev.size(); q++) {
+    if (kind[q] < 0) continue;
+    float t = 0;
+    cudaEventElapsedTime(&t, ev[q - 1], ev[q]);
+    ms[kind[q]] += t;
+    cnt[kind[q]] += 1;
+  }
+  for (cudaEvent_t e : ev) cudaEventDestroy(e);
   *done = k;
   return STS_OK;
 }
@@ -290,7 +352,7 @@ int sts_ctx::write_outputs() {
 }
 
 // WriteTempDataToFile and WriteIterationsInLoopsToFile (SIMPLE_TS_MPI.cpp:5838-6006).
-int sts_ctx::write_logs() {
+int sts_ctx::write_logs(bool iterations) {
   if (!opt.write_files) return STS_OK;
   if (int r = read_ctl()) return r;
   const Ctl& c = *h_ctl;
@@ -312,7 +374,7 @@ int sts_ctx::write_logs() {
       << "\t" << c.res_v0 << "\t" << c.res_v << std::endl;
     tmp_fresh = false;
   }
-  {
+  if (iterations) {
     std::ofstream o;
     if (iter_fresh) {
       if (hc.restart) o.open((hc.dir + "/Iterations_in_loops.txt").c_str(), std::ios::out | std::ios::app);
@@ -435,6 +497,8 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
                        &g.apy, &g.bpx, &g.bpy, &g.ScT1, &g.Tw_u, &g.Tw_v};
   for (double** f : fields)
     if (int r = c->alloc(f, Na)) return r;
+  for (int k = 0; k < 8; k++)
+    if (int r = c->alloc(&g.inv[k], Na)) return r;
   if (int r = c->alloc(&c->d_ctl, 1)) return r;
   g.ctl = c->d_ctl;
   if (int r = c->upload(g.u, h.u)) return r;
@@ -530,6 +594,40 @@ int sts_step(sts_ctx* ctx, int nsteps, int* steps_done) {
       return fail(STS_ERR_NONFINITE, "a residual became NaN or Inf");
     }
   }
+  if (steps_done) *steps_done = done;
+  return STS_OK;
+}
+
+int sts_step_timed(sts_ctx* ctx, int nsteps, int* steps_done, double* device_ms) {
+  if (!ctx || nsteps < 0) return fail(STS_ERR_ARG, "bad argument");
+  CU(cudaSetDevice(ctx->opt.device));
+  cudaEvent_t a, b;
+  CU(cudaEventCreate(&a));
+  CU(cudaEventCreate(&b));
+  CU(cudaEventRecord(a, ctx->s));
+  int done = 0;
+  int r = sts_step(ctx, nsteps, &done);
+  cudaEventRecord(b, ctx->s);
+  cudaEventSynchronize(b);
+  float t = 0;
+  cudaEventElapsedTime(&t, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (device_ms) *device_ms = t;
+  if (steps_done) *steps_done = done;
+  return r;
+}
+
+int sts_profile_steps(sts_ctx* ctx, int nsteps, double* kernel_ms, int* kernel_launches, int* steps_done) {
+  if (!ctx || nsteps < 0 || !kernel_ms || !kernel_launches) return fail(STS_ERR_ARG, "bad argument");
+  CU(cudaSetDevice(ctx->opt.device));
+  int done = 0;
+  if (ctx->finished) {
+    for (int q = 0; q < 8; q++) { kernel_ms[q] = 0; kernel_launches[q] = 0; }
+  } else if (int r = ctx->profile(nsteps, kernel_ms, kernel_launches, &done)) {
+    return r;
+  }
+  if (!ctx->h_ctl->continue_step) ctx->finished = true;
   if (steps_done) *steps_done = done;
   return STS_OK;
 }
@@ -650,7 +748,7 @@ int sts_run_case(const char* case_dir, const sts_options* opt) {
   const double hours = std::chrono::duration<double>(std::chrono::steady_clock::now() - ctx->t0).count() / 3600.0;
   ctx->hc.cfg.set("max_time_for_solve", hours);
   if (int q = ctx->write_outputs()) return q;
-  if (int q = ctx->write_logs()) return q;
+  if (int q = ctx->write_logs(false)) return q;  // the final log writes Tmp.txt only (SIMPLE_TS_MPI.cpp:4714)
   return STS_OK;
 }
 

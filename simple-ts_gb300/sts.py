@@ -26,8 +26,10 @@ STS_ERR_NONFINITE = -4
 EXPORTS = [
     "sts_default_options", "sts_open_case", "sts_step", "sts_get_field", "sts_set_field", "sts_dims",
     "sts_stats", "sts_sweep_history", "sts_write_outputs", "sts_run_case", "sts_sync", "sts_destroy",
-    "sts_last_error", "sts_inspect_case",
+    "sts_last_error", "sts_inspect_case", "sts_step_timed", "sts_profile_steps",
 ]
+
+KERNELS = ["step_begin", "assemble", "sweep", "correct", "face_rho", "boundary", "flux_diff", "step_end"]
 
 FIELDS = ["u", "v", "p", "T", "rho", "sqrt_T", "rho_u", "rho_v", "Fx", "Fy", "D_ux", "D_uy", "D_vx", "D_vy",
           "DTx", "DTy", "Gamma_xf", "Gamma_yf", "ScT1", "apx", "apy", "bpx", "bpy", "u_pseudo", "v_pseudo",
@@ -60,6 +62,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.sts_default_options.restype = None
     lib.sts_open_case.argtypes = [C.c_char_p, C.POINTER(Options), C.POINTER(P)]
     lib.sts_step.argtypes = [P, C.c_int, C.POINTER(C.c_int)]
+    lib.sts_step_timed.argtypes = [P, C.c_int, C.POINTER(C.c_int), dp]
+    lib.sts_profile_steps.argtypes = [P, C.c_int, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.sts_get_field.argtypes = [P, C.c_char_p, dp]
     lib.sts_set_field.argtypes = [P, C.c_char_p, dp]
     lib.sts_dims.argtypes = [P, C.POINTER(C.c_int), C.POINTER(C.c_int)]
@@ -116,6 +120,28 @@ class Solver:
             return done.value
         _check(r)
         return done.value
+
+    def step_timed(self, n: int):
+        """(steps taken, device milliseconds) measured with CUDA events on the library's stream."""
+        done, ms = C.c_int(), C.c_double()
+        _check(load().sts_step_timed(self._h, int(n), C.byref(done), C.byref(ms)))
+        return done.value, ms.value
+
+    def profile(self, n: int):
+        """Per-kernel device time (ms) and launch counts over n real steps."""
+        ms = np.zeros(8)
+        cnt = np.zeros(8, dtype=np.int32)
+        done = C.c_int()
+        _check(load().sts_profile_steps(self._h, int(n), _dptr(ms), cnt.ctypes.data_as(C.POINTER(C.c_int)),
+                                        C.byref(done)))
+        return done.value, dict(zip(KERNELS, ms)), dict(zip(KERNELS, cnt.tolist()))
+
+    def set_field_ptr(self, name: str, host_ptr: int):
+        """Upload from a raw host pointer (e.g. a pinned buffer) of Nx*Ny doubles."""
+        _check(load().sts_set_field(self._h, name.encode(), C.cast(C.c_void_p(host_ptr), C.POINTER(C.c_double))))
+
+    def get_field_ptr(self, name: str, host_ptr: int):
+        _check(load().sts_get_field(self._h, name.encode(), C.cast(C.c_void_p(host_ptr), C.POINTER(C.c_double))))
 
     def field(self, name: str) -> np.ndarray:
         n = self.Nx if name in ("hx", "x_v") else self.Ny if name in ("hy", "y_v") else self.Nx * self.Ny
