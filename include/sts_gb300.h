@@ -71,7 +71,7 @@ int sts_profile_steps(sts_ctx* ctx, int nsteps, double* kernel_ms, int* kernel_l
 
 /* Copies a field to host memory.  Names: u v p T rho sqrt_T rho_u rho_v Fx Fy D_ux D_uy
  * D_vx D_vy DTx DTy Gamma_xf Gamma_yf ScT1 apx apy bpx bpy u_pseudo v_pseudo d_p_c_12
- * d_p_c_34 Tw_u Tw_v (Nx*Ny doubles); hx x_v (Nx); hy y_v (Ny). */
+ * d_p_c_34 Tw_u Tw_v p_pr T_pr u_pr v_pr rho_pr (Nx*Ny doubles); hx x_v (Nx); hy y_v (Ny). */
 int sts_get_field(sts_ctx* ctx, const char* name, double* host_out);
 
 /* Overwrites u, v, p or T from host memory (Nx*Ny doubles); rho and sqrt_T follow on the next step. */
@@ -105,6 +105,30 @@ void sts_destroy(sts_ctx* ctx);
 
 /* Message of the last failure on this thread ("" if none). */
 const char* sts_last_error(void);
+
+/* Inputs of the coupled p-T Jacobi sweeps as device arrays owned by the caller (fields are
+ * Nx*Ny doubles in the reference layout, hx: Nx, hy: Ny; cls uses the class-byte layout of
+ * sts_inspect_case).  p and T hold the initial iterate and receive the final one. */
+typedef struct sts_sweep_fields {
+  int Nx, Ny;
+  int periodic;               /* Periodic_boundary_conditions_about_OX */
+  int given_u_xb, given_u_xe; /* Given_velocity_on_xb / _xe */
+  int Nx_o0, Nx_o1;           /* p/T solve range in x (define_area_for_solving) */
+  double ht, gamma1;
+  const unsigned char* cls;
+  const double *hx, *hy;
+  const double *Fx, *Fy, *DTx, *DTy, *u, *v, *rho, *ScT1, *apx, *apy, *bpx, *bpy, *p_pr, *T_pr, *Tw_u, *Tw_v;
+  double *p, *T;
+} sts_sweep_fields;
+
+/* The p-T sweep loop of one outer iteration (SIMPLE_TS_MPI.cpp:3786-4131) on caller-owned
+ * device arrays, bit-exact with the reference: fixed_sweeps = 1 runs exactly max_sweeps
+ * sweeps; 0 stops after at least 2 sweeps once max|dp| <= tol_p and max|dT| <= tol_T (or at
+ * max_sweeps).  Work is queued on `stream` (a cudaStream_t, NULL for the legacy stream) and the
+ * call returns when it is done.  Scratch (a second iterate, the sweep invariants and the
+ * reduction words: 10*Nx*Ny doubles + 20 KB) is allocated stream-ordered and freed by the call. */
+int sts_pt_sweeps(const sts_sweep_fields* f, int max_sweeps, int fixed_sweeps, double tol_p, double tol_T,
+                  void* stream, int* sweeps_done, double* res_p, double* res_T);
 
 /* Host-only inspection of a case directory (no device use): dims, obstacle ids
  * (vol_inf_fb, Nx*Ny), per-cell classes (Nx*Ny bytes: bits 0-1 u, 2-3 v, 4-5 p/T with

@@ -96,6 +96,31 @@ class Oracle:
             pass
 
 
+def pt_sweeps(Nx, Ny, periodic, given_xb, given_xe, Nx_o0, Nx_o1, ht, gamma1, cls, hx, hy, fields, p, T,
+              max_sweeps, fixed, tol_p, tol_T):
+    """The sweep loop of the oracle on host arrays; fields: dict of the sweep inputs (Nx*Ny each).
+    Returns (p, T, sweeps, res_p, res_T)."""
+    lib = load()
+    dp = C.POINTER(C.c_double)
+    names = ["Fx", "Fy", "DTx", "DTy", "u", "v", "rho", "ScT1", "apx", "apy", "bpx", "bpy", "p_pr", "T_pr",
+             "Tw_u", "Tw_v"]
+    lib.ora_pt_sweeps.argtypes = ([C.c_int] * 7 + [C.c_double] * 2 + [C.POINTER(C.c_ubyte)] + [dp] * 2 +
+                                  [dp] * len(names) + [dp, dp, C.c_int, C.c_int, C.c_double, C.c_double,
+                                                       C.POINTER(C.c_int), dp, dp])
+    arrs = [np.ascontiguousarray(fields[n], dtype=np.float64).reshape(-1) for n in names]
+    p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1).copy()
+    T = np.ascontiguousarray(T, dtype=np.float64).reshape(-1).copy()
+    cls = np.ascontiguousarray(cls, dtype=np.uint8).reshape(-1)
+    hx = np.ascontiguousarray(hx, dtype=np.float64)
+    hy = np.ascontiguousarray(hy, dtype=np.float64)
+    n, rp, rT = C.c_int(), C.c_double(), C.c_double()
+    lib.ora_pt_sweeps(Nx, Ny, int(periodic), int(given_xb), int(given_xe), Nx_o0, Nx_o1, ht, gamma1,
+                      cls.ctypes.data_as(C.POINTER(C.c_ubyte)), hx.ctypes.data_as(dp), hy.ctypes.data_as(dp),
+                      *[a.ctypes.data_as(dp) for a in arrs], p.ctypes.data_as(dp), T.ctypes.data_as(dp),
+                      int(max_sweeps), int(fixed), float(tol_p), float(tol_T), C.byref(n), C.byref(rp), C.byref(rT))
+    return p.reshape(Ny, Nx), T.reshape(Ny, Nx), n.value, rp.value, rT.value
+
+
 def run_cli(case_dir, fixed_sweeps=True):
     args = [EXE, case_dir] + ([] if fixed_sweeps else ["--residual"])
     return subprocess.run(args, capture_output=True, text=True, check=True)

@@ -340,6 +340,7 @@ struct Oracle {
   void bc_tjump();
   void bc_tjump_write();
   void bc_function_of_time();
+  void pt_sweeps();
   void nondim_refresh();
   // ======================= driver =======================
   bool setup();
@@ -1550,6 +1551,79 @@ bool Oracle::setup() {
   return true;
 }
 
+// coupled p-T Jacobi sweeps with the EOS substitution, SIMPLE_TS_MPI.cpp:3786-4131
+void Oracle::pt_sweeps() {
+  const std::vector<char>& b = vol;
+  // ---- coupled p-T Jacobi sweeps (:3786-4131) ----
+  continue_iter_p_c = false;
+  Iter_p_c = 0;
+  do {
+    std::swap(p, p_old);
+    std::swap(Temper, Temper_old);
+    const double* P = p_old;
+    const double* TT = Temper_old;
+    max_res_p[Iter] = 0;
+    max_res_T[Iter] = 0;
+    for (size_t c = 0; c < bc_o.size(); c++) {
+      Idx d = bc_idx(bc_o[c]);
+      uint i = d.i, j = d.j;
+      double aT1 = dmax(0, Fx[d.ij]) + DTx[d.ij];
+      double aT2 = dmax(0, -Fx[d.i1j]) + DTx[d.i1j];
+      double aT3 = dmax(0, Fy[d.ij]) + DTy[d.ij];
+      double aT4 = dmax(0, -Fy[d.ij1]) + DTy[d.ij1];
+      Temper[d.ij] =
+          (ht * (aT1 * (b[d.i_1j] * TT[d.i_1j] + (!b[d.i_1j]) * Tw_u[d.ij]) +
+                 aT2 * (b[d.i1j] * TT[d.i1j] + (!b[d.i1j]) * Tw_u[d.i1j]) +
+                 aT3 * (b[d.ij_1] * TT[d.ij_1] + (!b[d.ij_1]) * Tw_v[d.ij]) +
+                 aT4 * (b[d.ij1] * TT[d.ij1] + (!b[d.ij1]) * Tw_v[d.ij1]) +
+                 (1.0 - gamma1) * P[d.ij] * ((u[d.i1j] - u[d.ij]) * hy[j] + (v[d.ij1] - v[d.ij]) * hx[i])) +
+           ScT1[d.ij]) /
+          (ht * (aT1 + aT2 + aT3 + aT4 + Fx[d.i1j] - Fx[d.ij] + Fy[d.ij1] - Fy[d.ij]) + hx[i] * hy[j] * rho[d.ij]);
+      double rT = Temper[d.ij] - Temper_old[d.ij];
+      bool gxb = Given_velocity_on_xb * (i == Nx_o[0]);
+      bool gxe = Given_velocity_on_xe * (i == Nx_o[1] - 1);
+      p[d.ij] = (ht * (apx[d.ij] * P[d.i_1j] + apx[d.i1j] * P[d.i1j] + apy[d.ij] * P[d.ij_1] + apy[d.ij1] * P[d.ij1] +
+                       bpx[d.ij] - bpx[d.i1j] + bpy[d.ij] - bpy[d.ij1] + gxb * Fx[d.ij] - gxe * Fx[d.i1j]) +
+                 p_pr[d.ij] * hx[i] * hy[j] / (Temper_pr[d.ij])) /
+                (ht * (apx[d.ij] + apx[d.i1j] + apy[d.ij] + apy[d.ij1]) + hx[i] * hy[j] / (Temper[d.ij]));
+      double rp = p[d.ij] - p_old[d.ij];
+      if (max_res_T[Iter] < std::fabs(rT)) max_res_T[Iter] = std::fabs(rT);
+      if (max_res_p[Iter] < std::fabs(rp)) max_res_p[Iter] = std::fabs(rp);
+    }
+    for (size_t c = 0; c < nch_o.size(); c++) {
+      uint n = nch_o[c];
+      Idx d = clamped(n % Nx, n / Nx);
+      uint i = d.i, j = d.j;
+      double aT1 = dmax(0, Fx[d.ij]) + DTx[d.ij];
+      double aT2 = dmax(0, -Fx[d.i1j]) + DTx[d.i1j];
+      double aT3 = dmax(0, Fy[d.ij]) + DTy[d.ij];
+      double aT4 = dmax(0, -Fy[d.ij1]) + DTy[d.ij1];
+      Temper[d.ij] = (ht * (aT1 * TT[d.i_1j] + aT2 * TT[d.i1j] + aT3 * TT[d.ij_1] + aT4 * TT[d.ij1] +
+                            (1.0 - gamma1) * P[d.ij] * ((u[d.i1j] - u[d.ij]) * hy[j] + (v[d.ij1] - v[d.ij]) * hx[i])) +
+                      ScT1[d.ij]) /
+                     (ht * (aT1 + aT2 + aT3 + aT4 + Fx[d.i1j] - Fx[d.ij] + Fy[d.ij1] - Fy[d.ij]) + hx[i] * hy[j] * rho[d.ij]);
+      double rT = Temper[d.ij] - Temper_old[d.ij];
+      p[d.ij] = (ht * (apx[d.ij] * P[d.i_1j] + apx[d.i1j] * P[d.i1j] + apy[d.ij] * P[d.ij_1] + apy[d.ij1] * P[d.ij1] +
+                       bpx[d.ij] - bpx[d.i1j] + bpy[d.ij] - bpy[d.ij1]) +
+                 p_pr[d.ij] * hx[i] * hy[j] / (Temper_pr[d.ij])) /
+                (ht * (apx[d.ij] + apx[d.i1j] + apy[d.ij] + apy[d.ij1]) + hx[i] * hy[j] / (Temper[d.ij]));
+      double rp = p[d.ij] - p_old[d.ij];
+      if (max_res_p[Iter] < std::fabs(rp)) max_res_p[Iter] = std::fabs(rp);
+      if (max_res_T[Iter] < std::fabs(rT)) max_res_T[Iter] = std::fabs(rT);
+    }
+    if (Iter_p_c == 0) {
+      max_res_p0[Iter] = max_res_p[Iter];
+      max_res_T0[Iter] = max_res_T[Iter];
+    }
+    Iter_p_c++;
+    if (fixed_sweeps)
+      continue_iter_p_c = (Iter_p_c < N_I_p_c);
+    else
+      continue_iter_p_c = (Iter_p_c < 2) ||
+                          ((Iter_p_c < N_I_p_c) && ((MaxError_p_c < max_res_p[Iter]) || (MaxError_T < max_res_T[Iter])));
+  } while (continue_iter_p_c);
+}
+
 // one pass of the time loop body, SIMPLE_TS_MPI.cpp:3230-4691
 void Oracle::step() {
   std::memcpy(p_pr, p, Na * sizeof(double));
@@ -1714,73 +1788,7 @@ void Oracle::step() {
     std::memcpy(p_old, p, Na * sizeof(double));
     std::memcpy(Temper_old, Temper, Na * sizeof(double));
     // ---- coupled p-T Jacobi sweeps (:3786-4131) ----
-    continue_iter_p_c = false;
-    Iter_p_c = 0;
-    do {
-      std::swap(p, p_old);
-      std::swap(Temper, Temper_old);
-      const double* P = p_old;
-      const double* TT = Temper_old;
-      max_res_p[Iter] = 0;
-      max_res_T[Iter] = 0;
-      for (size_t c = 0; c < bc_o.size(); c++) {
-        Idx d = bc_idx(bc_o[c]);
-        uint i = d.i, j = d.j;
-        double aT1 = dmax(0, Fx[d.ij]) + DTx[d.ij];
-        double aT2 = dmax(0, -Fx[d.i1j]) + DTx[d.i1j];
-        double aT3 = dmax(0, Fy[d.ij]) + DTy[d.ij];
-        double aT4 = dmax(0, -Fy[d.ij1]) + DTy[d.ij1];
-        Temper[d.ij] =
-            (ht * (aT1 * (b[d.i_1j] * TT[d.i_1j] + (!b[d.i_1j]) * Tw_u[d.ij]) +
-                   aT2 * (b[d.i1j] * TT[d.i1j] + (!b[d.i1j]) * Tw_u[d.i1j]) +
-                   aT3 * (b[d.ij_1] * TT[d.ij_1] + (!b[d.ij_1]) * Tw_v[d.ij]) +
-                   aT4 * (b[d.ij1] * TT[d.ij1] + (!b[d.ij1]) * Tw_v[d.ij1]) +
-                   (1.0 - gamma1) * P[d.ij] * ((u[d.i1j] - u[d.ij]) * hy[j] + (v[d.ij1] - v[d.ij]) * hx[i])) +
-             ScT1[d.ij]) /
-            (ht * (aT1 + aT2 + aT3 + aT4 + Fx[d.i1j] - Fx[d.ij] + Fy[d.ij1] - Fy[d.ij]) + hx[i] * hy[j] * rho[d.ij]);
-        double rT = Temper[d.ij] - Temper_old[d.ij];
-        bool gxb = Given_velocity_on_xb * (i == Nx_o[0]);
-        bool gxe = Given_velocity_on_xe * (i == Nx_o[1] - 1);
-        p[d.ij] = (ht * (apx[d.ij] * P[d.i_1j] + apx[d.i1j] * P[d.i1j] + apy[d.ij] * P[d.ij_1] + apy[d.ij1] * P[d.ij1] +
-                         bpx[d.ij] - bpx[d.i1j] + bpy[d.ij] - bpy[d.ij1] + gxb * Fx[d.ij] - gxe * Fx[d.i1j]) +
-                   p_pr[d.ij] * hx[i] * hy[j] / (Temper_pr[d.ij])) /
-                  (ht * (apx[d.ij] + apx[d.i1j] + apy[d.ij] + apy[d.ij1]) + hx[i] * hy[j] / (Temper[d.ij]));
-        double rp = p[d.ij] - p_old[d.ij];
-        if (max_res_T[Iter] < std::fabs(rT)) max_res_T[Iter] = std::fabs(rT);
-        if (max_res_p[Iter] < std::fabs(rp)) max_res_p[Iter] = std::fabs(rp);
-      }
-      for (size_t c = 0; c < nch_o.size(); c++) {
-        uint n = nch_o[c];
-        Idx d = clamped(n % Nx, n / Nx);
-        uint i = d.i, j = d.j;
-        double aT1 = dmax(0, Fx[d.ij]) + DTx[d.ij];
-        double aT2 = dmax(0, -Fx[d.i1j]) + DTx[d.i1j];
-        double aT3 = dmax(0, Fy[d.ij]) + DTy[d.ij];
-        double aT4 = dmax(0, -Fy[d.ij1]) + DTy[d.ij1];
-        Temper[d.ij] = (ht * (aT1 * TT[d.i_1j] + aT2 * TT[d.i1j] + aT3 * TT[d.ij_1] + aT4 * TT[d.ij1] +
-                              (1.0 - gamma1) * P[d.ij] * ((u[d.i1j] - u[d.ij]) * hy[j] + (v[d.ij1] - v[d.ij]) * hx[i])) +
-                        ScT1[d.ij]) /
-                       (ht * (aT1 + aT2 + aT3 + aT4 + Fx[d.i1j] - Fx[d.ij] + Fy[d.ij1] - Fy[d.ij]) + hx[i] * hy[j] * rho[d.ij]);
-        double rT = Temper[d.ij] - Temper_old[d.ij];
-        p[d.ij] = (ht * (apx[d.ij] * P[d.i_1j] + apx[d.i1j] * P[d.i1j] + apy[d.ij] * P[d.ij_1] + apy[d.ij1] * P[d.ij1] +
-                         bpx[d.ij] - bpx[d.i1j] + bpy[d.ij] - bpy[d.ij1]) +
-                   p_pr[d.ij] * hx[i] * hy[j] / (Temper_pr[d.ij])) /
-                  (ht * (apx[d.ij] + apx[d.i1j] + apy[d.ij] + apy[d.ij1]) + hx[i] * hy[j] / (Temper[d.ij]));
-        double rp = p[d.ij] - p_old[d.ij];
-        if (max_res_p[Iter] < std::fabs(rp)) max_res_p[Iter] = std::fabs(rp);
-        if (max_res_T[Iter] < std::fabs(rT)) max_res_T[Iter] = std::fabs(rT);
-      }
-      if (Iter_p_c == 0) {
-        max_res_p0[Iter] = max_res_p[Iter];
-        max_res_T0[Iter] = max_res_T[Iter];
-      }
-      Iter_p_c++;
-      if (fixed_sweeps)
-        continue_iter_p_c = (Iter_p_c < N_I_p_c);
-      else
-        continue_iter_p_c = (Iter_p_c < 2) ||
-                            ((Iter_p_c < N_I_p_c) && ((MaxError_p_c < max_res_p[Iter]) || (MaxError_T < max_res_T[Iter])));
-    } while (continue_iter_p_c);
+    pt_sweeps();
     max_Iter_p_c[Iter] = Iter_p_c;
     step_sweeps += Iter_p_c;
     // ---- velocity correction (:4171-4305) ----
@@ -1976,6 +1984,53 @@ int ora_get_class(ora_handle* h, unsigned char* out) {
 
 int ora_get_mask(ora_handle* h, unsigned int* out) {
   std::memcpy(out, h->o.vol_inf_fb.data(), sizeof(unsigned int) * h->o.Na);
+  return 0;
+}
+
+// The p-T sweep loop alone (Oracle::pt_sweeps, the same code the time step runs) on host
+// arrays: cls uses the class-byte layout of ora_get_class (bits 4-5 p/T class, bit 6 fluid);
+// p and T hold the initial iterate and receive the result.
+int ora_pt_sweeps(int Nx, int Ny, int periodic, int given_xb, int given_xe, int Nx_o0, int Nx_o1, double ht,
+                  double gamma1, const unsigned char* cls, const double* hx, const double* hy, const double* Fx,
+                  const double* Fy, const double* DTx, const double* DTy, const double* u, const double* v,
+                  const double* rho, const double* ScT1, const double* apx, const double* apy, const double* bpx,
+                  const double* bpy, const double* p_pr, const double* T_pr, const double* Tw_u, const double* Tw_v,
+                  double* p, double* T, int max_sweeps, int fixed, double tol_p, double tol_T, int* sweeps_done,
+                  double* res_p, double* res_T) {
+  Oracle o;
+  const uint Na = (uint)(Nx * Ny);
+  o.Nx = (uint)Nx; o.Ny = (uint)Ny; o.Na = Na;
+  o.Periodic = periodic != 0;
+  o.Given_velocity_on_xb = given_xb != 0;
+  o.Given_velocity_on_xe = given_xe != 0;
+  o.Nx_o[0] = (uint)Nx_o0; o.Nx_o[1] = (uint)Nx_o1;
+  o.ht = ht; o.gamma1 = gamma1;
+  o.N_I_p_c = (uint)max_sweeps; o.fixed_sweeps = fixed != 0;
+  o.MaxError_p_c = tol_p; o.MaxError_T = tol_T;
+  auto cp = [&](std::vector<double>& dst, const double* src, uint n) { dst.assign(src, src + n); };
+  cp(o.hx, hx, (uint)Nx); cp(o.hy, hy, (uint)Ny);
+  cp(o.Fx, Fx, Na); cp(o.Fy, Fy, Na); cp(o.DTx, DTx, Na); cp(o.DTy, DTy, Na); cp(o.st_u0, u, Na); cp(o.st_v0, v, Na);
+  cp(o.st_r0, rho, Na); cp(o.ScT1, ScT1, Na); cp(o.apx, apx, Na); cp(o.apy, apy, Na); cp(o.bpx, bpx, Na);
+  cp(o.bpy, bpy, Na); cp(o.st_p1, p_pr, Na); cp(o.st_T1, T_pr, Na); cp(o.Tw_u, Tw_u, Na); cp(o.Tw_v, Tw_v, Na);
+  cp(o.st_p0, p, Na); cp(o.st_p2, p, Na); cp(o.st_T0, T, Na); cp(o.st_T2, T, Na);
+  o.u = o.st_u0.data(); o.v = o.st_v0.data(); o.rho = o.st_r0.data();
+  o.p = o.st_p0.data(); o.p_pr = o.st_p1.data(); o.p_old = o.st_p2.data();
+  o.Temper = o.st_T0.data(); o.Temper_pr = o.st_T1.data(); o.Temper_old = o.st_T2.data();
+  o.vol.assign(Na, 0);
+  for (uint c = 0; c < Na; c++) {
+    o.vol[c] = (cls[c] >> 6) & 1;
+    const int k = (cls[c] >> 4) & 3;
+    if (k == 1) o.nch_o.push_back(c);
+    else if (k == 2) o.bc_o.push_back(c);
+  }
+  o.max_res_p.assign(1, 0); o.max_res_T.assign(1, 0); o.max_res_p0.assign(1, 0); o.max_res_T0.assign(1, 0);
+  o.Iter = 0;
+  o.pt_sweeps();
+  std::memcpy(p, o.p, sizeof(double) * Na);
+  std::memcpy(T, o.Temper, sizeof(double) * Na);
+  if (sweeps_done) *sweeps_done = (int)o.Iter_p_c;
+  if (res_p) *res_p = o.max_res_p[0];
+  if (res_T) *res_T = o.max_res_T[0];
   return 0;
 }
 

@@ -395,6 +395,92 @@ int sts_ctx::write_logs(bool iterations) {
 
 namespace {
 
+// Scratch of one sweep-loop call: the second p and T buffers, the 8 sweep invariants and the
+// control block, carved out of one device region of scratch_bytes(Na) bytes.
+size_t scratch_bytes(size_t Na) { return sizeof(Ctl) + 256 + 10 * Na * sizeof(double); }
+
+// The sweep loop of sts_pt_sweeps on a given scratch region (no allocation here).
+int pt_sweeps_on(const sts_sweep_fields* f, int max_sweeps, int fixed, double tol_p, double tol_T, cudaStream_t s,
+                 char* scratch, int* sweeps_done, double* res_p, double* res_T) {
+  const size_t Na = (size_t)f->Nx * (size_t)f->Ny;
+  Geo g{};
+  g.Nx = f->Nx;
+  g.Ny = f->Ny;
+  g.Na = (int)Na;
+  g.bits = (f->periodic ? F_PERIODIC : 0) | (f->given_u_xb ? F_GIVEN_U_XB : 0) | (f->given_u_xe ? F_GIVEN_U_XE : 0) |
+           (fixed ? F_FIXED_SWEEPS : 0);
+  g.Nx_o0 = f->Nx_o0;
+  g.Nx_o1 = f->Nx_o1;
+  g.ht = f->ht;
+  g.gamma1 = f->gamma1;
+  g.MaxError_p_c = tol_p;
+  g.MaxError_T = tol_T;
+  g.N_I_p_c = max_sweeps;
+  g.cls = f->cls;
+  g.hx = f->hx; g.hy = f->hy;
+  g.Fx = const_cast<double*>(f->Fx); g.Fy = const_cast<double*>(f->Fy);
+  g.DTx = const_cast<double*>(f->DTx); g.DTy = const_cast<double*>(f->DTy);
+  g.u = const_cast<double*>(f->u); g.v = const_cast<double*>(f->v); g.rho = const_cast<double*>(f->rho);
+  g.ScT1 = const_cast<double*>(f->ScT1);
+  g.apx = const_cast<double*>(f->apx); g.apy = const_cast<double*>(f->apy);
+  g.bpx = const_cast<double*>(f->bpx); g.bpy = const_cast<double*>(f->bpy);
+  g.p_pr = const_cast<double*>(f->p_pr); g.T_pr = const_cast<double*>(f->T_pr);
+  g.Tw_u = const_cast<double*>(f->Tw_u); g.Tw_v = const_cast<double*>(f->Tw_v);
+  Ctl* ctl = (Ctl*)scratch;
+  double* arr = (double*)(scratch + ((sizeof(Ctl) + 255) / 256) * 256);
+  g.ctl = ctl;
+  g.p[0] = f->p;
+  g.T[0] = f->T;
+  g.p[1] = arr;
+  g.T[1] = arr + Na;
+  for (int k = 0; k < 8; k++) g.inv[k] = arr + (2 + k) * Na;
+  CU(cudaMemsetAsync(ctl, 0, sizeof(Ctl), s));  // buffer index, counters and maxima start at zero
+  const dim3 block(32, 8), grid((f->Nx + 31) / 32, (f->Ny + 7) / 8);
+  k_sweep_first<<<grid, block, 0, s>>>(g, 0, 0);
+  struct { unsigned cur, Iter, Iter_pr1, Iter_pr2, Iter_p_c, it_counter, pt_done; } head{};
+  const size_t head_off = offsetof(Ctl, cur);
+  if (fixed) {
+    for (int q = 1; q < max_sweeps; q++) k_sweep<<<grid, block, 0, s>>>(g, 0, 0);
+  } else {
+    int launched = 1;
+    for (;;) {
+      CU(cudaMemcpyAsync(&head, (char*)ctl + head_off, sizeof(head), cudaMemcpyDeviceToHost, s));
+      CU(cudaStreamSynchronize(s));
+      if (head.pt_done || launched >= max_sweeps) break;
+      for (int q = 0; q < 4 && launched < max_sweeps; q++, launched++) k_sweep<<<grid, block, 0, s>>>(g, 0, 0);
+    }
+  }
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(&head, (char*)ctl + head_off, sizeof(head), cudaMemcpyDeviceToHost, s));
+  double rp = 0, rT = 0;
+  unsigned status = 0;
+  CU(cudaMemcpyAsync(&rp, &ctl->res_p[0], sizeof(double), cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(&rT, &ctl->res_T[0], sizeof(double), cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(&status, &ctl->status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  if (head.cur == 1) {  // an odd number of sweeps left the result in the scratch buffers
+    CU(cudaMemcpyAsync(f->p, g.p[1], sizeof(double) * Na, cudaMemcpyDeviceToDevice, s));
+    CU(cudaMemcpyAsync(f->T, g.T[1], sizeof(double) * Na, cudaMemcpyDeviceToDevice, s));
+    CU(cudaStreamSynchronize(s));
+  }
+  if (sweeps_done) *sweeps_done = (int)head.Iter_p_c;
+  if (res_p) *res_p = rp;
+  if (res_T) *res_T = rT;
+  if (status & 1u) return fail(STS_ERR_NONFINITE, "a residual became NaN or Inf");
+  return STS_OK;
+}
+
+int check_sweep_args(const sts_sweep_fields* f, int max_sweeps) {
+  if (!f || max_sweeps < 1) return fail(STS_ERR_ARG, "bad argument");
+  if (f->Nx < 3 || f->Ny < 3) return fail(STS_ERR_ARG, "mesh must have at least 3 cells in each direction");
+  const void* ptrs[] = {f->cls, f->hx, f->hy, f->Fx, f->Fy, f->DTx, f->DTy, f->u, f->v, f->rho, f->ScT1, f->apx,
+                        f->apy, f->bpx, f->bpy, f->p_pr, f->T_pr, f->Tw_u, f->Tw_v, f->p, f->T};
+  for (const void* q : ptrs)
+    if (!q) return fail(STS_ERR_ARG, "null field pointer");
+  if (f->Nx_o0 < 0 || f->Nx_o1 > f->Nx) return fail(STS_ERR_ARG, "bad p/T solve range");
+  return STS_OK;
+}
+
 int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
   if (!dir || !out) return fail(STS_ERR_ARG, "null argument");
   sts_options opt;
@@ -646,6 +732,7 @@ int sts_get_field(sts_ctx* ctx, const char* name, double* out) {
   if (n == "y_v") { std::memcpy(out, ctx->hc.y_v.data(), sizeof(double) * g.Ny); return STS_OK; }
   struct { const char* k; const double* p; } tab[] = {
       {"u", g.u}, {"v", g.v}, {"p", g.p[cur]}, {"T", g.T[cur]}, {"rho", g.rho}, {"sqrt_T", g.sqrt_T},
+      {"p_pr", g.p_pr}, {"T_pr", g.T_pr}, {"u_pr", g.u_pr}, {"v_pr", g.v_pr}, {"rho_pr", g.rho_pr},
       {"rho_u", g.rho_u}, {"rho_v", g.rho_v}, {"Fx", g.Fx}, {"Fy", g.Fy}, {"D_ux", g.D_ux}, {"D_uy", g.D_uy},
       {"D_vx", g.D_vx}, {"D_vy", g.D_vy}, {"DTx", g.DTx}, {"DTy", g.DTy}, {"Gamma_xf", g.Gamma_xf},
       {"Gamma_yf", g.Gamma_yf}, {"ScT1", g.ScT1}, {"apx", g.apx}, {"apy", g.apy}, {"bpx", g.bpx}, {"bpy", g.bpy},
@@ -750,6 +837,19 @@ int sts_run_case(const char* case_dir, const sts_options* opt) {
   if (int q = ctx->write_outputs()) return q;
   if (int q = ctx->write_logs(false)) return q;  // the final log writes Tmp.txt only (SIMPLE_TS_MPI.cpp:4714)
   return STS_OK;
+}
+
+int sts_pt_sweeps(const sts_sweep_fields* f, int max_sweeps, int fixed_sweeps, double tol_p, double tol_T,
+                  void* stream, int* sweeps_done, double* res_p, double* res_T) {
+  g_err.clear();
+  if (int r = check_sweep_args(f, max_sweeps)) return r;
+  cudaStream_t s = (cudaStream_t)stream;
+  char* scratch = nullptr;
+  CU(cudaMallocAsync((void**)&scratch, scratch_bytes((size_t)f->Nx * f->Ny), s));
+  const int r = pt_sweeps_on(f, max_sweeps, fixed_sweeps, tol_p, tol_T, s, scratch, sweeps_done, res_p, res_T);
+  cudaFreeAsync(scratch, s);
+  cudaStreamSynchronize(s);
+  return r;
 }
 
 int sts_sync(sts_ctx* ctx) {

@@ -26,7 +26,7 @@ STS_ERR_NONFINITE = -4
 EXPORTS = [
     "sts_default_options", "sts_open_case", "sts_step", "sts_get_field", "sts_set_field", "sts_dims",
     "sts_stats", "sts_sweep_history", "sts_write_outputs", "sts_run_case", "sts_sync", "sts_destroy",
-    "sts_last_error", "sts_inspect_case", "sts_step_timed", "sts_profile_steps",
+    "sts_last_error", "sts_inspect_case", "sts_step_timed", "sts_profile_steps", "sts_pt_sweeps",
 ]
 
 KERNELS = ["step_begin", "assemble", "sweep", "correct", "face_rho", "boundary", "flux_diff", "step_end"]
@@ -206,3 +206,28 @@ def inspect_case(case_dir: str) -> dict:
                                 vol.ctypes.data_as(C.POINTER(C.c_uint)), cls.ctypes.data_as(C.POINTER(C.c_ubyte)),
                                 _dptr(hx), _dptr(hy), _dptr(xv), _dptr(yv)))
     return dict(Nx=Nx, Ny=Ny, vol=vol.reshape(Ny, Nx), cls=cls.reshape(Ny, Nx), hx=hx, hy=hy, x_v=xv, y_v=yv)
+
+
+class SweepFields(C.Structure):
+    """sts_sweep_fields: device pointers (ints) of the sweep inputs."""
+    _fields_ = [("Nx", C.c_int), ("Ny", C.c_int), ("periodic", C.c_int), ("given_u_xb", C.c_int),
+                ("given_u_xe", C.c_int), ("Nx_o0", C.c_int), ("Nx_o1", C.c_int), ("ht", C.c_double),
+                ("gamma1", C.c_double)] + [(n, C.c_void_p) for n in (
+                    "cls", "hx", "hy", "Fx", "Fy", "DTx", "DTy", "u", "v", "rho", "ScT1", "apx", "apy", "bpx", "bpy",
+                    "p_pr", "T_pr", "Tw_u", "Tw_v", "p", "T")]
+
+
+SWEEP_INPUTS = ["Fx", "Fy", "DTx", "DTy", "u", "v", "rho", "ScT1", "apx", "apy", "bpx", "bpy", "p_pr", "T_pr",
+                "Tw_u", "Tw_v"]
+
+
+def pt_sweeps(fields: SweepFields, max_sweeps: int, fixed_sweeps: bool, tol_p: float, tol_T: float,
+              stream: int = 0):
+    """Runs the p-T sweep loop on device arrays; returns (sweeps, res_p, res_T)."""
+    lib = load()
+    lib.sts_pt_sweeps.argtypes = [C.POINTER(SweepFields), C.c_int, C.c_int, C.c_double, C.c_double, C.c_void_p,
+                                  C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    n, rp, rT = C.c_int(), C.c_double(), C.c_double()
+    _check(lib.sts_pt_sweeps(C.byref(fields), int(max_sweeps), int(fixed_sweeps), float(tol_p), float(tol_T),
+                             C.c_void_p(stream), C.byref(n), C.byref(rp), C.byref(rT)))
+    return n.value, rp.value, rT.value
