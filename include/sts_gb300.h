@@ -130,6 +130,26 @@ typedef struct sts_sweep_fields {
 int sts_pt_sweeps(const sts_sweep_fields* f, int max_sweeps, int fixed_sweeps, double tol_p, double tol_T,
                   void* stream, int* sweeps_done, double* res_p, double* res_T);
 
+/* Largest mesh (Nx*Ny cells) that sts_pt_sweeps_noalloc accepts. */
+#define STS_NOALLOC_MAX_CELLS 32768
+
+/* sts_pt_sweeps for callers that must not allocate device memory: no cudaMalloc, cudaFree or
+ * other allocating call is made.  This entry point has no counterpart in the reference (which
+ * runs on the host only); it exists for programs whose device memory is owned by someone else
+ * -- a framework's caching pool or an embedding application that has reserved the device
+ * memory it is allowed to use -- and for time-critical loops that cannot afford the
+ * device-wide synchronisation and latency an allocation or free can cause.
+ * Inputs and outputs are the caller's device arrays, as for sts_pt_sweeps.  The scratch lives
+ * in one fixed device array inside the library, sized for STS_NOALLOC_MAX_CELLS cells (about
+ * 2.6 MB, held on every GPU that loads the library until the process exits); larger meshes are
+ * rejected with STS_ERR_ARG.  The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress) with the device current; make that first call before any stream
+ * capture.  All calls share the one array and it keeps the last call's contents (each call
+ * clears the counters it needs), so calls whose work overlaps on the GPU -- from several
+ * threads or streams at once -- race and must be serialised by the caller. */
+int sts_pt_sweeps_noalloc(const sts_sweep_fields* f, int max_sweeps, int fixed_sweeps, double tol_p, double tol_T,
+                          void* stream, int* sweeps_done, double* res_p, double* res_T);
+
 /* Host-only inspection of a case directory (no device use): dims, obstacle ids
  * (vol_inf_fb, Nx*Ny), per-cell classes (Nx*Ny bytes: bits 0-1 u, 2-3 v, 4-5 p/T with
  * 0 unsolved, 1 interior, 2 boundary; bit 6 fluid) and the mesh (hx, x_v: Nx; hy, y_v: Ny).

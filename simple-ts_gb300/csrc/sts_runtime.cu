@@ -9,6 +9,7 @@
 #include <ctime>
 #include <fstream>
 #include <memory>
+#include <mutex>
 #include <tuple>
 #include <algorithm>
 #include <iomanip>
@@ -850,6 +851,52 @@ int sts_pt_sweeps(const sts_sweep_fields* f, int max_sweeps, int fixed_sweeps, d
   cudaFreeAsync(scratch, s);
   cudaStreamSynchronize(s);
   return r;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Scratch of sts_pt_sweeps_noalloc: one fixed array per GPU that loads the library, laid out
+// like the allocated scratch of sts_pt_sweeps (control block, then 10 fields of Nx*Ny doubles).
+constexpr size_t kNoAllocBytes = sizeof(Ctl) + 256 + 10 * (size_t)STS_NOALLOC_MAX_CELLS * sizeof(double);
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+// Device address of g_noalloc_scratch on each device, looked up once with that device current
+// (in host code the array's name only stands in for the symbol; it is not a device address).
+std::mutex g_noalloc_mutex;
+std::vector<char*> g_noalloc_addr;
+
+int noalloc_scratch(char** out) {
+  int dev = 0;
+  CU(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if ((int)g_noalloc_addr.size() <= dev) g_noalloc_addr.resize(dev + 1, nullptr);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    CU(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_addr[dev] = (char*)p;
+  }
+  *out = g_noalloc_addr[dev];
+  return STS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sts_pt_sweeps_noalloc(const sts_sweep_fields* f, int max_sweeps, int fixed_sweeps, double tol_p, double tol_T,
+                          void* stream, int* sweeps_done, double* res_p, double* res_T) {
+  g_err.clear();
+  if (int r = check_sweep_args(f, max_sweeps)) return r;
+  if ((size_t)f->Nx * (size_t)f->Ny > (size_t)STS_NOALLOC_MAX_CELLS)
+    return fail(STS_ERR_ARG, "mesh of " + std::to_string((size_t)f->Nx * f->Ny) +
+                                 " cells exceeds the no-allocation limit of " + std::to_string(STS_NOALLOC_MAX_CELLS) +
+                                 " cells; use sts_pt_sweeps");
+  char* scratch = nullptr;
+  if (int r = noalloc_scratch(&scratch)) return r;
+  return pt_sweeps_on(f, max_sweeps, fixed_sweeps, tol_p, tol_T, (cudaStream_t)stream, scratch, sweeps_done, res_p,
+                      res_T);
 }
 
 int sts_sync(sts_ctx* ctx) {

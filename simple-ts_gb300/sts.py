@@ -27,6 +27,7 @@ EXPORTS = [
     "sts_default_options", "sts_open_case", "sts_step", "sts_get_field", "sts_set_field", "sts_dims",
     "sts_stats", "sts_sweep_history", "sts_write_outputs", "sts_run_case", "sts_sync", "sts_destroy",
     "sts_last_error", "sts_inspect_case", "sts_step_timed", "sts_profile_steps", "sts_pt_sweeps",
+    "sts_pt_sweeps_noalloc",
 ]
 
 KERNELS = ["step_begin", "assemble", "sweep", "correct", "face_rho", "boundary", "flux_diff", "step_end"]
@@ -230,4 +231,18 @@ def pt_sweeps(fields: SweepFields, max_sweeps: int, fixed_sweeps: bool, tol_p: f
     n, rp, rT = C.c_int(), C.c_double(), C.c_double()
     _check(lib.sts_pt_sweeps(C.byref(fields), int(max_sweeps), int(fixed_sweeps), float(tol_p), float(tol_T),
                              C.c_void_p(stream), C.byref(n), C.byref(rp), C.byref(rT)))
+    return n.value, rp.value, rT.value
+
+
+def pt_sweeps_noalloc(fields: SweepFields, max_sweeps: int, fixed_sweeps: bool, tol_p: float, tol_T: float,
+                      stream: int = 0):
+    """sts_pt_sweeps_noalloc: the same loop for callers that must not allocate device memory
+    (scratch in the library's fixed device array, meshes up to STS_NOALLOC_MAX_CELLS cells)."""
+    lib = load()
+    lib.sts_pt_sweeps_noalloc.argtypes = [C.POINTER(SweepFields), C.c_int, C.c_int, C.c_double, C.c_double,
+                                          C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                          C.POINTER(C.c_double)]
+    n, rp, rT = C.c_int(), C.c_double(), C.c_double()
+    _check(lib.sts_pt_sweeps_noalloc(C.byref(fields), int(max_sweeps), int(fixed_sweeps), float(tol_p),
+                                     float(tol_T), C.c_void_p(stream), C.byref(n), C.byref(rp), C.byref(rT)))
     return n.value, rp.value, rT.value
