@@ -42,6 +42,10 @@ BYTES_PER_CELL = {
     "step_begin": 10 * 8,
 }
 
+# DRAM bytes per launch measured by ncu on this workload (dram__bytes_read.sum +
+# dram__bytes_write.sum); None where no capture was taken
+TRAFFIC = {}
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -51,6 +55,10 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-variants", dest="variants", action="store_false",
+                    help="skip the FP64-fast and FP32-correction runs of the same workload")
+    ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2],
+                    help="precision mode of the --profile-target run")
     ap.add_argument("--profile-target", type=int, default=0,
                     help="only run this many steps kernel by kernel (a small target for ncu), then exit")
     return ap.parse_args()
@@ -62,7 +70,7 @@ def profile_target(args):
     import build as stsbuild
     stsbuild.build()
     _, d = make_case(args.workload)
-    s = sts.Solver(d, fixed_sweeps=False, use_graph=False)
+    s = sts.Solver(d, fixed_sweeps=False, use_graph=False, precision=args.precision)
     s.step(args.profile_target)
     s.sync()
     print(f"profile target: {args.workload}, {args.profile_target} steps, sweeps {list(s.sweep_history())}")
@@ -202,6 +210,43 @@ def config(case, Nx, Ny):
             "l2": "flushed before every timed step (256 MiB write); working set 42 MB < L2"}
 
 
+def timed_steps(s, steps, warmup, flush, barrier, clocks=None):
+    """Warm-up, then `steps` steps each after an L2 flush; device ms from CUDA events on the
+    library's stream.  Returns (steps done, total device ms, sweeps of the timed steps)."""
+    import torch
+    for _ in range(max(warmup, 3)):
+        s.step(1)
+    s.sync()
+    barrier()
+    total_ms, done = 0.0, 0
+    ctx = clocks if clocks is not None else _Null()
+    with ctx:
+        for _ in range(steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            n, ms = s.step_timed(1)
+            total_ms += ms
+            done += n
+    barrier()
+    return done, total_ms, (s.sweep_history()[-done:] if done else [])
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        pass
+
+
+def launches_per_step(kcnt, pn, precision):
+    """Kernels one step launches besides its sweeps, from a kernel-by-kernel profile pass."""
+    fixed = sum(v for k, v in kcnt.items() if k not in ("sweep", "sweep32")) / max(pn, 1)
+    # mode 2: the FP64 re-forming of the iterate (counted under sweep32) and the FP32 sweep
+    # that the FP64 sweep recomputes
+    return fixed + (2 if precision == 2 else 0)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -209,6 +254,7 @@ def main():
     if args.profile_target:
         return profile_target(args)
     rank, world, local = dist_env()
+    import numpy as np
     import torch
     torch.cuda.set_device(local)
     if world > 1:
@@ -218,8 +264,6 @@ def main():
     import build as stsbuild
     stsbuild.build()
     case, d = make_case(args.workload)
-    s = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local)
-    Na = s.Nx * s.Ny
     flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")
 
     def barrier():
@@ -228,30 +272,16 @@ def main():
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    # warm-up
-    for _ in range(max(args.warmup, 3)):
-        s.step(1)
-    s.sync()
-    h0 = len(s.sweep_history())
-    # timed region: K steps, each after an L2 flush, device time from events on the library stream
-    barrier()
-    total_ms, done = 0.0, 0
+    # headline: the FP64 path, bit-exact with the reference
+    s = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=sts.EXACT)
+    Nx, Ny = s.Nx, s.Ny
+    Na = Nx * Ny
     with Clocks(local) as clk:
-        for _ in range(args.steps):
-            flush.fill_(1.0)
-            torch.cuda.synchronize()
-            n, ms = s.step_timed(1)
-            total_ms += ms
-            done += n
-    barrier()
+        done, total_ms, sweeps = timed_steps(s, args.steps, args.warmup, flush, barrier)
     t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
     if world > 1:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
     total_ms = float(t.item())
-    sweeps = s.sweep_history()[-done:] if done else []
-    # kernels per step with one outer iteration: step_begin, assemble, S sweeps, correct,
-    # face_rho, boundary, flux_diff, step_end
-    launches = int(sum(7 + int(x) for x in sweeps))
     value = Na * done * world / (total_ms / 1e3)
 
     # e2e through the C ABI with host buffers: per step the state u, v, p, T goes host->device
@@ -275,27 +305,53 @@ def main():
 
     # per-kernel device time over a few more real steps (the roofline's dominant kernel)
     pn, kms, kcnt = s.profile(max(3, min(args.steps, 10)))
+    launches = int(round(sum(launches_per_step(kcnt, pn, 0) + int(x) for x in sweeps)))
     dom = max(kms, key=lambda k: kms[k])
     peak, peak_kind = peaks()
     avg_s = kms[dom] / 1e3 / max(kcnt[dom], 1)
     bpc = BYTES_PER_CELL.get(dom, 0)
     achieved = bpc * Na / avg_s / 1e9 if bpc else None
     roof = {"bound": "hbm", "kernel": "k_" + dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": (achieved / peak) if achieved else None, "traffic": None,
+            "frac": (achieved / peak) if achieved else None, "traffic": TRAFFIC.get(dom),
             "peak_source": peak_kind, "bytes_per_cell": bpc, "avg_launch_us": avg_s * 1e6,
-            "kernel_share": {k: round(v / sum(kms.values()), 4) for k, v in kms.items()}}
+            "kernel_share": {k: round(v / max(sum(kms.values()), 1e-30), 4) for k, v in kms.items()}}
+    s.close()
+
+    # the same workload in the faster precision modes, from the same initial state, with the
+    # per-field relative L2 distance from the FP64 path (bit-exact with the reference) after
+    # the same number of steps
+    variants = {}
+    if args.variants:
+        ref = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=sts.EXACT)
+        nref = max(args.warmup, 3) + args.steps
+        ref.step(nref)
+        base = {f: ref.field(f) for f in ("u", "v", "p", "T", "rho")}
+        ref.close()
+        for name, prec in (("fp64_fast", sts.FAST_FP64), ("fp32_corrections", sts.MIXED)):
+            v = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=prec)
+            vd, vms, vsw = timed_steps(v, args.steps, args.warmup, flush, barrier)
+            err = {f: float(np.linalg.norm(v.field(f) - base[f]) / np.linalg.norm(base[f])) for f in base}
+            vpn, vkms, vkcnt = v.profile(max(3, min(args.steps, 10)))
+            variants[name] = {
+                "precision_mode": prec, "value": Na * vd * world / (vms / 1e3), "ms_per_step": vms / max(vd, 1),
+                "speedup_vs_fp64": (Na * vd / (vms / 1e3)) / (Na * done / (total_ms / 1e3)) if done else None,
+                "rel_l2_vs_fp64": err,
+                "sweeps_per_step": float(np.mean(vsw)) if len(vsw) else 0.0,
+                "gpu_launches": int(round(sum(launches_per_step(vkcnt, vpn, prec) + int(x) for x in vsw))),
+                "kernel_ms_per_step": {k: round(x / max(vpn, 1), 5) for k, x in vkms.items() if x > 0}}
+            v.close()
 
     if rank == 0:
         cpu = cpu_baseline(d, args.cpu_seconds, start_steps=0)
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": done,
                 "warmup": max(args.warmup, 3), "ms_per_step": total_ms / max(done, 1), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": config(case, s.Nx, s.Ny), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
-                "clocks": clk.summary(), "gpu_launches": launches,
+                "config": config(case, Nx, Ny), "roofline": roof, "cpu_baseline": cpu,
+                "e2e": e2e, "clocks": clk.summary(), "gpu_launches": launches,
                 "sweeps_per_step": {"mean": float(sum(sweeps) / max(len(sweeps), 1)),
-                                    "max": int(max(sweeps)) if len(sweeps) else 0}}
+                                    "max": int(max(sweeps)) if len(sweeps) else 0},
+                "variants": variants}
         print(json.dumps(line), flush=True)
-    s.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 

@@ -43,9 +43,16 @@ typedef struct sts_options {
   int device;
   /* 1: sts_run_case writes dumps and logs into the case directory like the reference. */
   int write_files;
+  /* 0: FP64, bit-exact with the reference (default).
+   * 1: FP64 with reciprocal multiplies and fused multiply-adds in the assembly and the
+   *    flux/diffusion kernels (a few ulps from the reference per step).
+   * 2: as 1, and the p-T sweeps of the tolerance-terminated loop run in FP32 on correction
+   *    fields over FP64 base fields; the sweep that meets the tolerance is recomputed in FP64,
+   *    so the stopping residual is an FP64 update.  Fixed sweep counts run as mode 1. */
+  int precision;
 } sts_options;
 
-/* Fills *opt with the defaults (fixed_sweeps 1, use_graph 1, device 0, write_files 1). */
+/* Fills *opt with the defaults (fixed_sweeps 1, use_graph 1, device 0, write_files 1, precision 0). */
 void sts_default_options(sts_options* opt);
 
 /* Reads a case directory (EnteredData.txt, solve_*_b.txt, restart dumps when
@@ -65,7 +72,8 @@ int sts_step_timed(sts_ctx* ctx, int nsteps, int* steps_done, double* device_ms)
 
 /* Runs up to nsteps steps kernel by kernel with an event pair around every launch and
  * returns per-kernel device time and launch counts, indexed 0 step_begin, 1 assemble,
- * 2 sweep, 3 correct, 4 face_rho, 5 boundary, 6 flux_diff, 7 step_end (8 entries each).
+ * 2 sweep (FP64), 3 correct, 4 face_rho, 5 boundary, 6 flux_diff, 7 step_end, 8 FP32 sweep
+ * and the FP64 re-forming of its iterate (precision 2) -- 9 entries each.
  * The steps are real: the state advances exactly as with sts_step. */
 int sts_profile_steps(sts_ctx* ctx, int nsteps, double* kernel_ms, int* kernel_launches, int* steps_done);
 

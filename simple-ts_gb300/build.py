@@ -19,6 +19,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
 UNITS = [
     # (source, extra flags)
     ("sts_exact.cu", ["--fmad=false"]),
+    ("sts_fast.cu", []),
     ("sts_runtime.cu", []),
     ("sts_host.cpp", []),
 ]

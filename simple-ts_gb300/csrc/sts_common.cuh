@@ -96,6 +96,12 @@ struct Ctl {
   // per-step record (ring of the last 4096 steps)
   unsigned int hist_n;
   unsigned int hist_sweeps[4096];
+  // mixed-precision sweep loop
+  unsigned int ecur;          // which correction buffer holds the current FP32 iterate
+  unsigned int base;          // FP64 buffer holding the base iterate of the FP32 corrections
+  unsigned int confirm_fail;  // FP64 re-evaluation of the last FP32 sweep missed the tolerance
+  unsigned int sweeps32;      // FP32 sweeps taken in this run (statistics)
+  unsigned int stop32;        // the FP32 loop of this outer iteration met the stop rule
 };
 
 // Everything a kernel needs: constant parameters and device pointers.
@@ -125,6 +131,17 @@ struct Geo {
   double *u_pseudo, *v_pseudo, *d12, *d34, *apx, *apy, *bpx, *bpy, *ScT1, *Tw_u, *Tw_v;
   double* inv[8];  // loop-invariant parts of the sweep, written by the first sweep of an outer iteration
   Ctl* ctl;
+  // --- mixed-precision path (precision mode 1 and 2) ---
+  // reciprocals of the mesh sums the assembly divides by (1/hx, 1/hy, 1/(hx[i-1]+hx[i]),
+  // 1/(hx[i]+hx[i+1]), the same in y), and 1/ht
+  const double *rhx, *rhy, *rxx_m, *rxx_p, *ryy_m, *ryy_p;
+  double rht;
+  // FP32 correction sweeps: coefficients c[0..4] of the T correction, a[0..3] of the p
+  // numerator, the base-sweep values T1, q, Den and the first defects dT, dp; e_p/e_T are the
+  // double-buffered corrections (index ectl)
+  float *c32[5], *a32[4], *T1, *q1, *den1, *dT, *dp;
+  float *ep[2], *eT[2];
+  int precision;  // 0 bit-exact FP64, 1 FP64 with reciprocal/FMA assembly, 2 = 1 + FP32 correction sweeps
 };
 
 // Neighbour indices of one cell: ij_function / ij_function_PeriodicBC (SIMPLE_TS_MPI.cpp:140-232).

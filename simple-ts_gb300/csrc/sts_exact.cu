@@ -16,86 +16,9 @@
 #include "sts_common.cuh"
 #include "sts_kernels.h"
 
+#include "sts_device.cuh"
+
 namespace sts {
-
-namespace {
-
-__device__ __forceinline__ double dmax0(double a, double b) { return a > b ? a : b; }
-__device__ __forceinline__ double upwind_rho(double r0, double r1, double v1) {
-  return (v1 == 0) ? (0.5 * (r0 + r1)) : ((v1 > 0) ? r0 : r1);
-}
-__device__ __forceinline__ double Li(double f1, double f2, double h1, double h2) {
-  return (f1 * h2 + f2 * h1) / (h1 + h2);
-}
-__device__ __forceinline__ double Hi(double f1, double f2, double h1, double h2) {
-  return (h1 + h2) * f1 * f2 / (h1 * f2 + h2 * f1);
-}
-__device__ __forceinline__ double as_d(unsigned long long b) { return __longlong_as_double((long long)b); }
-__device__ __forceinline__ unsigned long long as_b(double d) { return (unsigned long long)__double_as_longlong(d); }
-
-constexpr int kMaxColumn = 1024;  // rows staged in shared memory by the inflow-column reductions
-
-// Running maximum that ignores NaN exactly like "if (m < fabs(r)) m = fabs(r)".
-__device__ __forceinline__ double mx(double m, double x) { return (m < x) ? x : m; }
-
-// Block-wide max of two non-negative values, folded into global maxima by bit pattern
-// (for non-negative IEEE doubles the bit patterns order like the values).
-__device__ void block_max2(double a, double b, unsigned long long* ga, unsigned long long* gb, unsigned int* status) {
-  __shared__ double sa[32], sb[32];
-  const int lane = (threadIdx.x + threadIdx.y * blockDim.x) & 31;
-  const int warp = (threadIdx.x + threadIdx.y * blockDim.x) >> 5;
-  const int nw = (blockDim.x * blockDim.y + 31) >> 5;
-  if (!(a <= 1.7976931348623157e308) && a == a) atomicOr(status, 1u);  // +inf
-  if (a != a || b != b) atomicOr(status, 1u);                           // NaN
-  for (int o = 16; o > 0; o >>= 1) {
-    a = mx(a, __shfl_xor_sync(0xffffffffu, a, o));
-    b = mx(b, __shfl_xor_sync(0xffffffffu, b, o));
-  }
-  if (lane == 0) { sa[warp] = a; sb[warp] = b; }
-  __syncthreads();
-  if (warp == 0) {
-    a = lane < nw ? sa[lane] : 0.0;
-    b = lane < nw ? sb[lane] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) {
-      a = mx(a, __shfl_xor_sync(0xffffffffu, a, o));
-      b = mx(b, __shfl_xor_sync(0xffffffffu, b, o));
-    }
-    if (lane == 0) {
-      if (a > 0) atomicMax(ga, as_b(a));
-      if (b > 0) atomicMax(gb, as_b(b));
-    }
-  }
-}
-
-// True for exactly one thread in the grid: the last thread (0,0) of the last block to finish.
-__device__ bool last_block(unsigned int* counter) {
-  __shared__ bool last;
-  __syncthreads();
-  if (threadIdx.x == 0 && threadIdx.y == 0) {
-    __threadfence();
-    const unsigned int nb = gridDim.x * gridDim.y;
-    const unsigned int t = atomicAdd(counter, 1u);
-    last = (t == nb - 1);
-    if (last) *counter = 0;
-  }
-  __syncthreads();
-  return last && threadIdx.x == 0 && threadIdx.y == 0;
-}
-
-struct Cell {
-  int i, j, ij;
-  bool ok;
-};
-__device__ __forceinline__ Cell cell(const Geo& g) {
-  Cell c;
-  c.i = blockIdx.x * blockDim.x + threadIdx.x;
-  c.j = blockIdx.y * blockDim.y + threadIdx.y;
-  c.ok = c.i < g.Nx && c.j < g.Ny;
-  c.ij = c.i + c.j * g.Nx;
-  return c;
-}
-
-}  // namespace
 
 // ---------------------------------------------------------------------------
 // start of a time step: *_pr copies and per-step counters (SIMPLE_TS_MPI.cpp:3233-3260)
@@ -382,7 +305,11 @@ __device__ __forceinline__ void sweep_cell(const Geo& g, const Cell& c, const do
 template <bool FIRST>
 __device__ __forceinline__ void sweep_body(const Geo& g, unsigned long long h_sweep, int in_graph) {
   Ctl* ctl = g.ctl;
-  if (ctl->pt_done) return;  // the loop already stopped: launch is a no-op
+  if (ctl->pt_done) {  // the loop already stopped: the launch is a no-op
+    if (in_graph && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+      cudaGraphSetConditional((cudaGraphConditionalHandle)h_sweep, 0);
+    return;
+  }
   Cell c = cell(g);
   const unsigned cur = ctl->cur;
   double rp = 0, rT = 0;
@@ -416,6 +343,116 @@ __device__ __forceinline__ void sweep_body(const Geo& g, unsigned long long h_sw
 }
 
 __global__ void k_sweep_first(Geo g, unsigned long long h_sweep, int in_graph) { sweep_body<true>(g, h_sweep, in_graph); }
+
+// ---------------------------------------------------------------------------
+// Mixed-precision sweep loop (precision mode 2).  Within one outer iteration the Jacobi map
+// G is affine in the neighbour temperatures and pressures except for the 1/T_new term of
+// the pressure denominator.  Writing the iterate as x = b + e (b: FP64 base = the iterate
+// before the loop, e: FP32 correction), the first FP64 sweep gives x1 = G(b) and the defect
+// d = x1 - b; every later sweep is e' = d + (G(b + e) - G(b)), evaluated in FP32 from the
+// correction alone:
+//   dT  = sum_k c_k e_T,k + c_5 e_p,P               (c_k = ht aT_k / den_T, c_5 = ht (1-gamma) divu / den_T)
+//   e_T' = d_T + dT
+//   g   = H dT / (T1 (T1 + dT))                     (H = hx hy, T1 = T of x1)
+//   e_p' = d_p + (sum_k a_k e_p,k + q1 g) / (Den1 - g)  (a_k = ht apx/apy, q1 = p of x1, Den1 = sa + H/T1)
+// which is the exact difference of the two FP64 updates, so FP32 only rounds correction-sized
+// numbers.  When the FP32 loop meets the reference's stop rule at sweep n, the iterate of
+// sweep n-1 is formed in FP64 (b + e) and sweep n is recomputed with the exact FP64 kernel,
+// whose residual decides -- the stopping test always uses FP64 updates.
+// ---------------------------------------------------------------------------
+__global__ void k_sweep_first_mixed(Geo g, unsigned long long h_sweep, int in_graph) {
+  Ctl* ctl = g.ctl;
+  Cell c = cell(g);
+  const unsigned cur = ctl->cur;
+  const double* __restrict__ P = g.p[cur];
+  const double* __restrict__ TT = g.T[cur];
+  double* __restrict__ pn = g.p[cur ^ 1];
+  double* __restrict__ Tn = g.T[cur ^ 1];
+  double rp = 0, rT = 0;
+  if (c.ok) {
+    const int ij = c.ij;
+    const uint8_t cl = g.cls[ij];
+    sweep_cell<true>(g, c, P, TT, pn, Tn, rp, rT);
+    if (cls_o(cl)) {
+      const Nb d = neighbours(c.i, c.j, g.Nx, g.Ny, g.bits & F_PERIODIC);
+      const double ht = g.ht;
+      const double denT = g.inv[5][ij];
+      const double Tnew = Tn[ij], pnew = pn[ij];
+      const int nb[4] = {d.i_1j, d.i1j, d.ij_1, d.ij1};
+      for (int k = 0; k < 4; k++) {
+        // a wall neighbour's term is a constant and sits in the defect
+        const bool f = cls_o(cl) == CLS_NCH || cls_fluid(g.cls[nb[k]]);
+        g.c32[k][ij] = f ? (float)(ht * g.inv[k][ij] / denT) : 0.0f;
+      }
+      g.c32[4][ij] = (float)(ht * (1.0 - g.gamma1) * g.inv[4][ij] / denT);
+      g.a32[0][ij] = (float)(ht * g.apx[d.ij]);
+      g.a32[1][ij] = (float)(ht * g.apx[d.i1j]);
+      g.a32[2][ij] = (float)(ht * g.apy[d.ij]);
+      g.a32[3][ij] = (float)(ht * g.apy[d.ij1]);
+      g.T1[ij] = (float)Tnew;
+      g.q1[ij] = (float)pnew;
+      g.den1[ij] = (float)(g.inv[7][ij] + g.hx[c.i] * g.hy[c.j] / Tnew);
+      const float dT = (float)(Tnew - TT[ij]), dp = (float)(pnew - P[ij]);
+      g.dT[ij] = dT;
+      g.dp[ij] = dp;
+      g.eT[0][ij] = dT;
+      g.ep[0][ij] = dp;
+    } else {
+      g.dT[ij] = 0.0f;
+      g.dp[ij] = 0.0f;
+      g.eT[0][ij] = 0.0f;
+      g.ep[0][ij] = 0.0f;
+      g.eT[1][ij] = 0.0f;
+      g.ep[1][ij] = 0.0f;
+    }
+  }
+  block_max2(rp, rT, &ctl->res_bits_p, &ctl->res_bits_T, &ctl->status);
+  if (last_block(&ctl->block_count)) {
+    const unsigned I = ctl->Iter < 64 ? ctl->Iter : 63;
+    const double res_p = as_d(atomicExch(&ctl->res_bits_p, 0ull));
+    const double res_T = as_d(atomicExch(&ctl->res_bits_T, 0ull));
+    ctl->res_p[I] = res_p;
+    ctl->res_T[I] = res_T;
+    ctl->res_p0[I] = res_p;
+    ctl->res_T0[I] = res_T;
+    const unsigned n = ++ctl->Iter_p_c;
+    ctl->ecur = 0;
+    ctl->base = cur;
+    ctl->stop32 = 0;
+    const bool cont = n < (unsigned)g.N_I_p_c;  // the stop rule needs two sweeps at least
+    if (!cont) {  // a single sweep was asked for: x1 is the result
+      ctl->cur = cur ^ 1;
+      ctl->pt_done = 1;
+      ctl->sweeps[I] = n;
+      ctl->step_sweeps += n;
+    }
+    if (in_graph) cudaGraphSetConditional((cudaGraphConditionalHandle)h_sweep, cont ? 1 : 0);
+  }
+}
+
+// Forms the FP64 iterate b + e of the sweep before the last FP32 one in the second FP64 buffer
+// and rewinds the sweep counter by one, so that the exact k_sweep that follows recomputes the
+// last sweep in FP64 and applies the stop rule to FP64 updates.
+__global__ void k_materialize(Geo g, unsigned long long h_confirm, int in_graph) {
+  Ctl* ctl = g.ctl;
+  const bool done = ctl->pt_done;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    if (in_graph && done) cudaGraphSetConditional((cudaGraphConditionalHandle)h_confirm, 0);
+  }
+  if (done) return;
+  Cell c = cell(g);
+  const unsigned b = ctl->base, src = ctl->ecur ^ 1;
+  if (c.ok) {
+    g.p[b ^ 1][c.ij] = g.p[b][c.ij] + (double)g.ep[src][c.ij];
+    g.T[b ^ 1][c.ij] = g.T[b][c.ij] + (double)g.eT[src][c.ij];
+  }
+  if (last_block(&ctl->block_count)) {
+    ctl->cur = b ^ 1;
+    ctl->Iter_p_c -= 1;
+    ctl->pt_done = 0;
+    ctl->stop32 = 0;
+  }
+}
 __global__ void k_sweep(Geo g, unsigned long long h_sweep, int in_graph) { sweep_body<false>(g, h_sweep, in_graph); }
 
 // ---------------------------------------------------------------------------
@@ -470,9 +507,8 @@ __global__ void k_face_rho(Geo g) {
 }
 
 // SolveFluxes (SIMPLE_TS_MPI.cpp:10440-10454) and SolveDiffisionTerms (:10457-10618)
-__global__ void k_flux_diff(Geo g) {
-  Cell c = cell(g);
-  if (!c.ok) return;
+
+__device__ __forceinline__ void flux_diff_cell(const Geo& g, const Cell& c) {
   const int i = c.i, j = c.j;
   const Nb d = neighbours(i, j, g.Nx, g.Ny, g.bits & F_PERIODIC);
   const double* __restrict__ hx = g.hx;
@@ -529,6 +565,20 @@ __global__ void k_flux_diff(Geo g) {
     g.DTy[d.ij] = 0;
 }
 
+// The zero-gradient temperature and pressure copies (phases `tail`) touch only ghost cells of p
+// and T, which the fluxes and diffusion terms do not read, so the first CTA does them too.
+__global__ void k_flux_diff(Geo g, unsigned tail) {
+  Cell c = cell(g);
+  if (c.ok) flux_diff_cell(g, c);
+  if (tail && blockIdx.x == 0 && blockIdx.y == 0) {
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x, nt = blockDim.x * blockDim.y;
+    const unsigned cur = g.ctl->cur;
+    if (tail & PH_TEMP) phase_temp(g, g.T[cur], tid, nt);
+    __syncthreads();
+    if (tail & PH_PRES) phase_pres(g, g.p[cur], tid, nt);
+  }
+}
+
 // ApplyBodiesConditionsToVariables on the device (SIMPLE_TS_MPI.cpp:6470-6584): a face takes the
 // velocity of the body it belongs to, or of the body on its low side; body cells take p, T and rho = 0.
 __global__ void k_apply_bodies(Geo g) {
@@ -561,9 +611,147 @@ __global__ void k_sqrt_rho(Geo g, int do_rho) {
 }
 
 // ---------------------------------------------------------------------------
-// Boundary work of one outer iteration, in the reference's order, in a single CTA
-// (the lists are O(perimeter)).  `phases` selects the parts (PH_* in sts_kernels.h).
+// Boundary work, in the reference's order.  The wall lists are O(perimeter) but carry FP64
+// divisions, so they run over the whole grid (k_bnd_walls, k_bnd_tjump); the short column
+// and row copies run in one CTA (k_boundary) or in the first CTA of k_flux_diff.
 // ---------------------------------------------------------------------------
+// loop control after the velocity correction: SIMPLE_TS_MPI.cpp:4347-4361 (coefficients), :4406-4450
+__device__ void do_control(const Geo& g, unsigned long long h_outer, int in_graph) {
+  Ctl* ctl = g.ctl;
+  const int TypeND = g.TypeND;
+  if (TypeND == 1 || TypeND == 2) {
+    ctl->cT = (1.0 / g.Re) * (ctl->u_given_xb_in_it * ctl->p_BC_xb / g.T_BC_xb);
+    ctl->cPch = (TypeND == 1) ? 0.5 : ctl->u_given_xb_in_it * ctl->u_given_xb_in_it / (g.gamma1 * g.Ma * g.Ma);
+  }
+  const double ru = as_d(ctl->res_bits_u), rv = as_d(ctl->res_bits_v);
+  ctl->res_u = ru;
+  ctl->res_v = rv;
+  const unsigned It = ++ctl->Iter;
+  if (It == 1) {
+    ctl->res_u0 = ru;
+    ctl->res_v0 = rv;
+  }
+  const unsigned I = (It - 1) < 64 ? It - 1 : 63;
+  const double rpI = ctl->res_p[I], rTI = ctl->res_T[I];
+  const bool ci = (It < (unsigned)g.N_I) &&
+                  (g.MaxError_Velocities < ru || g.MaxError_Velocities < rv || g.MaxError_p_c < rpI || g.MaxError_T < rTI);
+  const double stop = g.MaxError_to_stop_program;
+  const bool cs = ((double)ctl->it_counter < g.Nt) &&
+                  ((!(It <= 1 && ctl->Iter_p_c <= 2)) || stop < ru || stop < rv || stop < ctl->res_p0[I] ||
+                   stop < ctl->res_T0[I]);
+  ctl->continue_iter = ci;
+  ctl->continue_step = cs;
+  if (in_graph) cudaGraphSetConditional((cudaGraphConditionalHandle)h_outer, ci ? 1 : 0);
+}
+
+// BoundaryConditions_Velocities_SlipBC_u (SIMPLE_TS_MPI.cpp:7098-7213), entry k; an entry performs
+// only the writes that survive in the reference's sequential order (host-side analysis).
+__device__ void do_slip_u(const Geo& g, int k) {
+  const int Nx = g.Nx, Ny = g.Ny;
+  const bool per = g.bits & F_PERIODIC;
+  double* __restrict__ u = g.u;
+  auto fl = [&](int q) { return cls_fluid(g.cls[q]); };
+  const uint64_t bits = g.bits;
+  const bool kl = bits & F_KN_LOCAL;
+
+  const int node = g.slip_u[k];
+  const uint8_t fin = g.slip_u_fin[k];
+  const int j = node / Nx, i = node - j * Nx;
+  const Nb d = neighbours(i, j, Nx, Ny, per);
+  const Body& Bd = g.bodies[g.vol_id[d.ij] - 1];
+  const double FK = Bd.F_slip * g.Kn;
+  if (g.vol_id[d.ij_1] == 0) {
+    const int jm = j - (0 < j ? 1 : 0);
+    const double a_ij = kl ? FK / (g.rho_u[d.ij_1] * 0.5 * g.hy[jm]) : FK / (0.5 * g.hy[jm]);
+    const double a_i1j = kl ? FK / (g.rho_u[d.i1j_1] * 0.5 * g.hy[jm]) : FK / (0.5 * g.hy[jm]);
+    if ((fin & 1) && fl(d.i_1j_1)) u[d.ij] = (u[d.ij_1] * a_ij + Bd.u) / (1.0 + a_ij);
+    if ((fin & 2) && fl(d.i1j_1)) u[d.i1j] = (u[d.i1j_1] * a_i1j + Bd.u) / (1.0 + a_i1j);
+  } else {
+    const int jp = j + (j < (Ny - 1) ? 1 : 0);
+    const double a_ij = kl ? FK / (g.rho_u[d.ij1] * 0.5 * g.hy[jp]) : FK / (0.5 * g.hy[jp]);
+    const double a_i1j = kl ? FK / (g.rho_u[d.i1j1] * 0.5 * g.hy[jp]) : FK / (0.5 * g.hy[jp]);
+    if ((fin & 1) && fl(d.i_1j1)) u[d.ij] = (u[d.ij1] * a_ij + Bd.u) / (1.0 + a_ij);
+    if ((fin & 2) && fl(d.i1j1)) u[d.i1j] = (u[d.i1j1] * a_i1j + Bd.u) / (1.0 + a_i1j);
+  }
+}
+
+// BoundaryConditions_Velocities_SlipBC_v (SIMPLE_TS_MPI.cpp:7216-7331), entry k
+__device__ void do_slip_v(const Geo& g, int k) {
+  const int Nx = g.Nx, Ny = g.Ny;
+  const bool per = g.bits & F_PERIODIC;
+  double* __restrict__ v = g.v;
+  auto fl = [&](int q) { return cls_fluid(g.cls[q]); };
+  const uint64_t bits = g.bits;
+  const bool kl = bits & F_KN_LOCAL;
+
+  const int node = g.slip_v[k];
+  const uint8_t fin = g.slip_v_fin[k];
+  const int j = node / Nx, i = node - j * Nx;
+  const Nb d = neighbours(i, j, Nx, Ny, per);
+  const Body& Bd = g.bodies[g.vol_id[d.ij] - 1];
+  const double FK = Bd.F_slip * g.Kn;
+  if (g.vol_id[d.i_1j] == 0) {
+    const double a_ij = kl ? FK / (g.rho_v[d.i_1j] * 0.5 * g.hx[d.i_1]) : FK / (0.5 * g.hx[d.i_1]);
+    const double a_ij1 = kl ? FK / (g.rho_v[d.i_1j1] * 0.5 * g.hx[d.i_1]) : FK / (0.5 * g.hx[d.i_1]);
+    if ((fin & 1) && fl(d.i_1j_1)) v[d.ij] = (v[d.i_1j] * a_ij + Bd.v) / (1.0 + a_ij);
+    if ((fin & 2) && fl(d.i_1j1)) v[d.ij1] = (v[d.i_1j1] * a_ij1 + Bd.v) / (1.0 + a_ij1);
+  } else {
+    const double a_ij = kl ? FK / (g.rho_v[d.i1j] * 0.5 * g.hx[d.i1]) : FK / (0.5 * g.hx[d.i1]);
+    const double a_ij1 = kl ? FK / (g.rho_v[d.i1j1] * 0.5 * g.hx[d.i1]) : FK / (0.5 * g.hx[d.i1]);
+    if ((fin & 1) && fl(d.i1j_1)) v[d.ij] = (v[d.i1j] * a_ij + Bd.v) / (1.0 + a_ij);
+    if ((fin & 2) && fl(d.i1j1)) v[d.ij1] = (v[d.i1j1] * a_ij1 + Bd.v) / (1.0 + a_ij1);
+  }
+}
+
+// BoundaryConditions_Temperature_TemperatureJumpBC (SIMPLE_TS_MPI.cpp:7744-8045), entry k
+__device__ void do_tjump(const Geo& g, const double* __restrict__ T, int k) {
+  const int Nx = g.Nx, Ny = g.Ny;
+  const bool per = g.bits & F_PERIODIC;
+  auto fl = [&](int q) { return cls_fluid(g.cls[q]); };
+  const uint64_t bits = g.bits;
+  const bool kl = bits & F_KN_LOCAL;
+
+  const int node = g.tjump[k];
+  const uint8_t fin = g.tjump_fin[k];
+  const int j = node / Nx, i = node - j * Nx;
+  const Nb d = neighbours(i, j, Nx, Ny, per);
+  const int nb[4] = {d.i_1j, d.i1j, d.ij_1, d.ij1};
+  const int dst[4] = {d.ij, d.i1j, d.ij, d.ij1};
+  for (int q = 0; q < 4; q++) {
+    if (fl(nb[q]) || !(fin & (1 << q))) continue;
+    const Body& Bd = g.bodies[g.vol_id[nb[q]] - 1];
+    double* out = (q < 2) ? g.Tw_u : g.Tw_v;
+    double val;
+    if (Bd.jump) {
+      const double FK = kl ? (Bd.F_jump * g.Kn) / g.rho[d.ij] : Bd.F_jump * g.Kn;
+      const double a = FK / (0.5 * ((q < 2) ? g.hx[i] : g.hy[j]));
+      val = (a * T[d.ij] + Bd.T) / (1.0 + a);
+    } else if (Bd.dTdn0 != 0) {
+      val = T[d.ij];
+    } else {
+      val = Bd.T;
+    }
+    out[dst[q]] = val;
+  }
+}
+
+// ..._TemperatureJumpBC_WriteToMassiveToWriteDataToFile (SIMPLE_TS_MPI.cpp:8048-8099), entry k
+__device__ void do_tjump_write(const Geo& g, double* __restrict__ T, int k) {
+  const int Nx = g.Nx, Ny = g.Ny;
+  const bool per = g.bits & F_PERIODIC;
+  auto fl = [&](int q) { return cls_fluid(g.cls[q]); };
+
+  const int node = g.tjump[k];
+  const uint8_t fin = g.tjump_wr_fin[k];
+  const int j = node / Nx, i = node - j * Nx;
+  const Nb d = neighbours(i, j, Nx, Ny, per);
+  if ((fin & 1) && !fl(d.i_1j)) T[d.i_1j] = g.Tw_u[d.ij];
+  if ((fin & 2) && !fl(d.i1j)) T[d.i1j] = g.Tw_u[d.i1j];
+  if ((fin & 4) && !fl(d.ij_1)) T[d.ij_1] = g.Tw_v[d.ij];
+  if ((fin & 8) && !fl(d.ij1)) T[d.ij1] = g.Tw_v[d.ij1];
+}
+
+// Single-CTA boundary work; `phases` selects the parts (PH_* in sts_kernels.h).
 __global__ void __launch_bounds__(1024) k_boundary(Geo g, unsigned phases, unsigned long long h_outer, int in_graph) {
   Ctl* ctl = g.ctl;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -577,88 +765,15 @@ __global__ void __launch_bounds__(1024) k_boundary(Geo g, unsigned phases, unsig
   auto fl = [&](int k) { return cls_fluid(g.cls[k]); };
   const uint64_t bits = g.bits;
 
-  if (phases & PH_CONTROL) {
-    // SIMPLE_TS_MPI.cpp:4347-4361 (coefficients) and :4406-4450 (loop control)
-    if (tid == 0) {
-      const int TypeND = g.TypeND;
-      if (TypeND == 1 || TypeND == 2) {
-        ctl->cT = (1.0 / g.Re) * (ctl->u_given_xb_in_it * ctl->p_BC_xb / g.T_BC_xb);
-        ctl->cPch = (TypeND == 1) ? 0.5 : ctl->u_given_xb_in_it * ctl->u_given_xb_in_it / (g.gamma1 * g.Ma * g.Ma);
-      }
-      const double ru = as_d(ctl->res_bits_u), rv = as_d(ctl->res_bits_v);
-      ctl->res_u = ru;
-      ctl->res_v = rv;
-      const unsigned It = ++ctl->Iter;
-      if (It == 1) {
-        ctl->res_u0 = ru;
-        ctl->res_v0 = rv;
-      }
-      const unsigned I = (It - 1) < 64 ? It - 1 : 63;
-      const double rpI = ctl->res_p[I], rTI = ctl->res_T[I];
-      const bool ci = (It < (unsigned)g.N_I) &&
-                      (g.MaxError_Velocities < ru || g.MaxError_Velocities < rv || g.MaxError_p_c < rpI || g.MaxError_T < rTI);
-      const double stop = g.MaxError_to_stop_program;
-      const bool cs = ((double)ctl->it_counter < g.Nt) &&
-                      ((!(It <= 1 && ctl->Iter_p_c <= 2)) || stop < ru || stop < rv || stop < ctl->res_p0[I] ||
-                       stop < ctl->res_T0[I]);
-      ctl->continue_iter = ci;
-      ctl->continue_step = cs;
-      if (in_graph) cudaGraphSetConditional((cudaGraphConditionalHandle)h_outer, ci ? 1 : 0);
-    }
-  }
+  if ((phases & PH_CONTROL) && tid == 0) do_control(g, h_outer, in_graph);
   __syncthreads();
 
-  // BoundaryConditions_Velocities_SlipBC_u (SIMPLE_TS_MPI.cpp:7098-7213); every entry performs
-  // only the writes that survive in the reference's sequential order (host-side analysis).
-  if (phases & PH_SLIP_U) {
-    const bool kl = bits & F_KN_LOCAL;
-    for (int k = tid; k < g.n_slip_u; k += nt) {
-      const int node = g.slip_u[k];
-      const uint8_t fin = g.slip_u_fin[k];
-      const int j = node / Nx, i = node - j * Nx;
-      const Nb d = neighbours(i, j, Nx, Ny, per);
-      const Body& Bd = g.bodies[g.vol_id[d.ij] - 1];
-      const double FK = Bd.F_slip * g.Kn;
-      if (g.vol_id[d.ij_1] == 0) {
-        const int jm = j - (0 < j ? 1 : 0);
-        const double a_ij = kl ? FK / (g.rho_u[d.ij_1] * 0.5 * g.hy[jm]) : FK / (0.5 * g.hy[jm]);
-        const double a_i1j = kl ? FK / (g.rho_u[d.i1j_1] * 0.5 * g.hy[jm]) : FK / (0.5 * g.hy[jm]);
-        if ((fin & 1) && fl(d.i_1j_1)) u[d.ij] = (u[d.ij_1] * a_ij + Bd.u) / (1.0 + a_ij);
-        if ((fin & 2) && fl(d.i1j_1)) u[d.i1j] = (u[d.i1j_1] * a_i1j + Bd.u) / (1.0 + a_i1j);
-      } else {
-        const int jp = j + (j < (Ny - 1) ? 1 : 0);
-        const double a_ij = kl ? FK / (g.rho_u[d.ij1] * 0.5 * g.hy[jp]) : FK / (0.5 * g.hy[jp]);
-        const double a_i1j = kl ? FK / (g.rho_u[d.i1j1] * 0.5 * g.hy[jp]) : FK / (0.5 * g.hy[jp]);
-        if ((fin & 1) && fl(d.i_1j1)) u[d.ij] = (u[d.ij1] * a_ij + Bd.u) / (1.0 + a_ij);
-        if ((fin & 2) && fl(d.i1j1)) u[d.i1j] = (u[d.i1j1] * a_i1j + Bd.u) / (1.0 + a_i1j);
-      }
-    }
-  }
+  if (phases & PH_SLIP_U)
+    for (int k = tid; k < g.n_slip_u; k += nt) do_slip_u(g, k);
   __syncthreads();
 
-  // BoundaryConditions_Velocities_SlipBC_v (SIMPLE_TS_MPI.cpp:7216-7331)
-  if (phases & PH_SLIP_V) {
-    const bool kl = bits & F_KN_LOCAL;
-    for (int k = tid; k < g.n_slip_v; k += nt) {
-      const int node = g.slip_v[k];
-      const uint8_t fin = g.slip_v_fin[k];
-      const int j = node / Nx, i = node - j * Nx;
-      const Nb d = neighbours(i, j, Nx, Ny, per);
-      const Body& Bd = g.bodies[g.vol_id[d.ij] - 1];
-      const double FK = Bd.F_slip * g.Kn;
-      if (g.vol_id[d.i_1j] == 0) {
-        const double a_ij = kl ? FK / (g.rho_v[d.i_1j] * 0.5 * g.hx[d.i_1]) : FK / (0.5 * g.hx[d.i_1]);
-        const double a_ij1 = kl ? FK / (g.rho_v[d.i_1j1] * 0.5 * g.hx[d.i_1]) : FK / (0.5 * g.hx[d.i_1]);
-        if ((fin & 1) && fl(d.i_1j_1)) v[d.ij] = (v[d.i_1j] * a_ij + Bd.v) / (1.0 + a_ij);
-        if ((fin & 2) && fl(d.i_1j1)) v[d.ij1] = (v[d.i_1j1] * a_ij1 + Bd.v) / (1.0 + a_ij1);
-      } else {
-        const double a_ij = kl ? FK / (g.rho_v[d.i1j] * 0.5 * g.hx[d.i1]) : FK / (0.5 * g.hx[d.i1]);
-        const double a_ij1 = kl ? FK / (g.rho_v[d.i1j1] * 0.5 * g.hx[d.i1]) : FK / (0.5 * g.hx[d.i1]);
-        if ((fin & 1) && fl(d.i1j_1)) v[d.ij] = (v[d.i1j] * a_ij + Bd.v) / (1.0 + a_ij);
-        if ((fin & 2) && fl(d.i1j1)) v[d.ij1] = (v[d.i1j1] * a_ij1 + Bd.v) / (1.0 + a_ij1);
-      }
-    }
-  }
+  if (phases & PH_SLIP_V)
+    for (int k = tid; k < g.n_slip_v; k += nt) do_slip_v(g, k);
   __syncthreads();
 
   // BoundaryConditions_Velocities (SIMPLE_TS_MPI.cpp:6790-7096), each loop a phase
@@ -882,119 +997,36 @@ __global__ void __launch_bounds__(1024) k_boundary(Geo g, unsigned phases, unsig
   }
   __syncthreads();
 
-  // BoundaryConditions_Temperature_TemperatureJumpBC (SIMPLE_TS_MPI.cpp:7744-8045)
-  if (phases & (PH_TJUMP | PH_TJUMP_WRITE)) {
-    const bool kl = bits & F_KN_LOCAL;
-    for (int k = tid; k < g.n_tjump; k += nt) {
-      const int node = g.tjump[k];
-      const uint8_t fin = g.tjump_fin[k];
-      const int j = node / Nx, i = node - j * Nx;
-      const Nb d = neighbours(i, j, Nx, Ny, per);
-      const int nb[4] = {d.i_1j, d.i1j, d.ij_1, d.ij1};
-      const int dst[4] = {d.ij, d.i1j, d.ij, d.ij1};
-      for (int q = 0; q < 4; q++) {
-        if (fl(nb[q]) || !(fin & (1 << q))) continue;
-        const Body& Bd = g.bodies[g.vol_id[nb[q]] - 1];
-        double* out = (q < 2) ? g.Tw_u : g.Tw_v;
-        double val;
-        if (Bd.jump) {
-          const double FK = kl ? (Bd.F_jump * g.Kn) / g.rho[d.ij] : Bd.F_jump * g.Kn;
-          const double a = FK / (0.5 * ((q < 2) ? g.hx[i] : g.hy[j]));
-          val = (a * T[d.ij] + Bd.T) / (1.0 + a);
-        } else if (Bd.dTdn0 != 0) {
-          val = T[d.ij];
-        } else {
-          val = Bd.T;
-        }
-        out[dst[q]] = val;
-      }
-    }
-  }
+  if (phases & (PH_TJUMP | PH_TJUMP_WRITE))
+    for (int k = tid; k < g.n_tjump; k += nt) do_tjump(g, T, k);
   __syncthreads();
 
-  // BoundaryConditions_Temperature_TemperatureJumpBC_WriteToMassiveToWriteDataToFile (:8048-8099)
-  if (phases & PH_TJUMP_WRITE) {
-    for (int k = tid; k < g.n_tjump; k += nt) {
-      const int node = g.tjump[k];
-      const uint8_t fin = g.tjump_wr_fin[k];
-      const int j = node / Nx, i = node - j * Nx;
-      const Nb d = neighbours(i, j, Nx, Ny, per);
-      if ((fin & 1) && !fl(d.i_1j)) T[d.i_1j] = g.Tw_u[d.ij];
-      if ((fin & 2) && !fl(d.i1j)) T[d.i1j] = g.Tw_u[d.i1j];
-      if ((fin & 4) && !fl(d.ij_1)) T[d.ij_1] = g.Tw_v[d.ij];
-      if ((fin & 8) && !fl(d.ij1)) T[d.ij1] = g.Tw_v[d.ij1];
-    }
-  }
+  if (phases & PH_TJUMP_WRITE)
+    for (int k = tid; k < g.n_tjump; k += nt) do_tjump_write(g, T, k);
   __syncthreads();
 
-  // BoundaryConditions_Temperature (SIMPLE_TS_MPI.cpp:7650-7741)
-  if ((phases & PH_TEMP) && !per) {
-    if (bits & F_DTDX0_XB) {
-      for (int k = tid; k < Ny * g.Nx_o0; k += nt) {
-        const int j = k / g.Nx_o0, i = k - j * g.Nx_o0, n = g.Nx_o0 + j * Nx;
-        if (fl(n)) T[i + j * Nx] = T[n];
-      }
-      __syncthreads();
-    }
-    if (bits & F_DTDX0_XE) {
-      const int w = Nx - g.Nx_o1;
-      for (int k = tid; k < Ny * w; k += nt) {
-        const int j = k / w, i = g.Nx_o1 + (k - j * w), n = g.Nx_o1 - 1 + j * Nx;
-        if (fl(n)) T[i + j * Nx] = T[n];
-      }
-      __syncthreads();
-    }
-    if (bits & F_DTDY0_YB) {
-      for (int k = tid; k < Nx * g.Ny_o0; k += nt) {
-        const int jj = k / Nx, i = k - jj * Nx, n = i + g.Ny_o0 * Nx;
-        if (fl(n)) T[i + jj * Nx] = T[n];
-      }
-      __syncthreads();
-    }
-    if (bits & F_DTDY0_YE) {
-      const int w = Ny - g.Ny_o1;
-      for (int k = tid; k < Nx * w; k += nt) {
-        const int jj = k / Nx, i = k - jj * Nx, n = i + (g.Ny_o1 - 1) * Nx;
-        if (fl(n)) T[i + (g.Ny_o1 + jj) * Nx] = T[n];
-      }
-      __syncthreads();
-    }
-  }
+  if (phases & PH_TEMP) phase_temp(g, T, tid, nt);
   __syncthreads();
 
-  // BoundaryConditions_Pressure (SIMPLE_TS_MPI.cpp:7335-7428)
-  if ((phases & PH_PRES) && !per) {
-    if (bits & F_DPDX0_XB) {
-      for (int k = tid; k < Ny * g.Nx_o0; k += nt) {
-        const int j = k / g.Nx_o0, i = k - j * g.Nx_o0, n = g.Nx_o0 + j * Nx;
-        if (fl(n)) p[i + j * Nx] = p[n];
-      }
-      __syncthreads();
-    }
-    if (bits & F_DPDX0_XE) {
-      const int w = Nx - g.Nx_o1;
-      for (int k = tid; k < Ny * w; k += nt) {
-        const int j = k / w, i = g.Nx_o1 + (k - j * w), n = g.Nx_o1 - 1 + j * Nx;
-        if (fl(n)) p[i + j * Nx] = p[n];
-      }
-      __syncthreads();
-    }
-    if (bits & F_DPDY0_YB) {
-      for (int k = tid; k < Nx * g.Ny_o0; k += nt) {
-        const int jj = k / Nx, i = k - jj * Nx, n = i + g.Ny_o0 * Nx;
-        if (fl(n)) p[i + jj * Nx] = p[n];
-      }
-      __syncthreads();
-    }
-    if (bits & F_DPDY0_YE) {
-      const int w = Ny - g.Ny_o1;
-      for (int k = tid; k < Nx * w; k += nt) {
-        const int jj = k / Nx, i = k - jj * Nx, n = i + (g.Ny_o1 - 1) * Nx;
-        if (fl(n)) p[i + (g.Ny_o1 + jj) * Nx] = p[n];
-      }
-      __syncthreads();
-    }
-  }
+  if (phases & PH_PRES) phase_pres(g, p, tid, nt);
+}
+
+// Wall lists over the whole grid: loop control (one thread), slip u and slip v (independent:
+// they write u and v respectively).
+__global__ void k_bnd_walls(Geo g, unsigned phases, unsigned long long h_outer, int in_graph) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+  if ((phases & PH_CONTROL) && t == 0) do_control(g, h_outer, in_graph);
+  if (phases & PH_SLIP_U)
+    for (int k = t; k < g.n_slip_u; k += nt) do_slip_u(g, k);
+  if (phases & PH_SLIP_V)
+    for (int k = t; k < g.n_slip_v; k += nt) do_slip_v(g, k);
+}
+
+// Temperature-jump wall values over the whole grid.
+__global__ void k_bnd_tjump(Geo g) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+  const double* T = g.T[g.ctl->cur];
+  for (int k = t; k < g.n_tjump; k += nt) do_tjump(g, T, k);
 }
 
 // End of a time step: time-dependent inflow (SIMPLE_TS_MPI.cpp:8102-8144), per-step

@@ -26,9 +26,17 @@ __global__ void k_apply_bodies(Geo g);
 __global__ void k_assemble(Geo g, unsigned long long h_sweep, int in_graph);
 __global__ void k_sweep_first(Geo g, unsigned long long h_sweep, int in_graph);
 __global__ void k_sweep(Geo g, unsigned long long h_sweep, int in_graph);
+// mixed precision (precision modes 1, 2)
+__global__ void k_assemble_fast(Geo g, unsigned long long h_sweep, int in_graph);
+__global__ void k_flux_diff_fast(Geo g, unsigned tail);
+__global__ void k_sweep_first_mixed(Geo g, unsigned long long h_sweep, int in_graph);
+__global__ void k_sweep32(Geo g, unsigned long long h_sweep, int in_graph);
+__global__ void k_materialize(Geo g, unsigned long long h_confirm, int in_graph);
 __global__ void k_correct(Geo g);
 __global__ void k_face_rho(Geo g);
-__global__ void k_flux_diff(Geo g);
+__global__ void k_flux_diff(Geo g, unsigned tail);
+__global__ void k_bnd_walls(Geo g, unsigned phases, unsigned long long h_outer, int in_graph);
+__global__ void k_bnd_tjump(Geo g);
 __global__ void k_sqrt_rho(Geo g, int do_rho);
 __global__ void k_boundary(Geo g, unsigned phases, unsigned long long h_outer, int in_graph);
 __global__ void k_step_end(Geo g, unsigned long long h_step, int in_graph);

@@ -40,6 +40,9 @@ int fail(int code, const std::string& msg) {
       return fail(STS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));    \
   } while (0)
 
+// kernel kinds reported by sts_profile_steps
+constexpr int kProfileKinds = 9;
+
 }  // namespace
 
 struct sts_ctx {
@@ -92,6 +95,62 @@ struct sts_ctx {
   }
   // launches
   void boundary(unsigned ph) { k_boundary<<<1, 1024, 0, s>>>(g, ph, 0, 0); }
+  dim3 walls_grid() const {
+    const int n = g.n_slip_u + g.n_slip_v;
+    return dim3((unsigned)std::max(1, std::min((n + 255) / 256, 1024)));
+  }
+  dim3 tjump_grid() const { return dim3((unsigned)std::max(1, std::min((g.n_tjump + 255) / 256, 1024))); }
+  // boundary work and fluxes/diffusion of one outer iteration outside the graph; `mark`
+  // (optional) brackets the launches for the per-kernel profile
+  template <class M>
+  void boundary_step(M mark) {
+    mark(-1);
+    k_bnd_walls<<<walls_grid(), 256, 0, s>>>(g, PH_CONTROL | PH_SLIP_U | PH_SLIP_V, 0, 0);
+    k_boundary<<<1, 1024, 0, s>>>(g, PH_VEL | PH_PBEGIN, 0, 0);
+    k_bnd_tjump<<<tjump_grid(), 256, 0, s>>>(g);
+    mark(5);
+    mark(-1);
+    if (fast()) k_flux_diff_fast<<<grid, block, 0, s>>>(g, PH_TEMP | PH_PRES);
+    else k_flux_diff<<<grid, block, 0, s>>>(g, PH_TEMP | PH_PRES);
+    mark(6);
+  }
+  bool fast() const { return g.precision >= 1; }
+  bool mixed() const { return g.precision == 2 && !(hc.bits & F_FIXED_SWEEPS); }
+  // The sweep loop of one outer iteration outside the graph.  The device decides every stop;
+  // the host launches sweeps in batches (one at a time when profiling) and checks after each
+  // batch whether the loop has stopped.  `mark` brackets launches for the per-kernel profile.
+  template <class M>
+  int sweep_loop(M mark, int batch) {
+    const bool fixed = hc.bits & F_FIXED_SWEEPS;
+    const int Npc = (int)hc.cfg.n("N_I_p_c");
+    int launched = 1;
+    if (mixed()) {
+      mark(-1); k_sweep_first_mixed<<<grid, block, 0, s>>>(g, 0, 0); mark(2);
+      for (;;) {
+        if (int r = read_ctl()) return r;
+        if (h_ctl->pt_done || h_ctl->stop32 || launched >= Npc) break;
+        for (int q = 0; q < batch && launched < Npc; q++, launched++) {
+          mark(-1); k_sweep32<<<grid, block, 0, s>>>(g, 0, 0); mark(8);
+        }
+      }
+      mark(-1); k_materialize<<<grid, block, 0, s>>>(g, 0, 0); mark(8);
+      launched = (int)h_ctl->Iter_p_c - 1;  // the FP64 sweep that follows recomputes the last one
+    } else {
+      mark(-1); k_sweep_first<<<grid, block, 0, s>>>(g, 0, 0); mark(2);
+      if (fixed) {
+        for (int q = 1; q < Npc; q++) { mark(-1); k_sweep<<<grid, block, 0, s>>>(g, 0, 0); mark(2); }
+        return STS_OK;
+      }
+    }
+    for (;;) {
+      for (int q = 0; q < batch && launched < Npc; q++, launched++) {
+        mark(-1); k_sweep<<<grid, block, 0, s>>>(g, 0, 0); mark(2);
+      }
+      if (int r = read_ctl()) return r;
+      if (h_ctl->pt_done || launched >= Npc) break;
+    }
+    return STS_OK;
+  }
   int build_graph();
   int step_host(int n, int* done);
   int step_graph(int n, int* done);
@@ -158,19 +217,46 @@ int sts_ctx::build_graph() {
   cudaGraphConditionalHandle hw;
   CU(cudaGraphConditionalHandleCreate(&hw, b_outer, 1, cudaGraphCondAssignDefault));
   cudaGraphNode_t n_asm, n_sw, n_cor, n_rho, n_bnd, n_fd;
-  if (int r = add_kernel(&n_asm, b_outer, {}, k_assemble, grid, block, g, (unsigned long long)hw, 1)) return r;
-  cudaGraphNode_t n_first;
-  if (int r = add_kernel(&n_first, b_outer, {n_asm}, k_sweep_first, grid, block, g, (unsigned long long)hw, 1)) return r;
+  if (int r = add_kernel(&n_asm, b_outer, {}, fast() ? k_assemble_fast : k_assemble, grid, block, g,
+                         (unsigned long long)hw, 1))
+    return r;
+  cudaGraphNode_t n_first, n_one;
   cudaGraph_t b_sweep;
-  if (int r = add_while(&n_sw, b_outer, {n_first}, hw, &b_sweep)) return r;
-  cudaGraphNode_t n_one;
-  if (int r = add_kernel(&n_one, b_sweep, {}, k_sweep, grid, block, g, (unsigned long long)hw, 1)) return r;
+  if (mixed()) {
+    // first FP64 sweep -> WHILE(FP32 sweeps) -> b + e in FP64 -> exact sweep recomputing the
+    // last one -> WHILE(exact sweeps) while the FP64 update still misses the tolerance
+    if (int r = add_kernel(&n_first, b_outer, {n_asm}, k_sweep_first_mixed, grid, block, g, (unsigned long long)hw, 1))
+      return r;
+    cudaGraphNode_t n_w32, n_mat, n_conf;
+    if (int r = add_while(&n_w32, b_outer, {n_first}, hw, &b_sweep)) return r;
+    if (int r = add_kernel(&n_one, b_sweep, {}, k_sweep32, grid, block, g, (unsigned long long)hw, 1)) return r;
+    cudaGraphConditionalHandle hf;
+    CU(cudaGraphConditionalHandleCreate(&hf, b_outer, 0, cudaGraphCondAssignDefault));
+    if (int r = add_kernel(&n_mat, b_outer, {n_w32}, k_materialize, grid, block, g, (unsigned long long)hf, 1)) return r;
+    if (int r = add_kernel(&n_conf, b_outer, {n_mat}, k_sweep, grid, block, g, (unsigned long long)hf, 1)) return r;
+    cudaGraph_t b_fb;
+    if (int r = add_while(&n_sw, b_outer, {n_conf}, hf, &b_fb)) return r;
+    cudaGraphNode_t n_fb;
+    if (int r = add_kernel(&n_fb, b_fb, {}, k_sweep, grid, block, g, (unsigned long long)hf, 1)) return r;
+  } else {
+    if (int r = add_kernel(&n_first, b_outer, {n_asm}, k_sweep_first, grid, block, g, (unsigned long long)hw, 1))
+      return r;
+    if (int r = add_while(&n_sw, b_outer, {n_first}, hw, &b_sweep)) return r;
+    if (int r = add_kernel(&n_one, b_sweep, {}, k_sweep, grid, block, g, (unsigned long long)hw, 1)) return r;
+  }
   if (int r = add_kernel(&n_cor, b_outer, {n_sw}, k_correct, grid, block, g)) return r;
   if (int r = add_kernel(&n_rho, b_outer, {n_cor}, k_face_rho, grid, block, g)) return r;
-  if (int r = add_kernel(&n_bnd, b_outer, {n_rho}, k_boundary, dim3(1), dim3(1024), g, (unsigned)PH_ALL_STEP,
-                         (unsigned long long)ho, 1))
+  cudaGraphNode_t n_walls, n_tj;
+  if (int r = add_kernel(&n_walls, b_outer, {n_rho}, k_bnd_walls, walls_grid(), dim3(256), g,
+                         (unsigned)(PH_CONTROL | PH_SLIP_U | PH_SLIP_V), (unsigned long long)ho, 1))
     return r;
-  if (int r = add_kernel(&n_fd, b_outer, {n_bnd}, k_flux_diff, grid, block, g)) return r;
+  if (int r = add_kernel(&n_bnd, b_outer, {n_walls}, k_boundary, dim3(1), dim3(1024), g,
+                         (unsigned)(PH_VEL | PH_PBEGIN), (unsigned long long)0, 0))
+    return r;
+  if (int r = add_kernel(&n_tj, b_outer, {n_bnd}, k_bnd_tjump, tjump_grid(), dim3(256), g)) return r;
+  if (int r = add_kernel(&n_fd, b_outer, {n_tj}, fast() ? k_flux_diff_fast : k_flux_diff, grid, block, g,
+                         (unsigned)(PH_TEMP | PH_PRES)))
+    return r;
   CU(cudaGraphInstantiate(&exec, graph, 0));
   h_step = hs;
   h_outer = ho;
@@ -193,29 +279,17 @@ int sts_ctx::step_graph(int n, int* done) {
 // Kernel-by-kernel variant: the device still decides every sweep; the host only
 // checks after each batch of sweep launches whether the loop has stopped.
 int sts_ctx::step_host(int n, int* done) {
-  const bool fixed = hc.bits & F_FIXED_SWEEPS;
-  const int NI = (int)hc.cfg.n("N_I"), Npc = (int)hc.cfg.n("N_I_p_c");
+  const int NI = (int)hc.cfg.n("N_I");
   int k = 0;
   for (; k < n; k++) {
     k_step_begin<<<grid, block, 0, s>>>(g, 1, 0, 0);
     for (int outer = 0; outer < NI; outer++) {
-      k_assemble<<<grid, block, 0, s>>>(g, 0, 0);
-      k_sweep_first<<<grid, block, 0, s>>>(g, 0, 0);
-      if (fixed) {
-        for (int q = 1; q < Npc; q++) k_sweep<<<grid, block, 0, s>>>(g, 0, 0);
-      } else {
-        int launched = 1;
-        for (;;) {
-          const int batch = 4;
-          for (int q = 0; q < batch && launched < Npc; q++, launched++) k_sweep<<<grid, block, 0, s>>>(g, 0, 0);
-          if (int r = read_ctl()) return r;
-          if (h_ctl->pt_done || launched >= Npc) break;
-        }
-      }
+      if (fast()) k_assemble_fast<<<grid, block, 0, s>>>(g, 0, 0);
+      else k_assemble<<<grid, block, 0, s>>>(g, 0, 0);
+      if (int r = sweep_loop([](int) {}, 4)) return r;
       k_correct<<<grid, block, 0, s>>>(g);
       k_face_rho<<<grid, block, 0, s>>>(g);
-      k_boundary<<<1, 1024, 0, s>>>(g, PH_ALL_STEP, 0, 0);
-      k_flux_diff<<<grid, block, 0, s>>>(g);
+      boundary_step([](int) {});
       if (NI > 1) {
         if (int r = read_ctl()) return r;
         if (!h_ctl->continue_iter) break;
@@ -234,10 +308,10 @@ int sts_ctx::step_host(int n, int* done) {
 }
 
 // The launch loop with a CUDA event pair around every kernel: per-kernel device time.
-// kinds: 0 step_begin, 1 assemble, 2 sweep, 3 correct, 4 face_rho, 5 boundary, 6 flux_diff, 7 step_end
+// kinds: 0 step_begin, 1 assemble, 2 sweep (FP64), 3 correct, 4 face_rho, 5 boundary,
+// 6 flux_diff, 7 step_end, 8 FP32 sweep (with the FP64 re-forming of the iterate)
 int sts_ctx::profile(int n, double* ms, int* cnt, int* done) {
-  const bool fixed = hc.bits & F_FIXED_SWEEPS;
-  const int NI = (int)hc.cfg.n("N_I"), Npc = (int)hc.cfg.n("N_I_p_c");
+  const int NI = (int)hc.cfg.n("N_I");
   std::vector<cudaEvent_t> ev;
   std::vector<int> kind;
   auto mark = [&](int k) {
@@ -247,27 +321,20 @@ int sts_ctx::profile(int n, double* ms, int* cnt, int* done) {
     ev.push_back(a);
     kind.push_back(k);
   };
-  for (int q = 0; q < 8; q++) { ms[q] = 0; cnt[q] = 0; }
+  for (int q = 0; q < kProfileKinds; q++) { ms[q] = 0; cnt[q] = 0; }
   int k = 0;
   for (; k < n; k++) {
     mark(-1); k_step_begin<<<grid, block, 0, s>>>(g, 1, 0, 0); mark(0);
     for (int outer = 0; outer < NI; outer++) {
-      mark(-1); k_assemble<<<grid, block, 0, s>>>(g, 0, 0); mark(1);
+      mark(-1);
+      if (fast()) k_assemble_fast<<<grid, block, 0, s>>>(g, 0, 0);
+      else k_assemble<<<grid, block, 0, s>>>(g, 0, 0);
+      mark(1);
       // the sweep count of this outer iteration is only known afterwards: launch one at a time
-      for (int q = 0; q < Npc; q++) {
-        mark(-1);
-        if (q == 0) k_sweep_first<<<grid, block, 0, s>>>(g, 0, 0);
-        else k_sweep<<<grid, block, 0, s>>>(g, 0, 0);
-        mark(2);
-        if (!fixed) {
-          if (int r = read_ctl()) return r;
-          if (h_ctl->pt_done) break;
-        }
-      }
+      if (int r = sweep_loop(mark, 1)) return r;
       mark(-1); k_correct<<<grid, block, 0, s>>>(g); mark(3);
       mark(-1); k_face_rho<<<grid, block, 0, s>>>(g); mark(4);
-      mark(-1); k_boundary<<<1, 1024, 0, s>>>(g, PH_ALL_STEP, 0, 0); mark(5);
-      mark(-1); k_flux_diff<<<grid, block, 0, s>>>(g); mark(6);
+      boundary_step(mark);
       if (NI > 1) {
         if (int r = read_ctl()) return r;
         if (!h_ctl->continue_iter) break;
@@ -491,6 +558,7 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
   c->opt = opt;
   c->t0 = std::chrono::steady_clock::now();
   std::string err;
+  if (opt.precision < 0 || opt.precision > 2) return fail(STS_ERR_ARG, "precision must be 0, 1 or 2");
   if (!load_case(dir, opt.fixed_sweeps != 0, c->hc, err)) return fail(STS_ERR_INPUT, err);
   Case& h = c->hc;
   int ndev = 0;
@@ -586,6 +654,40 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
     if (int r = c->alloc(f, Na)) return r;
   for (int k = 0; k < 8; k++)
     if (int r = c->alloc(&g.inv[k], Na)) return r;
+  g.precision = opt.precision;
+  g.rht = 1.0 / g.ht;
+  if (g.precision >= 1) {
+    // reciprocals of the mesh widths and of the two-cell sums the assembly and the diffusion
+    // terms divide by; the neighbour indices are those of the kernels (periodic wrap in x, the
+    // y index above compared with Nx as in the reference's ScT1 code, clamped to the mesh)
+    const int Nx = h.Nx, Ny = h.Ny;
+    std::vector<double> rhx(Nx), rxm(Nx), rxp(Nx), rhy(Ny), rym(Ny), ryp(Ny);
+    for (int i = 0; i < Nx; i++) {
+      const Nb d = neighbours(i, 0, Nx, Ny, h.bits & F_PERIODIC);
+      rhx[i] = 1.0 / h.hx[i];
+      rxm[i] = 1.0 / (h.hx[d.i_1] + h.hx[i]);
+      rxp[i] = 1.0 / (h.hx[i] + h.hx[d.i1]);
+    }
+    for (int j = 0; j < Ny; j++) {
+      const int jm = j - (0 < j ? 1 : 0), jp = std::min(j + (j < Nx - 1 ? 1 : 0), Ny - 1);
+      rhy[j] = 1.0 / h.hy[j];
+      rym[j] = 1.0 / (h.hy[jm] + h.hy[j]);
+      ryp[j] = 1.0 / (h.hy[j] + h.hy[jp]);
+    }
+    double* t[6];
+    const std::vector<double>* src[6] = {&rhx, &rhy, &rxm, &rxp, &rym, &ryp};
+    for (int k = 0; k < 6; k++) {
+      if (int r = c->alloc(&t[k], src[k]->size())) return r;
+      if (int r = c->upload(t[k], *src[k])) return r;
+    }
+    g.rhx = t[0]; g.rhy = t[1]; g.rxx_m = t[2]; g.rxx_p = t[3]; g.ryy_m = t[4]; g.ryy_p = t[5];
+  }
+  if (g.precision == 2) {
+    float** f32[] = {&g.c32[0], &g.c32[1], &g.c32[2], &g.c32[3], &g.c32[4], &g.a32[0], &g.a32[1], &g.a32[2], &g.a32[3],
+                     &g.T1, &g.q1, &g.den1, &g.dT, &g.dp, &g.ep[0], &g.ep[1], &g.eT[0], &g.eT[1]};
+    for (float** f : f32)
+      if (int r = c->alloc(f, Na)) return r;
+  }
   if (int r = c->alloc(&c->d_ctl, 1)) return r;
   g.ctl = c->d_ctl;
   if (int r = c->upload(g.u, h.u)) return r;
@@ -638,7 +740,7 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
   k_sqrt_rho<<<G, B, 0, s>>>(g, 0);
   k_face_rho<<<G, B, 0, s>>>(g);
   c->boundary(PH_SLIP_U | PH_SLIP_V | PH_VEL | PH_PBEGIN | PH_TJUMP | PH_TEMP | PH_PRES);
-  k_flux_diff<<<G, B, 0, s>>>(g);
+  k_flux_diff<<<G, B, 0, s>>>(g, 0);
   if (int r = c->check()) return r;
   if (int r = c->read_ctl()) return r;
   *out = c.release();
@@ -655,6 +757,7 @@ void sts_default_options(sts_options* opt) {
   opt->use_graph = 1;
   opt->device = 0;
   opt->write_files = 1;
+  opt->precision = 0;
 }
 
 int sts_open_case(const char* case_dir, const sts_options* opt, sts_ctx** out) {
@@ -710,7 +813,7 @@ int sts_profile_steps(sts_ctx* ctx, int nsteps, double* kernel_ms, int* kernel_l
   CU(cudaSetDevice(ctx->opt.device));
   int done = 0;
   if (ctx->finished) {
-    for (int q = 0; q < 8; q++) { kernel_ms[q] = 0; kernel_launches[q] = 0; }
+    for (int q = 0; q < kProfileKinds; q++) { kernel_ms[q] = 0; kernel_launches[q] = 0; }
   } else if (int r = ctx->profile(nsteps, kernel_ms, kernel_launches, &done)) {
     return r;
   }

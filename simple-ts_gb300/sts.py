@@ -30,7 +30,10 @@ EXPORTS = [
     "sts_pt_sweeps_noalloc",
 ]
 
-KERNELS = ["step_begin", "assemble", "sweep", "correct", "face_rho", "boundary", "flux_diff", "step_end"]
+KERNELS = ["step_begin", "assemble", "sweep", "correct", "face_rho", "boundary", "flux_diff", "step_end", "sweep32"]
+
+# precision modes of sts_options.precision
+EXACT, FAST_FP64, MIXED = 0, 1, 2
 
 FIELDS = ["u", "v", "p", "T", "rho", "sqrt_T", "rho_u", "rho_v", "Fx", "Fy", "D_ux", "D_uy", "D_vx", "D_vy",
           "DTx", "DTy", "Gamma_xf", "Gamma_yf", "ScT1", "apx", "apy", "bpx", "bpy", "u_pseudo", "v_pseudo",
@@ -38,7 +41,8 @@ FIELDS = ["u", "v", "p", "T", "rho", "sqrt_T", "rho_u", "rho_v", "Fx", "Fy", "D_
 
 
 class Options(C.Structure):
-    _fields_ = [("fixed_sweeps", C.c_int), ("use_graph", C.c_int), ("device", C.c_int), ("write_files", C.c_int)]
+    _fields_ = [("fixed_sweeps", C.c_int), ("use_graph", C.c_int), ("device", C.c_int), ("write_files", C.c_int),
+                ("precision", C.c_int)]
 
 
 class StsError(RuntimeError):
@@ -88,13 +92,14 @@ def _check(code: int):
         raise StsError(code, load().sts_last_error().decode())
 
 
-def options(fixed_sweeps=True, use_graph=True, device=0, write_files=False) -> Options:
+def options(fixed_sweeps=True, use_graph=True, device=0, write_files=False, precision=EXACT) -> Options:
     o = Options()
     load().sts_default_options(C.byref(o))
     o.fixed_sweeps = int(fixed_sweeps)
     o.use_graph = int(use_graph)
     o.device = int(device)
     o.write_files = int(write_files)
+    o.precision = int(precision)
     return o
 
 
@@ -105,11 +110,11 @@ def _dptr(a: np.ndarray):
 class Solver:
     """One case on one GPU: the reference's solve loop behind the C ABI."""
 
-    def __init__(self, case_dir: str, fixed_sweeps=True, use_graph=True, device=0):
+    def __init__(self, case_dir: str, fixed_sweeps=True, use_graph=True, device=0, precision=EXACT):
         lib = load()
         self._h = C.c_void_p()
-        _check(lib.sts_open_case(case_dir.encode(), C.byref(options(fixed_sweeps, use_graph, device, False)),
-                                 C.byref(self._h)))
+        opt = options(fixed_sweeps, use_graph, device, False, precision)
+        _check(lib.sts_open_case(case_dir.encode(), C.byref(opt), C.byref(self._h)))
         nx, ny = C.c_int(), C.c_int()
         _check(lib.sts_dims(self._h, C.byref(nx), C.byref(ny)))
         self.Nx, self.Ny = nx.value, ny.value
@@ -130,8 +135,8 @@ class Solver:
 
     def profile(self, n: int):
         """Per-kernel device time (ms) and launch counts over n real steps."""
-        ms = np.zeros(8)
-        cnt = np.zeros(8, dtype=np.int32)
+        ms = np.zeros(len(KERNELS))
+        cnt = np.zeros(len(KERNELS), dtype=np.int32)
         done = C.c_int()
         _check(load().sts_profile_steps(self._h, int(n), _dptr(ms), cnt.ctypes.data_as(C.POINTER(C.c_int)),
                                         C.byref(done)))
@@ -189,9 +194,10 @@ class Solver:
             pass
 
 
-def run_case(case_dir: str, fixed_sweeps=True, use_graph=True, device=0, write_files=True):
+def run_case(case_dir: str, fixed_sweeps=True, use_graph=True, device=0, write_files=True, precision=EXACT):
     """The drop-in run: same effect as the reference binary in case_dir."""
-    _check(load().sts_run_case(case_dir.encode(), C.byref(options(fixed_sweeps, use_graph, device, write_files))))
+    opt = options(fixed_sweeps, use_graph, device, write_files, precision)
+    _check(load().sts_run_case(case_dir.encode(), C.byref(opt)))
 
 
 def inspect_case(case_dir: str) -> dict:
