@@ -34,7 +34,7 @@ L2_BYTES = 129 * 2 ** 20
 # algorithmic bytes per cell and launch of each kernel (stated in the design doc): arrays the
 # kernel must read once and write once for one cell, 8 bytes each, plus the 1-byte class
 BYTES_PER_CELL = {
-    "sweep": 32,          # read p, T of the iterate, write p, T
+    "sweep_loop": 32,     # per sweep: read p, T of the iterate, write p, T (times sweeps per launch)
     "assemble": 27 * 8 + 1,
     "flux_diff": 15 * 8 + 1,
     "correct": 10 * 8 + 1,
@@ -239,12 +239,9 @@ class _Null:
         pass
 
 
-def launches_per_step(kcnt, pn, precision):
-    """Kernels one step launches besides its sweeps, from a kernel-by-kernel profile pass."""
-    fixed = sum(v for k, v in kcnt.items() if k not in ("sweep", "sweep32")) / max(pn, 1)
-    # mode 2: the FP64 re-forming of the iterate (counted under sweep32) and the FP32 sweep
-    # that the FP64 sweep recomputes
-    return fixed + (2 if precision == 2 else 0)
+def launches_per_step(kcnt, pn):
+    """Kernels one step launches (the whole sweep loop is one), from a kernel-by-kernel profile pass."""
+    return sum(kcnt.values()) / max(pn, 1)
 
 
 def main():
@@ -305,11 +302,14 @@ def main():
 
     # per-kernel device time over a few more real steps (the roofline's dominant kernel)
     pn, kms, kcnt = s.profile(max(3, min(args.steps, 10)))
-    launches = int(round(sum(launches_per_step(kcnt, pn, 0) + int(x) for x in sweeps)))
+    psweeps = s.sweep_history()[-pn:] if pn else []
+    launches = int(round(launches_per_step(kcnt, pn) * done))
     dom = max(kms, key=lambda k: kms[k])
     peak, peak_kind = peaks()
     avg_s = kms[dom] / 1e3 / max(kcnt[dom], 1)
     bpc = BYTES_PER_CELL.get(dom, 0)
+    if dom == "sweep_loop":  # bytes per launch: per-sweep bytes times the sweeps one launch took
+        bpc *= float(sum(int(x) for x in psweeps)) / max(kcnt[dom], 1)
     achieved = bpc * Na / avg_s / 1e9 if bpc else None
     roof = {"bound": "hbm", "kernel": "k_" + dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "traffic": TRAFFIC.get(dom),
@@ -337,7 +337,7 @@ def main():
                 "speedup_vs_fp64": (Na * vd / (vms / 1e3)) / (Na * done / (total_ms / 1e3)) if done else None,
                 "rel_l2_vs_fp64": err,
                 "sweeps_per_step": float(np.mean(vsw)) if len(vsw) else 0.0,
-                "gpu_launches": int(round(sum(launches_per_step(vkcnt, vpn, prec) + int(x) for x in vsw))),
+                "gpu_launches": int(round(launches_per_step(vkcnt, vpn) * vd)),
                 "kernel_ms_per_step": {k: round(x / max(vpn, 1), 5) for k, x in vkms.items() if x > 0}}
             v.close()
 

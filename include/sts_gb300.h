@@ -72,8 +72,8 @@ int sts_step_timed(sts_ctx* ctx, int nsteps, int* steps_done, double* device_ms)
 
 /* Runs up to nsteps steps kernel by kernel with an event pair around every launch and
  * returns per-kernel device time and launch counts, indexed 0 step_begin, 1 assemble,
- * 2 sweep (FP64), 3 correct, 4 face_rho, 5 boundary, 6 flux_diff, 7 step_end, 8 FP32 sweep
- * and the FP64 re-forming of its iterate (precision 2) -- 9 entries each.
+ * 2 sweep loop (all p-T sweeps of an outer iteration, one launch), 3 correct, 4 face_rho,
+ * 5 boundary, 6 flux_diff, 7 step_end (8 entries each).
  * The steps are real: the state advances exactly as with sts_step. */
 int sts_profile_steps(sts_ctx* ctx, int nsteps, double* kernel_ms, int* kernel_launches, int* steps_done);
 

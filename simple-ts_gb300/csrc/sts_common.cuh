@@ -102,7 +102,15 @@ struct Ctl {
   unsigned int confirm_fail;  // FP64 re-evaluation of the last FP32 sweep missed the tolerance
   unsigned int sweeps32;      // FP32 sweeps taken in this run (statistics)
   unsigned int stop32;        // the FP32 loop of this outer iteration met the stop rule
+  // persistent sweep loops: grid barrier and per-sweep residual maxima (three slots used in
+  // rotation; all zero between launches)
+  unsigned int bar_count, bar_gen;
+  unsigned long long rb_p[3], rb_T[3];
+  unsigned int rebases;       // FP64 re-basings of the FP32 corrections in this run (statistics)
 };
+
+// Bits of Ctl::status.
+enum : unsigned { ST_NONFINITE = 1u, ST_BARRIER_TIMEOUT = 2u };
 
 // Everything a kernel needs: constant parameters and device pointers.
 struct Geo {

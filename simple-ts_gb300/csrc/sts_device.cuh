@@ -82,6 +82,118 @@ __device__ __forceinline__ Cell cell(const Geo& g) {
   return c;
 }
 
+// ---------------------------------------------------------------------------
+// Persistent sweep loops: one launch runs every p-T sweep of an outer iteration.  The grid is
+// no larger than the number of CTAs that fit on the GPU at once (cooperative launch), each CTA
+// takes 32x8-cell tiles in a grid-stride loop, and the CTAs meet at a grid barrier after every
+// sweep, where each reads the sweep's residual maxima and applies the stop rule itself.
+// ---------------------------------------------------------------------------
+constexpr unsigned kSpinLimit = 1u << 24;  // barrier polls before giving up (about a second)
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid-wide barrier on the counter/generation pair of the control block.  A CTA that waits
+// longer than kSpinLimit polls sets ST_BARRIER_TIMEOUT and returns false, so a launch whose
+// CTAs are not all resident ends with an error status instead of hanging.
+__device__ bool grid_barrier(Ctl* ctl) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    const unsigned g0 = ld_acquire(&ctl->bar_gen);
+    __threadfence();
+    int good = 1;
+    if (atomicAdd(&ctl->bar_count, 1u) == gridDim.x * gridDim.y - 1) {
+      atomicExch(&ctl->bar_count, 0u);
+      __threadfence();
+      atomicAdd(&ctl->bar_gen, 1u);
+    } else {
+      unsigned spins = 0;
+      while (ld_acquire(&ctl->bar_gen) == g0) {
+        if (++spins > kSpinLimit) {
+          atomicOr(&ctl->status, ST_BARRIER_TIMEOUT);
+          good = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    ok = good;
+  }
+  __syncthreads();
+  return ok;
+}
+
+__device__ __forceinline__ double ld_res(const unsigned long long* p) {
+  return as_d(*(const volatile unsigned long long*)p);
+}
+
+// Cell of thread (x, y) in tile t of a 32x8 tiling (tx tiles per row).
+__device__ __forceinline__ Cell tile_cell(const Geo& g, int t, int tx) {
+  Cell c;
+  const int ty = t / tx;
+  c.i = (t - ty * tx) * 32 + threadIdx.x;
+  c.j = ty * 8 + threadIdx.y;
+  c.ok = c.i < g.Nx && c.j < g.Ny;
+  c.ij = c.i + c.j * g.Nx;
+  return c;
+}
+
+// Folds a sweep's per-CTA residual maxima into slot n % 3, clears the slot sweep n+1 will use
+// (its last readers passed the barrier of sweep n-1 before this CTA could reach sweep n), meets
+// the other CTAs at the barrier and returns the sweep's global maxima.  False on a barrier timeout.
+__device__ __forceinline__ bool sweep_residual(Ctl* ctl, unsigned n, double rp, double rT, double& res_p,
+                                               double& res_T) {
+  const unsigned slot = n % 3, next = (n + 1) % 3;
+  block_max2(rp, rT, &ctl->rb_p[slot], &ctl->rb_T[slot], &ctl->status);
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    ctl->rb_p[next] = 0ull;
+    ctl->rb_T[next] = 0ull;
+  }
+  if (!grid_barrier(ctl)) return false;
+  res_p = ld_res(&ctl->rb_p[slot]);
+  res_T = ld_res(&ctl->rb_T[slot]);
+  return true;
+}
+
+// The reference's stop rule of the sweep loop (SIMPLE_TS_MPI.cpp:4087-4107), n sweeps taken.
+__device__ __forceinline__ bool sweep_continues(const Geo& g, unsigned n, double res_p, double res_T) {
+  if (g.bits & F_FIXED_SWEEPS) return n < (unsigned)g.N_I_p_c;
+  return (n < 2) || ((n < (unsigned)g.N_I_p_c) && ((g.MaxError_p_c < res_p) || (g.MaxError_T < res_T)));
+}
+
+// Bookkeeping of a finished loop by the last CTA to leave: current buffer, sweep counts, and
+// the residual slots cleared for the next launch.
+__device__ __forceinline__ void pt_loop_finish(Ctl* ctl, unsigned cur, unsigned n, unsigned I) {
+  if (last_block(&ctl->block_count)) {
+    ctl->cur = cur;
+    ctl->Iter_p_c = n;
+    ctl->pt_done = 1;
+    ctl->sweeps[I] = n;
+    ctl->step_sweeps += n;
+    for (int k = 0; k < 3; k++) {
+      ctl->rb_p[k] = 0ull;
+      ctl->rb_T[k] = 0ull;
+    }
+  }
+}
+
+// Records the residuals of sweep n (1-based) of outer iteration I (one thread of CTA 0).
+__device__ __forceinline__ void record_residual(Ctl* ctl, unsigned n, unsigned I, double res_p, double res_T) {
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    ctl->res_p[I] = res_p;
+    ctl->res_T[I] = res_T;
+    if (n == 1) {
+      ctl->res_p0[I] = res_p;
+      ctl->res_T0[I] = res_T;
+    }
+  }
+}
+
 // Zero-gradient copies into the ghost cells outside the p/T solve range, side by side in the
 // reference's order (x begin, x end, y begin, y end); a ghost cell takes the value of the
 // nearest solved cell of its row or column when that cell is fluid.  Called by every thread

@@ -344,116 +344,40 @@ __device__ __forceinline__ void sweep_body(const Geo& g, unsigned long long h_sw
 
 __global__ void k_sweep_first(Geo g, unsigned long long h_sweep, int in_graph) { sweep_body<true>(g, h_sweep, in_graph); }
 
-// ---------------------------------------------------------------------------
-// Mixed-precision sweep loop (precision mode 2).  Within one outer iteration the Jacobi map
-// G is affine in the neighbour temperatures and pressures except for the 1/T_new term of
-// the pressure denominator.  Writing the iterate as x = b + e (b: FP64 base = the iterate
-// before the loop, e: FP32 correction), the first FP64 sweep gives x1 = G(b) and the defect
-// d = x1 - b; every later sweep is e' = d + (G(b + e) - G(b)), evaluated in FP32 from the
-// correction alone:
-//   dT  = sum_k c_k e_T,k + c_5 e_p,P               (c_k = ht aT_k / den_T, c_5 = ht (1-gamma) divu / den_T)
-//   e_T' = d_T + dT
-//   g   = H dT / (T1 (T1 + dT))                     (H = hx hy, T1 = T of x1)
-//   e_p' = d_p + (sum_k a_k e_p,k + q1 g) / (Den1 - g)  (a_k = ht apx/apy, q1 = p of x1, Den1 = sa + H/T1)
-// which is the exact difference of the two FP64 updates, so FP32 only rounds correction-sized
-// numbers.  When the FP32 loop meets the reference's stop rule at sweep n, the iterate of
-// sweep n-1 is formed in FP64 (b + e) and sweep n is recomputed with the exact FP64 kernel,
-// whose residual decides -- the stopping test always uses FP64 updates.
-// ---------------------------------------------------------------------------
-__global__ void k_sweep_first_mixed(Geo g, unsigned long long h_sweep, int in_graph) {
-  Ctl* ctl = g.ctl;
-  Cell c = cell(g);
-  const unsigned cur = ctl->cur;
-  const double* __restrict__ P = g.p[cur];
-  const double* __restrict__ TT = g.T[cur];
-  double* __restrict__ pn = g.p[cur ^ 1];
-  double* __restrict__ Tn = g.T[cur ^ 1];
-  double rp = 0, rT = 0;
-  if (c.ok) {
-    const int ij = c.ij;
-    const uint8_t cl = g.cls[ij];
-    sweep_cell<true>(g, c, P, TT, pn, Tn, rp, rT);
-    if (cls_o(cl)) {
-      const Nb d = neighbours(c.i, c.j, g.Nx, g.Ny, g.bits & F_PERIODIC);
-      const double ht = g.ht;
-      const double denT = g.inv[5][ij];
-      const double Tnew = Tn[ij], pnew = pn[ij];
-      const int nb[4] = {d.i_1j, d.i1j, d.ij_1, d.ij1};
-      for (int k = 0; k < 4; k++) {
-        // a wall neighbour's term is a constant and sits in the defect
-        const bool f = cls_o(cl) == CLS_NCH || cls_fluid(g.cls[nb[k]]);
-        g.c32[k][ij] = f ? (float)(ht * g.inv[k][ij] / denT) : 0.0f;
-      }
-      g.c32[4][ij] = (float)(ht * (1.0 - g.gamma1) * g.inv[4][ij] / denT);
-      g.a32[0][ij] = (float)(ht * g.apx[d.ij]);
-      g.a32[1][ij] = (float)(ht * g.apx[d.i1j]);
-      g.a32[2][ij] = (float)(ht * g.apy[d.ij]);
-      g.a32[3][ij] = (float)(ht * g.apy[d.ij1]);
-      g.T1[ij] = (float)Tnew;
-      g.q1[ij] = (float)pnew;
-      g.den1[ij] = (float)(g.inv[7][ij] + g.hx[c.i] * g.hy[c.j] / Tnew);
-      const float dT = (float)(Tnew - TT[ij]), dp = (float)(pnew - P[ij]);
-      g.dT[ij] = dT;
-      g.dp[ij] = dp;
-      g.eT[0][ij] = dT;
-      g.ep[0][ij] = dp;
-    } else {
-      g.dT[ij] = 0.0f;
-      g.dp[ij] = 0.0f;
-      g.eT[0][ij] = 0.0f;
-      g.ep[0][ij] = 0.0f;
-      g.eT[1][ij] = 0.0f;
-      g.ep[1][ij] = 0.0f;
-    }
-  }
-  block_max2(rp, rT, &ctl->res_bits_p, &ctl->res_bits_T, &ctl->status);
-  if (last_block(&ctl->block_count)) {
-    const unsigned I = ctl->Iter < 64 ? ctl->Iter : 63;
-    const double res_p = as_d(atomicExch(&ctl->res_bits_p, 0ull));
-    const double res_T = as_d(atomicExch(&ctl->res_bits_T, 0ull));
-    ctl->res_p[I] = res_p;
-    ctl->res_T[I] = res_T;
-    ctl->res_p0[I] = res_p;
-    ctl->res_T0[I] = res_T;
-    const unsigned n = ++ctl->Iter_p_c;
-    ctl->ecur = 0;
-    ctl->base = cur;
-    ctl->stop32 = 0;
-    const bool cont = n < (unsigned)g.N_I_p_c;  // the stop rule needs two sweeps at least
-    if (!cont) {  // a single sweep was asked for: x1 is the result
-      ctl->cur = cur ^ 1;
-      ctl->pt_done = 1;
-      ctl->sweeps[I] = n;
-      ctl->step_sweeps += n;
-    }
-    if (in_graph) cudaGraphSetConditional((cudaGraphConditionalHandle)h_sweep, cont ? 1 : 0);
-  }
-}
-
-// Forms the FP64 iterate b + e of the sweep before the last FP32 one in the second FP64 buffer
-// and rewinds the sweep counter by one, so that the exact k_sweep that follows recomputes the
-// last sweep in FP64 and applies the stop rule to FP64 updates.
-__global__ void k_materialize(Geo g, unsigned long long h_confirm, int in_graph) {
-  Ctl* ctl = g.ctl;
-  const bool done = ctl->pt_done;
-  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
-    if (in_graph && done) cudaGraphSetConditional((cudaGraphConditionalHandle)h_confirm, 0);
-  }
-  if (done) return;
-  Cell c = cell(g);
-  const unsigned b = ctl->base, src = ctl->ecur ^ 1;
-  if (c.ok) {
-    g.p[b ^ 1][c.ij] = g.p[b][c.ij] + (double)g.ep[src][c.ij];
-    g.T[b ^ 1][c.ij] = g.T[b][c.ij] + (double)g.eT[src][c.ij];
-  }
-  if (last_block(&ctl->block_count)) {
-    ctl->cur = b ^ 1;
-    ctl->Iter_p_c -= 1;
-    ctl->pt_done = 0;
-    ctl->stop32 = 0;
-  }
-}
 __global__ void k_sweep(Geo g, unsigned long long h_sweep, int in_graph) { sweep_body<false>(g, h_sweep, in_graph); }
+
+// The whole sweep loop of one outer iteration in one cooperative launch: the same cell
+// arithmetic as k_sweep_first / k_sweep (so the same bits), with a grid barrier after every sweep.
+__global__ void __launch_bounds__(256) k_pt_loop(Geo g) {
+  Ctl* ctl = g.ctl;
+  const int tx = (g.Nx + 31) / 32, nt = tx * ((g.Ny + 7) / 8);
+  const unsigned I = ctl->Iter < 64 ? ctl->Iter : 63;
+  unsigned cur = ctl->cur, n = 0;
+  for (;;) {
+    const double* P = g.p[cur];
+    const double* TT = g.T[cur];
+    double* pn = g.p[cur ^ 1];
+    double* Tn = g.T[cur ^ 1];
+    double rp = 0, rT = 0;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+      const Cell c = tile_cell(g, t, tx);
+      if (!c.ok) continue;
+      double a = 0, b = 0;
+      if (n == 0) sweep_cell<true>(g, c, P, TT, pn, Tn, a, b);
+      else sweep_cell<false>(g, c, P, TT, pn, Tn, a, b);
+      if (a != a || b != b) atomicOr(&ctl->status, ST_NONFINITE);  // the max below skips NaN
+      rp = mx(rp, a);
+      rT = mx(rT, b);
+    }
+    double res_p, res_T;
+    if (!sweep_residual(ctl, n, rp, rT, res_p, res_T)) break;
+    n++;
+    cur ^= 1;
+    record_residual(ctl, n, I, res_p, res_T);
+    if (!sweep_continues(g, n, res_p, res_T)) break;
+  }
+  pt_loop_finish(ctl, cur, n, I);
+}
 
 // ---------------------------------------------------------------------------
 // velocity correction with L-inf residuals (SIMPLE_TS_MPI.cpp:4171-4305) and

@@ -208,52 +208,281 @@ __global__ void k_flux_diff_fast(Geo g, unsigned tail) {
   }
 }
 
-// FP32 correction sweep (see k_sweep_first_mixed): e' = d + (G(b + e) - G(b)).
-__global__ void k_sweep32(Geo g, unsigned long long h_sweep, int in_graph) {
-  Ctl* ctl = g.ctl;
-  if (ctl->pt_done || ctl->stop32) {
-    if (in_graph && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0)
-      cudaGraphSetConditional((cudaGraphConditionalHandle)h_sweep, 0);
-    return;
+// ---------------------------------------------------------------------------
+// p-T sweeps with reciprocal multiplies (precision modes 1 and 2): the reference's update
+// (SIMPLE_TS_MPI.cpp:3786-4131) with 1/den_T stored once per outer iteration and the pressure
+// denominator sa + H/T_new folded into one division, p_new = N T_new / (sa T_new + H).
+// The first sweep stores the loop invariants of a cell in inv[0..7]: the four neighbour weights
+// (a wall neighbour's weight already multiplied by the wall temperature), divu, 1/den_T, the
+// p_pr/T_pr term and ht * (sum of the p coefficients).  Returns false for unsolved cells, which
+// copy through.
+// ---------------------------------------------------------------------------
+template <bool FIRST>
+__device__ __forceinline__ bool sweep_cell_fast(const Geo& g, const Cell& c, const double* __restrict__ P,
+                                                const double* __restrict__ TT, double* __restrict__ pn,
+                                                double* __restrict__ Tn, double& Tnew, double& pnew, double& sa) {
+  const int ij = c.ij;
+  const uint8_t cl = g.cls[ij];
+  const int co = cls_o(cl);
+  if (!co) {
+    pnew = P[ij];
+    Tnew = TT[ij];
+    pn[ij] = pnew;
+    Tn[ij] = Tnew;
+    return false;
   }
-  Cell c = cell(g);
-  const unsigned src = ctl->ecur;
+  const int i = c.i, j = c.j;
+  const Nb d = neighbours(i, j, g.Nx, g.Ny, g.bits & F_PERIODIC);
+  const double* __restrict__ apx = g.apx;
+  const double* __restrict__ apy = g.apy;
+  const double ht = g.ht, H = g.hx[i] * g.hy[j];
+  auto fl = [&](int k) { return cls_fluid(g.cls[k]); };
+  double w1, w2, w3, w4, divu, rden, pc;
+  if (FIRST) {
+    const double* __restrict__ Fx = g.Fx;
+    const double* __restrict__ Fy = g.Fy;
+    const double aT1 = fmax(0.0, Fx[d.ij]) + g.DTx[d.ij];
+    const double aT2 = fmax(0.0, -Fx[d.i1j]) + g.DTx[d.i1j];
+    const double aT3 = fmax(0.0, Fy[d.ij]) + g.DTy[d.ij];
+    const double aT4 = fmax(0.0, -Fy[d.ij1]) + g.DTy[d.ij1];
+    divu = (g.u[d.i1j] - g.u[d.ij]) * g.hy[j] + (g.v[d.ij1] - g.v[d.ij]) * g.hx[i];
+    rden = 1.0 / (ht * (aT1 + aT2 + aT3 + aT4 + Fx[d.i1j] - Fx[d.ij] + Fy[d.ij1] - Fy[d.ij]) + H * g.rho[ij]);
+    w1 = aT1; w2 = aT2; w3 = aT3; w4 = aT4;
+    if (co == CLS_BC) {
+      if (!fl(d.i_1j)) w1 = aT1 * g.Tw_u[ij];
+      if (!fl(d.i1j)) w2 = aT2 * g.Tw_u[d.i1j];
+      if (!fl(d.ij_1)) w3 = aT3 * g.Tw_v[ij];
+      if (!fl(d.ij1)) w4 = aT4 * g.Tw_v[d.ij1];
+    }
+    pc = g.p_pr[ij] * H / g.T_pr[ij];
+    sa = ht * (apx[ij] + apx[d.i1j] + apy[ij] + apy[d.ij1]);
+    g.inv[0][ij] = w1; g.inv[1][ij] = w2; g.inv[2][ij] = w3; g.inv[3][ij] = w4;
+    g.inv[4][ij] = divu; g.inv[5][ij] = rden; g.inv[6][ij] = pc; g.inv[7][ij] = sa;
+  } else {
+    w1 = g.inv[0][ij]; w2 = g.inv[1][ij]; w3 = g.inv[2][ij]; w4 = g.inv[3][ij];
+    divu = g.inv[4][ij]; rden = g.inv[5][ij]; pc = g.inv[6][ij]; sa = g.inv[7][ij];
+  }
+  double t1, t2, t3, t4;
+  if (co == CLS_BC) {
+    t1 = fl(d.i_1j) ? w1 * TT[d.i_1j] : w1;
+    t2 = fl(d.i1j) ? w2 * TT[d.i1j] : w2;
+    t3 = fl(d.ij_1) ? w3 * TT[d.ij_1] : w3;
+    t4 = fl(d.ij1) ? w4 * TT[d.ij1] : w4;
+  } else {
+    t1 = w1 * TT[d.i_1j];
+    t2 = w2 * TT[d.i1j];
+    t3 = w3 * TT[d.ij_1];
+    t4 = w4 * TT[d.ij1];
+  }
+  Tnew = (ht * (t1 + t2 + t3 + t4 + (1.0 - g.gamma1) * P[ij] * divu) + g.ScT1[ij]) * rden;
+  double num = apx[ij] * P[d.i_1j] + apx[d.i1j] * P[d.i1j] + apy[ij] * P[d.ij_1] + apy[d.ij1] * P[d.ij1] +
+               g.bpx[ij] - g.bpx[d.i1j] + g.bpy[ij] - g.bpy[d.ij1];
+  if (co == CLS_BC) {
+    if ((g.bits & F_GIVEN_U_XB) && i == g.Nx_o0) num += g.Fx[ij];
+    if ((g.bits & F_GIVEN_U_XE) && i == g.Nx_o1 - 1) num -= g.Fx[d.i1j];
+  }
+  pnew = (ht * num + pc) * Tnew / (sa * Tnew + H);
+  Tn[ij] = Tnew;
+  pn[ij] = pnew;
+  return true;
+}
+
+// The sweep loop of mode 1 in one cooperative launch (see k_pt_loop).
+__global__ void __launch_bounds__(256) k_pt_loop_fast(Geo g) {
+  Ctl* ctl = g.ctl;
+  const int tx = (g.Nx + 31) / 32, nt = tx * ((g.Ny + 7) / 8);
+  const unsigned I = ctl->Iter < 64 ? ctl->Iter : 63;
+  unsigned cur = ctl->cur, n = 0;
+  for (;;) {
+    const double* P = g.p[cur];
+    const double* TT = g.T[cur];
+    double rp = 0, rT = 0;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+      const Cell c = tile_cell(g, t, tx);
+      if (!c.ok) continue;
+      double Tnew, pnew, sa;
+      const bool solved = (n == 0) ? sweep_cell_fast<true>(g, c, P, TT, g.p[cur ^ 1], g.T[cur ^ 1], Tnew, pnew, sa)
+                                   : sweep_cell_fast<false>(g, c, P, TT, g.p[cur ^ 1], g.T[cur ^ 1], Tnew, pnew, sa);
+      if (!solved) continue;
+      const double a = fabs(pnew - P[c.ij]), b = fabs(Tnew - TT[c.ij]);
+      if (a != a || b != b) atomicOr(&ctl->status, ST_NONFINITE);
+      rp = mx(rp, a);
+      rT = mx(rT, b);
+    }
+    double res_p, res_T;
+    if (!sweep_residual(ctl, n, rp, rT, res_p, res_T)) break;
+    n++;
+    cur ^= 1;
+    record_residual(ctl, n, I, res_p, res_T);
+    if (!sweep_continues(g, n, res_p, res_T)) break;
+  }
+  pt_loop_finish(ctl, cur, n, I);
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-precision sweep loop (precision mode 2, tolerance-terminated loops).  Within one outer
+// iteration the Jacobi map G is affine in the neighbour temperatures and pressures except for
+// the 1/T_new term of the pressure denominator.  Writing the iterate as x = b + e (b: FP64 base,
+// e: FP32 correction), an FP64 sweep from b gives x1 = G(b) and the defect d = x1 - b, and every
+// later sweep is e' = d + (G(b + e) - G(b)), evaluated in FP32 from the correction alone:
+//   dT   = sum_k c_k e_T,k + c_5 e_p,P                (c_k = ht w_k / den_T, c_5 = ht (1-gamma) divu / den_T)
+//   e_T' = d_T + dT
+//   q    = H dT / (T1 (T1 + dT))                      (H = hx hy, T1 = T of x1)
+//   e_p' = d_p + (sum_k a_k e_p,k + p1 q) / (Den1 - q)  (a_k = ht apx/apy, p1 = p of x1, Den1 = sa + H/T1)
+// which is the exact difference of two FP64 updates, so FP32 only rounds correction-sized numbers.
+// When the FP32 sweeps meet the reference's stop rule at sweep n, the iterate of sweep n-1 is
+// formed in FP64 (b + e) and sweep n is recomputed in FP64; its residual decides.  If it misses
+// the tolerance, the FP64 pair (x_{n-1}, x_n) becomes the new base and defect and the FP32 sweeps
+// go on from there with corrections of residual size.  A cell whose FP32 update is below the
+// resolution of its correction (kFloor32 |e|) counts as converged for the FP32 stop test only.
+// ---------------------------------------------------------------------------
+constexpr float kFloor32 = 8.0f / 16777216.0f;  // 8 units in the last place of an FP32 number
+
+// Base values of the FP32 corrections taken from an FP64 sweep x -> x1 of a solved cell.
+__device__ __forceinline__ void set_base(const Geo& g, const Cell& c, double T0, double p0, double T1, double p1,
+                                         double sa) {
+  const int ij = c.ij;
+  const double H = g.hx[c.i] * g.hy[c.j];
+  g.T1[ij] = (float)T1;
+  g.q1[ij] = (float)p1;
+  g.den1[ij] = (float)(sa + H / T1);
+  const float dT = (float)(T1 - T0), dp = (float)(p1 - p0);
+  g.dT[ij] = dT;
+  g.dp[ij] = dp;
+  g.eT[0][ij] = dT;
+  g.ep[0][ij] = dp;
+}
+
+// One FP32 correction sweep of a solved cell: e (buffer src) -> e' (buffer src ^ 1).
+__device__ __forceinline__ void sweep32_cell(const Geo& g, const Cell& c, unsigned src, float& rp, float& rT) {
+  const int ij = c.ij;
+  const Nb d = neighbours(c.i, c.j, g.Nx, g.Ny, g.bits & F_PERIODIC);
   const float* __restrict__ ep = g.ep[src];
   const float* __restrict__ eT = g.eT[src];
-  float* __restrict__ epn = g.ep[src ^ 1];
-  float* __restrict__ eTn = g.eT[src ^ 1];
-  float rp = 0.f, rT = 0.f;
-  if (c.ok && cls_o(g.cls[c.ij])) {
-    const int ij = c.ij;
-    const Nb d = neighbours(c.i, c.j, g.Nx, g.Ny, g.bits & F_PERIODIC);
-    const float dT = g.c32[0][ij] * eT[d.i_1j] + g.c32[1][ij] * eT[d.i1j] + g.c32[2][ij] * eT[d.ij_1] +
-                     g.c32[3][ij] * eT[d.ij1] + g.c32[4][ij] * ep[ij];
-    const float eTnew = g.dT[ij] + dT;
-    const float T1 = g.T1[ij];
-    const float H = (float)(g.hx[c.i] * g.hy[c.j]);
-    const float gg = H * dT / (T1 * (T1 + dT));
-    const float num = g.a32[0][ij] * ep[d.i_1j] + g.a32[1][ij] * ep[d.i1j] + g.a32[2][ij] * ep[d.ij_1] +
-                      g.a32[3][ij] * ep[d.ij1];
-    const float epnew = g.dp[ij] + (num + g.q1[ij] * gg) / (g.den1[ij] - gg);
-    eTn[ij] = eTnew;
-    epn[ij] = epnew;
-    rT = fabsf(eTnew - eT[ij]);
-    rp = fabsf(epnew - ep[ij]);
+  const float dT = g.c32[0][ij] * eT[d.i_1j] + g.c32[1][ij] * eT[d.i1j] + g.c32[2][ij] * eT[d.ij_1] +
+                   g.c32[3][ij] * eT[d.ij1] + g.c32[4][ij] * ep[ij];
+  const float eTnew = g.dT[ij] + dT;
+  const float T1 = g.T1[ij];
+  const float H = (float)(g.hx[c.i] * g.hy[c.j]);
+  const float q = H * dT / (T1 * (T1 + dT));
+  const float num = g.a32[0][ij] * ep[d.i_1j] + g.a32[1][ij] * ep[d.i1j] + g.a32[2][ij] * ep[d.ij_1] +
+                    g.a32[3][ij] * ep[d.ij1];
+  const float epnew = g.dp[ij] + (num + g.q1[ij] * q) / (g.den1[ij] - q);
+  g.eT[src ^ 1][ij] = eTnew;
+  g.ep[src ^ 1][ij] = epnew;
+  const float aT = fabsf(eTnew - eT[ij]), ap = fabsf(epnew - ep[ij]);
+  if (aT != aT || ap != ap) atomicOr(&g.ctl->status, ST_NONFINITE);
+  rT = fmaxf(rT, aT <= kFloor32 * fabsf(eTnew) ? 0.0f : aT);
+  rp = fmaxf(rp, ap <= kFloor32 * fabsf(epnew) ? 0.0f : ap);
+}
+
+__global__ void __launch_bounds__(256) k_pt_loop_mixed(Geo g) {
+  Ctl* ctl = g.ctl;
+  const bool lead = blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0;
+  const int tx = (g.Nx + 31) / 32, nt = tx * ((g.Ny + 7) / 8);
+  const unsigned I = ctl->Iter < 64 ? ctl->Iter : 63;
+  const double ht = g.ht, gm = 1.0 - g.gamma1;
+  unsigned base = ctl->cur, cur = base ^ 1, n = 0;
+  unsigned nred = 0;  // residual reductions so far (the slot rotation of sweep_residual)
+  double res_p, res_T;
+
+  // sweep 1 in FP64 from b, with the FP32 coefficients of this outer iteration
+  {
+    const double* P = g.p[base];
+    const double* TT = g.T[base];
+    double rp = 0, rT = 0;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+      const Cell c = tile_cell(g, t, tx);
+      if (!c.ok) continue;
+      const int ij = c.ij;
+      double Tnew, pnew, sa;
+      if (!sweep_cell_fast<true>(g, c, P, TT, g.p[base ^ 1], g.T[base ^ 1], Tnew, pnew, sa)) {
+        g.dT[ij] = 0.0f; g.dp[ij] = 0.0f;
+        g.eT[0][ij] = 0.0f; g.ep[0][ij] = 0.0f; g.eT[1][ij] = 0.0f; g.ep[1][ij] = 0.0f;
+        continue;
+      }
+      const double a = fabs(pnew - P[ij]), b = fabs(Tnew - TT[ij]);
+      if (a != a || b != b) atomicOr(&ctl->status, ST_NONFINITE);
+      rp = mx(rp, a);
+      rT = mx(rT, b);
+      const Nb d = neighbours(c.i, c.j, g.Nx, g.Ny, g.bits & F_PERIODIC);
+      const double r = ht * g.inv[5][ij];
+      const int nb[4] = {d.i_1j, d.i1j, d.ij_1, d.ij1};
+      for (int k = 0; k < 4; k++)  // a wall neighbour's term is a constant and sits in the defect
+        g.c32[k][ij] = (cls_o(g.cls[ij]) == CLS_NCH || cls_fluid(g.cls[nb[k]])) ? (float)(r * g.inv[k][ij]) : 0.0f;
+      g.c32[4][ij] = (float)(r * gm * g.inv[4][ij]);
+      g.a32[0][ij] = (float)(ht * g.apx[ij]);
+      g.a32[1][ij] = (float)(ht * g.apx[d.i1j]);
+      g.a32[2][ij] = (float)(ht * g.apy[ij]);
+      g.a32[3][ij] = (float)(ht * g.apy[d.ij1]);
+      set_base(g, c, TT[ij], P[ij], Tnew, pnew, sa);
+    }
+    if (!sweep_residual(ctl, nred++, rp, rT, res_p, res_T)) {
+      pt_loop_finish(ctl, base, n, I);
+      return;
+    }
+    n = 1;
+    record_residual(ctl, n, I, res_p, res_T);
+    if (n >= (unsigned)g.N_I_p_c) {  // a single sweep was asked for: x1 is the result
+      pt_loop_finish(ctl, cur, n, I);
+      return;
+    }
   }
-  block_max2((double)rp, (double)rT, &ctl->res_bits_p, &ctl->res_bits_T, &ctl->status);
-  if (last_block(&ctl->block_count)) {
-    const unsigned I = ctl->Iter < 64 ? ctl->Iter : 63;
-    const double res_p = as_d(atomicExch(&ctl->res_bits_p, 0ull));
-    const double res_T = as_d(atomicExch(&ctl->res_bits_T, 0ull));
-    ctl->res_p[I] = res_p;
-    ctl->res_T[I] = res_T;
-    const unsigned n = ++ctl->Iter_p_c;
-    ctl->sweeps32++;
-    const bool cont = (n < 2) || ((n < (unsigned)g.N_I_p_c) && ((g.MaxError_p_c < res_p) || (g.MaxError_T < res_T)));
-    ctl->ecur = src ^ 1;
-    if (!cont) ctl->stop32 = 1;
-    if (in_graph) cudaGraphSetConditional((cudaGraphConditionalHandle)h_sweep, cont ? 1 : 0);
+
+  unsigned ec = 0;  // buffer of the latest correction
+  for (;;) {
+    // FP32 sweep n+1
+    float rp = 0.f, rT = 0.f;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+      const Cell c = tile_cell(g, t, tx);
+      if (c.ok && cls_o(g.cls[c.ij])) sweep32_cell(g, c, ec, rp, rT);
+    }
+    if (!sweep_residual(ctl, nred++, (double)rp, (double)rT, res_p, res_T)) break;
+    n++;
+    ec ^= 1;
+    if (lead) ctl->sweeps32++;
+    if ((n < (unsigned)g.N_I_p_c) && ((g.MaxError_p_c < res_p) || (g.MaxError_T < res_T))) continue;
+
+    // the iterate of sweep n-1 in FP64: b + e (buffer ec ^ 1)
+    const unsigned prev = ec ^ 1;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+      const Cell c = tile_cell(g, t, tx);
+      if (!c.ok) continue;
+      g.p[base ^ 1][c.ij] = g.p[base][c.ij] + (double)g.ep[prev][c.ij];
+      g.T[base ^ 1][c.ij] = g.T[base][c.ij] + (double)g.eT[prev][c.ij];
+    }
+    if (!grid_barrier(ctl)) break;
+    n--;
+
+    // sweep n again, in FP64, into the base buffer; its residual decides
+    {
+      const double* P = g.p[base ^ 1];
+      const double* TT = g.T[base ^ 1];
+      double rp64 = 0, rT64 = 0;
+      for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+        const Cell c = tile_cell(g, t, tx);
+        if (!c.ok) continue;
+        double Tnew, pnew, sa;
+        if (!sweep_cell_fast<false>(g, c, P, TT, g.p[base], g.T[base], Tnew, pnew, sa)) continue;
+        const double a = fabs(pnew - P[c.ij]), b = fabs(Tnew - TT[c.ij]);
+        if (a != a || b != b) atomicOr(&ctl->status, ST_NONFINITE);
+        rp64 = mx(rp64, a);
+        rT64 = mx(rT64, b);
+        set_base(g, c, TT[c.ij], P[c.ij], Tnew, pnew, sa);  // used only if the loop goes on
+      }
+      if (!sweep_residual(ctl, nred++, rp64, rT64, res_p, res_T)) break;
+    }
+    n++;
+    record_residual(ctl, n, I, res_p, res_T);
+    cur = base;
+    if (!sweep_continues(g, n, res_p, res_T)) break;
+    // re-base: x_{n-1} (buffer base ^ 1) and the defect x_n - x_{n-1} written above
+    base ^= 1;
+    cur = base ^ 1;
+    ec = 0;
+    if (lead) ctl->rebases++;
   }
+  pt_loop_finish(ctl, cur, n, I);
 }
 
 }  // namespace sts

@@ -26,12 +26,13 @@ __global__ void k_apply_bodies(Geo g);
 __global__ void k_assemble(Geo g, unsigned long long h_sweep, int in_graph);
 __global__ void k_sweep_first(Geo g, unsigned long long h_sweep, int in_graph);
 __global__ void k_sweep(Geo g, unsigned long long h_sweep, int in_graph);
-// mixed precision (precision modes 1, 2)
+// the whole sweep loop of an outer iteration in one cooperative launch (grid <= resident CTAs)
+__global__ void k_pt_loop(Geo g);
+// precision modes 1 and 2
 __global__ void k_assemble_fast(Geo g, unsigned long long h_sweep, int in_graph);
 __global__ void k_flux_diff_fast(Geo g, unsigned tail);
-__global__ void k_sweep_first_mixed(Geo g, unsigned long long h_sweep, int in_graph);
-__global__ void k_sweep32(Geo g, unsigned long long h_sweep, int in_graph);
-__global__ void k_materialize(Geo g, unsigned long long h_confirm, int in_graph);
+__global__ void k_pt_loop_fast(Geo g);
+__global__ void k_pt_loop_mixed(Geo g);
 __global__ void k_correct(Geo g);
 __global__ void k_face_rho(Geo g);
 __global__ void k_flux_diff(Geo g, unsigned tail);

@@ -41,7 +41,7 @@ int fail(int code, const std::string& msg) {
   } while (0)
 
 // kernel kinds reported by sts_profile_steps
-constexpr int kProfileKinds = 9;
+constexpr int kProfileKinds = 8;
 
 }  // namespace
 
@@ -58,7 +58,7 @@ struct sts_ctx {
   // graph
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  unsigned long long h_step = 0, h_outer = 0, h_sweep = 0;
+  unsigned long long h_step = 0, h_outer = 0;
   std::chrono::steady_clock::time_point t0;
   bool tmp_fresh = true, iter_fresh = true;
 
@@ -116,39 +116,23 @@ struct sts_ctx {
   }
   bool fast() const { return g.precision >= 1; }
   bool mixed() const { return g.precision == 2 && !(hc.bits & F_FIXED_SWEEPS); }
-  // The sweep loop of one outer iteration outside the graph.  The device decides every stop;
-  // the host launches sweeps in batches (one at a time when profiling) and checks after each
-  // batch whether the loop has stopped.  `mark` brackets launches for the per-kernel profile.
-  template <class M>
-  int sweep_loop(M mark, int batch) {
-    const bool fixed = hc.bits & F_FIXED_SWEEPS;
-    const int Npc = (int)hc.cfg.n("N_I_p_c");
-    int launched = 1;
-    if (mixed()) {
-      mark(-1); k_sweep_first_mixed<<<grid, block, 0, s>>>(g, 0, 0); mark(2);
-      for (;;) {
-        if (int r = read_ctl()) return r;
-        if (h_ctl->pt_done || h_ctl->stop32 || launched >= Npc) break;
-        for (int q = 0; q < batch && launched < Npc; q++, launched++) {
-          mark(-1); k_sweep32<<<grid, block, 0, s>>>(g, 0, 0); mark(8);
-        }
-      }
-      mark(-1); k_materialize<<<grid, block, 0, s>>>(g, 0, 0); mark(8);
-      launched = (int)h_ctl->Iter_p_c - 1;  // the FP64 sweep that follows recomputes the last one
-    } else {
-      mark(-1); k_sweep_first<<<grid, block, 0, s>>>(g, 0, 0); mark(2);
-      if (fixed) {
-        for (int q = 1; q < Npc; q++) { mark(-1); k_sweep<<<grid, block, 0, s>>>(g, 0, 0); mark(2); }
-        return STS_OK;
-      }
-    }
-    for (;;) {
-      for (int q = 0; q < batch && launched < Npc; q++, launched++) {
-        mark(-1); k_sweep<<<grid, block, 0, s>>>(g, 0, 0); mark(2);
-      }
-      if (int r = read_ctl()) return r;
-      if (h_ctl->pt_done || launched >= Npc) break;
-    }
+  // the persistent sweep-loop kernel of this context and its grid (CTAs that fit at once)
+  void (*pt_kernel() const)(Geo) { return mixed() ? k_pt_loop_mixed : (fast() ? k_pt_loop_fast : k_pt_loop); }
+  dim3 pt_grid;
+  int size_pt_grid() {
+    int dev = 0, sms = 0, per_sm = 0;
+    CU(cudaGetDevice(&dev));
+    CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pt_kernel(), 256, 0));
+    if (per_sm < 1) return fail(STS_ERR_CUDA, "the sweep-loop kernel does not fit on a multiprocessor");
+    const int tiles = (int)(grid.x * grid.y);
+    pt_grid = dim3((unsigned)std::max(1, std::min(tiles, per_sm * sms)));
+    return STS_OK;
+  }
+  // the sweep loop of one outer iteration outside the graph: one cooperative launch
+  int pt_loop() {
+    void* args[] = {(void*)&g};
+    CU(cudaLaunchCooperativeKernel((const void*)pt_kernel(), pt_grid, dim3(32, 8), args, 0, s));
     return STS_OK;
   }
   int build_graph();
@@ -196,8 +180,8 @@ int add_while(cudaGraphNode_t* node, cudaGraph_t graph, const std::vector<cudaGr
 }  // namespace
 
 // The whole multi-step loop as one graph:
-//   WHILE(step) { step_begin -> WHILE(outer) { assemble -> WHILE(sweep){sweep} -> correct ->
-//                 face_rho -> boundary -> flux_diff } -> step_end }
+//   WHILE(step) { step_begin -> WHILE(outer) { assemble -> sweep loop (one cooperative kernel) ->
+//                 correct -> face_rho -> walls -> boundary -> T-jump -> flux_diff } -> step_end }
 // Every decision (sweep count, outer iterations, end of run) is taken on the device.
 int sts_ctx::build_graph() {
   CU(cudaGraphCreate(&graph, 0));
@@ -214,35 +198,15 @@ int sts_ctx::build_graph() {
   if (int r = add_while(&n_outer, b_step, {n_begin}, ho, &b_outer)) return r;
   if (int r = add_kernel(&n_end, b_step, {n_outer}, k_step_end, dim3(1), dim3(1024), g, (unsigned long long)hs, 1))
     return r;
-  cudaGraphConditionalHandle hw;
-  CU(cudaGraphConditionalHandleCreate(&hw, b_outer, 1, cudaGraphCondAssignDefault));
   cudaGraphNode_t n_asm, n_sw, n_cor, n_rho, n_bnd, n_fd;
   if (int r = add_kernel(&n_asm, b_outer, {}, fast() ? k_assemble_fast : k_assemble, grid, block, g,
-                         (unsigned long long)hw, 1))
+                         (unsigned long long)0, 0))
     return r;
-  cudaGraphNode_t n_first, n_one;
-  cudaGraph_t b_sweep;
-  if (mixed()) {
-    // first FP64 sweep -> WHILE(FP32 sweeps) -> b + e in FP64 -> exact sweep recomputing the
-    // last one -> WHILE(exact sweeps) while the FP64 update still misses the tolerance
-    if (int r = add_kernel(&n_first, b_outer, {n_asm}, k_sweep_first_mixed, grid, block, g, (unsigned long long)hw, 1))
-      return r;
-    cudaGraphNode_t n_w32, n_mat, n_conf;
-    if (int r = add_while(&n_w32, b_outer, {n_first}, hw, &b_sweep)) return r;
-    if (int r = add_kernel(&n_one, b_sweep, {}, k_sweep32, grid, block, g, (unsigned long long)hw, 1)) return r;
-    cudaGraphConditionalHandle hf;
-    CU(cudaGraphConditionalHandleCreate(&hf, b_outer, 0, cudaGraphCondAssignDefault));
-    if (int r = add_kernel(&n_mat, b_outer, {n_w32}, k_materialize, grid, block, g, (unsigned long long)hf, 1)) return r;
-    if (int r = add_kernel(&n_conf, b_outer, {n_mat}, k_sweep, grid, block, g, (unsigned long long)hf, 1)) return r;
-    cudaGraph_t b_fb;
-    if (int r = add_while(&n_sw, b_outer, {n_conf}, hf, &b_fb)) return r;
-    cudaGraphNode_t n_fb;
-    if (int r = add_kernel(&n_fb, b_fb, {}, k_sweep, grid, block, g, (unsigned long long)hf, 1)) return r;
-  } else {
-    if (int r = add_kernel(&n_first, b_outer, {n_asm}, k_sweep_first, grid, block, g, (unsigned long long)hw, 1))
-      return r;
-    if (int r = add_while(&n_sw, b_outer, {n_first}, hw, &b_sweep)) return r;
-    if (int r = add_kernel(&n_one, b_sweep, {}, k_sweep, grid, block, g, (unsigned long long)hw, 1)) return r;
+  if (int r = add_kernel(&n_sw, b_outer, {n_asm}, pt_kernel(), pt_grid, dim3(32, 8), g)) return r;
+  {
+    cudaLaunchAttributeValue v{};
+    v.cooperative = 1;
+    CU(cudaGraphKernelNodeSetAttribute(n_sw, cudaLaunchAttributeCooperative, &v));
   }
   if (int r = add_kernel(&n_cor, b_outer, {n_sw}, k_correct, grid, block, g)) return r;
   if (int r = add_kernel(&n_rho, b_outer, {n_cor}, k_face_rho, grid, block, g)) return r;
@@ -260,7 +224,6 @@ int sts_ctx::build_graph() {
   CU(cudaGraphInstantiate(&exec, graph, 0));
   h_step = hs;
   h_outer = ho;
-  h_sweep = hw;
   return STS_OK;
 }
 
@@ -286,7 +249,7 @@ int sts_ctx::step_host(int n, int* done) {
     for (int outer = 0; outer < NI; outer++) {
       if (fast()) k_assemble_fast<<<grid, block, 0, s>>>(g, 0, 0);
       else k_assemble<<<grid, block, 0, s>>>(g, 0, 0);
-      if (int r = sweep_loop([](int) {}, 4)) return r;
+      if (int r = pt_loop()) return r;
       k_correct<<<grid, block, 0, s>>>(g);
       k_face_rho<<<grid, block, 0, s>>>(g);
       boundary_step([](int) {});
@@ -308,8 +271,8 @@ int sts_ctx::step_host(int n, int* done) {
 }
 
 // The launch loop with a CUDA event pair around every kernel: per-kernel device time.
-// kinds: 0 step_begin, 1 assemble, 2 sweep (FP64), 3 correct, 4 face_rho, 5 boundary,
-// 6 flux_diff, 7 step_end, 8 FP32 sweep (with the FP64 re-forming of the iterate)
+// kinds: 0 step_begin, 1 assemble, 2 sweep loop, 3 correct, 4 face_rho, 5 boundary,
+// 6 flux_diff, 7 step_end
 int sts_ctx::profile(int n, double* ms, int* cnt, int* done) {
   const int NI = (int)hc.cfg.n("N_I");
   std::vector<cudaEvent_t> ev;
@@ -330,8 +293,9 @@ int sts_ctx::profile(int n, double* ms, int* cnt, int* done) {
       if (fast()) k_assemble_fast<<<grid, block, 0, s>>>(g, 0, 0);
       else k_assemble<<<grid, block, 0, s>>>(g, 0, 0);
       mark(1);
-      // the sweep count of this outer iteration is only known afterwards: launch one at a time
-      if (int r = sweep_loop(mark, 1)) return r;
+      mark(-1);
+      if (int r = pt_loop()) return r;
+      mark(2);
       mark(-1); k_correct<<<grid, block, 0, s>>>(g); mark(3);
       mark(-1); k_face_rho<<<grid, block, 0, s>>>(g); mark(4);
       boundary_step(mark);
@@ -714,6 +678,7 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
 
   c->block = dim3(32, 8);
   c->grid = dim3((h.Nx + 31) / 32, (h.Ny + 7) / 8);
+  if (int r = c->size_pt_grid()) return r;
   const dim3 G = c->grid, B = c->block;
   cudaStream_t s = c->s;
 
@@ -779,7 +744,11 @@ int sts_step(sts_ctx* ctx, int nsteps, int* steps_done) {
     int r = ctx->opt.use_graph ? ctx->step_graph(nsteps, &done) : ctx->step_host(nsteps, &done);
     if (r) return r;
     if (!ctx->h_ctl->continue_step) ctx->finished = true;
-    if (ctx->h_ctl->status & ~status_before & 1u) {
+    if (ctx->h_ctl->status & ST_BARRIER_TIMEOUT) {
+      ctx->finished = true;  // the device state is no longer consistent
+      return fail(STS_ERR_CUDA, "a grid barrier of the sweep loop timed out");
+    }
+    if (ctx->h_ctl->status & ~status_before & ST_NONFINITE) {
       if (steps_done) *steps_done = done;
       return fail(STS_ERR_NONFINITE, "a residual became NaN or Inf");
     }
@@ -816,6 +785,10 @@ int sts_profile_steps(sts_ctx* ctx, int nsteps, double* kernel_ms, int* kernel_l
     for (int q = 0; q < kProfileKinds; q++) { kernel_ms[q] = 0; kernel_launches[q] = 0; }
   } else if (int r = ctx->profile(nsteps, kernel_ms, kernel_launches, &done)) {
     return r;
+  }
+  if (ctx->h_ctl->status & ST_BARRIER_TIMEOUT) {
+    ctx->finished = true;
+    return fail(STS_ERR_CUDA, "a grid barrier of the sweep loop timed out");
   }
   if (!ctx->h_ctl->continue_step) ctx->finished = true;
   if (steps_done) *steps_done = done;

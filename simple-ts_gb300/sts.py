@@ -30,7 +30,7 @@ EXPORTS = [
     "sts_pt_sweeps_noalloc",
 ]
 
-KERNELS = ["step_begin", "assemble", "sweep", "correct", "face_rho", "boundary", "flux_diff", "step_end", "sweep32"]
+KERNELS = ["step_begin", "assemble", "sweep_loop", "correct", "face_rho", "boundary", "flux_diff", "step_end"]
 
 # precision modes of sts_options.precision
 EXACT, FAST_FP64, MIXED = 0, 1, 2

@@ -101,6 +101,23 @@ def test_full_size_channel_matches_oracle(lib_built, oracle_built):
         np.testing.assert_array_equal(g.sweep_history(), o.sweeps())
 
 
+@pytest.mark.parametrize("which,steps", [("channel_2048", 2), ("channel_ma2.43", 3)])
+def test_large_meshes_match_oracle(which, steps, lib_built, oracle_built):
+    """Meshes with more 32x8 tiles than resident CTAs (the sweep loop's CTAs take several tiles)."""
+    import ora
+    import sts
+    case = sc.config_case(which, Nt=steps)
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        o = ora.Oracle(d, fixed_sweeps=False)
+        g = sts.Solver(d, fixed_sweeps=False)
+        assert g.step(steps) == o.step(steps) == steps
+        for f in ("u", "v", "p", "T", "rho"):
+            np.testing.assert_array_equal(g.field(f), o.field(f), err_msg=f)
+        np.testing.assert_array_equal(g.sweep_history(), o.sweeps())
+        g.close()
+
+
 def test_nonfinite_residual_is_reported(lib_built):
     import sts
     case = sc.channel_case("c", 40, 6, 0.3, 0.002, 1e-3, 10)
