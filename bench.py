@@ -42,9 +42,10 @@ BYTES_PER_CELL = {
     "step_begin": 10 * 8,
 }
 
-# DRAM bytes per launch measured by ncu on this workload (dram__bytes_read.sum +
-# dram__bytes_write.sum); None where no capture was taken
-TRAFFIC = {}
+# DRAM bytes per launch measured by ncu on this workload, FP64 path (dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch of the second time step, cold cache); None where no
+# capture was taken
+TRAFFIC = {"assemble": 20981504 + 768, "sweep_loop": 18981888 + 27648}
 
 
 def parse():

@@ -158,6 +158,13 @@ int sts_pt_sweeps(const sts_sweep_fields* f, int max_sweeps, int fixed_sweeps, d
 int sts_pt_sweeps_noalloc(const sts_sweep_fields* f, int max_sweeps, int fixed_sweeps, double tol_p, double tol_T,
                           void* stream, int* sweeps_done, double* res_p, double* res_T);
 
+/* Self-check of the library's division through correctly rounded reciprocals (used by the FP64
+ * kernels for divisors fixed by the mesh or by the outer iteration; Markstein's method) against
+ * IEEE division on `device`: n pseudo-random operand pairs from `seed`, *mismatches receives the
+ * number of results that differ in any bit (0 is the only passing answer).  No counterpart in
+ * the reference, which divides with the host's IEEE division. */
+int sts_check_division(unsigned long long n, unsigned long long seed, int device, unsigned long long* mismatches);
+
 /* Host-only inspection of a case directory (no device use): dims, obstacle ids
  * (vol_inf_fb, Nx*Ny), per-cell classes (Nx*Ny bytes: bits 0-1 u, 2-3 v, 4-5 p/T with
  * 0 unsolved, 1 interior, 2 boundary; bit 6 fluid) and the mesh (hx, x_v: Nx; hy, y_v: Ny).

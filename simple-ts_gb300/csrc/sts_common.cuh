@@ -91,17 +91,13 @@ struct Ctl {
   unsigned int continue_iter, continue_step;
   unsigned int steps_left; // multi-step graph launches count down here
   unsigned int block_count;  // last-block detection
-  unsigned int status;     // bit 0: non-finite residual seen
+  unsigned int status;     // ST_* bits
   unsigned int step_sweeps;  // sum of sweeps in the current step
   // per-step record (ring of the last 4096 steps)
   unsigned int hist_n;
   unsigned int hist_sweeps[4096];
-  // mixed-precision sweep loop
-  unsigned int ecur;          // which correction buffer holds the current FP32 iterate
-  unsigned int base;          // FP64 buffer holding the base iterate of the FP32 corrections
-  unsigned int confirm_fail;  // FP64 re-evaluation of the last FP32 sweep missed the tolerance
-  unsigned int sweeps32;      // FP32 sweeps taken in this run (statistics)
-  unsigned int stop32;        // the FP32 loop of this outer iteration met the stop rule
+  // mixed-precision sweep loop statistics
+  unsigned int sweeps32;      // FP32 sweeps taken in this run
   // persistent sweep loops: grid barrier and per-sweep residual maxima (three slots used in
   // rotation; all zero between launches)
   unsigned int bar_count, bar_gen;
@@ -137,19 +133,19 @@ struct Geo {
   double *u, *v, *u_pr, *v_pr, *p[2], *T[2], *p_pr, *T_pr, *rho, *rho_pr, *sqrt_T, *rho_u, *rho_v;
   double *Fx, *Fy, *D_ux, *D_uy, *D_vx, *D_vy, *DTx, *DTy, *Gamma_xf, *Gamma_yf;
   double *u_pseudo, *v_pseudo, *d12, *d34, *apx, *apy, *bpx, *bpy, *ScT1, *Tw_u, *Tw_v;
-  double* inv[8];  // loop-invariant parts of the sweep, written by the first sweep of an outer iteration
+  double* inv[9];  // loop-invariant parts of the sweep, written by the first sweep of an outer iteration
   Ctl* ctl;
-  // --- mixed-precision path (precision mode 1 and 2) ---
-  // reciprocals of the mesh sums the assembly divides by (1/hx, 1/hy, 1/(hx[i-1]+hx[i]),
-  // 1/(hx[i]+hx[i+1]), the same in y), and 1/ht
-  const double *rhx, *rhy, *rxx_m, *rxx_p, *ryy_m, *ryy_p;
-  double rht;
+  // correctly rounded reciprocals of the mesh quantities the kernels divide by: 1/hx, 1/hy,
+  // 1/(hx[i-1]+hx[i]), 1/(hx[i]+hx[i+1]), the same in y, 1/(3 hx), 1/(3 hy), 1/ht and 1/3
+  const double *rhx, *rhy, *rxx_m, *rxx_p, *ryy_m, *ryy_p, *r3x, *r3y;
+  double rht, r3;
+  // --- precision modes 1 and 2 ---
   // FP32 correction sweeps: coefficients c[0..4] of the T correction, a[0..3] of the p
   // numerator, the base-sweep values T1, q, Den and the first defects dT, dp; e_p/e_T are the
-  // double-buffered corrections (index ectl)
+  // double-buffered corrections
   float *c32[5], *a32[4], *T1, *q1, *den1, *dT, *dp;
   float *ep[2], *eT[2];
-  int precision;  // 0 bit-exact FP64, 1 FP64 with reciprocal/FMA assembly, 2 = 1 + FP32 correction sweeps
+  int precision;  // 0 bit-exact FP64, 1 FP64 with reciprocal/FMA arithmetic, 2 = 1 + FP32 correction sweeps
 };
 
 // Neighbour indices of one cell: ij_function / ij_function_PeriodicBC (SIMPLE_TS_MPI.cpp:140-232).

@@ -20,6 +20,25 @@ __device__ __forceinline__ double Hi(double f1, double f2, double h1, double h2)
 __device__ __forceinline__ double as_d(unsigned long long b) { return __longlong_as_double((long long)b); }
 __device__ __forceinline__ unsigned long long as_b(double d) { return (unsigned long long)__double_as_longlong(d); }
 
+// Correctly rounded a / b from y = RN(1/b), the division by a correctly rounded reciprocal of
+// P. Markstein (IBM J. Res. Develop. 34(1), 1990; Muller et al., Handbook of Floating-Point
+// Arithmetic, 2nd ed., sec. 4.9): q0 = RN(a y) is within two units in the last place of a/b;
+// one correction with the fused remainder makes it faithful, and for a faithful q the remainder
+// r = a - b q is exact and RN(q + r y) = RN(a / b).  Valid when nothing overflows or underflows:
+// operands outside 2^-900 <= |a| <= 2^900 or 2^-100 <= |b| <= 2^100 (zeros, subnormals,
+// infinities and NaN included) take the IEEE division instead.  Explicit _rn intrinsics, so the
+// result does not depend on the file's contraction flags.
+__device__ __forceinline__ double div_cr(double a, double b, double y) {
+  const unsigned ea = ((unsigned)__double2hiint(a) >> 20) & 0x7ffu;
+  const unsigned eb = ((unsigned)__double2hiint(b) >> 20) & 0x7ffu;
+  if (ea - 123u > 1800u || eb - 923u > 200u) return __ddiv_rn(a, b);
+  double q = __dmul_rn(a, y);
+  double r = __fma_rn(-b, q, a);
+  q = __fma_rn(r, y, q);
+  r = __fma_rn(-b, q, a);
+  return __fma_rn(r, y, q);
+}
+
 constexpr int kMaxColumn = 1024;  // rows staged in shared memory by the inflow-column reductions
 
 // Running maximum that ignores NaN exactly like "if (m < fabs(r)) m = fabs(r)".

@@ -204,7 +204,9 @@ __global__ void k_assemble(Geo g, unsigned long long h_sweep, int in_graph) {
 // Invariants: a_k = aT_k, or aT_k * T_wall for a wall neighbour (the bc form multiplies the
 // wall temperature by aT_k and adds exact zeros), divu, the T denominator, the p_pr/T_pr
 // term and ht * (sum of the p coefficients).
-template <bool FIRST>
+// RCP: the first sweep also stores RN(1/den_T) in inv[8] and later sweeps divide by den_T through
+// it (div_cr, the same bits as the IEEE quotient).
+template <bool FIRST, bool RCP = false>
 __device__ __forceinline__ void sweep_cell(const Geo& g, const Cell& c, const double* __restrict__ P,
                                            const double* __restrict__ TT, double* __restrict__ pn,
                                            double* __restrict__ Tn, double& rp, double& rT) {
@@ -264,6 +266,7 @@ __device__ __forceinline__ void sweep_cell(const Geo& g, const Cell& c, const do
     g.inv[5][ij] = denT;
     g.inv[6][ij] = pc;
     g.inv[7][ij] = sa;
+    if (RCP) g.inv[8][ij] = 1.0 / denT;
     double num = apx[d.ij] * P[d.i_1j] + apx[d.i1j] * P[d.i1j] + apy[d.ij] * P[d.ij_1] + apy[d.ij1] * P[d.ij1] +
                  g.bpx[d.ij] - g.bpx[d.i1j] + g.bpy[d.ij] - g.bpy[d.ij1];
     if (co == CLS_BC) {
@@ -286,7 +289,8 @@ __device__ __forceinline__ void sweep_cell(const Geo& g, const Cell& c, const do
       t3 = w3 * TT[d.ij_1];
       t4 = w4 * TT[d.ij1];
     }
-    Tnew = (ht * (t1 + t2 + t3 + t4 + (1.0 - g.gamma1) * P[d.ij] * g.inv[4][ij]) + g.ScT1[d.ij]) / g.inv[5][ij];
+    const double X = ht * (t1 + t2 + t3 + t4 + (1.0 - g.gamma1) * P[d.ij] * g.inv[4][ij]) + g.ScT1[d.ij];
+    Tnew = RCP ? div_cr(X, g.inv[5][ij], g.inv[8][ij]) : X / g.inv[5][ij];
     double num = apx[d.ij] * P[d.i_1j] + apx[d.i1j] * P[d.i1j] + apy[d.ij] * P[d.ij_1] + apy[d.ij1] * P[d.ij1] +
                  g.bpx[d.ij] - g.bpx[d.i1j] + g.bpy[d.ij] - g.bpy[d.ij1];
     if (co == CLS_BC) {
@@ -363,8 +367,8 @@ __global__ void __launch_bounds__(256) k_pt_loop(Geo g) {
       const Cell c = tile_cell(g, t, tx);
       if (!c.ok) continue;
       double a = 0, b = 0;
-      if (n == 0) sweep_cell<true>(g, c, P, TT, pn, Tn, a, b);
-      else sweep_cell<false>(g, c, P, TT, pn, Tn, a, b);
+      if (n == 0) sweep_cell<true, true>(g, c, P, TT, pn, Tn, a, b);
+      else sweep_cell<false, true>(g, c, P, TT, pn, Tn, a, b);
       if (a != a || b != b) atomicOr(&ctl->status, ST_NONFINITE);  // the max below skips NaN
       rp = mx(rp, a);
       rT = mx(rT, b);
@@ -446,43 +450,54 @@ __device__ __forceinline__ void flux_diff_cell(const Geo& g, const Cell& c) {
   const bool b_ws = cls_fluid(g.cls[d.i_1j_1]), b_s = cls_fluid(g.cls[d.ij_1]), b_w = cls_fluid(g.cls[d.i_1j]),
              b_p = cls_fluid(g.cls[d.ij]);
   const int jm = j - (0 < j ? 1 : 0);
+  // divisions by mesh sums through their correctly rounded reciprocals (same bits as IEEE):
+  // a divisor (m1 h1 + m2 h2) with masks m is h1, h2 or the rounded sum
+  const double ry = g.ryy_m[j], rx = g.rxx_m[i];
+  auto LiY = [&](double f1, double f2) { return div_cr(f1 * hy[j] + f2 * hy[jm], hy[jm] + hy[j], ry); };
+  auto LiX = [&](double f1, double f2) { return div_cr(f1 * hx[i] + f2 * hx[d.i_1], hx[d.i_1] + hx[i], rx); };
+  auto rsum = [](bool a, bool b, double r_both, double r_a, double r_b) { return a ? (b ? r_both : r_a) : r_b; };
   double Gy = g.Gamma_yf[d.ij], Gx = g.Gamma_xf[d.ij];
   if (b_ws && b_s && b_w && b_p) {
-    Gy = 0.5 * (Li(sT[d.i_1j_1], sT[d.i_1j], hy[jm], hy[j]) + Li(sT[d.ij_1], sT[d.ij], hy[jm], hy[j]));
+    Gy = 0.5 * (LiY(sT[d.i_1j_1], sT[d.i_1j]) + LiY(sT[d.ij_1], sT[d.ij]));
   } else if (b_ws || b_s || b_w || b_p) {
-    Gy = 0.5 * ((double)(b_ws && b_w) * Li(sT[d.i_1j_1], sT[d.i_1j], hy[jm], hy[j]) +
+    Gy = 0.5 * ((double)(b_ws && b_w) * LiY(sT[d.i_1j_1], sT[d.i_1j]) +
                 (double)(b_ws != b_w) * sqrt(Tw_v[d.i_1j]) +
-                (double)(b_s && b_p) * Li(sT[d.ij_1], sT[d.ij], hy[jm], hy[j]) + (double)(b_s != b_p) * sqrt(Tw_v[d.ij]) +
-                (double)((!(b_ws && b_w)) || (!(b_s && b_p))) * Li(sqrt(Tw_u[d.ij_1]), sqrt(Tw_u[d.ij]), hy[jm], hy[j]));
+                (double)(b_s && b_p) * LiY(sT[d.ij_1], sT[d.ij]) + (double)(b_s != b_p) * sqrt(Tw_v[d.ij]) +
+                (double)((!(b_ws && b_w)) || (!(b_s && b_p))) * LiY(sqrt(Tw_u[d.ij_1]), sqrt(Tw_u[d.ij])));
   }
   g.Gamma_yf[d.ij] = Gy;
-  g.D_ux[d.ij] = cT * sT[d.i_1j] * (hy[j] / hx[d.i_1]);
+  g.D_ux[d.ij] = cT * sT[d.i_1j] * div_cr(hy[j], hx[d.i_1], g.rhx[d.i_1]);
   if ((b_p && b_w) || (b_s && b_ws))
-    g.D_uy[d.ij] = cT * Gy * ((hx[i] + hx[d.i_1]) / ((double)(b_p * b_w) * hy[j] + (double)(b_s * b_ws) * hy[jm]));
+    g.D_uy[d.ij] = cT * Gy * div_cr(hx[i] + hx[d.i_1], (double)(b_p * b_w) * hy[j] + (double)(b_s * b_ws) * hy[jm],
+                                    rsum(b_p && b_w, b_s && b_ws, ry, g.rhy[j], g.rhy[jm]));
   else
     g.D_uy[d.ij] = 0;
   if (b_ws && b_s && b_w && b_p) {
-    Gx = 0.5 * (Li(sT[d.i_1j_1], sT[d.ij_1], hx[d.i_1], hx[i]) + Li(sT[d.i_1j], sT[d.ij], hx[d.i_1], hx[i]));
+    Gx = 0.5 * (LiX(sT[d.i_1j_1], sT[d.ij_1]) + LiX(sT[d.i_1j], sT[d.ij]));
   } else if (b_ws || b_s || b_w || b_p) {
-    Gx = 0.5 * ((double)(b_ws && b_s) * Li(sT[d.i_1j_1], sT[d.ij_1], hx[d.i_1], hx[i]) +
+    Gx = 0.5 * ((double)(b_ws && b_s) * LiX(sT[d.i_1j_1], sT[d.ij_1]) +
                 (double)(b_ws != b_s) * sqrt(Tw_u[d.ij_1]) +
-                (double)(b_w && b_p) * Li(sT[d.i_1j], sT[d.ij], hx[d.i_1], hx[i]) + (double)(b_w != b_p) * sqrt(Tw_u[d.ij]) +
-                (double)((!(b_ws && b_s)) || (!(b_w && b_p))) * Li(sqrt(Tw_v[d.i_1j]), sqrt(Tw_v[d.ij]), hx[d.i_1], hx[i]));
+                (double)(b_w && b_p) * LiX(sT[d.i_1j], sT[d.ij]) + (double)(b_w != b_p) * sqrt(Tw_u[d.ij]) +
+                (double)((!(b_ws && b_s)) || (!(b_w && b_p))) * LiX(sqrt(Tw_v[d.i_1j]), sqrt(Tw_v[d.ij])));
   }
   g.Gamma_xf[d.ij] = Gx;
   if ((b_p && b_s) || (b_w && b_ws))
-    g.D_vx[d.ij] = cT * Gx * ((hy[j] + hy[jm]) / ((double)(b_p * b_s) * hx[i] + (double)(b_w * b_ws) * hx[d.i_1]));
+    g.D_vx[d.ij] = cT * Gx * div_cr(hy[j] + hy[jm], (double)(b_p * b_s) * hx[i] + (double)(b_w * b_ws) * hx[d.i_1],
+                                    rsum(b_p && b_s, b_w && b_ws, rx, g.rhx[i], g.rhx[d.i_1]));
   else
     g.D_vx[d.ij] = 0;
-  g.D_vy[d.ij] = cT * sT[d.ij_1] * (hx[i] / hy[jm]);
+  g.D_vy[d.ij] = cT * sT[d.ij_1] * div_cr(hx[i], hy[jm], g.rhy[jm]);
+  // 1 / (0.5 s) = 2 (1 / s) exactly
   if (b_p || b_w)
-    g.DTx[d.ij] = cT1 * (hy[j] / (0.5 * ((double)b_p * hx[i] + (double)b_w * hx[d.i_1]))) *
+    g.DTx[d.ij] = cT1 * div_cr(hy[j], 0.5 * ((double)b_p * hx[i] + (double)b_w * hx[d.i_1]),
+                               2.0 * rsum(b_p, b_w, rx, g.rhx[i], g.rhx[d.i_1])) *
                   ((double)((!b_p) || (!b_w)) * sqrt(Tw_u[d.ij]) +
                    (double)(b_p * b_w) * Hi(sT[d.i_1j], sT[d.ij], hx[d.i_1], hx[i]));
   else
     g.DTx[d.ij] = 0;
   if (b_p || b_s)
-    g.DTy[d.ij] = cT1 * (hx[i] / (0.5 * ((double)b_p * hy[j] + (double)b_s * hy[jm]))) *
+    g.DTy[d.ij] = cT1 * div_cr(hx[i], 0.5 * ((double)b_p * hy[j] + (double)b_s * hy[jm]),
+                               2.0 * rsum(b_p, b_s, ry, g.rhy[j], g.rhy[jm])) *
                   ((double)((!b_p) || (!b_s)) * sqrt(Tw_v[d.ij]) +
                    (double)(b_p * b_s) * Hi(sT[d.ij_1], sT[d.ij], hy[jm], hy[j]));
   else
@@ -983,6 +998,48 @@ __global__ void k_step_end(Geo g, unsigned long long h_step, int in_graph) {
     if (in_graph)
       cudaGraphSetConditional((cudaGraphConditionalHandle)h_step, (ctl->steps_left > 0 && ctl->continue_step) ? 1 : 0);
   }
+}
+
+}  // namespace sts
+
+namespace sts {
+
+// Self-check of div_cr against the IEEE quotient on n pseudo-random operand pairs (a splitmix64
+// stream from `seed`): random signs and significands, dividend exponents over 2^-920..2^920 (so
+// some pairs take the IEEE fallback), divisor exponents over 2^-110..2^110, one divisor in eight
+// with an all-ones significand, and every fourth dividend formed as a rounded product q*b so
+// that the quotient is exact or within an ulp of a representable number.  Counts the pairs whose
+// results differ in any bit.
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long& s) {
+  unsigned long long z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ double make_double(unsigned long long bits, int exp_lo, int exp_hi, bool all_ones) {
+  const unsigned long long mant = all_ones ? 0xFFFFFFFFFFFFFull : (bits & 0xFFFFFFFFFFFFFull);
+  const int span = exp_hi - exp_lo + 1;
+  const int e = exp_lo + (int)((bits >> 52) % (unsigned long long)span);
+  const unsigned long long sign = (bits >> 63) << 63;
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 1023) << 52) | mant));
+}
+
+__global__ void k_check_division(unsigned long long n, unsigned long long seed, unsigned long long* bad) {
+  unsigned long long local = 0;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n; k += stride) {
+    unsigned long long st = seed ^ (k * 0xD1B54A32D192ED03ull);
+    const unsigned long long r1 = splitmix64(st), r2 = splitmix64(st), r3 = splitmix64(st);
+    const double b = make_double(r2, -110, 110, (r3 & 7) == 0);
+    double a = make_double(r1, -920, 920, false);
+    if (((r3 >> 3) & 3) == 0) a = __dmul_rn(make_double(r1, -700, 700, false), b);
+    const double y = __ddiv_rn(1.0, b);
+    const double q1 = div_cr(a, b, y), q2 = __ddiv_rn(a, b);
+    if (__double_as_longlong(q1) != __double_as_longlong(q2)) local++;
+  }
+  for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+  if ((threadIdx.x & 31) == 0 && local) atomicAdd(bad, local);
 }
 
 }  // namespace sts

@@ -28,6 +28,8 @@ __global__ void k_sweep_first(Geo g, unsigned long long h_sweep, int in_graph);
 __global__ void k_sweep(Geo g, unsigned long long h_sweep, int in_graph);
 // the whole sweep loop of an outer iteration in one cooperative launch (grid <= resident CTAs)
 __global__ void k_pt_loop(Geo g);
+// self-check of the correctly rounded division by a reciprocal against IEEE division
+__global__ void k_check_division(unsigned long long n, unsigned long long seed, unsigned long long* bad);
 // precision modes 1 and 2
 __global__ void k_assemble_fast(Geo g, unsigned long long h_sweep, int in_graph);
 __global__ void k_flux_diff_fast(Geo g, unsigned tail);

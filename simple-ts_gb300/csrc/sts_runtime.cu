@@ -616,35 +616,39 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
                        &g.apy, &g.bpx, &g.bpy, &g.ScT1, &g.Tw_u, &g.Tw_v};
   for (double** f : fields)
     if (int r = c->alloc(f, Na)) return r;
-  for (int k = 0; k < 8; k++)
+  for (int k = 0; k < 9; k++)
     if (int r = c->alloc(&g.inv[k], Na)) return r;
   g.precision = opt.precision;
-  g.rht = 1.0 / g.ht;
-  if (g.precision >= 1) {
-    // reciprocals of the mesh widths and of the two-cell sums the assembly and the diffusion
-    // terms divide by; the neighbour indices are those of the kernels (periodic wrap in x, the
-    // y index above compared with Nx as in the reference's ScT1 code, clamped to the mesh)
+  {
+    // correctly rounded reciprocals (IEEE division here) of the mesh quantities the kernels
+    // divide by; the neighbour indices are those of the kernels (periodic wrap in x, the y index
+    // above compared with Nx as in the reference's ScT1 code, clamped to the mesh)
     const int Nx = h.Nx, Ny = h.Ny;
-    std::vector<double> rhx(Nx), rxm(Nx), rxp(Nx), rhy(Ny), rym(Ny), ryp(Ny);
+    std::vector<double> rhx(Nx), rxm(Nx), rxp(Nx), r3x(Nx), rhy(Ny), rym(Ny), ryp(Ny), r3y(Ny);
     for (int i = 0; i < Nx; i++) {
       const Nb d = neighbours(i, 0, Nx, Ny, h.bits & F_PERIODIC);
       rhx[i] = 1.0 / h.hx[i];
       rxm[i] = 1.0 / (h.hx[d.i_1] + h.hx[i]);
       rxp[i] = 1.0 / (h.hx[i] + h.hx[d.i1]);
+      r3x[i] = 1.0 / (h.hx[i] * 3.0);
     }
     for (int j = 0; j < Ny; j++) {
       const int jm = j - (0 < j ? 1 : 0), jp = std::min(j + (j < Nx - 1 ? 1 : 0), Ny - 1);
       rhy[j] = 1.0 / h.hy[j];
       rym[j] = 1.0 / (h.hy[jm] + h.hy[j]);
       ryp[j] = 1.0 / (h.hy[j] + h.hy[jp]);
+      r3y[j] = 1.0 / (h.hy[j] * 3.0);
     }
-    double* t[6];
-    const std::vector<double>* src[6] = {&rhx, &rhy, &rxm, &rxp, &rym, &ryp};
-    for (int k = 0; k < 6; k++) {
+    double* t[8];
+    const std::vector<double>* src[8] = {&rhx, &rhy, &rxm, &rxp, &rym, &ryp, &r3x, &r3y};
+    for (int k = 0; k < 8; k++) {
       if (int r = c->alloc(&t[k], src[k]->size())) return r;
       if (int r = c->upload(t[k], *src[k])) return r;
     }
     g.rhx = t[0]; g.rhy = t[1]; g.rxx_m = t[2]; g.rxx_p = t[3]; g.ryy_m = t[4]; g.ryy_p = t[5];
+    g.r3x = t[6]; g.r3y = t[7];
+    g.rht = 1.0 / g.ht;
+    g.r3 = 1.0 / 3.0;
   }
   if (g.precision == 2) {
     float** f32[] = {&g.c32[0], &g.c32[1], &g.c32[2], &g.c32[3], &g.c32[4], &g.a32[0], &g.a32[1], &g.a32[2], &g.a32[3],
@@ -999,6 +1003,22 @@ int sts_inspect_case(const char* case_dir, int* Nx, int* Ny, unsigned int* vol_o
   if (hy_out) std::memcpy(hy_out, h.hy.data(), sizeof(double) * h.Ny);
   if (xv_out) std::memcpy(xv_out, h.x_v.data(), sizeof(double) * h.Nx);
   if (yv_out) std::memcpy(yv_out, h.y_v.data(), sizeof(double) * h.Ny);
+  return STS_OK;
+}
+
+int sts_check_division(unsigned long long n, unsigned long long seed, int device, unsigned long long* mismatches) {
+  if (!mismatches) return fail(STS_ERR_ARG, "null argument");
+  CU(cudaSetDevice(device));
+  unsigned long long* d = nullptr;
+  CU(cudaMalloc(&d, sizeof(unsigned long long)));
+  cudaError_t e = cudaMemset(d, 0, sizeof(unsigned long long));
+  if (e == cudaSuccess) {
+    k_check_division<<<1216, 256>>>(n, seed, d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(mismatches, d, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(STS_ERR_CUDA, std::string("sts_check_division: ") + cudaGetErrorString(e));
   return STS_OK;
 }
 

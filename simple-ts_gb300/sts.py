@@ -27,7 +27,7 @@ EXPORTS = [
     "sts_default_options", "sts_open_case", "sts_step", "sts_get_field", "sts_set_field", "sts_dims",
     "sts_stats", "sts_sweep_history", "sts_write_outputs", "sts_run_case", "sts_sync", "sts_destroy",
     "sts_last_error", "sts_inspect_case", "sts_step_timed", "sts_profile_steps", "sts_pt_sweeps",
-    "sts_pt_sweeps_noalloc",
+    "sts_pt_sweeps_noalloc", "sts_check_division",
 ]
 
 KERNELS = ["step_begin", "assemble", "sweep_loop", "correct", "face_rho", "boundary", "flux_diff", "step_end"]
@@ -252,3 +252,12 @@ def pt_sweeps_noalloc(fields: SweepFields, max_sweeps: int, fixed_sweeps: bool, 
     _check(lib.sts_pt_sweeps_noalloc(C.byref(fields), int(max_sweeps), int(fixed_sweeps), float(tol_p),
                                      float(tol_T), C.c_void_p(stream), C.byref(n), C.byref(rp), C.byref(rT)))
     return n.value, rp.value, rT.value
+
+
+def check_division(n: int, seed: int = 1, device: int = 0) -> int:
+    """Pairs (of n) where the library's reciprocal-based division differs from IEEE division."""
+    lib = load()
+    lib.sts_check_division.argtypes = [C.c_ulonglong, C.c_ulonglong, C.c_int, C.POINTER(C.c_ulonglong)]
+    out = C.c_ulonglong()
+    _check(lib.sts_check_division(int(n), int(seed), int(device), C.byref(out)))
+    return out.value
