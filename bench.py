@@ -245,12 +245,71 @@ def launches_per_step(kcnt, pn):
     return sum(kcnt.values()) / max(pn, 1)
 
 
+def batch_bench(args):
+    """The 64-case batch (nx ~ U{200..800}, ny = nx/10, Mach, Kn and square position drawn
+    with seed 20261204): all cases advance together, one launch per kernel and step.  Prints a
+    JSON line of the same shape as the main bench (no e2e, no CPU baseline)."""
+    import numpy as np
+    import torch
+    import sts
+    import sts_cases as sc
+    import build as stsbuild
+    stsbuild.build()
+    cases = sc.batch_cases(n=64, Nt=10 ** 7)
+    root = tempfile.mkdtemp(prefix="sts_batch_")
+    dirs = []
+    for k, c in enumerate(cases):
+        d = os.path.join(root, f"c{k:02d}")
+        os.makedirs(d)
+        c.write(d)
+        dirs.append(d)
+    flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")
+    out = {}
+    base = None
+    for name, prec in (("fp64_exact", sts.EXACT), ("fp64_fast", sts.FAST_FP64), ("fp32_corrections", sts.MIXED)):
+        b = sts.Batch(dirs, fixed_sweeps=False, precision=prec)
+        cells = sum(c.Nx * c.Ny for c in b.cases)
+        for _ in range(max(args.warmup, 3)):
+            b.step(1)
+        total, done = 0.0, 0
+        with Clocks(0) as clk:
+            for _ in range(args.steps):
+                flush.fill_(1.0)
+                torch.cuda.synchronize()
+                n, ms = b.step_timed(1)
+                total += ms
+                done += n
+        fields = {f: np.concatenate([c.field(f).ravel() for c in b.cases]) for f in ("u", "v", "p", "T", "rho")}
+        sweeps = np.concatenate([c.sweep_history()[-done:] for c in b.cases])
+        r = {"value": cells * done / (total / 1e3), "ms_per_step": total / max(done, 1),
+             "sweeps_per_step": float(np.mean(sweeps)), "clocks": clk.summary()}
+        if base is None:
+            base = fields
+        else:
+            r["rel_l2_vs_fp64"] = {f: float(np.linalg.norm(fields[f] - base[f]) / np.linalg.norm(base[f]))
+                                   for f in fields}
+        out[name] = r
+        b.close()
+    head = out["fp64_exact"]
+    line = {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": head["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "batch of 64 channel cases, nx ~ U{200..800}, ny = nx/10, seed 20261204",
+                       "cells_per_step": cells, "residual_tolerance": 1e-8,
+                       "l2": "flushed before every timed step (256 MiB write)"},
+            "clocks": head["clocks"], "variants": {k: v for k, v in out.items() if k != "fp64_exact"},
+            "sweeps_per_step": head["sweeps_per_step"]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return reference_arm(args)
     if args.profile_target:
         return profile_target(args)
+    if args.workload == "batch64":
+        return batch_bench(args)
     rank, world, local = dist_env()
     import numpy as np
     import torch

@@ -165,6 +165,31 @@ int sts_pt_sweeps_noalloc(const sts_sweep_fields* f, int max_sweeps, int fixed_s
  * the reference, which divides with the host's IEEE division. */
 int sts_check_division(unsigned long long n, unsigned long long seed, int device, unsigned long long* mismatches);
 
+/* Batches: many independent cases advanced together on one GPU.  Every kernel of a step is
+ * launched once for all cases and the p-T sweep loops of all cases run in one cooperative
+ * launch, each case with its own stop rule; the step loop is one CUDA graph.  The reference
+ * runs one case per process (or per MPI job); a batch is the GB300 form of running many such
+ * jobs side by side, with the same results as running each case alone.  Restrictions: at most
+ * 256 cases, N_I = 1 in every case, one sweep mode (opt->fixed_sweeps) and one precision for
+ * the whole batch.  opt->use_graph and opt->write_files are ignored (graph, no files). */
+typedef struct sts_batch sts_batch;
+int sts_open_batch(const char* const* case_dirs, int ncases, const sts_options* opt, sts_batch** out);
+
+/* Advances every case by up to nsteps time steps; a case whose run ended (Nt, steady-state stop)
+ * stays where it stopped.  *steps_done receives the most steps any case took. */
+int sts_batch_step(sts_batch* b, int nsteps, int* steps_done);
+
+/* sts_batch_step with a CUDA event pair around the work; *device_ms receives the device time. */
+int sts_batch_step_timed(sts_batch* b, int nsteps, int* steps_done, double* device_ms);
+
+/* The context of case `index` (borrowed: valid until sts_batch_destroy).  sts_get_field,
+ * sts_set_field, sts_dims, sts_stats, sts_sweep_history and sts_write_outputs work on it;
+ * sts_step and sts_profile_steps return STS_ERR_ARG, and sts_destroy leaves it to the batch. */
+int sts_batch_case(sts_batch* b, int index, sts_ctx** out);
+
+/* Releases the batch and its cases. */
+void sts_batch_destroy(sts_batch* b);
+
 /* Host-only inspection of a case directory (no device use): dims, obstacle ids
  * (vol_inf_fb, Nx*Ny), per-cell classes (Nx*Ny bytes: bits 0-1 u, 2-3 v, 4-5 p/T with
  * 0 unsolved, 1 interior, 2 boundary; bit 6 fluid) and the mesh (hx, x_v: Nx; hy, y_v: Ny).

@@ -98,11 +98,19 @@ struct Ctl {
   unsigned int hist_sweeps[4096];
   // mixed-precision sweep loop statistics
   unsigned int sweeps32;      // FP32 sweeps taken in this run
-  // persistent sweep loops: grid barrier and per-sweep residual maxima (three slots used in
-  // rotation; all zero between launches)
-  unsigned int bar_count, bar_gen;
+  unsigned int rebases;       // FP64 re-basings of the FP32 corrections in this run
+  // persistent sweep loop: per-sweep residual maxima (three slots used in rotation; all zero
+  // between launches)
   unsigned long long rb_p[3], rb_T[3];
-  unsigned int rebases;       // FP64 re-basings of the FP32 corrections in this run (statistics)
+  unsigned int running;       // the case takes part in the current step (batches; 1 otherwise)
+};
+
+// Most cases one batch may hold (the sweep loop keeps their state in shared memory).
+constexpr int kMaxBatchCases = 256;
+
+// Grid barrier and exit ticket of one persistent sweep-loop launch (one per context or batch).
+struct LoopCtl {
+  unsigned int bar_count, bar_gen, status, block_count;
 };
 
 // Bits of Ctl::status.

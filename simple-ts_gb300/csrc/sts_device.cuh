@@ -115,25 +115,25 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   return v;
 }
 
-// Grid-wide barrier on the counter/generation pair of the control block.  A CTA that waits
-// longer than kSpinLimit polls sets ST_BARRIER_TIMEOUT and returns false, so a launch whose
-// CTAs are not all resident ends with an error status instead of hanging.
-__device__ bool grid_barrier(Ctl* ctl) {
+// Grid-wide barrier on the counter/generation pair of a LoopCtl.  A CTA that waits longer than
+// kSpinLimit polls sets ST_BARRIER_TIMEOUT and returns false, so a launch whose CTAs are not all
+// resident ends with an error status instead of hanging.
+__device__ bool grid_barrier(LoopCtl* lc) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0 && threadIdx.y == 0) {
-    const unsigned g0 = ld_acquire(&ctl->bar_gen);
+    const unsigned g0 = ld_acquire(&lc->bar_gen);
     __threadfence();
     int good = 1;
-    if (atomicAdd(&ctl->bar_count, 1u) == gridDim.x * gridDim.y - 1) {
-      atomicExch(&ctl->bar_count, 0u);
+    if (atomicAdd(&lc->bar_count, 1u) == gridDim.x * gridDim.y - 1) {
+      atomicExch(&lc->bar_count, 0u);
       __threadfence();
-      atomicAdd(&ctl->bar_gen, 1u);
+      atomicAdd(&lc->bar_gen, 1u);
     } else {
       unsigned spins = 0;
-      while (ld_acquire(&ctl->bar_gen) == g0) {
+      while (ld_acquire(&lc->bar_gen) == g0) {
         if (++spins > kSpinLimit) {
-          atomicOr(&ctl->status, ST_BARRIER_TIMEOUT);
+          atomicOr(&lc->status, ST_BARRIER_TIMEOUT);
           good = 0;
           break;
         }
@@ -162,38 +162,120 @@ __device__ __forceinline__ Cell tile_cell(const Geo& g, int t, int tx) {
   return c;
 }
 
-// Folds a sweep's per-CTA residual maxima into slot n % 3, clears the slot sweep n+1 will use
-// (its last readers passed the barrier of sweep n-1 before this CTA could reach sweep n), meets
-// the other CTAs at the barrier and returns the sweep's global maxima.  False on a barrier timeout.
-__device__ __forceinline__ bool sweep_residual(Ctl* ctl, unsigned n, double rp, double rT, double& res_p,
-                                               double& res_T) {
-  const unsigned slot = n % 3, next = (n + 1) % 3;
-  block_max2(rp, rT, &ctl->rb_p[slot], &ctl->rb_T[slot], &ctl->status);
-  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
-    ctl->rb_p[next] = 0ull;
-    ctl->rb_T[next] = 0ull;
-  }
-  if (!grid_barrier(ctl)) return false;
-  res_p = ld_res(&ctl->rb_p[slot]);
-  res_T = ld_res(&ctl->rb_T[slot]);
-  return true;
-}
-
 // The reference's stop rule of the sweep loop (SIMPLE_TS_MPI.cpp:4087-4107), n sweeps taken.
 __device__ __forceinline__ bool sweep_continues(const Geo& g, unsigned n, double res_p, double res_T) {
   if (g.bits & F_FIXED_SWEEPS) return n < (unsigned)g.N_I_p_c;
   return (n < 2) || ((n < (unsigned)g.N_I_p_c) && ((g.MaxError_p_c < res_p) || (g.MaxError_T < res_T)));
 }
 
-// Bookkeeping of a finished loop by the last CTA to leave: current buffer, sweep counts, and
-// the residual slots cleared for the next launch.
-__device__ __forceinline__ void pt_loop_finish(Ctl* ctl, unsigned cur, unsigned n, unsigned I) {
-  if (last_block(&ctl->block_count)) {
-    ctl->cur = cur;
-    ctl->Iter_p_c = n;
+// Records the residuals of sweep n (1-based) of outer iteration I.
+__device__ __forceinline__ void record_residual(Ctl* ctl, unsigned n, unsigned I, double res_p, double res_T) {
+  ctl->res_p[I] = res_p;
+  ctl->res_T[I] = res_T;
+  if (n == 1) {
+    ctl->res_p0[I] = res_p;
+    ctl->res_T0[I] = res_T;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The persistent sweep loop of one or many cases.  Every case runs a small state machine
+// (LoopCase) whose passes -- a sweep, or for the FP32-correction loop also the re-forming of
+// an FP64 iterate -- all take one round.  In a round every CTA takes its share of the tiles of
+// all cases still running, folds the pass's residual maxima into the case's slot round % 3,
+// and meets the others at the grid barrier; then every CTA advances every case's state from
+// the same numbers, so all CTAs agree without further communication.  The loop ends when
+// every case has met its stop rule; the last CTA to leave writes the cases' loop results.
+// Ops supplies pass() (one cell of the current pass) and advance() (the state transition).
+// ---------------------------------------------------------------------------
+enum : unsigned char { PS_FIRST = 0, PS_SWEEP = 1, PS_SWEEP32 = 2, PS_MATERIALIZE = 3, PS_CONFIRM = 4, PS_DONE = 255 };
+
+struct LoopCase {
+  unsigned n;     // sweeps counted so far (the reference's Iter_p_c)
+  unsigned cur;   // FP64 buffer with the latest iterate
+  unsigned base;  // FP64 buffer with the base of the FP32 corrections
+  unsigned I;     // outer iteration (row of the residual records)
+  unsigned char phase, ec, active, pad;  // ec: correction buffer with the latest FP32 iterate
+};
+
+// SINGLE: one case whose Geo g0 is a kernel parameter (gs, tile_case, tile_first unused).
+template <class Ops, bool SINGLE>
+__device__ __forceinline__ void pt_loop_rounds(const Geo& g0, const Geo* __restrict__ gs,
+                                               const int* __restrict__ tile_case, const int* __restrict__ tile_first,
+                                               int ncases, int ntiles, LoopCtl* lc) {
+  auto G = [&](int c) -> const Geo& { return SINGLE ? g0 : gs[c]; };
+  __shared__ LoopCase sc[kMaxBatchCases];
+  __shared__ bool last;
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x, nthr = blockDim.x * blockDim.y;
+  const bool lead = blockIdx.x == 0 && blockIdx.y == 0;
+  for (int c = tid; c < ncases; c += nthr) {
+    const Ctl* ctl = G(c).ctl;
+    LoopCase s;
+    s.n = 0;
+    s.cur = ctl->cur;
+    s.base = s.cur;
+    s.I = ctl->Iter < 64 ? ctl->Iter : 63;
+    s.ec = 0;
+    s.active = ctl->running ? 1 : 0;
+    s.phase = s.active ? PS_FIRST : PS_DONE;
+    s.pad = 0;
+    sc[c] = s;
+  }
+  __syncthreads();
+  for (unsigned round = 0;; round++) {
+    const unsigned slot = round % 3;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const int c = SINGLE ? 0 : tile_case[t];
+      const LoopCase s = sc[c];
+      if (s.phase == PS_DONE) continue;  // uniform over the CTA
+      const Geo& g = G(c);
+      const Cell cl = tile_cell(g, SINGLE ? t : t - tile_first[c], (g.Nx + 31) / 32);
+      double rp = 0, rT = 0;
+      if (cl.ok) Ops::pass(g, cl, s, rp, rT);
+      if (s.phase != PS_MATERIALIZE) block_max2(rp, rT, &g.ctl->rb_p[slot], &g.ctl->rb_T[slot], &g.ctl->status);
+    }
+    // clear the slot of the next round (its last readers passed the previous barrier)
+    if (lead)
+      for (int c = tid; c < ncases; c += nthr) {
+        G(c).ctl->rb_p[(round + 1) % 3] = 0ull;
+        G(c).ctl->rb_T[(round + 1) % 3] = 0ull;
+      }
+    if (!grid_barrier(lc)) break;
+    int any = 0;
+    for (int c = tid; c < ncases; c += nthr) {
+      LoopCase s = sc[c];
+      if (s.phase == PS_DONE) continue;
+      double res_p = 0, res_T = 0;
+      if (s.phase != PS_MATERIALIZE) {
+        res_p = ld_res(&G(c).ctl->rb_p[slot]);
+        res_T = ld_res(&G(c).ctl->rb_T[slot]);
+      }
+      Ops::advance(G(c), lead, s, res_p, res_T);
+      sc[c] = s;
+      any |= (s.phase != PS_DONE);
+    }
+    if (!__syncthreads_or(any)) break;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    last = atomicAdd(&lc->block_count, 1u) == gridDim.x * gridDim.y - 1;
+    if (last) lc->block_count = 0;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const unsigned lstatus = *(volatile unsigned*)&lc->status;
+  for (int c = tid; c < ncases; c += nthr) {
+    const LoopCase s = sc[c];
+    if (!s.active) continue;
+    Ctl* ctl = G(c).ctl;
+    if (lstatus) atomicOr(&ctl->status, lstatus);  // a barrier timeout ends the run of every case
+    ctl->cur = s.cur;
+    ctl->Iter_p_c = s.n;
     ctl->pt_done = 1;
-    ctl->sweeps[I] = n;
-    ctl->step_sweeps += n;
+    ctl->sweeps[s.I] = s.n;
+    ctl->step_sweeps += s.n;
     for (int k = 0; k < 3; k++) {
       ctl->rb_p[k] = 0ull;
       ctl->rb_T[k] = 0ull;
@@ -201,16 +283,24 @@ __device__ __forceinline__ void pt_loop_finish(Ctl* ctl, unsigned cur, unsigned 
   }
 }
 
-// Records the residuals of sweep n (1-based) of outer iteration I (one thread of CTA 0).
-__device__ __forceinline__ void record_residual(Ctl* ctl, unsigned n, unsigned I, double res_p, double res_T) {
-  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
-    ctl->res_p[I] = res_p;
-    ctl->res_T[I] = res_T;
-    if (n == 1) {
-      ctl->res_p0[I] = res_p;
-      ctl->res_T0[I] = res_T;
-    }
-  }
+// The FP64 loops' state transition (exact and mode-1 sweeps): count the sweep, flip the
+// buffers, apply the stop rule.
+__device__ __forceinline__ void advance_fp64(const Geo& g, bool lead, LoopCase& s, double res_p, double res_T) {
+  s.n++;
+  s.cur ^= 1;
+  if (lead) record_residual(g.ctl, s.n, s.I, res_p, res_T);
+  s.phase = sweep_continues(g, s.n, res_p, res_T) ? PS_SWEEP : PS_DONE;
+}
+
+// A batched kernel's CTA (x, y, z) works on case z: the case's Geo is staged in shared memory.
+// Returns whether the case takes part in the current step.
+__device__ __forceinline__ bool stage_geo(Geo& sg, const Geo* __restrict__ gs) {
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x, nthr = blockDim.x * blockDim.y;
+  const unsigned* src = reinterpret_cast<const unsigned*>(&gs[blockIdx.z]);
+  unsigned* dst = reinterpret_cast<unsigned*>(&sg);
+  for (int k = tid; k < (int)(sizeof(Geo) / 4); k += nthr) dst[k] = src[k];
+  __syncthreads();
+  return *(volatile unsigned*)&sg.ctl->running != 0;
 }
 
 // Zero-gradient copies into the ghost cells outside the p/T solve range, side by side in the

@@ -23,7 +23,7 @@ namespace sts {
 // ---------------------------------------------------------------------------
 // start of a time step: *_pr copies and per-step counters (SIMPLE_TS_MPI.cpp:3233-3260)
 // ---------------------------------------------------------------------------
-__global__ void k_step_begin(Geo g, int counters, unsigned long long h_outer, int in_graph) {
+__device__ __forceinline__ void k_step_begin_body(const Geo& g, int counters, unsigned long long h_outer, int in_graph) {
   Cell c = cell(g);
   Ctl* ctl = g.ctl;
   const unsigned cur = ctl->cur;
@@ -48,12 +48,43 @@ __global__ void k_step_begin(Geo g, int counters, unsigned long long h_outer, in
     ctl->step_sweeps = 0;
   }
 }
+__global__ void k_step_begin(Geo g, int counters, unsigned long long h_outer, int in_graph) {
+  k_step_begin_body(g, counters, h_outer, in_graph);
+}
+
+// Batched start of a step: a case takes part while its run goes on and steps are left; cases
+// that stopped skip every kernel of the step (stage_geo reads the flag).
+__global__ void kb_step_begin(const Geo* gs) {
+  __shared__ Geo sg;
+  stage_geo(sg, gs);
+  Ctl* ctl = sg.ctl;
+  const bool running = ctl->continue_step && ctl->steps_left > 0;
+  __syncthreads();
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) ctl->running = running ? 1u : 0u;
+  if (running) k_step_begin_body(sg, 1, 0ull, 0);
+}
+
+// Steps the next batched launch may take, for every case.
+__global__ void kb_set_steps(const Geo* gs, int ncases, unsigned n) {
+  for (int c = threadIdx.x; c < ncases; c += blockDim.x) gs[c].ctl->steps_left = n;
+}
+
+// The batched step loop goes on while any case runs and has steps left.
+__global__ void kb_continue(const Geo* gs, int ncases, unsigned long long h_step) {
+  int any = 0;
+  for (int c = threadIdx.x; c < ncases; c += blockDim.x) {
+    const Ctl* ctl = gs[c].ctl;
+    any |= (ctl->continue_step && ctl->steps_left > 0) ? 1 : 0;
+  }
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0) cudaGraphSetConditional((cudaGraphConditionalHandle)h_step, any ? 1 : 0);
+}
 
 // ---------------------------------------------------------------------------
 // momentum coefficients (u: SIMPLE_TS_MPI.cpp:3269-3344 bc, :3478-3545 nch;
 // v: :3373-3450 bc, :3561-3630 nch) and the energy source ScT1 (:3655-3756)
 // ---------------------------------------------------------------------------
-__global__ void k_assemble(Geo g, unsigned long long h_sweep, int in_graph) {
+__device__ __forceinline__ void assemble_body(const Geo& g, unsigned long long h_sweep, int in_graph) {
   Cell c = cell(g);
   Ctl* ctl = g.ctl;
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
@@ -191,6 +222,12 @@ __global__ void k_assemble(Geo g, unsigned long long h_sweep, int in_graph) {
                         (dudx + dvdy) * (dudx + dvdy) * 2.0 / 3.0) +
                    g.p_pr[d.ij] * hx[i] * hy[j];
   }
+}
+__global__ void k_assemble(Geo g, unsigned long long h_sweep, int in_graph) { assemble_body(g, h_sweep, in_graph); }
+__global__ void kb_assemble(const Geo* gs, unsigned long long h_sweep, int in_graph) {
+  __shared__ Geo sg;
+  if (!stage_geo(sg, gs)) return;
+  assemble_body(sg, h_sweep, in_graph);
 }
 
 // ---------------------------------------------------------------------------
@@ -350,44 +387,40 @@ __global__ void k_sweep_first(Geo g, unsigned long long h_sweep, int in_graph) {
 
 __global__ void k_sweep(Geo g, unsigned long long h_sweep, int in_graph) { sweep_body<false>(g, h_sweep, in_graph); }
 
-// The whole sweep loop of one outer iteration in one cooperative launch: the same cell
-// arithmetic as k_sweep_first / k_sweep (so the same bits), with a grid barrier after every sweep.
-__global__ void __launch_bounds__(256) k_pt_loop(Geo g) {
-  Ctl* ctl = g.ctl;
-  const int tx = (g.Nx + 31) / 32, nt = tx * ((g.Ny + 7) / 8);
-  const unsigned I = ctl->Iter < 64 ? ctl->Iter : 63;
-  unsigned cur = ctl->cur, n = 0;
-  for (;;) {
-    const double* P = g.p[cur];
-    const double* TT = g.T[cur];
-    double* pn = g.p[cur ^ 1];
-    double* Tn = g.T[cur ^ 1];
-    double rp = 0, rT = 0;
-    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
-      const Cell c = tile_cell(g, t, tx);
-      if (!c.ok) continue;
-      double a = 0, b = 0;
-      if (n == 0) sweep_cell<true, true>(g, c, P, TT, pn, Tn, a, b);
-      else sweep_cell<false, true>(g, c, P, TT, pn, Tn, a, b);
-      if (a != a || b != b) atomicOr(&ctl->status, ST_NONFINITE);  // the max below skips NaN
-      rp = mx(rp, a);
-      rT = mx(rT, b);
-    }
-    double res_p, res_T;
-    if (!sweep_residual(ctl, n, rp, rT, res_p, res_T)) break;
-    n++;
-    cur ^= 1;
-    record_residual(ctl, n, I, res_p, res_T);
-    if (!sweep_continues(g, n, res_p, res_T)) break;
+// The whole sweep loop of one outer iteration, for one case or a batch, in one cooperative
+// launch: the same cell arithmetic as k_sweep_first / k_sweep (so the same bits), one sweep per
+// round of pt_loop_rounds.
+struct ExactOps {
+  static __device__ __forceinline__ void pass(const Geo& g, const Cell& c, const LoopCase& s, double& rp, double& rT) {
+    const double* P = g.p[s.cur];
+    const double* TT = g.T[s.cur];
+    double* pn = g.p[s.cur ^ 1];
+    double* Tn = g.T[s.cur ^ 1];
+    double a = 0, b = 0;
+    if (s.phase == PS_FIRST) sweep_cell<true, true>(g, c, P, TT, pn, Tn, a, b);
+    else sweep_cell<false, true>(g, c, P, TT, pn, Tn, a, b);
+    if (a != a || b != b) atomicOr(&g.ctl->status, ST_NONFINITE);  // the block max skips NaN
+    rp = a;
+    rT = b;
   }
-  pt_loop_finish(ctl, cur, n, I);
+  static __device__ __forceinline__ void advance(const Geo& g, bool lead, LoopCase& s, double res_p, double res_T) {
+    advance_fp64(g, lead, s, res_p, res_T);
+  }
+};
+
+__global__ void __launch_bounds__(256, 4) k_pt_loop(Geo g, int ntiles, LoopCtl* lc) {
+  pt_loop_rounds<ExactOps, true>(g, nullptr, nullptr, nullptr, 1, ntiles, lc);
+}
+__global__ void __launch_bounds__(256, 4) kb_pt_loop(const Geo* gs, const int* tile_case, const int* tile_first,
+                                                     int ncases, int ntiles, LoopCtl* lc) {
+  pt_loop_rounds<ExactOps, false>(gs[0], gs, tile_case, tile_first, ncases, ntiles, lc);
 }
 
 // ---------------------------------------------------------------------------
 // velocity correction with L-inf residuals (SIMPLE_TS_MPI.cpp:4171-4305) and
 // sqrt(T), rho = p/T (:4323-4330)
 // ---------------------------------------------------------------------------
-__global__ void k_correct(Geo g) {
+__device__ __forceinline__ void correct_body(const Geo& g) {
   Cell c = cell(g);
   Ctl* ctl = g.ctl;
   const unsigned cur = ctl->cur;
@@ -415,9 +448,15 @@ __global__ void k_correct(Geo g) {
   }
   block_max2(ru, rv, &ctl->res_bits_u, &ctl->res_bits_v, &ctl->status);
 }
+__global__ void k_correct(Geo g) { correct_body(g); }
+__global__ void kb_correct(const Geo* gs) {
+  __shared__ Geo sg;
+  if (!stage_geo(sg, gs)) return;
+  correct_body(sg);
+}
 
 // Solve_rho_in_middle_points (SIMPLE_TS_MPI.cpp:10382-10437)
-__global__ void k_face_rho(Geo g) {
+__device__ __forceinline__ void face_rho_body(const Geo& g) {
   Cell c = cell(g);
   if (!c.ok) return;
   const Nb d = neighbours(c.i, c.j, g.Nx, g.Ny, g.bits & F_PERIODIC);
@@ -432,6 +471,12 @@ __global__ void k_face_rho(Geo g) {
   else rv = 0.0;
   g.rho_u[d.ij] = ru;
   g.rho_v[d.ij] = rv;
+}
+__global__ void k_face_rho(Geo g) { face_rho_body(g); }
+__global__ void kb_face_rho(const Geo* gs) {
+  __shared__ Geo sg;
+  if (!stage_geo(sg, gs)) return;
+  face_rho_body(sg);
 }
 
 // SolveFluxes (SIMPLE_TS_MPI.cpp:10440-10454) and SolveDiffisionTerms (:10457-10618)
@@ -506,7 +551,7 @@ __device__ __forceinline__ void flux_diff_cell(const Geo& g, const Cell& c) {
 
 // The zero-gradient temperature and pressure copies (phases `tail`) touch only ghost cells of p
 // and T, which the fluxes and diffusion terms do not read, so the first CTA does them too.
-__global__ void k_flux_diff(Geo g, unsigned tail) {
+__device__ __forceinline__ void flux_diff_body(const Geo& g, unsigned tail) {
   Cell c = cell(g);
   if (c.ok) flux_diff_cell(g, c);
   if (tail && blockIdx.x == 0 && blockIdx.y == 0) {
@@ -516,6 +561,12 @@ __global__ void k_flux_diff(Geo g, unsigned tail) {
     __syncthreads();
     if (tail & PH_PRES) phase_pres(g, g.p[cur], tid, nt);
   }
+}
+__global__ void k_flux_diff(Geo g, unsigned tail) { flux_diff_body(g, tail); }
+__global__ void kb_flux_diff(const Geo* gs, unsigned tail) {
+  __shared__ Geo sg;
+  if (!stage_geo(sg, gs)) return;
+  flux_diff_body(sg, tail);
 }
 
 // ApplyBodiesConditionsToVariables on the device (SIMPLE_TS_MPI.cpp:6470-6584): a face takes the
@@ -691,7 +742,7 @@ __device__ void do_tjump_write(const Geo& g, double* __restrict__ T, int k) {
 }
 
 // Single-CTA boundary work; `phases` selects the parts (PH_* in sts_kernels.h).
-__global__ void __launch_bounds__(1024) k_boundary(Geo g, unsigned phases, unsigned long long h_outer, int in_graph) {
+__device__ __forceinline__ void boundary_body(const Geo& g, unsigned phases, unsigned long long h_outer, int in_graph) {
   Ctl* ctl = g.ctl;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int Nx = g.Nx, Ny = g.Ny;
@@ -949,10 +1000,16 @@ __global__ void __launch_bounds__(1024) k_boundary(Geo g, unsigned phases, unsig
 
   if (phases & PH_PRES) phase_pres(g, p, tid, nt);
 }
+__global__ void __launch_bounds__(1024) k_boundary(Geo g, unsigned phases, unsigned long long h_outer, int in_graph) { boundary_body(g, phases, h_outer, in_graph); }
+__global__ void __launch_bounds__(1024) kb_boundary(const Geo* gs, unsigned phases, unsigned long long h_outer, int in_graph) {
+  __shared__ Geo sg;
+  if (!stage_geo(sg, gs)) return;
+  boundary_body(sg, phases, h_outer, in_graph);
+}
 
 // Wall lists over the whole grid: loop control (one thread), slip u and slip v (independent:
 // they write u and v respectively).
-__global__ void k_bnd_walls(Geo g, unsigned phases, unsigned long long h_outer, int in_graph) {
+__device__ __forceinline__ void bnd_walls_body(const Geo& g, unsigned phases, unsigned long long h_outer, int in_graph) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
   if ((phases & PH_CONTROL) && t == 0) do_control(g, h_outer, in_graph);
   if (phases & PH_SLIP_U)
@@ -960,17 +1017,29 @@ __global__ void k_bnd_walls(Geo g, unsigned phases, unsigned long long h_outer, 
   if (phases & PH_SLIP_V)
     for (int k = t; k < g.n_slip_v; k += nt) do_slip_v(g, k);
 }
+__global__ void k_bnd_walls(Geo g, unsigned phases, unsigned long long h_outer, int in_graph) { bnd_walls_body(g, phases, h_outer, in_graph); }
+__global__ void kb_bnd_walls(const Geo* gs, unsigned phases, unsigned long long h_outer, int in_graph) {
+  __shared__ Geo sg;
+  if (!stage_geo(sg, gs)) return;
+  bnd_walls_body(sg, phases, h_outer, in_graph);
+}
 
 // Temperature-jump wall values over the whole grid.
-__global__ void k_bnd_tjump(Geo g) {
+__device__ __forceinline__ void bnd_tjump_body(const Geo& g) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
   const double* T = g.T[g.ctl->cur];
   for (int k = t; k < g.n_tjump; k += nt) do_tjump(g, T, k);
 }
+__global__ void k_bnd_tjump(Geo g) { bnd_tjump_body(g); }
+__global__ void kb_bnd_tjump(const Geo* gs) {
+  __shared__ Geo sg;
+  if (!stage_geo(sg, gs)) return;
+  bnd_tjump_body(sg);
+}
 
 // End of a time step: time-dependent inflow (SIMPLE_TS_MPI.cpp:8102-8144), per-step
 // record and the multi-step loop condition.
-__global__ void k_step_end(Geo g, unsigned long long h_step, int in_graph) {
+__device__ __forceinline__ void step_end_body(const Geo& g, unsigned long long h_step, int in_graph) {
   Ctl* ctl = g.ctl;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int Nx = g.Nx, Ny = g.Ny;
@@ -998,6 +1067,12 @@ __global__ void k_step_end(Geo g, unsigned long long h_step, int in_graph) {
     if (in_graph)
       cudaGraphSetConditional((cudaGraphConditionalHandle)h_step, (ctl->steps_left > 0 && ctl->continue_step) ? 1 : 0);
   }
+}
+__global__ void k_step_end(Geo g, unsigned long long h_step, int in_graph) { step_end_body(g, h_step, in_graph); }
+__global__ void kb_step_end(const Geo* gs, unsigned long long h_step, int in_graph) {
+  __shared__ Geo sg;
+  if (!stage_geo(sg, gs)) return;
+  step_end_body(sg, h_step, in_graph);
 }
 
 }  // namespace sts

@@ -15,7 +15,7 @@
 namespace sts {
 
 // u/v momentum coefficients and ScT1 (SIMPLE_TS_MPI.cpp:3269-3756) with reciprocal multiplies.
-__global__ void k_assemble_fast(Geo g, unsigned long long h_sweep, int in_graph) {
+__device__ __forceinline__ void assemble_fast_body(const Geo& g, unsigned long long h_sweep, int in_graph) {
   Cell c = cell(g);
   Ctl* ctl = g.ctl;
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
@@ -142,9 +142,15 @@ __global__ void k_assemble_fast(Geo g, unsigned long long h_sweep, int in_graph)
                    g.p_pr[d.ij] * hx[i] * hy[j];
   }
 }
+__global__ void k_assemble_fast(Geo g, unsigned long long h_sweep, int in_graph) { assemble_fast_body(g, h_sweep, in_graph); }
+__global__ void kb_assemble_fast(const Geo* gs, unsigned long long h_sweep, int in_graph) {
+  __shared__ Geo sg;
+  if (!stage_geo(sg, gs)) return;
+  assemble_fast_body(sg, h_sweep, in_graph);
+}
 
 // Fluxes and diffusion coefficients (SIMPLE_TS_MPI.cpp:10440-10618) with reciprocal multiplies.
-__global__ void k_flux_diff_fast(Geo g, unsigned tail) {
+__device__ __forceinline__ void flux_diff_fast_body(const Geo& g, unsigned tail) {
   Cell c = cell(g);
   if (c.ok) {
     const int i = c.i, j = c.j;
@@ -206,6 +212,12 @@ __global__ void k_flux_diff_fast(Geo g, unsigned tail) {
     __syncthreads();
     if (tail & PH_PRES) phase_pres(g, g.p[cur], tid, nt);
   }
+}
+__global__ void k_flux_diff_fast(Geo g, unsigned tail) { flux_diff_fast_body(g, tail); }
+__global__ void kb_flux_diff_fast(const Geo* gs, unsigned tail) {
+  __shared__ Geo sg;
+  if (!stage_geo(sg, gs)) return;
+  flux_diff_fast_body(sg, tail);
 }
 
 // ---------------------------------------------------------------------------
@@ -287,36 +299,31 @@ __device__ __forceinline__ bool sweep_cell_fast(const Geo& g, const Cell& c, con
   return true;
 }
 
-// The sweep loop of mode 1 in one cooperative launch (see k_pt_loop).
-__global__ void __launch_bounds__(256) k_pt_loop_fast(Geo g) {
-  Ctl* ctl = g.ctl;
-  const int tx = (g.Nx + 31) / 32, nt = tx * ((g.Ny + 7) / 8);
-  const unsigned I = ctl->Iter < 64 ? ctl->Iter : 63;
-  unsigned cur = ctl->cur, n = 0;
-  for (;;) {
-    const double* P = g.p[cur];
-    const double* TT = g.T[cur];
-    double rp = 0, rT = 0;
-    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
-      const Cell c = tile_cell(g, t, tx);
-      if (!c.ok) continue;
-      double Tnew, pnew, sa;
-      const bool solved = (n == 0) ? sweep_cell_fast<true>(g, c, P, TT, g.p[cur ^ 1], g.T[cur ^ 1], Tnew, pnew, sa)
-                                   : sweep_cell_fast<false>(g, c, P, TT, g.p[cur ^ 1], g.T[cur ^ 1], Tnew, pnew, sa);
-      if (!solved) continue;
-      const double a = fabs(pnew - P[c.ij]), b = fabs(Tnew - TT[c.ij]);
-      if (a != a || b != b) atomicOr(&ctl->status, ST_NONFINITE);
-      rp = mx(rp, a);
-      rT = mx(rT, b);
-    }
-    double res_p, res_T;
-    if (!sweep_residual(ctl, n, rp, rT, res_p, res_T)) break;
-    n++;
-    cur ^= 1;
-    record_residual(ctl, n, I, res_p, res_T);
-    if (!sweep_continues(g, n, res_p, res_T)) break;
+// The sweep loop of mode 1 (see k_pt_loop).
+struct FastOps {
+  static __device__ __forceinline__ void pass(const Geo& g, const Cell& c, const LoopCase& s, double& rp, double& rT) {
+    const double* P = g.p[s.cur];
+    const double* TT = g.T[s.cur];
+    double Tnew, pnew, sa;
+    const bool solved = (s.phase == PS_FIRST)
+                            ? sweep_cell_fast<true>(g, c, P, TT, g.p[s.cur ^ 1], g.T[s.cur ^ 1], Tnew, pnew, sa)
+                            : sweep_cell_fast<false>(g, c, P, TT, g.p[s.cur ^ 1], g.T[s.cur ^ 1], Tnew, pnew, sa);
+    if (!solved) return;
+    rp = fabs(pnew - P[c.ij]);
+    rT = fabs(Tnew - TT[c.ij]);
+    if (rp != rp || rT != rT) atomicOr(&g.ctl->status, ST_NONFINITE);
   }
-  pt_loop_finish(ctl, cur, n, I);
+  static __device__ __forceinline__ void advance(const Geo& g, bool lead, LoopCase& s, double res_p, double res_T) {
+    advance_fp64(g, lead, s, res_p, res_T);
+  }
+};
+
+__global__ void __launch_bounds__(256, 4) k_pt_loop_fast(Geo g, int ntiles, LoopCtl* lc) {
+  pt_loop_rounds<FastOps, true>(g, nullptr, nullptr, nullptr, 1, ntiles, lc);
+}
+__global__ void __launch_bounds__(256, 4) kb_pt_loop_fast(const Geo* gs, const int* tile_case, const int* tile_first,
+                                                          int ncases, int ntiles, LoopCtl* lc) {
+  pt_loop_rounds<FastOps, false>(gs[0], gs, tile_case, tile_first, ncases, ntiles, lc);
 }
 
 // ---------------------------------------------------------------------------
@@ -376,113 +383,110 @@ __device__ __forceinline__ void sweep32_cell(const Geo& g, const Cell& c, unsign
   rp = fmaxf(rp, ap <= kFloor32 * fabsf(epnew) ? 0.0f : ap);
 }
 
-__global__ void __launch_bounds__(256) k_pt_loop_mixed(Geo g) {
-  Ctl* ctl = g.ctl;
-  const bool lead = blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0;
-  const int tx = (g.Nx + 31) / 32, nt = tx * ((g.Ny + 7) / 8);
-  const unsigned I = ctl->Iter < 64 ? ctl->Iter : 63;
-  const double ht = g.ht, gm = 1.0 - g.gamma1;
-  unsigned base = ctl->cur, cur = base ^ 1, n = 0;
-  unsigned nred = 0;  // residual reductions so far (the slot rotation of sweep_residual)
-  double res_p, res_T;
-
-  // sweep 1 in FP64 from b, with the FP32 coefficients of this outer iteration
-  {
-    const double* P = g.p[base];
-    const double* TT = g.T[base];
-    double rp = 0, rT = 0;
-    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
-      const Cell c = tile_cell(g, t, tx);
-      if (!c.ok) continue;
-      const int ij = c.ij;
-      double Tnew, pnew, sa;
-      if (!sweep_cell_fast<true>(g, c, P, TT, g.p[base ^ 1], g.T[base ^ 1], Tnew, pnew, sa)) {
-        g.dT[ij] = 0.0f; g.dp[ij] = 0.0f;
-        g.eT[0][ij] = 0.0f; g.ep[0][ij] = 0.0f; g.eT[1][ij] = 0.0f; g.ep[1][ij] = 0.0f;
-        continue;
-      }
-      const double a = fabs(pnew - P[ij]), b = fabs(Tnew - TT[ij]);
-      if (a != a || b != b) atomicOr(&ctl->status, ST_NONFINITE);
-      rp = mx(rp, a);
-      rT = mx(rT, b);
-      const Nb d = neighbours(c.i, c.j, g.Nx, g.Ny, g.bits & F_PERIODIC);
-      const double r = ht * g.inv[5][ij];
-      const int nb[4] = {d.i_1j, d.i1j, d.ij_1, d.ij1};
-      for (int k = 0; k < 4; k++)  // a wall neighbour's term is a constant and sits in the defect
-        g.c32[k][ij] = (cls_o(g.cls[ij]) == CLS_NCH || cls_fluid(g.cls[nb[k]])) ? (float)(r * g.inv[k][ij]) : 0.0f;
-      g.c32[4][ij] = (float)(r * gm * g.inv[4][ij]);
-      g.a32[0][ij] = (float)(ht * g.apx[ij]);
-      g.a32[1][ij] = (float)(ht * g.apx[d.i1j]);
-      g.a32[2][ij] = (float)(ht * g.apy[ij]);
-      g.a32[3][ij] = (float)(ht * g.apy[d.ij1]);
-      set_base(g, c, TT[ij], P[ij], Tnew, pnew, sa);
-    }
-    if (!sweep_residual(ctl, nred++, rp, rT, res_p, res_T)) {
-      pt_loop_finish(ctl, base, n, I);
-      return;
-    }
-    n = 1;
-    record_residual(ctl, n, I, res_p, res_T);
-    if (n >= (unsigned)g.N_I_p_c) {  // a single sweep was asked for: x1 is the result
-      pt_loop_finish(ctl, cur, n, I);
-      return;
-    }
-  }
-
-  unsigned ec = 0;  // buffer of the latest correction
-  for (;;) {
-    // FP32 sweep n+1
-    float rp = 0.f, rT = 0.f;
-    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
-      const Cell c = tile_cell(g, t, tx);
-      if (c.ok && cls_o(g.cls[c.ij])) sweep32_cell(g, c, ec, rp, rT);
-    }
-    if (!sweep_residual(ctl, nred++, (double)rp, (double)rT, res_p, res_T)) break;
-    n++;
-    ec ^= 1;
-    if (lead) ctl->sweeps32++;
-    if ((n < (unsigned)g.N_I_p_c) && ((g.MaxError_p_c < res_p) || (g.MaxError_T < res_T))) continue;
-
-    // the iterate of sweep n-1 in FP64: b + e (buffer ec ^ 1)
-    const unsigned prev = ec ^ 1;
-    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
-      const Cell c = tile_cell(g, t, tx);
-      if (!c.ok) continue;
-      g.p[base ^ 1][c.ij] = g.p[base][c.ij] + (double)g.ep[prev][c.ij];
-      g.T[base ^ 1][c.ij] = g.T[base][c.ij] + (double)g.eT[prev][c.ij];
-    }
-    if (!grid_barrier(ctl)) break;
-    n--;
-
-    // sweep n again, in FP64, into the base buffer; its residual decides
-    {
-      const double* P = g.p[base ^ 1];
-      const double* TT = g.T[base ^ 1];
-      double rp64 = 0, rT64 = 0;
-      for (int t = blockIdx.x; t < nt; t += gridDim.x) {
-        const Cell c = tile_cell(g, t, tx);
-        if (!c.ok) continue;
+struct MixedOps {
+  static __device__ __forceinline__ void pass(const Geo& g, const Cell& c, const LoopCase& s, double& rp, double& rT) {
+    const int ij = c.ij;
+    const unsigned base = s.base;
+    switch (s.phase) {
+      case PS_FIRST: {  // FP64 sweep from b into base ^ 1, with the FP32 coefficients of this outer iteration
+        const double* P = g.p[base];
+        const double* TT = g.T[base];
         double Tnew, pnew, sa;
-        if (!sweep_cell_fast<false>(g, c, P, TT, g.p[base], g.T[base], Tnew, pnew, sa)) continue;
-        const double a = fabs(pnew - P[c.ij]), b = fabs(Tnew - TT[c.ij]);
-        if (a != a || b != b) atomicOr(&ctl->status, ST_NONFINITE);
-        rp64 = mx(rp64, a);
-        rT64 = mx(rT64, b);
-        set_base(g, c, TT[c.ij], P[c.ij], Tnew, pnew, sa);  // used only if the loop goes on
+        if (!sweep_cell_fast<true>(g, c, P, TT, g.p[base ^ 1], g.T[base ^ 1], Tnew, pnew, sa)) {
+          g.dT[ij] = 0.0f; g.dp[ij] = 0.0f;
+          g.eT[0][ij] = 0.0f; g.ep[0][ij] = 0.0f; g.eT[1][ij] = 0.0f; g.ep[1][ij] = 0.0f;
+          return;
+        }
+        rp = fabs(pnew - P[ij]);
+        rT = fabs(Tnew - TT[ij]);
+        if (rp != rp || rT != rT) atomicOr(&g.ctl->status, ST_NONFINITE);
+        const Nb d = neighbours(c.i, c.j, g.Nx, g.Ny, g.bits & F_PERIODIC);
+        const double ht = g.ht, r = ht * g.inv[5][ij];
+        const int nb[4] = {d.i_1j, d.i1j, d.ij_1, d.ij1};
+        for (int k = 0; k < 4; k++)  // a wall neighbour's term is a constant and sits in the defect
+          g.c32[k][ij] = (cls_o(g.cls[ij]) == CLS_NCH || cls_fluid(g.cls[nb[k]])) ? (float)(r * g.inv[k][ij]) : 0.0f;
+        g.c32[4][ij] = (float)(r * (1.0 - g.gamma1) * g.inv[4][ij]);
+        g.a32[0][ij] = (float)(ht * g.apx[ij]);
+        g.a32[1][ij] = (float)(ht * g.apx[d.i1j]);
+        g.a32[2][ij] = (float)(ht * g.apy[ij]);
+        g.a32[3][ij] = (float)(ht * g.apy[d.ij1]);
+        set_base(g, c, TT[ij], P[ij], Tnew, pnew, sa);
+        return;
       }
-      if (!sweep_residual(ctl, nred++, rp64, rT64, res_p, res_T)) break;
+      case PS_SWEEP32: {
+        if (!cls_o(g.cls[ij])) return;
+        float fp = 0.f, fT = 0.f;
+        sweep32_cell(g, c, s.ec, fp, fT);
+        rp = fp;
+        rT = fT;
+        return;
+      }
+      case PS_MATERIALIZE:  // the iterate of the sweep before the last FP32 one, in FP64
+        g.p[base ^ 1][ij] = g.p[base][ij] + (double)g.ep[s.ec ^ 1][ij];
+        g.T[base ^ 1][ij] = g.T[base][ij] + (double)g.eT[s.ec ^ 1][ij];
+        return;
+      case PS_CONFIRM: {  // that sweep again in FP64 into the base buffer; exports for a re-basing
+        const double* P = g.p[base ^ 1];
+        const double* TT = g.T[base ^ 1];
+        double Tnew, pnew, sa;
+        if (!sweep_cell_fast<false>(g, c, P, TT, g.p[base], g.T[base], Tnew, pnew, sa)) return;
+        rp = fabs(pnew - P[ij]);
+        rT = fabs(Tnew - TT[ij]);
+        if (rp != rp || rT != rT) atomicOr(&g.ctl->status, ST_NONFINITE);
+        set_base(g, c, TT[ij], P[ij], Tnew, pnew, sa);
+        return;
+      }
+      default:
+        return;
     }
-    n++;
-    record_residual(ctl, n, I, res_p, res_T);
-    cur = base;
-    if (!sweep_continues(g, n, res_p, res_T)) break;
-    // re-base: x_{n-1} (buffer base ^ 1) and the defect x_n - x_{n-1} written above
-    base ^= 1;
-    cur = base ^ 1;
-    ec = 0;
-    if (lead) ctl->rebases++;
   }
-  pt_loop_finish(ctl, cur, n, I);
+  static __device__ __forceinline__ void advance(const Geo& g, bool lead, LoopCase& s, double res_p, double res_T) {
+    Ctl* ctl = g.ctl;
+    switch (s.phase) {
+      case PS_FIRST:
+        s.n = 1;
+        if (lead) record_residual(ctl, s.n, s.I, res_p, res_T);
+        s.cur = s.base ^ 1;
+        s.ec = 0;
+        s.phase = (s.n >= (unsigned)g.N_I_p_c) ? PS_DONE : PS_SWEEP32;  // a single sweep: x1 is the result
+        break;
+      case PS_SWEEP32:
+        s.n++;
+        s.ec ^= 1;
+        if (lead) ctl->sweeps32++;
+        s.phase = ((s.n < (unsigned)g.N_I_p_c) && ((g.MaxError_p_c < res_p) || (g.MaxError_T < res_T)))
+                      ? PS_SWEEP32 : PS_MATERIALIZE;
+        break;
+      case PS_MATERIALIZE:
+        s.n--;
+        s.phase = PS_CONFIRM;
+        break;
+      case PS_CONFIRM:
+        s.n++;
+        if (lead) record_residual(ctl, s.n, s.I, res_p, res_T);
+        s.cur = s.base;
+        if (!sweep_continues(g, s.n, res_p, res_T)) {
+          s.phase = PS_DONE;
+        } else {  // re-base: x_{n-1} (buffer base ^ 1) and the defect x_n - x_{n-1} written by the pass
+          s.base ^= 1;
+          s.cur = s.base ^ 1;
+          s.ec = 0;
+          if (lead) ctl->rebases++;
+          s.phase = PS_SWEEP32;
+        }
+        break;
+      default:
+        break;
+    }
+  }
+};
+
+__global__ void __launch_bounds__(256, 4) k_pt_loop_mixed(Geo g, int ntiles, LoopCtl* lc) {
+  pt_loop_rounds<MixedOps, true>(g, nullptr, nullptr, nullptr, 1, ntiles, lc);
+}
+__global__ void __launch_bounds__(256, 4) kb_pt_loop_mixed(const Geo* gs, const int* tile_case, const int* tile_first,
+                                                          int ncases, int ntiles, LoopCtl* lc) {
+  pt_loop_rounds<MixedOps, false>(gs[0], gs, tile_case, tile_first, ncases, ntiles, lc);
 }
 
 }  // namespace sts

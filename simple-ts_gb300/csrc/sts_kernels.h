@@ -21,20 +21,13 @@ enum : unsigned {
   PH_ALL_STEP = PH_CONTROL | PH_SLIP_U | PH_SLIP_V | PH_VEL | PH_PBEGIN | PH_TJUMP | PH_TEMP | PH_PRES,
 };
 
+// Per-case kernels.  Each k_X takes the case's Geo by value; its batched form kb_X takes the
+// device array of the batch's Geos and runs case blockIdx.z (cases outside the step return).
 __global__ void k_step_begin(Geo g, int counters, unsigned long long h_outer, int in_graph);
 __global__ void k_apply_bodies(Geo g);
 __global__ void k_assemble(Geo g, unsigned long long h_sweep, int in_graph);
 __global__ void k_sweep_first(Geo g, unsigned long long h_sweep, int in_graph);
 __global__ void k_sweep(Geo g, unsigned long long h_sweep, int in_graph);
-// the whole sweep loop of an outer iteration in one cooperative launch (grid <= resident CTAs)
-__global__ void k_pt_loop(Geo g);
-// self-check of the correctly rounded division by a reciprocal against IEEE division
-__global__ void k_check_division(unsigned long long n, unsigned long long seed, unsigned long long* bad);
-// precision modes 1 and 2
-__global__ void k_assemble_fast(Geo g, unsigned long long h_sweep, int in_graph);
-__global__ void k_flux_diff_fast(Geo g, unsigned tail);
-__global__ void k_pt_loop_fast(Geo g);
-__global__ void k_pt_loop_mixed(Geo g);
 __global__ void k_correct(Geo g);
 __global__ void k_face_rho(Geo g);
 __global__ void k_flux_diff(Geo g, unsigned tail);
@@ -43,5 +36,35 @@ __global__ void k_bnd_tjump(Geo g);
 __global__ void k_sqrt_rho(Geo g, int do_rho);
 __global__ void k_boundary(Geo g, unsigned phases, unsigned long long h_outer, int in_graph);
 __global__ void k_step_end(Geo g, unsigned long long h_step, int in_graph);
+__global__ void kb_step_begin(const Geo* gs);
+__global__ void kb_set_steps(const Geo* gs, int ncases, unsigned n);
+__global__ void kb_continue(const Geo* gs, int ncases, unsigned long long h_step);
+__global__ void kb_assemble(const Geo* gs, unsigned long long h_sweep, int in_graph);
+__global__ void kb_correct(const Geo* gs);
+__global__ void kb_face_rho(const Geo* gs);
+__global__ void kb_flux_diff(const Geo* gs, unsigned tail);
+__global__ void kb_bnd_walls(const Geo* gs, unsigned phases, unsigned long long h_outer, int in_graph);
+__global__ void kb_bnd_tjump(const Geo* gs);
+__global__ void kb_boundary(const Geo* gs, unsigned phases, unsigned long long h_outer, int in_graph);
+__global__ void kb_step_end(const Geo* gs, unsigned long long h_step, int in_graph);
+// The whole sweep loop of an outer iteration in one cooperative launch (grid <= resident CTAs):
+// k_ for one case (ntiles 32x8 tiles), kb_ for ncases cases, where tile_case[t] is the case of
+// global tile t and tile_first[c] the first tile of case c.
+__global__ void k_pt_loop(Geo g, int ntiles, LoopCtl* lc);
+__global__ void kb_pt_loop(const Geo* gs, const int* tile_case, const int* tile_first, int ncases, int ntiles,
+                           LoopCtl* lc);
+// self-check of the correctly rounded division by a reciprocal against IEEE division
+__global__ void k_check_division(unsigned long long n, unsigned long long seed, unsigned long long* bad);
+// precision modes 1 and 2
+__global__ void k_assemble_fast(Geo g, unsigned long long h_sweep, int in_graph);
+__global__ void k_flux_diff_fast(Geo g, unsigned tail);
+__global__ void kb_assemble_fast(const Geo* gs, unsigned long long h_sweep, int in_graph);
+__global__ void kb_flux_diff_fast(const Geo* gs, unsigned tail);
+__global__ void k_pt_loop_fast(Geo g, int ntiles, LoopCtl* lc);
+__global__ void k_pt_loop_mixed(Geo g, int ntiles, LoopCtl* lc);
+__global__ void kb_pt_loop_fast(const Geo* gs, const int* tile_case, const int* tile_first, int ncases, int ntiles,
+                                LoopCtl* lc);
+__global__ void kb_pt_loop_mixed(const Geo* gs, const int* tile_case, const int* tile_first, int ncases, int ntiles,
+                                 LoopCtl* lc);
 
 }  // namespace sts

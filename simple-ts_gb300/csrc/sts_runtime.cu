@@ -59,6 +59,10 @@ struct sts_ctx {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   unsigned long long h_step = 0, h_outer = 0;
+  // the sweep loop's grid barrier and the case's 32x8 tiles
+  LoopCtl* d_lc = nullptr;
+  int ntiles = 0;
+  bool in_batch = false;  // stepped by an sts_batch, not by sts_step
   std::chrono::steady_clock::time_point t0;
   bool tmp_fresh = true, iter_fresh = true;
 
@@ -117,7 +121,8 @@ struct sts_ctx {
   bool fast() const { return g.precision >= 1; }
   bool mixed() const { return g.precision == 2 && !(hc.bits & F_FIXED_SWEEPS); }
   // the persistent sweep-loop kernel of this context and its grid (CTAs that fit at once)
-  void (*pt_kernel() const)(Geo) { return mixed() ? k_pt_loop_mixed : (fast() ? k_pt_loop_fast : k_pt_loop); }
+  using PtKernel = void (*)(Geo, int, LoopCtl*);
+  PtKernel pt_kernel() const { return mixed() ? k_pt_loop_mixed : (fast() ? k_pt_loop_fast : k_pt_loop); }
   dim3 pt_grid;
   int size_pt_grid() {
     int dev = 0, sms = 0, per_sm = 0;
@@ -125,13 +130,12 @@ struct sts_ctx {
     CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pt_kernel(), 256, 0));
     if (per_sm < 1) return fail(STS_ERR_CUDA, "the sweep-loop kernel does not fit on a multiprocessor");
-    const int tiles = (int)(grid.x * grid.y);
-    pt_grid = dim3((unsigned)std::max(1, std::min(tiles, per_sm * sms)));
+    pt_grid = dim3((unsigned)std::max(1, std::min(ntiles, per_sm * sms)));
     return STS_OK;
   }
   // the sweep loop of one outer iteration outside the graph: one cooperative launch
   int pt_loop() {
-    void* args[] = {(void*)&g};
+    void* args[] = {(void*)&g, (void*)&ntiles, (void*)&d_lc};
     CU(cudaLaunchCooperativeKernel((const void*)pt_kernel(), pt_grid, dim3(32, 8), args, 0, s));
     return STS_OK;
   }
@@ -202,7 +206,7 @@ int sts_ctx::build_graph() {
   if (int r = add_kernel(&n_asm, b_outer, {}, fast() ? k_assemble_fast : k_assemble, grid, block, g,
                          (unsigned long long)0, 0))
     return r;
-  if (int r = add_kernel(&n_sw, b_outer, {n_asm}, pt_kernel(), pt_grid, dim3(32, 8), g)) return r;
+  if (int r = add_kernel(&n_sw, b_outer, {n_asm}, pt_kernel(), pt_grid, dim3(32, 8), g, ntiles, d_lc)) return r;
   {
     cudaLaunchAttributeValue v{};
     v.cooperative = 1;
@@ -678,10 +682,13 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
   ct.u_gas_nd = cf.d("u_gas_nd");
   ct.it = h.restart ? h.it_begin : 0.0;
   ct.continue_step = 1;
+  ct.running = 1;
   CU(cudaMemcpyAsync(c->d_ctl, c->h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, c->s));
 
   c->block = dim3(32, 8);
   c->grid = dim3((h.Nx + 31) / 32, (h.Ny + 7) / 8);
+  c->ntiles = (int)(c->grid.x * c->grid.y);
+  if (int r = c->alloc(&c->d_lc, 1)) return r;
   if (int r = c->size_pt_grid()) return r;
   const dim3 G = c->grid, B = c->block;
   cudaStream_t s = c->s;
@@ -741,6 +748,7 @@ int sts_open_case(const char* case_dir, const sts_options* opt, sts_ctx** out) {
 
 int sts_step(sts_ctx* ctx, int nsteps, int* steps_done) {
   if (!ctx || nsteps < 0) return fail(STS_ERR_ARG, "bad argument");
+  if (ctx->in_batch) return fail(STS_ERR_ARG, "the case belongs to a batch: step it with sts_batch_step");
   int done = 0;
   if (!ctx->finished && nsteps > 0) {
     CU(cudaSetDevice(ctx->opt.device));
@@ -783,6 +791,7 @@ int sts_step_timed(sts_ctx* ctx, int nsteps, int* steps_done, double* device_ms)
 
 int sts_profile_steps(sts_ctx* ctx, int nsteps, double* kernel_ms, int* kernel_launches, int* steps_done) {
   if (!ctx || nsteps < 0 || !kernel_ms || !kernel_launches) return fail(STS_ERR_ARG, "bad argument");
+  if (ctx->in_batch) return fail(STS_ERR_ARG, "the case belongs to a batch");
   CU(cudaSetDevice(ctx->opt.device));
   int done = 0;
   if (ctx->finished) {
@@ -985,7 +994,9 @@ int sts_sync(sts_ctx* ctx) {
   return STS_OK;
 }
 
-void sts_destroy(sts_ctx* ctx) { delete ctx; }
+void sts_destroy(sts_ctx* ctx) {
+  if (ctx && !ctx->in_batch) delete ctx;  // a batch's cases are released with the batch
+}
 
 const char* sts_last_error(void) { return g_err.c_str(); }
 
@@ -1021,5 +1032,216 @@ int sts_check_division(unsigned long long n, unsigned long long seed, int device
   if (e != cudaSuccess) return fail(STS_ERR_CUDA, std::string("sts_check_division: ") + cudaGetErrorString(e));
   return STS_OK;
 }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batches: many independent cases advanced together, every kernel of a step launched once
+// for all of them (CTA z = case) and the sweep loops of all cases in one cooperative launch.
+// ---------------------------------------------------------------------------
+struct sts_batch {
+  std::vector<sts_ctx*> cases;
+  cudaStream_t s = nullptr;
+  std::vector<void*> allocs;
+  Geo* d_geos = nullptr;
+  int* d_tile_case = nullptr;
+  int* d_tile_first = nullptr;
+  LoopCtl* d_lc = nullptr;
+  int ncases = 0, ntiles = 0, precision = 0;
+  bool fixed = true;
+  dim3 cell_grid, walls_grid, tjump_grid, pt_grid;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<unsigned> counter_before;
+
+  ~sts_batch() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (void* p : allocs) cudaFree(p);
+    if (s) cudaStreamDestroy(s);
+    for (sts_ctx* c : cases) delete c;
+  }
+  template <class T>
+  int alloc(T** p, size_t n) {
+    void* q = nullptr;
+    CU(cudaMalloc(&q, sizeof(T) * (n ? n : 1)));
+    allocs.push_back(q);
+    *p = (T*)q;
+    return STS_OK;
+  }
+  bool fast() const { return precision >= 1; }
+  using PtKernel = void (*)(const Geo*, const int*, const int*, int, int, LoopCtl*);
+  PtKernel pt_kernel() const {
+    return (precision == 2 && !fixed) ? kb_pt_loop_mixed : (fast() ? kb_pt_loop_fast : kb_pt_loop);
+  }
+  int build_graph();
+};
+
+int sts_batch::build_graph() {
+  CU(cudaGraphCreate(&graph, 0));
+  cudaGraphConditionalHandle hs;
+  CU(cudaGraphConditionalHandleCreate(&hs, graph, 1, cudaGraphCondAssignDefault));
+  cudaGraphNode_t n_step;
+  cudaGraph_t b;
+  if (int r = add_while(&n_step, graph, {}, hs, &b)) return r;
+  const dim3 blk(32, 8);
+  const Geo* G = d_geos;
+  cudaGraphNode_t n[11];
+  if (int r = add_kernel(&n[0], b, {}, kb_step_begin, cell_grid, blk, G)) return r;
+  if (int r = add_kernel(&n[1], b, {n[0]}, fast() ? kb_assemble_fast : kb_assemble, cell_grid, blk, G,
+                         (unsigned long long)0, 0))
+    return r;
+  if (int r = add_kernel(&n[2], b, {n[1]}, pt_kernel(), pt_grid, blk, G, (const int*)d_tile_case,
+                         (const int*)d_tile_first, ncases, ntiles, d_lc))
+    return r;
+  {
+    cudaLaunchAttributeValue v{};
+    v.cooperative = 1;
+    CU(cudaGraphKernelNodeSetAttribute(n[2], cudaLaunchAttributeCooperative, &v));
+  }
+  if (int r = add_kernel(&n[3], b, {n[2]}, kb_correct, cell_grid, blk, G)) return r;
+  if (int r = add_kernel(&n[4], b, {n[3]}, kb_face_rho, cell_grid, blk, G)) return r;
+  if (int r = add_kernel(&n[5], b, {n[4]}, kb_bnd_walls, walls_grid, dim3(256), G,
+                         (unsigned)(PH_CONTROL | PH_SLIP_U | PH_SLIP_V), (unsigned long long)0, 0))
+    return r;
+  if (int r = add_kernel(&n[6], b, {n[5]}, kb_boundary, dim3(1, 1, ncases), dim3(1024), G,
+                         (unsigned)(PH_VEL | PH_PBEGIN), (unsigned long long)0, 0))
+    return r;
+  if (int r = add_kernel(&n[7], b, {n[6]}, kb_bnd_tjump, tjump_grid, dim3(256), G)) return r;
+  if (int r = add_kernel(&n[8], b, {n[7]}, fast() ? kb_flux_diff_fast : kb_flux_diff, cell_grid, blk, G,
+                         (unsigned)(PH_TEMP | PH_PRES)))
+    return r;
+  if (int r = add_kernel(&n[9], b, {n[8]}, kb_step_end, dim3(1, 1, ncases), dim3(1024), G, (unsigned long long)0, 0))
+    return r;
+  if (int r = add_kernel(&n[10], b, {n[9]}, kb_continue, dim3(1), dim3(256), G, ncases, (unsigned long long)hs))
+    return r;
+  CU(cudaGraphInstantiate(&exec, graph, 0));
+  return STS_OK;
+}
+
+extern "C" {
+
+int sts_open_batch(const char* const* case_dirs, int ncases, const sts_options* opt_in, sts_batch** out) {
+  g_err.clear();
+  if (out) *out = nullptr;
+  if (!case_dirs || !out || ncases < 1) return fail(STS_ERR_ARG, "bad argument");
+  if (ncases > kMaxBatchCases) return fail(STS_ERR_ARG, "too many cases for one batch");
+  sts_options opt;
+  sts_default_options(&opt);
+  if (opt_in) opt = *opt_in;
+  opt.write_files = 0;
+  opt.use_graph = 1;
+  std::unique_ptr<sts_batch> b(new sts_batch);
+  b->precision = opt.precision;
+  b->fixed = opt.fixed_sweeps != 0;
+  for (int k = 0; k < ncases; k++) {
+    if (!case_dirs[k]) return fail(STS_ERR_ARG, "null case directory");
+    sts_ctx* c = nullptr;
+    if (int r = open_impl(case_dirs[k], &opt, &c)) return r;
+    c->in_batch = true;
+    b->cases.push_back(c);
+    if ((int)c->hc.cfg.n("N_I") != 1)
+      return fail(STS_ERR_ARG, std::string("batched cases need N_I = 1: ") + case_dirs[k]);
+  }
+  CU(cudaSetDevice(opt.device));
+  CU(cudaDeviceSynchronize());  // every case's set-up is done
+  CU(cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking));
+  b->ncases = ncases;
+  std::vector<Geo> geos;
+  std::vector<int> tile_case, tile_first;
+  unsigned gx = 1, gy = 1, wx = 1, tx = 1;
+  for (int k = 0; k < ncases; k++) {
+    sts_ctx* c = b->cases[k];
+    geos.push_back(c->g);
+    tile_first.push_back((int)tile_case.size());
+    for (int t = 0; t < c->ntiles; t++) tile_case.push_back(k);
+    gx = std::max(gx, c->grid.x);
+    gy = std::max(gy, c->grid.y);
+    wx = std::max(wx, c->walls_grid().x);
+    tx = std::max(tx, c->tjump_grid().x);
+  }
+  b->ntiles = (int)tile_case.size();
+  if (int r = b->alloc(&b->d_geos, ncases)) return r;
+  if (int r = b->alloc(&b->d_tile_case, tile_case.size())) return r;
+  if (int r = b->alloc(&b->d_tile_first, tile_first.size())) return r;
+  if (int r = b->alloc(&b->d_lc, 1)) return r;
+  CU(cudaMemcpy(b->d_geos, geos.data(), sizeof(Geo) * ncases, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(b->d_tile_case, tile_case.data(), sizeof(int) * tile_case.size(), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(b->d_tile_first, tile_first.data(), sizeof(int) * tile_first.size(), cudaMemcpyHostToDevice));
+  CU(cudaMemset(b->d_lc, 0, sizeof(LoopCtl)));
+  b->cell_grid = dim3(gx, gy, (unsigned)ncases);
+  b->walls_grid = dim3(wx, 1, (unsigned)ncases);
+  b->tjump_grid = dim3(tx, 1, (unsigned)ncases);
+  int sms = 0, per_sm = 0;
+  CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, opt.device));
+  CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b->pt_kernel(), 256, 0));
+  if (per_sm < 1) return fail(STS_ERR_CUDA, "the sweep-loop kernel does not fit on a multiprocessor");
+  b->pt_grid = dim3((unsigned)std::max(1, std::min(b->ntiles, per_sm * sms)));
+  if (int r = b->build_graph()) return r;
+  *out = b.release();
+  return STS_OK;
+}
+
+int sts_batch_step(sts_batch* b, int nsteps, int* steps_done) {
+  if (!b || nsteps < 0) return fail(STS_ERR_ARG, "bad argument");
+  int done = 0;
+  if (nsteps > 0) {
+    sts_ctx* c0 = b->cases[0];
+    CU(cudaSetDevice(c0->opt.device));
+    std::vector<unsigned> before(b->ncases), status_before(b->ncases);
+    for (int k = 0; k < b->ncases; k++) {
+      before[k] = b->cases[k]->h_ctl->it_counter;
+      status_before[k] = b->cases[k]->h_ctl->status;
+    }
+    for (sts_ctx* c : b->cases) CU(cudaStreamSynchronize(c->s));  // field uploads of the cases land first
+    kb_set_steps<<<1, 256, 0, b->s>>>(b->d_geos, b->ncases, (unsigned)nsteps);
+    CU(cudaGetLastError());
+    CU(cudaGraphLaunch(b->exec, b->s));
+    CU(cudaStreamSynchronize(b->s));
+    bool nonfinite = false;
+    for (int k = 0; k < b->ncases; k++) {
+      sts_ctx* c = b->cases[k];
+      if (int r = c->read_ctl()) return r;
+      done = std::max(done, (int)(c->h_ctl->it_counter - before[k]));
+      if (!c->h_ctl->continue_step) c->finished = true;
+      if (c->h_ctl->status & ST_BARRIER_TIMEOUT) return fail(STS_ERR_CUDA, "a grid barrier of the sweep loop timed out");
+      if (c->h_ctl->status & ~status_before[k] & ST_NONFINITE) nonfinite = true;
+    }
+    if (nonfinite) {
+      if (steps_done) *steps_done = done;
+      return fail(STS_ERR_NONFINITE, "a residual became NaN or Inf in at least one case");
+    }
+  }
+  if (steps_done) *steps_done = done;
+  return STS_OK;
+}
+
+int sts_batch_step_timed(sts_batch* b, int nsteps, int* steps_done, double* device_ms) {
+  if (!b || nsteps < 0) return fail(STS_ERR_ARG, "bad argument");
+  CU(cudaSetDevice(b->cases[0]->opt.device));
+  cudaEvent_t e0, e1;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  CU(cudaEventRecord(e0, b->s));
+  int done = 0;
+  const int r = sts_batch_step(b, nsteps, &done);
+  cudaEventRecord(e1, b->s);
+  cudaEventSynchronize(e1);
+  float t = 0;
+  cudaEventElapsedTime(&t, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (device_ms) *device_ms = t;
+  if (steps_done) *steps_done = done;
+  return r;
+}
+
+int sts_batch_case(sts_batch* b, int index, sts_ctx** out) {
+  if (!b || !out || index < 0 || index >= b->ncases) return fail(STS_ERR_ARG, "bad case index");
+  *out = b->cases[index];
+  return STS_OK;
+}
+
+void sts_batch_destroy(sts_batch* b) { delete b; }
 
 }  // extern "C"

@@ -27,7 +27,8 @@ EXPORTS = [
     "sts_default_options", "sts_open_case", "sts_step", "sts_get_field", "sts_set_field", "sts_dims",
     "sts_stats", "sts_sweep_history", "sts_write_outputs", "sts_run_case", "sts_sync", "sts_destroy",
     "sts_last_error", "sts_inspect_case", "sts_step_timed", "sts_profile_steps", "sts_pt_sweeps",
-    "sts_pt_sweeps_noalloc", "sts_check_division",
+    "sts_pt_sweeps_noalloc", "sts_check_division", "sts_open_batch", "sts_batch_step", "sts_batch_step_timed",
+    "sts_batch_case", "sts_batch_destroy",
 ]
 
 KERNELS = ["step_begin", "assemble", "sweep_loop", "correct", "face_rho", "boundary", "flux_diff", "step_end"]
@@ -110,11 +111,15 @@ def _dptr(a: np.ndarray):
 class Solver:
     """One case on one GPU: the reference's solve loop behind the C ABI."""
 
-    def __init__(self, case_dir: str, fixed_sweeps=True, use_graph=True, device=0, precision=EXACT):
+    def __init__(self, case_dir: str, fixed_sweeps=True, use_graph=True, device=0, precision=EXACT, _handle=None):
         lib = load()
-        self._h = C.c_void_p()
-        opt = options(fixed_sweeps, use_graph, device, False, precision)
-        _check(lib.sts_open_case(case_dir.encode(), C.byref(opt), C.byref(self._h)))
+        self._owned = _handle is None
+        if _handle is None:
+            self._h = C.c_void_p()
+            opt = options(fixed_sweeps, use_graph, device, False, precision)
+            _check(lib.sts_open_case(case_dir.encode(), C.byref(opt), C.byref(self._h)))
+        else:
+            self._h = _handle
         nx, ny = C.c_int(), C.c_int()
         _check(lib.sts_dims(self._h, C.byref(nx), C.byref(ny)))
         self.Nx, self.Ny = nx.value, ny.value
@@ -178,7 +183,8 @@ class Solver:
 
     def close(self):
         if self._h:
-            load().sts_destroy(self._h)
+            if self._owned:
+                load().sts_destroy(self._h)
             self._h = C.c_void_p()
 
     def __enter__(self):
@@ -261,3 +267,53 @@ def check_division(n: int, seed: int = 1, device: int = 0) -> int:
     out = C.c_ulonglong()
     _check(lib.sts_check_division(int(n), int(seed), int(device), C.byref(out)))
     return out.value
+
+
+class Batch:
+    """Many independent cases advanced together (one launch per kernel and step for all)."""
+
+    def __init__(self, case_dirs, fixed_sweeps=False, device=0, precision=EXACT):
+        lib = load()
+        lib.sts_open_batch.argtypes = [C.POINTER(C.c_char_p), C.c_int, C.POINTER(Options), C.POINTER(C.c_void_p)]
+        lib.sts_batch_step.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int)]
+        lib.sts_batch_step_timed.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        lib.sts_batch_case.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
+        lib.sts_batch_destroy.argtypes = [C.c_void_p]
+        dirs = (C.c_char_p * len(case_dirs))(*[d.encode() for d in case_dirs])
+        self._h = C.c_void_p()
+        opt = options(fixed_sweeps, True, device, False, precision)
+        _check(lib.sts_open_batch(dirs, len(case_dirs), C.byref(opt), C.byref(self._h)))
+        self.cases = []
+        for k in range(len(case_dirs)):
+            h = C.c_void_p()
+            _check(lib.sts_batch_case(self._h, k, C.byref(h)))
+            self.cases.append(Solver("", _handle=h))
+
+    def step(self, n: int = 1) -> int:
+        done = C.c_int()
+        _check(load().sts_batch_step(self._h, int(n), C.byref(done)))
+        return done.value
+
+    def step_timed(self, n: int):
+        done, ms = C.c_int(), C.c_double()
+        _check(load().sts_batch_step_timed(self._h, int(n), C.byref(done), C.byref(ms)))
+        return done.value, ms.value
+
+    def close(self):
+        if self._h:
+            for c in self.cases:
+                c._h = C.c_void_p()
+            load().sts_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
