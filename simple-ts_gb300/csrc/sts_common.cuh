@@ -149,9 +149,9 @@ struct Geo {
   double rht, r3;
   // --- precision modes 1 and 2 ---
   // FP32 correction sweeps: coefficients c[0..4] of the T correction, a[0..3] of the p
-  // numerator, the base-sweep values T1, q, Den and the first defects dT, dp; e_p/e_T are the
+  // numerator, the base-sweep values T1, H/T1, p1, Den and the defects dT, dp; e_p/e_T are the
   // double-buffered corrections
-  float *c32[5], *a32[4], *T1, *q1, *den1, *dT, *dp;
+  float *c32[5], *a32[4], *T1, *hT, *q1, *den1, *dT, *dp;
   float *ep[2], *eT[2];
   int precision;  // 0 bit-exact FP64, 1 FP64 with reciprocal/FMA arithmetic, 2 = 1 + FP32 correction sweeps
 };

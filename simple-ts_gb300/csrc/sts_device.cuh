@@ -44,31 +44,82 @@ constexpr int kMaxColumn = 1024;  // rows staged in shared memory by the inflow-
 // Running maximum that ignores NaN exactly like "if (m < fabs(r)) m = fabs(r)".
 __device__ __forceinline__ double mx(double m, double x) { return (m < x) ? x : m; }
 
-// Block-wide max of two non-negative values, folded into global maxima by bit pattern
-// (for non-negative IEEE doubles the bit patterns order like the values).
-__device__ void block_max2(double a, double b, unsigned long long* ga, unsigned long long* gb, unsigned int* status) {
-  __shared__ double sa[32], sb[32];
+// Block-wide max of two non-negative values, folded into global maxima by bit pattern: for
+// non-negative IEEE numbers the bit patterns order like the values, so the reduction runs on
+// the integer pipes (the FP64 pipe is the scarce one).  NaN is left out of the maximum, as the
+// reference's "if (m < fabs(r)) m = fabs(r)" leaves it out, and flagged in *status together
+// with +inf.
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) { return a > b ? a : b; }
+
+__device__ void block_max2_bits(unsigned long long a, unsigned long long b, unsigned long long* ga,
+                                unsigned long long* gb) {
+  __shared__ unsigned long long sa[32], sb[32];
   const int lane = (threadIdx.x + threadIdx.y * blockDim.x) & 31;
   const int warp = (threadIdx.x + threadIdx.y * blockDim.x) >> 5;
   const int nw = (blockDim.x * blockDim.y + 31) >> 5;
-  if (!(a <= 1.7976931348623157e308) && a == a) atomicOr(status, 1u);  // +inf
-  if (a != a || b != b) atomicOr(status, 1u);                           // NaN
   for (int o = 16; o > 0; o >>= 1) {
-    a = mx(a, __shfl_xor_sync(0xffffffffu, a, o));
-    b = mx(b, __shfl_xor_sync(0xffffffffu, b, o));
+    a = umax64(a, __shfl_xor_sync(0xffffffffu, a, o));
+    b = umax64(b, __shfl_xor_sync(0xffffffffu, b, o));
   }
   if (lane == 0) { sa[warp] = a; sb[warp] = b; }
   __syncthreads();
   if (warp == 0) {
-    a = lane < nw ? sa[lane] : 0.0;
-    b = lane < nw ? sb[lane] : 0.0;
+    a = lane < nw ? sa[lane] : 0ull;
+    b = lane < nw ? sb[lane] : 0ull;
     for (int o = 16; o > 0; o >>= 1) {
-      a = mx(a, __shfl_xor_sync(0xffffffffu, a, o));
-      b = mx(b, __shfl_xor_sync(0xffffffffu, b, o));
+      a = umax64(a, __shfl_xor_sync(0xffffffffu, a, o));
+      b = umax64(b, __shfl_xor_sync(0xffffffffu, b, o));
     }
     if (lane == 0) {
-      if (a > 0) atomicMax(ga, as_b(a));
-      if (b > 0) atomicMax(gb, as_b(b));
+      if (a) atomicMax(ga, a);
+      if (b) atomicMax(gb, b);
+    }
+  }
+}
+
+// Bit pattern of a residual for the maximum: NaN and +inf set the status bit, NaN counts as 0.
+__device__ __forceinline__ unsigned long long res_bits(double x, unsigned int* status) {
+  const unsigned long long m = as_b(x) & 0x7fffffffffffffffull;
+  if (m >= 0x7ff0000000000000ull) {
+    atomicOr(status, 1u);
+    if (m > 0x7ff0000000000000ull) return 0ull;
+  }
+  return m;
+}
+
+__device__ __forceinline__ void block_max2(double a, double b, unsigned long long* ga, unsigned long long* gb,
+                                           unsigned int* status) {
+  block_max2_bits(res_bits(a, status), res_bits(b, status), ga, gb);
+}
+
+// The same for FP32 residuals: reduced as 32-bit patterns, folded in as doubles (exact widening).
+__device__ void block_max2_f(float a, float b, unsigned long long* ga, unsigned long long* gb, unsigned int* status) {
+  __shared__ unsigned sa[32], sb[32];
+  unsigned ua = __float_as_uint(a) & 0x7fffffffu, ub = __float_as_uint(b) & 0x7fffffffu;
+  if (ua >= 0x7f800000u || ub >= 0x7f800000u) {
+    atomicOr(status, 1u);
+    if (ua > 0x7f800000u) ua = 0u;
+    if (ub > 0x7f800000u) ub = 0u;
+  }
+  const int lane = (threadIdx.x + threadIdx.y * blockDim.x) & 31;
+  const int warp = (threadIdx.x + threadIdx.y * blockDim.x) >> 5;
+  const int nw = (blockDim.x * blockDim.y + 31) >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    ua = max(ua, __shfl_xor_sync(0xffffffffu, ua, o));
+    ub = max(ub, __shfl_xor_sync(0xffffffffu, ub, o));
+  }
+  if (lane == 0) { sa[warp] = ua; sb[warp] = ub; }
+  __syncthreads();
+  if (warp == 0) {
+    ua = lane < nw ? sa[lane] : 0u;
+    ub = lane < nw ? sb[lane] : 0u;
+    for (int o = 16; o > 0; o >>= 1) {
+      ua = max(ua, __shfl_xor_sync(0xffffffffu, ua, o));
+      ub = max(ub, __shfl_xor_sync(0xffffffffu, ub, o));
+    }
+    if (lane == 0) {
+      if (ua) atomicMax(ga, as_b((double)__uint_as_float(ua)));
+      if (ub) atomicMax(gb, as_b((double)__uint_as_float(ub)));
     }
   }
 }
@@ -230,9 +281,15 @@ __device__ __forceinline__ void pt_loop_rounds(const Geo& g0, const Geo* __restr
       if (s.phase == PS_DONE) continue;  // uniform over the CTA
       const Geo& g = G(c);
       const Cell cl = tile_cell(g, SINGLE ? t : t - tile_first[c], (g.Nx + 31) / 32);
-      double rp = 0, rT = 0;
-      if (cl.ok) Ops::pass(g, cl, s, rp, rT);
-      if (s.phase != PS_MATERIALIZE) block_max2(rp, rT, &g.ctl->rb_p[slot], &g.ctl->rb_T[slot], &g.ctl->status);
+      if (s.phase == PS_SWEEP32) {  // FP32 residuals, reduced as floats
+        float rp = 0.f, rT = 0.f;
+        if (cl.ok) Ops::pass32(g, cl, s, rp, rT);
+        block_max2_f(rp, rT, &g.ctl->rb_p[slot], &g.ctl->rb_T[slot], &g.ctl->status);
+      } else {
+        double rp = 0, rT = 0;
+        if (cl.ok) Ops::pass(g, cl, s, rp, rT);
+        if (s.phase != PS_MATERIALIZE) block_max2(rp, rT, &g.ctl->rb_p[slot], &g.ctl->rb_T[slot], &g.ctl->status);
+      }
     }
     // clear the slot of the next round (its last readers passed the previous barrier)
     if (lead)

@@ -399,10 +399,10 @@ struct ExactOps {
     double a = 0, b = 0;
     if (s.phase == PS_FIRST) sweep_cell<true, true>(g, c, P, TT, pn, Tn, a, b);
     else sweep_cell<false, true>(g, c, P, TT, pn, Tn, a, b);
-    if (a != a || b != b) atomicOr(&g.ctl->status, ST_NONFINITE);  // the block max skips NaN
     rp = a;
     rT = b;
   }
+  static __device__ __forceinline__ void pass32(const Geo&, const Cell&, const LoopCase&, float&, float&) {}
   static __device__ __forceinline__ void advance(const Geo& g, bool lead, LoopCase& s, double res_p, double res_T) {
     advance_fp64(g, lead, s, res_p, res_T);
   }

@@ -311,8 +311,8 @@ struct FastOps {
     if (!solved) return;
     rp = fabs(pnew - P[c.ij]);
     rT = fabs(Tnew - TT[c.ij]);
-    if (rp != rp || rT != rT) atomicOr(&g.ctl->status, ST_NONFINITE);
   }
+  static __device__ __forceinline__ void pass32(const Geo&, const Cell&, const LoopCase&, float&, float&) {}
   static __device__ __forceinline__ void advance(const Geo& g, bool lead, LoopCase& s, double res_p, double res_T) {
     advance_fp64(g, lead, s, res_p, res_T);
   }
@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(256, 4) kb_pt_loop_fast(const Geo* gs, const i
 // later sweep is e' = d + (G(b + e) - G(b)), evaluated in FP32 from the correction alone:
 //   dT   = sum_k c_k e_T,k + c_5 e_p,P                (c_k = ht w_k / den_T, c_5 = ht (1-gamma) divu / den_T)
 //   e_T' = d_T + dT
-//   q    = H dT / (T1 (T1 + dT))                      (H = hx hy, T1 = T of x1)
+//   q    = (H/T1) dT / (T1 + dT)                      (H = hx hy, T1 = T of x1)
 //   e_p' = d_p + (sum_k a_k e_p,k + p1 q) / (Den1 - q)  (a_k = ht apx/apy, p1 = p of x1, Den1 = sa + H/T1)
 // which is the exact difference of two FP64 updates, so FP32 only rounds correction-sized numbers.
 // When the FP32 sweeps meet the reference's stop rule at sweep n, the iterate of sweep n-1 is
@@ -349,10 +349,11 @@ constexpr float kFloor32 = 8.0f / 16777216.0f;  // 8 units in the last place of 
 __device__ __forceinline__ void set_base(const Geo& g, const Cell& c, double T0, double p0, double T1, double p1,
                                          double sa) {
   const int ij = c.ij;
-  const double H = g.hx[c.i] * g.hy[c.j];
+  const double hT = g.hx[c.i] * g.hy[c.j] / T1;
   g.T1[ij] = (float)T1;
+  g.hT[ij] = (float)hT;
   g.q1[ij] = (float)p1;
-  g.den1[ij] = (float)(sa + H / T1);
+  g.den1[ij] = (float)(sa + hT);
   const float dT = (float)(T1 - T0), dp = (float)(p1 - p0);
   g.dT[ij] = dT;
   g.dp[ij] = dp;
@@ -369,18 +370,15 @@ __device__ __forceinline__ void sweep32_cell(const Geo& g, const Cell& c, unsign
   const float dT = g.c32[0][ij] * eT[d.i_1j] + g.c32[1][ij] * eT[d.i1j] + g.c32[2][ij] * eT[d.ij_1] +
                    g.c32[3][ij] * eT[d.ij1] + g.c32[4][ij] * ep[ij];
   const float eTnew = g.dT[ij] + dT;
-  const float T1 = g.T1[ij];
-  const float H = (float)(g.hx[c.i] * g.hy[c.j]);
-  const float q = H * dT / (T1 * (T1 + dT));
+  const float q = g.hT[ij] * dT / (g.T1[ij] + dT);
   const float num = g.a32[0][ij] * ep[d.i_1j] + g.a32[1][ij] * ep[d.i1j] + g.a32[2][ij] * ep[d.ij_1] +
                     g.a32[3][ij] * ep[d.ij1];
   const float epnew = g.dp[ij] + (num + g.q1[ij] * q) / (g.den1[ij] - q);
   g.eT[src ^ 1][ij] = eTnew;
   g.ep[src ^ 1][ij] = epnew;
   const float aT = fabsf(eTnew - eT[ij]), ap = fabsf(epnew - ep[ij]);
-  if (aT != aT || ap != ap) atomicOr(&g.ctl->status, ST_NONFINITE);
-  rT = fmaxf(rT, aT <= kFloor32 * fabsf(eTnew) ? 0.0f : aT);
-  rp = fmaxf(rp, ap <= kFloor32 * fabsf(epnew) ? 0.0f : ap);
+  rT = aT <= kFloor32 * fabsf(eTnew) ? 0.0f : aT;
+  rp = ap <= kFloor32 * fabsf(epnew) ? 0.0f : ap;
 }
 
 struct MixedOps {
@@ -399,7 +397,6 @@ struct MixedOps {
         }
         rp = fabs(pnew - P[ij]);
         rT = fabs(Tnew - TT[ij]);
-        if (rp != rp || rT != rT) atomicOr(&g.ctl->status, ST_NONFINITE);
         const Nb d = neighbours(c.i, c.j, g.Nx, g.Ny, g.bits & F_PERIODIC);
         const double ht = g.ht, r = ht * g.inv[5][ij];
         const int nb[4] = {d.i_1j, d.i1j, d.ij_1, d.ij1};
@@ -413,14 +410,6 @@ struct MixedOps {
         set_base(g, c, TT[ij], P[ij], Tnew, pnew, sa);
         return;
       }
-      case PS_SWEEP32: {
-        if (!cls_o(g.cls[ij])) return;
-        float fp = 0.f, fT = 0.f;
-        sweep32_cell(g, c, s.ec, fp, fT);
-        rp = fp;
-        rT = fT;
-        return;
-      }
       case PS_MATERIALIZE:  // the iterate of the sweep before the last FP32 one, in FP64
         g.p[base ^ 1][ij] = g.p[base][ij] + (double)g.ep[s.ec ^ 1][ij];
         g.T[base ^ 1][ij] = g.T[base][ij] + (double)g.eT[s.ec ^ 1][ij];
@@ -432,13 +421,15 @@ struct MixedOps {
         if (!sweep_cell_fast<false>(g, c, P, TT, g.p[base], g.T[base], Tnew, pnew, sa)) return;
         rp = fabs(pnew - P[ij]);
         rT = fabs(Tnew - TT[ij]);
-        if (rp != rp || rT != rT) atomicOr(&g.ctl->status, ST_NONFINITE);
         set_base(g, c, TT[ij], P[ij], Tnew, pnew, sa);
         return;
       }
       default:
         return;
     }
+  }
+  static __device__ __forceinline__ void pass32(const Geo& g, const Cell& c, const LoopCase& s, float& rp, float& rT) {
+    if (cls_o(g.cls[c.ij])) sweep32_cell(g, c, s.ec, rp, rT);
   }
   static __device__ __forceinline__ void advance(const Geo& g, bool lead, LoopCase& s, double res_p, double res_T) {
     Ctl* ctl = g.ctl;

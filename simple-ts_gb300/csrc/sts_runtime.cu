@@ -656,7 +656,7 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
   }
   if (g.precision == 2) {
     float** f32[] = {&g.c32[0], &g.c32[1], &g.c32[2], &g.c32[3], &g.c32[4], &g.a32[0], &g.a32[1], &g.a32[2], &g.a32[3],
-                     &g.T1, &g.q1, &g.den1, &g.dT, &g.dp, &g.ep[0], &g.ep[1], &g.eT[0], &g.eT[1]};
+                     &g.T1, &g.hT, &g.q1, &g.den1, &g.dT, &g.dp, &g.ep[0], &g.ep[1], &g.eT[0], &g.eT[1]};
     for (float** f : f32)
       if (int r = c->alloc(f, Na)) return r;
   }
