@@ -266,8 +266,9 @@ def batch_bench(args):
     flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")
     out = {}
     base = None
-    for name, prec in (("fp64_exact", sts.EXACT), ("fp64_fast", sts.FAST_FP64), ("fp32_corrections", sts.MIXED)):
-        b = sts.Batch(dirs, fixed_sweeps=False, precision=prec)
+    for name, prec, warm in (("fp64_exact", sts.EXACT, 0), ("fp64_fast", sts.FAST_FP64, 0),
+                             ("fp32_corrections", sts.MIXED, 0), ("fp32_corrections_warm2", sts.MIXED, 2)):
+        b = sts.Batch(dirs, fixed_sweeps=False, precision=prec, warm_start=warm)
         cells = sum(c.Nx * c.Ny for c in b.cases)
         for _ in range(max(args.warmup, 3)):
             b.step(1)
@@ -387,13 +388,15 @@ def main():
         ref.step(nref)
         base = {f: ref.field(f) for f in ("u", "v", "p", "T", "rho")}
         ref.close()
-        for name, prec in (("fp64_fast", sts.FAST_FP64), ("fp32_corrections", sts.MIXED)):
-            v = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=prec)
+        for name, prec, warm in (("fp64_fast", sts.FAST_FP64, 0), ("fp32_corrections", sts.MIXED, 0),
+                                 ("fp64_exact_warm2", sts.EXACT, 2), ("fp32_corrections_warm2", sts.MIXED, 2)):
+            v = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=prec, warm_start=warm)
             vd, vms, vsw = timed_steps(v, args.steps, args.warmup, flush, barrier)
             err = {f: float(np.linalg.norm(v.field(f) - base[f]) / np.linalg.norm(base[f])) for f in base}
             vpn, vkms, vkcnt = v.profile(max(3, min(args.steps, 10)))
             variants[name] = {
-                "precision_mode": prec, "value": Na * vd * world / (vms / 1e3), "ms_per_step": vms / max(vd, 1),
+                "precision_mode": prec, "warm_start": warm, "value": Na * vd * world / (vms / 1e3),
+                "ms_per_step": vms / max(vd, 1),
                 "speedup_vs_fp64": (Na * vd / (vms / 1e3)) / (Na * done / (total_ms / 1e3)) if done else None,
                 "rel_l2_vs_fp64": err,
                 "sweeps_per_step": float(np.mean(vsw)) if len(vsw) else 0.0,

@@ -50,9 +50,18 @@ typedef struct sts_options {
    *    fields over FP64 base fields; the sweep that meets the tolerance is recomputed in FP64,
    *    so the stopping residual is an FP64 update.  Fixed sweep counts run as mode 1. */
   int precision;
+  /* Initial iterate of every step's p-T sweeps (no counterpart in the reference, which starts from
+   * the previous step's p and T):
+   * 0: the previous step's values (the reference);
+   * 1: linear extrapolation in time, p_n + (p_n - p_{n-1}), on the solved cells;
+   * 2: quadratic extrapolation, 3 (p_n - p_{n-1}) + p_{n-2} (linear on the second step).
+   * The sweeps still iterate to the same tolerance, so the result moves only within it; the
+   * sweep count falls.  Meaningful for tolerance-terminated loops (fixed_sweeps = 0). */
+  int warm_start;
 } sts_options;
 
-/* Fills *opt with the defaults (fixed_sweeps 1, use_graph 1, device 0, write_files 1, precision 0). */
+/* Fills *opt with the defaults (fixed_sweeps 1, use_graph 1, device 0, write_files 1, precision 0,
+ * warm_start 0). */
 void sts_default_options(sts_options* opt);
 
 /* Reads a case directory (EnteredData.txt, solve_*_b.txt, restart dumps when

@@ -37,16 +37,19 @@ def load():
         lib.ora_get_class.argtypes = [P, C.POINTER(C.c_ubyte)]
         lib.ora_sweeps.argtypes = [P, C.POINTER(C.c_uint), C.c_int]
         lib.ora_stats.argtypes = [P, C.POINTER(C.c_double)]
+        lib.ora_set_warm_start.argtypes = [P, C.c_int]
         _lib = lib
     return _lib
 
 
 class Oracle:
-    def __init__(self, case_dir, fixed_sweeps=True, write_files=False):
+    def __init__(self, case_dir, fixed_sweeps=True, write_files=False, warm_start=0):
         lib = load()
         self._h = lib.ora_open(case_dir.encode(), int(fixed_sweeps), int(write_files))
         if not self._h:
             raise RuntimeError(f"oracle could not open {case_dir}")
+        if warm_start:
+            lib.ora_set_warm_start(self._h, int(warm_start))
         nx, ny = C.c_int(), C.c_int()
         lib.ora_dims(self._h, C.byref(nx), C.byref(ny))
         self.Nx, self.Ny = nx.value, ny.value

@@ -183,6 +183,12 @@ struct Oracle {
   std::string dir;
   bool write_files = true;
   bool fixed_sweeps = true;      // FIXED_NUMBER_OF_ITERATIONS_LOOP_3 (SIMPLE_TS_MPI.cpp:56)
+  // Warm start of the p-T sweeps (not in the reference; the GB300 library's option of the same
+  // name): 1 starts every step's sweeps from the linear extrapolation p_n + (p_n - p_{n-1}) on the
+  // solved cells instead of p_n.  The first step, with no history, starts from p_n.
+  int warm_start = 0;
+  std::vector<double> p_m1, T_m1, p_m2, T_m2;
+  int warm_ready = 0;  // steps of history
   bool check_wallclock = false;  // honour max_time_for_solve (CLI only)
   bool apply_saves = false;      // periodic WriteSolvedDataToFile inside step() (CLI only)
   bool finished = false;
@@ -1634,6 +1640,32 @@ void Oracle::step() {
   for (uint c = 0; c < Iter; c++) {
     max_res_p[c] = 0; max_res_T[c] = 0; max_res_p0[c] = 0; max_res_T0[c] = 0; max_Iter_p_c[c] = 0;
   }
+  if (warm_start) {
+    if (!warm_ready) {
+      p_m1.assign(p, p + Na);
+      T_m1.assign(Temper, Temper + Na);
+      p_m2 = p_m1;
+      T_m2 = T_m1;
+    } else {
+      const bool quad = warm_start == 2 && warm_ready >= 2;
+      for (const std::vector<uint>* list : {&nch_o, &bc_o})
+        for (uint n : *list) {
+          const double x = p[n], y = Temper[n];
+          if (quad) {
+            p[n] = 3.0 * (x - p_m1[n]) + p_m2[n];
+            Temper[n] = 3.0 * (y - T_m1[n]) + T_m2[n];
+          } else {
+            p[n] = x + (x - p_m1[n]);
+            Temper[n] = y + (y - T_m1[n]);
+          }
+          p_m2[n] = p_m1[n];
+          T_m2[n] = T_m1[n];
+          p_m1[n] = x;
+          T_m1[n] = y;
+        }
+    }
+    warm_ready++;
+  }
   it += ht;
   it_counter++;
   Iter_pr2 = Iter_pr1;
@@ -1906,6 +1938,8 @@ ora_handle* ora_open(const char* dir, int fixed_sweeps, int write_files) {
 
 // Runs up to n time steps; stops early when the reference's continue rule says so.
 // Returns the number of steps taken.
+void ora_set_warm_start(ora_handle* h, int mode) { h->o.warm_start = mode; }
+
 int ora_step(ora_handle* h, int n) {
   int k = 0;
   for (; k < n; k++) {

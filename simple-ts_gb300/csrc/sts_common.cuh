@@ -103,6 +103,7 @@ struct Ctl {
   // between launches)
   unsigned long long rb_p[3], rb_T[3];
   unsigned int running;       // the case takes part in the current step (batches; 1 otherwise)
+  unsigned int warm_ready;    // steps of history the warm start has
 };
 
 // Most cases one batch may hold (the sweep loop keeps their state in shared memory).
@@ -154,6 +155,10 @@ struct Geo {
   float *c32[5], *a32[4], *T1, *hT, *q1, *den1, *dT, *dp;
   float *ep[2], *eT[2];
   int precision;  // 0 bit-exact FP64, 1 FP64 with reciprocal/FMA arithmetic, 2 = 1 + FP32 correction sweeps
+  // warm start of the sweeps: 0 none (the reference), 1 linear and 2 quadratic extrapolation in
+  // time of p and T on the solved cells; p_m[k], T_m[k] hold the values of k+1 steps back
+  int warm_start;
+  double *p_m[2], *T_m[2];
 };
 
 // Neighbour indices of one cell: ij_function / ij_function_PeriodicBC (SIMPLE_TS_MPI.cpp:140-232).

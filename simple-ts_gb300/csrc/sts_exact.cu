@@ -33,6 +33,27 @@ __device__ __forceinline__ void k_step_begin_body(const Geo& g, int counters, un
     g.p_pr[c.ij] = g.p[cur][c.ij];
     g.T_pr[c.ij] = g.T[cur][c.ij];
     g.rho_pr[c.ij] = g.rho[c.ij];
+    // warm start: the sweeps of this step start from p, T extrapolated in time on the solved
+    // cells (the first step, without history, from the current values)
+    if (counters && g.warm_start && cls_o(g.cls[c.ij])) {
+      const int n = c.ij;
+      const double x = g.p[cur][n], y = g.T[cur][n];
+      const unsigned r = ctl->warm_ready;
+      if (r == 0) {
+        g.p_m[0][n] = x; g.p_m[1][n] = x;
+        g.T_m[0][n] = y; g.T_m[1][n] = y;
+      } else {
+        if (g.warm_start == 2 && r >= 2) {
+          g.p[cur][n] = 3.0 * (x - g.p_m[0][n]) + g.p_m[1][n];
+          g.T[cur][n] = 3.0 * (y - g.T_m[0][n]) + g.T_m[1][n];
+        } else {
+          g.p[cur][n] = x + (x - g.p_m[0][n]);
+          g.T[cur][n] = y + (y - g.T_m[0][n]);
+        }
+        g.p_m[1][n] = g.p_m[0][n]; g.p_m[0][n] = x;
+        g.T_m[1][n] = g.T_m[0][n]; g.T_m[0][n] = y;
+      }
+    }
   }
   if (counters && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
     if (in_graph) cudaGraphSetConditional((cudaGraphConditionalHandle)h_outer, 1);
@@ -1061,6 +1082,7 @@ __device__ __forceinline__ void step_end_body(const Geo& g, unsigned long long h
     }
   }
   if (tid == 0) {
+    if (g.warm_start) ctl->warm_ready++;
     ctl->hist_sweeps[ctl->hist_n % 4096u] = ctl->step_sweeps;
     ctl->hist_n++;
     if (ctl->steps_left > 0) ctl->steps_left--;

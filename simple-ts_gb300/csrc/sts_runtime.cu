@@ -527,6 +527,7 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
   c->t0 = std::chrono::steady_clock::now();
   std::string err;
   if (opt.precision < 0 || opt.precision > 2) return fail(STS_ERR_ARG, "precision must be 0, 1 or 2");
+  if (opt.warm_start < 0 || opt.warm_start > 2) return fail(STS_ERR_ARG, "warm_start must be 0, 1 or 2");
   if (!load_case(dir, opt.fixed_sweeps != 0, c->hc, err)) return fail(STS_ERR_INPUT, err);
   Case& h = c->hc;
   int ndev = 0;
@@ -654,6 +655,12 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
     g.rht = 1.0 / g.ht;
     g.r3 = 1.0 / 3.0;
   }
+  g.warm_start = opt.warm_start;
+  if (g.warm_start)
+    for (int k = 0; k < 2; k++) {
+      if (int r = c->alloc(&g.p_m[k], Na)) return r;
+      if (int r = c->alloc(&g.T_m[k], Na)) return r;
+    }
   if (g.precision == 2) {
     float** f32[] = {&g.c32[0], &g.c32[1], &g.c32[2], &g.c32[3], &g.c32[4], &g.a32[0], &g.a32[1], &g.a32[2], &g.a32[3],
                      &g.T1, &g.hT, &g.q1, &g.den1, &g.dT, &g.dp, &g.ep[0], &g.ep[1], &g.eT[0], &g.eT[1]};
@@ -734,6 +741,7 @@ void sts_default_options(sts_options* opt) {
   opt->device = 0;
   opt->write_files = 1;
   opt->precision = 0;
+  opt->warm_start = 0;
 }
 
 int sts_open_case(const char* case_dir, const sts_options* opt, sts_ctx** out) {

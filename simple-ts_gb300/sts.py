@@ -43,7 +43,7 @@ FIELDS = ["u", "v", "p", "T", "rho", "sqrt_T", "rho_u", "rho_v", "Fx", "Fy", "D_
 
 class Options(C.Structure):
     _fields_ = [("fixed_sweeps", C.c_int), ("use_graph", C.c_int), ("device", C.c_int), ("write_files", C.c_int),
-                ("precision", C.c_int)]
+                ("precision", C.c_int), ("warm_start", C.c_int)]
 
 
 class StsError(RuntimeError):
@@ -93,7 +93,8 @@ def _check(code: int):
         raise StsError(code, load().sts_last_error().decode())
 
 
-def options(fixed_sweeps=True, use_graph=True, device=0, write_files=False, precision=EXACT) -> Options:
+def options(fixed_sweeps=True, use_graph=True, device=0, write_files=False, precision=EXACT,
+            warm_start=0) -> Options:
     o = Options()
     load().sts_default_options(C.byref(o))
     o.fixed_sweeps = int(fixed_sweeps)
@@ -101,6 +102,7 @@ def options(fixed_sweeps=True, use_graph=True, device=0, write_files=False, prec
     o.device = int(device)
     o.write_files = int(write_files)
     o.precision = int(precision)
+    o.warm_start = int(warm_start)
     return o
 
 
@@ -111,12 +113,13 @@ def _dptr(a: np.ndarray):
 class Solver:
     """One case on one GPU: the reference's solve loop behind the C ABI."""
 
-    def __init__(self, case_dir: str, fixed_sweeps=True, use_graph=True, device=0, precision=EXACT, _handle=None):
+    def __init__(self, case_dir: str, fixed_sweeps=True, use_graph=True, device=0, precision=EXACT, warm_start=0,
+                 _handle=None):
         lib = load()
         self._owned = _handle is None
         if _handle is None:
             self._h = C.c_void_p()
-            opt = options(fixed_sweeps, use_graph, device, False, precision)
+            opt = options(fixed_sweeps, use_graph, device, False, precision, warm_start)
             _check(lib.sts_open_case(case_dir.encode(), C.byref(opt), C.byref(self._h)))
         else:
             self._h = _handle
@@ -272,7 +275,7 @@ def check_division(n: int, seed: int = 1, device: int = 0) -> int:
 class Batch:
     """Many independent cases advanced together (one launch per kernel and step for all)."""
 
-    def __init__(self, case_dirs, fixed_sweeps=False, device=0, precision=EXACT):
+    def __init__(self, case_dirs, fixed_sweeps=False, device=0, precision=EXACT, warm_start=0):
         lib = load()
         lib.sts_open_batch.argtypes = [C.POINTER(C.c_char_p), C.c_int, C.POINTER(Options), C.POINTER(C.c_void_p)]
         lib.sts_batch_step.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int)]
@@ -281,7 +284,7 @@ class Batch:
         lib.sts_batch_destroy.argtypes = [C.c_void_p]
         dirs = (C.c_char_p * len(case_dirs))(*[d.encode() for d in case_dirs])
         self._h = C.c_void_p()
-        opt = options(fixed_sweeps, True, device, False, precision)
+        opt = options(fixed_sweeps, True, device, False, precision, warm_start)
         _check(lib.sts_open_batch(dirs, len(case_dirs), C.byref(opt), C.byref(self._h)))
         self.cases = []
         for k in range(len(case_dirs)):

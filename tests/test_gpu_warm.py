@@ -1,0 +1,86 @@
+"""Warm start of the p-T sweeps (extrapolation in time of p and T): the GPU equals the oracle
+with the same warm start bit for bit, the sweep count falls, and the answer stays within the
+tolerance-level distance of the reference's (cold-start) run."""
+import tempfile
+
+import numpy as np
+import pytest
+
+import sts_cases as sc
+from conftest import golden_case
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["u", "v", "p", "T", "rho"]
+
+
+@pytest.mark.parametrize("warm", [1, 2])
+@pytest.mark.parametrize("name", ["channel_ma2.43_60x12_resid", "rayleigh_benard_32x16_resid",
+                                  "channel_circle_120x12_resid"])
+def test_warm_start_matches_oracle(name, warm, lib_built, oracle_built):
+    import ora
+    import sts
+    case, fixed = golden_case(name)
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        o = ora.Oracle(d, fixed_sweeps=fixed, warm_start=warm)
+        for use_graph in (True, False):
+            g = sts.Solver(d, fixed_sweeps=fixed, use_graph=use_graph, warm_start=warm)
+            assert g.step(10) == 10
+            if use_graph:
+                assert o.step(10) == 10
+            for f in FIELDS:
+                np.testing.assert_array_equal(g.field(f), o.field(f), err_msg=f"{f} graph={use_graph}")
+            np.testing.assert_array_equal(g.sweep_history(), o.sweeps())
+            g.close()
+
+
+def test_warm_start_cuts_sweeps_within_tolerance(lib_built, oracle_built):
+    import ora
+    import sts
+    case = sc.rayleigh_benard_case("rb", 64, 32, Nt=60)
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        cold = ora.Oracle(d, fixed_sweeps=False)
+        cold.step(60)
+        g = sts.Solver(d, fixed_sweeps=False, warm_start=2, precision=sts.MIXED)
+        assert g.step(60) == 60
+        hw, hc = g.sweep_history()[10:], cold.sweeps()[10:]
+        print("sweeps per step: cold", hc.mean(), "warm", hw.mean())
+        assert hw.mean() < 0.75 * hc.mean()
+        for f in ("p", "T"):
+            e = np.linalg.norm(g.field(f) - cold.field(f)) / np.linalg.norm(cold.field(f))
+            print(f, e)
+            assert e < 1e-6
+        g.close()
+
+
+def test_batch_warm_start_equals_single(lib_built):
+    import os
+    import sts
+    cases = sc.batch_cases(n=3, Nt=40, nx_range=(40, 100))
+    with tempfile.TemporaryDirectory() as root:
+        dirs = []
+        for k, c in enumerate(cases):
+            d = os.path.join(root, f"c{k}")
+            os.makedirs(d)
+            c.write(d)
+            dirs.append(d)
+        b = sts.Batch(dirs, fixed_sweeps=False, warm_start=2)
+        assert b.step(8) == 8
+        for k, d in enumerate(dirs):
+            s = sts.Solver(d, fixed_sweeps=False, warm_start=2)
+            s.step(8)
+            for f in FIELDS:
+                np.testing.assert_array_equal(b.cases[k].field(f), s.field(f), err_msg=f"case {k} {f}")
+            s.close()
+        b.close()
+
+
+def test_bad_warm_start_rejected(lib_built):
+    import sts
+    case = sc.channel_case("c", 20, 6, 0.2, 0.002, 1e-3, 5)
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        with pytest.raises(sts.StsError):
+            sts.Solver(d, warm_start=7)
