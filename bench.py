@@ -70,6 +70,13 @@ def profile_target(args):
     import sts
     import build as stsbuild
     stsbuild.build()
+    if args.workload == "batch64":
+        dirs = batch_dirs()
+        b = sts.Batch(dirs, fixed_sweeps=False, precision=args.precision, use_graph=False)
+        b.step(args.profile_target)
+        print(f"profile target: batch64, {args.profile_target} steps, {sum(c.Nx * c.Ny for c in b.cases)} cells")
+        b.close()
+        return
     _, d = make_case(args.workload)
     s = sts.Solver(d, fixed_sweeps=False, use_graph=False, precision=args.precision)
     s.step(args.profile_target)
@@ -245,16 +252,9 @@ def launches_per_step(kcnt, pn):
     return sum(kcnt.values()) / max(pn, 1)
 
 
-def batch_bench(args):
-    """The 64-case batch (nx ~ U{200..800}, ny = nx/10, Mach, Kn and square position drawn
-    with seed 20261204): all cases advance together, one launch per kernel and step.  Prints a
-    JSON line of the same shape as the main bench (no e2e, no CPU baseline)."""
-    import numpy as np
-    import torch
-    import sts
+def batch_dirs():
+    """Case directories of the 64-case batch (seed 20261204)."""
     import sts_cases as sc
-    import build as stsbuild
-    stsbuild.build()
     cases = sc.batch_cases(n=64, Nt=10 ** 7)
     root = tempfile.mkdtemp(prefix="sts_batch_")
     dirs = []
@@ -263,11 +263,25 @@ def batch_bench(args):
         os.makedirs(d)
         c.write(d)
         dirs.append(d)
+    return dirs
+
+
+def batch_bench(args):
+    """The 64-case batch (nx ~ U{200..800}, ny = nx/10, Mach, Kn and square position drawn
+    with seed 20261204): all cases advance together, one launch per kernel and step.  Prints a
+    JSON line of the same shape as the main bench (no e2e, no CPU baseline)."""
+    import numpy as np
+    import torch
+    import sts
+    import build as stsbuild
+    stsbuild.build()
+    dirs = batch_dirs()
     flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")
     out = {}
     base = None
     for name, prec, warm in (("fp64_exact", sts.EXACT, 0), ("fp64_fast", sts.FAST_FP64, 0),
-                             ("fp32_corrections", sts.MIXED, 0), ("fp32_corrections_warm2", sts.MIXED, 2)):
+                             ("fp32_corrections", sts.MIXED, 0), ("fp32_corrections_warm2", sts.MIXED, 2),
+                             ("fp32_corrections_learned", sts.MIXED, 3)):
         b = sts.Batch(dirs, fixed_sweeps=False, precision=prec, warm_start=warm)
         cells = sum(c.Nx * c.Ny for c in b.cases)
         for _ in range(max(args.warmup, 3)):
@@ -389,7 +403,8 @@ def main():
         base = {f: ref.field(f) for f in ("u", "v", "p", "T", "rho")}
         ref.close()
         for name, prec, warm in (("fp64_fast", sts.FAST_FP64, 0), ("fp32_corrections", sts.MIXED, 0),
-                                 ("fp64_exact_warm2", sts.EXACT, 2), ("fp32_corrections_warm2", sts.MIXED, 2)):
+                                 ("fp64_exact_warm2", sts.EXACT, 2), ("fp32_corrections_warm2", sts.MIXED, 2),
+                                 ("fp32_corrections_learned", sts.MIXED, 3)):
             v = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=prec, warm_start=warm)
             vd, vms, vsw = timed_steps(v, args.steps, args.warmup, flush, barrier)
             err = {f: float(np.linalg.norm(v.field(f) - base[f]) / np.linalg.norm(base[f])) for f in base}

@@ -54,7 +54,10 @@ typedef struct sts_options {
    * the previous step's p and T):
    * 0: the previous step's values (the reference);
    * 1: linear extrapolation in time, p_n + (p_n - p_{n-1}), on the solved cells;
-   * 2: quadratic extrapolation, 3 (p_n - p_{n-1}) + p_{n-2} (linear on the second step).
+   * 2: quadratic extrapolation, 3 (p_n - p_{n-1}) + p_{n-2} (linear on the second step);
+   * 3: a linear predictor learned from the run itself: p_n + sum_k w_k (p_{n-k} - p_{n-k-1}),
+   *    k = 0..2, with w refitted every step by least squares on the last 6 steps (separately
+   *    for p and T; quadratic extrapolation until the history is long enough).
    * The sweeps still iterate to the same tolerance, so the result moves only within it; the
    * sweep count falls.  Meaningful for tolerance-terminated loops (fixed_sweeps = 0). */
   int warm_start;
@@ -180,7 +183,8 @@ int sts_check_division(unsigned long long n, unsigned long long seed, int device
  * runs one case per process (or per MPI job); a batch is the GB300 form of running many such
  * jobs side by side, with the same results as running each case alone.  Restrictions: at most
  * 256 cases, N_I = 1 in every case, one sweep mode (opt->fixed_sweeps) and one precision for
- * the whole batch.  opt->use_graph and opt->write_files are ignored (graph, no files). */
+ * the whole batch.  opt->use_graph = 0 launches the kernels step by step from the host (same
+ * results; for per-kernel profiling); opt->write_files is ignored. */
 typedef struct sts_batch sts_batch;
 int sts_open_batch(const char* const* case_dirs, int ncases, const sts_options* opt, sts_batch** out);
 

@@ -189,6 +189,11 @@ struct Oracle {
   int warm_start = 0;
   std::vector<double> p_m1, T_m1, p_m2, T_m2;
   int warm_ready = 0;  // steps of history
+  // mode 3: x0 = x_n + sum_k w_k D_{n-k} (D_j = x_j - x_{j-1}), k = 0..2, with w fitted by least
+  // squares on the last kWin steps of the trajectory (see warm_ar)
+  static constexpr int kRing = 9, kWin = 6;
+  std::vector<std::vector<double>> Dp, DT;  // ring of differences on the solved cells
+  void warm_ar();
   bool check_wallclock = false;  // honour max_time_for_solve (CLI only)
   bool apply_saves = false;      // periodic WriteSolvedDataToFile inside step() (CLI only)
   bool finished = false;
@@ -1630,6 +1635,85 @@ void Oracle::pt_sweeps() {
   } while (continue_iter_p_c);
 }
 
+// Least-squares fit and application of the mode-3 warm start.  With D_t = x_t - x_{t-1} on the
+// solved cells and the regressors in the difference basis d(t) = (D_t, D_t - D_{t-1},
+// D_t - 2 D_{t-1} + D_{t-2}) (the same span as D_t, D_{t-1}, D_{t-2}, but well conditioned when the
+// trajectory is smooth), c minimises sum over the last kWin steps s of |D_s - c . d(s-1)|^2;
+// the step's initial iterate is x_n + c . d(n), i.e. x_n + w_0 D_n + w_1 D_{n-1} + w_2 D_{n-2}
+// with w = (c0 + c1 + c2, -c1 - 2 c2, c2).  Until kWin + 3 differences exist, and whenever the
+// normal equations are (nearly) singular, w = (2, -1, 0) (quadratic extrapolation; (1, 0, 0)
+// on the second step).
+void Oracle::warm_ar() {
+  std::vector<uint> cells(nch_o);
+  cells.insert(cells.end(), bc_o.begin(), bc_o.end());
+  const size_t m = cells.size();
+  if (!warm_ready) {
+    p_m1.assign(p, p + Na);
+    T_m1.assign(Temper, Temper + Na);
+    Dp.assign(kRing, std::vector<double>(m, 0.0));
+    DT.assign(kRing, std::vector<double>(m, 0.0));
+    warm_ready = 1;
+    return;
+  }
+  const int h = warm_ready - 1;  // index of the newest difference
+  for (size_t q = 0; q < m; q++) {
+    const uint n = cells[q];
+    Dp[h % kRing][q] = p[n] - p_m1[n];
+    DT[h % kRing][q] = Temper[n] - T_m1[n];
+    p_m1[n] = p[n];
+    T_m1[n] = Temper[n];
+  }
+  const int have = h + 1;
+  for (int f = 0; f < 2; f++) {
+    const std::vector<std::vector<double>>& R = f ? DT : Dp;
+    auto D = [&](int t, size_t q) { return R[t % kRing][q]; };
+    double* x = f ? Temper : p;
+    double w[3] = {2.0, -1.0, 0.0};
+    if (have < 2) {
+      w[0] = 1.0;
+      w[1] = 0.0;
+    }
+    if (have >= 3 + kWin) {
+      double G[3][3] = {{0}}, r[3] = {0};
+      for (int s = h - kWin + 1; s <= h; s++)
+        for (size_t q = 0; q < m; q++) {
+          const double a0 = D(s - 1, q), a1 = D(s - 1, q) - D(s - 2, q);
+          const double a2 = D(s - 1, q) - 2.0 * D(s - 2, q) + D(s - 3, q);
+          const double a[3] = {a0, a1, a2}, y = D(s, q);
+          for (int i = 0; i < 3; i++) {
+            r[i] += a[i] * y;
+            for (int j = 0; j < 3; j++) G[i][j] += a[i] * a[j];
+          }
+        }
+      const double det = G[0][0] * (G[1][1] * G[2][2] - G[1][2] * G[2][1]) -
+                         G[0][1] * (G[1][0] * G[2][2] - G[1][2] * G[2][0]) +
+                         G[0][2] * (G[1][0] * G[2][1] - G[1][1] * G[2][0]);
+      const double scale = G[0][0] * G[1][1] * G[2][2];
+      if (scale > 0 && std::fabs(det) > 1e-6 * scale) {
+        double c[3];
+        for (int i = 0; i < 3; i++) {
+          double Gi[3][3];
+          for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) Gi[a][b] = (b == i) ? r[a] : G[a][b];
+          c[i] = (Gi[0][0] * (Gi[1][1] * Gi[2][2] - Gi[1][2] * Gi[2][1]) -
+                  Gi[0][1] * (Gi[1][0] * Gi[2][2] - Gi[1][2] * Gi[2][0]) +
+                  Gi[0][2] * (Gi[1][0] * Gi[2][1] - Gi[1][1] * Gi[2][0])) / det;
+        }
+        w[0] = c[0] + c[1] + c[2];
+        w[1] = -c[1] - 2.0 * c[2];
+        w[2] = c[2];
+      }
+    }
+    for (size_t q = 0; q < m; q++) {
+      double e = w[0] * D(h, q);
+      if (have >= 2) e += w[1] * D(h - 1, q);
+      if (have >= 3) e += w[2] * D(h - 2, q);
+      x[cells[q]] += e;
+    }
+  }
+  warm_ready++;
+}
+
 // one pass of the time loop body, SIMPLE_TS_MPI.cpp:3230-4691
 void Oracle::step() {
   std::memcpy(p_pr, p, Na * sizeof(double));
@@ -1640,7 +1724,9 @@ void Oracle::step() {
   for (uint c = 0; c < Iter; c++) {
     max_res_p[c] = 0; max_res_T[c] = 0; max_res_p0[c] = 0; max_res_T0[c] = 0; max_Iter_p_c[c] = 0;
   }
-  if (warm_start) {
+  if (warm_start == 3) {
+    warm_ar();
+  } else if (warm_start) {
     if (!warm_ready) {
       p_m1.assign(p, p + Na);
       T_m1.assign(Temper, Temper + Na);

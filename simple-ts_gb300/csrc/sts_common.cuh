@@ -104,7 +104,14 @@ struct Ctl {
   unsigned long long rb_p[3], rb_T[3];
   unsigned int running;       // the case takes part in the current step (batches; 1 otherwise)
   unsigned int warm_ready;    // steps of history the warm start has
+  // mode 3: per step, the normal-equation terms of its newest target (6 Gram entries and 3
+  // right-hand sides, for p and for T) over the last kWarmWin steps, and the fitted weights
+  double warm_acc[6][2][9];
+  double warm_w[2][3];
 };
+
+// Learned warm start: differences kept, and steps of the least-squares window.
+constexpr int kWarmRing = 4, kWarmWin = 6;
 
 // Most cases one batch may hold (the sweep loop keeps their state in shared memory).
 constexpr int kMaxBatchCases = 256;
@@ -156,9 +163,13 @@ struct Geo {
   float *ep[2], *eT[2];
   int precision;  // 0 bit-exact FP64, 1 FP64 with reciprocal/FMA arithmetic, 2 = 1 + FP32 correction sweeps
   // warm start of the sweeps: 0 none (the reference), 1 linear and 2 quadratic extrapolation in
-  // time of p and T on the solved cells; p_m[k], T_m[k] hold the values of k+1 steps back
+  // time of p and T on the solved cells, 3 the fitted linear predictor; p_m[k], T_m[k] hold the
+  // values of k+1 steps back
   int warm_start;
   double *p_m[2], *T_m[2];
+  // mode 3: ring of the last kWarmRing step differences of p and T, per-CTA partial sums
+  double *Dp[4], *DT[4];
+  float* warm_part;
 };
 
 // Neighbour indices of one cell: ij_function / ij_function_PeriodicBC (SIMPLE_TS_MPI.cpp:140-232).

@@ -35,7 +35,7 @@ __device__ __forceinline__ void k_step_begin_body(const Geo& g, int counters, un
     g.rho_pr[c.ij] = g.rho[c.ij];
     // warm start: the sweeps of this step start from p, T extrapolated in time on the solved
     // cells (the first step, without history, from the current values)
-    if (counters && g.warm_start && cls_o(g.cls[c.ij])) {
+    if (counters && (g.warm_start == 1 || g.warm_start == 2) && cls_o(g.cls[c.ij])) {
       const int n = c.ij;
       const double x = g.p[cur][n], y = g.T[cur][n];
       const unsigned r = ctl->warm_ready;
@@ -90,15 +90,179 @@ __global__ void kb_set_steps(const Geo* gs, int ncases, unsigned n) {
   for (int c = threadIdx.x; c < ncases; c += blockDim.x) gs[c].ctl->steps_left = n;
 }
 
-// The batched step loop goes on while any case runs and has steps left.
-__global__ void kb_continue(const Geo* gs, int ncases, unsigned long long h_step) {
+// The batched step loop goes on while any case runs and has steps left: sets the graph's loop
+// condition, or *flag outside a graph.
+__global__ void kb_continue(const Geo* gs, int ncases, unsigned long long h_step, unsigned* flag) {
   int any = 0;
   for (int c = threadIdx.x; c < ncases; c += blockDim.x) {
     const Ctl* ctl = gs[c].ctl;
     any |= (ctl->continue_step && ctl->steps_left > 0) ? 1 : 0;
   }
   any = __syncthreads_or(any);
-  if (threadIdx.x == 0) cudaGraphSetConditional((cudaGraphConditionalHandle)h_step, any ? 1 : 0);
+  if (threadIdx.x == 0) {
+    if (flag) *flag = any ? 1u : 0u;
+    else cudaGraphSetConditional((cudaGraphConditionalHandle)h_step, any ? 1 : 0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Learned warm start (mode 3).  The sweeps of a step start from x_n + w0 D_n + w1 D_{n-1} +
+// w2 D_{n-2} (D_t = x_t - x_{t-1} on the solved cells), a linear predictor fitted by least
+// squares on the solver's own trajectory: over the last kWarmWin steps s, D_s is regressed on
+// d(s-1) = (D_{s-1}, D_{s-1} - D_{s-2}, D_{s-1} - 2 D_{s-2} + D_{s-3}) -- the span of the three
+// previous differences in a basis that stays well conditioned on smooth trajectories.  Each
+// step adds its target's Gram and right-hand-side terms (products of the FP64 differences
+// rounded to FP32, summed per CTA in FP32 and across CTAs in FP64 in a fixed order) and drops
+// the oldest; the 3x3 system is solved by Cramer's rule.  Until kWarmWin + 3 differences exist,
+// or when the system is nearly singular, the weights are those of quadratic extrapolation
+// (linear on the second step).  p and T have their own weights.
+// warm_diff: the new difference and its normal-equation terms; warm_fit: one CTA per case
+// sums them and solves; warm_apply: the initial iterate.
+// ---------------------------------------------------------------------------
+constexpr int kWarmTerms = 9;  // per field: Gram entries 00 01 02 11 12 22, then right-hand sides 0 1 2
+
+__device__ __forceinline__ void warm_diff_body(const Geo& g) {
+  Cell c = cell(g);
+  const Ctl* ctl = g.ctl;
+  const unsigned r = ctl->warm_ready, cur = ctl->cur;
+  float t[2 * kWarmTerms];
+  for (int k = 0; k < 2 * kWarmTerms; k++) t[k] = 0.f;
+  if (c.ok && cls_o(g.cls[c.ij])) {
+    const int n = c.ij;
+    const double x = g.p[cur][n], y = g.T[cur][n];
+    if (r >= 1) {
+      const unsigned h = r - 1;
+      const double dn[2] = {x - g.p_m[0][n], y - g.T_m[0][n]};
+      g.Dp[h % kWarmRing][n] = dn[0];
+      g.DT[h % kWarmRing][n] = dn[1];
+      if (h >= 3) {
+        for (int f = 0; f < 2; f++) {
+          double* const* R = f ? g.DT : g.Dp;
+          const double d1 = R[(h - 1) % kWarmRing][n], d2 = R[(h - 2) % kWarmRing][n], d3 = R[(h - 3) % kWarmRing][n];
+          const float a0 = (float)d1, a1 = (float)(d1 - d2), a2 = (float)(d1 - 2.0 * d2 + d3), yy = (float)dn[f];
+          float* o = t + f * kWarmTerms;
+          o[0] = a0 * a0; o[1] = a0 * a1; o[2] = a0 * a2; o[3] = a1 * a1; o[4] = a1 * a2; o[5] = a2 * a2;
+          o[6] = a0 * yy; o[7] = a1 * yy; o[8] = a2 * yy;
+        }
+      }
+    }
+    g.p_m[0][n] = x;
+    g.T_m[0][n] = y;
+  }
+  // CTA sums, written as partials indexed by the case's own 32x8 tiling, so one case alone and
+  // the same case in a batch (whose grid is that of the largest case) add them in the same order
+  __shared__ float part[8][2 * kWarmTerms];
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x, lane = tid & 31, warp = tid >> 5;
+  for (int k = 0; k < 2 * kWarmTerms; k++) {
+    float v = t[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) part[warp][k] = v;
+  }
+  __syncthreads();
+  const int tx = (g.Nx + 31) / 32, ty = (g.Ny + 7) / 8;
+  if (tid < 2 * kWarmTerms && (int)blockIdx.x < tx && (int)blockIdx.y < ty) {
+    float v = 0.f;
+    for (int w = 0; w < (int)((blockDim.x * blockDim.y) >> 5); w++) v += part[w][tid];
+    g.warm_part[(blockIdx.x + blockIdx.y * tx) * (2 * kWarmTerms) + tid] = v;
+  }
+}
+
+__device__ __forceinline__ double det3(const double m[3][3]) {
+  return m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) - m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+         m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+}
+
+// One CTA of 32 x 2*kWarmTerms threads per case: warp k sums term k over the case's CTAs.
+__device__ __forceinline__ void warm_fit_body(const Geo& g) {
+  Ctl* ctl = g.ctl;
+  const unsigned r = ctl->warm_ready;
+  const int nblocks = ((g.Nx + 31) / 32) * ((g.Ny + 7) / 8);
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x, lane = tid & 31, k = tid >> 5;
+  __shared__ double sum[2 * kWarmTerms];
+  if (r >= 4 && k < 2 * kWarmTerms) {
+    double v = 0.0;
+    for (int b = lane; b < nblocks; b += 32) v += (double)g.warm_part[b * (2 * kWarmTerms) + k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) sum[k] = v;
+  }
+  __syncthreads();
+  if (tid != 0) return;
+  if (r == 0) {
+    ctl->warm_ready = 1;
+    return;
+  }
+  const unsigned h = r - 1, have = h + 1;
+  if (h >= 3)
+    for (int q = 0; q < 2 * kWarmTerms; q++) ctl->warm_acc[h % kWarmWin][q / kWarmTerms][q % kWarmTerms] = sum[q];
+  for (int f = 0; f < 2; f++) {
+    double w[3] = {2.0, -1.0, 0.0};
+    if (have < 2) {
+      w[0] = 1.0;
+      w[1] = 0.0;
+    }
+    if (have >= 3u + kWarmWin) {
+      double a[kWarmTerms] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      for (int s2 = 0; s2 < kWarmWin; s2++)
+        for (int q = 0; q < kWarmTerms; q++) a[q] += ctl->warm_acc[s2][f][q];
+      const double G[3][3] = {{a[0], a[1], a[2]}, {a[1], a[3], a[4]}, {a[2], a[4], a[5]}};
+      const double rhs[3] = {a[6], a[7], a[8]};
+      const double det = det3(G), scale = G[0][0] * G[1][1] * G[2][2];
+      if (scale > 0 && fabs(det) > 1e-6 * scale) {
+        double cc[3];
+        for (int i = 0; i < 3; i++) {
+          double Gi[3][3];
+          for (int x = 0; x < 3; x++)
+            for (int y = 0; y < 3; y++) Gi[x][y] = (y == i) ? rhs[x] : G[x][y];
+          cc[i] = det3(Gi) / det;
+        }
+        w[0] = cc[0] + cc[1] + cc[2];
+        w[1] = -cc[1] - 2.0 * cc[2];
+        w[2] = cc[2];
+      }
+    }
+    for (int q = 0; q < 3; q++) ctl->warm_w[f][q] = w[q];
+  }
+  ctl->warm_ready = r + 1;
+}
+
+__device__ __forceinline__ void warm_apply_body(const Geo& g) {
+  Cell c = cell(g);
+  const Ctl* ctl = g.ctl;
+  const unsigned r = ctl->warm_ready;  // already counts this step
+  if (r < 2 || !c.ok || !cls_o(g.cls[c.ij])) return;
+  const unsigned h = r - 2, have = h + 1, cur = ctl->cur;
+  const int n = c.ij;
+  double ep = ctl->warm_w[0][0] * g.Dp[h % kWarmRing][n];
+  double eT = ctl->warm_w[1][0] * g.DT[h % kWarmRing][n];
+  if (have >= 2) {
+    ep += ctl->warm_w[0][1] * g.Dp[(h - 1) % kWarmRing][n];
+    eT += ctl->warm_w[1][1] * g.DT[(h - 1) % kWarmRing][n];
+  }
+  if (have >= 3) {
+    ep += ctl->warm_w[0][2] * g.Dp[(h - 2) % kWarmRing][n];
+    eT += ctl->warm_w[1][2] * g.DT[(h - 2) % kWarmRing][n];
+  }
+  g.p[cur][n] += ep;
+  g.T[cur][n] += eT;
+}
+
+__global__ void k_warm_diff(Geo g) { warm_diff_body(g); }
+__global__ void k_warm_fit(Geo g) { warm_fit_body(g); }
+__global__ void k_warm_apply(Geo g) { warm_apply_body(g); }
+__global__ void kb_warm_diff(const Geo* gs) {
+  __shared__ Geo sg;
+  if (!stage_geo(sg, gs)) return;
+  warm_diff_body(sg);
+}
+__global__ void kb_warm_fit(const Geo* gs) {
+  __shared__ Geo sg;
+  if (!stage_geo(sg, gs)) return;
+  warm_fit_body(sg);
+}
+__global__ void kb_warm_apply(const Geo* gs) {
+  __shared__ Geo sg;
+  if (!stage_geo(sg, gs)) return;
+  warm_apply_body(sg);
 }
 
 // ---------------------------------------------------------------------------
@@ -1082,7 +1246,7 @@ __device__ __forceinline__ void step_end_body(const Geo& g, unsigned long long h
     }
   }
   if (tid == 0) {
-    if (g.warm_start) ctl->warm_ready++;
+    if (g.warm_start == 1 || g.warm_start == 2) ctl->warm_ready++;
     ctl->hist_sweeps[ctl->hist_n % 4096u] = ctl->step_sweeps;
     ctl->hist_n++;
     if (ctl->steps_left > 0) ctl->steps_left--;

@@ -36,9 +36,15 @@ __global__ void k_bnd_tjump(Geo g);
 __global__ void k_sqrt_rho(Geo g, int do_rho);
 __global__ void k_boundary(Geo g, unsigned phases, unsigned long long h_outer, int in_graph);
 __global__ void k_step_end(Geo g, unsigned long long h_step, int in_graph);
+__global__ void k_warm_diff(Geo g);
+__global__ void k_warm_fit(Geo g);
+__global__ void k_warm_apply(Geo g);
+__global__ void kb_warm_diff(const Geo* gs);
+__global__ void kb_warm_fit(const Geo* gs);
+__global__ void kb_warm_apply(const Geo* gs);
 __global__ void kb_step_begin(const Geo* gs);
 __global__ void kb_set_steps(const Geo* gs, int ncases, unsigned n);
-__global__ void kb_continue(const Geo* gs, int ncases, unsigned long long h_step);
+__global__ void kb_continue(const Geo* gs, int ncases, unsigned long long h_step, unsigned* flag);
 __global__ void kb_assemble(const Geo* gs, unsigned long long h_sweep, int in_graph);
 __global__ void kb_correct(const Geo* gs);
 __global__ void kb_face_rho(const Geo* gs);

@@ -118,6 +118,16 @@ struct sts_ctx {
     else k_flux_diff<<<grid, block, 0, s>>>(g, PH_TEMP | PH_PRES);
     mark(6);
   }
+  // the learned warm start's kernels after the start of a step (mode 3)
+  template <class M>
+  void warm_launches(M mark) {
+    if (g.warm_start != 3) return;
+    mark(-1);
+    k_warm_diff<<<grid, block, 0, s>>>(g);
+    k_warm_fit<<<1, 576, 0, s>>>(g);
+    k_warm_apply<<<grid, block, 0, s>>>(g);
+    mark(0);
+  }
   bool fast() const { return g.precision >= 1; }
   bool mixed() const { return g.precision == 2 && !(hc.bits & F_FIXED_SWEEPS); }
   // the persistent sweep-loop kernel of this context and its grid (CTAs that fit at once)
@@ -198,6 +208,13 @@ int sts_ctx::build_graph() {
   CU(cudaGraphConditionalHandleCreate(&ho, b_step, 1, cudaGraphCondAssignDefault));
   cudaGraphNode_t n_begin, n_outer, n_end;
   if (int r = add_kernel(&n_begin, b_step, {}, k_step_begin, grid, block, g, 1, (unsigned long long)ho, 1)) return r;
+  if (g.warm_start == 3) {
+    cudaGraphNode_t w[3];
+    if (int r = add_kernel(&w[0], b_step, {n_begin}, k_warm_diff, grid, block, g)) return r;
+    if (int r = add_kernel(&w[1], b_step, {w[0]}, k_warm_fit, dim3(1), dim3(576), g)) return r;
+    if (int r = add_kernel(&w[2], b_step, {w[1]}, k_warm_apply, grid, block, g)) return r;
+    n_begin = w[2];
+  }
   cudaGraph_t b_outer;
   if (int r = add_while(&n_outer, b_step, {n_begin}, ho, &b_outer)) return r;
   if (int r = add_kernel(&n_end, b_step, {n_outer}, k_step_end, dim3(1), dim3(1024), g, (unsigned long long)hs, 1))
@@ -250,6 +267,7 @@ int sts_ctx::step_host(int n, int* done) {
   int k = 0;
   for (; k < n; k++) {
     k_step_begin<<<grid, block, 0, s>>>(g, 1, 0, 0);
+    warm_launches([](int) {});
     for (int outer = 0; outer < NI; outer++) {
       if (fast()) k_assemble_fast<<<grid, block, 0, s>>>(g, 0, 0);
       else k_assemble<<<grid, block, 0, s>>>(g, 0, 0);
@@ -292,6 +310,7 @@ int sts_ctx::profile(int n, double* ms, int* cnt, int* done) {
   int k = 0;
   for (; k < n; k++) {
     mark(-1); k_step_begin<<<grid, block, 0, s>>>(g, 1, 0, 0); mark(0);
+    warm_launches(mark);
     for (int outer = 0; outer < NI; outer++) {
       mark(-1);
       if (fast()) k_assemble_fast<<<grid, block, 0, s>>>(g, 0, 0);
@@ -527,7 +546,7 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
   c->t0 = std::chrono::steady_clock::now();
   std::string err;
   if (opt.precision < 0 || opt.precision > 2) return fail(STS_ERR_ARG, "precision must be 0, 1 or 2");
-  if (opt.warm_start < 0 || opt.warm_start > 2) return fail(STS_ERR_ARG, "warm_start must be 0, 1 or 2");
+  if (opt.warm_start < 0 || opt.warm_start > 3) return fail(STS_ERR_ARG, "warm_start must be 0, 1, 2 or 3");
   if (!load_case(dir, opt.fixed_sweeps != 0, c->hc, err)) return fail(STS_ERR_INPUT, err);
   Case& h = c->hc;
   int ndev = 0;
@@ -661,6 +680,14 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
       if (int r = c->alloc(&g.p_m[k], Na)) return r;
       if (int r = c->alloc(&g.T_m[k], Na)) return r;
     }
+  if (g.warm_start == 3) {
+    for (int k = 0; k < kWarmRing; k++) {
+      if (int r = c->alloc(&g.Dp[k], Na)) return r;
+      if (int r = c->alloc(&g.DT[k], Na)) return r;
+    }
+    const size_t nb = (size_t)((h.Nx + 31) / 32) * ((h.Ny + 7) / 8);
+    if (int r = c->alloc(&g.warm_part, nb * 18)) return r;  // 2 fields x 9 normal-equation terms
+  }
   if (g.precision == 2) {
     float** f32[] = {&g.c32[0], &g.c32[1], &g.c32[2], &g.c32[3], &g.c32[4], &g.a32[0], &g.a32[1], &g.a32[2], &g.a32[3],
                      &g.T1, &g.hT, &g.q1, &g.den1, &g.dT, &g.dp, &g.ep[0], &g.ep[1], &g.eT[0], &g.eT[1]};
@@ -1063,6 +1090,7 @@ struct sts_batch {
   std::vector<unsigned> counter_before;
 
   ~sts_batch() {
+    if (h_flag) cudaFreeHost(h_flag);
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     for (void* p : allocs) cudaFree(p);
@@ -1083,7 +1111,47 @@ struct sts_batch {
     return (precision == 2 && !fixed) ? kb_pt_loop_mixed : (fast() ? kb_pt_loop_fast : kb_pt_loop);
   }
   int build_graph();
+  int step_host(int n);
+  bool use_graph = true;
+  bool warm3 = false;
+  unsigned* d_flag = nullptr;
+  unsigned* h_flag = nullptr;
 };
+
+// The batched step loop launched kernel by kernel (for per-kernel profiling): the same kernels
+// as the graph, the loop condition read back after every step.
+int sts_batch::step_host(int n) {
+  const dim3 blk(32, 8);
+  const Geo* G = d_geos;
+  for (int k = 0; k < n; k++) {
+    kb_step_begin<<<cell_grid, blk, 0, s>>>(G);
+    if (warm3) {
+      kb_warm_diff<<<cell_grid, blk, 0, s>>>(G);
+      kb_warm_fit<<<dim3(1, 1, ncases), 576, 0, s>>>(G);
+      kb_warm_apply<<<cell_grid, blk, 0, s>>>(G);
+    }
+    if (fast()) kb_assemble_fast<<<cell_grid, blk, 0, s>>>(G, 0ull, 0);
+    else kb_assemble<<<cell_grid, blk, 0, s>>>(G, 0ull, 0);
+    const int* tc = d_tile_case;
+    const int* tf = d_tile_first;
+    void* args[] = {(void*)&G, (void*)&tc, (void*)&tf, (void*)&ncases, (void*)&ntiles, (void*)&d_lc};
+    CU(cudaLaunchCooperativeKernel((const void*)pt_kernel(), pt_grid, blk, args, 0, s));
+    kb_correct<<<cell_grid, blk, 0, s>>>(G);
+    kb_face_rho<<<cell_grid, blk, 0, s>>>(G);
+    kb_bnd_walls<<<walls_grid, 256, 0, s>>>(G, PH_CONTROL | PH_SLIP_U | PH_SLIP_V, 0ull, 0);
+    kb_boundary<<<dim3(1, 1, ncases), 1024, 0, s>>>(G, PH_VEL | PH_PBEGIN, 0ull, 0);
+    kb_bnd_tjump<<<tjump_grid, 256, 0, s>>>(G);
+    if (fast()) kb_flux_diff_fast<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
+    else kb_flux_diff<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
+    kb_step_end<<<dim3(1, 1, ncases), 1024, 0, s>>>(G, 0ull, 0);
+    kb_continue<<<1, 256, 0, s>>>(G, ncases, 0ull, d_flag);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(h_flag, d_flag, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    if (!*h_flag) break;
+  }
+  return STS_OK;
+}
 
 int sts_batch::build_graph() {
   CU(cudaGraphCreate(&graph, 0));
@@ -1096,6 +1164,13 @@ int sts_batch::build_graph() {
   const Geo* G = d_geos;
   cudaGraphNode_t n[11];
   if (int r = add_kernel(&n[0], b, {}, kb_step_begin, cell_grid, blk, G)) return r;
+  if (warm3) {
+    cudaGraphNode_t w[3];
+    if (int r = add_kernel(&w[0], b, {n[0]}, kb_warm_diff, cell_grid, blk, G)) return r;
+    if (int r = add_kernel(&w[1], b, {w[0]}, kb_warm_fit, dim3(1, 1, ncases), dim3(576), G)) return r;
+    if (int r = add_kernel(&w[2], b, {w[1]}, kb_warm_apply, cell_grid, blk, G)) return r;
+    n[0] = w[2];
+  }
   if (int r = add_kernel(&n[1], b, {n[0]}, fast() ? kb_assemble_fast : kb_assemble, cell_grid, blk, G,
                          (unsigned long long)0, 0))
     return r;
@@ -1121,7 +1196,8 @@ int sts_batch::build_graph() {
     return r;
   if (int r = add_kernel(&n[9], b, {n[8]}, kb_step_end, dim3(1, 1, ncases), dim3(1024), G, (unsigned long long)0, 0))
     return r;
-  if (int r = add_kernel(&n[10], b, {n[9]}, kb_continue, dim3(1), dim3(256), G, ncases, (unsigned long long)hs))
+  if (int r = add_kernel(&n[10], b, {n[9]}, kb_continue, dim3(1), dim3(256), G, ncases, (unsigned long long)hs,
+                         (unsigned*)nullptr))
     return r;
   CU(cudaGraphInstantiate(&exec, graph, 0));
   return STS_OK;
@@ -1138,8 +1214,8 @@ int sts_open_batch(const char* const* case_dirs, int ncases, const sts_options* 
   sts_default_options(&opt);
   if (opt_in) opt = *opt_in;
   opt.write_files = 0;
-  opt.use_graph = 1;
   std::unique_ptr<sts_batch> b(new sts_batch);
+  b->use_graph = opt.use_graph != 0;
   b->precision = opt.precision;
   b->fixed = opt.fixed_sweeps != 0;
   for (int k = 0; k < ncases; k++) {
@@ -1169,6 +1245,7 @@ int sts_open_batch(const char* const* case_dirs, int ncases, const sts_options* 
     tx = std::max(tx, c->tjump_grid().x);
   }
   b->ntiles = (int)tile_case.size();
+  b->warm3 = opt.warm_start == 3;
   if (int r = b->alloc(&b->d_geos, ncases)) return r;
   if (int r = b->alloc(&b->d_tile_case, tile_case.size())) return r;
   if (int r = b->alloc(&b->d_tile_first, tile_first.size())) return r;
@@ -1185,7 +1262,10 @@ int sts_open_batch(const char* const* case_dirs, int ncases, const sts_options* 
   CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b->pt_kernel(), 256, 0));
   if (per_sm < 1) return fail(STS_ERR_CUDA, "the sweep-loop kernel does not fit on a multiprocessor");
   b->pt_grid = dim3((unsigned)std::max(1, std::min(b->ntiles, per_sm * sms)));
-  if (int r = b->build_graph()) return r;
+  if (int r = b->alloc(&b->d_flag, 1)) return r;
+  CU(cudaMallocHost(&b->h_flag, sizeof(unsigned)));
+  if (b->use_graph)
+    if (int r = b->build_graph()) return r;
   *out = b.release();
   return STS_OK;
 }
@@ -1204,7 +1284,11 @@ int sts_batch_step(sts_batch* b, int nsteps, int* steps_done) {
     for (sts_ctx* c : b->cases) CU(cudaStreamSynchronize(c->s));  // field uploads of the cases land first
     kb_set_steps<<<1, 256, 0, b->s>>>(b->d_geos, b->ncases, (unsigned)nsteps);
     CU(cudaGetLastError());
-    CU(cudaGraphLaunch(b->exec, b->s));
+    if (b->use_graph) {
+      CU(cudaGraphLaunch(b->exec, b->s));
+    } else if (int r = b->step_host(nsteps)) {
+      return r;
+    }
     CU(cudaStreamSynchronize(b->s));
     bool nonfinite = false;
     for (int k = 0; k < b->ncases; k++) {

@@ -275,7 +275,7 @@ def check_division(n: int, seed: int = 1, device: int = 0) -> int:
 class Batch:
     """Many independent cases advanced together (one launch per kernel and step for all)."""
 
-    def __init__(self, case_dirs, fixed_sweeps=False, device=0, precision=EXACT, warm_start=0):
+    def __init__(self, case_dirs, fixed_sweeps=False, device=0, precision=EXACT, warm_start=0, use_graph=True):
         lib = load()
         lib.sts_open_batch.argtypes = [C.POINTER(C.c_char_p), C.c_int, C.POINTER(Options), C.POINTER(C.c_void_p)]
         lib.sts_batch_step.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int)]
@@ -284,7 +284,7 @@ class Batch:
         lib.sts_batch_destroy.argtypes = [C.c_void_p]
         dirs = (C.c_char_p * len(case_dirs))(*[d.encode() for d in case_dirs])
         self._h = C.c_void_p()
-        opt = options(fixed_sweeps, True, device, False, precision, warm_start)
+        opt = options(fixed_sweeps, use_graph, device, False, precision, warm_start)
         _check(lib.sts_open_batch(dirs, len(case_dirs), C.byref(opt), C.byref(self._h)))
         self.cases = []
         for k in range(len(case_dirs)):

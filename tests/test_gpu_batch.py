@@ -108,3 +108,18 @@ def test_batch_fixed_sweeps_matches_oracle(lib_built, oracle_built):
             for f in FIELDS:
                 np.testing.assert_array_equal(b.cases[k].field(f), o.field(f), err_msg=f"case {k} {f}")
         b.close()
+
+
+def test_batch_launch_mode_equals_graph(lib_built):
+    import sts
+    cases = small_batch(3, Nt=40, seed=5)
+    with tempfile.TemporaryDirectory() as root:
+        dirs = write_all(cases, root)
+        a = sts.Batch(dirs, fixed_sweeps=False, precision=2, use_graph=True)
+        b = sts.Batch(dirs, fixed_sweeps=False, precision=2, use_graph=False)
+        assert a.step(6) == b.step(6) == 6
+        for k in range(len(dirs)):
+            for f in FIELDS:
+                np.testing.assert_array_equal(a.cases[k].field(f), b.cases[k].field(f), err_msg=f"case {k} {f}")
+        a.close()
+        b.close()

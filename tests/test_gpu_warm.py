@@ -84,3 +84,51 @@ def test_bad_warm_start_rejected(lib_built):
         case.write(d)
         with pytest.raises(sts.StsError):
             sts.Solver(d, warm_start=7)
+
+
+@pytest.mark.parametrize("which,scale,steps", [("channel_ma0.1", 1.0, 40), ("rayleigh_benard", 0.125, 60),
+                                               ("channel_ma2.43", 0.25, 40)])
+def test_learned_warm_start(which, scale, steps, lib_built, oracle_built):
+    """Mode 3 against the oracle's mode 3 (its least-squares sums run in another order, so the
+    comparison is to the tolerance level, not bit for bit) and against the cold start."""
+    import ora
+    import sts
+    case = sc.config_case(which, scale=scale, Nt=steps)
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        o3 = ora.Oracle(d, fixed_sweeps=False, warm_start=3)
+        o3.step(steps)
+        cold = ora.Oracle(d, fixed_sweeps=False)
+        cold.step(steps)
+        g = sts.Solver(d, fixed_sweeps=False, warm_start=3)
+        assert g.step(steps) == steps
+        hg, ho, hc = g.sweep_history()[10:], o3.sweeps()[10:], cold.sweeps()[10:]
+        print(which, "sweeps per step: cold", hc.mean(), "oracle mode 3", ho.mean(), "gpu mode 3", hg.mean())
+        assert abs(hg.mean() - ho.mean()) <= 0.3
+        assert hg.mean() <= 0.8 * hc.mean()
+        for f in ("p", "T", "u"):
+            e = np.linalg.norm(g.field(f) - o3.field(f)) / np.linalg.norm(o3.field(f))
+            assert e < 1e-6, (f, e)
+        g.close()
+
+
+def test_batch_learned_warm_start_equals_single(lib_built):
+    import os
+    import sts
+    cases = sc.batch_cases(n=3, Nt=40, nx_range=(40, 100))
+    with tempfile.TemporaryDirectory() as root:
+        dirs = []
+        for k, c in enumerate(cases):
+            d = os.path.join(root, f"c{k}")
+            os.makedirs(d)
+            c.write(d)
+            dirs.append(d)
+        b = sts.Batch(dirs, fixed_sweeps=False, warm_start=3, precision=2)
+        assert b.step(14) == 14
+        for k, d in enumerate(dirs):
+            s = sts.Solver(d, fixed_sweeps=False, warm_start=3, precision=2)
+            s.step(14)
+            for f in FIELDS:
+                np.testing.assert_array_equal(b.cases[k].field(f), s.field(f), err_msg=f"case {k} {f}")
+            s.close()
+        b.close()
