@@ -58,7 +58,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-variants", dest="variants", action="store_false",
                     help="skip the FP64-fast and FP32-correction runs of the same workload")
-    ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2],
+    ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2, 3],
                     help="precision mode of the --profile-target run")
     ap.add_argument("--profile-target", type=int, default=0,
                     help="only run this many steps kernel by kernel (a small target for ncu), then exit")
@@ -281,6 +281,7 @@ def batch_bench(args):
     base = None
     for name, prec, warm in (("fp64_exact", sts.EXACT, 0), ("fp64_fast", sts.FAST_FP64, 0),
                              ("fp32_corrections", sts.MIXED, 0), ("fp32_corrections_warm2", sts.MIXED, 2),
+                             ("fp32_corrections_df", sts.MIXED_DF, 0), ("fp32_corrections_df_warm2", sts.MIXED_DF, 2),
                              ("fp32_corrections_learned", sts.MIXED, 3)):
         b = sts.Batch(dirs, fixed_sweeps=False, precision=prec, warm_start=warm)
         cells = sum(c.Nx * c.Ny for c in b.cases)
@@ -403,6 +404,7 @@ def main():
         base = {f: ref.field(f) for f in ("u", "v", "p", "T", "rho")}
         ref.close()
         for name, prec, warm in (("fp64_fast", sts.FAST_FP64, 0), ("fp32_corrections", sts.MIXED, 0),
+                                 ("fp32_corrections_df", sts.MIXED_DF, 0), ("fp32_corrections_df_warm2", sts.MIXED_DF, 2),
                                  ("fp64_exact_warm2", sts.EXACT, 2), ("fp32_corrections_warm2", sts.MIXED, 2),
                                  ("fp32_corrections_learned", sts.MIXED, 3)):
             v = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=prec, warm_start=warm)

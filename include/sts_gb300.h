@@ -48,7 +48,10 @@ typedef struct sts_options {
    *    flux/diffusion kernels (a few ulps from the reference per step).
    * 2: as 1, and the p-T sweeps of the tolerance-terminated loop run in FP32 on correction
    *    fields over FP64 base fields; the sweep that meets the tolerance is recomputed in FP64,
-   *    so the stopping residual is an FP64 update.  Fixed sweep counts run as mode 1. */
+   *    so the stopping residual is an FP64 update.  Fixed sweep counts run as mode 1.
+   * 3: as 2, with the FP64 arithmetic of the assembly, the flux/diffusion kernel and the FP64
+   *    sweeps done in double-float (pairs of FP32 numbers, about 47 significant bits) on the FP32
+   *    pipes; fields stay FP64 in memory. */
   int precision;
   /* Initial iterate of every step's p-T sweeps (no counterpart in the reference, which starts from
    * the previous step's p and T):
@@ -176,6 +179,12 @@ int sts_pt_sweeps_noalloc(const sts_sweep_fields* f, int max_sweeps, int fixed_s
  * number of results that differ in any bit (0 is the only passing answer).  No counterpart in
  * the reference, which divides with the host's IEEE division. */
 int sts_check_division(unsigned long long n, unsigned long long seed, int device, unsigned long long* mismatches);
+
+/* Self-check of the double-float arithmetic of precision mode 3 against FP64 on `device`: n
+ * pseudo-random operand pairs from `seed` (random signs, magnitudes 2^-40 .. 2^40); max_rel_err[0..4]
+ * receive the largest relative errors of the FP64 -> double-float conversion, add (relative to
+ * |a| + |b|), multiply, divide and square root.  No counterpart in the reference. */
+int sts_check_double_float(unsigned long long n, unsigned long long seed, int device, double* max_rel_err);
 
 /* Batches: many independent cases advanced together on one GPU.  Every kernel of a step is
  * launched once for all cases and the p-T sweep loops of all cases run in one cooperative

@@ -351,14 +351,15 @@ __device__ __forceinline__ void advance_fp64(const Geo& g, bool lead, LoopCase& 
 
 // A batched kernel's CTA (x, y, z) works on case z: the case's Geo is staged in shared memory.
 // Returns whether the case takes part in the current step.
-__device__ __forceinline__ bool stage_geo(Geo& sg, const Geo* __restrict__ gs) {
+__device__ __forceinline__ bool stage_geo(Geo& sg, const Geo* __restrict__ gs, unsigned which) {
   const int tid = threadIdx.x + threadIdx.y * blockDim.x, nthr = blockDim.x * blockDim.y;
-  const unsigned* src = reinterpret_cast<const unsigned*>(&gs[blockIdx.z]);
+  const unsigned* src = reinterpret_cast<const unsigned*>(&gs[which]);
   unsigned* dst = reinterpret_cast<unsigned*>(&sg);
   for (int k = tid; k < (int)(sizeof(Geo) / 4); k += nthr) dst[k] = src[k];
   __syncthreads();
   return *(volatile unsigned*)&sg.ctl->running != 0;
 }
+__device__ __forceinline__ bool stage_geo(Geo& sg, const Geo* __restrict__ gs) { return stage_geo(sg, gs, blockIdx.z); }
 
 // Zero-gradient copies into the ghost cells outside the p/T solve range, side by side in the
 // reference's order (x begin, x end, y begin, y end); a ghost cell takes the value of the

@@ -10,12 +10,17 @@
 
 #include "sts_common.cuh"
 #include "sts_device.cuh"
+#include "sts_df.cuh"
 #include "sts_kernels.h"
 
 namespace sts {
 
-// u/v momentum coefficients and ScT1 (SIMPLE_TS_MPI.cpp:3269-3756) with reciprocal multiplies.
-__device__ __forceinline__ void assemble_fast_body(const Geo& g, unsigned long long h_sweep, int in_graph) {
+// u/v momentum coefficients and ScT1 (SIMPLE_TS_MPI.cpp:3269-3756) with reciprocal multiplies,
+// in FP64 (R = double) or double-float (R = df).
+// parts: bit 0 the u faces, bit 1 the v faces, bit 2 ScT1 (the double-float kernel runs the three
+// as separate CTAs, for three times the warps on a latency-bound kernel).
+template <class R>
+__device__ __forceinline__ void assemble_t(const Geo& g, unsigned long long h_sweep, int in_graph, unsigned parts = 7u) {
   Cell c = cell(g);
   Ctl* ctl = g.ctl;
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
@@ -32,115 +37,111 @@ __device__ __forceinline__ void assemble_fast_body(const Geo& g, unsigned long l
   if (!(cl & 0x3F)) return;
   const int i = c.i, j = c.j, Nx = g.Nx;
   const Nb d = neighbours(i, j, g.Nx, g.Ny, g.bits & F_PERIODIC);
-  const double cT = ctl->cT, cPch = ctl->cPch, ht = g.ht, rht = g.rht;
-  const double third = 1.0 / 3.0, two_third = 2.0 / 3.0;
-  const double* __restrict__ hx = g.hx;
-  const double* __restrict__ hy = g.hy;
-  const double* __restrict__ u = g.u;
-  const double* __restrict__ v = g.v;
-  const double* __restrict__ Fx = g.Fx;
-  const double* __restrict__ Fy = g.Fy;
-  const double* __restrict__ sT = g.sqrt_T;
-  const double* __restrict__ rho = g.rho;
-  const double* __restrict__ rho_pr = g.rho_pr;
-  auto B = [&](int k) -> double { return cls_fluid(g.cls[k]) ? 1.0 : 0.0; };
+  const R cT = num<R>(ctl->cT), cPch = num<R>(ctl->cPch), ht = num<R>(g.ht), rht = num<R>(g.rht);
+  const R third = num<R>(1.0 / 3.0), two_third = num<R>(2.0 / 3.0), one = num<R>(1.0), half = num<R>(0.5);
+  const Arr<R> hx{g.hx}, hy{g.hy}, u{g.u}, v{g.v}, Fx{g.Fx}, Fy{g.Fy}, sT{g.sqrt_T}, rho{g.rho}, rho_pr{g.rho_pr};
+  auto A = [](const double* p) { return Arr<R>{p}; };
+  auto B = [&](int k) -> R { return cls_fluid(g.cls[k]) ? one : num<R>(0.0); };
   auto BB = [&](int k) -> bool { return cls_fluid(g.cls[k]); };
   const bool bc_u = cls_u(cl) == CLS_BC, bc_v = cls_v(cl) == CLS_BC, bc_o = cls_o(cl) == CLS_BC;
 
-  if (cls_u(cl)) {
-    const double F_xu1 = 0.5 * (Fx[d.i_1j] + Fx[d.ij]);
-    const double F_xu2 = 0.5 * (Fx[d.ij] + Fx[d.i1j]);
-    const double r3a = third * g.rhx[i], r3b = third * g.rhx[d.i_1];
-    const double m1 = bc_u ? B(d.i1j) : 1.0, m2 = bc_u ? B(d.i_2j) : 1.0;
-    const double mN = bc_u ? B(d.ij1) : 1.0, mNW = bc_u ? B(d.i_1j1) : 1.0;
-    const double mS = bc_u ? B(d.ij_1) : 1.0, mSW = bc_u ? B(d.i_1j_1) : 1.0;
-    const double Scu = cT * (m1 * u[d.i1j] * sT[d.ij] * hy[j] * r3a + m2 * u[d.i_1j] * sT[d.i_1j] * hy[j] * r3b +
-                             g.Gamma_yf[d.ij1] * (v[d.ij1] * mN - v[d.i_1j1] * mNW) -
-                             g.Gamma_yf[d.ij] * (v[d.ij] * mS - v[d.i_1j] * mSW) -
+  if ((parts & 1u) && cls_u(cl)) {
+    const R F_xu1 = half * (Fx[d.i_1j] + Fx[d.ij]);
+    const R F_xu2 = half * (Fx[d.ij] + Fx[d.i1j]);
+    const R r3a = third * A(g.rhx)[i], r3b = third * A(g.rhx)[d.i_1];
+    const R m1 = bc_u ? B(d.i1j) : one, m2 = bc_u ? B(d.i_2j) : one;
+    const R mN = bc_u ? B(d.ij1) : one, mNW = bc_u ? B(d.i_1j1) : one;
+    const R mS = bc_u ? B(d.ij_1) : one, mSW = bc_u ? B(d.i_1j_1) : one;
+    const R Scu = cT * (m1 * u[d.i1j] * sT[d.ij] * hy[j] * r3a + m2 * u[d.i_1j] * sT[d.i_1j] * hy[j] * r3b +
+                             A(g.Gamma_yf)[d.ij1] * (v[d.ij1] * mN - v[d.i_1j1] * mNW) -
+                             A(g.Gamma_yf)[d.ij] * (v[d.ij] * mS - v[d.i_1j] * mSW) -
                              sT[d.ij] * (v[d.ij1] * mN - v[d.ij] * mS) * two_third +
                              sT[d.i_1j] * (v[d.i_1j1] * mNW - v[d.i_1j] * mSW) * two_third);
-    const double Spu = -(g.D_ux[d.ij] + g.D_ux[d.i1j]) * third;
-    const double au1 = fmax(0.0, F_xu1) + g.D_ux[d.ij];
-    const double au2 = fmax(0.0, -F_xu2) + g.D_ux[d.i1j];
-    const double au3 = 0.5 * (fmax(0.0, Fy[d.i_1j]) + fmax(0.0, Fy[d.ij])) + g.D_uy[d.ij];
-    const double au4 = 0.5 * (fmax(0.0, -Fy[d.i_1j1]) + fmax(0.0, -Fy[d.ij1])) + g.D_uy[d.ij1];
-    const double bu3 = (rho_pr[d.i_1j] * hx[d.i_1] + rho_pr[d.ij] * hx[i]) * g.u_pr[d.ij] * hy[j] * 0.5 * rht + Scu;
-    const double au0 = au1 + au2 + au3 + au4 + 0.5 * (-Fy[d.i_1j] - Fy[d.ij] + Fy[d.i_1j1] + Fy[d.ij1]) + F_xu2 -
-                       F_xu1 - Spu + (rho[d.i_1j] * hx[d.i_1] + rho[d.ij] * hx[i]) * hy[j] * 0.5 * rht;
-    const double rau0 = 1.0 / au0;
-    const double up = (au1 * m1 * u[d.i_1j] + au2 * m2 * u[d.i1j] + au3 * u[d.ij_1] + au4 * u[d.ij1] + bu3) * rau0;
-    const double dpc = cPch * hy[j] * rau0;
-    const double hr = hy[j] * g.rho_u[d.ij];
-    g.u_pseudo[d.ij] = up;
-    g.d12[d.ij] = dpc;
-    g.apx[d.ij] = dpc * hr;
-    g.bpx[d.ij] = bc_u ? B(d.i_1j) * B(d.ij) * hr * up : hr * up;
+    const R Spu = -(A(g.D_ux)[d.ij] + A(g.D_ux)[d.i1j]) * third;
+    const R au1 = fmax0(F_xu1) + A(g.D_ux)[d.ij];
+    const R au2 = fmax0(-F_xu2) + A(g.D_ux)[d.i1j];
+    const R au3 = half * (fmax0(Fy[d.i_1j]) + fmax0(Fy[d.ij])) + A(g.D_uy)[d.ij];
+    const R au4 = half * (fmax0(-Fy[d.i_1j1]) + fmax0(-Fy[d.ij1])) + A(g.D_uy)[d.ij1];
+    const R bu3 = (rho_pr[d.i_1j] * hx[d.i_1] + rho_pr[d.ij] * hx[i]) * A(g.u_pr)[d.ij] * hy[j] * half * rht + Scu;
+    const R au0 = au1 + au2 + au3 + au4 + half * (-Fy[d.i_1j] - Fy[d.ij] + Fy[d.i_1j1] + Fy[d.ij1]) + F_xu2 -
+                       F_xu1 - Spu + (rho[d.i_1j] * hx[d.i_1] + rho[d.ij] * hx[i]) * hy[j] * half * rht;
+    const R rau0 = one / au0;
+    const R up = (au1 * m1 * u[d.i_1j] + au2 * m2 * u[d.i1j] + au3 * u[d.ij_1] + au4 * u[d.ij1] + bu3) * rau0;
+    const R dpc = cPch * hy[j] * rau0;
+    const R hr = hy[j] * A(g.rho_u)[d.ij];
+    g.u_pseudo[d.ij] = to_double(up);
+    g.d12[d.ij] = to_double(dpc);
+    g.apx[d.ij] = to_double(dpc * hr);
+    g.bpx[d.ij] = to_double(bc_u ? B(d.i_1j) * B(d.ij) * hr * up : hr * up);
   }
 
-  if (cls_v(cl)) {
+  if ((parts & 2u) && cls_v(cl)) {
     const int jm = j - ((j - 1) >= 0 ? 1 : 0);
     const int far = d.ij_1 - ((j - 2) >= 0 ? Nx : 0);
-    const double F_yv3 = 0.5 * (Fy[d.ij_1] + Fy[d.ij]);
-    const double F_yv4 = 0.5 * (Fy[d.ij] + Fy[d.ij1]);
-    const double r3a = third * g.rhy[j], r3b = third * g.rhy[jm];
-    const double mN = bc_v ? B(d.ij1) : 1.0, mF = bc_v ? B(far) : 1.0;
-    const double mE = bc_v ? B(d.i1j) : 1.0, mSE = bc_v ? B(d.i1j_1) : 1.0;
-    const double mW = bc_v ? B(d.i_1j) : 1.0, mSW = bc_v ? B(d.i_1j_1) : 1.0;
-    const double Scv = cT * (mN * v[d.ij1] * sT[d.ij] * hx[i] * r3a + mF * v[d.ij_1] * sT[d.ij_1] * hx[i] * r3b +
-                             g.Gamma_xf[d.i1j] * (u[d.i1j] * mE - u[d.i1j_1] * mSE) -
-                             g.Gamma_xf[d.ij] * (u[d.ij] * mW - u[d.ij_1] * mSW) -
+    const R F_yv3 = half * (Fy[d.ij_1] + Fy[d.ij]);
+    const R F_yv4 = half * (Fy[d.ij] + Fy[d.ij1]);
+    const R r3a = third * A(g.rhy)[j], r3b = third * A(g.rhy)[jm];
+    const R mN = bc_v ? B(d.ij1) : one, mF = bc_v ? B(far) : one;
+    const R mE = bc_v ? B(d.i1j) : one, mSE = bc_v ? B(d.i1j_1) : one;
+    const R mW = bc_v ? B(d.i_1j) : one, mSW = bc_v ? B(d.i_1j_1) : one;
+    const R Scv = cT * (mN * v[d.ij1] * sT[d.ij] * hx[i] * r3a + mF * v[d.ij_1] * sT[d.ij_1] * hx[i] * r3b +
+                             A(g.Gamma_xf)[d.i1j] * (u[d.i1j] * mE - u[d.i1j_1] * mSE) -
+                             A(g.Gamma_xf)[d.ij] * (u[d.ij] * mW - u[d.ij_1] * mSW) -
                              sT[d.ij] * (u[d.i1j] * mE - u[d.ij] * mW) * two_third +
                              sT[d.ij_1] * (u[d.i1j_1] * mSE - u[d.ij_1] * mSW) * two_third) -
-                       g.c_Fr_v * (rho[d.ij_1] * hx[i] * 0.5 * hy[jm] + rho[d.ij] * hx[i] * 0.5 * hy[j]);
-    const double Spv = -(g.D_vy[d.ij] + g.D_vy[d.ij1]) * third;
-    const double av1 = 0.5 * (fmax(0.0, Fx[d.ij]) + fmax(0.0, Fx[d.ij_1])) + g.D_vx[d.ij];
-    const double av2 = 0.5 * (fmax(0.0, -Fx[d.i1j]) + fmax(0.0, -Fx[d.i1j_1])) + g.D_vx[d.i1j];
-    const double av3 = fmax(0.0, F_yv3) + g.D_vy[d.ij];
-    const double av4 = fmax(0.0, -F_yv4) + g.D_vy[d.ij1];
-    const double bv3 = (rho_pr[d.ij_1] * hy[j - 1] + rho_pr[d.ij] * hy[j]) * g.v_pr[d.ij] * hx[i] * 0.5 * rht + Scv;
-    const double av0 = av1 + av2 + av3 + av4 + 0.5 * (Fx[d.i1j] - Fx[d.ij] + Fx[d.i1j_1] - Fx[d.ij_1]) + F_yv4 -
-                       F_yv3 - Spv + (rho[d.ij_1] * hy[j - 1] + rho[d.ij] * hy[j]) * hx[i] * 0.5 * rht;
-    const double rav0 = 1.0 / av0;
-    const double vp = (av1 * v[d.i_1j] + av2 * v[d.i1j] + av3 * mF * v[d.ij_1] + av4 * mN * v[d.ij1] + bv3) * rav0;
-    const double dpc = cPch * hx[i] * rav0;
-    const double hr = hx[i] * g.rho_v[d.ij];
-    g.v_pseudo[d.ij] = vp;
-    g.d34[d.ij] = dpc;
-    g.apy[d.ij] = dpc * hr;
-    g.bpy[d.ij] = bc_v ? B(d.ij - Nx) * B(d.ij) * hr * vp : hr * vp;
+                       num<R>(g.c_Fr_v) * (rho[d.ij_1] * hx[i] * half * hy[jm] + rho[d.ij] * hx[i] * half * hy[j]);
+    const R Spv = -(A(g.D_vy)[d.ij] + A(g.D_vy)[d.ij1]) * third;
+    const R av1 = half * (fmax0(Fx[d.ij]) + fmax0(Fx[d.ij_1])) + A(g.D_vx)[d.ij];
+    const R av2 = half * (fmax0(-Fx[d.i1j]) + fmax0(-Fx[d.i1j_1])) + A(g.D_vx)[d.i1j];
+    const R av3 = fmax0(F_yv3) + A(g.D_vy)[d.ij];
+    const R av4 = fmax0(-F_yv4) + A(g.D_vy)[d.ij1];
+    const R bv3 = (rho_pr[d.ij_1] * hy[j - 1] + rho_pr[d.ij] * hy[j]) * A(g.v_pr)[d.ij] * hx[i] * half * rht + Scv;
+    const R av0 = av1 + av2 + av3 + av4 + half * (Fx[d.i1j] - Fx[d.ij] + Fx[d.i1j_1] - Fx[d.ij_1]) + F_yv4 -
+                       F_yv3 - Spv + (rho[d.ij_1] * hy[j - 1] + rho[d.ij] * hy[j]) * hx[i] * half * rht;
+    const R rav0 = one / av0;
+    const R vp = (av1 * v[d.i_1j] + av2 * v[d.i1j] + av3 * mF * v[d.ij_1] + av4 * mN * v[d.ij1] + bv3) * rav0;
+    const R dpc = cPch * hx[i] * rav0;
+    const R hr = hx[i] * A(g.rho_v)[d.ij];
+    g.v_pseudo[d.ij] = to_double(vp);
+    g.d34[d.ij] = to_double(dpc);
+    g.apy[d.ij] = to_double(dpc * hr);
+    g.bpy[d.ij] = to_double(bc_v ? B(d.ij - Nx) * B(d.ij) * hr * vp : hr * vp);
   }
 
-  if (cls_o(cl)) {
-    double dudx, dvdy, s0, s1, s2, s3;
+  if ((parts & 4u) && cls_o(cl)) {
+    R dudx, dvdy, s0, s1, s2, s3;
     if (bc_o) {
-      dudx = (B(d.i1j) * u[d.i1j] - B(d.i_1j) * u[d.ij]) * g.rhx[i];
-      dvdy = (B(d.ij1) * v[d.ij1] - B(d.ij_1) * v[d.ij]) * g.rhy[j];
+      dudx = (B(d.i1j) * u[d.i1j] - B(d.i_1j) * u[d.ij]) * A(g.rhx)[i];
+      dvdy = (B(d.ij1) * v[d.ij1] - B(d.ij_1) * v[d.ij]) * A(g.rhy)[j];
       // (mask * h_low + h) picks h alone or the two-cell sum
-      const double ys = (BB(d.i_1j_1) && BB(d.ij_1)) ? g.ryy_m[j] : g.rhy[j];
-      const double xs = (BB(d.i_1j_1) && BB(d.i_1j)) ? g.rxx_m[i] : g.rhx[i];
-      const double ys1 = (BB(d.ij_1) && BB(d.i1j_1)) ? g.ryy_m[j] : g.rhy[j];
-      const double xs1 = (BB(d.i1j_1) && BB(d.i1j)) ? g.rxx_p[i] : g.rhx[i];
-      const double yn2 = (BB(d.i_1j1) && BB(d.ij1)) ? g.ryy_p[j] : g.rhy[j];
-      const double xs2 = (BB(d.i_1j) && BB(d.i_1j1)) ? g.rxx_m[i] : g.rhx[i];
-      const double yn3 = (BB(d.ij1) && BB(d.i1j1)) ? g.ryy_p[j] : g.rhy[j];
-      const double xs3 = (BB(d.i1j) && BB(d.i1j1)) ? g.rxx_p[i] : g.rhx[i];
+      const R ys = (BB(d.i_1j_1) && BB(d.ij_1)) ? A(g.ryy_m)[j] : A(g.rhy)[j];
+      const R xs = (BB(d.i_1j_1) && BB(d.i_1j)) ? A(g.rxx_m)[i] : A(g.rhx)[i];
+      const R ys1 = (BB(d.ij_1) && BB(d.i1j_1)) ? A(g.ryy_m)[j] : A(g.rhy)[j];
+      const R xs1 = (BB(d.i1j_1) && BB(d.i1j)) ? A(g.rxx_p)[i] : A(g.rhx)[i];
+      const R yn2 = (BB(d.i_1j1) && BB(d.ij1)) ? A(g.ryy_p)[j] : A(g.rhy)[j];
+      const R xs2 = (BB(d.i_1j) && BB(d.i_1j1)) ? A(g.rxx_m)[i] : A(g.rhx)[i];
+      const R yn3 = (BB(d.ij1) && BB(d.i1j1)) ? A(g.ryy_p)[j] : A(g.rhy)[j];
+      const R xs3 = (BB(d.i1j) && BB(d.i1j1)) ? A(g.rxx_p)[i] : A(g.rhx)[i];
       s0 = (u[d.ij] - u[d.ij_1]) * ys + (v[d.ij] - v[d.i_1j]) * xs;
       s1 = (u[d.i1j] - u[d.i1j_1]) * ys1 + (v[d.i1j] - v[d.ij]) * xs1;
       s2 = (u[d.ij1] - u[d.ij]) * yn2 + (v[d.ij1] - v[d.i_1j1]) * xs2;
       s3 = (u[d.i1j1] - u[d.i1j]) * yn3 + (v[d.i1j1] - v[d.ij1]) * xs3;
     } else {
-      dudx = (u[d.i1j] - u[d.ij]) * g.rhx[i];
-      dvdy = (v[d.ij1] - v[d.ij]) * g.rhy[j];
-      s0 = (u[d.ij] - u[d.ij_1]) * g.ryy_m[j] + (v[d.ij] - v[d.i_1j]) * g.rxx_m[i];
-      s1 = (u[d.i1j] - u[d.i1j_1]) * g.ryy_m[j] + (v[d.i1j] - v[d.ij]) * g.rxx_p[i];
-      s2 = (u[d.ij1] - u[d.ij]) * g.ryy_p[j] + (v[d.ij1] - v[d.i_1j1]) * g.rxx_m[i];
-      s3 = (u[d.i1j1] - u[d.i1j]) * g.ryy_p[j] + (v[d.i1j1] - v[d.ij1]) * g.rxx_p[i];
+      dudx = (u[d.i1j] - u[d.ij]) * A(g.rhx)[i];
+      dvdy = (v[d.ij1] - v[d.ij]) * A(g.rhy)[j];
+      s0 = (u[d.ij] - u[d.ij_1]) * A(g.ryy_m)[j] + (v[d.ij] - v[d.i_1j]) * A(g.rxx_m)[i];
+      s1 = (u[d.i1j] - u[d.i1j_1]) * A(g.ryy_m)[j] + (v[d.i1j] - v[d.ij]) * A(g.rxx_p)[i];
+      s2 = (u[d.ij1] - u[d.ij]) * A(g.ryy_p)[j] + (v[d.ij1] - v[d.i_1j1]) * A(g.rxx_m)[i];
+      s3 = (u[d.i1j1] - u[d.i1j]) * A(g.ryy_p)[j] + (v[d.i1j1] - v[d.ij1]) * A(g.rxx_p)[i];
     }
-    const double dd = dudx + dvdy;
-    g.ScT1[d.ij] = ht * sT[d.ij] * g.cT2 * hx[i] * hy[j] *
-                       (2.0 * (dudx * dudx + dvdy * dvdy) + s0 * s0 + s1 * s1 + s2 * s2 + s3 * s3 - dd * dd * two_third) +
-                   g.p_pr[d.ij] * hx[i] * hy[j];
+    const R dd = dudx + dvdy;
+    g.ScT1[d.ij] = to_double(ht * sT[d.ij] * num<R>(g.cT2) * hx[i] * hy[j] *
+                       (num<R>(2.0) * (dudx * dudx + dvdy * dvdy) + s0 * s0 + s1 * s1 + s2 * s2 + s3 * s3 - dd * dd * two_third) +
+                   A(g.p_pr)[d.ij] * hx[i] * hy[j]);
   }
+}
+__device__ __forceinline__ void assemble_fast_body(const Geo& g, unsigned long long h_sweep, int in_graph) {
+  assemble_t<double>(g, h_sweep, in_graph);
 }
 __global__ void k_assemble_fast(Geo g, unsigned long long h_sweep, int in_graph) { assemble_fast_body(g, h_sweep, in_graph); }
 __global__ void kb_assemble_fast(const Geo* gs, unsigned long long h_sweep, int in_graph) {
@@ -149,58 +150,66 @@ __global__ void kb_assemble_fast(const Geo* gs, unsigned long long h_sweep, int 
   assemble_fast_body(sg, h_sweep, in_graph);
 }
 
-// Fluxes and diffusion coefficients (SIMPLE_TS_MPI.cpp:10440-10618) with reciprocal multiplies.
-__device__ __forceinline__ void flux_diff_fast_body(const Geo& g, unsigned tail) {
+// Fluxes and diffusion coefficients (SIMPLE_TS_MPI.cpp:10440-10618) with reciprocal multiplies,
+// in FP64 (R = double) or double-float (R = df).  Gamma keeps its stored value where no branch
+// computes it (no FP64 -> double-float -> FP64 round trip).
+template <class R>
+__device__ __forceinline__ void flux_diff_t(const Geo& g, unsigned tail) {
   Cell c = cell(g);
   if (c.ok) {
     const int i = c.i, j = c.j;
     const Nb d = neighbours(i, j, g.Nx, g.Ny, g.bits & F_PERIODIC);
-    const double* __restrict__ hx = g.hx;
-    const double* __restrict__ hy = g.hy;
-    const double* __restrict__ sT = g.sqrt_T;
-    const double* __restrict__ Tw_u = g.Tw_u;
-    const double* __restrict__ Tw_v = g.Tw_v;
-    const double cT = g.ctl->cT, cT1 = g.cT1;
-    g.Fx[d.ij] = hy[j] * g.rho_u[d.ij] * g.u[d.ij];
-    g.Fy[d.ij] = hx[i] * g.rho_v[d.ij] * g.v[d.ij];
+    const Arr<R> hx{g.hx}, hy{g.hy}, sT{g.sqrt_T}, Tw_u{g.Tw_u}, Tw_v{g.Tw_v}, rhx{g.rhx}, rhy{g.rhy};
+    const R cT = num<R>(g.ctl->cT), cT1 = num<R>(g.cT1), half = num<R>(0.5), zero = num<R>(0.0);
+    g.Fx[d.ij] = to_double(hy[j] * Arr<R>{g.rho_u}[d.ij] * Arr<R>{g.u}[d.ij]);
+    g.Fy[d.ij] = to_double(hx[i] * Arr<R>{g.rho_v}[d.ij] * Arr<R>{g.v}[d.ij]);
     const bool b_ws = cls_fluid(g.cls[d.i_1j_1]), b_s = cls_fluid(g.cls[d.ij_1]), b_w = cls_fluid(g.cls[d.i_1j]),
                b_p = cls_fluid(g.cls[d.ij]);
     const int jm = j - (0 < j ? 1 : 0);
-    const double ry = g.ryy_m[j], rx = g.rxx_m[i];
-    auto LiY = [&](double f1, double f2) { return (f1 * hy[j] + f2 * hy[jm]) * ry; };
-    auto LiX = [&](double f1, double f2) { return (f1 * hx[i] + f2 * hx[d.i_1]) * rx; };
-    double Gy = g.Gamma_yf[d.ij], Gx = g.Gamma_xf[d.ij];
+    const R ry = Arr<R>{g.ryy_m}[j], rx = Arr<R>{g.rxx_m}[i];
+    auto LiY = [&](R f1, R f2) { return (f1 * hy[j] + f2 * hy[jm]) * ry; };
+    auto LiX = [&](R f1, R f2) { return (f1 * hx[i] + f2 * hx[d.i_1]) * rx; };
+    R Gy, Gx;
     if (b_ws && b_s && b_w && b_p) {
-      Gy = 0.5 * (LiY(sT[d.i_1j_1], sT[d.i_1j]) + LiY(sT[d.ij_1], sT[d.ij]));
-      Gx = 0.5 * (LiX(sT[d.i_1j_1], sT[d.ij_1]) + LiX(sT[d.i_1j], sT[d.ij]));
+      Gy = half * (LiY(sT[d.i_1j_1], sT[d.i_1j]) + LiY(sT[d.ij_1], sT[d.ij]));
+      Gx = half * (LiX(sT[d.i_1j_1], sT[d.ij_1]) + LiX(sT[d.i_1j], sT[d.ij]));
+      g.Gamma_yf[d.ij] = to_double(Gy);
+      g.Gamma_xf[d.ij] = to_double(Gx);
     } else if (b_ws || b_s || b_w || b_p) {
-      Gy = 0.5 * ((b_ws && b_w) ? LiY(sT[d.i_1j_1], sT[d.i_1j]) : 0.0) + 0.5 * ((b_ws != b_w) ? sqrt(Tw_v[d.i_1j]) : 0.0) +
-           0.5 * ((b_s && b_p) ? LiY(sT[d.ij_1], sT[d.ij]) : 0.0) + 0.5 * ((b_s != b_p) ? sqrt(Tw_v[d.ij]) : 0.0) +
-           0.5 * (((!(b_ws && b_w)) || (!(b_s && b_p))) ? LiY(sqrt(Tw_u[d.ij_1]), sqrt(Tw_u[d.ij])) : 0.0);
-      Gx = 0.5 * ((b_ws && b_s) ? LiX(sT[d.i_1j_1], sT[d.ij_1]) : 0.0) + 0.5 * ((b_ws != b_s) ? sqrt(Tw_u[d.ij_1]) : 0.0) +
-           0.5 * ((b_w && b_p) ? LiX(sT[d.i_1j], sT[d.ij]) : 0.0) + 0.5 * ((b_w != b_p) ? sqrt(Tw_u[d.ij]) : 0.0) +
-           0.5 * (((!(b_ws && b_s)) || (!(b_w && b_p))) ? LiX(sqrt(Tw_v[d.i_1j]), sqrt(Tw_v[d.ij])) : 0.0);
+      Gy = half * ((b_ws && b_w) ? LiY(sT[d.i_1j_1], sT[d.i_1j]) : zero) +
+           half * ((b_ws != b_w) ? dsqrt(Tw_v[d.i_1j]) : zero) + half * ((b_s && b_p) ? LiY(sT[d.ij_1], sT[d.ij]) : zero) +
+           half * ((b_s != b_p) ? dsqrt(Tw_v[d.ij]) : zero) +
+           half * (((!(b_ws && b_w)) || (!(b_s && b_p))) ? LiY(dsqrt(Tw_u[d.ij_1]), dsqrt(Tw_u[d.ij])) : zero);
+      Gx = half * ((b_ws && b_s) ? LiX(sT[d.i_1j_1], sT[d.ij_1]) : zero) +
+           half * ((b_ws != b_s) ? dsqrt(Tw_u[d.ij_1]) : zero) + half * ((b_w && b_p) ? LiX(sT[d.i_1j], sT[d.ij]) : zero) +
+           half * ((b_w != b_p) ? dsqrt(Tw_u[d.ij]) : zero) +
+           half * (((!(b_ws && b_s)) || (!(b_w && b_p))) ? LiX(dsqrt(Tw_v[d.i_1j]), dsqrt(Tw_v[d.ij])) : zero);
+      g.Gamma_yf[d.ij] = to_double(Gy);
+      g.Gamma_xf[d.ij] = to_double(Gx);
+    } else {
+      Gy = Arr<R>{g.Gamma_yf}[d.ij];
+      Gx = Arr<R>{g.Gamma_xf}[d.ij];
     }
-    g.Gamma_yf[d.ij] = Gy;
-    g.Gamma_xf[d.ij] = Gx;
-    g.D_ux[d.ij] = cT * sT[d.i_1j] * hy[j] * g.rhx[d.i_1];
-    g.D_vy[d.ij] = cT * sT[d.ij_1] * hx[i] * g.rhy[jm];
+    g.D_ux[d.ij] = to_double(cT * sT[d.i_1j] * hy[j] * rhx[d.i_1]);
+    g.D_vy[d.ij] = to_double(cT * sT[d.ij_1] * hx[i] * rhy[jm]);
     const bool pw = b_p && b_w, sws = b_s && b_ws, ps = b_p && b_s, wws = b_w && b_ws;
-    g.D_uy[d.ij] = (pw || sws) ? cT * Gy * (hx[i] + hx[d.i_1]) * ((pw && sws) ? ry : (pw ? g.rhy[j] : g.rhy[jm])) : 0.0;
-    g.D_vx[d.ij] = (ps || wws) ? cT * Gx * (hy[j] + hy[jm]) * ((ps && wws) ? rx : (ps ? g.rhx[i] : g.rhx[d.i_1])) : 0.0;
+    g.D_uy[d.ij] =
+        (pw || sws) ? to_double(cT * Gy * (hx[i] + hx[d.i_1]) * ((pw && sws) ? ry : (pw ? rhy[j] : rhy[jm]))) : 0.0;
+    g.D_vx[d.ij] =
+        (ps || wws) ? to_double(cT * Gx * (hy[j] + hy[jm]) * ((ps && wws) ? rx : (ps ? rhx[i] : rhx[d.i_1]))) : 0.0;
     if (b_p || b_w) {
-      const double rs = pw ? rx : (b_p ? g.rhx[i] : g.rhx[d.i_1]);
-      const double face = pw ? (hx[d.i_1] + hx[i]) * sT[d.i_1j] * sT[d.ij] / (hx[d.i_1] * sT[d.ij] + hx[i] * sT[d.i_1j])
-                             : sqrt(Tw_u[d.ij]);
-      g.DTx[d.ij] = cT1 * hy[j] * 2.0 * rs * face;
+      const R rs = pw ? rx : (b_p ? rhx[i] : rhx[d.i_1]);
+      const R face = pw ? (hx[d.i_1] + hx[i]) * sT[d.i_1j] * sT[d.ij] / (hx[d.i_1] * sT[d.ij] + hx[i] * sT[d.i_1j])
+                        : dsqrt(Tw_u[d.ij]);
+      g.DTx[d.ij] = to_double(cT1 * hy[j] * num<R>(2.0) * rs * face);
     } else {
       g.DTx[d.ij] = 0.0;
     }
     if (b_p || b_s) {
-      const double rs = ps ? ry : (b_p ? g.rhy[j] : g.rhy[jm]);
-      const double face = ps ? (hy[jm] + hy[j]) * sT[d.ij_1] * sT[d.ij] / (hy[jm] * sT[d.ij] + hy[j] * sT[d.ij_1])
-                             : sqrt(Tw_v[d.ij]);
-      g.DTy[d.ij] = cT1 * hx[i] * 2.0 * rs * face;
+      const R rs = ps ? ry : (b_p ? rhy[j] : rhy[jm]);
+      const R face = ps ? (hy[jm] + hy[j]) * sT[d.ij_1] * sT[d.ij] / (hy[jm] * sT[d.ij] + hy[j] * sT[d.ij_1])
+                        : dsqrt(Tw_v[d.ij]);
+      g.DTy[d.ij] = to_double(cT1 * hx[i] * num<R>(2.0) * rs * face);
     } else {
       g.DTy[d.ij] = 0.0;
     }
@@ -213,6 +222,7 @@ __device__ __forceinline__ void flux_diff_fast_body(const Geo& g, unsigned tail)
     if (tail & PH_PRES) phase_pres(g, g.p[cur], tid, nt);
   }
 }
+__device__ __forceinline__ void flux_diff_fast_body(const Geo& g, unsigned tail) { flux_diff_t<double>(g, tail); }
 __global__ void k_flux_diff_fast(Geo g, unsigned tail) { flux_diff_fast_body(g, tail); }
 __global__ void kb_flux_diff_fast(const Geo* gs, unsigned tail) {
   __shared__ Geo sg;
@@ -229,74 +239,80 @@ __global__ void kb_flux_diff_fast(const Geo* gs, unsigned tail) {
 // p_pr/T_pr term and ht * (sum of the p coefficients).  Returns false for unsolved cells, which
 // copy through.
 // ---------------------------------------------------------------------------
-template <bool FIRST>
-__device__ __forceinline__ bool sweep_cell_fast(const Geo& g, const Cell& c, const double* __restrict__ P,
-                                                const double* __restrict__ TT, double* __restrict__ pn,
-                                                double* __restrict__ Tn, double& Tnew, double& pnew, double& sa) {
+template <bool FIRST, class R>
+__device__ __forceinline__ bool sweep_cell_t(const Geo& g, const Cell& c, const double* __restrict__ P,
+                                             const double* __restrict__ TT, double* __restrict__ pn,
+                                             double* __restrict__ Tn, R& Tnew, R& pnew, R& sa) {
   const int ij = c.ij;
   const uint8_t cl = g.cls[ij];
   const int co = cls_o(cl);
   if (!co) {
-    pnew = P[ij];
-    Tnew = TT[ij];
-    pn[ij] = pnew;
-    Tn[ij] = Tnew;
+    pn[ij] = P[ij];
+    Tn[ij] = TT[ij];
+    pnew = num<R>(P[ij]);
+    Tnew = num<R>(TT[ij]);
     return false;
   }
   const int i = c.i, j = c.j;
   const Nb d = neighbours(i, j, g.Nx, g.Ny, g.bits & F_PERIODIC);
-  const double* __restrict__ apx = g.apx;
-  const double* __restrict__ apy = g.apy;
-  const double ht = g.ht, H = g.hx[i] * g.hy[j];
+  const Arr<R> apx{g.apx}, apy{g.apy}, Pv{P}, Tv{TT};
+  const R ht = num<R>(g.ht), H = num<R>(g.hx[i]) * num<R>(g.hy[j]);
   auto fl = [&](int k) { return cls_fluid(g.cls[k]); };
-  double w1, w2, w3, w4, divu, rden, pc;
+  R w1, w2, w3, w4, divu, rden, pc;
   if (FIRST) {
-    const double* __restrict__ Fx = g.Fx;
-    const double* __restrict__ Fy = g.Fy;
-    const double aT1 = fmax(0.0, Fx[d.ij]) + g.DTx[d.ij];
-    const double aT2 = fmax(0.0, -Fx[d.i1j]) + g.DTx[d.i1j];
-    const double aT3 = fmax(0.0, Fy[d.ij]) + g.DTy[d.ij];
-    const double aT4 = fmax(0.0, -Fy[d.ij1]) + g.DTy[d.ij1];
-    divu = (g.u[d.i1j] - g.u[d.ij]) * g.hy[j] + (g.v[d.ij1] - g.v[d.ij]) * g.hx[i];
-    rden = 1.0 / (ht * (aT1 + aT2 + aT3 + aT4 + Fx[d.i1j] - Fx[d.ij] + Fy[d.ij1] - Fy[d.ij]) + H * g.rho[ij]);
+    const Arr<R> Fx{g.Fx}, Fy{g.Fy}, DTx{g.DTx}, DTy{g.DTy}, u{g.u}, v{g.v};
+    const R aT1 = fmax0(Fx[d.ij]) + DTx[d.ij];
+    const R aT2 = fmax0(-Fx[d.i1j]) + DTx[d.i1j];
+    const R aT3 = fmax0(Fy[d.ij]) + DTy[d.ij];
+    const R aT4 = fmax0(-Fy[d.ij1]) + DTy[d.ij1];
+    divu = (u[d.i1j] - u[d.ij]) * num<R>(g.hy[j]) + (v[d.ij1] - v[d.ij]) * num<R>(g.hx[i]);
+    rden = num<R>(1.0) / (ht * (aT1 + aT2 + aT3 + aT4 + Fx[d.i1j] - Fx[d.ij] + Fy[d.ij1] - Fy[d.ij]) +
+                          H * num<R>(g.rho[ij]));
     w1 = aT1; w2 = aT2; w3 = aT3; w4 = aT4;
     if (co == CLS_BC) {
-      if (!fl(d.i_1j)) w1 = aT1 * g.Tw_u[ij];
-      if (!fl(d.i1j)) w2 = aT2 * g.Tw_u[d.i1j];
-      if (!fl(d.ij_1)) w3 = aT3 * g.Tw_v[ij];
-      if (!fl(d.ij1)) w4 = aT4 * g.Tw_v[d.ij1];
+      if (!fl(d.i_1j)) w1 = aT1 * num<R>(g.Tw_u[ij]);
+      if (!fl(d.i1j)) w2 = aT2 * num<R>(g.Tw_u[d.i1j]);
+      if (!fl(d.ij_1)) w3 = aT3 * num<R>(g.Tw_v[ij]);
+      if (!fl(d.ij1)) w4 = aT4 * num<R>(g.Tw_v[d.ij1]);
     }
-    pc = g.p_pr[ij] * H / g.T_pr[ij];
+    pc = num<R>(g.p_pr[ij]) * H / num<R>(g.T_pr[ij]);
     sa = ht * (apx[ij] + apx[d.i1j] + apy[ij] + apy[d.ij1]);
-    g.inv[0][ij] = w1; g.inv[1][ij] = w2; g.inv[2][ij] = w3; g.inv[3][ij] = w4;
-    g.inv[4][ij] = divu; g.inv[5][ij] = rden; g.inv[6][ij] = pc; g.inv[7][ij] = sa;
+    g.inv[0][ij] = to_double(w1); g.inv[1][ij] = to_double(w2); g.inv[2][ij] = to_double(w3);
+    g.inv[3][ij] = to_double(w4); g.inv[4][ij] = to_double(divu); g.inv[5][ij] = to_double(rden);
+    g.inv[6][ij] = to_double(pc); g.inv[7][ij] = to_double(sa);
   } else {
-    w1 = g.inv[0][ij]; w2 = g.inv[1][ij]; w3 = g.inv[2][ij]; w4 = g.inv[3][ij];
-    divu = g.inv[4][ij]; rden = g.inv[5][ij]; pc = g.inv[6][ij]; sa = g.inv[7][ij];
+    w1 = num<R>(g.inv[0][ij]); w2 = num<R>(g.inv[1][ij]); w3 = num<R>(g.inv[2][ij]); w4 = num<R>(g.inv[3][ij]);
+    divu = num<R>(g.inv[4][ij]); rden = num<R>(g.inv[5][ij]); pc = num<R>(g.inv[6][ij]); sa = num<R>(g.inv[7][ij]);
   }
-  double t1, t2, t3, t4;
+  R t1, t2, t3, t4;
   if (co == CLS_BC) {
-    t1 = fl(d.i_1j) ? w1 * TT[d.i_1j] : w1;
-    t2 = fl(d.i1j) ? w2 * TT[d.i1j] : w2;
-    t3 = fl(d.ij_1) ? w3 * TT[d.ij_1] : w3;
-    t4 = fl(d.ij1) ? w4 * TT[d.ij1] : w4;
+    t1 = fl(d.i_1j) ? w1 * Tv[d.i_1j] : w1;
+    t2 = fl(d.i1j) ? w2 * Tv[d.i1j] : w2;
+    t3 = fl(d.ij_1) ? w3 * Tv[d.ij_1] : w3;
+    t4 = fl(d.ij1) ? w4 * Tv[d.ij1] : w4;
   } else {
-    t1 = w1 * TT[d.i_1j];
-    t2 = w2 * TT[d.i1j];
-    t3 = w3 * TT[d.ij_1];
-    t4 = w4 * TT[d.ij1];
+    t1 = w1 * Tv[d.i_1j];
+    t2 = w2 * Tv[d.i1j];
+    t3 = w3 * Tv[d.ij_1];
+    t4 = w4 * Tv[d.ij1];
   }
-  Tnew = (ht * (t1 + t2 + t3 + t4 + (1.0 - g.gamma1) * P[ij] * divu) + g.ScT1[ij]) * rden;
-  double num = apx[ij] * P[d.i_1j] + apx[d.i1j] * P[d.i1j] + apy[ij] * P[d.ij_1] + apy[d.ij1] * P[d.ij1] +
-               g.bpx[ij] - g.bpx[d.i1j] + g.bpy[ij] - g.bpy[d.ij1];
+  Tnew = (ht * (t1 + t2 + t3 + t4 + num<R>(1.0 - g.gamma1) * Pv[ij] * divu) + num<R>(g.ScT1[ij])) * rden;
+  R nm = apx[ij] * Pv[d.i_1j] + apx[d.i1j] * Pv[d.i1j] + apy[ij] * Pv[d.ij_1] + apy[d.ij1] * Pv[d.ij1] +
+         num<R>(g.bpx[ij]) - num<R>(g.bpx[d.i1j]) + num<R>(g.bpy[ij]) - num<R>(g.bpy[d.ij1]);
   if (co == CLS_BC) {
-    if ((g.bits & F_GIVEN_U_XB) && i == g.Nx_o0) num += g.Fx[ij];
-    if ((g.bits & F_GIVEN_U_XE) && i == g.Nx_o1 - 1) num -= g.Fx[d.i1j];
+    if ((g.bits & F_GIVEN_U_XB) && i == g.Nx_o0) nm = nm + num<R>(g.Fx[ij]);
+    if ((g.bits & F_GIVEN_U_XE) && i == g.Nx_o1 - 1) nm = nm - num<R>(g.Fx[d.i1j]);
   }
-  pnew = (ht * num + pc) * Tnew / (sa * Tnew + H);
-  Tn[ij] = Tnew;
-  pn[ij] = pnew;
+  pnew = (ht * nm + pc) * Tnew / (sa * Tnew + H);
+  Tn[ij] = to_double(Tnew);
+  pn[ij] = to_double(pnew);
   return true;
+}
+template <bool FIRST>
+__device__ __forceinline__ bool sweep_cell_fast(const Geo& g, const Cell& c, const double* __restrict__ P,
+                                                const double* __restrict__ TT, double* __restrict__ pn,
+                                                double* __restrict__ Tn, double& Tnew, double& pnew, double& sa) {
+  return sweep_cell_t<FIRST, double>(g, c, P, TT, pn, Tn, Tnew, pnew, sa);
 }
 
 // The sweep loop of mode 1 (see k_pt_loop).
@@ -345,16 +361,17 @@ __global__ void __launch_bounds__(256, 4) kb_pt_loop_fast(const Geo* gs, const i
 // ---------------------------------------------------------------------------
 constexpr float kFloor32 = 8.0f / 16777216.0f;  // 8 units in the last place of an FP32 number
 
-// Base values of the FP32 corrections taken from an FP64 sweep x -> x1 of a solved cell.
-__device__ __forceinline__ void set_base(const Geo& g, const Cell& c, double T0, double p0, double T1, double p1,
-                                         double sa) {
+// Base values of the FP32 corrections taken from an FP64 sweep x -> x1 of a solved cell
+// (x, x1 in FP64 or double-float).
+template <class R>
+__device__ __forceinline__ void set_base(const Geo& g, const Cell& c, R T0, R p0, R T1, R p1, R sa) {
   const int ij = c.ij;
-  const double hT = g.hx[c.i] * g.hy[c.j] / T1;
-  g.T1[ij] = (float)T1;
-  g.hT[ij] = (float)hT;
-  g.q1[ij] = (float)p1;
-  g.den1[ij] = (float)(sa + hT);
-  const float dT = (float)(T1 - T0), dp = (float)(p1 - p0);
+  const R hT = num<R>(g.hx[c.i]) * num<R>(g.hy[c.j]) / T1;
+  g.T1[ij] = to_float(T1);
+  g.hT[ij] = to_float(hT);
+  g.q1[ij] = to_float(p1);
+  g.den1[ij] = to_float(sa + hT);
+  const float dT = to_float(T1 - T0), dp = to_float(p1 - p0);
   g.dT[ij] = dT;
   g.dp[ij] = dp;
   g.eT[0][ij] = dT;
@@ -381,7 +398,9 @@ __device__ __forceinline__ void sweep32_cell(const Geo& g, const Cell& c, unsign
   rp = ap <= kFloor32 * fabsf(epnew) ? 0.0f : ap;
 }
 
-struct MixedOps {
+// R: the arithmetic of the FP64 sweeps (FP64, or double-float in precision mode 3).
+template <class R>
+struct MixedOpsT {
   static __device__ __forceinline__ void pass(const Geo& g, const Cell& c, const LoopCase& s, double& rp, double& rT) {
     const int ij = c.ij;
     const unsigned base = s.base;
@@ -389,39 +408,42 @@ struct MixedOps {
       case PS_FIRST: {  // FP64 sweep from b into base ^ 1, with the FP32 coefficients of this outer iteration
         const double* P = g.p[base];
         const double* TT = g.T[base];
-        double Tnew, pnew, sa;
-        if (!sweep_cell_fast<true>(g, c, P, TT, g.p[base ^ 1], g.T[base ^ 1], Tnew, pnew, sa)) {
+        R Tnew, pnew, sa;
+        if (!sweep_cell_t<true, R>(g, c, P, TT, g.p[base ^ 1], g.T[base ^ 1], Tnew, pnew, sa)) {
           g.dT[ij] = 0.0f; g.dp[ij] = 0.0f;
           g.eT[0][ij] = 0.0f; g.ep[0][ij] = 0.0f; g.eT[1][ij] = 0.0f; g.ep[1][ij] = 0.0f;
           return;
         }
-        rp = fabs(pnew - P[ij]);
-        rT = fabs(Tnew - TT[ij]);
+        const R P0 = num<R>(P[ij]), T0 = num<R>(TT[ij]);
+        rp = to_double(dabs(pnew - P0));
+        rT = to_double(dabs(Tnew - T0));
         const Nb d = neighbours(c.i, c.j, g.Nx, g.Ny, g.bits & F_PERIODIC);
-        const double ht = g.ht, r = ht * g.inv[5][ij];
+        const R ht = num<R>(g.ht), r = ht * num<R>(g.inv[5][ij]);
         const int nb[4] = {d.i_1j, d.i1j, d.ij_1, d.ij1};
         for (int k = 0; k < 4; k++)  // a wall neighbour's term is a constant and sits in the defect
-          g.c32[k][ij] = (cls_o(g.cls[ij]) == CLS_NCH || cls_fluid(g.cls[nb[k]])) ? (float)(r * g.inv[k][ij]) : 0.0f;
-        g.c32[4][ij] = (float)(r * (1.0 - g.gamma1) * g.inv[4][ij]);
-        g.a32[0][ij] = (float)(ht * g.apx[ij]);
-        g.a32[1][ij] = (float)(ht * g.apx[d.i1j]);
-        g.a32[2][ij] = (float)(ht * g.apy[ij]);
-        g.a32[3][ij] = (float)(ht * g.apy[d.ij1]);
-        set_base(g, c, TT[ij], P[ij], Tnew, pnew, sa);
+          g.c32[k][ij] =
+              (cls_o(g.cls[ij]) == CLS_NCH || cls_fluid(g.cls[nb[k]])) ? to_float(r * num<R>(g.inv[k][ij])) : 0.0f;
+        g.c32[4][ij] = to_float(r * num<R>(1.0 - g.gamma1) * num<R>(g.inv[4][ij]));
+        g.a32[0][ij] = to_float(ht * num<R>(g.apx[ij]));
+        g.a32[1][ij] = to_float(ht * num<R>(g.apx[d.i1j]));
+        g.a32[2][ij] = to_float(ht * num<R>(g.apy[ij]));
+        g.a32[3][ij] = to_float(ht * num<R>(g.apy[d.ij1]));
+        set_base<R>(g, c, T0, P0, Tnew, pnew, sa);
         return;
       }
       case PS_MATERIALIZE:  // the iterate of the sweep before the last FP32 one, in FP64
-        g.p[base ^ 1][ij] = g.p[base][ij] + (double)g.ep[s.ec ^ 1][ij];
-        g.T[base ^ 1][ij] = g.T[base][ij] + (double)g.eT[s.ec ^ 1][ij];
+        g.p[base ^ 1][ij] = g.p[base][ij] + widen(g.ep[s.ec ^ 1][ij]);
+        g.T[base ^ 1][ij] = g.T[base][ij] + widen(g.eT[s.ec ^ 1][ij]);
         return;
       case PS_CONFIRM: {  // that sweep again in FP64 into the base buffer; exports for a re-basing
         const double* P = g.p[base ^ 1];
         const double* TT = g.T[base ^ 1];
-        double Tnew, pnew, sa;
-        if (!sweep_cell_fast<false>(g, c, P, TT, g.p[base], g.T[base], Tnew, pnew, sa)) return;
-        rp = fabs(pnew - P[ij]);
-        rT = fabs(Tnew - TT[ij]);
-        set_base(g, c, TT[ij], P[ij], Tnew, pnew, sa);
+        R Tnew, pnew, sa;
+        if (!sweep_cell_t<false, R>(g, c, P, TT, g.p[base], g.T[base], Tnew, pnew, sa)) return;
+        const R P0 = num<R>(P[ij]), T0 = num<R>(TT[ij]);
+        rp = to_double(dabs(pnew - P0));
+        rT = to_double(dabs(Tnew - T0));
+        set_base<R>(g, c, T0, P0, Tnew, pnew, sa);
         return;
       }
       default:
@@ -473,11 +495,78 @@ struct MixedOps {
 };
 
 __global__ void __launch_bounds__(256, 4) k_pt_loop_mixed(Geo g, int ntiles, LoopCtl* lc) {
-  pt_loop_rounds<MixedOps, true>(g, nullptr, nullptr, nullptr, 1, ntiles, lc);
+  pt_loop_rounds<MixedOpsT<double>, true>(g, nullptr, nullptr, nullptr, 1, ntiles, lc);
 }
 __global__ void __launch_bounds__(256, 4) kb_pt_loop_mixed(const Geo* gs, const int* tile_case, const int* tile_first,
                                                           int ncases, int ntiles, LoopCtl* lc) {
-  pt_loop_rounds<MixedOps, false>(gs[0], gs, tile_case, tile_first, ncases, ntiles, lc);
+  pt_loop_rounds<MixedOpsT<double>, false>(gs[0], gs, tile_case, tile_first, ncases, ntiles, lc);
+}
+
+// Self-check of the double-float arithmetic against FP64 on n pseudo-random operand pairs of
+// random sign and magnitude 2^-40 .. 2^40: the largest relative error of the FP64 -> double-float
+// conversion and of add, multiply, divide and square root, as bit patterns in err[0..4] (folded
+// with atomicMax; non-negative doubles order like their bits).  Additions are checked against
+// |a| + |b| (the error bound of a double-word sum is relative to the operands, not the result).
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ double rand_val(unsigned long long r) {
+  const int e = (int)((r >> 52) % 81ull) - 40;
+  const unsigned long long bits = ((r >> 63) << 63) | ((unsigned long long)(e + 1023) << 52) | (r & 0xFFFFFFFFFFFFFull);
+  return __longlong_as_double((long long)bits);
+}
+__global__ void k_check_df(unsigned long long n, unsigned long long seed, unsigned long long* err) {
+  double m[5] = {0, 0, 0, 0, 0};
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n; k += stride) {
+    const double a = rand_val(mix64(seed + 2 * k)), b = rand_val(mix64(seed + 2 * k + 1));
+    const df A = to_df(a), B = to_df(b);
+    m[0] = fmax(m[0], fabs(to_double(A) - a) / fabs(a));
+    m[1] = fmax(m[1], fabs(to_double(A + B) - (a + b)) / (fabs(a) + fabs(b)));
+    m[2] = fmax(m[2], fabs(to_double(A * B) - a * b) / fabs(a * b));
+    m[3] = fmax(m[3], fabs(to_double(A / B) - a / b) / fabs(a / b));
+    const double sa = ::sqrt(fabs(a));
+    m[4] = fmax(m[4], fabs(to_double(dsqrt(dabs(A))) - sa) / sa);
+  }
+  for (int q = 0; q < 5; q++) atomicMax(&err[q], (unsigned long long)__double_as_longlong(m[q]));
+}
+
+// ---------------------------------------------------------------------------
+// Precision mode 3: precision mode 2 with the FP64 arithmetic of the assembly, the fluxes and
+// diffusion terms and the FP64 sweeps done in double-float (sts_df.cuh) on GB300's FP32 pipes;
+// fields stay FP64 in memory, the FP32 correction sweeps are those of mode 2.
+// ---------------------------------------------------------------------------
+// grid z: 3 parts (k_) or 3 parts per case (kb_, z = 3 case + part)
+__device__ __forceinline__ void assemble_df_part(const Geo& g, unsigned long long h_sweep, int in_graph, unsigned part) {
+  switch (part) {  // each part compiled on its own (constant mask)
+    case 0: assemble_t<df>(g, h_sweep, in_graph, 1u); break;
+    case 1: assemble_t<df>(g, h_sweep, in_graph, 2u); break;
+    default: assemble_t<df>(g, h_sweep, in_graph, 4u); break;
+  }
+}
+__global__ void __launch_bounds__(256, 3) k_assemble_df(Geo g, unsigned long long h_sweep, int in_graph) {
+  assemble_df_part(g, h_sweep, in_graph, blockIdx.z);
+}
+__global__ void __launch_bounds__(256, 3) kb_assemble_df(const Geo* gs, unsigned long long h_sweep, int in_graph) {
+  __shared__ Geo sg;
+  if (!stage_geo(sg, gs, blockIdx.z / 3)) return;
+  assemble_df_part(sg, h_sweep, in_graph, blockIdx.z % 3);
+}
+__global__ void __launch_bounds__(256, 4) k_flux_diff_df(Geo g, unsigned tail) { flux_diff_t<df>(g, tail); }
+__global__ void __launch_bounds__(256, 4) kb_flux_diff_df(const Geo* gs, unsigned tail) {
+  __shared__ Geo sg;
+  if (!stage_geo(sg, gs)) return;
+  flux_diff_t<df>(sg, tail);
+}
+__global__ void __launch_bounds__(256, 4) k_pt_loop_mixed_df(Geo g, int ntiles, LoopCtl* lc) {
+  pt_loop_rounds<MixedOpsT<df>, true>(g, nullptr, nullptr, nullptr, 1, ntiles, lc);
+}
+__global__ void __launch_bounds__(256, 4) kb_pt_loop_mixed_df(const Geo* gs, const int* tile_case,
+                                                             const int* tile_first, int ncases, int ntiles,
+                                                             LoopCtl* lc) {
+  pt_loop_rounds<MixedOpsT<df>, false>(gs[0], gs, tile_case, tile_first, ncases, ntiles, lc);
 }
 
 }  // namespace sts

@@ -72,5 +72,14 @@ __global__ void kb_pt_loop_fast(const Geo* gs, const int* tile_case, const int* 
                                 LoopCtl* lc);
 __global__ void kb_pt_loop_mixed(const Geo* gs, const int* tile_case, const int* tile_first, int ncases, int ntiles,
                                  LoopCtl* lc);
+// precision mode 3: double-float arithmetic in the FP64-bound kernels
+__global__ void k_check_df(unsigned long long n, unsigned long long seed, unsigned long long* err);
+__global__ void k_assemble_df(Geo g, unsigned long long h_sweep, int in_graph);
+__global__ void kb_assemble_df(const Geo* gs, unsigned long long h_sweep, int in_graph);
+__global__ void k_flux_diff_df(Geo g, unsigned tail);
+__global__ void kb_flux_diff_df(const Geo* gs, unsigned tail);
+__global__ void k_pt_loop_mixed_df(Geo g, int ntiles, LoopCtl* lc);
+__global__ void kb_pt_loop_mixed_df(const Geo* gs, const int* tile_case, const int* tile_first, int ncases, int ntiles,
+                                    LoopCtl* lc);
 
 }  // namespace sts

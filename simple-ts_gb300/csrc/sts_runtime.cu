@@ -114,8 +114,7 @@ struct sts_ctx {
     k_bnd_tjump<<<tjump_grid(), 256, 0, s>>>(g);
     mark(5);
     mark(-1);
-    if (fast()) k_flux_diff_fast<<<grid, block, 0, s>>>(g, PH_TEMP | PH_PRES);
-    else k_flux_diff<<<grid, block, 0, s>>>(g, PH_TEMP | PH_PRES);
+    flux_kernel()<<<grid, block, 0, s>>>(g, PH_TEMP | PH_PRES);
     mark(6);
   }
   // the learned warm start's kernels after the start of a step (mode 3)
@@ -129,10 +128,22 @@ struct sts_ctx {
     mark(0);
   }
   bool fast() const { return g.precision >= 1; }
-  bool mixed() const { return g.precision == 2 && !(hc.bits & F_FIXED_SWEEPS); }
+  bool mixed() const { return g.precision >= 2 && !(hc.bits & F_FIXED_SWEEPS); }
+  using AsmKernel = void (*)(Geo, unsigned long long, int);
+  using FluxKernel = void (*)(Geo, unsigned);
+  AsmKernel asm_kernel() const {
+    return g.precision == 3 ? k_assemble_df : (fast() ? k_assemble_fast : k_assemble);
+  }
+  dim3 asm_grid() const { return g.precision == 3 ? dim3(grid.x, grid.y, 3) : grid; }
+  FluxKernel flux_kernel() const {
+    return g.precision == 3 ? k_flux_diff_df : (fast() ? k_flux_diff_fast : k_flux_diff);
+  }
   // the persistent sweep-loop kernel of this context and its grid (CTAs that fit at once)
   using PtKernel = void (*)(Geo, int, LoopCtl*);
-  PtKernel pt_kernel() const { return mixed() ? k_pt_loop_mixed : (fast() ? k_pt_loop_fast : k_pt_loop); }
+  PtKernel pt_kernel() const {
+    if (mixed()) return g.precision == 3 ? k_pt_loop_mixed_df : k_pt_loop_mixed;
+    return fast() ? k_pt_loop_fast : k_pt_loop;
+  }
   dim3 pt_grid;
   int size_pt_grid() {
     int dev = 0, sms = 0, per_sm = 0;
@@ -220,7 +231,7 @@ int sts_ctx::build_graph() {
   if (int r = add_kernel(&n_end, b_step, {n_outer}, k_step_end, dim3(1), dim3(1024), g, (unsigned long long)hs, 1))
     return r;
   cudaGraphNode_t n_asm, n_sw, n_cor, n_rho, n_bnd, n_fd;
-  if (int r = add_kernel(&n_asm, b_outer, {}, fast() ? k_assemble_fast : k_assemble, grid, block, g,
+  if (int r = add_kernel(&n_asm, b_outer, {}, asm_kernel(), asm_grid(), block, g,
                          (unsigned long long)0, 0))
     return r;
   if (int r = add_kernel(&n_sw, b_outer, {n_asm}, pt_kernel(), pt_grid, dim3(32, 8), g, ntiles, d_lc)) return r;
@@ -239,7 +250,7 @@ int sts_ctx::build_graph() {
                          (unsigned)(PH_VEL | PH_PBEGIN), (unsigned long long)0, 0))
     return r;
   if (int r = add_kernel(&n_tj, b_outer, {n_bnd}, k_bnd_tjump, tjump_grid(), dim3(256), g)) return r;
-  if (int r = add_kernel(&n_fd, b_outer, {n_tj}, fast() ? k_flux_diff_fast : k_flux_diff, grid, block, g,
+  if (int r = add_kernel(&n_fd, b_outer, {n_tj}, flux_kernel(), grid, block, g,
                          (unsigned)(PH_TEMP | PH_PRES)))
     return r;
   CU(cudaGraphInstantiate(&exec, graph, 0));
@@ -269,8 +280,7 @@ int sts_ctx::step_host(int n, int* done) {
     k_step_begin<<<grid, block, 0, s>>>(g, 1, 0, 0);
     warm_launches([](int) {});
     for (int outer = 0; outer < NI; outer++) {
-      if (fast()) k_assemble_fast<<<grid, block, 0, s>>>(g, 0, 0);
-      else k_assemble<<<grid, block, 0, s>>>(g, 0, 0);
+      asm_kernel()<<<asm_grid(), block, 0, s>>>(g, 0, 0);
       if (int r = pt_loop()) return r;
       k_correct<<<grid, block, 0, s>>>(g);
       k_face_rho<<<grid, block, 0, s>>>(g);
@@ -313,8 +323,7 @@ int sts_ctx::profile(int n, double* ms, int* cnt, int* done) {
     warm_launches(mark);
     for (int outer = 0; outer < NI; outer++) {
       mark(-1);
-      if (fast()) k_assemble_fast<<<grid, block, 0, s>>>(g, 0, 0);
-      else k_assemble<<<grid, block, 0, s>>>(g, 0, 0);
+      asm_kernel()<<<asm_grid(), block, 0, s>>>(g, 0, 0);
       mark(1);
       mark(-1);
       if (int r = pt_loop()) return r;
@@ -545,7 +554,7 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
   c->opt = opt;
   c->t0 = std::chrono::steady_clock::now();
   std::string err;
-  if (opt.precision < 0 || opt.precision > 2) return fail(STS_ERR_ARG, "precision must be 0, 1 or 2");
+  if (opt.precision < 0 || opt.precision > 3) return fail(STS_ERR_ARG, "precision must be 0, 1, 2 or 3");
   if (opt.warm_start < 0 || opt.warm_start > 3) return fail(STS_ERR_ARG, "warm_start must be 0, 1, 2 or 3");
   if (!load_case(dir, opt.fixed_sweeps != 0, c->hc, err)) return fail(STS_ERR_INPUT, err);
   Case& h = c->hc;
@@ -688,7 +697,7 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
     const size_t nb = (size_t)((h.Nx + 31) / 32) * ((h.Ny + 7) / 8);
     if (int r = c->alloc(&g.warm_part, nb * 18)) return r;  // 2 fields x 9 normal-equation terms
   }
-  if (g.precision == 2) {
+  if (g.precision >= 2) {
     float** f32[] = {&g.c32[0], &g.c32[1], &g.c32[2], &g.c32[3], &g.c32[4], &g.a32[0], &g.a32[1], &g.a32[2], &g.a32[3],
                      &g.T1, &g.hT, &g.q1, &g.den1, &g.dT, &g.dp, &g.ep[0], &g.ep[1], &g.eT[0], &g.eT[1]};
     for (float** f : f32)
@@ -1052,6 +1061,24 @@ int sts_inspect_case(const char* case_dir, int* Nx, int* Ny, unsigned int* vol_o
   return STS_OK;
 }
 
+int sts_check_double_float(unsigned long long n, unsigned long long seed, int device, double* max_rel_err) {
+  if (!max_rel_err) return fail(STS_ERR_ARG, "null argument");
+  CU(cudaSetDevice(device));
+  unsigned long long* d = nullptr;
+  CU(cudaMalloc(&d, 5 * sizeof(unsigned long long)));
+  cudaError_t e = cudaMemset(d, 0, 5 * sizeof(unsigned long long));
+  if (e == cudaSuccess) {
+    k_check_df<<<1216, 256>>>(n, seed, d);
+    e = cudaGetLastError();
+  }
+  unsigned long long h[5] = {0, 0, 0, 0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(STS_ERR_CUDA, std::string("sts_check_double_float: ") + cudaGetErrorString(e));
+  for (int q = 0; q < 5; q++) std::memcpy(&max_rel_err[q], &h[q], sizeof(double));
+  return STS_OK;
+}
+
 int sts_check_division(unsigned long long n, unsigned long long seed, int device, unsigned long long* mismatches) {
   if (!mismatches) return fail(STS_ERR_ARG, "null argument");
   CU(cudaSetDevice(device));
@@ -1108,7 +1135,8 @@ struct sts_batch {
   bool fast() const { return precision >= 1; }
   using PtKernel = void (*)(const Geo*, const int*, const int*, int, int, LoopCtl*);
   PtKernel pt_kernel() const {
-    return (precision == 2 && !fixed) ? kb_pt_loop_mixed : (fast() ? kb_pt_loop_fast : kb_pt_loop);
+    if (precision >= 2 && !fixed) return precision == 3 ? kb_pt_loop_mixed_df : kb_pt_loop_mixed;
+    return fast() ? kb_pt_loop_fast : kb_pt_loop;
   }
   int build_graph();
   int step_host(int n);
@@ -1130,7 +1158,8 @@ int sts_batch::step_host(int n) {
       kb_warm_fit<<<dim3(1, 1, ncases), 576, 0, s>>>(G);
       kb_warm_apply<<<cell_grid, blk, 0, s>>>(G);
     }
-    if (fast()) kb_assemble_fast<<<cell_grid, blk, 0, s>>>(G, 0ull, 0);
+    if (precision == 3) kb_assemble_df<<<dim3(cell_grid.x, cell_grid.y, 3 * ncases), blk, 0, s>>>(G, 0ull, 0);
+    else if (fast()) kb_assemble_fast<<<cell_grid, blk, 0, s>>>(G, 0ull, 0);
     else kb_assemble<<<cell_grid, blk, 0, s>>>(G, 0ull, 0);
     const int* tc = d_tile_case;
     const int* tf = d_tile_first;
@@ -1141,7 +1170,8 @@ int sts_batch::step_host(int n) {
     kb_bnd_walls<<<walls_grid, 256, 0, s>>>(G, PH_CONTROL | PH_SLIP_U | PH_SLIP_V, 0ull, 0);
     kb_boundary<<<dim3(1, 1, ncases), 1024, 0, s>>>(G, PH_VEL | PH_PBEGIN, 0ull, 0);
     kb_bnd_tjump<<<tjump_grid, 256, 0, s>>>(G);
-    if (fast()) kb_flux_diff_fast<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
+    if (precision == 3) kb_flux_diff_df<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
+    else if (fast()) kb_flux_diff_fast<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
     else kb_flux_diff<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
     kb_step_end<<<dim3(1, 1, ncases), 1024, 0, s>>>(G, 0ull, 0);
     kb_continue<<<1, 256, 0, s>>>(G, ncases, 0ull, d_flag);
@@ -1171,7 +1201,8 @@ int sts_batch::build_graph() {
     if (int r = add_kernel(&w[2], b, {w[1]}, kb_warm_apply, cell_grid, blk, G)) return r;
     n[0] = w[2];
   }
-  if (int r = add_kernel(&n[1], b, {n[0]}, fast() ? kb_assemble_fast : kb_assemble, cell_grid, blk, G,
+  if (int r = add_kernel(&n[1], b, {n[0]}, precision == 3 ? kb_assemble_df : (fast() ? kb_assemble_fast : kb_assemble),
+                         precision == 3 ? dim3(cell_grid.x, cell_grid.y, 3 * ncases) : cell_grid, blk, G,
                          (unsigned long long)0, 0))
     return r;
   if (int r = add_kernel(&n[2], b, {n[1]}, pt_kernel(), pt_grid, blk, G, (const int*)d_tile_case,
@@ -1191,7 +1222,8 @@ int sts_batch::build_graph() {
                          (unsigned)(PH_VEL | PH_PBEGIN), (unsigned long long)0, 0))
     return r;
   if (int r = add_kernel(&n[7], b, {n[6]}, kb_bnd_tjump, tjump_grid, dim3(256), G)) return r;
-  if (int r = add_kernel(&n[8], b, {n[7]}, fast() ? kb_flux_diff_fast : kb_flux_diff, cell_grid, blk, G,
+  if (int r = add_kernel(&n[8], b, {n[7]}, precision == 3 ? kb_flux_diff_df : (fast() ? kb_flux_diff_fast : kb_flux_diff),
+                         cell_grid, blk, G,
                          (unsigned)(PH_TEMP | PH_PRES)))
     return r;
   if (int r = add_kernel(&n[9], b, {n[8]}, kb_step_end, dim3(1, 1, ncases), dim3(1024), G, (unsigned long long)0, 0))

@@ -28,13 +28,13 @@ EXPORTS = [
     "sts_stats", "sts_sweep_history", "sts_write_outputs", "sts_run_case", "sts_sync", "sts_destroy",
     "sts_last_error", "sts_inspect_case", "sts_step_timed", "sts_profile_steps", "sts_pt_sweeps",
     "sts_pt_sweeps_noalloc", "sts_check_division", "sts_open_batch", "sts_batch_step", "sts_batch_step_timed",
-    "sts_batch_case", "sts_batch_destroy",
+    "sts_batch_case", "sts_batch_destroy", "sts_check_double_float",
 ]
 
 KERNELS = ["step_begin", "assemble", "sweep_loop", "correct", "face_rho", "boundary", "flux_diff", "step_end"]
 
 # precision modes of sts_options.precision
-EXACT, FAST_FP64, MIXED = 0, 1, 2
+EXACT, FAST_FP64, MIXED, MIXED_DF = 0, 1, 2, 3
 
 FIELDS = ["u", "v", "p", "T", "rho", "sqrt_T", "rho_u", "rho_v", "Fx", "Fy", "D_ux", "D_uy", "D_vx", "D_vy",
           "DTx", "DTy", "Gamma_xf", "Gamma_yf", "ScT1", "apx", "apy", "bpx", "bpy", "u_pseudo", "v_pseudo",
@@ -320,3 +320,12 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def check_double_float(n: int, seed: int = 1, device: int = 0):
+    """Largest relative errors of the double-float conversion, add, multiply, divide and sqrt."""
+    lib = load()
+    lib.sts_check_double_float.argtypes = [C.c_ulonglong, C.c_ulonglong, C.c_int, C.POINTER(C.c_double)]
+    out = (C.c_double * 5)()
+    _check(lib.sts_check_double_float(int(n), int(seed), int(device), out))
+    return dict(zip(["convert", "add", "mul", "div", "sqrt"], list(out)))

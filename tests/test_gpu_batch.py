@@ -51,7 +51,7 @@ def test_batch_matches_oracle_per_case(lib_built, oracle_built):
         b.close()
 
 
-@pytest.mark.parametrize("precision", [1, 2])
+@pytest.mark.parametrize("precision", [1, 2, 3])
 def test_batch_equals_single_runs(precision, lib_built):
     import sts
     cases = small_batch(4, Nt=40, seed=7)

@@ -10,3 +10,13 @@ pytestmark = pytest.mark.gpu
 def test_reciprocal_division_matches_ieee(seed, lib_built):
     import sts
     assert sts.check_division(1 << 28, seed) == 0
+
+
+def test_double_float_arithmetic_accuracy(lib_built):
+    """Precision mode 3's double-float words carry about 47 bits: every basic operation must stay
+    within a few units of 2^-47 of the FP64 result."""
+    import sts
+    err = sts.check_double_float(1 << 24, seed=3)
+    print(err)
+    for k, e in err.items():
+        assert e < 2.0 ** -44, (k, e)

@@ -57,23 +57,24 @@ def test_fast_fp64_within_1e10(name, lib_built, oracle_built):
         assert e <= (REL_FP64_V if f == "v" else REL_FP64), (f, e)
 
 
+@pytest.mark.parametrize("mode", [2, 3])
 @pytest.mark.parametrize("name", ["channel_ma2.43_60x12_resid", "rayleigh_benard_32x16_resid",
                                   "channel_circle_120x12_resid", "channel_ma0.1_80x8_resid"])
-def test_mixed_error_per_field(name, lib_built, oracle_built):
-    import sts
+def test_mixed_error_per_field(name, mode, lib_built, oracle_built):
     case, fixed = golden_case(name)
     assert not fixed
-    err, hist, o, g = run_pair(case, fixed, 10, sts.MIXED)
+    err, hist, o, g = run_pair(case, fixed, 10, mode)
     oh = o.sweeps()
     g.close()
-    print(name, "mode 2", err, "sweeps", hist.tolist(), "oracle", oh.tolist())
+    print(name, "mode", mode, err, "sweeps", hist.tolist(), "oracle", oh.tolist())
     for f, e in err.items():
         assert e <= REL_MIXED, (f, e)
 
 
-def test_mixed_meets_tolerance_every_step(lib_built):
-    """The stopping residual of every step is an FP64 update and meets MaxError_p_c / MaxError_T
-    (or the sweep cap was reached)."""
+@pytest.mark.parametrize("mode", [2, 3])
+def test_mixed_meets_tolerance_every_step(mode, lib_built):
+    """The stopping residual of every step is an FP64 (mode 3: double-float) update and meets
+    MaxError_p_c / MaxError_T (or the sweep cap was reached)."""
     import sts
     case = sc.config_case("channel_ma0.1", Nt=30)
     tol_p = float(case.entered["MaxError_p_c"])
@@ -81,7 +82,7 @@ def test_mixed_meets_tolerance_every_step(lib_built):
     cap = int(case.entered["N_I_p_c"])
     with tempfile.TemporaryDirectory() as d:
         case.write(d)
-        g = sts.Solver(d, fixed_sweeps=False, precision=sts.MIXED)
+        g = sts.Solver(d, fixed_sweeps=False, precision=mode)
         for _ in range(30):
             assert g.step(1) == 1
             st = g.stats()
@@ -91,13 +92,14 @@ def test_mixed_meets_tolerance_every_step(lib_built):
         g.close()
 
 
-def test_mixed_graph_and_launches_agree(lib_built):
+@pytest.mark.parametrize("mode", [2, 3])
+def test_mixed_graph_and_launches_agree(mode, lib_built):
     import sts
     case = sc.channel_case("c", 100, 10, 0.3, 0.002, 1e-3, 40)
     with tempfile.TemporaryDirectory() as d:
         case.write(d)
-        a = sts.Solver(d, fixed_sweeps=False, use_graph=True, precision=sts.MIXED)
-        b = sts.Solver(d, fixed_sweeps=False, use_graph=False, precision=sts.MIXED)
+        a = sts.Solver(d, fixed_sweeps=False, use_graph=True, precision=mode)
+        b = sts.Solver(d, fixed_sweeps=False, use_graph=False, precision=mode)
         assert a.step(12) == b.step(12) == 12
         for f in FIELDS:
             np.testing.assert_array_equal(a.field(f), b.field(f))
@@ -127,4 +129,4 @@ def test_bad_precision_rejected(lib_built):
     with tempfile.TemporaryDirectory() as d:
         case.write(d)
         with pytest.raises(sts.StsError):
-            sts.Solver(d, precision=3)
+            sts.Solver(d, precision=4)
