@@ -254,6 +254,8 @@ struct Oracle {
   int Nt_save_solved_data_counter = 0, Nt_save_temp_data_counter = 0;
   uint Nt_save_DragCoefficient_counter = 0;
   bool ToCheckForFileIsNow_Tmp = true, ToCheckForFileIsNow_Iterations_in_loops = true;
+  bool ToCheckForFileIsNow_CD = true, ToCheckForFileIsNow_p_u_x_b = true;
+  std::vector<double> continuity_st, continuity;
 
   // ---- mesh ----
   std::vector<double> x_f, y_f, hx, hy, x_v, y_v;
@@ -358,6 +360,8 @@ struct Oracle {
   void step();
   void write_solved();
   void write_temp();
+  void write_drag();
+  void solve_continuity();
   void write_iterations();
   void finish();
   std::string path(const std::string& f) const { return dir + "/" + f; }
@@ -1294,6 +1298,156 @@ void Oracle::write_solved() {
   o << it << std::endl;
 }
 
+// WriteDragCoefficient, SIMPLE_TS_MPI.cpp:8147-8578 (serial path): drag coefficients of the
+// flagged bodies (CD.<body>.txt), the short-format summary and the inflow pressure-control log.
+void Oracle::write_drag() {
+  if (!write_files) return;
+  double CD_fr_x = 0, CD_p_x = 0;
+  const uint nbodies = (uint)bodies.size();
+  for (uint counter = 0; counter < nbodies; counter++) {
+    if (!bodies[counter].drag) continue;
+    double CD_fr_bottom = 0, CD_p_bottom = 0, S_bottom = 0, CD_fr_front = 0, CD_p_front = 0, S_front = 0;
+    double CD_fr_top = 0, CD_p_top = 0, S_top = 0, CD_fr_behind = 0, CD_p_behind = 0, S_behind = 0;
+    for (uint i = Nx_o[0]; i < Nx_o[1]; i++)
+      for (uint j = Ny_o[0]; j < Ny_o[1]; j++) {
+        const uint node = i + j * Nx;
+        if (vol_inf_fb[node] - 1 != counter) continue;
+        const Idx d = clamped(i, j);  // ij_function_i_and_j_to_the_boundaries, also for periodic cases
+        if (vol[d.ij_1]) {
+          CD_fr_bottom += hx[i] * std::sqrt(Tw_v[d.ij]) *
+                          ((u[d.ij_1] - u[d.ij]) / hy[j - 1 * (j < (Ny - 1))] +
+                           (u[d.i1j_1] - u[d.i1j]) / hy[j - 1 * (j < (Ny - 1))]);
+          CD_p_bottom += p[d.ij_1] * hx[i];
+          S_bottom += hx[i];
+        }
+        if (vol[d.i_1j]) {
+          CD_fr_front += hy[j] * std::sqrt(Tw_u[d.ij]) *
+                         ((v[d.i_1j] - v[d.ij]) / hx[d.i_1] + (v[d.i_1j1] - v[d.ij1]) / hx[d.i_1]);
+          CD_p_front += p[d.i_1j] * hy[j];
+          S_front += hy[j];
+        }
+        if (vol[d.ij1]) {
+          CD_fr_top += hx[i] * std::sqrt(Tw_v[d.ij1]) *
+                       ((u[d.ij1] - u[d.ij]) / hy[j + 1 * (0 < j)] + (u[d.i1j1] - u[d.i1j]) / hy[j + 1 * (0 < j)]);
+          CD_p_top += p[d.ij1] * hx[i];
+          S_top += hx[i];
+        }
+        if (vol[d.i1j]) {
+          CD_fr_behind += hy[j] * std::sqrt(Tw_u[d.i1j]) *
+                          ((v[d.i1j] - v[d.ij]) / hx[d.i1] + (v[d.i1j1] - v[d.ij1]) / hx[d.i1]);
+          CD_p_behind += p[d.i1j] * hy[j];
+          S_behind += hy[j];
+        }
+      }
+    double c_CD_p = 0, c_CD_fr = 0;
+    if (TypeND == 1) {
+      c_CD_p = 1.0 / (u_given_xb_in_it * u_given_xb_in_it * (p_BC_xb / T_BC_xb));
+      c_CD_fr = 2.0 / (Re * u_given_xb_in_it);
+    } else if (TypeND == 2) {
+      c_CD_p = 2.0 / (gamma1 * Ma * Ma * (p_BC_xb / T_BC_xb));
+      c_CD_fr = 2.0 / (Re * u_given_xb_in_it);
+    } else if (TypeND == 3) {
+      c_CD_p = 1.0 / (u_given_xb_in_it * u_given_xb_in_it * (p_BC_xb / T_BC_xb));
+      c_CD_fr = (5.0 / 8.0) * std::sqrt(M_PI) * Kn / (u_given_xb_in_it * u_given_xb_in_it * (p_BC_xb / T_BC_xb));
+    }
+    CD_fr_bottom = c_CD_fr * CD_fr_bottom;
+    CD_p_bottom = c_CD_p * CD_p_bottom;
+    CD_fr_front = c_CD_fr * CD_fr_front;
+    CD_p_front = c_CD_p * CD_p_front;
+    CD_fr_top = c_CD_fr * CD_fr_top;
+    CD_p_top = c_CD_p * CD_p_top;
+    CD_fr_behind = c_CD_fr * CD_fr_behind;
+    CD_p_behind = c_CD_p * CD_p_behind;
+    CD_fr_x = (CD_fr_top / S_top) + (CD_fr_bottom / S_bottom);
+    CD_p_x = (CD_p_front / S_front) - (CD_p_behind / S_behind);
+    std::ostringstream name;
+    name << "CD." << counter << ".txt";
+    std::ofstream o;
+    if (ToCheckForFileIsNow_CD && !ToReadSolvedDataFromFile) o.open(path(name.str()).c_str());
+    else o.open(path(name.str()).c_str(), std::ios::out | std::ios::app);
+    const int w = 30;
+    if (!ToReadSolvedDataFromFile && ToCheckForFileIsNow_CD) {
+      const char* hdr[16] = {"//it (number of step by time) 00", "ht (step by time) 01", "CD_fr_x (CD from friction) 02",
+                             "CD_p_x (CD from pressure) 03", "S_for_CD_bottom 04", "S_for_CD_front 05",
+                             "S_for_CD_top 06", "S_for_CD_behind 07", "CD_fr_bottom 08", "CD_p_bottom 09",
+                             "CD_fr_front 10", "CD_p_front 11", "CD_fr_top 12", "CD_p_top 13", "CD_fr_behind 14",
+                             "CD_p_behind 15"};
+      for (const char* h : hdr) o << std::setw(w) << h;
+      o << std::endl;
+    }
+    o << std::setw(w) << it << std::setiosflags(std::ios::scientific) << std::setprecision(10);
+    const double vals[15] = {ht, CD_fr_x, CD_p_x, S_bottom, S_front, S_top, S_behind, CD_fr_bottom,
+                             CD_p_bottom, CD_fr_front, CD_p_front, CD_fr_top, CD_p_top, CD_fr_behind, CD_p_behind};
+    for (double x : vals) o << std::setw(w) << x;
+    o << std::endl;
+    ToCheckForFileIsNow_CD = false;
+  }
+  if (WriteDataInShortFormat_kind == 1) {
+    double q_xb = 0, q_xe = 0;
+    for (uint j = 0; j < Ny; j++) {
+      const uint n = 0 + j * Nx;
+      if (vol[n]) q_xb += rho[n] * u[n] * hy[j];
+    }
+    for (uint j = 0; j < Ny; j++) {
+      const uint n = Nx_u[1] + j * Nx;
+      if (vol[n]) q_xe += rho[n] * u[n] * hy[j];
+    }
+    std::ofstream o(path("DataInShortFormat.txt").c_str());
+    const int w = 30;
+    o << std::setiosflags(std::ios::scientific) << std::setprecision(15) << std::setw(w) << Re << std::setw(w) << Kn
+      << std::setw(w) << CD_p_x + CD_fr_x << std::setw(w) << CD_p_x << std::setw(w) << u_gas_nd << std::setw(w) << q_xb
+      << std::setw(w) << q_xe << std::setw(w) << p_BC_xb << std::setw(w) << p_BC_xe << std::endl;
+  }
+  if (Pressure_BC) {
+    std::ofstream o;
+    if (ToCheckForFileIsNow_p_u_x_b && !ToReadSolvedDataFromFile) o.open(path("p_and_u_xb_it.txt").c_str());
+    else o.open(path("p_and_u_xb_it.txt").c_str(), std::ios::out | std::ios::app);
+    const int w = 30;
+    if (!ToReadSolvedDataFromFile && ToCheckForFileIsNow_p_u_x_b) {
+      const char* hdr[7] = {"//it (number of step by time)", "ht (step by time)", "p_BC_xb", "u_given_xb_in_it",
+                            "u_given_xb_in_it_max", "u_given_xb_in_it_mean", "p_correction"};
+      for (const char* h : hdr) o << std::setw(w) << h;
+      o << std::endl;
+    }
+    o << std::setw(w) << it << std::setiosflags(std::ios::scientific) << std::setprecision(15) << std::setw(w) << ht
+      << std::setw(w) << p_BC_xb << std::setw(w) << u_given_xb_in_it << std::setw(w) << u_given_xb_in_it_max
+      << std::setw(w) << u_given_xb_in_it_mean << std::setw(w) << p_correction << std::endl;
+    ToCheckForFileIsNow_p_u_x_b = false;
+  }
+}
+
+// SolveContinuityEquation, SIMPLE_TS_MPI.cpp:10621-10714 (serial path): the fluxes again, then the
+// steady and unsteady continuity residuals of every cell, written as dumps.
+void Oracle::solve_continuity() {
+  solve_fluxes();
+  continuity_st.assign(Na, 0.0);
+  continuity.assign(Na, 0.0);
+  for (uint j = 0; j < Ny - 1; j++)
+    for (uint i = 0; i < Nx - 1; i++) {
+      const Idx d = Periodic ? periodic(i, j) : clamped(i, j);
+      continuity_st[d.ij] = Fx[d.i1j] - Fx[d.ij] + Fy[d.ij1] - Fy[d.ij];
+      continuity[d.ij] = (rho[d.ij] - rho_pr[d.ij]) * hx[i] * hy[j] / ht + continuity_st[d.ij];
+    }
+  if (!write_files) return;
+  std::ostringstream its;
+  its << it;
+  if (ToWriteSolvedDataToBinaryFile) {
+    write_bin(path("ContinuityEquation_stationary.bin"), continuity_st.data(), sizeof(double) * Na);
+    write_bin(path("ContinuityEquation.bin"), continuity.data(), sizeof(double) * Na);
+    if (ToWriteSolvedDataToNewFiles) {
+      write_bin(path("ContinuityEquation_stationary." + its.str() + ".bin"), continuity_st.data(), sizeof(double) * Na);
+      write_bin(path("ContinuityEquation." + its.str() + ".bin"), continuity.data(), sizeof(double) * Na);
+    }
+  } else {
+    write_txt(path("ContinuityEquation_stationary.txt"), continuity_st.data(), Na);
+    write_txt(path("ContinuityEquation.txt"), continuity.data(), Na);
+    if (ToWriteSolvedDataToNewFiles) {
+      write_txt(path("ContinuityEquation_stationary." + its.str() + ".txt"), continuity_st.data(), Na);
+      write_txt(path("ContinuityEquation." + its.str() + ".txt"), continuity.data(), Na);
+    }
+  }
+}
+
 // WriteTempDataToFile, SIMPLE_TS_MPI.cpp:5838-5942
 void Oracle::write_temp() {
   if (!write_files) return;
@@ -1970,16 +2124,23 @@ void Oracle::step() {
     bc_pressure();
     solve_fluxes();
     solve_diffusion();
+    if (ToSolveContinuityEquation) solve_continuity();  // :4588-4591
   } while (continue_iter);
   sweeps_per_step.push_back(step_sweeps);
   bc_function_of_time();
   Nt_save_solved_data_counter++;
   if (Nt_save_solved_data_counter >= Nt_save_solved_data) {
-    if (apply_saves) write_solved();
+    if (apply_saves) {
+      write_solved();
+      if (ToSolveContinuityEquation) solve_continuity();  // :4635-4643
+    }
     Nt_save_solved_data_counter = 0;
   }
   Nt_save_DragCoefficient_counter++;
-  if (Nt_save_DragCoefficient_counter >= Nt_save_DragCoefficient) Nt_save_DragCoefficient_counter = 0;
+  if (Nt_save_DragCoefficient_counter >= Nt_save_DragCoefficient) {
+    if (apply_saves) write_drag();
+    Nt_save_DragCoefficient_counter = 0;
+  }
   Nt_save_temp_data_counter++;
   if (Nt_save_temp_data_counter >= Nt_save_temp_data) {
     write_temp();
@@ -1994,6 +2155,8 @@ void Oracle::finish() {
                       max_residual_in_v < MaxError_to_stop_program && max_res_p[Iter - 1] < MaxError_to_stop_program &&
                       max_res_T[Iter - 1] < MaxError_to_stop_program;
   write_solved();
+  if (ToSolveContinuityEquation) solve_continuity();
+  write_drag();
   write_temp();
 }
 

@@ -242,9 +242,14 @@ class Case:
 
 
 def read_field(directory: str, name: str, Nx: int, Ny: int) -> np.ndarray:
-    """Read one reference dump (raw native-endian array, WriteReadData.h:107-134)."""
+    """Read one reference dump: raw native-endian array (WriteReadData.h:107-134), or the text
+    form with one value per line (WriteReadData.h:139-173) when no .bin exists."""
     dt = "<u4" if name == "vol_inf_fb" else "<f8"
-    a = np.fromfile(os.path.join(directory, f"{name}.bin"), dtype=dt)
+    path = os.path.join(directory, f"{name}.bin")
+    if os.path.exists(path):
+        a = np.fromfile(path, dtype=dt)
+    else:
+        a = np.loadtxt(os.path.join(directory, f"{name}.txt"), dtype=np.float64).astype(dt)
     if a.size != Nx * Ny:
         raise ValueError(f"{name}.bin holds {a.size} values, expected {Nx * Ny}")
     return a.reshape(Ny, Nx)

@@ -5,7 +5,9 @@ serial build with and without FIXED_NUMBER_OF_ITERATIONS_LOOP_3) and run on case
 directories written by sts_cases.py.  For each case the fixture keeps, after the
 run: the four field dumps u, v, p, Temper (in full for small meshes, as SHA-256 of
 the raw little-endian bytes otherwise), vol_inf_fb, the sweep count of every step
-(Iterations_in_loops.txt) and Tmp.txt.
+(Iterations_in_loops.txt) and Tmp.txt, and the SHA-256 of every file the run writes into the
+case directory (mesh files, drag-coefficient and pressure-control logs, continuity dumps ...)
+except EnteredData.txt, whose rewrite records the wall-clock time.
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -39,6 +41,19 @@ def cases():
     c.restart = sc.channel_initial_state(c, sc.inflow_velocity(0.5))
     out.append(("channel_circle_120x12_resid", c, False))
     out.append(("channel_ma0.1_400x40_resid_5steps", sc.config_case("channel_ma0.1", Nt=5), False))
+    # the diagnostics of the time loop: drag coefficients of every body every 2 steps, the
+    # short-format summary and the continuity residual dumps (binary and text)
+    c = sc.channel_case("c", 80, 8, 0.3, 0.002, 1e-3, 6)
+    c.entered.update(Nt_save_DragCoefficient=2, WriteDataInShortFormat_kind=1, ToSolveContinuityEquation=1)
+    for P in c.polygons:
+        P.drag = 1
+    out.append(("channel_diagnostics_80x8_resid", c, False))
+    c = sc.rayleigh_benard_case("rb", 32, 16, Nt=5)
+    c.entered.update(ToSolveContinuityEquation=1, ToWriteSolvedDataToBinaryFile=0, Nt_save_DragCoefficient=3,
+                     N_I_p_c=3)
+    for P in c.polygons:
+        P.drag = 1
+    out.append(("rayleigh_benard_diagnostics_txt_32x16_fixed", c, True))
     return out
 
 
@@ -56,6 +71,7 @@ def run_one(name, case, fixed, exe, copy_files=()):
         for f in copy_files:
             shutil.copy(f, d)
         import subprocess
+        before = {f: hashlib.sha256(open(os.path.join(d, f), "rb").read()).hexdigest() for f in os.listdir(d)}
         subprocess.run([exe], cwd=d, capture_output=True, check=True)
         e = sc.read_entered_data(os.path.join(d, "EnteredData.txt"))
         Nx, Ny = int(e["Nx"]), int(e["Ny"])
@@ -68,6 +84,9 @@ def run_one(name, case, fixed, exe, copy_files=()):
         lines = open(os.path.join(d, "Iterations_in_loops.txt")).read().split("\n")
         rec["sweeps"] = [int(l.split()[-1]) for l in lines if l.strip() and not l.startswith("it")]
         rec["tmp_txt"] = open(os.path.join(d, "Tmp.txt")).read()
+        after = {f: hashlib.sha256(open(os.path.join(d, f), "rb").read()).hexdigest() for f in os.listdir(d)}
+        rec["files"] = {f: h for f, h in sorted(after.items())
+                        if f != "EnteredData.txt" and before.get(f) != h}  # what the run wrote
         small = Nx * Ny <= 4000
         if small:
             np.savez_compressed(os.path.join(OUT, name + ".npz"), **arrays)
@@ -95,7 +114,7 @@ def main():
                        [os.path.join(SHIPPED, "solve_polyhedrons_b.txt")])
         mine = run_one("shipped_example_5steps", sc.shipped_example(5), True, exes["simple_ts_fixed"])
         for k in orig:
-            if k.startswith("sha256") or k == "sweeps":
+            if k.startswith("sha256") or k in ("sweeps", "files"):
                 assert orig[k] == mine[k], ("restated example differs from the shipped files", k)
         records.append(mine)
         print(mine["name"], mine["Nx"], mine["Ny"], mine["sweeps"])

@@ -11,7 +11,12 @@ from conftest import GOLDEN, golden_case
 
 NAMES = ["channel_ma0.1_80x8_resid", "channel_ma0.1_80x8_fixed", "channel_ma2.43_60x12_resid",
          "rayleigh_benard_32x16_resid", "channel_circle_120x12_resid", "channel_ma0.1_400x40_resid_5steps",
-         "shipped_example_5steps"]
+         "channel_diagnostics_80x8_resid", "rayleigh_benard_diagnostics_txt_32x16_fixed", "shipped_example_5steps"]
+
+
+def file_sha(path):
+    with open(path, "rb") as f:
+        return hashlib.sha256(f.read()).hexdigest()
 
 
 def sha(a):
@@ -38,6 +43,11 @@ def test_oracle_matches_reference_dumps(name, oracle_built, golden_records):
         lines = open(os.path.join(d, "Iterations_in_loops.txt")).read().split("\n")
         sweeps = [int(l.split()[-1]) for l in lines if l.strip() and not l.startswith("it")]
         assert sweeps == rec["sweeps"]
+        # every file the reference wrote (mesh, drag-coefficient, pressure-control and
+        # continuity outputs included), byte for byte
+        for f, h in rec["files"].items():
+            assert os.path.exists(os.path.join(d, f)), f
+            assert file_sha(os.path.join(d, f)) == h, f
 
 
 def test_oracle_library_matches_cli(oracle_built, golden_records):
