@@ -1067,9 +1067,9 @@ __device__ __forceinline__ void boundary_body(const Geo& g, unsigned phases, uns
     __shared__ int ratio_side;  // 0: nothing, 1: inlet columns, 2: outlet columns
     // the inflow column is staged in shared memory by all threads; thread 0 then folds it
     // in the reference's order (the mean is an ordered sum)
-    // (the column maximum and mean only feed correction methods 1 and 2)
+    // (the column maximum and mean feed correction methods 1 and 2 and the pressure-control log)
     __shared__ double col_u[kMaxColumn], col_h[kMaxColumn];
-    const bool need_col = (g.p_corr_method == 1 || g.p_corr_method == 2);
+    const bool need_col = (g.p_corr_method == 1 || g.p_corr_method == 2) || (bits & F_PRESSURE_BC);
     const bool staged = need_col && Ny <= kMaxColumn;
     if (staged) {
       for (int j = tid; j < Ny; j += nt) {
@@ -1301,6 +1301,98 @@ __global__ void k_check_division(unsigned long long n, unsigned long long seed, 
   }
   for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
   if ((threadIdx.x & 31) == 0 && local) atomicAdd(bad, local);
+}
+
+}  // namespace sts
+
+namespace sts {
+
+// ---------------------------------------------------------------------------
+// Diagnostics of the time loop.
+// Drag-coefficient sums of WriteDragCoefficient (SIMPLE_TS_MPI.cpp:8147-8275): thread k adds up
+// list k -- the cells of one flagged body that have a fluid neighbour, in the reference's loop
+// order (i outer, j inner over the p/T solve range) -- sequentially, so the sums are the
+// reference's bit for bit; out[12 k ..] = friction, pressure and area sums of the bottom,
+// front, top and behind faces.  Thread nlist adds the inflow and outflow mass fluxes of the
+// short-format summary (:8471-8491) into out[12 nlist], out[12 nlist + 1].
+// ---------------------------------------------------------------------------
+__global__ void k_drag(Geo g, const int* cells, const int* first, int nlist, double* out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int Nx = g.Nx, Ny = g.Ny;
+  const double* u = g.u;
+  const double* v = g.v;
+  const double* p = g.p[g.ctl->cur];
+  const double* hx = g.hx;
+  const double* hy = g.hy;
+  auto fl = [&](int q) { return cls_fluid(g.cls[q]); };
+  if (k < nlist) {
+    double fb = 0, pb = 0, sb = 0, ff = 0, pf = 0, sf = 0, ft = 0, pt = 0, st = 0, fh = 0, ph = 0, sh = 0;
+    for (int q = first[k]; q < first[k + 1]; q++) {
+      const int node = cells[q], j = node / Nx, i = node - j * Nx;
+      const Nb d = neighbours(i, j, Nx, Ny, false);  // ij_function_i_and_j_to_the_boundaries
+      if (fl(d.ij_1)) {
+        const double h = hy[j - (j < (Ny - 1) ? 1 : 0)];
+        fb += hx[i] * sqrt(g.Tw_v[d.ij]) * ((u[d.ij_1] - u[d.ij]) / h + (u[d.i1j_1] - u[d.i1j]) / h);
+        pb += p[d.ij_1] * hx[i];
+        sb += hx[i];
+      }
+      if (fl(d.i_1j)) {
+        ff += hy[j] * sqrt(g.Tw_u[d.ij]) * ((v[d.i_1j] - v[d.ij]) / hx[d.i_1] + (v[d.i_1j1] - v[d.ij1]) / hx[d.i_1]);
+        pf += p[d.i_1j] * hy[j];
+        sf += hy[j];
+      }
+      if (fl(d.ij1)) {
+        const double h = hy[j + (0 < j ? 1 : 0)];
+        ft += hx[i] * sqrt(g.Tw_v[d.ij1]) * ((u[d.ij1] - u[d.ij]) / h + (u[d.i1j1] - u[d.i1j]) / h);
+        pt += p[d.ij1] * hx[i];
+        st += hx[i];
+      }
+      if (fl(d.i1j)) {
+        fh += hy[j] * sqrt(g.Tw_u[d.i1j]) * ((v[d.i1j] - v[d.ij]) / hx[d.i1] + (v[d.i1j1] - v[d.ij1]) / hx[d.i1]);
+        ph += p[d.i1j] * hy[j];
+        sh += hy[j];
+      }
+    }
+    double* o = out + 12 * k;
+    o[0] = fb; o[1] = pb; o[2] = sb; o[3] = ff; o[4] = pf; o[5] = sf;
+    o[6] = ft; o[7] = pt; o[8] = st; o[9] = fh; o[10] = ph; o[11] = sh;
+  } else if (k == nlist) {
+    double qb = 0, qe = 0;
+    for (int j = 0; j < Ny; j++) {
+      const int n = 0 + j * Nx;
+      if (fl(n)) qb += g.rho[n] * u[n] * hy[j];
+    }
+    for (int j = 0; j < Ny; j++) {
+      const int n = g.Nx_u1 + j * Nx;
+      if (fl(n)) qe += g.rho[n] * u[n] * hy[j];
+    }
+    out[12 * nlist] = qb;
+    out[12 * nlist + 1] = qe;
+  }
+}
+
+// SolveFluxes (SIMPLE_TS_MPI.cpp:10440-10454) alone, as SolveContinuityEquation calls it.
+__global__ void k_fluxes(Geo g) {
+  Cell c = cell(g);
+  if (!c.ok) return;
+  g.Fx[c.ij] = g.hy[c.j] * g.rho_u[c.ij] * g.u[c.ij];
+  g.Fy[c.ij] = g.hx[c.i] * g.rho_v[c.ij] * g.v[c.ij];
+}
+
+// The steady and unsteady continuity residuals of SolveContinuityEquation
+// (SIMPLE_TS_MPI.cpp:10624-10641); cells of the last row and column stay zero.
+__global__ void k_continuity(Geo g, double* st, double* ce) {
+  Cell c = cell(g);
+  if (!c.ok) return;
+  if (c.i >= g.Nx - 1 || c.j >= g.Ny - 1) {
+    st[c.ij] = 0.0;
+    ce[c.ij] = 0.0;
+    return;
+  }
+  const Nb d = neighbours(c.i, c.j, g.Nx, g.Ny, g.bits & F_PERIODIC);
+  const double s = g.Fx[d.i1j] - g.Fx[d.ij] + g.Fy[d.ij1] - g.Fy[d.ij];
+  st[d.ij] = s;
+  ce[d.ij] = (g.rho[d.ij] - g.rho_pr[d.ij]) * g.hx[c.i] * g.hy[c.j] / g.ht + s;
 }
 
 }  // namespace sts

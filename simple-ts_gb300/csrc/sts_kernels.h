@@ -59,6 +59,11 @@ __global__ void kb_step_end(const Geo* gs, unsigned long long h_step, int in_gra
 __global__ void k_pt_loop(Geo g, int ntiles, LoopCtl* lc);
 __global__ void kb_pt_loop(const Geo* gs, const int* tile_case, const int* tile_first, int ncases, int ntiles,
                            LoopCtl* lc);
+// diagnostics of the time loop: drag-coefficient and mass-flux sums, the fluxes alone, the
+// continuity residuals
+__global__ void k_drag(Geo g, const int* cells, const int* first, int nlist, double* out);
+__global__ void k_fluxes(Geo g);
+__global__ void k_continuity(Geo g, double* st, double* ce);
 // self-check of the correctly rounded division by a reciprocal against IEEE division
 __global__ void k_check_division(unsigned long long n, unsigned long long seed, unsigned long long* bad);
 // precision modes 1 and 2

@@ -65,6 +65,14 @@ struct sts_ctx {
   bool in_batch = false;  // stepped by an sts_batch, not by sts_step
   std::chrono::steady_clock::time_point t0;
   bool tmp_fresh = true, iter_fresh = true;
+  // diagnostics (WriteDragCoefficient, SolveContinuityEquation): the cells of every flagged
+  // body with a fluid neighbour in the reference's loop order, the sums, the continuity dumps
+  std::vector<int> drag_bodies;  // body index (0-based id) of each list
+  int* d_drag_cells = nullptr;
+  int* d_drag_first = nullptr;
+  double* d_drag_out = nullptr;
+  double *d_cont_st = nullptr, *d_cont = nullptr;
+  bool cd_fresh = true, pu_fresh = true;
 
   ~sts_ctx() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -161,6 +169,9 @@ struct sts_ctx {
     return STS_OK;
   }
   int build_graph();
+  int write_mesh();
+  int write_drag();
+  int continuity();
   int step_host(int n, int* done);
   int step_graph(int n, int* done);
   int write_outputs();
@@ -379,6 +390,129 @@ std::string num(double x) {
 
 // WriteSolvedDataToFile (SIMPLE_TS_MPI.cpp:5564-5731): the wall-temperature overwrite is a
 // side effect on the state, then the dumps, it_begin.txt and EnteredData.txt.
+// The mesh files written while the mesh is built (SIMPLE_TS_MPI.cpp:2252-2259).
+int sts_ctx::write_mesh() {
+  if (!opt.write_files) return STS_OK;
+  const std::string dir = hc.dir + "/";
+  write_txt(dir + "x_f.txt", hc.x_f.data(), hc.Nx + 1);
+  write_txt(dir + "hx.txt", hc.hx.data(), hc.Nx);
+  write_txt(dir + "x_v.txt", hc.x_v.data(), hc.Nx);
+  write_txt(dir + "y_f.txt", hc.y_f.data(), hc.Ny + 1);
+  write_txt(dir + "hy.txt", hc.hy.data(), hc.Ny);
+  write_txt(dir + "y_v.txt", hc.y_v.data(), hc.Ny);
+  return STS_OK;
+}
+
+// WriteDragCoefficient (SIMPLE_TS_MPI.cpp:8147-8578, serial path): the sums on the device
+// (k_drag), the coefficients and the three logs on the host with the reference's arithmetic
+// and formats: CD.<body>.txt for the flagged bodies, DataInShortFormat.txt, p_and_u_xb_it.txt.
+int sts_ctx::write_drag() {
+  if (!opt.write_files) return STS_OK;
+  const Config& cf = hc.cfg;
+  const int nl = (int)drag_bodies.size();
+  std::vector<double> sums(12 * nl + 2, 0.0);
+  k_drag<<<1, std::max(32, ((nl + 1 + 31) / 32) * 32), 0, s>>>(g, d_drag_cells, d_drag_first, nl, d_drag_out);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(sums.data(), d_drag_out, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost, s));
+  if (int r = read_ctl()) return r;
+  const Ctl& c = *h_ctl;
+  const std::string dir = hc.dir + "/";
+  const bool restart = cf.b("ToReadSolvedDataFromFile");
+  const int TypeND = (int)cf.n("TypeOfNonDimensiolization");
+  const double Re = cf.d("Re"), Ma = cf.d("Ma"), Kn = cf.d("Kn"), gamma1 = cf.d("gamma1"), T_BC_xb = cf.d("T_BC_xb");
+  const double ht = cf.d("ht"), ug = c.u_given_xb_in_it;
+  double CD_fr_x = 0, CD_p_x = 0;
+  const int w = 30;
+  for (int k = 0; k < nl; k++) {
+    const double* q = &sums[12 * k];
+    double c_CD_p = 0, c_CD_fr = 0;
+    if (TypeND == 1) {
+      c_CD_p = 1.0 / (ug * ug * (c.p_BC_xb / T_BC_xb));
+      c_CD_fr = 2.0 / (Re * ug);
+    } else if (TypeND == 2) {
+      c_CD_p = 2.0 / (gamma1 * Ma * Ma * (c.p_BC_xb / T_BC_xb));
+      c_CD_fr = 2.0 / (Re * ug);
+    } else if (TypeND == 3) {
+      c_CD_p = 1.0 / (ug * ug * (c.p_BC_xb / T_BC_xb));
+      c_CD_fr = (5.0 / 8.0) * std::sqrt(M_PI) * Kn / (ug * ug * (c.p_BC_xb / T_BC_xb));
+    }
+    const double fb = c_CD_fr * q[0], pb = c_CD_p * q[1], ff = c_CD_fr * q[3], pf = c_CD_p * q[4];
+    const double ft = c_CD_fr * q[6], pt = c_CD_p * q[7], fh = c_CD_fr * q[9], ph = c_CD_p * q[10];
+    CD_fr_x = (ft / q[8]) + (fb / q[2]);
+    CD_p_x = (pf / q[5]) - (ph / q[11]);
+    const std::string name = dir + "CD." + std::to_string(drag_bodies[k]) + ".txt";
+    std::ofstream o;
+    if (cd_fresh && !restart) o.open(name.c_str());
+    else o.open(name.c_str(), std::ios::out | std::ios::app);
+    if (!restart && cd_fresh) {
+      const char* hdr[16] = {"//it (number of step by time) 00", "ht (step by time) 01", "CD_fr_x (CD from friction) 02",
+                             "CD_p_x (CD from pressure) 03", "S_for_CD_bottom 04", "S_for_CD_front 05",
+                             "S_for_CD_top 06", "S_for_CD_behind 07", "CD_fr_bottom 08", "CD_p_bottom 09",
+                             "CD_fr_front 10", "CD_p_front 11", "CD_fr_top 12", "CD_p_top 13", "CD_fr_behind 14",
+                             "CD_p_behind 15"};
+      for (const char* hh : hdr) o << std::setw(w) << hh;
+      o << std::endl;
+    }
+    o << std::setw(w) << c.it << std::setiosflags(std::ios::scientific) << std::setprecision(10);
+    const double vals[15] = {ht, CD_fr_x, CD_p_x, q[2], q[5], q[8], q[11], fb, pb, ff, pf, ft, pt, fh, ph};
+    for (double x : vals) o << std::setw(w) << x;
+    o << std::endl;
+  }
+  if (nl > 0) cd_fresh = false;
+  if (cf.n("WriteDataInShortFormat_kind") == 1) {
+    std::ofstream o((dir + "DataInShortFormat.txt").c_str());
+    o << std::setiosflags(std::ios::scientific) << std::setprecision(15) << std::setw(w) << Re << std::setw(w) << Kn
+      << std::setw(w) << CD_p_x + CD_fr_x << std::setw(w) << CD_p_x << std::setw(w) << c.u_gas_nd << std::setw(w)
+      << sums[12 * nl] << std::setw(w) << sums[12 * nl + 1] << std::setw(w) << c.p_BC_xb << std::setw(w) << c.p_BC_xe
+      << std::endl;
+  }
+  if (hc.bits & F_PRESSURE_BC) {
+    const std::string name = dir + "p_and_u_xb_it.txt";
+    std::ofstream o;
+    if (pu_fresh && !restart) o.open(name.c_str());
+    else o.open(name.c_str(), std::ios::out | std::ios::app);
+    if (!restart && pu_fresh) {
+      const char* hdr[7] = {"//it (number of step by time)", "ht (step by time)", "p_BC_xb", "u_given_xb_in_it",
+                            "u_given_xb_in_it_max", "u_given_xb_in_it_mean", "p_correction"};
+      for (const char* hh : hdr) o << std::setw(w) << hh;
+      o << std::endl;
+    }
+    o << std::setw(w) << c.it << std::setiosflags(std::ios::scientific) << std::setprecision(15) << std::setw(w) << ht
+      << std::setw(w) << c.p_BC_xb << std::setw(w) << c.u_given_xb_in_it << std::setw(w) << c.u_in_max
+      << std::setw(w) << c.u_in_mean << std::setw(w) << c.p_correction << std::endl;
+    pu_fresh = false;
+  }
+  return STS_OK;
+}
+
+// SolveContinuityEquation (SIMPLE_TS_MPI.cpp:10621-10714, serial path): the fluxes again (as the
+// reference does; this is also what the next step's assembly sees), the residuals, the dumps.
+int sts_ctx::continuity() {
+  k_fluxes<<<grid, block, 0, s>>>(g);
+  k_continuity<<<grid, block, 0, s>>>(g, d_cont_st, d_cont);
+  CU(cudaGetLastError());
+  if (!opt.write_files) return STS_OK;
+  const int Na = hc.Na;
+  std::vector<double> st(Na), ce(Na);
+  CU(cudaMemcpyAsync(st.data(), d_cont_st, sizeof(double) * Na, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(ce.data(), d_cont, sizeof(double) * Na, cudaMemcpyDeviceToHost, s));
+  if (int r = read_ctl()) return r;
+  const std::string dir = hc.dir + "/", its = num(h_ctl->it);
+  const bool bin = hc.cfg.b("ToWriteSolvedDataToBinaryFile"), newf = hc.cfg.b("ToWriteSolvedDataToNewFiles");
+  const std::string ext = bin ? ".bin" : ".txt";
+  auto put = [&](const std::string& f, const std::vector<double>& a) {
+    if (bin) write_bin(f, a.data(), sizeof(double) * Na);
+    else write_txt(f, a.data(), Na);
+  };
+  put(dir + "ContinuityEquation_stationary" + ext, st);
+  put(dir + "ContinuityEquation" + ext, ce);
+  if (newf) {
+    put(dir + "ContinuityEquation_stationary." + its + ext, st);
+    put(dir + "ContinuityEquation." + its + ext, ce);
+  }
+  return STS_OK;
+}
+
 int sts_ctx::write_outputs() {
   boundary(PH_TJUMP | PH_TJUMP_WRITE);
   if (int r = check()) return r;
@@ -732,6 +866,34 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
   c->grid = dim3((h.Nx + 31) / 32, (h.Ny + 7) / 8);
   c->ntiles = (int)(c->grid.x * c->grid.y);
   if (int r = c->alloc(&c->d_lc, 1)) return r;
+  if (int r = c->write_mesh()) return r;
+  {
+    // drag lists: the cells of each flagged body with a fluid neighbour, in WriteDragCoefficient's
+    // loop order (i outer, j inner over the p/T solve range, SIMPLE_TS_MPI.cpp:8203-8206)
+    std::vector<int> cells, first(1, 0);
+    for (int b = 0; b < (int)h.bodies.size(); b++) {
+      if (!h.bodies[b].drag) continue;
+      for (int i = h.Nx_o[0]; i < h.Nx_o[1]; i++)
+        for (int j = h.Ny_o[0]; j < h.Ny_o[1]; j++) {
+          const int node = i + j * h.Nx;
+          if ((int)h.vol_file[node] - 1 != b) continue;
+          const Nb d = neighbours(i, j, h.Nx, h.Ny, false);
+          auto fl = [&](int q) { return cls_fluid(h.cls[q]); };
+          if (fl(d.ij_1) || fl(d.i_1j) || fl(d.ij1) || fl(d.i1j)) cells.push_back(node);
+        }
+      c->drag_bodies.push_back(b);
+      first.push_back((int)cells.size());
+    }
+    if (int r = c->alloc(&c->d_drag_cells, cells.size())) return r;
+    if (int r = c->alloc(&c->d_drag_first, first.size())) return r;
+    if (int r = c->alloc(&c->d_drag_out, 12 * c->drag_bodies.size() + 2)) return r;
+    if (int r = c->upload(c->d_drag_cells, cells)) return r;
+    if (int r = c->upload(c->d_drag_first, first)) return r;
+    if (cf.b("ToSolveContinuityEquation")) {
+      if (int r = c->alloc(&c->d_cont_st, Na)) return r;
+      if (int r = c->alloc(&c->d_cont, Na)) return r;
+    }
+  }
   if (int r = c->size_pt_grid()) return r;
   const dim3 G = c->grid, B = c->block;
   cudaStream_t s = c->s;
@@ -947,17 +1109,33 @@ int sts_run_case(const char* case_dir, const sts_options* opt) {
   const Config& cf = ctx->hc.cfg;
   const long save_every = cf.n("Nt_save_solved_data") > 0 ? cf.n("Nt_save_solved_data") : 1;
   const long log_every = cf.n("Nt_save_temp_data") > 0 ? cf.n("Nt_save_temp_data") : 1;
-  long save_c = 0, log_c = 0;
+  const long drag_every = cf.n("Nt_save_DragCoefficient") > 0 ? cf.n("Nt_save_DragCoefficient") : 1;
+  const bool cont = cf.b("ToSolveContinuityEquation");
+  // the continuity dumps of every step's last outer iteration (SIMPLE_TS_MPI.cpp:4588-4591) only
+  // outlive the step when they go to per-step files
+  const bool cont_each_step = cont && cf.b("ToWriteSolvedDataToNewFiles");
+  long save_c = 0, log_c = 0, drag_c = 0;
   while (!ctx->finished) {
-    const long chunk = std::min(save_every - save_c, log_every - log_c);
+    long chunk = std::min(save_every - save_c, std::min(log_every - log_c, drag_every - drag_c));
+    if (cont_each_step) chunk = 1;
     int done = 0;
     const int r = sts_step(ctx, (int)chunk, &done);
     if (r && r != STS_ERR_NONFINITE) return r;
     save_c += done;
     log_c += done;
+    drag_c += done;
+    // the reference's order after a step: saves (with the continuity dumps), drag, logs
+    if (cont_each_step && done > 0 && save_c < save_every)
+      if (int q = ctx->continuity()) return q;
     if (save_c >= save_every) {
       if (int q = ctx->write_outputs()) return q;
+      if (cont)
+        if (int q = ctx->continuity()) return q;
       save_c = 0;
+    }
+    if (drag_c >= drag_every) {
+      if (int q = ctx->write_drag()) return q;
+      drag_c = 0;
     }
     if (log_c >= log_every) {
       if (int q = ctx->write_logs()) return q;
@@ -969,6 +1147,9 @@ int sts_run_case(const char* case_dir, const sts_options* opt) {
   const double hours = std::chrono::duration<double>(std::chrono::steady_clock::now() - ctx->t0).count() / 3600.0;
   ctx->hc.cfg.set("max_time_for_solve", hours);
   if (int q = ctx->write_outputs()) return q;
+  if (cont)
+    if (int q = ctx->continuity()) return q;
+  if (int q = ctx->write_drag()) return q;
   if (int q = ctx->write_logs(false)) return q;  // the final log writes Tmp.txt only (SIMPLE_TS_MPI.cpp:4714)
   return STS_OK;
 }

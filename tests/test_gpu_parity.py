@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 
 NAMES = ["channel_ma0.1_80x8_resid", "channel_ma0.1_80x8_fixed", "channel_ma2.43_60x12_resid",
          "rayleigh_benard_32x16_resid", "channel_circle_120x12_resid", "channel_ma0.1_400x40_resid_5steps",
-         "shipped_example_5steps"]
+         "channel_diagnostics_80x8_resid", "rayleigh_benard_diagnostics_txt_32x16_fixed", "shipped_example_5steps"]
 
 ALL_FIELDS = ["u", "v", "p", "T", "rho", "sqrt_T", "rho_u", "rho_v", "Fx", "Fy", "D_ux", "D_uy", "D_vx", "D_vy",
               "DTx", "DTy", "Gamma_xf", "Gamma_yf", "ScT1", "apx", "apy", "bpx", "bpy", "u_pseudo", "v_pseudo",
@@ -40,6 +40,11 @@ def test_dropin_run_matches_reference_dumps(name, use_graph, lib_built, golden_r
         lines = open(os.path.join(d, "Iterations_in_loops.txt")).read().split("\n")
         assert [int(l.split()[-1]) for l in lines if l.strip() and not l.startswith("it")] == rec["sweeps"]
         assert open(os.path.join(d, "Tmp.txt")).read() == rec["tmp_txt"]
+        # every file the reference wrote: mesh, drag coefficients, pressure control, continuity
+        for f, h in rec["files"].items():
+            assert os.path.exists(os.path.join(d, f)), f
+            from make_golden import file_digest
+            assert file_digest(os.path.join(d, f)) == h, f
 
 
 @pytest.mark.parametrize("name", ["channel_ma2.43_60x12_resid", "rayleigh_benard_32x16_resid",

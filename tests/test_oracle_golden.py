@@ -15,8 +15,8 @@ NAMES = ["channel_ma0.1_80x8_resid", "channel_ma0.1_80x8_fixed", "channel_ma2.43
 
 
 def file_sha(path):
-    with open(path, "rb") as f:
-        return hashlib.sha256(f.read()).hexdigest()
+    from make_golden import file_digest
+    return file_digest(path)
 
 
 def sha(a):
