@@ -92,6 +92,23 @@ def dist_env():
     return rank, world, local
 
 
+def slowest(x, world, device="cuda"):
+    """The largest x over all ranks: a job's time is that of its slowest rank."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank, world, seconds):
+    """Whole-job throughput: every rank advanced its own replica by units_per_rank in at most
+    `seconds` (weak scaling, no collective on the data path)."""
+    return units_per_rank * world / seconds
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -351,11 +368,8 @@ def main():
     Na = Nx * Ny
     with Clocks(local) as clk:
         done, total_ms, sweeps = timed_steps(s, args.steps, args.warmup, flush, barrier)
-    t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    total_ms = float(t.item())
-    value = Na * done * world / (total_ms / 1e3)
+    total_ms = slowest(total_ms, world)
+    value = job_rate(Na * done, world, total_ms / 1e3)
 
     # e2e through the C ABI with host buffers: per step the state u, v, p, T goes host->device
     # from pinned memory, one step runs, and the new state comes back device->host.
@@ -372,8 +386,8 @@ def main():
         for f, b in pins.items():
             s.get_field_ptr(f, b.data_ptr())
     barrier()
-    e2e_s = time.perf_counter() - t0
-    e2e = {"value": Na * e2e_steps * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 4 * Na * 8,
+    e2e_s = slowest(time.perf_counter() - t0, world)
+    e2e = {"value": job_rate(Na * e2e_steps, world, e2e_s), "unit": UNIT, "h2d_bytes_per_step": 4 * Na * 8,
            "d2h_bytes_per_step": 4 * Na * 8}
 
     # per-kernel device time over a few more real steps (the roofline's dominant kernel)
