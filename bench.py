@@ -45,7 +45,7 @@ BYTES_PER_CELL = {
 # DRAM bytes per launch measured by ncu on this workload, FP64 path (dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch of the second time step, cold cache); None where no
 # capture was taken
-TRAFFIC = {"assemble": 20981504 + 768, "sweep_loop": 18981888 + 27648}
+TRAFFIC = {"assemble": 20980736 + 256, "sweep_loop": 18984192 + 19712}
 
 
 def parse():
