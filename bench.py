@@ -335,6 +335,20 @@ def batch_bench(args):
     print(json.dumps(line), flush=True)
 
 
+def warm_summary(plain_value, plain_sweeps, variants):
+    """The comparison the metric names: the warm-started FP32-correction path against plain GPU
+    Jacobi (the FP64 bit-exact path), both at the same per-step residual tolerance."""
+    warm = {k: v for k, v in variants.items() if v.get("warm_start", 0) and v.get("precision_mode", 0) >= 2}
+    if not warm or not len(plain_sweeps):
+        return None
+    best = max(warm, key=lambda k: warm[k]["value"])
+    ps = float(sum(plain_sweeps) / len(plain_sweeps))
+    return {"plain_gpu_jacobi": {"path": "FP64 bit-exact, cold start", "value": plain_value, "sweeps_per_step": ps},
+            "warm_start": {"path": best, "value": warm[best]["value"], "sweeps_per_step": warm[best]["sweeps_per_step"]},
+            "speedup": warm[best]["value"] / plain_value,
+            "sweep_ratio": ps / max(warm[best]["sweeps_per_step"], 1e-30)}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -444,7 +458,8 @@ def main():
                 "e2e": e2e, "clocks": clk.summary(), "gpu_launches": launches,
                 "sweeps_per_step": {"mean": float(sum(sweeps) / max(len(sweeps), 1)),
                                     "max": int(max(sweeps)) if len(sweeps) else 0},
-                "variants": variants}
+                "variants": variants,
+                "warm_start_vs_plain": warm_summary(value, sweeps, variants)}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
