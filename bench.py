@@ -335,6 +335,37 @@ def batch_bench(args):
     print(json.dumps(line), flush=True)
 
 
+def checkpoint_bench(d, local, barrier, every=10, saves=10):
+    """Milliseconds per FP64 step with the reference's binary dumps (u, v, p, Temper, vol_inf_fb,
+    it_begin.txt, EnteredData.txt) written every `every` steps: not at all, synchronously (the
+    reference's order: stepping waits for the files), and from the checkpoint thread
+    (sts_write_outputs_async; the wait for the last files is inside the timed region)."""
+    import sts
+    ms = {}
+    for mode in ("no_saves", "sync", "async"):
+        s = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=sts.EXACT)
+        s.step(3)
+        if mode != "no_saves":
+            s.write_outputs()  # the first save makes the snapshot buffers and the writer thread
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(saves):
+            s.step(every)
+            if mode == "sync":
+                s.write_outputs()
+            elif mode == "async":
+                s.write_outputs_async()
+        s.wait_outputs()
+        s.sync()
+        ms[mode] = (time.perf_counter() - t0) * 1e3 / (every * saves)
+        s.close()
+    cost_sync, cost_async = ms["sync"] - ms["no_saves"], ms["async"] - ms["no_saves"]
+    Na = s.Nx * s.Ny
+    return {"every_steps": every, "saves": saves, "bytes_per_save": Na * (4 * 8 + 4),
+            "ms_per_step": {k: round(v, 5) for k, v in ms.items()},
+            "save_cost_hidden": round(1.0 - cost_async / cost_sync, 3) if cost_sync > 0 else None}
+
+
 def warm_summary(plain_value, plain_sweeps, variants):
     """The comparison the metric names: the warm-started FP32-correction path against plain GPU
     Jacobi (the FP64 bit-exact path), both at the same per-step residual tolerance."""
@@ -449,6 +480,8 @@ def main():
                 "kernel_ms_per_step": {k: round(x / max(vpn, 1), 5) for k, x in vkms.items() if x > 0}}
             v.close()
 
+    ckpt = checkpoint_bench(d, local, barrier) if args.variants else None
+
     if rank == 0:
         cpu = cpu_baseline(d, args.cpu_seconds, start_steps=0)
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": done,
@@ -459,7 +492,8 @@ def main():
                 "sweeps_per_step": {"mean": float(sum(sweeps) / max(len(sweeps), 1)),
                                     "max": int(max(sweeps)) if len(sweeps) else 0},
                 "variants": variants,
-                "warm_start_vs_plain": warm_summary(value, sweeps, variants)}
+                "warm_start_vs_plain": warm_summary(value, sweeps, variants),
+                "checkpoint": ckpt}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

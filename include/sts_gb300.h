@@ -64,10 +64,15 @@ typedef struct sts_options {
    * The sweeps still iterate to the same tolerance, so the result moves only within it; the
    * sweep count falls.  Meaningful for tolerance-terminated loops (fixed_sweeps = 0). */
   int warm_start;
+  /* 1: sts_run_case's periodic dumps (WriteSolvedDataToFile, SIMPLE_TS_MPI.cpp:4625-4646) are
+   *    written from a host thread while the next steps run (see sts_write_outputs_async);
+   *    the run still returns only after every file is complete (default);
+   * 0: each save is on disk before stepping resumes, as in the reference. */
+  int async_save;
 } sts_options;
 
 /* Fills *opt with the defaults (fixed_sweeps 1, use_graph 1, device 0, write_files 1, precision 0,
- * warm_start 0). */
+ * warm_start 0, async_save 1). */
 void sts_default_options(sts_options* opt);
 
 /* Reads a case directory (EnteredData.txt, solve_*_b.txt, restart dumps when
@@ -114,6 +119,19 @@ int sts_sweep_history(sts_ctx* ctx, unsigned int* out, int cap, int* n_out);
  * Temper.bin vol_inf_fb.bin it_begin.txt into the case directory (WriteSolvedDataToFile,
  * SIMPLE_TS_MPI.cpp:5564-5731). */
 int sts_write_outputs(sts_ctx* ctx);
+
+/* sts_write_outputs without waiting for the files: the wall-temperature overwrite and a
+ * device-to-device snapshot of u, v, p, T are queued on the context's stream, a second stream
+ * copies the snapshot to pinned host memory and a host thread writes the files, while the
+ * caller goes on stepping.  The files hold the state of the call, not of later steps.  Two
+ * snapshots can be pending; a third call waits for the older one.  Memory, made at the first
+ * save: 64 bytes per cell on the device and 64 pinned on the host.  Saves are written in call
+ * order.  The files are complete after sts_wait_outputs, sts_write_outputs or sts_destroy.
+ * Asynchronous counterpart of WriteSolvedDataToFile (SIMPLE_TS_MPI.cpp:5564-5731). */
+int sts_write_outputs_async(sts_ctx* ctx);
+
+/* Waits until every save of the context is on disk; returns the first error among them. */
+int sts_wait_outputs(sts_ctx* ctx);
 
 /* Whole drop-in run of a case directory: open, step until the run ends, with the
  * periodic saves and logs of the reference (Tmp.txt, Iterations_in_loops.txt), and the

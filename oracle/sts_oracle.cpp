@@ -1292,8 +1292,16 @@ void Oracle::write_solved() {
       if (ToWriteSolvedDataToNewFiles) write_txt(path(std::string(names[k]) + "." + its.str() + ".txt"), src[k], Na);
     }
   }
-  if (ToWriteSolvedDataToBinaryFile) write_bin(path("vol_inf_fb.bin"), vol_inf_fb.data(), sizeof(uint) * Na);
-  else write_txt_u(path("vol_inf_fb.txt"), vol_inf_fb.data(), Na);
+  // the per-save copy of vol_inf_fb is named vol_inf_fb.<it>.bin, but vol_inf_fb.txt.<it>.txt in
+  // text mode (SIMPLE_TS_MPI.cpp:5614, :5668)
+  if (ToWriteSolvedDataToBinaryFile) {
+    write_bin(path("vol_inf_fb.bin"), vol_inf_fb.data(), sizeof(uint) * Na);
+    if (ToWriteSolvedDataToNewFiles)
+      write_bin(path("vol_inf_fb." + its.str() + ".bin"), vol_inf_fb.data(), sizeof(uint) * Na);
+  } else {
+    write_txt_u(path("vol_inf_fb.txt"), vol_inf_fb.data(), Na);
+    if (ToWriteSolvedDataToNewFiles) write_txt_u(path("vol_inf_fb.txt." + its.str() + ".txt"), vol_inf_fb.data(), Na);
+  }
   std::ofstream o(path("it_begin.txt").c_str());
   o << it << std::endl;
 }

@@ -22,6 +22,7 @@ UNITS = [
     ("sts_fast.cu", []),
     ("sts_runtime.cu", []),
     ("sts_host.cpp", []),
+    ("sts_checkpoint.cpp", []),
 ]
 
 LIB = os.path.join(BUILD, "libsts_gb300.so")
@@ -60,7 +61,7 @@ def build(force=False, verbose=False):
         if p.wait() != 0:
             raise RuntimeError(f"compiling {src} failed")
     if force or _stale(LIB, objs):
-        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcuda"]
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcuda", "-lpthread"]
         subprocess.check_call(cmd)
     main = os.path.join(CSRC, "sts_main.cpp")
     if force or _stale(EXE, [main, LIB]):

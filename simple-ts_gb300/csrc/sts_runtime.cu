@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "sts_checkpoint.h"
 #include "sts_common.cuh"
 #include "sts_host.h"
 #include "sts_kernels.h"
@@ -73,8 +74,11 @@ struct sts_ctx {
   double* d_drag_out = nullptr;
   double *d_cont_st = nullptr, *d_cont = nullptr;
   bool cd_fresh = true, pu_fresh = true;
+  // checkpoint dumps (made at the first save)
+  std::unique_ptr<Checkpointer> saver;
 
   ~sts_ctx() {
+    saver.reset();  // writes out pending saves before the buffers and the stream go
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     for (void* p : allocs) cudaFree(p);
@@ -174,7 +178,8 @@ struct sts_ctx {
   int continuity();
   int step_host(int n, int* done);
   int step_graph(int n, int* done);
-  int write_outputs();
+  int write_outputs(bool wait_files);
+  int wait_outputs();
   int write_logs(bool iterations = true);
   int profile(int n, double* ms, int* cnt, int* done);
 };
@@ -365,31 +370,6 @@ int sts_ctx::profile(int n, double* ms, int* cnt, int* done) {
   return STS_OK;
 }
 
-namespace {
-
-void write_bin(const std::string& f, const void* a, size_t bytes) {
-  FILE* fp = std::fopen(f.c_str(), "wb");
-  if (!fp) return;
-  std::fwrite(a, 1, bytes, fp);
-  std::fclose(fp);
-}
-
-template <class T>
-void write_txt(const std::string& f, const T* a, int n) {
-  std::ofstream o(f.c_str());
-  for (int k = 0; k < n; k++) o << std::setiosflags(std::ios::scientific) << std::setprecision(15) << a[k] << "\n";
-}
-
-std::string num(double x) {
-  std::ostringstream o;
-  o << x;
-  return o.str();
-}
-
-}  // namespace
-
-// WriteSolvedDataToFile (SIMPLE_TS_MPI.cpp:5564-5731): the wall-temperature overwrite is a
-// side effect on the state, then the dumps, it_begin.txt and EnteredData.txt.
 // The mesh files written while the mesh is built (SIMPLE_TS_MPI.cpp:2252-2259).
 int sts_ctx::write_mesh() {
   if (!opt.write_files) return STS_OK;
@@ -513,39 +493,37 @@ int sts_ctx::continuity() {
   return STS_OK;
 }
 
-int sts_ctx::write_outputs() {
+// WriteSolvedDataToFile (SIMPLE_TS_MPI.cpp:5564-5731): the wall-temperature overwrite is a
+// side effect on the state; then a snapshot of u, v, p, T is taken on the stream and its dumps,
+// it_begin.txt and EnteredData.txt are written by the checkpoint thread.  wait_files: return
+// only once they are on disk.
+int sts_ctx::write_outputs(bool wait_files) {
   boundary(PH_TJUMP | PH_TJUMP_WRITE);
   if (int r = check()) return r;
   if (!opt.write_files) return STS_OK;
-  const int Na = hc.Na;
-  std::vector<double> buf(Na);
   if (int r = read_ctl()) return r;
+  if (!saver) saver.reset(new Checkpointer(opt.device, (size_t)hc.Na));
   const unsigned cur = h_ctl->cur;
   const double* src[4] = {g.u, g.v, g.p[cur], g.T[cur]};
-  const char* names[4] = {"u", "v", "p", "Temper"};
-  const bool bin = hc.cfg.b("ToWriteSolvedDataToBinaryFile");
-  const bool newf = hc.cfg.b("ToWriteSolvedDataToNewFiles");
-  const std::string its = num(h_ctl->it);
-  for (int k = 0; k < 4; k++) {
-    CU(cudaMemcpy(buf.data(), src[k], sizeof(double) * Na, cudaMemcpyDeviceToHost));
-    const std::string base = hc.dir + "/" + names[k];
-    if (bin) {
-      write_bin(base + ".bin", buf.data(), sizeof(double) * Na);
-      if (newf) write_bin(base + "." + its + ".bin", buf.data(), sizeof(double) * Na);
-    } else {
-      write_txt(base + ".txt", buf.data(), Na);
-      if (newf) write_txt(base + "." + its + ".txt", buf.data(), Na);
-    }
-  }
-  if (bin) {
-    write_bin(hc.dir + "/vol_inf_fb.bin", hc.vol_file.data(), sizeof(uint32_t) * Na);
-    if (newf) write_bin(hc.dir + "/vol_inf_fb." + its + ".bin", hc.vol_file.data(), sizeof(uint32_t) * Na);
-  } else {
-    write_txt(hc.dir + "/vol_inf_fb.txt", hc.vol_file.data(), Na);
-  }
-  std::ofstream itf((hc.dir + "/it_begin.txt").c_str());
-  itf << h_ctl->it << std::endl;
-  write_config(hc.dir + "/EnteredData.txt", hc.cfg);
+  DumpSpec d;
+  d.dir = hc.dir;
+  d.it = h_ctl->it;
+  d.bin = hc.cfg.b("ToWriteSolvedDataToBinaryFile");
+  d.newf = hc.cfg.b("ToWriteSolvedDataToNewFiles");
+  d.cfg = hc.cfg;
+  d.vol = hc.vol_file.data();
+  std::string err;
+  if (int r = saver->save(s, src, std::move(d), err)) return fail(r, err);
+  if (wait_files)
+    if (int r = saver->wait(err)) return fail(r, err);
+  return STS_OK;
+}
+
+// Every checkpoint taken so far is on disk.
+int sts_ctx::wait_outputs() {
+  std::string err;
+  if (saver)
+    if (int r = saver->wait(err)) return fail(r, err);
   return STS_OK;
 }
 
@@ -905,7 +883,7 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
     c->boundary(PH_VEL);
     k_step_begin<<<G, B, 0, s>>>(g, 0, 0, 0);
     k_face_rho<<<G, B, 0, s>>>(g);
-    if (int r = c->write_outputs()) return r;  // the set-up save (SIMPLE_TS_MPI.cpp:2863)
+    if (int r = c->write_outputs(!opt.async_save)) return r;  // the set-up save (SIMPLE_TS_MPI.cpp:2863)
   }
   for (double* f : {g.d12, g.d34, g.apx, g.apy, g.bpx, g.bpy, g.Gamma_yf, g.Gamma_xf, g.Fx, g.Fy, g.u_pseudo,
                     g.v_pseudo, g.D_ux, g.D_uy, g.D_vx, g.D_vy, g.DTx, g.DTy, g.ScT1, g.rho_u, g.rho_v})
@@ -940,6 +918,7 @@ void sts_default_options(sts_options* opt) {
   opt->write_files = 1;
   opt->precision = 0;
   opt->warm_start = 0;
+  opt->async_save = 1;
 }
 
 int sts_open_case(const char* case_dir, const sts_options* opt, sts_ctx** out) {
@@ -1093,9 +1072,26 @@ int sts_write_outputs(sts_ctx* ctx) {
   CU(cudaSetDevice(ctx->opt.device));
   const int w = ctx->opt.write_files;
   ctx->opt.write_files = 1;
-  const int r = ctx->write_outputs();
+  const int r = ctx->write_outputs(true);
   ctx->opt.write_files = w;
   return r;
+}
+
+int sts_write_outputs_async(sts_ctx* ctx) {
+  if (!ctx) return fail(STS_ERR_ARG, "null context");
+  if (ctx->in_batch) return fail(STS_ERR_ARG, "the case belongs to a batch");
+  CU(cudaSetDevice(ctx->opt.device));
+  const int w = ctx->opt.write_files;
+  ctx->opt.write_files = 1;
+  const int r = ctx->write_outputs(false);
+  ctx->opt.write_files = w;
+  return r;
+}
+
+int sts_wait_outputs(sts_ctx* ctx) {
+  if (!ctx) return fail(STS_ERR_ARG, "null context");
+  CU(cudaSetDevice(ctx->opt.device));
+  return ctx->wait_outputs();
 }
 
 int sts_run_case(const char* case_dir, const sts_options* opt) {
@@ -1128,7 +1124,7 @@ int sts_run_case(const char* case_dir, const sts_options* opt) {
     if (cont_each_step && done > 0 && save_c < save_every)
       if (int q = ctx->continuity()) return q;
     if (save_c >= save_every) {
-      if (int q = ctx->write_outputs()) return q;
+      if (int q = ctx->write_outputs(!o.async_save)) return q;
       if (cont)
         if (int q = ctx->continuity()) return q;
       save_c = 0;
@@ -1146,7 +1142,7 @@ int sts_run_case(const char* case_dir, const sts_options* opt) {
   // after the loop (SIMPLE_TS_MPI.cpp:4695-4714)
   const double hours = std::chrono::duration<double>(std::chrono::steady_clock::now() - ctx->t0).count() / 3600.0;
   ctx->hc.cfg.set("max_time_for_solve", hours);
-  if (int q = ctx->write_outputs()) return q;
+  if (int q = ctx->write_outputs(true)) return q;  // also waits for the periodic saves
   if (cont)
     if (int q = ctx->continuity()) return q;
   if (int q = ctx->write_drag()) return q;

@@ -28,7 +28,8 @@ EXPORTS = [
     "sts_stats", "sts_sweep_history", "sts_write_outputs", "sts_run_case", "sts_sync", "sts_destroy",
     "sts_last_error", "sts_inspect_case", "sts_step_timed", "sts_profile_steps", "sts_pt_sweeps",
     "sts_pt_sweeps_noalloc", "sts_check_division", "sts_open_batch", "sts_batch_step", "sts_batch_step_timed",
-    "sts_batch_case", "sts_batch_destroy", "sts_check_double_float",
+    "sts_batch_case", "sts_batch_destroy", "sts_check_double_float", "sts_write_outputs_async",
+    "sts_wait_outputs",
 ]
 
 KERNELS = ["step_begin", "assemble", "sweep_loop", "correct", "face_rho", "boundary", "flux_diff", "step_end"]
@@ -43,7 +44,7 @@ FIELDS = ["u", "v", "p", "T", "rho", "sqrt_T", "rho_u", "rho_v", "Fx", "Fy", "D_
 
 class Options(C.Structure):
     _fields_ = [("fixed_sweeps", C.c_int), ("use_graph", C.c_int), ("device", C.c_int), ("write_files", C.c_int),
-                ("precision", C.c_int), ("warm_start", C.c_int)]
+                ("precision", C.c_int), ("warm_start", C.c_int), ("async_save", C.c_int)]
 
 
 class StsError(RuntimeError):
@@ -76,6 +77,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.sts_stats.argtypes = [P, dp]
     lib.sts_sweep_history.argtypes = [P, C.POINTER(C.c_uint), C.c_int, C.POINTER(C.c_int)]
     lib.sts_write_outputs.argtypes = [P]
+    lib.sts_write_outputs_async.argtypes = [P]
+    lib.sts_wait_outputs.argtypes = [P]
     lib.sts_run_case.argtypes = [C.c_char_p, C.POINTER(Options)]
     lib.sts_sync.argtypes = [P]
     lib.sts_destroy.argtypes = [P]
@@ -94,7 +97,7 @@ def _check(code: int):
 
 
 def options(fixed_sweeps=True, use_graph=True, device=0, write_files=False, precision=EXACT,
-            warm_start=0) -> Options:
+            warm_start=0, async_save=True) -> Options:
     o = Options()
     load().sts_default_options(C.byref(o))
     o.fixed_sweeps = int(fixed_sweeps)
@@ -103,6 +106,7 @@ def options(fixed_sweeps=True, use_graph=True, device=0, write_files=False, prec
     o.write_files = int(write_files)
     o.precision = int(precision)
     o.warm_start = int(warm_start)
+    o.async_save = int(async_save)
     return o
 
 
@@ -179,7 +183,16 @@ class Solver:
         return out[: n.value]
 
     def write_outputs(self):
+        """The reference's dumps of the current state, on disk when this returns."""
         _check(load().sts_write_outputs(self._h))
+
+    def write_outputs_async(self):
+        """The same dumps, written from a host thread while later steps run; complete after
+        wait_outputs(), write_outputs() or close()."""
+        _check(load().sts_write_outputs_async(self._h))
+
+    def wait_outputs(self):
+        _check(load().sts_wait_outputs(self._h))
 
     def sync(self):
         _check(load().sts_sync(self._h))
@@ -203,9 +216,10 @@ class Solver:
             pass
 
 
-def run_case(case_dir: str, fixed_sweeps=True, use_graph=True, device=0, write_files=True, precision=EXACT):
+def run_case(case_dir: str, fixed_sweeps=True, use_graph=True, device=0, write_files=True, precision=EXACT,
+             async_save=True):
     """The drop-in run: same effect as the reference binary in case_dir."""
-    opt = options(fixed_sweeps, use_graph, device, write_files, precision)
+    opt = options(fixed_sweeps, use_graph, device, write_files, precision, async_save=async_save)
     _check(load().sts_run_case(case_dir.encode(), C.byref(opt)))
 
 

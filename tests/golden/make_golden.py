@@ -54,6 +54,16 @@ def cases():
     for P in c.polygons:
         P.drag = 1
     out.append(("rayleigh_benard_diagnostics_txt_32x16_fixed", c, True))
+    # periodic saves that each keep their own copy (ToWriteSolvedDataToNewFiles): every dump of
+    # every save is a file of its own, named by the time of the save; binary with the continuity
+    # dumps of every step, and text
+    c = sc.channel_case("c", 80, 8, 0.3, 0.002, 1e-3, 8)
+    c.entered.update(Nt_save_solved_data=2, ToWriteSolvedDataToNewFiles=1, ToSolveContinuityEquation=1)
+    out.append(("channel_newfiles_80x8_resid", c, False))
+    c = sc.rayleigh_benard_case("rb", 32, 16, Nt=4)
+    c.entered.update(Nt_save_solved_data=1, ToWriteSolvedDataToNewFiles=1, ToWriteSolvedDataToBinaryFile=0,
+                     N_I_p_c=3)
+    out.append(("rayleigh_benard_newfiles_txt_32x16_fixed", c, True))
     return out
 
 

@@ -11,7 +11,8 @@ from conftest import GOLDEN, golden_case
 
 NAMES = ["channel_ma0.1_80x8_resid", "channel_ma0.1_80x8_fixed", "channel_ma2.43_60x12_resid",
          "rayleigh_benard_32x16_resid", "channel_circle_120x12_resid", "channel_ma0.1_400x40_resid_5steps",
-         "channel_diagnostics_80x8_resid", "rayleigh_benard_diagnostics_txt_32x16_fixed", "shipped_example_5steps"]
+         "channel_diagnostics_80x8_resid", "rayleigh_benard_diagnostics_txt_32x16_fixed", "channel_newfiles_80x8_resid",
+         "rayleigh_benard_newfiles_txt_32x16_fixed", "shipped_example_5steps"]
 
 
 def file_sha(path):
