@@ -56,10 +56,15 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--warm-lead", type=int, default=40,
+                    help="untimed steps before the timed ones for warm-started variants (the learned "
+                         "predictors fit on the run's own history, which fills in the first 10 steps)")
     ap.add_argument("--no-variants", dest="variants", action="store_false",
                     help="skip the FP64-fast and FP32-correction runs of the same workload")
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2, 3],
                     help="precision mode of the --profile-target run")
+    ap.add_argument("--warm-start", type=int, default=0, choices=[0, 1, 2, 3, 4],
+                    help="warm start of the --profile-target run")
     ap.add_argument("--profile-target", type=int, default=0,
                     help="only run this many steps kernel by kernel (a small target for ncu), then exit")
     return ap.parse_args()
@@ -72,13 +77,13 @@ def profile_target(args):
     stsbuild.build()
     if args.workload == "batch64":
         dirs = batch_dirs()
-        b = sts.Batch(dirs, fixed_sweeps=False, precision=args.precision, use_graph=False)
+        b = sts.Batch(dirs, fixed_sweeps=False, precision=args.precision, use_graph=False, warm_start=args.warm_start)
         b.step(args.profile_target)
         print(f"profile target: batch64, {args.profile_target} steps, {sum(c.Nx * c.Ny for c in b.cases)} cells")
         b.close()
         return
     _, d = make_case(args.workload)
-    s = sts.Solver(d, fixed_sweeps=False, use_graph=False, precision=args.precision)
+    s = sts.Solver(d, fixed_sweeps=False, use_graph=False, precision=args.precision, warm_start=args.warm_start)
     s.step(args.profile_target)
     s.sync()
     print(f"profile target: {args.workload}, {args.profile_target} steps, sweeps {list(s.sweep_history())}")
@@ -299,10 +304,13 @@ def batch_bench(args):
     for name, prec, warm in (("fp64_exact", sts.EXACT, 0), ("fp64_fast", sts.FAST_FP64, 0),
                              ("fp32_corrections", sts.MIXED, 0), ("fp32_corrections_warm2", sts.MIXED, 2),
                              ("fp32_corrections_df", sts.MIXED_DF, 0), ("fp32_corrections_df_warm2", sts.MIXED_DF, 2),
-                             ("fp32_corrections_learned", sts.MIXED, 3)):
+                             ("fp32_corrections_learned", sts.MIXED, 3), ("fp32_corrections_conv", sts.MIXED, 4),
+                             ("fp32_corrections_df_conv", sts.MIXED_DF, 4)):
         b = sts.Batch(dirs, fixed_sweeps=False, precision=prec, warm_start=warm)
         cells = sum(c.Nx * c.Ny for c in b.cases)
-        for _ in range(max(args.warmup, 3)):
+        w = max(args.warmup, 3)
+        lead = max(args.warm_lead, w) if warm else w
+        for _ in range(lead):
             b.step(1)
         total, done = 0.0, 0
         with Clocks(0) as clk:
@@ -316,10 +324,17 @@ def batch_bench(args):
         sweeps = np.concatenate([c.sweep_history()[-done:] for c in b.cases])
         r = {"value": cells * done / (total / 1e3), "ms_per_step": total / max(done, 1),
              "sweeps_per_step": float(np.mean(sweeps)), "clocks": clk.summary()}
+        r["untimed_steps"] = lead
         if base is None:
-            base = fields
+            base = {w: fields}
+            # the bit-exact fields at the step count of the warm-started variants
+            for _ in range(max(args.warm_lead, w) - w):
+                b.step(1)
+            base[max(args.warm_lead, w)] = {f: np.concatenate([c.field(f).ravel() for c in b.cases])
+                                             for f in ("u", "v", "p", "T", "rho")}
         else:
-            r["rel_l2_vs_fp64"] = {f: float(np.linalg.norm(fields[f] - base[f]) / np.linalg.norm(base[f]))
+            ref = base[lead]
+            r["rel_l2_vs_fp64"] = {f: float(np.linalg.norm(fields[f] - ref[f]) / np.linalg.norm(ref[f]))
                                    for f in fields}
         out[name] = r
         b.close()
@@ -458,20 +473,26 @@ def main():
     variants = {}
     if args.variants:
         ref = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=sts.EXACT)
-        nref = max(args.warmup, 3) + args.steps
-        ref.step(nref)
-        base = {f: ref.field(f) for f in ("u", "v", "p", "T", "rho")}
+        w = max(args.warmup, 3)
+        ref.step(w + args.steps)
+        base = {w: {f: ref.field(f) for f in ("u", "v", "p", "T", "rho")}}
+        lead_w = max(args.warm_lead, w)
+        ref.step(lead_w - w)
+        base[lead_w] = {f: ref.field(f) for f in ("u", "v", "p", "T", "rho")}
         ref.close()
         for name, prec, warm in (("fp64_fast", sts.FAST_FP64, 0), ("fp32_corrections", sts.MIXED, 0),
                                  ("fp32_corrections_df", sts.MIXED_DF, 0), ("fp32_corrections_df_warm2", sts.MIXED_DF, 2),
                                  ("fp64_exact_warm2", sts.EXACT, 2), ("fp32_corrections_warm2", sts.MIXED, 2),
-                                 ("fp32_corrections_learned", sts.MIXED, 3)):
+                                 ("fp32_corrections_learned", sts.MIXED, 3), ("fp64_exact_conv", sts.EXACT, 4),
+                                 ("fp32_corrections_conv", sts.MIXED, 4), ("fp32_corrections_df_conv", sts.MIXED_DF, 4)):
             v = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=prec, warm_start=warm)
-            vd, vms, vsw = timed_steps(v, args.steps, args.warmup, flush, barrier)
-            err = {f: float(np.linalg.norm(v.field(f) - base[f]) / np.linalg.norm(base[f])) for f in base}
+            lead = lead_w if warm else w
+            vd, vms, vsw = timed_steps(v, args.steps, lead, flush, barrier)
+            ref_f = base[lead]
+            err = {f: float(np.linalg.norm(v.field(f) - ref_f[f]) / np.linalg.norm(ref_f[f])) for f in ref_f}
             vpn, vkms, vkcnt = v.profile(max(3, min(args.steps, 10)))
             variants[name] = {
-                "precision_mode": prec, "warm_start": warm, "value": Na * vd * world / (vms / 1e3),
+                "precision_mode": prec, "warm_start": warm, "untimed_steps": lead, "value": Na * vd * world / (vms / 1e3),
                 "ms_per_step": vms / max(vd, 1),
                 "speedup_vs_fp64": (Na * vd / (vms / 1e3)) / (Na * done / (total_ms / 1e3)) if done else None,
                 "rel_l2_vs_fp64": err,

@@ -60,7 +60,12 @@ typedef struct sts_options {
    * 2: quadratic extrapolation, 3 (p_n - p_{n-1}) + p_{n-2} (linear on the second step);
    * 3: a linear predictor learned from the run itself: p_n + sum_k w_k (p_{n-k} - p_{n-k-1}),
    *    k = 0..2, with w refitted every step by least squares on the last 6 steps (separately
-   *    for p and T; quadratic extrapolation until the history is long enough).
+   *    for p and T; quadratic extrapolation until the history is long enough);
+   * 4: a 3x3 convolutional predictor learned from the run itself: where the solution moves (cells
+   *    within 3 cells of one whose last change exceeds 0.1 of the largest), the step's change is a
+   *    linear function of 36 features of the cell's neighbourhood in the last four changes,
+   *    refitted every step by least squares on the last 6 steps; elsewhere mode 2.  Tracks fronts
+   *    that move across cells, which extrapolation in time cannot.
    * The sweeps still iterate to the same tolerance, so the result moves only within it; the
    * sweep count falls.  Meaningful for tolerance-terminated loops (fixed_sweeps = 0). */
   int warm_start;

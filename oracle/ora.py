@@ -38,6 +38,7 @@ def load():
         lib.ora_sweeps.argtypes = [P, C.POINTER(C.c_uint), C.c_int]
         lib.ora_stats.argtypes = [P, C.POINTER(C.c_double)]
         lib.ora_set_warm_start.argtypes = [P, C.c_int]
+        lib.ora_set_guess.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib = lib
     return _lib
 
@@ -56,6 +57,14 @@ class Oracle:
 
     def step(self, n=1):
         return load().ora_step(self._h, int(n))
+
+    def set_guess(self, p, T):
+        """The next step's p-T sweeps start from these fields (Nx*Ny each) on the solved cells."""
+        pa = np.ascontiguousarray(p, dtype=np.float64).ravel()
+        ta = np.ascontiguousarray(T, dtype=np.float64).ravel()
+        assert pa.size == ta.size == self.Nx * self.Ny
+        self._keep = (pa, ta)
+        load().ora_set_guess(self._h, pa.ctypes.data_as(C.POINTER(C.c_double)), ta.ctypes.data_as(C.POINTER(C.c_double)))
 
     def field(self, name):
         n = self.Nx if name in ("hx", "x_v") else self.Ny if name in ("hy", "y_v") else self.Nx * self.Ny

@@ -194,6 +194,19 @@ struct Oracle {
   static constexpr int kRing = 9, kWin = 6;
   std::vector<std::vector<double>> Dp, DT;  // ring of differences on the solved cells
   void warm_ar();
+  // an initial iterate supplied from outside for the next step only (predictor studies, and
+  // replaying a guess the GPU library computed): replaces p and T on the solved cells after the
+  // step's previous-value copies, where the warm start acts
+  std::vector<double> guess_p, guess_T;
+  // mode 4: the convolutional predictor (see warm_conv)
+  static constexpr int kCFeat = 36, kCTerms = 36 * 37 / 2 + 36, kCWin = 6, kCRing = 5;
+  std::vector<float> cD[2][kCRing];
+  std::vector<unsigned char> cact[2], csolved;
+  std::vector<double> cgram;
+  float conv_w[2][kCFeat] = {};
+  bool conv_ok[2] = {false, false};
+  void warm_conv();
+  void conv_features(int f, unsigned t, int i, int j, float* out) const;
   bool check_wallclock = false;  // honour max_time_for_solve (CLI only)
   bool apply_saves = false;      // periodic WriteSolvedDataToFile inside step() (CLI only)
   bool finished = false;
@@ -1876,6 +1889,267 @@ void Oracle::warm_ar() {
   warm_ready++;
 }
 
+// Mode 4 (no counterpart in the reference): the 36 features of cell (i, j) for the step whose
+// newest difference has index t: for each of the time-basis fields D_t, D_t - D_{t-1} and the
+// second and third differences (FP32, from the stored FP32 differences), the 3x3 neighbourhood
+// (clamped at the mesh edge) resolved into value, gradient and curvature along x, each of those
+// into value, gradient and curvature along y.
+void Oracle::conv_features(int f, unsigned t, int i, int j, float* out) const {
+  float S[4][3][3];
+  for (int dj = -1; dj <= 1; dj++) {
+    const int jj = std::min(std::max(j + dj, 0), (int)Ny - 1);
+    for (int di = -1; di <= 1; di++) {
+      const int ii = std::min(std::max(i + di, 0), (int)Nx - 1);
+      const size_t n = (size_t)ii + (size_t)jj * Nx;
+      const float d0 = cD[f][t % kCRing][n], d1 = cD[f][(t - 1) % kCRing][n];
+      const float d2 = cD[f][(t - 2) % kCRing][n], d3 = cD[f][(t - 3) % kCRing][n];
+      const float e1 = d0 - d1, e1b = d1 - d2, e1c = d2 - d3;
+      const float e2 = e1 - e1b, e2b = e1b - e1c;
+      S[0][dj + 1][di + 1] = d0;
+      S[1][dj + 1][di + 1] = e1;
+      S[2][dj + 1][di + 1] = e2;
+      S[3][dj + 1][di + 1] = e2 - e2b;
+    }
+  }
+  for (int k = 0; k < 4; k++) {
+    float row[3][3];
+    for (int r = 0; r < 3; r++) {
+      const float w = S[k][r][0], c = S[k][r][1], e = S[k][r][2];
+      row[r][0] = c;
+      row[r][1] = 0.5f * (e - w);
+      row[r][2] = (e + w) - 2.0f * c;
+    }
+    for (int q = 0; q < 3; q++) {
+      const float lo = row[0][q], c = row[1][q], hi = row[2][q];
+      out[k * 9 + q * 3 + 0] = c;
+      out[k * 9 + q * 3 + 1] = 0.5f * (hi - lo);
+      out[k * 9 + q * 3 + 2] = (hi + lo) - 2.0f * c;
+    }
+  }
+}
+
+static inline unsigned f32_bits(float x) {
+  unsigned u;
+  std::memcpy(&u, &x, 4);
+  return u;
+}
+static inline float bits_f32(unsigned u) {
+  float x;
+  std::memcpy(&x, &u, 4);
+  return x;
+}
+
+// Mode 4: the GB300 library's convolutional warm start, restated sequentially.  Per field, the
+// step differences D_t = x_t - x_{t-1} are kept in FP32; the step starts from quadratic
+// extrapolation (mode 2) except on the active cells -- within a diamond of radius 3 of a cell with
+// |D_h| > 0.1 max |D_h| (x wrapped on periodic meshes) -- where it starts from x_h + w . features.
+// The weights solve least squares over the last 6 training pairs (features of step t-1 on the
+// cells active at t-1, target D_t): normal-equation terms summed in FP32 per strip of 32x2 cells
+// (rows in cell order), with compensated FP32 sums over the non-empty strips of each segment of 64
+// strips and over the non-empty segments, in FP64 over the 6 window slots in slot order; ridge
+// 1e-11 of the mean diagonal; FP32 Gauss-Jordan elimination without pivoting.  Every operation has the
+// library's order, so the initial iterates agree bit for bit.
+void Oracle::warm_conv() {
+  const unsigned r = (unsigned)warm_ready;
+  if (csolved.empty()) {
+    csolved.assign(Na, 0);
+    for (const std::vector<uint>* list : {&nch_o, &bc_o})
+      for (uint n : *list) csolved[n] = 1;
+    for (int f = 0; f < 2; f++)
+      for (int k = 0; k < kCRing; k++) cD[f][k].assign(Na, 0.f);
+    cact[0].assign(Na, 0);
+    cact[1].assign(Na, 0);
+    cgram.assign((size_t)kCWin * 2 * kCTerms, 0.0);
+    p_m1.assign(Na, 0.0); p_m2.assign(Na, 0.0);
+    T_m1.assign(Na, 0.0); T_m2.assign(Na, 0.0);
+  }
+  unsigned mx[2] = {0u, 0u};
+  for (uint n = 0; n < Na; n++) {
+    if (csolved[n]) {
+      const double x = p[n], y = Temper[n];
+      if (r == 0) {
+        p_m1[n] = x; p_m2[n] = x;
+        T_m1[n] = y; T_m2[n] = y;
+      } else {
+        const double dx = x - p_m1[n], dy = y - T_m1[n];
+        const float fx = (float)dx, fy = (float)dy;
+        cD[0][(r - 1) % kCRing][n] = fx;
+        cD[1][(r - 1) % kCRing][n] = fy;
+        mx[0] = std::max(mx[0], f32_bits(std::fabs(fx)));
+        mx[1] = std::max(mx[1], f32_bits(std::fabs(fy)));
+        if (r >= 2) {
+          p[n] = 3.0 * dx + p_m2[n];
+          Temper[n] = 3.0 * dy + T_m2[n];
+        } else {
+          p[n] = x + dx;
+          Temper[n] = y + dy;
+        }
+        p_m2[n] = p_m1[n]; p_m1[n] = x;
+        T_m2[n] = T_m1[n]; T_m1[n] = y;
+      }
+    } else if (r >= 1) {
+      cD[0][(r - 1) % kCRing][n] = 0.f;
+      cD[1][(r - 1) % kCRing][n] = 0.f;
+    }
+  }
+  warm_ready = (int)r + 1;
+  if (r == 0) return;
+  const unsigned h = r - 1;
+  // active cells of the newest difference
+  const float thr[2] = {0.1f * bits_f32(mx[0]), 0.1f * bits_f32(mx[1])};
+  for (int j = 0; j < (int)Ny; j++)
+    for (int i = 0; i < (int)Nx; i++) {
+      const size_t n = (size_t)i + (size_t)j * Nx;
+      unsigned char bits = 0;
+      if (csolved[n])
+        for (int dj = -3; dj <= 3; dj++) {
+          const int jj = j + dj;
+          if (jj < 0 || jj >= (int)Ny) continue;
+          const int rx = 3 - std::abs(dj);
+          for (int di = -rx; di <= rx; di++) {
+            int ii = i + di;
+            if (Periodic) ii = (ii + (int)Nx) % (int)Nx;
+            else if (ii < 0 || ii >= (int)Nx) continue;
+            const size_t q = (size_t)ii + (size_t)jj * Nx;
+            if (std::fabs(cD[0][h % kCRing][q]) > thr[0]) bits |= 1;
+            if (std::fabs(cD[1][h % kCRing][q]) > thr[1]) bits |= 2;
+          }
+        }
+      cact[h & 1][n] = bits;
+    }
+  // the newest training pair
+  if (h >= 4) {
+    const int nsx = ((int)Nx + 31) / 32, nsy = ((int)Ny + 1) / 2, nstrips = nsx * nsy;
+    std::vector<float> F(64 * (kCFeat + 1)), part(kCTerms);
+    // per strip and field: row count and FP32 terms
+    std::vector<int> nrows(2 * nstrips, 0);
+    std::vector<float> parts((size_t)nstrips * 2 * kCTerms, 0.f);
+    for (int sy = 0; sy < nsy; sy++)
+      for (int sx = 0; sx < nsx; sx++)
+        for (int f = 0; f < 2; f++) {
+          int rows = 0;
+          for (int j = 2 * sy; j < 2 * sy + 2 && j < (int)Ny; j++)
+            for (int i = 32 * sx; i < 32 * sx + 32 && i < (int)Nx; i++) {
+              const size_t n = (size_t)i + (size_t)j * Nx;
+              if (!((cact[(h - 1) & 1][n] >> f) & 1)) continue;
+              conv_features(f, h - 1, i, j, &F[rows * (kCFeat + 1)]);
+              F[rows * (kCFeat + 1) + kCFeat] = cD[f][h % kCRing][n];
+              rows++;
+            }
+          if (!rows) continue;
+          int e = 0;
+          for (int a = 0; a < kCFeat; a++)
+            for (int b = a; b < kCFeat; b++, e++) {
+              float t = 0.f;
+              for (int q = 0; q < rows; q++) t = t + F[q * (kCFeat + 1) + a] * F[q * (kCFeat + 1) + b];
+              part[e] = t;
+            }
+          for (int a = 0; a < kCFeat; a++, e++) {
+            float t = 0.f;
+            for (int q = 0; q < rows; q++) t = t + F[q * (kCFeat + 1) + a] * F[q * (kCFeat + 1) + kCFeat];
+            part[e] = t;
+          }
+          const int strip = sx + sy * nsx;
+          nrows[f * nstrips + strip] = rows;
+          std::copy(part.begin(), part.end(), parts.begin() + ((size_t)strip * 2 + f) * kCTerms);
+        }
+    // compensated FP32 sums (Neumaier) over the non-empty strips of each segment of 64 strips, then
+    // over the non-empty segments, in index order
+    auto neumaier = [](float& sm, float& cm, float x) {
+      const float t = sm + x;
+      if (std::fabs(sm) >= std::fabs(x)) cm = cm + ((sm - t) + x);
+      else cm = cm + ((x - t) + sm);
+      sm = t;
+    };
+    const int nseg = (nstrips + 63) / 64;
+    const unsigned pair = h - 4;
+    for (int f = 0; f < 2; f++) {
+      std::vector<float> seg((size_t)nseg * kCTerms);
+      std::vector<int> seg_rows(nseg, 0);
+      for (int g = 0; g < nseg; g++) {
+        const int s0 = g * 64, ns = std::min(64, nstrips - s0);
+        for (int q = 0; q < ns; q++) seg_rows[g] += nrows[f * nstrips + s0 + q];
+        for (int e = 0; e < kCTerms; e++) {
+          float sm = 0.f, cm = 0.f;
+          for (int q = 0; q < ns; q++)
+            if (nrows[f * nstrips + s0 + q] > 0) neumaier(sm, cm, parts[((size_t)(s0 + q) * 2 + f) * kCTerms + e]);
+          seg[(size_t)g * kCTerms + e] = sm + cm;
+        }
+      }
+      for (int e = 0; e < kCTerms; e++) {
+        float sm = 0.f, cm = 0.f;
+        for (int g = 0; g < nseg; g++)
+          if (seg_rows[g] > 0) neumaier(sm, cm, seg[(size_t)g * kCTerms + e]);
+        cgram[((size_t)(pair % kCWin) * 2 + f) * kCTerms + e] = (double)(sm + cm);
+      }
+    }
+    for (int f = 0; f < 2; f++) {
+      conv_ok[f] = false;
+      if (pair + 1 < (unsigned)kCWin) continue;
+      std::vector<double> G(kCTerms);
+      for (int q = 0; q < kCTerms; q++) {
+        double v = 0.0;
+        for (int w = 0; w < kCWin; w++) v = v + cgram[((size_t)w * 2 + f) * kCTerms + q];
+        G[q] = v;
+      }
+      double tr = 0.0;
+      for (int a = 0, e = 0; a < kCFeat; a++) {
+        tr = tr + G[e];
+        e += kCFeat - a;
+      }
+      const double lam = 1e-11 * tr / (double)kCFeat;
+      // Gauss-Jordan elimination without pivoting on [matrix | right-hand side]
+      float M[kCFeat][kCFeat + 1], y[kCFeat];
+      int e = 0;
+      for (int a = 0; a < kCFeat; a++)
+        for (int b = a; b < kCFeat; b++, e++) {
+          if (a == b) M[a][a] = (float)(G[e] + lam);
+          else M[a][b] = M[b][a] = (float)G[e];
+        }
+      for (int a = 0; a < kCFeat; a++, e++) M[a][kCFeat] = (float)G[e];
+      bool ok = true;
+      for (int k = 0; k < kCFeat && ok; k++) {
+        const float piv = M[k][k];
+        if (!(piv > 0.f && piv < 3.0e38f)) {
+          ok = false;
+          break;
+        }
+        const float rp = 1.0f / piv;
+        float u[kCFeat + 1];
+        for (int j = k + 1; j <= kCFeat; j++) u[j] = M[k][j] * rp;
+        for (int i = 0; i < kCFeat; i++) {
+          if (i == k) continue;
+          for (int j = k + 1; j <= kCFeat; j++) M[i][j] = M[i][j] - M[i][k] * u[j];
+        }
+        for (int j = k + 1; j <= kCFeat; j++) M[k][j] = u[j];
+      }
+      if (!ok) continue;
+      for (int k = 0; k < kCFeat; k++) y[k] = M[k][kCFeat];
+      bool finite = true;
+      for (int k = 0; k < kCFeat; k++) finite = finite && std::isfinite(y[k]);
+      for (int k = 0; k < kCFeat; k++) conv_w[f][k] = y[k];
+      conv_ok[f] = finite;
+    }
+  } else {
+    conv_ok[0] = conv_ok[1] = false;
+  }
+  // the stencil's start on the active cells
+  for (int j = 0; j < (int)Ny; j++)
+    for (int i = 0; i < (int)Nx; i++) {
+      const size_t n = (size_t)i + (size_t)j * Nx;
+      const unsigned char bits = cact[h & 1][n];
+      for (int f = 0; f < 2; f++) {
+        if (!((bits >> f) & 1) || !conv_ok[f]) continue;
+        float feat[kCFeat];
+        conv_features(f, h, i, j, feat);
+        float corr = 0.f;
+        for (int k = 0; k < kCFeat; k++) corr = corr + conv_w[f][k] * feat[k];
+        if (f == 0) p[n] = p_m1[n] + (double)corr;
+        else Temper[n] = T_m1[n] + (double)corr;
+      }
+    }
+}
+
 // one pass of the time loop body, SIMPLE_TS_MPI.cpp:3230-4691
 void Oracle::step() {
   std::memcpy(p_pr, p, Na * sizeof(double));
@@ -1886,8 +2160,18 @@ void Oracle::step() {
   for (uint c = 0; c < Iter; c++) {
     max_res_p[c] = 0; max_res_T[c] = 0; max_res_p0[c] = 0; max_res_T0[c] = 0; max_Iter_p_c[c] = 0;
   }
-  if (warm_start == 3) {
+  if (!guess_p.empty()) {
+    for (const std::vector<uint>* list : {&nch_o, &bc_o})
+      for (uint n : *list) {
+        p[n] = guess_p[n];
+        Temper[n] = guess_T[n];
+      }
+    guess_p.clear();
+    guess_T.clear();
+  } else if (warm_start == 3) {
     warm_ar();
+  } else if (warm_start == 4) {
+    warm_conv();
   } else if (warm_start) {
     if (!warm_ready) {
       p_m1.assign(p, p + Na);
@@ -2196,6 +2480,12 @@ ora_handle* ora_open(const char* dir, int fixed_sweeps, int write_files) {
 // Runs up to n time steps; stops early when the reference's continue rule says so.
 // Returns the number of steps taken.
 void ora_set_warm_start(ora_handle* h, int mode) { h->o.warm_start = mode; }
+
+// The next step's sweeps start from p_guess, T_guess (Nx*Ny each) on the solved cells.
+void ora_set_guess(ora_handle* h, const double* p_guess, const double* T_guess) {
+  h->o.guess_p.assign(p_guess, p_guess + h->o.Na);
+  h->o.guess_T.assign(T_guess, T_guess + h->o.Na);
+}
 
 int ora_step(ora_handle* h, int n) {
   int k = 0;

@@ -20,6 +20,7 @@ UNITS = [
     # (source, extra flags)
     ("sts_exact.cu", ["--fmad=false"]),
     ("sts_fast.cu", []),
+    ("sts_learn.cu", ["--fmad=false"]),
     ("sts_runtime.cu", []),
     ("sts_host.cpp", []),
     ("sts_checkpoint.cpp", []),

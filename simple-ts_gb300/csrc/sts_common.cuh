@@ -108,10 +108,23 @@ struct Ctl {
   // right-hand sides, for p and for T) over the last kWarmWin steps, and the fitted weights
   double warm_acc[6][2][9];
   double warm_w[2][3];
+  // mode 4: max |D| of the newest step difference per field (float bit patterns, by step
+  // parity), the fitted stencil weights and whether this step's fit succeeded, per field
+  unsigned int conv_max[2][2];
+  float conv_w[2][36];
+  unsigned int conv_ok[2];
+  unsigned int conv_ticket[6];  // segment-sum CTAs done, per (field, block of 256 terms)
 };
 
 // Learned warm start: differences kept, and steps of the least-squares window.
 constexpr int kWarmRing = 4, kWarmWin = 6;
+
+// Convolutional warm start (mode 4): features per cell (4 time-difference orders x 9 spatial
+// basis values of the 3x3 neighbourhood), normal-equation terms per field (upper triangle of the
+// 36x36 Gram matrix, then the 36 right-hand sides), steps in the least-squares window, ring of
+// stored step differences, and the strips of 32x2 cells whose partial sums are kept apart.
+constexpr int kConvFeat = 36, kConvTerms = kConvFeat * (kConvFeat + 1) / 2 + kConvFeat, kConvWin = 6,
+              kConvRing = 5, kConvStripX = 32, kConvStripY = 2, kConvSeg = 64;
 
 // Most cases one batch may hold (the sweep loop keeps their state in shared memory).
 constexpr int kMaxBatchCases = 256;
@@ -163,13 +176,26 @@ struct Geo {
   float *ep[2], *eT[2];
   int precision;  // 0 bit-exact FP64, 1 FP64 with reciprocal/FMA arithmetic, 2 = 1 + FP32 correction sweeps
   // warm start of the sweeps: 0 none (the reference), 1 linear and 2 quadratic extrapolation in
-  // time of p and T on the solved cells, 3 the fitted linear predictor; p_m[k], T_m[k] hold the
-  // values of k+1 steps back
+  // time of p and T on the solved cells, 3 the fitted linear predictor, 4 the fitted 3x3 stencil
+  // predictor on the cells where the solution moves; p_m[k], T_m[k] hold the values of k+1
+  // steps back
   int warm_start;
   double *p_m[2], *T_m[2];
   // mode 3: ring of the last kWarmRing step differences of p and T, per-CTA partial sums
   double *Dp[4], *DT[4];
   float* warm_part;
+  // mode 4: ring of step differences per field (FP32), active-cell flags by step parity (bit 0 p,
+  // bit 1 T), per-strip FP32 partial sums [strip][field][term] and row counts [field][strip] of
+  // the newest training pair, their sums over segments of kConvSeg strips [segment][field][term]
+  // and row counts [field x 3 term blocks][segment], FP64 sums of the last kConvWin pairs
+  // [slot][field][term]
+  float* cD[2][kConvRing];
+  uint8_t* cact[2];
+  float* cpart;
+  int* cnrows;
+  float* cseg;
+  int* cseg_rows;
+  double* cgram;
 };
 
 // Neighbour indices of one cell: ij_function / ij_function_PeriodicBC (SIMPLE_TS_MPI.cpp:140-232).

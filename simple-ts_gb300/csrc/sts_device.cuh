@@ -39,6 +39,54 @@ __device__ __forceinline__ double div_cr(double a, double b, double y) {
   return __fma_rn(r, y, q);
 }
 
+// Convolutional warm start (warm_start 4), at the start of a step on a solved cell n holding
+// x = p_n, y = T_n: the newest step differences D (FP32, ring slot r-1) and the quadratic start
+// of warm_start 2; m receives |D| as float bit patterns for the per-field maximum.
+__device__ __forceinline__ void conv_step_begin_cell(const Geo& g, int n, unsigned cur, unsigned r, unsigned m[2]) {
+  const double x = g.p[cur][n], y = g.T[cur][n];
+  if (r == 0) {
+    g.p_m[0][n] = x; g.p_m[1][n] = x;
+    g.T_m[0][n] = y; g.T_m[1][n] = y;
+    return;
+  }
+  const double dx = x - g.p_m[0][n], dy = y - g.T_m[0][n];
+  const float fx = (float)dx, fy = (float)dy;
+  g.cD[0][(r - 1) % kConvRing][n] = fx;
+  g.cD[1][(r - 1) % kConvRing][n] = fy;
+  m[0] = __float_as_uint(fabsf(fx));
+  m[1] = __float_as_uint(fabsf(fy));
+  if (r >= 2) {
+    g.p[cur][n] = 3.0 * dx + g.p_m[1][n];
+    g.T[cur][n] = 3.0 * dy + g.T_m[1][n];
+  } else {
+    g.p[cur][n] = x + dx;
+    g.T[cur][n] = y + dy;
+  }
+  g.p_m[1][n] = g.p_m[0][n]; g.p_m[0][n] = x;
+  g.T_m[1][n] = g.T_m[0][n]; g.T_m[0][n] = y;
+}
+
+// Per-field maximum of |D| over the block, folded into the step's slot (non-negative floats
+// order like their bit patterns; NaN lands above every number); the other parity's slot, the next
+// step's, is cleared by the first block.  Every thread of the block calls this.
+__device__ __forceinline__ void conv_block_max(const Geo& g, unsigned r, const unsigned m[2]) {
+  if (r == 0) return;
+  __shared__ unsigned wm[2][32];
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int nw = (blockDim.x * blockDim.y + 31) >> 5;
+  for (int f = 0; f < 2; f++) {
+    const unsigned v = __reduce_max_sync(0xffffffffu, m[f]);
+    if (lane == 0) wm[f][warp] = v;
+  }
+  __syncthreads();
+  if (tid < 2) {
+    unsigned v = 0;
+    for (int w = 0; w < nw; w++) v = max(v, wm[tid][w]);
+    if (v) atomicMax(&g.ctl->conv_max[(r - 1) & 1][tid], v);
+    if (blockIdx.x == 0 && blockIdx.y == 0) g.ctl->conv_max[r & 1][tid] = 0u;
+  }
+}
+
 constexpr int kMaxColumn = 1024;  // rows staged in shared memory by the inflow-column reductions
 
 // Running maximum that ignores NaN exactly like "if (m < fabs(r)) m = fabs(r)".

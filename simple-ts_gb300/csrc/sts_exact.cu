@@ -27,6 +27,9 @@ __device__ __forceinline__ void k_step_begin_body(const Geo& g, int counters, un
   Cell c = cell(g);
   Ctl* ctl = g.ctl;
   const unsigned cur = ctl->cur;
+  // warm_start 4: the newest step differences and their maxima (the model's kernels follow)
+  const unsigned conv_r = ctl->warm_ready;
+  unsigned conv_m[2] = {0u, 0u};
   if (c.ok) {
     g.u_pr[c.ij] = g.u[c.ij];
     g.v_pr[c.ij] = g.v[c.ij];
@@ -54,7 +57,16 @@ __device__ __forceinline__ void k_step_begin_body(const Geo& g, int counters, un
         g.T_m[1][n] = g.T_m[0][n]; g.T_m[0][n] = y;
       }
     }
+    if (counters && g.warm_start == 4) {
+      if (cls_o(g.cls[c.ij])) {
+        conv_step_begin_cell(g, c.ij, cur, conv_r, conv_m);
+      } else if (conv_r >= 1) {
+        g.cD[0][(conv_r - 1) % kConvRing][c.ij] = 0.f;
+        g.cD[1][(conv_r - 1) % kConvRing][c.ij] = 0.f;
+      }
+    }
   }
+  if (counters && g.warm_start == 4) conv_block_max(g, conv_r, conv_m);
   if (counters && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
     if (in_graph) cudaGraphSetConditional((cudaGraphConditionalHandle)h_outer, 1);
     for (unsigned k = 0; k < ctl->Iter && k < 64; k++) {
@@ -1246,7 +1258,7 @@ __device__ __forceinline__ void step_end_body(const Geo& g, unsigned long long h
     }
   }
   if (tid == 0) {
-    if (g.warm_start == 1 || g.warm_start == 2) ctl->warm_ready++;
+    if (g.warm_start == 1 || g.warm_start == 2 || g.warm_start == 4) ctl->warm_ready++;
     ctl->hist_sweeps[ctl->hist_n % 4096u] = ctl->step_sweeps;
     ctl->hist_n++;
     if (ctl->steps_left > 0) ctl->steps_left--;

@@ -129,15 +129,32 @@ struct sts_ctx {
     flux_kernel()<<<grid, block, 0, s>>>(g, PH_TEMP | PH_PRES);
     mark(6);
   }
-  // the learned warm start's kernels after the start of a step (mode 3)
+  // strips of the convolutional warm start's normal-equation kernel
+  dim3 strip_grid() const {
+    return dim3((unsigned)((g.Nx + kConvStripX - 1) / kConvStripX), (unsigned)((g.Ny + kConvStripY - 1) / kConvStripY));
+  }
+  // its segment sums: one CTA per (segment of kConvSeg strips, field x 3 blocks of 256 terms)
+  dim3 seg_grid() const {
+    const dim3 sg = strip_grid();
+    return dim3((sg.x * sg.y + kConvSeg - 1) / kConvSeg, 6);
+  }
+  // the learned warm starts' kernels after the start of a step (modes 3 and 4)
   template <class M>
   void warm_launches(M mark) {
-    if (g.warm_start != 3) return;
-    mark(-1);
-    k_warm_diff<<<grid, block, 0, s>>>(g);
-    k_warm_fit<<<1, 576, 0, s>>>(g);
-    k_warm_apply<<<grid, block, 0, s>>>(g);
-    mark(0);
+    if (g.warm_start == 3) {
+      mark(-1);
+      k_warm_diff<<<grid, block, 0, s>>>(g);
+      k_warm_fit<<<1, 576, 0, s>>>(g);
+      k_warm_apply<<<grid, block, 0, s>>>(g);
+      mark(0);
+    } else if (g.warm_start == 4) {
+      mark(-1);
+      k_conv_gram<<<strip_grid(), dim3(kConvStripX, kConvStripY), 0, s>>>(g);
+      k_conv_reduce<<<seg_grid(), 256, 0, s>>>(g);
+      k_conv_solve<<<2, 256, 0, s>>>(g);
+      k_conv_apply<<<grid, block, 0, s>>>(g);
+      mark(0);
+    }
   }
   bool fast() const { return g.precision >= 1; }
   bool mixed() const { return g.precision >= 2 && !(hc.bits & F_FIXED_SWEEPS); }
@@ -250,7 +267,17 @@ int sts_ctx::build_graph() {
   if (int r = add_kernel(&n_asm, b_outer, {}, asm_kernel(), asm_grid(), block, g,
                          (unsigned long long)0, 0))
     return r;
-  if (int r = add_kernel(&n_sw, b_outer, {n_asm}, pt_kernel(), pt_grid, dim3(32, 8), g, ntiles, d_lc)) return r;
+  // warm_start 4: the predictor's kernels (first outer iteration only) beside the assembly
+  std::vector<cudaGraphNode_t> before_sweeps{n_asm};
+  if (g.warm_start == 4) {
+    cudaGraphNode_t w[4];
+    if (int r = add_kernel(&w[0], b_outer, {}, k_conv_gram, strip_grid(), dim3(kConvStripX, kConvStripY), g)) return r;
+    if (int r = add_kernel(&w[1], b_outer, {w[0]}, k_conv_reduce, seg_grid(), dim3(256), g)) return r;
+    if (int r = add_kernel(&w[2], b_outer, {w[1]}, k_conv_solve, dim3(2), dim3(256), g)) return r;
+    if (int r = add_kernel(&w[3], b_outer, {w[2]}, k_conv_apply, grid, block, g)) return r;
+    before_sweeps.push_back(w[3]);
+  }
+  if (int r = add_kernel(&n_sw, b_outer, before_sweeps, pt_kernel(), pt_grid, dim3(32, 8), g, ntiles, d_lc)) return r;
   {
     cudaLaunchAttributeValue v{};
     v.cooperative = 1;
@@ -667,7 +694,7 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
   c->t0 = std::chrono::steady_clock::now();
   std::string err;
   if (opt.precision < 0 || opt.precision > 3) return fail(STS_ERR_ARG, "precision must be 0, 1, 2 or 3");
-  if (opt.warm_start < 0 || opt.warm_start > 3) return fail(STS_ERR_ARG, "warm_start must be 0, 1, 2 or 3");
+  if (opt.warm_start < 0 || opt.warm_start > 4) return fail(STS_ERR_ARG, "warm_start must be 0, 1, 2, 3 or 4");
   if (!load_case(dir, opt.fixed_sweeps != 0, c->hc, err)) return fail(STS_ERR_INPUT, err);
   Case& h = c->hc;
   int ndev = 0;
@@ -808,6 +835,20 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
     }
     const size_t nb = (size_t)((h.Nx + 31) / 32) * ((h.Ny + 7) / 8);
     if (int r = c->alloc(&g.warm_part, nb * 18)) return r;  // 2 fields x 9 normal-equation terms
+  }
+  if (g.warm_start == 4) {
+    for (int f = 0; f < 2; f++)
+      for (int k = 0; k < kConvRing; k++)
+        if (int r = c->alloc(&g.cD[f][k], Na)) return r;
+    for (int k = 0; k < 2; k++)
+      if (int r = c->alloc(&g.cact[k], Na)) return r;
+    const size_t ns = (size_t)((h.Nx + kConvStripX - 1) / kConvStripX) * ((h.Ny + kConvStripY - 1) / kConvStripY);
+    if (int r = c->alloc(&g.cpart, ns * 2 * kConvTerms)) return r;
+    if (int r = c->alloc(&g.cnrows, ns * 2)) return r;
+    const size_t nseg = (ns + kConvSeg - 1) / kConvSeg;
+    if (int r = c->alloc(&g.cseg, nseg * 2 * kConvTerms)) return r;
+    if (int r = c->alloc(&g.cseg_rows, nseg * 6)) return r;
+    if (int r = c->alloc(&g.cgram, (size_t)kConvWin * 2 * kConvTerms)) return r;
   }
   if (g.precision >= 2) {
     float** f32[] = {&g.c32[0], &g.c32[1], &g.c32[2], &g.c32[3], &g.c32[4], &g.a32[0], &g.a32[1], &g.a32[2], &g.a32[3],
@@ -1318,7 +1359,8 @@ struct sts_batch {
   int build_graph();
   int step_host(int n);
   bool use_graph = true;
-  bool warm3 = false;
+  bool warm3 = false, warm4 = false;
+  dim3 strip_grid, seg_grid;  // strips and strip segments of the largest case, one grid layer per case
   unsigned* d_flag = nullptr;
   unsigned* h_flag = nullptr;
 };
@@ -1334,6 +1376,11 @@ int sts_batch::step_host(int n) {
       kb_warm_diff<<<cell_grid, blk, 0, s>>>(G);
       kb_warm_fit<<<dim3(1, 1, ncases), 576, 0, s>>>(G);
       kb_warm_apply<<<cell_grid, blk, 0, s>>>(G);
+    } else if (warm4) {
+      kb_conv_gram<<<strip_grid, dim3(kConvStripX, kConvStripY), 0, s>>>(G);
+      kb_conv_reduce<<<seg_grid, 256, 0, s>>>(G);
+      kb_conv_solve<<<dim3(2, 1, ncases), 256, 0, s>>>(G);
+      kb_conv_apply<<<cell_grid, blk, 0, s>>>(G);
     }
     if (precision == 3) kb_assemble_df<<<dim3(cell_grid.x, cell_grid.y, 3 * ncases), blk, 0, s>>>(G, 0ull, 0);
     else if (fast()) kb_assemble_fast<<<cell_grid, blk, 0, s>>>(G, 0ull, 0);
@@ -1371,18 +1418,28 @@ int sts_batch::build_graph() {
   const Geo* G = d_geos;
   cudaGraphNode_t n[11];
   if (int r = add_kernel(&n[0], b, {}, kb_step_begin, cell_grid, blk, G)) return r;
+  cudaGraphNode_t conv_last = nullptr;
   if (warm3) {
     cudaGraphNode_t w[3];
     if (int r = add_kernel(&w[0], b, {n[0]}, kb_warm_diff, cell_grid, blk, G)) return r;
     if (int r = add_kernel(&w[1], b, {w[0]}, kb_warm_fit, dim3(1, 1, ncases), dim3(576), G)) return r;
     if (int r = add_kernel(&w[2], b, {w[1]}, kb_warm_apply, cell_grid, blk, G)) return r;
     n[0] = w[2];
+  } else if (warm4) {
+    cudaGraphNode_t w[4];  // hang off the step start, not the assembly
+    if (int r = add_kernel(&w[0], b, {n[0]}, kb_conv_gram, strip_grid, dim3(kConvStripX, kConvStripY), G)) return r;
+    if (int r = add_kernel(&w[1], b, {w[0]}, kb_conv_reduce, seg_grid, dim3(256), G)) return r;
+    if (int r = add_kernel(&w[2], b, {w[1]}, kb_conv_solve, dim3(2, 1, ncases), dim3(256), G)) return r;
+    if (int r = add_kernel(&w[3], b, {w[2]}, kb_conv_apply, cell_grid, blk, G)) return r;
+    conv_last = w[3];  // beside the assembly; the sweep loop waits for both
   }
   if (int r = add_kernel(&n[1], b, {n[0]}, precision == 3 ? kb_assemble_df : (fast() ? kb_assemble_fast : kb_assemble),
                          precision == 3 ? dim3(cell_grid.x, cell_grid.y, 3 * ncases) : cell_grid, blk, G,
                          (unsigned long long)0, 0))
     return r;
-  if (int r = add_kernel(&n[2], b, {n[1]}, pt_kernel(), pt_grid, blk, G, (const int*)d_tile_case,
+  std::vector<cudaGraphNode_t> before_sweeps{n[1]};
+  if (conv_last) before_sweeps.push_back(conv_last);
+  if (int r = add_kernel(&n[2], b, before_sweeps, pt_kernel(), pt_grid, blk, G, (const int*)d_tile_case,
                          (const int*)d_tile_first, ncases, ntiles, d_lc))
     return r;
   {
@@ -1442,7 +1499,7 @@ int sts_open_batch(const char* const* case_dirs, int ncases, const sts_options* 
   b->ncases = ncases;
   std::vector<Geo> geos;
   std::vector<int> tile_case, tile_first;
-  unsigned gx = 1, gy = 1, wx = 1, tx = 1;
+  unsigned gx = 1, gy = 1, wx = 1, tx = 1, sx = 1, sy = 1, sgx = 1;
   for (int k = 0; k < ncases; k++) {
     sts_ctx* c = b->cases[k];
     geos.push_back(c->g);
@@ -1452,9 +1509,15 @@ int sts_open_batch(const char* const* case_dirs, int ncases, const sts_options* 
     gy = std::max(gy, c->grid.y);
     wx = std::max(wx, c->walls_grid().x);
     tx = std::max(tx, c->tjump_grid().x);
+    sx = std::max(sx, c->strip_grid().x);
+    sy = std::max(sy, c->strip_grid().y);
+    sgx = std::max(sgx, c->seg_grid().x);
   }
   b->ntiles = (int)tile_case.size();
   b->warm3 = opt.warm_start == 3;
+  b->warm4 = opt.warm_start == 4;
+  b->strip_grid = dim3(sx, sy, (unsigned)ncases);
+  b->seg_grid = dim3(sgx, 6, (unsigned)ncases);
   if (int r = b->alloc(&b->d_geos, ncases)) return r;
   if (int r = b->alloc(&b->d_tile_case, tile_case.size())) return r;
   if (int r = b->alloc(&b->d_tile_first, tile_first.size())) return r;

@@ -132,3 +132,76 @@ def test_batch_learned_warm_start_equals_single(lib_built):
                 np.testing.assert_array_equal(b.cases[k].field(f), s.field(f), err_msg=f"case {k} {f}")
             s.close()
         b.close()
+
+
+@pytest.mark.parametrize("which,scale,steps", [("channel_ma2.43", 0.25, 30), ("rayleigh_benard", 0.125, 30),
+                                               ("channel_ma0.1", 0.5, 30)])
+def test_conv_warm_start_matches_oracle(which, scale, steps, lib_built, oracle_built):
+    """Mode 4 (the convolutional predictor fitted every step) against the oracle's restatement:
+    the FP32 features, strip sums, window sums, Cholesky solve and prediction run in the same
+    order on both, so every field and every sweep count agree bit for bit, in graph and launch
+    modes, from the steps where the fit is still filling its window to those where it acts."""
+    import ora
+    import sts
+    case = sc.config_case(which, scale=scale, Nt=steps)
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        o = ora.Oracle(d, fixed_sweeps=False, warm_start=4)
+        assert o.step(steps) == steps
+        for use_graph in (True, False):
+            g = sts.Solver(d, fixed_sweeps=False, use_graph=use_graph, warm_start=4)
+            assert g.step(steps) == steps
+            for f in FIELDS:
+                np.testing.assert_array_equal(g.field(f), o.field(f), err_msg=f"{f} graph={use_graph}")
+            np.testing.assert_array_equal(g.sweep_history(), o.sweeps())
+            g.close()
+
+
+def test_conv_warm_start_gain(lib_built, oracle_built):
+    """What the fitted stencil adds: on the supersonic channel (a front that moves a fraction of
+    a cell per step), once its window has seen the front move, it takes fewer sweeps than
+    quadratic extrapolation and little more than half the cold start's, and the fields stay
+    within the tolerance-level distance of the cold-start run."""
+    import ora
+    import sts
+    case = sc.config_case("channel_ma2.43", scale=0.5, Nt=80)
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        cold = ora.Oracle(d, fixed_sweeps=False)
+        cold.step(80)
+        runs = {}
+        for warm in (2, 4):
+            g = sts.Solver(d, fixed_sweeps=False, warm_start=warm, precision=sts.MIXED)
+            assert g.step(80) == 80
+            runs[warm] = (g.sweep_history()[40:].mean(), {f: g.field(f) for f in ("p", "T")})
+            g.close()
+        hc = cold.sweeps()[40:80].mean()
+        print("sweeps per step: cold", hc, "quadratic", runs[2][0], "stencil", runs[4][0])
+        assert runs[4][0] < runs[2][0]
+        assert runs[4][0] <= 0.55 * hc
+        for f in ("p", "T"):
+            e = np.linalg.norm(runs[4][1][f] - cold.field(f)) / np.linalg.norm(cold.field(f))
+            assert e < 1e-6, (f, e)
+
+
+def test_batch_conv_warm_start_equals_single(lib_built):
+    import os
+    import sts
+    cases = sc.batch_cases(n=3, Nt=40, nx_range=(40, 100))
+    with tempfile.TemporaryDirectory() as root:
+        dirs = []
+        for k, c in enumerate(cases):
+            d = os.path.join(root, f"c{k}")
+            os.makedirs(d)
+            c.write(d)
+            dirs.append(d)
+        b = sts.Batch(dirs, fixed_sweeps=False, warm_start=4, precision=2)
+        assert b.step(16) == 16
+        for k, d in enumerate(dirs):
+            s = sts.Solver(d, fixed_sweeps=False, warm_start=4, precision=2)
+            s.step(16)
+            for f in FIELDS:
+                np.testing.assert_array_equal(b.cases[k].field(f), s.field(f), err_msg=f"case {k} {f}")
+            np.testing.assert_array_equal(b.cases[k].sweep_history(), s.sweep_history())
+            s.close()
+        b.close()
