@@ -202,7 +202,7 @@ struct Oracle {
   static constexpr int kCFeat = 36, kCTerms = 36 * 37 / 2 + 36, kCWin = 6, kCRing = 5;
   std::vector<float> cD[2][kCRing];
   std::vector<unsigned char> cact[2], csolved;
-  std::vector<double> cgram;
+  std::vector<float> cgram;
   float conv_w[2][kCFeat] = {};
   bool conv_ok[2] = {false, false};
   void warm_conv();
@@ -1945,9 +1945,9 @@ static inline float bits_f32(unsigned u) {
 // |D_h| > 0.1 max |D_h| (x wrapped on periodic meshes) -- where it starts from x_h + w . features.
 // The weights solve least squares over the last 6 training pairs (features of step t-1 on the
 // cells active at t-1, target D_t): normal-equation terms summed in FP32 per strip of 32x2 cells
-// (rows in cell order), with compensated FP32 sums over the non-empty strips of each segment of 64
-// strips and over the non-empty segments, in FP64 over the 6 window slots in slot order; ridge
-// 1e-11 of the mean diagonal; FP32 Gauss-Jordan elimination without pivoting.  Every operation has the
+// (rows in cell order), with compensated FP32 sums over the strips with rows of each 32x8 tile,
+// over the tiles with rows (tile order) and over the 6 window slots (slot order); ridge 1e-11 of
+// the mean diagonal (FP64 trace); FP32 Gauss-Jordan elimination without pivoting.  Every operation has the
 // library's order, so the initial iterates agree bit for bit.
 void Oracle::warm_conv() {
   const unsigned r = (unsigned)warm_ready;
@@ -1959,7 +1959,7 @@ void Oracle::warm_conv() {
       for (int k = 0; k < kCRing; k++) cD[f][k].assign(Na, 0.f);
     cact[0].assign(Na, 0);
     cact[1].assign(Na, 0);
-    cgram.assign((size_t)kCWin * 2 * kCTerms, 0.0);
+    cgram.assign((size_t)kCWin * 2 * kCTerms, 0.f);
     p_m1.assign(Na, 0.0); p_m2.assign(Na, 0.0);
     T_m1.assign(Na, 0.0); T_m2.assign(Na, 0.0);
   }
@@ -2018,83 +2018,72 @@ void Oracle::warm_conv() {
       cact[h & 1][n] = bits;
     }
   // the newest training pair
+  auto neumaier = [](float& sm, float& cm, float x) {
+    const float t = sm + x;
+    if (std::fabs(sm) >= std::fabs(x)) cm = cm + ((sm - t) + x);
+    else cm = cm + ((x - t) + sm);
+    sm = t;
+  };
   if (h >= 4) {
-    const int nsx = ((int)Nx + 31) / 32, nsy = ((int)Ny + 1) / 2, nstrips = nsx * nsy;
-    std::vector<float> F(64 * (kCFeat + 1)), part(kCTerms);
-    // per strip and field: row count and FP32 terms
-    std::vector<int> nrows(2 * nstrips, 0);
-    std::vector<float> parts((size_t)nstrips * 2 * kCTerms, 0.f);
-    for (int sy = 0; sy < nsy; sy++)
-      for (int sx = 0; sx < nsx; sx++)
+    // the newest training pair: per 32x8 tile, per strip of 32x2 cells (rows in cell order) the
+    // FP32 terms; compensated sums over the tile's strips with rows, then over the tiles with rows
+    const int ntx = ((int)Nx + 31) / 32, nty = ((int)Ny + 7) / 8;
+    std::vector<float> F(64 * (kCFeat + 1));
+    std::vector<float> total(2 * kCTerms), tot_c(2 * kCTerms, 0.f);
+    std::fill(total.begin(), total.end(), 0.f);
+    for (int ty = 0; ty < nty; ty++)
+      for (int tx = 0; tx < ntx; tx++)
         for (int f = 0; f < 2; f++) {
-          int rows = 0;
-          for (int j = 2 * sy; j < 2 * sy + 2 && j < (int)Ny; j++)
-            for (int i = 32 * sx; i < 32 * sx + 32 && i < (int)Nx; i++) {
-              const size_t n = (size_t)i + (size_t)j * Nx;
-              if (!((cact[(h - 1) & 1][n] >> f) & 1)) continue;
-              conv_features(f, h - 1, i, j, &F[rows * (kCFeat + 1)]);
-              F[rows * (kCFeat + 1) + kCFeat] = cD[f][h % kCRing][n];
-              rows++;
-            }
-          if (!rows) continue;
-          int e = 0;
-          for (int a = 0; a < kCFeat; a++)
-            for (int b = a; b < kCFeat; b++, e++) {
+          float strip_terms[4][kCTerms];
+          int rows_of[4] = {0, 0, 0, 0};
+          for (int sidx = 0; sidx < 4; sidx++) {
+            int rows = 0;
+            for (int j = 8 * ty + 2 * sidx; j < 8 * ty + 2 * sidx + 2 && j < (int)Ny; j++)
+              for (int i = 32 * tx; i < 32 * tx + 32 && i < (int)Nx; i++) {
+                const size_t n = (size_t)i + (size_t)j * Nx;
+                if (!((cact[(h - 1) & 1][n] >> f) & 1)) continue;
+                conv_features(f, h - 1, i, j, &F[rows * (kCFeat + 1)]);
+                F[rows * (kCFeat + 1) + kCFeat] = cD[f][h % kCRing][n];
+                rows++;
+              }
+            rows_of[sidx] = rows;
+            int e = 0;
+            for (int a = 0; a < kCFeat; a++)
+              for (int b = a; b < kCFeat; b++, e++) {
+                float t = 0.f;
+                for (int q = 0; q < rows; q++) t = t + F[q * (kCFeat + 1) + a] * F[q * (kCFeat + 1) + b];
+                strip_terms[sidx][e] = t;
+              }
+            for (int a = 0; a < kCFeat; a++, e++) {
               float t = 0.f;
-              for (int q = 0; q < rows; q++) t = t + F[q * (kCFeat + 1) + a] * F[q * (kCFeat + 1) + b];
-              part[e] = t;
+              for (int q = 0; q < rows; q++) t = t + F[q * (kCFeat + 1) + a] * F[q * (kCFeat + 1) + kCFeat];
+              strip_terms[sidx][e] = t;
             }
-          for (int a = 0; a < kCFeat; a++, e++) {
-            float t = 0.f;
-            for (int q = 0; q < rows; q++) t = t + F[q * (kCFeat + 1) + a] * F[q * (kCFeat + 1) + kCFeat];
-            part[e] = t;
           }
-          const int strip = sx + sy * nsx;
-          nrows[f * nstrips + strip] = rows;
-          std::copy(part.begin(), part.end(), parts.begin() + ((size_t)strip * 2 + f) * kCTerms);
+          if (rows_of[0] + rows_of[1] + rows_of[2] + rows_of[3] == 0) continue;
+          for (int e = 0; e < kCTerms; e++) {
+            float sm = 0.f, cm = 0.f;
+            for (int sidx = 0; sidx < 4; sidx++)
+              if (rows_of[sidx] > 0) neumaier(sm, cm, strip_terms[sidx][e]);
+            neumaier(total[f * kCTerms + e], tot_c[f * kCTerms + e], sm + cm);
+          }
         }
-    // compensated FP32 sums (Neumaier) over the non-empty strips of each segment of 64 strips, then
-    // over the non-empty segments, in index order
-    auto neumaier = [](float& sm, float& cm, float x) {
-      const float t = sm + x;
-      if (std::fabs(sm) >= std::fabs(x)) cm = cm + ((sm - t) + x);
-      else cm = cm + ((x - t) + sm);
-      sm = t;
-    };
-    const int nseg = (nstrips + 63) / 64;
     const unsigned pair = h - 4;
-    for (int f = 0; f < 2; f++) {
-      std::vector<float> seg((size_t)nseg * kCTerms);
-      std::vector<int> seg_rows(nseg, 0);
-      for (int g = 0; g < nseg; g++) {
-        const int s0 = g * 64, ns = std::min(64, nstrips - s0);
-        for (int q = 0; q < ns; q++) seg_rows[g] += nrows[f * nstrips + s0 + q];
-        for (int e = 0; e < kCTerms; e++) {
-          float sm = 0.f, cm = 0.f;
-          for (int q = 0; q < ns; q++)
-            if (nrows[f * nstrips + s0 + q] > 0) neumaier(sm, cm, parts[((size_t)(s0 + q) * 2 + f) * kCTerms + e]);
-          seg[(size_t)g * kCTerms + e] = sm + cm;
-        }
-      }
-      for (int e = 0; e < kCTerms; e++) {
-        float sm = 0.f, cm = 0.f;
-        for (int g = 0; g < nseg; g++)
-          if (seg_rows[g] > 0) neumaier(sm, cm, seg[(size_t)g * kCTerms + e]);
-        cgram[((size_t)(pair % kCWin) * 2 + f) * kCTerms + e] = (double)(sm + cm);
-      }
-    }
+    for (int f = 0; f < 2; f++)
+      for (int e = 0; e < kCTerms; e++)
+        cgram[((size_t)(pair % kCWin) * 2 + f) * kCTerms + e] = total[f * kCTerms + e] + tot_c[f * kCTerms + e];
     for (int f = 0; f < 2; f++) {
       conv_ok[f] = false;
       if (pair + 1 < (unsigned)kCWin) continue;
-      std::vector<double> G(kCTerms);
+      std::vector<float> G(kCTerms);
       for (int q = 0; q < kCTerms; q++) {
-        double v = 0.0;
-        for (int w = 0; w < kCWin; w++) v = v + cgram[((size_t)w * 2 + f) * kCTerms + q];
-        G[q] = v;
+        float sm = 0.f, cm = 0.f;
+        for (int w = 0; w < kCWin; w++) neumaier(sm, cm, cgram[((size_t)w * 2 + f) * kCTerms + q]);
+        G[q] = sm + cm;
       }
       double tr = 0.0;
       for (int a = 0, e = 0; a < kCFeat; a++) {
-        tr = tr + G[e];
+        tr = tr + (double)G[e];
         e += kCFeat - a;
       }
       const double lam = 1e-11 * tr / (double)kCFeat;
@@ -2103,10 +2092,10 @@ void Oracle::warm_conv() {
       int e = 0;
       for (int a = 0; a < kCFeat; a++)
         for (int b = a; b < kCFeat; b++, e++) {
-          if (a == b) M[a][a] = (float)(G[e] + lam);
-          else M[a][b] = M[b][a] = (float)G[e];
+          if (a == b) M[a][a] = (float)((double)G[e] + lam);
+          else M[a][b] = M[b][a] = G[e];
         }
-      for (int a = 0; a < kCFeat; a++, e++) M[a][kCFeat] = (float)G[e];
+      for (int a = 0; a < kCFeat; a++, e++) M[a][kCFeat] = G[e];
       bool ok = true;
       for (int k = 0; k < kCFeat && ok; k++) {
         const float piv = M[k][k];

@@ -113,7 +113,6 @@ struct Ctl {
   unsigned int conv_max[2][2];
   float conv_w[2][36];
   unsigned int conv_ok[2];
-  unsigned int conv_ticket[6];  // segment-sum CTAs done, per (field, block of 256 terms)
 };
 
 // Learned warm start: differences kept, and steps of the least-squares window.
@@ -122,9 +121,9 @@ constexpr int kWarmRing = 4, kWarmWin = 6;
 // Convolutional warm start (mode 4): features per cell (4 time-difference orders x 9 spatial
 // basis values of the 3x3 neighbourhood), normal-equation terms per field (upper triangle of the
 // 36x36 Gram matrix, then the 36 right-hand sides), steps in the least-squares window, ring of
-// stored step differences, and the strips of 32x2 cells whose partial sums are kept apart.
+// stored step differences, and the strips of 32x2 cells whose FP32 partial sums are kept apart.
 constexpr int kConvFeat = 36, kConvTerms = kConvFeat * (kConvFeat + 1) / 2 + kConvFeat, kConvWin = 6,
-              kConvRing = 5, kConvStripX = 32, kConvStripY = 2, kConvSeg = 64;
+              kConvRing = 5, kConvStripX = 32, kConvStripY = 2;
 
 // Most cases one batch may hold (the sweep loop keeps their state in shared memory).
 constexpr int kMaxBatchCases = 256;
@@ -185,17 +184,13 @@ struct Geo {
   double *Dp[4], *DT[4];
   float* warm_part;
   // mode 4: ring of step differences per field (FP32), active-cell flags by step parity (bit 0 p,
-  // bit 1 T), per-strip FP32 partial sums [strip][field][term] and row counts [field][strip] of
-  // the newest training pair, their sums over segments of kConvSeg strips [segment][field][term]
-  // and row counts [field x 3 term blocks][segment], FP64 sums of the last kConvWin pairs
-  // [slot][field][term]
+  // bit 1 T), per-tile (32x8) sums of the newest training pair's terms [tile][field][term] and row
+  // counts [field][tile], sums of the last kConvWin pairs [slot][field][term]
   float* cD[2][kConvRing];
   uint8_t* cact[2];
   float* cpart;
-  int* cnrows;
-  float* cseg;
-  int* cseg_rows;
-  double* cgram;
+  int* crows;
+  float* cgram;
 };
 
 // Neighbour indices of one cell: ij_function / ij_function_PeriodicBC (SIMPLE_TS_MPI.cpp:140-232).

@@ -43,13 +43,12 @@ __global__ void kb_warm_diff(const Geo* gs);
 __global__ void kb_warm_fit(const Geo* gs);
 __global__ void kb_warm_apply(const Geo* gs);
 // convolutional warm start (warm_start 4), sts_learn.cu (k_step_begin stores the differences):
-// k_conv_gram on strips of kConvStripX x kConvStripY cells (one CTA each), k_conv_reduce on
-// (segments of kConvSeg strips, 6) CTAs of 256, k_conv_solve with one CTA of 256 per field
+// k_conv_gram and k_conv_apply on the 32x8 cell tiles, k_conv_solve with one CTA of
+// kConvSolveThreads per field
+constexpr int kConvSolveThreads = 37 * 7;
 __global__ void k_conv_gram(Geo g);
-__global__ void k_conv_reduce(Geo g);
 __global__ void k_conv_solve(Geo g);
 __global__ void k_conv_apply(Geo g);
-__global__ void kb_conv_reduce(const Geo* gs);
 __global__ void kb_conv_gram(const Geo* gs);
 __global__ void kb_conv_solve(const Geo* gs);
 __global__ void kb_conv_apply(const Geo* gs);

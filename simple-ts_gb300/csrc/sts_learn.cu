@@ -17,20 +17,20 @@
 // (a shock that advances a fraction of a cell per step) that extrapolation in time cannot.
 //
 // Arithmetic: FP32 features; normal-equation terms summed in FP32 over the rows of a strip of 32x2
-// cells (cell order), then with compensated FP32 sums (Neumaier) over the non-empty strips of each
-// segment of kConvSeg strips and over the non-empty segments, both in index order; FP64 over the
-// window in slot order; a ridge of 1e-11 of the mean diagonal; Gauss-Jordan elimination in FP32.  This file is compiled without fused multiply-adds and every sum has a
-// fixed order, so the result does not depend on scheduling and the CPU oracle reproduces it bit
-// for bit.  (GB300's FP64 pipe does about 2 adds per clock per SM: the sums over strips stay on
-// the FP32 pipes and are spread over many CTAs.)
+// cells (cell order), then with compensated FP32 sums (Neumaier) over the strips with rows of each
+// 32x8 tile (strip order), over the tiles with rows (tile order) and over the window (slot order);
+// a ridge of 1e-11 of the mean diagonal (FP64 trace); Gauss-Jordan elimination in FP32.  This
+// file is compiled without fused multiply-adds and every sum has a fixed order, so the result does
+// not depend on scheduling and the CPU oracle reproduces it bit for bit.  (GB300's FP64 pipe does
+// about 2 adds per clock per SM: the sums stay on the FP32 pipes.)
 //
 // Per step: k_step_begin stores the newest differences, writes the quadratic start and folds
-// max |D| (conv_step_begin_cell, conv_block_max); then, in the step's first outer iteration and
-// in a graph beside the assembly kernel (which reads neither p nor T of the iterate; the sweep loop
-// waits for both), conv_gram (per-strip terms of the newest
-// training pair), conv_reduce (segment sums and the pair's total), conv_solve (one CTA per
-// field: window, ridge, elimination) and conv_apply (active flags of the newest difference,
-// start).
+// max |D| (conv_step_begin_cell, conv_block_max); conv_apply, beside the assembly kernel (which
+// reads neither p nor T of the iterate; the sweep loop waits for both), marks the active cells and
+// writes the stencil's start there with the weights fitted at the end of the previous step; after
+// the sweeps, beside the correction and boundary kernels (which write p and T only outside the
+// solved cells), conv_gram forms the newest training pair's terms per tile and conv_solve sums
+// them into the window and solves for the next step's weights.
 #include <cuda_runtime.h>
 
 #include "sts_common.cuh"
@@ -125,190 +125,201 @@ __device__ __forceinline__ void neumaier(float& s, float& c, float x) {
   s = t;
 }
 
-// One CTA per strip of 32x2 cells: the FP32 normal-equation terms of the newest training pair
-// (features of the previous step on its active cells, target the newest difference).  A strip
-// without active cells only records that.
+// One CTA per tile of 32x8 cells, i.e. four strips of 32x2 cells, at the end of a step (after the
+// sweeps): the normal-equation terms of the training pair whose target is the coming difference
+// D_{h+1} = x_{n+1} - x_n -- the step's final iterate less the start-of-step value, rounded to
+// FP32 exactly as the next step's start stores it -- and whose features are those of the newest
+// stored difference D_h on its active cells; summed in FP32 over each strip's rows in cell order,
+// then over the tile's strips with rows in strip order (compensated).  A tile without active
+// cells only records that.  (The pair is the one the next step would form; forming it now lets
+// the fit run beside the step's last kernels instead of on the next step's path.)
 __device__ __forceinline__ void conv_gram_body(const Geo& g) {
   const Ctl* ctl = g.ctl;
-  const unsigned r = ctl->warm_ready;
-  if (r < 5 || ctl->Iter != 0) return;  // a training pair needs five differences; first outer iteration only
+  const unsigned r = ctl->warm_ready, cur = ctl->cur;
+  if (r < 4) return;  // the features need four stored differences
   const unsigned h = r - 1;
   const int Nx = g.Nx, Ny = g.Ny;
-  const int nsx = (Nx + kConvStripX - 1) / kConvStripX, nsy = (Ny + kConvStripY - 1) / kConvStripY;
-  if ((int)blockIdx.x >= nsx || (int)blockIdx.y >= nsy) return;
-  const int strip = blockIdx.x + blockIdx.y * nsx, nstrips = nsx * nsy;
-  const int tid = threadIdx.x + kConvStripX * threadIdx.y;
-  const int i = blockIdx.x * kConvStripX + threadIdx.x, j = blockIdx.y * kConvStripY + threadIdx.y;
+  constexpr int TX = 32, TY = 8, NS = TY / kConvStripY, SR = kConvStripX * kConvStripY;
+  const int ntx = (Nx + TX - 1) / TX, nty = (Ny + TY - 1) / TY, ntiles = ntx * nty;
+  if ((int)blockIdx.x >= ntx || (int)blockIdx.y >= nty) return;
+  const int tile = blockIdx.x + blockIdx.y * ntx;
+  const int tid = threadIdx.x + TX * threadIdx.y, lane = threadIdx.x;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
   const bool in = i < Nx && j < Ny;
   const int n = i + j * Nx;
-  const unsigned bits = in ? g.cact[(h - 1) & 1][n] : 0u;
+  const unsigned bits = in ? g.cact[h & 1][n] : 0u;
   if (!__syncthreads_or(bits != 0u)) {
-    if (tid < 2) g.cnrows[tid * nstrips + strip] = 0;
+    if (tid < 2) g.crows[tid * ntiles + tile] = 0;
     return;
   }
-  // the previous step's four differences over the strip and a margin of one (clamped to the mesh)
-  const int i0 = blockIdx.x * kConvStripX, j0 = blockIdx.y * kConvStripY;
-  constexpr int kFx = kConvStripX + 2, kFy = kConvStripY + 2;
-  __shared__ float Df[2][4][kFy][kFx];
-  stage<2 * 4 * kFy * kFx, kConvStripX * kConvStripY>(&Df[0][0][0][0], tid, [&](int k) {
-    const int f = k / (4 * kFy * kFx), rem = k - f * (4 * kFy * kFx);
-    const int t = rem / (kFy * kFx), rem2 = rem - t * (kFy * kFx), yy = rem2 / kFx, xx = rem2 - yy * kFx;
-    const int jj = min(max(j0 - 1 + yy, 0), Ny - 1), ii = min(max(i0 - 1 + xx, 0), Nx - 1);
-    return g.cD[f][(h - 1 - t) % kConvRing][ii + jj * Nx];
-  });
-  __shared__ float Tg[2][kConvStripY][kConvStripX];  // the target: the newest difference
-  stage<2 * kConvStripY * kConvStripX, kConvStripX * kConvStripY>(&Tg[0][0][0], tid, [&](int k) {
-    const int f = k / (kConvStripY * kConvStripX), rem = k - f * (kConvStripY * kConvStripX);
-    const int yy = rem / kConvStripX, xx = rem - yy * kConvStripX;
-    const int jj = min(j0 + yy, Ny - 1), ii = min(i0 + xx, Nx - 1);
-    return g.cD[f][h % kConvRing][ii + jj * Nx];
-  });
-  __shared__ float F[kConvStripX * kConvStripY][kConvFeat + 1];
-  __shared__ int wcount[kConvStripY];
-  const int lane = threadIdx.x;
-  __syncthreads();
+  __shared__ float Df[4][TY + 2][TX + 2];          // D_{h..h-3} of one field, margin one (clamped)
+  __shared__ float F[NS][SR][kConvFeat + 1];       // per strip: active rows' features and target
+  __shared__ int wcount[TY];
+  float* P = &F[0][0][0];                          // the strips' terms, after F is used: [NS][kConvTerms]
+  const int s = threadIdx.y / kConvStripY, t64 = threadIdx.x + TX * (threadIdx.y % kConvStripY);
   for (int f = 0; f < 2; f++) {
-    const bool act = (bits >> f) & 1u;
+    stage<4 * (TY + 2) * (TX + 2), TX * TY>(&Df[0][0][0], tid, [&](int k) {
+      const int t = k / ((TY + 2) * (TX + 2)), rem = k - t * ((TY + 2) * (TX + 2));
+      const int yy = rem / (TX + 2), xx = rem - yy * (TX + 2);
+      const int jj = min(max(j0 - 1 + yy, 0), Ny - 1), ii = min(max(i0 - 1 + xx, 0), Nx - 1);
+      return g.cD[f][(h - t) % kConvRing][ii + jj * Nx];
+    });
+    const bool act = (bits >> f) & 1u;  // active cells are solved cells
+    const float target = act ? (float)((f ? g.T[cur][n] : g.p[cur][n]) - (f ? g.T_m[0][n] : g.p_m[0][n])) : 0.f;
     const unsigned bal = __ballot_sync(0xffffffffu, act);
     if (lane == 0) wcount[threadIdx.y] = __popc(bal);
     __syncthreads();
-    int nrows = 0, pos = 0;
-    for (int w = 0; w < kConvStripY; w++) {
-      if (w < (int)threadIdx.y) pos += wcount[w];
-      nrows += wcount[w];
-    }
-    pos += __popc(bal & ((1u << lane) - 1u));
+    int nr[NS];
+    for (int q = 0; q < NS; q++) nr[q] = wcount[kConvStripY * q] + wcount[kConvStripY * q + 1];
+    const int pos = ((threadIdx.y % kConvStripY) ? wcount[threadIdx.y - 1] : 0) + __popc(bal & ((1u << lane) - 1u));
     if (act) {
       const int x0 = threadIdx.x + 1, y0 = threadIdx.y + 1;
-      conv_features_from([&](int k, int dj, int di) { return Df[f][k][y0 + dj][x0 + di]; }, F[pos]);
-      F[pos][kConvFeat] = Tg[f][threadIdx.y][threadIdx.x];
+      conv_features_from([&](int k, int dj, int di) { return Df[k][y0 + dj][x0 + di]; }, F[s][pos]);
+      F[s][pos][kConvFeat] = target;
     }
     __syncthreads();
-    if (tid == 0) g.cnrows[f * nstrips + strip] = nrows;
-    if (nrows > 0) {
-      // each thread's terms e = tid + 64 k accumulate side by side (every term still sums its
-      // rows in order)
-      constexpr int kNT = kConvStripX * kConvStripY, kPerT = (kConvTerms + kNT - 1) / kNT;
+    // each strip's 64 threads: terms e = t64 + 64 k accumulate side by side, every term over the
+    // strip's rows in order
+    constexpr int kPerT = (kConvTerms + SR - 1) / SR;
+    float acc[kPerT];
+    for (int k = 0; k < kPerT; k++) acc[k] = 0.f;
+    if (nr[s] > 0) {
       int ta[kPerT], tb[kPerT];
-      float acc[kPerT];
       for (int k = 0; k < kPerT; k++) {
-        const int e = tid + k * kNT;
+        const int e = t64 + k * SR;
         if (e < kConvTerms) conv_term(e, ta[k], tb[k]);
         else ta[k] = tb[k] = 0;
-        acc[k] = 0.f;
       }
-      for (int q = 0; q < nrows; q++)
+      for (int q = 0; q < nr[s]; q++)
 #pragma unroll
-        for (int k = 0; k < kPerT; k++) acc[k] = acc[k] + F[q][ta[k]] * F[q][tb[k]];
-      float* out = g.cpart + ((size_t)strip * 2 + f) * kConvTerms;
-      for (int k = 0; k < kPerT; k++) {
-        const int e = tid + k * kNT;
-        if (e < kConvTerms) out[e] = acc[k];
-      }
+        for (int k = 0; k < kPerT; k++) acc[k] = acc[k] + F[s][q][ta[k]] * F[s][q][tb[k]];
     }
+    __syncthreads();  // F is read no more: its space takes the strips' terms
+    for (int k = 0; k < kPerT; k++) {
+      const int e = t64 + k * SR;
+      if (e < kConvTerms) P[s * kConvTerms + e] = acc[k];
+    }
+    __syncthreads();
+    for (int e = tid; e < kConvTerms; e += TX * TY) {
+      float sum = 0.f, cmp = 0.f;
+      for (int q = 0; q < NS; q++)
+        if (nr[q] > 0) neumaier(sum, cmp, P[q * kConvTerms + e]);
+      g.cpart[((size_t)tile * 2 + f) * kConvTerms + e] = sum + cmp;
+    }
+    if (tid == 0) g.crows[f * ntiles + tile] = nr[0] + nr[1] + nr[2] + nr[3];
     __syncthreads();
   }
 }
 
-// CTA (segment, field x 3 blocks of 256 terms): the sums over the non-empty strips of a segment of
-// kConvSeg strips, in strip order.  The last CTA of each (field, term block) to finish -- a ticket
-// counter -- then sums the non-empty segments in order and writes the pair's FP64 window slot.
-__device__ __forceinline__ void conv_reduce_body(const Geo& g) {
-  Ctl* ctl = g.ctl;
-  const unsigned r = ctl->warm_ready;
-  if (r < 5 || ctl->Iter != 0) return;  // no training pair yet, or not the step's first outer iteration
-  const unsigned pair = r - 5;
-  const int nsx = (g.Nx + kConvStripX - 1) / kConvStripX, nsy = (g.Ny + kConvStripY - 1) / kConvStripY;
-  const int nstrips = nsx * nsy, nseg = (nstrips + kConvSeg - 1) / kConvSeg;
-  const int seg = blockIdx.x, yb = blockIdx.y, f = yb / 3, tid = threadIdx.x;
-  if (seg >= nseg) return;
-  const int e = (yb % 3) * 256 + tid, s0 = seg * kConvSeg, ns = min(kConvSeg, nstrips - s0);
-  __shared__ int cnt[kConvSeg];
-  __shared__ bool last;
-  if (tid < ns) cnt[tid] = g.cnrows[f * nstrips + s0 + tid];
-  __syncthreads();
-  if (tid == 0) {
-    int rows = 0;
-    for (int q = 0; q < ns; q++) rows += cnt[q];
-    g.cseg_rows[yb * nseg + seg] = rows;
-  }
-  if (e < kConvTerms) {
-    float sum = 0.f, cmp = 0.f;
-    for (int q0 = 0; q0 < ns; q0 += 16) {  // sixteen loads in flight, then the ordered sum
-      float v[16];
-#pragma unroll
-      for (int u = 0; u < 16; u++) {
-        const int q = q0 + u;
-        v[u] = (q < ns && cnt[q] > 0) ? g.cpart[((size_t)(s0 + q) * 2 + f) * kConvTerms + e] : 0.f;
-      }
-#pragma unroll
-      for (int u = 0; u < 16; u++)
-        if (q0 + u < ns && cnt[q0 + u] > 0) neumaier(sum, cmp, v[u]);
-    }
-    g.cseg[((size_t)seg * 2 + f) * kConvTerms + e] = sum + cmp;
-  }
-  __threadfence();
-  __syncthreads();
-  if (tid == 0) {
-    const unsigned t = atomicAdd(&ctl->conv_ticket[yb], 1u);
-    last = (t == (unsigned)nseg - 1u);
-    if (last) ctl->conv_ticket[yb] = 0u;
-  }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  if (e >= kConvTerms) return;
-  const int* rows = g.cseg_rows + yb * nseg;
-  float sum = 0.f, cmp = 0.f;
-  for (int q0 = 0; q0 < nseg; q0 += 16) {
-    float v[16];
-    int rw[16];
-#pragma unroll
-    for (int u = 0; u < 16; u++) {
-      const int q = q0 + u;
-      rw[u] = q < nseg ? rows[q] : 0;
-      v[u] = q < nseg ? g.cseg[((size_t)q * 2 + f) * kConvTerms + e] : 0.f;
-    }
-#pragma unroll
-    for (int u = 0; u < 16; u++)
-      if (rw[u] > 0) neumaier(sum, cmp, v[u]);
-  }
-  g.cgram[((size_t)(pair % kConvWin) * 2 + f) * kConvTerms + e] = (double)(sum + cmp);
-}
+// One CTA of 37 x 7 threads per field, after conv_gram: the pair's total over the tiles with rows
+// (tile order, compensated FP32) into the window ring; once the window is full, the weights for the
+// next step: the window sum (slot order,
+// compensated), the ridge (FP64 trace), and the FP32 system solved by Gauss-Jordan elimination
+// without pivoting (the matrix is symmetric positive definite): at pivot k, with
+// u_j = M_kj (1 / M_kk), row k becomes u and every other row i has M_ij - M_ik u_j, j > k, the
+// right-hand side included; after the last pivot the right-hand side holds the weights.  Thread
+// (c, g) owns column c and rows g, g + 7, ...; two buffers, one barrier per pivot.
+constexpr int kSolveCols = kConvFeat + 1, kSolveRowGroups = 7, kSolveThreads = kSolveCols * kSolveRowGroups;
+static_assert(kSolveThreads == kConvSolveThreads, "launch size of k_conv_solve");
 
-// One CTA of 256 threads per field: once the window is full, the FP64 window sum, the ridge, and
-// the FP32 system solved by Gauss-Jordan elimination without pivoting (the matrix is symmetric
-// positive definite): at pivot k, with u_j = M_kj / M_kk (a reciprocal, then products), row k
-// becomes u and every other row i has M_ij - M_ik u_j, j > k, the right-hand side included; after
-// the last pivot the right-hand side holds the weights.  Two buffers, one barrier per pivot.
 __device__ __forceinline__ void conv_solve_body(const Geo& g) {
   Ctl* ctl = g.ctl;
   const unsigned r = ctl->warm_ready;
   const int f = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
-  if (ctl->Iter != 0) return;  // the step's first outer iteration only
-  if (r < 5 || r - 5 + 1 < (unsigned)kConvWin) {  // the window is not full yet
+  if (r < 4) {
+    if (tid == 0) ctl->conv_ok[f] = 0u;
+    return;
+  }
+  const unsigned pair = r - 4;  // pairs formed so far, less one
+  constexpr int TX = 32, TY = 8;
+  const int ntiles = ((g.Nx + TX - 1) / TX) * ((g.Ny + TY - 1) / TY);
+  constexpr int kPerT = (kConvTerms + kSolveThreads - 1) / kSolveThreads;
+  constexpr int kChunk = 2048, kFlags = (kChunk + kSolveThreads - 1) / kSolveThreads;
+  __shared__ int list[kChunk];
+  __shared__ int wsum[32];
+  __shared__ int count;
+  float sum[kPerT], cmp[kPerT];
+  for (int k = 0; k < kPerT; k++) sum[k] = cmp[k] = 0.f;
+  const int* rows = g.crows + f * ntiles;
+  for (int t0 = 0; t0 < ntiles; t0 += kChunk) {
+    // ordered list of the chunk's tiles with rows: block-wide exclusive scan of the flags
+    int fl[kFlags], mine = 0;
+#pragma unroll
+    for (int q = 0; q < kFlags; q++) {
+      const int t = t0 + tid * kFlags + q;
+      fl[q] = (t < ntiles && tid * kFlags + q < kChunk) ? (rows[t] > 0) : 0;
+    }
+    for (int q = 0; q < kFlags; q++) mine += fl[q];
+    const int lane = tid & 31, warp = tid >> 5, nw = (nt + 31) >> 5;
+    // the last warp of the block may be partial: its shuffles name only the lanes it has
+    const unsigned wmask = (warp == nw - 1 && (nt & 31)) ? ((1u << (nt & 31)) - 1u) : 0xffffffffu;
+    int incl = mine;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(wmask, incl, o);
+      if (lane >= o) incl += v;
+    }
+    if (lane == 31 || tid == nt - 1) wsum[warp] = incl;
+    __syncthreads();
+    int before = 0, total = 0;
+    for (int w = 0; w < nw; w++) {
+      if (w < warp) before += wsum[w];
+      total += wsum[w];
+    }
+    int pos = before + incl - mine;
+    for (int q = 0; q < kFlags; q++)
+      if (fl[q]) list[pos++] = t0 + tid * kFlags + q;
+    if (tid == 0) count = total;
+    __syncthreads();
+    const int cnt = count;
+    for (int q0 = 0; q0 < cnt; q0 += 8) {  // eight tiles' loads in flight, then the ordered sums
+      float v[8][kPerT];
+#pragma unroll
+      for (int u = 0; u < 8; u++)
+#pragma unroll
+        for (int k = 0; k < kPerT; k++) {
+          const int e = tid + k * nt;
+          v[u][k] = (q0 + u < cnt && e < kConvTerms) ? g.cpart[((size_t)list[q0 + u] * 2 + f) * kConvTerms + e] : 0.f;
+        }
+#pragma unroll
+      for (int u = 0; u < 8; u++)
+        if (q0 + u < cnt)
+#pragma unroll
+          for (int k = 0; k < kPerT; k++) neumaier(sum[k], cmp[k], v[u][k]);
+    }
+    __syncthreads();
+  }
+  for (int k = 0; k < kPerT; k++) {
+    const int e = tid + k * nt;
+    if (e < kConvTerms) g.cgram[((size_t)(pair % kConvWin) * 2 + f) * kConvTerms + e] = sum[k] + cmp[k];
+  }
+  __syncthreads();
+  if (pair + 1 < (unsigned)kConvWin) {
     if (tid == 0) ctl->conv_ok[f] = 0u;
     return;
   }
   constexpr int n = kConvFeat, W = n + 1;
-  __shared__ double G[kConvTerms];
+  __shared__ float Gw[kConvTerms];
   __shared__ float M[2][n][W + 1];
   __shared__ double lam;
-  for (int e = tid; e < kConvTerms; e += nt) {
-    double x[kConvWin];
+  for (int k = 0; k < kPerT; k++) {
+    const int e = tid + k * nt;
+    if (e < kConvTerms) {
+      float x[kConvWin];
 #pragma unroll
-    for (int q = 0; q < kConvWin; q++) x[q] = g.cgram[((size_t)q * 2 + f) * kConvTerms + e];
-    double v = 0.0;
+      for (int q = 0; q < kConvWin; q++) x[q] = g.cgram[((size_t)q * 2 + f) * kConvTerms + e];
+      float ws = 0.f, wc = 0.f;
 #pragma unroll
-    for (int q = 0; q < kConvWin; q++) v = v + x[q];
-    G[e] = v;
+      for (int q = 0; q < kConvWin; q++) neumaier(ws, wc, x[q]);
+      Gw[e] = ws + wc;
+    }
   }
   __syncthreads();
   if (tid == 0) {
     double tr = 0.0;
     for (int a = 0, e = 0; a < n; a++) {
-      tr = tr + G[e];  // entry (a, a)
-      e += n - a;      // first entry of the next row
+      tr = tr + (double)Gw[e];  // entry (a, a)
+      e += n - a;               // first entry of the next row
     }
     lam = kConvRidge * tr / (double)n;
   }
@@ -316,11 +327,12 @@ __device__ __forceinline__ void conv_solve_body(const Geo& g) {
   for (int e = tid; e < kConvTerms; e += nt) {
     int a, b;
     conv_term(e, a, b);
-    if (b == n) M[0][a][n] = (float)G[e];
-    else if (a == b) M[0][a][a] = (float)(G[e] + lam);
-    else M[0][a][b] = M[0][b][a] = (float)G[e];
+    if (b == n) M[0][a][n] = Gw[e];
+    else if (a == b) M[0][a][a] = (float)((double)Gw[e] + lam);
+    else M[0][a][b] = M[0][b][a] = Gw[e];
   }
   __syncthreads();
+  const int c = tid % kSolveCols, rg = tid / kSolveCols;
   for (int k = 0; k < n; k++) {
     const float (*src)[W + 1] = M[k & 1];
     float (*dst)[W + 1] = M[(k + 1) & 1];
@@ -329,12 +341,9 @@ __device__ __forceinline__ void conv_solve_body(const Geo& g) {
       if (tid == 0) ctl->conv_ok[f] = 0u;
       return;
     }
-    const float rp = 1.0f / piv;
-    const int ncol = n - k;  // columns k+1 .. n
-    for (int idx = tid; idx < n * ncol; idx += nt) {
-      const int i = idx / ncol, j = k + 1 + (idx - i * ncol);
-      const float u = src[k][j] * rp;
-      dst[i][j] = (i == k) ? u : src[i][j] - src[i][k] * u;
+    if (c > k && rg < kSolveRowGroups) {
+      const float u = src[k][c] * (1.0f / piv);
+      for (int i = rg; i < n; i += kSolveRowGroups) dst[i][c] = (i == k) ? u : src[i][c] - src[i][k] * u;
     }
     __syncthreads();
   }
@@ -414,14 +423,8 @@ __device__ __forceinline__ void conv_apply_body(const Geo& g) {
 }  // namespace
 
 __global__ void k_conv_gram(Geo g) { conv_gram_body(g); }
-__global__ void k_conv_reduce(Geo g) { conv_reduce_body(g); }
 __global__ void k_conv_solve(Geo g) { conv_solve_body(g); }
 __global__ void k_conv_apply(Geo g) { conv_apply_body(g); }
-__global__ void kb_conv_reduce(const Geo* gs) {
-  __shared__ Geo sg;
-  if (!stage_geo(sg, gs)) return;
-  conv_reduce_body(sg);
-}
 __global__ void kb_conv_gram(const Geo* gs) {
   __shared__ Geo sg;
   if (!stage_geo(sg, gs)) return;

@@ -129,15 +129,6 @@ struct sts_ctx {
     flux_kernel()<<<grid, block, 0, s>>>(g, PH_TEMP | PH_PRES);
     mark(6);
   }
-  // strips of the convolutional warm start's normal-equation kernel
-  dim3 strip_grid() const {
-    return dim3((unsigned)((g.Nx + kConvStripX - 1) / kConvStripX), (unsigned)((g.Ny + kConvStripY - 1) / kConvStripY));
-  }
-  // its segment sums: one CTA per (segment of kConvSeg strips, field x 3 blocks of 256 terms)
-  dim3 seg_grid() const {
-    const dim3 sg = strip_grid();
-    return dim3((sg.x * sg.y + kConvSeg - 1) / kConvSeg, 6);
-  }
   // the learned warm starts' kernels after the start of a step (modes 3 and 4)
   template <class M>
   void warm_launches(M mark) {
@@ -149,12 +140,18 @@ struct sts_ctx {
       mark(0);
     } else if (g.warm_start == 4) {
       mark(-1);
-      k_conv_gram<<<strip_grid(), dim3(kConvStripX, kConvStripY), 0, s>>>(g);
-      k_conv_reduce<<<seg_grid(), 256, 0, s>>>(g);
-      k_conv_solve<<<2, 256, 0, s>>>(g);
       k_conv_apply<<<grid, block, 0, s>>>(g);
       mark(0);
     }
+  }
+  // warm_start 4: the fit for the next step's start, once the step's iterate is final
+  template <class M>
+  void warm_train(M mark) {
+    if (g.warm_start != 4) return;
+    mark(-1);
+    k_conv_gram<<<grid, block, 0, s>>>(g);
+    k_conv_solve<<<2, kConvSolveThreads, 0, s>>>(g);
+    mark(0);
   }
   bool fast() const { return g.precision >= 1; }
   bool mixed() const { return g.precision >= 2 && !(hc.bits & F_FIXED_SWEEPS); }
@@ -270,12 +267,9 @@ int sts_ctx::build_graph() {
   // warm_start 4: the predictor's kernels (first outer iteration only) beside the assembly
   std::vector<cudaGraphNode_t> before_sweeps{n_asm};
   if (g.warm_start == 4) {
-    cudaGraphNode_t w[4];
-    if (int r = add_kernel(&w[0], b_outer, {}, k_conv_gram, strip_grid(), dim3(kConvStripX, kConvStripY), g)) return r;
-    if (int r = add_kernel(&w[1], b_outer, {w[0]}, k_conv_reduce, seg_grid(), dim3(256), g)) return r;
-    if (int r = add_kernel(&w[2], b_outer, {w[1]}, k_conv_solve, dim3(2), dim3(256), g)) return r;
-    if (int r = add_kernel(&w[3], b_outer, {w[2]}, k_conv_apply, grid, block, g)) return r;
-    before_sweeps.push_back(w[3]);
+    cudaGraphNode_t w;
+    if (int r = add_kernel(&w, b_outer, {}, k_conv_apply, grid, block, g)) return r;
+    before_sweeps.push_back(w);
   }
   if (int r = add_kernel(&n_sw, b_outer, before_sweeps, pt_kernel(), pt_grid, dim3(32, 8), g, ntiles, d_lc)) return r;
   {
@@ -284,6 +278,11 @@ int sts_ctx::build_graph() {
     CU(cudaGraphKernelNodeSetAttribute(n_sw, cudaLaunchAttributeCooperative, &v));
   }
   if (int r = add_kernel(&n_cor, b_outer, {n_sw}, k_correct, grid, block, g)) return r;
+  if (g.warm_start == 4) {  // the fit for the next step, beside the step's last kernels
+    cudaGraphNode_t w[2];
+    if (int r = add_kernel(&w[0], b_outer, {n_sw}, k_conv_gram, grid, block, g)) return r;
+    if (int r = add_kernel(&w[1], b_outer, {w[0]}, k_conv_solve, dim3(2), dim3(kConvSolveThreads), g)) return r;
+  }
   if (int r = add_kernel(&n_rho, b_outer, {n_cor}, k_face_rho, grid, block, g)) return r;
   cudaGraphNode_t n_walls, n_tj;
   if (int r = add_kernel(&n_walls, b_outer, {n_rho}, k_bnd_walls, walls_grid(), dim3(256), g,
@@ -333,6 +332,7 @@ int sts_ctx::step_host(int n, int* done) {
         if (!h_ctl->continue_iter) break;
       }
     }
+    warm_train([](int) {});
     k_step_end<<<1, 1024, 0, s>>>(g, 0, 0);
     if (int r = check()) return r;
     if (int r = read_ctl()) return r;
@@ -379,6 +379,7 @@ int sts_ctx::profile(int n, double* ms, int* cnt, int* done) {
         if (!h_ctl->continue_iter) break;
       }
     }
+    warm_train(mark);
     mark(-1); k_step_end<<<1, 1024, 0, s>>>(g, 0, 0); mark(7);
     if (int r = check()) return r;
     if (int r = read_ctl()) return r;
@@ -842,12 +843,9 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
         if (int r = c->alloc(&g.cD[f][k], Na)) return r;
     for (int k = 0; k < 2; k++)
       if (int r = c->alloc(&g.cact[k], Na)) return r;
-    const size_t ns = (size_t)((h.Nx + kConvStripX - 1) / kConvStripX) * ((h.Ny + kConvStripY - 1) / kConvStripY);
-    if (int r = c->alloc(&g.cpart, ns * 2 * kConvTerms)) return r;
-    if (int r = c->alloc(&g.cnrows, ns * 2)) return r;
-    const size_t nseg = (ns + kConvSeg - 1) / kConvSeg;
-    if (int r = c->alloc(&g.cseg, nseg * 2 * kConvTerms)) return r;
-    if (int r = c->alloc(&g.cseg_rows, nseg * 6)) return r;
+    const size_t nt = (size_t)((h.Nx + 31) / 32) * ((h.Ny + 7) / 8);
+    if (int r = c->alloc(&g.cpart, nt * 2 * kConvTerms)) return r;
+    if (int r = c->alloc(&g.crows, nt * 2)) return r;
     if (int r = c->alloc(&g.cgram, (size_t)kConvWin * 2 * kConvTerms)) return r;
   }
   if (g.precision >= 2) {
@@ -1360,7 +1358,6 @@ struct sts_batch {
   int step_host(int n);
   bool use_graph = true;
   bool warm3 = false, warm4 = false;
-  dim3 strip_grid, seg_grid;  // strips and strip segments of the largest case, one grid layer per case
   unsigned* d_flag = nullptr;
   unsigned* h_flag = nullptr;
 };
@@ -1377,9 +1374,6 @@ int sts_batch::step_host(int n) {
       kb_warm_fit<<<dim3(1, 1, ncases), 576, 0, s>>>(G);
       kb_warm_apply<<<cell_grid, blk, 0, s>>>(G);
     } else if (warm4) {
-      kb_conv_gram<<<strip_grid, dim3(kConvStripX, kConvStripY), 0, s>>>(G);
-      kb_conv_reduce<<<seg_grid, 256, 0, s>>>(G);
-      kb_conv_solve<<<dim3(2, 1, ncases), 256, 0, s>>>(G);
       kb_conv_apply<<<cell_grid, blk, 0, s>>>(G);
     }
     if (precision == 3) kb_assemble_df<<<dim3(cell_grid.x, cell_grid.y, 3 * ncases), blk, 0, s>>>(G, 0ull, 0);
@@ -1397,6 +1391,10 @@ int sts_batch::step_host(int n) {
     if (precision == 3) kb_flux_diff_df<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
     else if (fast()) kb_flux_diff_fast<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
     else kb_flux_diff<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
+    if (warm4) {
+      kb_conv_gram<<<cell_grid, blk, 0, s>>>(G);
+      kb_conv_solve<<<dim3(2, 1, ncases), kConvSolveThreads, 0, s>>>(G);
+    }
     kb_step_end<<<dim3(1, 1, ncases), 1024, 0, s>>>(G, 0ull, 0);
     kb_continue<<<1, 256, 0, s>>>(G, ncases, 0ull, d_flag);
     CU(cudaGetLastError());
@@ -1426,12 +1424,9 @@ int sts_batch::build_graph() {
     if (int r = add_kernel(&w[2], b, {w[1]}, kb_warm_apply, cell_grid, blk, G)) return r;
     n[0] = w[2];
   } else if (warm4) {
-    cudaGraphNode_t w[4];  // hang off the step start, not the assembly
-    if (int r = add_kernel(&w[0], b, {n[0]}, kb_conv_gram, strip_grid, dim3(kConvStripX, kConvStripY), G)) return r;
-    if (int r = add_kernel(&w[1], b, {w[0]}, kb_conv_reduce, seg_grid, dim3(256), G)) return r;
-    if (int r = add_kernel(&w[2], b, {w[1]}, kb_conv_solve, dim3(2, 1, ncases), dim3(256), G)) return r;
-    if (int r = add_kernel(&w[3], b, {w[2]}, kb_conv_apply, cell_grid, blk, G)) return r;
-    conv_last = w[3];  // beside the assembly; the sweep loop waits for both
+    cudaGraphNode_t w;  // beside the assembly; the sweep loop waits for both
+    if (int r = add_kernel(&w, b, {n[0]}, kb_conv_apply, cell_grid, blk, G)) return r;
+    conv_last = w;
   }
   if (int r = add_kernel(&n[1], b, {n[0]}, precision == 3 ? kb_assemble_df : (fast() ? kb_assemble_fast : kb_assemble),
                          precision == 3 ? dim3(cell_grid.x, cell_grid.y, 3 * ncases) : cell_grid, blk, G,
@@ -1460,7 +1455,14 @@ int sts_batch::build_graph() {
                          cell_grid, blk, G,
                          (unsigned)(PH_TEMP | PH_PRES)))
     return r;
-  if (int r = add_kernel(&n[9], b, {n[8]}, kb_step_end, dim3(1, 1, ncases), dim3(1024), G, (unsigned long long)0, 0))
+  std::vector<cudaGraphNode_t> before_end{n[8]};
+  if (warm4) {  // the fit for the next step, beside the step's last kernels
+    cudaGraphNode_t w[2];
+    if (int r = add_kernel(&w[0], b, {n[2]}, kb_conv_gram, cell_grid, blk, G)) return r;
+    if (int r = add_kernel(&w[1], b, {w[0]}, kb_conv_solve, dim3(2, 1, ncases), dim3(kConvSolveThreads), G)) return r;
+    before_end.push_back(w[1]);
+  }
+  if (int r = add_kernel(&n[9], b, before_end, kb_step_end, dim3(1, 1, ncases), dim3(1024), G, (unsigned long long)0, 0))
     return r;
   if (int r = add_kernel(&n[10], b, {n[9]}, kb_continue, dim3(1), dim3(256), G, ncases, (unsigned long long)hs,
                          (unsigned*)nullptr))
@@ -1499,7 +1501,7 @@ int sts_open_batch(const char* const* case_dirs, int ncases, const sts_options* 
   b->ncases = ncases;
   std::vector<Geo> geos;
   std::vector<int> tile_case, tile_first;
-  unsigned gx = 1, gy = 1, wx = 1, tx = 1, sx = 1, sy = 1, sgx = 1;
+  unsigned gx = 1, gy = 1, wx = 1, tx = 1;
   for (int k = 0; k < ncases; k++) {
     sts_ctx* c = b->cases[k];
     geos.push_back(c->g);
@@ -1509,15 +1511,10 @@ int sts_open_batch(const char* const* case_dirs, int ncases, const sts_options* 
     gy = std::max(gy, c->grid.y);
     wx = std::max(wx, c->walls_grid().x);
     tx = std::max(tx, c->tjump_grid().x);
-    sx = std::max(sx, c->strip_grid().x);
-    sy = std::max(sy, c->strip_grid().y);
-    sgx = std::max(sgx, c->seg_grid().x);
   }
   b->ntiles = (int)tile_case.size();
   b->warm3 = opt.warm_start == 3;
   b->warm4 = opt.warm_start == 4;
-  b->strip_grid = dim3(sx, sy, (unsigned)ncases);
-  b->seg_grid = dim3(sgx, 6, (unsigned)ncases);
   if (int r = b->alloc(&b->d_geos, ncases)) return r;
   if (int r = b->alloc(&b->d_tile_case, tile_case.size())) return r;
   if (int r = b->alloc(&b->d_tile_first, tile_first.size())) return r;
