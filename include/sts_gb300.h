@@ -107,7 +107,8 @@ int sts_profile_steps(sts_ctx* ctx, int nsteps, double* kernel_ms, int* kernel_l
  * d_p_c_34 Tw_u Tw_v p_pr T_pr u_pr v_pr rho_pr (Nx*Ny doubles); hx x_v (Nx); hy y_v (Ny). */
 int sts_get_field(sts_ctx* ctx, const char* name, double* host_out);
 
-/* Overwrites u, v, p or T from host memory (Nx*Ny doubles); rho and sqrt_T follow on the next step. */
+/* Overwrites u, v, p or T from host memory (Nx*Ny doubles); rho and sqrt_T follow on the next step.
+ * With a warm start (sts_options.warm_start), setting p or T starts its history over. */
 int sts_set_field(sts_ctx* ctx, const char* name, const double* host_in);
 
 /* Mesh size. */

@@ -184,10 +184,11 @@ struct Geo {
   double *Dp[4], *DT[4];
   float* warm_part;
   // mode 4: ring of step differences per field (FP32), active-cell flags by step parity (bit 0 p,
-  // bit 1 T), per-tile (32x8) sums of the newest training pair's terms [tile][field][term] and row
+  // bit 1 T; bits 2 and 3: the stencil's start in cnext for p, T), per-tile (32x8) sums of the newest training pair's terms [tile][field][term] and row
   // counts [field][tile], sums of the last kConvWin pairs [slot][field][term]
   float* cD[2][kConvRing];
   uint8_t* cact[2];
+  double* cnext[2];  // the stencil's start for the next step, on the cells flagged for it
   float* cpart;
   int* crows;
   float* cgram;

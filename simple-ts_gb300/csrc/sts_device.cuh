@@ -40,8 +40,9 @@ __device__ __forceinline__ double div_cr(double a, double b, double y) {
 }
 
 // Convolutional warm start (warm_start 4), at the start of a step on a solved cell n holding
-// x = p_n, y = T_n: the newest step differences D (FP32, ring slot r-1) and the quadratic start
-// of warm_start 2; m receives |D| as float bit patterns for the per-field maximum.
+// x = p_n, y = T_n: the newest step differences D (FP32, ring slot r-1), the quadratic start of
+// warm_start 2, replaced by the stencil's start where the end of the previous step prepared one;
+// m receives |D| as float bit patterns for the per-field maximum.
 __device__ __forceinline__ void conv_step_begin_cell(const Geo& g, int n, unsigned cur, unsigned r, unsigned m[2]) {
   const double x = g.p[cur][n], y = g.T[cur][n];
   if (r == 0) {
@@ -64,6 +65,10 @@ __device__ __forceinline__ void conv_step_begin_cell(const Geo& g, int n, unsign
   }
   g.p_m[1][n] = g.p_m[0][n]; g.p_m[0][n] = x;
   g.T_m[1][n] = g.T_m[0][n]; g.T_m[0][n] = y;
+  // the stencil's start, prepared at the end of the previous step on the cells it flagged
+  const uint8_t b = g.cact[(r - 1) & 1][n];
+  if (b & 4u) g.p[cur][n] = g.cnext[0][n];
+  if (b & 8u) g.T[cur][n] = g.cnext[1][n];
 }
 
 // Per-field maximum of |D| over the block, folded into the step's slot (non-negative floats

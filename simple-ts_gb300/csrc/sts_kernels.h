@@ -42,16 +42,19 @@ __global__ void k_warm_apply(Geo g);
 __global__ void kb_warm_diff(const Geo* gs);
 __global__ void kb_warm_fit(const Geo* gs);
 __global__ void kb_warm_apply(const Geo* gs);
-// convolutional warm start (warm_start 4), sts_learn.cu (k_step_begin stores the differences):
-// k_conv_gram and k_conv_apply on the 32x8 cell tiles, k_conv_solve with one CTA of
-// kConvSolveThreads per field
+// convolutional warm start (warm_start 4), sts_learn.cu (k_step_begin stores the differences and
+// takes the prepared start): at the end of a step k_conv_gram -> {k_conv_solve, k_conv_next} ->
+// k_conv_predict; k_conv_gram, k_conv_next and k_conv_predict on the 32x8 cell tiles,
+// k_conv_solve with one CTA of kConvSolveThreads per field
 constexpr int kConvSolveThreads = 37 * 7;
 __global__ void k_conv_gram(Geo g);
 __global__ void k_conv_solve(Geo g);
-__global__ void k_conv_apply(Geo g);
+__global__ void k_conv_next(Geo g);
+__global__ void k_conv_predict(Geo g);
 __global__ void kb_conv_gram(const Geo* gs);
 __global__ void kb_conv_solve(const Geo* gs);
-__global__ void kb_conv_apply(const Geo* gs);
+__global__ void kb_conv_next(const Geo* gs);
+__global__ void kb_conv_predict(const Geo* gs);
 __global__ void kb_step_begin(const Geo* gs);
 __global__ void kb_set_steps(const Geo* gs, int ncases, unsigned n);
 __global__ void kb_continue(const Geo* gs, int ncases, unsigned long long h_step, unsigned* flag);

@@ -24,13 +24,14 @@
 // not depend on scheduling and the CPU oracle reproduces it bit for bit.  (GB300's FP64 pipe does
 // about 2 adds per clock per SM: the sums stay on the FP32 pipes.)
 //
-// Per step: k_step_begin stores the newest differences, writes the quadratic start and folds
-// max |D| (conv_step_begin_cell, conv_block_max); conv_apply, beside the assembly kernel (which
-// reads neither p nor T of the iterate; the sweep loop waits for both), marks the active cells and
-// writes the stencil's start there with the weights fitted at the end of the previous step; after
-// the sweeps, beside the correction and boundary kernels (which write p and T only outside the
-// solved cells), conv_gram forms the newest training pair's terms per tile and conv_solve sums
-// them into the window and solves for the next step's weights.
+// Per step: k_step_begin stores the newest differences, writes the quadratic start, takes the
+// stencil's start where one was prepared, and clears the coming maximum (conv_step_begin_cell,
+// conv_block_max).  After the sweeps, beside the correction and boundary kernels (which write p
+// and T only outside the solved cells; the step ends when both are done): conv_gram forms the
+// terms of the training pair whose target is the coming difference, conv_solve fits the weights,
+// conv_next stores the coming difference and its maximum, and conv_predict flags the active cells
+// and prepares the next step's start there -- everything the next step's start needs, computed
+// from the final iterate while the GPU is mostly idle.
 #include <cuda_runtime.h>
 
 #include "sts_common.cuh"
@@ -136,6 +137,10 @@ __device__ __forceinline__ void neumaier(float& s, float& c, float x) {
 __device__ __forceinline__ void conv_gram_body(const Geo& g) {
   const Ctl* ctl = g.ctl;
   const unsigned r = ctl->warm_ready, cur = ctl->cur;
+  // conv_next folds the coming difference's maximum once this kernel is done (with several
+  // outer iterations, only the last one's counts)
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < 2 && threadIdx.y == 0)
+    const_cast<Ctl*>(ctl)->conv_max[r & 1][threadIdx.x] = 0u;
   if (r < 4) return;  // the features need four stored differences
   const unsigned h = r - 1;
   const int Nx = g.Nx, Ny = g.Ny;
@@ -356,14 +361,48 @@ __device__ __forceinline__ void conv_solve_body(const Geo& g) {
   }
 }
 
-// Per 32x8 tile: the active flags of the newest difference (cells within kConvReach steps of a
-// source, |D_h| > kConvAlpha max |D_h|; x wrapped on periodic meshes), then on the active cells
-// the stencil's start x_h + sum_k w_k feature_k.
-__device__ __forceinline__ void conv_apply_body(const Geo& g) {
+// End of a step, all cells: the coming difference D_r = x_{n+1} - x_n (FP32; 0 off the solved
+// cells) into its ring slot -- the value the next step's start stores there again -- and its
+// per-field maximum (cleared by conv_gram) for the active flags.
+__device__ __forceinline__ void conv_next_body(const Geo& g) {
+  Cell c = cell(g);
   const Ctl* ctl = g.ctl;
   const unsigned r = ctl->warm_ready, cur = ctl->cur;
-  if (r < 1 || ctl->Iter != 0) return;  // the step's first outer iteration only
-  const unsigned h = r - 1;
+  unsigned m[2] = {0u, 0u};
+  if (c.ok) {
+    const int n = c.ij;
+    float d[2] = {0.f, 0.f};
+    if (solved_cell(g, n)) {
+      d[0] = (float)(g.p[cur][n] - g.p_m[0][n]);
+      d[1] = (float)(g.T[cur][n] - g.T_m[0][n]);
+      m[0] = __float_as_uint(fabsf(d[0]));
+      m[1] = __float_as_uint(fabsf(d[1]));
+    }
+    g.cD[0][r % kConvRing][n] = d[0];
+    g.cD[1][r % kConvRing][n] = d[1];
+  }
+  __shared__ unsigned wm[2][32];
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int nw = (blockDim.x * blockDim.y + 31) >> 5;
+  for (int f = 0; f < 2; f++) {
+    const unsigned v = __reduce_max_sync(0xffffffffu, m[f]);
+    if (lane == 0) wm[f][warp] = v;
+  }
+  __syncthreads();
+  if (tid < 2) {
+    unsigned v = 0;
+    for (int w = 0; w < nw; w++) v = max(v, wm[tid][w]);
+    if (v) atomicMax(&g.ctl->conv_max[r & 1][tid], v);
+  }
+}
+
+// End of a step, per 32x8 tile: the active flags of the coming difference D_r (cells within
+// kConvReach steps of a source, |D_r| > kConvAlpha max |D_r|; x wrapped on periodic meshes), and
+// on the active cells, with the weights just fitted, the stencil's start for the next step,
+// x_{n+1} + sum_k w_k feature_k, kept in cnext and flagged for k_step_begin (bits 2 and 3).
+__device__ __forceinline__ void conv_predict_body(const Geo& g) {
+  const Ctl* ctl = g.ctl;
+  const unsigned r = ctl->warm_ready, cur = ctl->cur;
   const int Nx = g.Nx, Ny = g.Ny;
   constexpr int TX = 32, TY = 8, R = kConvReach, HX = TX + 2 * R, HY = TY + 2 * R;
   const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
@@ -379,13 +418,13 @@ __device__ __forceinline__ void conv_apply_body(const Geo& g) {
     const int yy = rem / HX, xx = rem - yy * HX, jj = j0 - R + yy;
     int ii = i0 - R + xx;
     if (per) ii = (ii + Nx) % Nx;
-    return (jj >= 0 && jj < Ny && ii >= 0 && ii < Nx) ? g.cD[f][h % kConvRing][ii + jj * Nx] : 0.f;
+    return (jj >= 0 && jj < Ny && ii >= 0 && ii < Nx) ? g.cD[f][r % kConvRing][ii + jj * Nx] : 0.f;
   });
   __syncthreads();
   unsigned bits = 0;
   if (in && solved_cell(g, n)) {
-    const float thr0 = kConvAlpha * __uint_as_float(ctl->conv_max[h & 1][0]);
-    const float thr1 = kConvAlpha * __uint_as_float(ctl->conv_max[h & 1][1]);
+    const float thr0 = kConvAlpha * __uint_as_float(ctl->conv_max[r & 1][0]);
+    const float thr1 = kConvAlpha * __uint_as_float(ctl->conv_max[r & 1][1]);
     for (int dj = -R; dj <= R; dj++) {
       const int rx = R - (dj < 0 ? -dj : dj);
       for (int di = -rx; di <= rx; di++) {
@@ -395,9 +434,9 @@ __device__ __forceinline__ void conv_apply_body(const Geo& g) {
       }
     }
   }
-  if (in) g.cact[h & 1][n] = (uint8_t)bits;
-  const unsigned use = (ctl->conv_ok[0] ? 1u : 0u) | (ctl->conv_ok[1] ? 2u : 0u);
-  if (!__syncthreads_or((bits & use) != 0u)) return;
+  const unsigned use = bits & ((ctl->conv_ok[0] ? 1u : 0u) | (ctl->conv_ok[1] ? 2u : 0u));
+  if (in) g.cact[r & 1][n] = (uint8_t)(bits | (use << 2));
+  if (!__syncthreads_or(use != 0u)) return;
   // the four newest differences over the tile and a margin of one (clamped to the mesh)
   __shared__ float Dt[2][4][TY + 2][TX + 2];
   stage<2 * 4 * (TY + 2) * (TX + 2), TX * TY>(&Dt[0][0][0][0], tid, [&](int k) {
@@ -405,18 +444,17 @@ __device__ __forceinline__ void conv_apply_body(const Geo& g) {
     const int t = rem / ((TY + 2) * (TX + 2)), rem2 = rem - t * ((TY + 2) * (TX + 2));
     const int yy = rem2 / (TX + 2), xx = rem2 - yy * (TX + 2);
     const int jj = min(max(j0 - 1 + yy, 0), Ny - 1), ii = min(max(i0 - 1 + xx, 0), Nx - 1);
-    return g.cD[f][(h - t) % kConvRing][ii + jj * Nx];
+    return g.cD[f][(r - t) % kConvRing][ii + jj * Nx];
   });
   __syncthreads();
   for (int f = 0; f < 2; f++) {
-    if (!((bits & use) >> f & 1u)) continue;
+    if (!((use >> f) & 1u)) continue;
     float feat[kConvFeat];
     const int x0 = threadIdx.x + 1, y0 = threadIdx.y + 1;
     conv_features_from([&](int k, int dj, int di) { return Dt[f][k][y0 + dj][x0 + di]; }, feat);
     float corr = 0.f;
     for (int k = 0; k < kConvFeat; k++) corr = corr + ctl->conv_w[f][k] * feat[k];
-    if (f == 0) g.p[cur][n] = g.p_m[0][n] + (double)corr;
-    else g.T[cur][n] = g.T_m[0][n] + (double)corr;
+    g.cnext[f][n] = (f == 0 ? g.p[cur][n] : g.T[cur][n]) + (double)corr;
   }
 }
 
@@ -424,7 +462,8 @@ __device__ __forceinline__ void conv_apply_body(const Geo& g) {
 
 __global__ void k_conv_gram(Geo g) { conv_gram_body(g); }
 __global__ void k_conv_solve(Geo g) { conv_solve_body(g); }
-__global__ void k_conv_apply(Geo g) { conv_apply_body(g); }
+__global__ void k_conv_next(Geo g) { conv_next_body(g); }
+__global__ void k_conv_predict(Geo g) { conv_predict_body(g); }
 __global__ void kb_conv_gram(const Geo* gs) {
   __shared__ Geo sg;
   if (!stage_geo(sg, gs)) return;
@@ -435,10 +474,15 @@ __global__ void kb_conv_solve(const Geo* gs) {
   if (!stage_geo(sg, gs)) return;
   conv_solve_body(sg);
 }
-__global__ void kb_conv_apply(const Geo* gs) {
+__global__ void kb_conv_next(const Geo* gs) {
   __shared__ Geo sg;
   if (!stage_geo(sg, gs)) return;
-  conv_apply_body(sg);
+  conv_next_body(sg);
+}
+__global__ void kb_conv_predict(const Geo* gs) {
+  __shared__ Geo sg;
+  if (!stage_geo(sg, gs)) return;
+  conv_predict_body(sg);
 }
 
 }  // namespace sts

@@ -138,19 +138,17 @@ struct sts_ctx {
       k_warm_fit<<<1, 576, 0, s>>>(g);
       k_warm_apply<<<grid, block, 0, s>>>(g);
       mark(0);
-    } else if (g.warm_start == 4) {
-      mark(-1);
-      k_conv_apply<<<grid, block, 0, s>>>(g);
-      mark(0);
     }
   }
-  // warm_start 4: the fit for the next step's start, once the step's iterate is final
+  // warm_start 4: the fit and the next step's start, once the step's iterate is final
   template <class M>
   void warm_train(M mark) {
     if (g.warm_start != 4) return;
     mark(-1);
     k_conv_gram<<<grid, block, 0, s>>>(g);
     k_conv_solve<<<2, kConvSolveThreads, 0, s>>>(g);
+    k_conv_next<<<grid, block, 0, s>>>(g);
+    k_conv_predict<<<grid, block, 0, s>>>(g);
     mark(0);
   }
   bool fast() const { return g.precision >= 1; }
@@ -266,11 +264,7 @@ int sts_ctx::build_graph() {
     return r;
   // warm_start 4: the predictor's kernels (first outer iteration only) beside the assembly
   std::vector<cudaGraphNode_t> before_sweeps{n_asm};
-  if (g.warm_start == 4) {
-    cudaGraphNode_t w;
-    if (int r = add_kernel(&w, b_outer, {}, k_conv_apply, grid, block, g)) return r;
-    before_sweeps.push_back(w);
-  }
+
   if (int r = add_kernel(&n_sw, b_outer, before_sweeps, pt_kernel(), pt_grid, dim3(32, 8), g, ntiles, d_lc)) return r;
   {
     cudaLaunchAttributeValue v{};
@@ -278,10 +272,12 @@ int sts_ctx::build_graph() {
     CU(cudaGraphKernelNodeSetAttribute(n_sw, cudaLaunchAttributeCooperative, &v));
   }
   if (int r = add_kernel(&n_cor, b_outer, {n_sw}, k_correct, grid, block, g)) return r;
-  if (g.warm_start == 4) {  // the fit for the next step, beside the step's last kernels
-    cudaGraphNode_t w[2];
+  if (g.warm_start == 4) {  // the fit and the next step's start, beside the step's last kernels
+    cudaGraphNode_t w[4];
     if (int r = add_kernel(&w[0], b_outer, {n_sw}, k_conv_gram, grid, block, g)) return r;
     if (int r = add_kernel(&w[1], b_outer, {w[0]}, k_conv_solve, dim3(2), dim3(kConvSolveThreads), g)) return r;
+    if (int r = add_kernel(&w[2], b_outer, {w[0]}, k_conv_next, grid, block, g)) return r;
+    if (int r = add_kernel(&w[3], b_outer, {w[1], w[2]}, k_conv_predict, grid, block, g)) return r;
   }
   if (int r = add_kernel(&n_rho, b_outer, {n_cor}, k_face_rho, grid, block, g)) return r;
   cudaGraphNode_t n_walls, n_tj;
@@ -841,8 +837,10 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
     for (int f = 0; f < 2; f++)
       for (int k = 0; k < kConvRing; k++)
         if (int r = c->alloc(&g.cD[f][k], Na)) return r;
-    for (int k = 0; k < 2; k++)
+    for (int k = 0; k < 2; k++) {
       if (int r = c->alloc(&g.cact[k], Na)) return r;
+      if (int r = c->alloc(&g.cnext[k], Na)) return r;
+    }
     const size_t nt = (size_t)((h.Nx + 31) / 32) * ((h.Ny + 7) / 8);
     if (int r = c->alloc(&g.cpart, nt * 2 * kConvTerms)) return r;
     if (int r = c->alloc(&g.crows, nt * 2)) return r;
@@ -1074,6 +1072,11 @@ int sts_set_field(sts_ctx* ctx, const char* name, const double* in) {
   else if (n == "T") dst = g.T[cur];
   if (!dst) return fail(STS_ERR_ARG, "field cannot be set: " + n);
   CU(cudaMemcpyAsync(dst, in, sizeof(double) * g.Na, cudaMemcpyHostToDevice, ctx->s));
+  if (g.warm_start && (n == "p" || n == "T")) {
+    // the warm start's history no longer describes the state: it starts over
+    static const unsigned zero = 0;
+    CU(cudaMemcpyAsync(&g.ctl->warm_ready, &zero, sizeof(unsigned), cudaMemcpyHostToDevice, ctx->s));
+  }
   CU(cudaStreamSynchronize(ctx->s));
   return STS_OK;
 }
@@ -1373,8 +1376,6 @@ int sts_batch::step_host(int n) {
       kb_warm_diff<<<cell_grid, blk, 0, s>>>(G);
       kb_warm_fit<<<dim3(1, 1, ncases), 576, 0, s>>>(G);
       kb_warm_apply<<<cell_grid, blk, 0, s>>>(G);
-    } else if (warm4) {
-      kb_conv_apply<<<cell_grid, blk, 0, s>>>(G);
     }
     if (precision == 3) kb_assemble_df<<<dim3(cell_grid.x, cell_grid.y, 3 * ncases), blk, 0, s>>>(G, 0ull, 0);
     else if (fast()) kb_assemble_fast<<<cell_grid, blk, 0, s>>>(G, 0ull, 0);
@@ -1394,6 +1395,8 @@ int sts_batch::step_host(int n) {
     if (warm4) {
       kb_conv_gram<<<cell_grid, blk, 0, s>>>(G);
       kb_conv_solve<<<dim3(2, 1, ncases), kConvSolveThreads, 0, s>>>(G);
+      kb_conv_next<<<cell_grid, blk, 0, s>>>(G);
+      kb_conv_predict<<<cell_grid, blk, 0, s>>>(G);
     }
     kb_step_end<<<dim3(1, 1, ncases), 1024, 0, s>>>(G, 0ull, 0);
     kb_continue<<<1, 256, 0, s>>>(G, ncases, 0ull, d_flag);
@@ -1416,25 +1419,18 @@ int sts_batch::build_graph() {
   const Geo* G = d_geos;
   cudaGraphNode_t n[11];
   if (int r = add_kernel(&n[0], b, {}, kb_step_begin, cell_grid, blk, G)) return r;
-  cudaGraphNode_t conv_last = nullptr;
   if (warm3) {
     cudaGraphNode_t w[3];
     if (int r = add_kernel(&w[0], b, {n[0]}, kb_warm_diff, cell_grid, blk, G)) return r;
     if (int r = add_kernel(&w[1], b, {w[0]}, kb_warm_fit, dim3(1, 1, ncases), dim3(576), G)) return r;
     if (int r = add_kernel(&w[2], b, {w[1]}, kb_warm_apply, cell_grid, blk, G)) return r;
     n[0] = w[2];
-  } else if (warm4) {
-    cudaGraphNode_t w;  // beside the assembly; the sweep loop waits for both
-    if (int r = add_kernel(&w, b, {n[0]}, kb_conv_apply, cell_grid, blk, G)) return r;
-    conv_last = w;
   }
   if (int r = add_kernel(&n[1], b, {n[0]}, precision == 3 ? kb_assemble_df : (fast() ? kb_assemble_fast : kb_assemble),
                          precision == 3 ? dim3(cell_grid.x, cell_grid.y, 3 * ncases) : cell_grid, blk, G,
                          (unsigned long long)0, 0))
     return r;
-  std::vector<cudaGraphNode_t> before_sweeps{n[1]};
-  if (conv_last) before_sweeps.push_back(conv_last);
-  if (int r = add_kernel(&n[2], b, before_sweeps, pt_kernel(), pt_grid, blk, G, (const int*)d_tile_case,
+  if (int r = add_kernel(&n[2], b, {n[1]}, pt_kernel(), pt_grid, blk, G, (const int*)d_tile_case,
                          (const int*)d_tile_first, ncases, ntiles, d_lc))
     return r;
   {
@@ -1456,11 +1452,13 @@ int sts_batch::build_graph() {
                          (unsigned)(PH_TEMP | PH_PRES)))
     return r;
   std::vector<cudaGraphNode_t> before_end{n[8]};
-  if (warm4) {  // the fit for the next step, beside the step's last kernels
-    cudaGraphNode_t w[2];
+  if (warm4) {  // the fit and the next step's start, beside the step's last kernels
+    cudaGraphNode_t w[4];
     if (int r = add_kernel(&w[0], b, {n[2]}, kb_conv_gram, cell_grid, blk, G)) return r;
     if (int r = add_kernel(&w[1], b, {w[0]}, kb_conv_solve, dim3(2, 1, ncases), dim3(kConvSolveThreads), G)) return r;
-    before_end.push_back(w[1]);
+    if (int r = add_kernel(&w[2], b, {w[0]}, kb_conv_next, cell_grid, blk, G)) return r;
+    if (int r = add_kernel(&w[3], b, {w[1], w[2]}, kb_conv_predict, cell_grid, blk, G)) return r;
+    before_end.push_back(w[3]);
   }
   if (int r = add_kernel(&n[9], b, before_end, kb_step_end, dim3(1, 1, ncases), dim3(1024), G, (unsigned long long)0, 0))
     return r;
