@@ -1033,7 +1033,10 @@ int sts_profile_steps(sts_ctx* ctx, int nsteps, double* kernel_ms, int* kernel_l
 int sts_get_field(sts_ctx* ctx, const char* name, double* out) {
   if (!ctx || !name || !out) return fail(STS_ERR_ARG, "null argument");
   CU(cudaSetDevice(ctx->opt.device));
-  if (int r = ctx->read_ctl()) return r;
+  // which p/T buffer is current: every step of a single context ends with its control block read
+  // back; a batch's case is refreshed here
+  if (ctx->in_batch)
+    if (int r = ctx->read_ctl()) return r;
   const Geo& g = ctx->g;
   const std::string n(name);
   const unsigned cur = ctx->h_ctl->cur;
@@ -1061,7 +1064,8 @@ int sts_get_field(sts_ctx* ctx, const char* name, double* out) {
 int sts_set_field(sts_ctx* ctx, const char* name, const double* in) {
   if (!ctx || !name || !in) return fail(STS_ERR_ARG, "null argument");
   CU(cudaSetDevice(ctx->opt.device));
-  if (int r = ctx->read_ctl()) return r;
+  if (ctx->in_batch)
+    if (int r = ctx->read_ctl()) return r;
   const Geo& g = ctx->g;
   const std::string n(name);
   const unsigned cur = ctx->h_ctl->cur;
