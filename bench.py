@@ -241,10 +241,13 @@ def config(case, Nx, Ny):
 
 
 def timed_steps(s, steps, warmup, flush, barrier, clocks=None):
-    """Warm-up, then `steps` steps each after an L2 flush; device ms from CUDA events on the
-    library's stream.  Returns (steps done, total device ms, sweeps of the timed steps)."""
+    """Autotuning steps and warm-up, then `steps` steps each after an L2 flush; device ms from CUDA
+    events on the library's stream.  Returns (steps done, total device ms, sweeps of the timed
+    steps)."""
     import torch
-    for _ in range(max(warmup, 3)):
+    # the autotuner's steps (real steps, launched kernel by kernel) come before the warm-up
+    pre = max(warmup, 3) + s.autotune_result()["steps_left"]
+    for _ in range(pre):
         s.step(1)
     s.sync()
     barrier()
@@ -258,6 +261,7 @@ def timed_steps(s, steps, warmup, flush, barrier, clocks=None):
             total_ms += ms
             done += n
     barrier()
+    s.steps_before_timing = pre
     return done, total_ms, (s.sweep_history()[-done:] if done else [])
 
 
@@ -358,7 +362,7 @@ def checkpoint_bench(d, local, barrier, every=10, saves=10):
     import sts
     ms = {}
     for mode in ("no_saves", "sync", "async"):
-        s = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=sts.EXACT)
+        s = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=sts.EXACT, autotune=False)
         s.step(3)
         if mode != "no_saves":
             s.write_outputs()  # the first save makes the snapshot buffers and the writer thread
@@ -436,6 +440,7 @@ def main():
     Na = Nx * Ny
     with Clocks(local) as clk:
         done, total_ms, sweeps = timed_steps(s, args.steps, args.warmup, flush, barrier)
+    launch_shapes = s.autotune_result()
     total_ms = slowest(total_ms, world)
     value = job_rate(Na * done, world, total_ms / 1e3)
 
@@ -480,14 +485,20 @@ def main():
     # the same number of steps
     variants = {}
     if args.variants:
-        ref = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=sts.EXACT)
         w = max(args.warmup, 3)
-        ref.step(w + args.steps)
-        base = {w: {f: ref.field(f) for f in ("u", "v", "p", "T", "rho")}}
         lead_w = max(args.warm_lead, w)
-        ref.step(lead_w - w)
-        base[lead_w] = {f: ref.field(f) for f in ("u", "v", "p", "T", "rho")}
-        ref.close()
+        base = {}
+
+        def base_at(n):
+            """The bit-exact path's fields after n steps (launch shapes do not change them)."""
+            if n not in base:
+                ref = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=sts.EXACT,
+                                 autotune=False)
+                ref.step(n)
+                base[n] = {f: ref.field(f) for f in ("u", "v", "p", "T", "rho")}
+                ref.close()
+            return base[n]
+
         for name, prec, warm in (("fp64_fast", sts.FAST_FP64, 0), ("fp32_corrections", sts.MIXED, 0),
                                  ("fp32_corrections_df", sts.MIXED_DF, 0), ("fp32_corrections_df_warm2", sts.MIXED_DF, 2),
                                  ("fp64_exact_warm2", sts.EXACT, 2), ("fp32_corrections_warm2", sts.MIXED, 2),
@@ -496,11 +507,12 @@ def main():
             v = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=prec, warm_start=warm)
             lead = lead_w if warm else w
             vd, vms, vsw = timed_steps(v, args.steps, lead, flush, barrier)
-            ref_f = base[lead]
+            ref_f = base_at(v.steps_before_timing + vd)
             err = {f: float(np.linalg.norm(v.field(f) - ref_f[f]) / np.linalg.norm(ref_f[f])) for f in ref_f}
             vpn, vkms, vkcnt = v.profile(max(3, min(args.steps, 10)))
             variants[name] = {
-                "precision_mode": prec, "warm_start": warm, "untimed_steps": lead, "value": Na * vd * world / (vms / 1e3),
+                "precision_mode": prec, "warm_start": warm, "untimed_steps": v.steps_before_timing,
+                "value": Na * vd * world / (vms / 1e3),
                 "ms_per_step": vms / max(vd, 1),
                 "speedup_vs_fp64": (Na * vd / (vms / 1e3)) / (Na * done / (total_ms / 1e3)) if done else None,
                 "rel_l2_vs_fp64": err,
@@ -510,6 +522,17 @@ def main():
             v.close()
 
     ckpt = checkpoint_bench(d, local, barrier) if args.variants else None
+
+    # the FP64 bit-exact path with the default launch shapes (no autotuning), beside the headline,
+    # which uses the shapes the autotuner chose on the run's first steps (the shapes change no result)
+    tuned = None
+    if args.variants:
+        t = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=sts.EXACT, autotune=False)
+        td, tms, tsw = timed_steps(t, args.steps, args.warmup, flush, barrier)
+        tuned = {"value": Na * td * world / (tms / 1e3), "ms_per_step": tms / max(td, 1),
+                 "sweeps_per_step": float(np.mean(tsw)) if len(tsw) else 0.0,
+                 "launch_shapes": t.autotune_result()}
+        t.close()
 
     if rank == 0:
         cpu = cpu_baseline(d, args.cpu_seconds, start_steps=0)
@@ -522,7 +545,7 @@ def main():
                                     "max": int(max(sweeps)) if len(sweeps) else 0},
                 "variants": variants,
                 "warm_start_vs_plain": warm_summary(value, sweeps, variants),
-                "checkpoint": ckpt}
+                "checkpoint": ckpt, "untuned_fp64": tuned, "launch_shapes": launch_shapes}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

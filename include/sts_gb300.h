@@ -74,10 +74,16 @@ typedef struct sts_options {
    *    the run still returns only after every file is complete (default);
    * 0: each save is on disk before stepping resumes, as in the reference. */
   int async_save;
+  /* 1: the first steps of the run choose the launch shapes -- the sweep loop's CTAs per SM and the
+   *    assembly kernel's block shape -- by timing each candidate on real steps launched kernel by
+   *    kernel (1 + 2 x max(CTAs per SM that fit, 3) steps); results do not depend on launch shapes,
+   *    so the run is the same bit for bit; the graph is built with the chosen shapes (default);
+   * 0: the largest number of CTAs that fit and 32x8 blocks. */
+  int autotune;
 } sts_options;
 
 /* Fills *opt with the defaults (fixed_sweeps 1, use_graph 1, device 0, write_files 1, precision 0,
- * warm_start 0, async_save 1). */
+ * warm_start 0, async_save 1, autotune 1). */
 void sts_default_options(sts_options* opt);
 
 /* Reads a case directory (EnteredData.txt, solve_*_b.txt, restart dumps when
@@ -138,6 +144,10 @@ int sts_write_outputs_async(sts_ctx* ctx);
 
 /* Waits until every save of the context is on disk; returns the first error among them. */
 int sts_wait_outputs(sts_ctx* ctx);
+
+/* The launch shapes in use: tuning steps still to come (sts_options.autotune), the sweep loop's
+ * CTAs per SM and the assembly kernel's block (x, y).  No counterpart in the reference. */
+int sts_autotune_result(sts_ctx* ctx, int* steps_left, int* ctas_per_sm, int* asm_block_x, int* asm_block_y);
 
 /* Whole drop-in run of a case directory: open, step until the run ends, with the
  * periodic saves and logs of the reference (Tmp.txt, Iterations_in_loops.txt), and the

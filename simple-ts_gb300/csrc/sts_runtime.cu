@@ -153,12 +153,32 @@ struct sts_ctx {
   }
   bool fast() const { return g.precision >= 1; }
   bool mixed() const { return g.precision >= 2 && !(hc.bits & F_FIXED_SWEEPS); }
+  // launch shapes (neither changes any result: every cell is computed on its own and the residual
+  // reductions are maxima): the assembly kernel's block and the sweep loop's CTAs per SM, chosen
+  // by the autotuner from the run's first steps
+  dim3 asm_block{32, 8, 1};
+  int sms = 0, pt_per_sm_max = 0, pt_per_sm = 0;  // pt_per_sm 0: as many as fit
+  struct TuneStat {
+    double ms = 0, sweeps = 0;
+    int n = 0;
+  };
+  static constexpr int kTuneRounds = 2;
+  int tune_left = 0, tune_idx = 0;
+  std::vector<TuneStat> tune_pt, tune_asm;
+  static dim3 asm_shape(int k) {
+    static const dim3 shapes[3] = {dim3(32, 8), dim3(64, 4), dim3(128, 2)};
+    return shapes[k];
+  }
+  int tune_step(int* done);
+  void tune_choose();
   using AsmKernel = void (*)(Geo, unsigned long long, int);
   using FluxKernel = void (*)(Geo, unsigned);
   AsmKernel asm_kernel() const {
     return g.precision == 3 ? k_assemble_df : (fast() ? k_assemble_fast : k_assemble);
   }
-  dim3 asm_grid() const { return g.precision == 3 ? dim3(grid.x, grid.y, 3) : grid; }
+  dim3 asm_grid() const {
+    return dim3((g.Nx + asm_block.x - 1) / asm_block.x, (g.Ny + asm_block.y - 1) / asm_block.y, g.precision == 3 ? 3 : 1);
+  }
   FluxKernel flux_kernel() const {
     return g.precision == 3 ? k_flux_diff_df : (fast() ? k_flux_diff_fast : k_flux_diff);
   }
@@ -170,12 +190,14 @@ struct sts_ctx {
   }
   dim3 pt_grid;
   int size_pt_grid() {
-    int dev = 0, sms = 0, per_sm = 0;
+    int dev = 0, per_sm = 0;
     CU(cudaGetDevice(&dev));
     CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pt_kernel(), 256, 0));
     if (per_sm < 1) return fail(STS_ERR_CUDA, "the sweep-loop kernel does not fit on a multiprocessor");
-    pt_grid = dim3((unsigned)std::max(1, std::min(ntiles, per_sm * sms)));
+    pt_per_sm_max = per_sm;
+    const int use = (pt_per_sm > 0 && pt_per_sm <= per_sm) ? pt_per_sm : per_sm;
+    pt_grid = dim3((unsigned)std::max(1, std::min(ntiles, use * sms)));
     return STS_OK;
   }
   // the sweep loop of one outer iteration outside the graph: one cooperative launch
@@ -259,7 +281,7 @@ int sts_ctx::build_graph() {
   if (int r = add_kernel(&n_end, b_step, {n_outer}, k_step_end, dim3(1), dim3(1024), g, (unsigned long long)hs, 1))
     return r;
   cudaGraphNode_t n_asm, n_sw, n_cor, n_rho, n_bnd, n_fd;
-  if (int r = add_kernel(&n_asm, b_outer, {}, asm_kernel(), asm_grid(), block, g,
+  if (int r = add_kernel(&n_asm, b_outer, {}, asm_kernel(), asm_grid(), asm_block, g,
                          (unsigned long long)0, 0))
     return r;
   // warm_start 4: the predictor's kernels (first outer iteration only) beside the assembly
@@ -318,7 +340,7 @@ int sts_ctx::step_host(int n, int* done) {
     k_step_begin<<<grid, block, 0, s>>>(g, 1, 0, 0);
     warm_launches([](int) {});
     for (int outer = 0; outer < NI; outer++) {
-      asm_kernel()<<<asm_grid(), block, 0, s>>>(g, 0, 0);
+      asm_kernel()<<<asm_grid(), asm_block, 0, s>>>(g, 0, 0);
       if (int r = pt_loop()) return r;
       k_correct<<<grid, block, 0, s>>>(g);
       k_face_rho<<<grid, block, 0, s>>>(g);
@@ -339,6 +361,84 @@ int sts_ctx::step_host(int n, int* done) {
   }
   *done = k;
   return STS_OK;
+}
+
+// One step launched kernel by kernel for the autotuner: the step's assembly kernels run with the
+// block shape of candidate tune_idx % 3 and its sweep loops with tune_idx % per_sm_max + 1 CTAs per
+// SM; event pairs time both.  The step is a real step (launch shapes do not change results).
+int sts_ctx::tune_step(int* done) {
+  const int NI = (int)hc.cfg.n("N_I");
+  const int npt = (int)tune_pt.size(), nasm = (int)tune_asm.size();
+  const bool record = tune_idx >= 0;  // index -1: one warm-up step, not recorded
+  const int pc = record ? tune_idx % npt : npt - 1, ac = record ? tune_idx % nasm : 0;
+  asm_block = asm_shape(ac);
+  pt_per_sm = pc + 1;
+  if (int r = size_pt_grid()) return r;
+  std::vector<cudaEvent_t> ev;
+  auto mark = [&]() {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, s);
+    ev.push_back(e);
+  };
+  k_step_begin<<<grid, block, 0, s>>>(g, 1, 0, 0);
+  warm_launches([](int) {});
+  int outer = 0;
+  for (; outer < NI; outer++) {
+    mark();
+    asm_kernel()<<<asm_grid(), asm_block, 0, s>>>(g, 0, 0);
+    mark();
+    if (int r = pt_loop()) return r;
+    mark();
+    k_correct<<<grid, block, 0, s>>>(g);
+    k_face_rho<<<grid, block, 0, s>>>(g);
+    boundary_step([](int) {});
+    if (NI > 1) {
+      if (int r = read_ctl()) return r;
+      if (!h_ctl->continue_iter) {
+        outer++;
+        break;
+      }
+    }
+  }
+  warm_train([](int) {});
+  k_step_end<<<1, 1024, 0, s>>>(g, 0, 0);
+  if (int r = check()) return r;
+  if (int r = read_ctl()) return r;
+  double t_asm = 0, t_pt = 0;
+  for (size_t k = 0; k + 2 < ev.size(); k += 3) {
+    float a = 0, b = 0;
+    cudaEventElapsedTime(&a, ev[k], ev[k + 1]);
+    cudaEventElapsedTime(&b, ev[k + 1], ev[k + 2]);
+    t_asm += a;
+    t_pt += b;
+  }
+  for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  if (record) {
+    tune_asm[ac].ms += t_asm;
+    tune_asm[ac].n += outer;
+    tune_pt[pc].ms += t_pt;
+    tune_pt[pc].sweeps += h_ctl->step_sweeps;
+    tune_pt[pc].n += 1;
+  }
+  tune_idx++;
+  if (--tune_left == 0) tune_choose();
+  *done = 1;
+  return STS_OK;
+}
+
+// The fastest block shape per assembly launch and CTAs per SM per sweep; the graph, built after
+// the tuning steps, uses them.
+void sts_ctx::tune_choose() {
+  int best_a = 0, best_p = (int)tune_pt.size() - 1;
+  for (int k = 0; k < (int)tune_asm.size(); k++)
+    if (tune_asm[k].n && tune_asm[k].ms / tune_asm[k].n < tune_asm[best_a].ms / std::max(tune_asm[best_a].n, 1)) best_a = k;
+  auto per_sweep = [&](int k) { return tune_pt[k].sweeps > 0 ? tune_pt[k].ms / tune_pt[k].sweeps : 1e30; };
+  for (int k = 0; k < (int)tune_pt.size(); k++)
+    if (per_sweep(k) < per_sweep(best_p)) best_p = k;
+  asm_block = asm_shape(best_a);
+  pt_per_sm = best_p + 1;
+  size_pt_grid();
 }
 
 // The launch loop with a CUDA event pair around every kernel: per-kernel device time.
@@ -362,7 +462,7 @@ int sts_ctx::profile(int n, double* ms, int* cnt, int* done) {
     warm_launches(mark);
     for (int outer = 0; outer < NI; outer++) {
       mark(-1);
-      asm_kernel()<<<asm_grid(), block, 0, s>>>(g, 0, 0);
+      asm_kernel()<<<asm_grid(), asm_block, 0, s>>>(g, 0, 0);
       mark(1);
       mark(-1);
       if (int r = pt_loop()) return r;
@@ -910,6 +1010,12 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
     }
   }
   if (int r = c->size_pt_grid()) return r;
+  if (opt.autotune) {
+    c->tune_pt.assign(c->pt_per_sm_max, sts_ctx::TuneStat{});
+    c->tune_asm.assign(3, sts_ctx::TuneStat{});
+    c->tune_idx = -1;  // one warm-up step first
+    c->tune_left = 1 + sts_ctx::kTuneRounds * std::max(c->pt_per_sm_max, 3);
+  }
   const dim3 G = c->grid, B = c->block;
   cudaStream_t s = c->s;
 
@@ -956,6 +1062,7 @@ void sts_default_options(sts_options* opt) {
   opt->precision = 0;
   opt->warm_start = 0;
   opt->async_save = 1;
+  opt->autotune = 1;
 }
 
 int sts_open_case(const char* case_dir, const sts_options* opt, sts_ctx** out) {
@@ -975,8 +1082,20 @@ int sts_step(sts_ctx* ctx, int nsteps, int* steps_done) {
   if (!ctx->finished && nsteps > 0) {
     CU(cudaSetDevice(ctx->opt.device));
     const unsigned status_before = ctx->h_ctl->status;
-    int r = ctx->opt.use_graph ? ctx->step_graph(nsteps, &done) : ctx->step_host(nsteps, &done);
-    if (r) return r;
+    // the autotuner's steps come first (real steps, launched kernel by kernel)
+    while (ctx->tune_left > 0 && done < nsteps && !ctx->finished) {
+      int d = 0;
+      if (int r = ctx->tune_step(&d)) return r;
+      done += d;
+      if (!ctx->h_ctl->continue_step) ctx->finished = true;
+      if (ctx->h_ctl->status & (ST_BARRIER_TIMEOUT | ST_NONFINITE)) break;
+    }
+    if (done < nsteps && !ctx->finished && !(ctx->h_ctl->status & ~status_before & (ST_BARRIER_TIMEOUT | ST_NONFINITE))) {
+      int d = 0;
+      int r = ctx->opt.use_graph ? ctx->step_graph(nsteps - done, &d) : ctx->step_host(nsteps - done, &d);
+      if (r) return r;
+      done += d;
+    }
     if (!ctx->h_ctl->continue_step) ctx->finished = true;
     if (ctx->h_ctl->status & ST_BARRIER_TIMEOUT) {
       ctx->finished = true;  // the device state is no longer consistent
@@ -1110,6 +1229,15 @@ int sts_sweep_history(sts_ctx* ctx, unsigned int* out, int cap, int* n_out) {
   const unsigned n = (unsigned)cap < avail ? (unsigned)cap : avail;
   for (unsigned k = 0; k < n; k++) out[k] = c.hist_sweeps[(c.hist_n - n + k) % 4096u];
   if (n_out) *n_out = (int)n;
+  return STS_OK;
+}
+
+int sts_autotune_result(sts_ctx* ctx, int* steps_left, int* ctas_per_sm, int* asm_block_x, int* asm_block_y) {
+  if (!ctx) return fail(STS_ERR_ARG, "null context");
+  if (steps_left) *steps_left = ctx->tune_left;
+  if (ctas_per_sm) *ctas_per_sm = ctx->pt_per_sm > 0 ? ctx->pt_per_sm : ctx->pt_per_sm_max;
+  if (asm_block_x) *asm_block_x = (int)ctx->asm_block.x;
+  if (asm_block_y) *asm_block_y = (int)ctx->asm_block.y;
   return STS_OK;
 }
 

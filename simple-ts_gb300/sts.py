@@ -29,7 +29,7 @@ EXPORTS = [
     "sts_last_error", "sts_inspect_case", "sts_step_timed", "sts_profile_steps", "sts_pt_sweeps",
     "sts_pt_sweeps_noalloc", "sts_check_division", "sts_open_batch", "sts_batch_step", "sts_batch_step_timed",
     "sts_batch_case", "sts_batch_destroy", "sts_check_double_float", "sts_write_outputs_async",
-    "sts_wait_outputs",
+    "sts_wait_outputs", "sts_autotune_result",
 ]
 
 KERNELS = ["step_begin", "assemble", "sweep_loop", "correct", "face_rho", "boundary", "flux_diff", "step_end"]
@@ -44,7 +44,8 @@ FIELDS = ["u", "v", "p", "T", "rho", "sqrt_T", "rho_u", "rho_v", "Fx", "Fy", "D_
 
 class Options(C.Structure):
     _fields_ = [("fixed_sweeps", C.c_int), ("use_graph", C.c_int), ("device", C.c_int), ("write_files", C.c_int),
-                ("precision", C.c_int), ("warm_start", C.c_int), ("async_save", C.c_int)]
+                ("precision", C.c_int), ("warm_start", C.c_int), ("async_save", C.c_int),
+                ("autotune", C.c_int)]
 
 
 class StsError(RuntimeError):
@@ -79,6 +80,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.sts_write_outputs.argtypes = [P]
     lib.sts_write_outputs_async.argtypes = [P]
     lib.sts_wait_outputs.argtypes = [P]
+    ip = C.POINTER(C.c_int)
+    lib.sts_autotune_result.argtypes = [P, ip, ip, ip, ip]
     lib.sts_run_case.argtypes = [C.c_char_p, C.POINTER(Options)]
     lib.sts_sync.argtypes = [P]
     lib.sts_destroy.argtypes = [P]
@@ -97,7 +100,7 @@ def _check(code: int):
 
 
 def options(fixed_sweeps=True, use_graph=True, device=0, write_files=False, precision=EXACT,
-            warm_start=0, async_save=True) -> Options:
+            warm_start=0, async_save=True, autotune=True) -> Options:
     o = Options()
     load().sts_default_options(C.byref(o))
     o.fixed_sweeps = int(fixed_sweeps)
@@ -107,6 +110,7 @@ def options(fixed_sweeps=True, use_graph=True, device=0, write_files=False, prec
     o.precision = int(precision)
     o.warm_start = int(warm_start)
     o.async_save = int(async_save)
+    o.autotune = int(autotune)
     return o
 
 
@@ -118,12 +122,12 @@ class Solver:
     """One case on one GPU: the reference's solve loop behind the C ABI."""
 
     def __init__(self, case_dir: str, fixed_sweeps=True, use_graph=True, device=0, precision=EXACT, warm_start=0,
-                 _handle=None):
+                 autotune=True, _handle=None):
         lib = load()
         self._owned = _handle is None
         if _handle is None:
             self._h = C.c_void_p()
-            opt = options(fixed_sweeps, use_graph, device, False, precision, warm_start)
+            opt = options(fixed_sweeps, use_graph, device, False, precision, warm_start, autotune=autotune)
             _check(lib.sts_open_case(case_dir.encode(), C.byref(opt), C.byref(self._h)))
         else:
             self._h = _handle
@@ -193,6 +197,12 @@ class Solver:
 
     def wait_outputs(self):
         _check(load().sts_wait_outputs(self._h))
+
+    def autotune_result(self) -> dict:
+        """Launch shapes in use: tuning steps still to come, sweep-loop CTAs per SM, assembly block."""
+        v = [C.c_int() for _ in range(4)]
+        _check(load().sts_autotune_result(self._h, *[C.byref(x) for x in v]))
+        return {"steps_left": v[0].value, "ctas_per_sm": v[1].value, "asm_block": (v[2].value, v[3].value)}
 
     def sync(self):
         _check(load().sts_sync(self._h))

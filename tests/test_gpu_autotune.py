@@ -1,0 +1,35 @@
+"""The autotuner picks launch shapes on the run's first steps; launch shapes cannot change results,
+so a tuned run equals an untuned one bit for bit."""
+import tempfile
+
+import numpy as np
+import pytest
+
+import sts_cases as sc
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["u", "v", "p", "T", "rho"]
+
+
+@pytest.mark.parametrize("precision", [0, 2])
+def test_tuned_run_equals_untuned(precision, lib_built):
+    import sts
+    case = sc.config_case("channel_ma2.43", scale=0.25, Nt=40)
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        a = sts.Solver(d, fixed_sweeps=False, precision=precision, autotune=True)
+        b = sts.Solver(d, fixed_sweeps=False, precision=precision, autotune=False)
+        left = a.autotune_result()["steps_left"]
+        assert left > 0
+        assert a.step(left + 6) == b.step(left + 6) == left + 6
+        res = a.autotune_result()
+        print(res)
+        assert res["steps_left"] == 0
+        assert res["ctas_per_sm"] >= 1
+        assert res["asm_block"] in ((32, 8), (64, 4), (128, 2))
+        for f in FIELDS:
+            np.testing.assert_array_equal(a.field(f), b.field(f), err_msg=f)
+        np.testing.assert_array_equal(a.sweep_history(), b.sweep_history())
+        a.close()
+        b.close()
