@@ -445,19 +445,18 @@ def main():
     value = job_rate(Na * done, world, total_ms / 1e3)
 
     # e2e through the C ABI with host buffers: per step the state u, v, p, T goes host->device
-    # from pinned memory, one step runs, and the new state comes back device->host.
+    # from pinned memory (sts_set_state), one step runs, and the new state comes back
+    # device->host (sts_get_state).
     pins = {f: torch.empty(Na, dtype=torch.float64).pin_memory() for f in ("u", "v", "p", "T")}
-    for f, b in pins.items():
-        s.get_field_ptr(f, b.data_ptr())
+    ptrs = [pins[f].data_ptr() for f in ("u", "v", "p", "T")]
+    s.get_state_ptr(*ptrs)
     barrier()
     e2e_steps = max(1, min(args.steps, 20))
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        for f, b in pins.items():
-            s.set_field_ptr(f, b.data_ptr())
+        s.set_state_ptr(*ptrs)
         s.step(1)
-        for f, b in pins.items():
-            s.get_field_ptr(f, b.data_ptr())
+        s.get_state_ptr(*ptrs)
     barrier()
     e2e_s = slowest(time.perf_counter() - t0, world)
     e2e = {"value": job_rate(Na * e2e_steps, world, e2e_s), "unit": UNIT, "h2d_bytes_per_step": 4 * Na * 8,

@@ -117,6 +117,14 @@ int sts_get_field(sts_ctx* ctx, const char* name, double* host_out);
  * With a warm start (sts_options.warm_start), setting p or T starts its history over. */
 int sts_set_field(sts_ctx* ctx, const char* name, const double* host_in);
 
+/* The state the reference dumps -- u, v, p, T (Nx*Ny doubles each) -- to or from host memory in
+ * one call: the four copies are queued together and the call returns once they are done (one
+ * synchronisation instead of four).  For callers that exchange the whole state every step; host
+ * buffers in pinned memory copy fastest.  sts_set_state has sts_set_field's effect on each field
+ * (a warm start's history starts over). */
+int sts_set_state(sts_ctx* ctx, const double* u_in, const double* v_in, const double* p_in, const double* T_in);
+int sts_get_state(sts_ctx* ctx, double* u_out, double* v_out, double* p_out, double* T_out);
+
 /* Mesh size. */
 int sts_dims(sts_ctx* ctx, int* Nx, int* Ny);
 

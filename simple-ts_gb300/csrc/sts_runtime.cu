@@ -1204,6 +1204,42 @@ int sts_set_field(sts_ctx* ctx, const char* name, const double* in) {
   return STS_OK;
 }
 
+int sts_set_state(sts_ctx* ctx, const double* u_in, const double* v_in, const double* p_in, const double* T_in) {
+  if (!ctx || !u_in || !v_in || !p_in || !T_in) return fail(STS_ERR_ARG, "null argument");
+  CU(cudaSetDevice(ctx->opt.device));
+  if (ctx->in_batch)
+    if (int r = ctx->read_ctl()) return r;
+  const Geo& g = ctx->g;
+  const unsigned cur = ctx->h_ctl->cur;
+  const size_t bytes = sizeof(double) * g.Na;
+  CU(cudaMemcpyAsync(g.u, u_in, bytes, cudaMemcpyHostToDevice, ctx->s));
+  CU(cudaMemcpyAsync(g.v, v_in, bytes, cudaMemcpyHostToDevice, ctx->s));
+  CU(cudaMemcpyAsync(g.p[cur], p_in, bytes, cudaMemcpyHostToDevice, ctx->s));
+  CU(cudaMemcpyAsync(g.T[cur], T_in, bytes, cudaMemcpyHostToDevice, ctx->s));
+  if (g.warm_start) {
+    static const unsigned zero = 0;
+    CU(cudaMemcpyAsync(&g.ctl->warm_ready, &zero, sizeof(unsigned), cudaMemcpyHostToDevice, ctx->s));
+  }
+  CU(cudaStreamSynchronize(ctx->s));
+  return STS_OK;
+}
+
+int sts_get_state(sts_ctx* ctx, double* u_out, double* v_out, double* p_out, double* T_out) {
+  if (!ctx || !u_out || !v_out || !p_out || !T_out) return fail(STS_ERR_ARG, "null argument");
+  CU(cudaSetDevice(ctx->opt.device));
+  if (ctx->in_batch)
+    if (int r = ctx->read_ctl()) return r;
+  const Geo& g = ctx->g;
+  const unsigned cur = ctx->h_ctl->cur;
+  const size_t bytes = sizeof(double) * g.Na;
+  CU(cudaMemcpyAsync(u_out, g.u, bytes, cudaMemcpyDeviceToHost, ctx->s));
+  CU(cudaMemcpyAsync(v_out, g.v, bytes, cudaMemcpyDeviceToHost, ctx->s));
+  CU(cudaMemcpyAsync(p_out, g.p[cur], bytes, cudaMemcpyDeviceToHost, ctx->s));
+  CU(cudaMemcpyAsync(T_out, g.T[cur], bytes, cudaMemcpyDeviceToHost, ctx->s));
+  CU(cudaStreamSynchronize(ctx->s));
+  return STS_OK;
+}
+
 int sts_dims(sts_ctx* ctx, int* Nx, int* Ny) {
   if (!ctx) return fail(STS_ERR_ARG, "null context");
   if (Nx) *Nx = ctx->g.Nx;

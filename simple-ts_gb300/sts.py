@@ -29,7 +29,7 @@ EXPORTS = [
     "sts_last_error", "sts_inspect_case", "sts_step_timed", "sts_profile_steps", "sts_pt_sweeps",
     "sts_pt_sweeps_noalloc", "sts_check_division", "sts_open_batch", "sts_batch_step", "sts_batch_step_timed",
     "sts_batch_case", "sts_batch_destroy", "sts_check_double_float", "sts_write_outputs_async",
-    "sts_wait_outputs", "sts_autotune_result",
+    "sts_wait_outputs", "sts_autotune_result", "sts_set_state", "sts_get_state",
 ]
 
 KERNELS = ["step_begin", "assemble", "sweep_loop", "correct", "face_rho", "boundary", "flux_diff", "step_end"]
@@ -82,6 +82,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.sts_wait_outputs.argtypes = [P]
     ip = C.POINTER(C.c_int)
     lib.sts_autotune_result.argtypes = [P, ip, ip, ip, ip]
+    lib.sts_set_state.argtypes = [P, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.sts_get_state.argtypes = [P, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.sts_run_case.argtypes = [C.c_char_p, C.POINTER(Options)]
     lib.sts_sync.argtypes = [P]
     lib.sts_destroy.argtypes = [P]
@@ -197,6 +199,14 @@ class Solver:
 
     def wait_outputs(self):
         _check(load().sts_wait_outputs(self._h))
+
+    def set_state_ptr(self, u, v, p, T):
+        """u, v, p, T from raw host pointers (Nx*Ny doubles each) in one call."""
+        _check(load().sts_set_state(self._h, u, v, p, T))
+
+    def get_state_ptr(self, u, v, p, T):
+        """u, v, p, T to raw host pointers (Nx*Ny doubles each) in one call."""
+        _check(load().sts_get_state(self._h, u, v, p, T))
 
     def autotune_result(self) -> dict:
         """Launch shapes in use: tuning steps still to come, sweep-loop CTAs per SM, assembly block."""
