@@ -314,6 +314,7 @@ def batch_bench(args):
         cells = sum(c.Nx * c.Ny for c in b.cases)
         w = max(args.warmup, 3)
         lead = max(args.warm_lead, w) if warm else w
+        lead += b.autotune_result()["steps_left"]  # the autotuner's steps come before the warm-up
         for _ in range(lead):
             b.step(1)
         total, done = 0.0, 0
@@ -329,15 +330,18 @@ def batch_bench(args):
         r = {"value": cells * done / (total / 1e3), "ms_per_step": total / max(done, 1),
              "sweeps_per_step": float(np.mean(sweeps)), "clocks": clk.summary()}
         r["untimed_steps"] = lead
-        if base is None:
-            base = {w: fields}
-            # the bit-exact fields at the step count of the warm-started variants
-            for _ in range(max(args.warm_lead, w) - w):
-                b.step(1)
-            base[max(args.warm_lead, w)] = {f: np.concatenate([c.field(f).ravel() for c in b.cases])
-                                             for f in ("u", "v", "p", "T", "rho")}
+        r["launch_shapes"] = b.autotune_result()
+        if name == "fp64_exact":
+            base = {lead + done: fields}
         else:
-            ref = base[lead]
+            n_ref = lead + done
+            if n_ref not in base:  # the bit-exact fields after the same number of steps
+                rb = sts.Batch(dirs, fixed_sweeps=False, precision=sts.EXACT, autotune=False)
+                rb.step(n_ref)
+                base[n_ref] = {f: np.concatenate([c.field(f).ravel() for c in rb.cases])
+                               for f in ("u", "v", "p", "T", "rho")}
+                rb.close()
+            ref = base[n_ref]
             r["rel_l2_vs_fp64"] = {f: float(np.linalg.norm(fields[f] - ref[f]) / np.linalg.norm(ref[f]))
                                    for f in fields}
         out[name] = r

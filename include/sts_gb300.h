@@ -254,6 +254,10 @@ int sts_batch_case(sts_batch* b, int index, sts_ctx** out);
 /* Releases the batch and its cases. */
 void sts_batch_destroy(sts_batch* b);
 
+/* sts_autotune_result for a batch: its tuning steps still to come, its sweep loop's CTAs per SM
+ * and its assembly block (x, y).  No counterpart in the reference. */
+int sts_batch_autotune_result(sts_batch* b, int* steps_left, int* ctas_per_sm, int* asm_block_x, int* asm_block_y);
+
 /* Host-only inspection of a case directory (no device use): dims, obstacle ids
  * (vol_inf_fb, Nx*Ny), per-cell classes (Nx*Ny bytes: bits 0-1 u, 2-3 v, 4-5 p/T with
  * 0 unsolved, 1 interior, 2 boundary; bit 6 fluid) and the mesh (hx, x_v: Nx; hy, y_v: Ny).

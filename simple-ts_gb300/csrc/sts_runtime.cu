@@ -1531,6 +1531,25 @@ struct sts_batch {
   bool warm3 = false, warm4 = false;
   unsigned* d_flag = nullptr;
   unsigned* h_flag = nullptr;
+  // launch shapes (autotuned as for a single case: assembly block, sweep-loop CTAs per SM)
+  dim3 asm_block{32, 8, 1};
+  int max_nx = 1, max_ny = 1, sms = 0, per_sm_max = 0, per_sm = 0;
+  int tune_left = 0, tune_idx = -1;
+  std::vector<sts_ctx::TuneStat> tune_pt, tune_asm;
+  dim3 asm_grid() const {
+    return dim3((max_nx + asm_block.x - 1) / asm_block.x, (max_ny + asm_block.y - 1) / asm_block.y,
+                (unsigned)ncases * (precision == 3 ? 3u : 1u));
+  }
+  void size_pt() {
+    const int use = (per_sm > 0 && per_sm <= per_sm_max) ? per_sm : per_sm_max;
+    pt_grid = dim3((unsigned)std::max(1, std::min(ntiles, use * sms)));
+  }
+  void launch_assemble() {
+    if (precision == 3) kb_assemble_df<<<asm_grid(), asm_block, 0, s>>>(d_geos, 0ull, 0);
+    else if (fast()) kb_assemble_fast<<<asm_grid(), asm_block, 0, s>>>(d_geos, 0ull, 0);
+    else kb_assemble<<<asm_grid(), asm_block, 0, s>>>(d_geos, 0ull, 0);
+  }
+  int tune_step();
 };
 
 // The batched step loop launched kernel by kernel (for per-kernel profiling): the same kernels
@@ -1545,9 +1564,7 @@ int sts_batch::step_host(int n) {
       kb_warm_fit<<<dim3(1, 1, ncases), 576, 0, s>>>(G);
       kb_warm_apply<<<cell_grid, blk, 0, s>>>(G);
     }
-    if (precision == 3) kb_assemble_df<<<dim3(cell_grid.x, cell_grid.y, 3 * ncases), blk, 0, s>>>(G, 0ull, 0);
-    else if (fast()) kb_assemble_fast<<<cell_grid, blk, 0, s>>>(G, 0ull, 0);
-    else kb_assemble<<<cell_grid, blk, 0, s>>>(G, 0ull, 0);
+    launch_assemble();
     const int* tc = d_tile_case;
     const int* tf = d_tile_first;
     void* args[] = {(void*)&G, (void*)&tc, (void*)&tf, (void*)&ncases, (void*)&ntiles, (void*)&d_lc};
@@ -1576,6 +1593,90 @@ int sts_batch::step_host(int n) {
   return STS_OK;
 }
 
+// One batched step for the autotuner, launched kernel by kernel: the assembly with block shape
+// tune_idx % 3, the sweep loop with tune_idx % per_sm_max + 1 CTAs per SM, both timed by event pairs;
+// the loop is compared per round (the most sweeps any case took).  A real step.
+int sts_batch::tune_step() {
+  const bool record = tune_idx >= 0;
+  const int npt = (int)tune_pt.size(), nasm = (int)tune_asm.size();
+  const int pc = record ? tune_idx % npt : npt - 1, ac = record ? tune_idx % nasm : 0;
+  asm_block = sts_ctx::asm_shape(ac);
+  per_sm = pc + 1;
+  size_pt();
+  cudaEvent_t ev[3];
+  for (cudaEvent_t& e : ev) CU(cudaEventCreate(&e));
+  const dim3 blk(32, 8);
+  const Geo* G = d_geos;
+  kb_set_steps<<<1, 256, 0, s>>>(G, ncases, 1u);
+  kb_step_begin<<<cell_grid, blk, 0, s>>>(G);
+  if (warm3) {
+    kb_warm_diff<<<cell_grid, blk, 0, s>>>(G);
+    kb_warm_fit<<<dim3(1, 1, ncases), 576, 0, s>>>(G);
+    kb_warm_apply<<<cell_grid, blk, 0, s>>>(G);
+  }
+  CU(cudaEventRecord(ev[0], s));
+  launch_assemble();
+  CU(cudaEventRecord(ev[1], s));
+  const int* tc = d_tile_case;
+  const int* tf = d_tile_first;
+  void* args[] = {(void*)&G, (void*)&tc, (void*)&tf, (void*)&ncases, (void*)&ntiles, (void*)&d_lc};
+  CU(cudaLaunchCooperativeKernel((const void*)pt_kernel(), pt_grid, blk, args, 0, s));
+  CU(cudaEventRecord(ev[2], s));
+  kb_correct<<<cell_grid, blk, 0, s>>>(G);
+  kb_face_rho<<<cell_grid, blk, 0, s>>>(G);
+  kb_bnd_walls<<<walls_grid, 256, 0, s>>>(G, PH_CONTROL | PH_SLIP_U | PH_SLIP_V, 0ull, 0);
+  kb_boundary<<<dim3(1, 1, ncases), 1024, 0, s>>>(G, PH_VEL | PH_PBEGIN, 0ull, 0);
+  kb_bnd_tjump<<<tjump_grid, 256, 0, s>>>(G);
+  if (precision == 3) kb_flux_diff_df<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
+  else if (fast()) kb_flux_diff_fast<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
+  else kb_flux_diff<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
+  if (warm4) {
+    kb_conv_gram<<<cell_grid, blk, 0, s>>>(G);
+    kb_conv_solve<<<dim3(2, 1, ncases), kConvSolveThreads, 0, s>>>(G);
+    kb_conv_next<<<cell_grid, blk, 0, s>>>(G);
+    kb_conv_predict<<<cell_grid, blk, 0, s>>>(G);
+  }
+  kb_step_end<<<dim3(1, 1, ncases), 1024, 0, s>>>(G, 0ull, 0);
+  CU(cudaGetLastError());
+  CU(cudaStreamSynchronize(s));
+  float ta = 0, tp = 0;
+  cudaEventElapsedTime(&ta, ev[0], ev[1]);
+  cudaEventElapsedTime(&tp, ev[1], ev[2]);
+  for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  unsigned rounds = 0;
+  for (sts_ctx* c : cases) {
+    if (int r = c->read_ctl()) return r;
+    rounds = std::max(rounds, c->h_ctl->step_sweeps);
+  }
+  if (record) {
+    tune_asm[ac].ms += ta;
+    tune_asm[ac].n += 1;
+    tune_pt[pc].ms += tp;
+    tune_pt[pc].sweeps += rounds;
+    tune_pt[pc].n += 1;
+  }
+  tune_idx++;
+  if (--tune_left == 0) {
+    int best_a = 0, best_p = npt - 1;
+    for (int k = 0; k < nasm; k++)
+      if (tune_asm[k].n && tune_asm[k].ms / tune_asm[k].n < tune_asm[best_a].ms / std::max(tune_asm[best_a].n, 1)) best_a = k;
+    auto per_round = [&](int k) { return tune_pt[k].sweeps > 0 ? tune_pt[k].ms / tune_pt[k].sweeps : 1e30; };
+    for (int k = 0; k < npt; k++)
+      if (per_round(k) < per_round(best_p)) best_p = k;
+    asm_block = sts_ctx::asm_shape(best_a);
+    per_sm = best_p + 1;
+    size_pt();
+    if (use_graph) {  // rebuilt with the chosen shapes
+      if (exec) cudaGraphExecDestroy(exec);
+      if (graph) cudaGraphDestroy(graph);
+      exec = nullptr;
+      graph = nullptr;
+      if (int r = build_graph()) return r;
+    }
+  }
+  return STS_OK;
+}
+
 int sts_batch::build_graph() {
   CU(cudaGraphCreate(&graph, 0));
   cudaGraphConditionalHandle hs;
@@ -1595,8 +1696,7 @@ int sts_batch::build_graph() {
     n[0] = w[2];
   }
   if (int r = add_kernel(&n[1], b, {n[0]}, precision == 3 ? kb_assemble_df : (fast() ? kb_assemble_fast : kb_assemble),
-                         precision == 3 ? dim3(cell_grid.x, cell_grid.y, 3 * ncases) : cell_grid, blk, G,
-                         (unsigned long long)0, 0))
+                         asm_grid(), asm_block, G, (unsigned long long)0, 0))
     return r;
   if (int r = add_kernel(&n[2], b, {n[1]}, pt_kernel(), pt_grid, blk, G, (const int*)d_tile_case,
                          (const int*)d_tile_first, ncases, ntiles, d_lc))
@@ -1675,6 +1775,8 @@ int sts_open_batch(const char* const* case_dirs, int ncases, const sts_options* 
     for (int t = 0; t < c->ntiles; t++) tile_case.push_back(k);
     gx = std::max(gx, c->grid.x);
     gy = std::max(gy, c->grid.y);
+    b->max_nx = std::max(b->max_nx, c->g.Nx);
+    b->max_ny = std::max(b->max_ny, c->g.Ny);
     wx = std::max(wx, c->walls_grid().x);
     tx = std::max(tx, c->tjump_grid().x);
   }
@@ -1696,7 +1798,14 @@ int sts_open_batch(const char* const* case_dirs, int ncases, const sts_options* 
   CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, opt.device));
   CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b->pt_kernel(), 256, 0));
   if (per_sm < 1) return fail(STS_ERR_CUDA, "the sweep-loop kernel does not fit on a multiprocessor");
-  b->pt_grid = dim3((unsigned)std::max(1, std::min(b->ntiles, per_sm * sms)));
+  b->sms = sms;
+  b->per_sm_max = per_sm;
+  b->size_pt();
+  if (opt.autotune) {
+    b->tune_pt.assign(per_sm, sts_ctx::TuneStat{});
+    b->tune_asm.assign(3, sts_ctx::TuneStat{});
+    b->tune_left = 1 + sts_ctx::kTuneRounds * std::max(per_sm, 3);
+  }
   if (int r = b->alloc(&b->d_flag, 1)) return r;
   CU(cudaMallocHost(&b->h_flag, sizeof(unsigned)));
   if (b->use_graph)
@@ -1717,12 +1826,23 @@ int sts_batch_step(sts_batch* b, int nsteps, int* steps_done) {
       status_before[k] = b->cases[k]->h_ctl->status;
     }
     for (sts_ctx* c : b->cases) CU(cudaStreamSynchronize(c->s));  // field uploads of the cases land first
-    kb_set_steps<<<1, 256, 0, b->s>>>(b->d_geos, b->ncases, (unsigned)nsteps);
-    CU(cudaGetLastError());
-    if (b->use_graph) {
-      CU(cudaGraphLaunch(b->exec, b->s));
-    } else if (int r = b->step_host(nsteps)) {
-      return r;
+    // the autotuner's steps come first (real steps, launched kernel by kernel)
+    int tuned = 0;
+    while (b->tune_left > 0 && tuned < nsteps) {
+      if (int r = b->tune_step()) return r;
+      tuned++;
+      bool any = false;
+      for (sts_ctx* c : b->cases) any = any || c->h_ctl->continue_step;
+      if (!any) break;
+    }
+    if (tuned < nsteps) {
+      kb_set_steps<<<1, 256, 0, b->s>>>(b->d_geos, b->ncases, (unsigned)(nsteps - tuned));
+      CU(cudaGetLastError());
+      if (b->use_graph) {
+        CU(cudaGraphLaunch(b->exec, b->s));
+      } else if (int r = b->step_host(nsteps - tuned)) {
+        return r;
+      }
     }
     CU(cudaStreamSynchronize(b->s));
     bool nonfinite = false;
@@ -1770,5 +1890,14 @@ int sts_batch_case(sts_batch* b, int index, sts_ctx** out) {
 }
 
 void sts_batch_destroy(sts_batch* b) { delete b; }
+
+int sts_batch_autotune_result(sts_batch* b, int* steps_left, int* ctas_per_sm, int* asm_block_x, int* asm_block_y) {
+  if (!b) return fail(STS_ERR_ARG, "null batch");
+  if (steps_left) *steps_left = b->tune_left;
+  if (ctas_per_sm) *ctas_per_sm = b->per_sm > 0 ? b->per_sm : b->per_sm_max;
+  if (asm_block_x) *asm_block_x = (int)b->asm_block.x;
+  if (asm_block_y) *asm_block_y = (int)b->asm_block.y;
+  return STS_OK;
+}
 
 }  // extern "C"

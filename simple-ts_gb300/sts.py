@@ -29,7 +29,7 @@ EXPORTS = [
     "sts_last_error", "sts_inspect_case", "sts_step_timed", "sts_profile_steps", "sts_pt_sweeps",
     "sts_pt_sweeps_noalloc", "sts_check_division", "sts_open_batch", "sts_batch_step", "sts_batch_step_timed",
     "sts_batch_case", "sts_batch_destroy", "sts_check_double_float", "sts_write_outputs_async",
-    "sts_wait_outputs", "sts_autotune_result", "sts_set_state", "sts_get_state",
+    "sts_wait_outputs", "sts_autotune_result", "sts_set_state", "sts_get_state", "sts_batch_autotune_result",
 ]
 
 KERNELS = ["step_begin", "assemble", "sweep_loop", "correct", "face_rho", "boundary", "flux_diff", "step_end"]
@@ -309,16 +309,19 @@ def check_division(n: int, seed: int = 1, device: int = 0) -> int:
 class Batch:
     """Many independent cases advanced together (one launch per kernel and step for all)."""
 
-    def __init__(self, case_dirs, fixed_sweeps=False, device=0, precision=EXACT, warm_start=0, use_graph=True):
+    def __init__(self, case_dirs, fixed_sweeps=False, device=0, precision=EXACT, warm_start=0, use_graph=True,
+                 autotune=True):
         lib = load()
         lib.sts_open_batch.argtypes = [C.POINTER(C.c_char_p), C.c_int, C.POINTER(Options), C.POINTER(C.c_void_p)]
         lib.sts_batch_step.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int)]
         lib.sts_batch_step_timed.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]
         lib.sts_batch_case.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
         lib.sts_batch_destroy.argtypes = [C.c_void_p]
+        ip = C.POINTER(C.c_int)
+        lib.sts_batch_autotune_result.argtypes = [C.c_void_p, ip, ip, ip, ip]
         dirs = (C.c_char_p * len(case_dirs))(*[d.encode() for d in case_dirs])
         self._h = C.c_void_p()
-        opt = options(fixed_sweeps, use_graph, device, False, precision, warm_start)
+        opt = options(fixed_sweeps, use_graph, device, False, precision, warm_start, autotune=autotune)
         _check(lib.sts_open_batch(dirs, len(case_dirs), C.byref(opt), C.byref(self._h)))
         self.cases = []
         for k in range(len(case_dirs)):
@@ -330,6 +333,12 @@ class Batch:
         done = C.c_int()
         _check(load().sts_batch_step(self._h, int(n), C.byref(done)))
         return done.value
+
+    def autotune_result(self) -> dict:
+        """Launch shapes in use: tuning steps still to come, sweep-loop CTAs per SM, assembly block."""
+        v = [C.c_int() for _ in range(4)]
+        _check(load().sts_batch_autotune_result(self._h, *[C.byref(x) for x in v]))
+        return {"steps_left": v[0].value, "ctas_per_sm": v[1].value, "asm_block": (v[2].value, v[3].value)}
 
     def step_timed(self, n: int):
         done, ms = C.c_int(), C.c_double()

@@ -33,3 +33,29 @@ def test_tuned_run_equals_untuned(precision, lib_built):
         np.testing.assert_array_equal(a.sweep_history(), b.sweep_history())
         a.close()
         b.close()
+
+
+def test_tuned_batch_equals_untuned(lib_built):
+    import os
+    import sts
+    cases = sc.batch_cases(n=3, Nt=40, nx_range=(40, 100))
+    with tempfile.TemporaryDirectory() as root:
+        dirs = []
+        for k, c in enumerate(cases):
+            d = os.path.join(root, f"c{k}")
+            os.makedirs(d)
+            c.write(d)
+            dirs.append(d)
+        a = sts.Batch(dirs, fixed_sweeps=False, precision=2, autotune=True)
+        b = sts.Batch(dirs, fixed_sweeps=False, precision=2, autotune=False)
+        left = a.autotune_result()["steps_left"]
+        assert left > 0
+        assert a.step(left + 4) == b.step(left + 4) == left + 4
+        res = a.autotune_result()
+        print(res)
+        assert res["steps_left"] == 0 and res["asm_block"] in ((32, 8), (64, 4), (128, 2))
+        for k in range(len(dirs)):
+            for f in FIELDS:
+                np.testing.assert_array_equal(a.cases[k].field(f), b.cases[k].field(f), err_msg=f"case {k} {f}")
+        a.close()
+        b.close()
