@@ -43,9 +43,18 @@ BYTES_PER_CELL = {
 }
 
 # DRAM bytes per launch measured by ncu on this workload, FP64 path (dram__bytes_read.sum +
-# dram__bytes_write.sum of one launch of the second time step, cold cache); None where no
+# dram__bytes_write.sum of one launch of the fourteenth time step, cold cache); None where no
 # capture was taken
-TRAFFIC = {"assemble": 20980736 + 256, "sweep_loop": 18984192 + 19712}
+TRAFFIC = {"assemble": 20982016 + 512, "sweep_loop": 18983680 + 13568, "flux_diff": 9731840}
+
+# FP64 instructions per cell of the FP64 path's kernels (per cell and sweep for the sweep loop),
+# counted by ncu on this workload (smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on
+# of one launch divided by its 1203 x 123 cells and, for the sweep loop, by its 8 sweeps).  The
+# kernels are bound by the FP64 unit, so their roofline is this work at the device's measured
+# FP64 rates (sts_fp64_rates) against the measured launch time.
+FP64_OPS = {"assemble": {"add": 104.24, "mul": 134.77, "fma": 371.65},
+            "sweep_loop": {"add": 22.75, "mul": 16.55, "fma": 19.22},
+            "flux_diff": {"add": 23.58, "mul": 65.25, "fma": 63.57}}
 
 
 def parse():
@@ -176,6 +185,25 @@ def peaks():
         return d["hbm_gbs"], "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def fp64_roof(dom, kms, kcnt, psweeps, Na, device):
+    """The FP64-unit roofline of the dominant kernel: its counted FP64 instructions per launch
+    at the device's measured add/multiply/FMA rates, against its measured launch time."""
+    import sts
+    ops = FP64_OPS.get(dom)
+    if not ops or not kcnt.get(dom):
+        return None
+    rates = sts.fp64_rates(device)
+    units = float(Na)
+    if dom == "sweep_loop":
+        units *= float(sum(int(x) for x in psweeps)) / kcnt[dom]
+    launch_s = kms[dom] / 1e3 / kcnt[dom]
+    roof_s = sum(ops[k] * units / (rates[k] * 1e9) for k in ops)
+    total = sum(ops.values()) * units
+    return {"achieved": total / launch_s / 1e9, "peak_at_mix": total / roof_s / 1e9, "unit": "FP64 Gop/s",
+            "frac": roof_s / launch_s, "ops_per_cell": ops, "measured_rates_gops": rates,
+            "source": "FP64 instruction counts per cell from ncu; rates measured on this GPU by sts_fp64_rates"}
 
 
 def make_case(workload):
@@ -480,7 +508,8 @@ def main():
     roof = {"bound": "hbm", "kernel": "k_" + dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "traffic": TRAFFIC.get(dom),
             "peak_source": peak_kind, "bytes_per_cell": bpc, "avg_launch_us": avg_s * 1e6,
-            "kernel_share": {k: round(v / max(sum(kms.values()), 1e-30), 4) for k, v in kms.items()}}
+            "kernel_share": {k: round(v / max(sum(kms.values()), 1e-30), 4) for k, v in kms.items()},
+            "fp64_pipe": fp64_roof(dom, kms, kcnt, psweeps, Na, local)}
     s.close()
 
     # the same workload in the faster precision modes, from the same initial state, with the

@@ -222,6 +222,13 @@ int sts_pt_sweeps_noalloc(const sts_sweep_fields* f, int max_sweeps, int fixed_s
  * the reference, which divides with the host's IEEE division. */
 int sts_check_division(unsigned long long n, unsigned long long seed, int device, unsigned long long* mismatches);
 
+/* FP64 throughput of `device`, measured: gops[0..2] receive the rates (10^9 operations per
+ * second) of dependent-free FP64 adds, multiplies and fused multiply-adds in a loop that keeps
+ * the FP64 unit busy (about 2 ms in all).  The roofline of the bit-exact kernels, which are
+ * bound by the FP64 unit rather than by memory, is taken against these rates.  No counterpart
+ * in the reference. */
+int sts_fp64_rates(int device, double* gops);
+
 /* Self-check of the double-float arithmetic of precision mode 3 against FP64 on `device`: n
  * pseudo-random operand pairs from `seed` (random signs, magnitudes 2^-40 .. 2^40); max_rel_err[0..4]
  * receive the largest relative errors of the FP64 -> double-float conversion, add (relative to

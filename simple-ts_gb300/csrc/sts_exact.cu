@@ -1315,6 +1315,33 @@ __global__ void k_check_division(unsigned long long n, unsigned long long seed, 
   if ((threadIdx.x & 31) == 0 && local) atomicAdd(bad, local);
 }
 
+// FP64 throughput of the device: every thread advances 8 independent chains `iters` times with
+// one operation each (op 0: add, 1: multiply, 2: fused multiply-add), so the FP64 unit, not
+// latency, sets the time.  The chains stay near 1 (factors and addends are tiny perturbations);
+// each thread stores its sum so that nothing is optimised away.
+__global__ void k_fp64_rate(int op, int iters, double c_mul, double c_add, double* out) {
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) x[k] = 1.0 + (double)(threadIdx.x * 8 + k) * 1e-9;
+  if (op == 0) {
+    for (int it = 0; it < iters; it++)
+#pragma unroll
+      for (int k = 0; k < 8; k++) x[k] = __dadd_rn(x[k], c_add);
+  } else if (op == 1) {
+    for (int it = 0; it < iters; it++)
+#pragma unroll
+      for (int k = 0; k < 8; k++) x[k] = __dmul_rn(x[k], c_mul);
+  } else {
+    for (int it = 0; it < iters; it++)
+#pragma unroll
+      for (int k = 0; k < 8; k++) x[k] = __fma_rn(x[k], c_mul, c_add);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) s += x[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace sts
 
 namespace sts {

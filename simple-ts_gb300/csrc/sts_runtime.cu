@@ -1482,6 +1482,38 @@ int sts_check_division(unsigned long long n, unsigned long long seed, int device
   return STS_OK;
 }
 
+int sts_fp64_rates(int device, double* gops) {
+  if (!gops) return fail(STS_ERR_ARG, "null argument");
+  CU(cudaSetDevice(device));
+  int sms = 0;
+  CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  const int blocks = 4 * sms, threads = 256, iters = 256;
+  double* d = nullptr;
+  CU(cudaMalloc(&d, sizeof(double) * blocks * threads));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  for (int op = 0; op < 3 && e == cudaSuccess; op++) {
+    float best = 0.0f;
+    for (int rep = 0; rep < 4 && e == cudaSuccess; rep++) {
+      cudaEventRecord(e0);
+      k_fp64_rate<<<blocks, threads>>>(op, iters, 0.99999999, 1e-12, d);
+      cudaEventRecord(e1);
+      e = cudaEventSynchronize(e1);
+      if (e == cudaSuccess) e = cudaGetLastError();
+      float ms = 0.0f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (e == cudaSuccess && rep > 0 && (best == 0.0f || ms < best)) best = ms;  // rep 0 warms up
+    }
+    gops[op] = best > 0.0f ? (double)blocks * threads * iters * 8 / ((double)best * 1e6) : 0.0;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(STS_ERR_CUDA, std::string("sts_fp64_rates: ") + cudaGetErrorString(e));
+  return STS_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

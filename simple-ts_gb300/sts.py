@@ -27,7 +27,7 @@ EXPORTS = [
     "sts_default_options", "sts_open_case", "sts_step", "sts_get_field", "sts_set_field", "sts_dims",
     "sts_stats", "sts_sweep_history", "sts_write_outputs", "sts_run_case", "sts_sync", "sts_destroy",
     "sts_last_error", "sts_inspect_case", "sts_step_timed", "sts_profile_steps", "sts_pt_sweeps",
-    "sts_pt_sweeps_noalloc", "sts_check_division", "sts_open_batch", "sts_batch_step", "sts_batch_step_timed",
+    "sts_pt_sweeps_noalloc", "sts_check_division", "sts_fp64_rates", "sts_open_batch", "sts_batch_step", "sts_batch_step_timed",
     "sts_batch_case", "sts_batch_destroy", "sts_check_double_float", "sts_write_outputs_async",
     "sts_wait_outputs", "sts_autotune_result", "sts_set_state", "sts_get_state", "sts_batch_autotune_result",
 ]
@@ -304,6 +304,15 @@ def check_division(n: int, seed: int = 1, device: int = 0) -> int:
     out = C.c_ulonglong()
     _check(lib.sts_check_division(int(n), int(seed), int(device), C.byref(out)))
     return out.value
+
+
+def fp64_rates(device: int = 0):
+    """Measured FP64 add, multiply and fused multiply-add rates of the device (10^9 op/s)."""
+    lib = load()
+    lib.sts_fp64_rates.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    out = (C.c_double * 3)()
+    _check(lib.sts_fp64_rates(int(device), out))
+    return {"add": out[0], "mul": out[1], "fma": out[2]}
 
 
 class Batch:

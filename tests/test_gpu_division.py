@@ -20,3 +20,15 @@ def test_double_float_arithmetic_accuracy(lib_built):
     print(err)
     for k, e in err.items():
         assert e < 2.0 ** -44, (k, e)
+
+
+def test_fp64_rates(lib_built):
+    """The FP64 throughput the bit-exact kernels' roofline is taken against: positive and within
+    a plausible range for one GPU, with the fused multiply-add no slower than a plain add or
+    multiply (one FP64 instruction each)."""
+    import sts
+    r = sts.fp64_rates()
+    print(r)
+    for k in ("add", "mul", "fma"):
+        assert 10.0 < r[k] < 1.0e5, (k, r[k])
+    assert r["fma"] > 0.8 * min(r["add"], r["mul"])
