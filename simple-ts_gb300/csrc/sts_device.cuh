@@ -20,19 +20,28 @@ __device__ __forceinline__ double Hi(double f1, double f2, double h1, double h2)
 __device__ __forceinline__ double as_d(unsigned long long b) { return __longlong_as_double((long long)b); }
 __device__ __forceinline__ unsigned long long as_b(double d) { return (unsigned long long)__double_as_longlong(d); }
 
+// The IEEE quotient, out of line: the rare operands div_cr cannot take branch here instead of
+// being evaluated (predicated) beside every fast division.
+__device__ __noinline__ double div_ieee(double a, double b) { return __ddiv_rn(a, b); }
+
 // Correctly rounded a / b from y = RN(1/b), the division by a correctly rounded reciprocal of
 // P. Markstein (IBM J. Res. Develop. 34(1), 1990; Muller et al., Handbook of Floating-Point
 // Arithmetic, 2nd ed., sec. 4.9): q0 = RN(a y) is within two units in the last place of a/b;
 // one correction with the fused remainder makes it faithful, and for a faithful q the remainder
 // r = a - b q is exact and RN(q + r y) = RN(a / b).  Valid when nothing overflows or underflows:
-// operands outside 2^-900 <= |a| <= 2^900 or 2^-100 <= |b| <= 2^100 (zeros, subnormals,
-// infinities and NaN included) take the IEEE division instead.  Explicit _rn intrinsics, so the
-// result does not depend on the file's contraction flags.
+// operands outside 2^-900 <= |a| <= 2^900 or 2^-100 <= |b| <= 2^100 (subnormals, infinities
+// and NaN included) take the IEEE division instead.  A zero dividend is exact: a y is the zero
+// whose sign is sign(a) xor sign(b) (y carries b's sign), the IEEE quotient 0 / b; zeros are
+// common in the fields (v vanishes over much of a channel), so they stay on the fast path.
+// Explicit _rn intrinsics, so the result does not depend on the file's contraction flags.
 __device__ __forceinline__ double div_cr(double a, double b, double y) {
-  const unsigned ea = ((unsigned)__double2hiint(a) >> 20) & 0x7ffu;
+  const unsigned ha = (unsigned)__double2hiint(a);
+  const unsigned ea = (ha >> 20) & 0x7ffu;
   const unsigned eb = ((unsigned)__double2hiint(b) >> 20) & 0x7ffu;
-  if (ea - 123u > 1800u || eb - 923u > 200u) return __ddiv_rn(a, b);
+  const bool za = ((ha & 0x7fffffffu) | (unsigned)__double2loint(a)) == 0u;
+  if ((ea - 123u > 1800u && !za) || eb - 923u > 200u) return div_ieee(a, b);
   double q = __dmul_rn(a, y);
+  if (za) return q;
   double r = __fma_rn(-b, q, a);
   q = __fma_rn(r, y, q);
   r = __fma_rn(-b, q, a);

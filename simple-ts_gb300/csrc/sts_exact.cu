@@ -317,25 +317,27 @@ __device__ __forceinline__ void assemble_body(const Geo& g, unsigned long long h
     const double F_xu2 = 0.5 * (Fx[d.ij] + Fx[d.i1j]);
     double Scu;
     if (cu == CLS_BC) {
-      Scu = cT * (B(d.i1j) * u[d.i1j] * sT[d.ij] * hy[j] / (hx[i] * 3.0) +
-                  B(d.i_2j) * u[d.i_1j] * sT[d.i_1j] * hy[j] / (hx[d.i_1] * 3.0) +
+      Scu = cT * (div_cr(B(d.i1j) * u[d.i1j] * sT[d.ij] * hy[j], hx[i] * 3.0, g.r3x[i]) +
+                  div_cr(B(d.i_2j) * u[d.i_1j] * sT[d.i_1j] * hy[j], hx[d.i_1] * 3.0, g.r3x[d.i_1]) +
                   g.Gamma_yf[d.ij1] * (v[d.ij1] * B(d.ij1) - v[d.i_1j1] * B(d.i_1j1)) -
                   g.Gamma_yf[d.ij] * (v[d.ij] * B(d.ij_1) - v[d.i_1j] * B(d.i_1j_1)) -
-                  sT[d.ij] * (v[d.ij1] * B(d.ij1) - v[d.ij] * B(d.ij_1)) * 2.0 / 3.0 +
-                  sT[d.i_1j] * (v[d.i_1j1] * B(d.i_1j1) - v[d.i_1j] * B(d.i_1j_1)) * 2.0 / 3.0);
+                  div_cr(sT[d.ij] * (v[d.ij1] * B(d.ij1) - v[d.ij] * B(d.ij_1)) * 2.0, 3.0, g.r3) +
+                  div_cr(sT[d.i_1j] * (v[d.i_1j1] * B(d.i_1j1) - v[d.i_1j] * B(d.i_1j_1)) * 2.0, 3.0, g.r3));
     } else {
-      Scu = cT * (u[d.i1j] * sT[d.ij] * hy[j] / (hx[i] * 3.0) + u[d.i_1j] * sT[d.i_1j] * hy[j] / (hx[d.i_1] * 3.0) +
+      Scu = cT * (div_cr(u[d.i1j] * sT[d.ij] * hy[j], hx[i] * 3.0, g.r3x[i]) +
+                  div_cr(u[d.i_1j] * sT[d.i_1j] * hy[j], hx[d.i_1] * 3.0, g.r3x[d.i_1]) +
                   g.Gamma_yf[d.ij1] * (v[d.ij1] - v[d.i_1j1]) - g.Gamma_yf[d.ij] * (v[d.ij] - v[d.i_1j]) -
-                  sT[d.ij] * (v[d.ij1] - v[d.ij]) * 2.0 / 3.0 + sT[d.i_1j] * (v[d.i_1j1] - v[d.i_1j]) * 2.0 / 3.0);
+                  div_cr(sT[d.ij] * (v[d.ij1] - v[d.ij]) * 2.0, 3.0, g.r3) +
+                  div_cr(sT[d.i_1j] * (v[d.i_1j1] - v[d.i_1j]) * 2.0, 3.0, g.r3));
     }
-    const double Spu = -(g.D_ux[d.ij] + g.D_ux[d.i1j]) / 3.0;
+    const double Spu = div_cr(-(g.D_ux[d.ij] + g.D_ux[d.i1j]), 3.0, g.r3);
     const double au1 = dmax0(0, F_xu1) + g.D_ux[d.ij];
     const double au2 = dmax0(0, -F_xu2) + g.D_ux[d.i1j];
     const double au3 = 0.5 * (dmax0(0, Fy[d.i_1j]) + dmax0(0, Fy[d.ij])) + g.D_uy[d.ij];
     const double au4 = 0.5 * (dmax0(0, -Fy[d.i_1j1]) + dmax0(0, -Fy[d.ij1])) + g.D_uy[d.ij1];
-    const double bu3 = (rho_pr[d.i_1j] * hx[d.i_1] + rho_pr[d.ij] * hx[i]) * g.u_pr[d.ij] * hy[j] * 0.5 / ht + Scu;
+    const double bu3 = div_cr((rho_pr[d.i_1j] * hx[d.i_1] + rho_pr[d.ij] * hx[i]) * g.u_pr[d.ij] * hy[j] * 0.5, ht, g.rht) + Scu;
     const double au0 = au1 + au2 + au3 + au4 + 0.5 * (-Fy[d.i_1j] - Fy[d.ij] + Fy[d.i_1j1] + Fy[d.ij1]) + F_xu2 - F_xu1 -
-                       Spu + (rho[d.i_1j] * hx[d.i_1] + rho[d.ij] * hx[i]) * hy[j] * 0.5 / ht;
+                       Spu + div_cr((rho[d.i_1j] * hx[d.i_1] + rho[d.ij] * hx[i]) * hy[j] * 0.5, ht, g.rht);
     double up;
     if (cu == CLS_BC)
       up = (au1 * B(d.i1j) * u[d.i_1j] + au2 * B(d.i_2j) * u[d.i1j] + au3 * u[d.ij_1] + au4 * u[d.ij1] + bu3) / au0;
@@ -357,27 +359,29 @@ __device__ __forceinline__ void assemble_body(const Geo& g, unsigned long long h
     const double F_yv4 = 0.5 * (Fy[d.ij] + Fy[d.ij1]);
     double Scv;
     if (cv == CLS_BC) {
-      Scv = cT * (B(d.ij1) * v[d.ij1] * sT[d.ij] * hx[i] / (hy[j] * 3.0) +
-                  B(far) * v[d.ij_1] * sT[d.ij_1] * hx[i] / (hy[jm] * 3.0) +
+      Scv = cT * (div_cr(B(d.ij1) * v[d.ij1] * sT[d.ij] * hx[i], hy[j] * 3.0, g.r3y[j]) +
+                  div_cr(B(far) * v[d.ij_1] * sT[d.ij_1] * hx[i], hy[jm] * 3.0, g.r3y[jm]) +
                   g.Gamma_xf[d.i1j] * (u[d.i1j] * B(d.i1j) - u[d.i1j_1] * B(d.i1j_1)) -
                   g.Gamma_xf[d.ij] * (u[d.ij] * B(d.i_1j) - u[d.ij_1] * B(d.i_1j_1)) -
-                  sT[d.ij] * (u[d.i1j] * B(d.i1j) - u[d.ij] * B(d.i_1j)) * 2.0 / 3.0 +
-                  sT[d.ij_1] * (u[d.i1j_1] * B(d.i1j_1) - u[d.ij_1] * B(d.i_1j_1)) * 2.0 / 3.0) -
+                  div_cr(sT[d.ij] * (u[d.i1j] * B(d.i1j) - u[d.ij] * B(d.i_1j)) * 2.0, 3.0, g.r3) +
+                  div_cr(sT[d.ij_1] * (u[d.i1j_1] * B(d.i1j_1) - u[d.ij_1] * B(d.i_1j_1)) * 2.0, 3.0, g.r3)) -
             g.c_Fr_v * (rho[d.ij_1] * hx[i] * 0.5 * hy[jm] + rho[d.ij] * hx[i] * 0.5 * hy[j]);
     } else {
-      Scv = cT * (v[d.ij1] * sT[d.ij] * hx[i] / (hy[j] * 3.0) + v[d.ij_1] * sT[d.ij_1] * hx[i] / (hy[j - 1] * 3.0) +
+      Scv = cT * (div_cr(v[d.ij1] * sT[d.ij] * hx[i], hy[j] * 3.0, g.r3y[j]) +
+                  div_cr(v[d.ij_1] * sT[d.ij_1] * hx[i], hy[j - 1] * 3.0, g.r3y[j - 1]) +
                   g.Gamma_xf[d.i1j] * (u[d.i1j] - u[d.i1j_1]) - g.Gamma_xf[d.ij] * (u[d.ij] - u[d.ij_1]) -
-                  sT[d.ij] * (u[d.i1j] - u[d.ij]) * 2.0 / 3.0 + sT[d.ij_1] * (u[d.i1j_1] - u[d.ij_1]) * 2.0 / 3.0) -
+                  div_cr(sT[d.ij] * (u[d.i1j] - u[d.ij]) * 2.0, 3.0, g.r3) +
+                  div_cr(sT[d.ij_1] * (u[d.i1j_1] - u[d.ij_1]) * 2.0, 3.0, g.r3)) -
             g.c_Fr_v * (rho[d.ij_1] * hx[i] * 0.5 * hy[j - 1] + rho[d.ij] * hx[i] * 0.5 * hy[j]);
     }
-    const double Spv = -(g.D_vy[d.ij] + g.D_vy[d.ij1]) / 3.0;
+    const double Spv = div_cr(-(g.D_vy[d.ij] + g.D_vy[d.ij1]), 3.0, g.r3);
     const double av1 = 0.5 * (dmax0(0, Fx[d.ij]) + dmax0(0, Fx[d.ij_1])) + g.D_vx[d.ij];
     const double av2 = 0.5 * (dmax0(0, -Fx[d.i1j]) + dmax0(0, -Fx[d.i1j_1])) + g.D_vx[d.i1j];
     const double av3 = dmax0(0, F_yv3) + g.D_vy[d.ij];
     const double av4 = dmax0(0, -F_yv4) + g.D_vy[d.ij1];
-    const double bv3 = (rho_pr[d.ij_1] * hy[j - 1] + rho_pr[d.ij] * hy[j]) * g.v_pr[d.ij] * hx[i] * 0.5 / ht + Scv;
+    const double bv3 = div_cr((rho_pr[d.ij_1] * hy[j - 1] + rho_pr[d.ij] * hy[j]) * g.v_pr[d.ij] * hx[i] * 0.5, ht, g.rht) + Scv;
     const double av0 = av1 + av2 + av3 + av4 + 0.5 * (Fx[d.i1j] - Fx[d.ij] + Fx[d.i1j_1] - Fx[d.ij_1]) + F_yv4 - F_yv3 -
-                       Spv + (rho[d.ij_1] * hy[j - 1] + rho[d.ij] * hy[j]) * hx[i] * 0.5 / ht;
+                       Spv + div_cr((rho[d.ij_1] * hy[j - 1] + rho[d.ij] * hy[j]) * hx[i] * 0.5, ht, g.rht);
     double vp;
     if (cv == CLS_BC)
       vp = (av1 * v[d.i_1j] + av2 * v[d.i1j] + av3 * B(far) * v[d.ij_1] + av4 * B(d.ij1) * v[d.ij1] + bv3) / av0;
@@ -396,8 +400,8 @@ __device__ __forceinline__ void assemble_body(const Geo& g, unsigned long long h
     const int jm = j - (0 < j ? 1 : 0), jp = j + (j < (Nx - 1) ? 1 : 0);  // j is compared with Nx here (:3677)
     double dudx, dvdy, s0, s1, s2, s3;
     if (co == CLS_BC) {
-      dudx = (B(d.i1j) * u[d.i1j] - B(d.i_1j) * u[d.ij]) / hx[i];
-      dvdy = (B(d.ij1) * v[d.ij1] - B(d.ij_1) * v[d.ij]) / hy[j];
+      dudx = div_cr(B(d.i1j) * u[d.i1j] - B(d.i_1j) * u[d.ij], hx[i], g.rhx[i]);
+      dvdy = div_cr(B(d.ij1) * v[d.ij1] - B(d.ij_1) * v[d.ij], hy[j], g.rhy[j]);
       s0 = ((u[d.ij] - u[d.ij_1]) / ((double)(BB(d.i_1j_1) && BB(d.ij_1)) * hy[jm] + hy[j])) +
            ((v[d.ij] - v[d.i_1j]) / ((double)(BB(d.i_1j_1) && BB(d.i_1j)) * hx[d.i_1] + hx[i]));
       s1 = ((u[d.i1j] - u[d.i1j_1]) / ((double)(BB(d.ij_1) && BB(d.i1j_1)) * hy[jm] + hy[j])) +
@@ -407,16 +411,19 @@ __device__ __forceinline__ void assemble_body(const Geo& g, unsigned long long h
       s3 = ((u[d.i1j1] - u[d.i1j]) / (hy[j] + (double)(BB(d.ij1) && BB(d.i1j1)) * hy[jp])) +
            ((v[d.i1j1] - v[d.ij1]) / (hx[i] + (double)(BB(d.i1j) && BB(d.i1j1)) * hx[d.i1]));
     } else {
-      dudx = (u[d.i1j] - u[d.ij]) / hx[i];
-      dvdy = (v[d.ij1] - v[d.ij]) / hy[j];
-      s0 = ((u[d.ij] - u[d.ij_1]) / (hy[jm] + hy[j])) + ((v[d.ij] - v[d.i_1j]) / (hx[d.i_1] + hx[i]));
-      s1 = ((u[d.i1j] - u[d.i1j_1]) / (hy[jm] + hy[j])) + ((v[d.i1j] - v[d.ij]) / (hx[i] + hx[d.i1]));
-      s2 = ((u[d.ij1] - u[d.ij]) / (hy[j] + hy[jp])) + ((v[d.ij1] - v[d.i_1j1]) / (hx[d.i_1] + hx[i]));
-      s3 = ((u[d.i1j1] - u[d.i1j]) / (hy[j] + hy[jp])) + ((v[d.i1j1] - v[d.ij1]) / (hx[i] + hx[d.i1]));
+      // the interior cells' sums hy[jm] + hy[j], hy[j] + hy[jp] and their x counterparts have
+      // correctly rounded reciprocal tables (jp as here, clamped to the mesh for the table)
+      const double rym = g.ryy_m[j], ryp = g.ryy_p[j], rxm = g.rxx_m[i], rxp = g.rxx_p[i];
+      dudx = div_cr(u[d.i1j] - u[d.ij], hx[i], g.rhx[i]);
+      dvdy = div_cr(v[d.ij1] - v[d.ij], hy[j], g.rhy[j]);
+      s0 = div_cr(u[d.ij] - u[d.ij_1], hy[jm] + hy[j], rym) + div_cr(v[d.ij] - v[d.i_1j], hx[d.i_1] + hx[i], rxm);
+      s1 = div_cr(u[d.i1j] - u[d.i1j_1], hy[jm] + hy[j], rym) + div_cr(v[d.i1j] - v[d.ij], hx[i] + hx[d.i1], rxp);
+      s2 = div_cr(u[d.ij1] - u[d.ij], hy[j] + hy[jp], ryp) + div_cr(v[d.ij1] - v[d.i_1j1], hx[d.i_1] + hx[i], rxm);
+      s3 = div_cr(u[d.i1j1] - u[d.i1j], hy[j] + hy[jp], ryp) + div_cr(v[d.i1j1] - v[d.ij1], hx[i] + hx[d.i1], rxp);
     }
     g.ScT1[d.ij] = ht * sT[d.ij] * g.cT2 * hx[i] * hy[j] *
                        (2.0 * (dudx * dudx + dvdy * dvdy) + s0 * s0 + s1 * s1 + s2 * s2 + s3 * s3 -
-                        (dudx + dvdy) * (dudx + dvdy) * 2.0 / 3.0) +
+                        div_cr((dudx + dvdy) * (dudx + dvdy) * 2.0, 3.0, g.r3)) +
                    g.p_pr[d.ij] * hx[i] * hy[j];
   }
 }
@@ -1280,9 +1287,10 @@ namespace sts {
 // Self-check of div_cr against the IEEE quotient on n pseudo-random operand pairs (a splitmix64
 // stream from `seed`): random signs and significands, dividend exponents over 2^-920..2^920 (so
 // some pairs take the IEEE fallback), divisor exponents over 2^-110..2^110, one divisor in eight
-// with an all-ones significand, and every fourth dividend formed as a rounded product q*b so
-// that the quotient is exact or within an ulp of a representable number.  Counts the pairs whose
-// results differ in any bit.
+// with an all-ones significand, every fourth dividend formed as a rounded product q*b so that
+// the quotient is exact or within an ulp of a representable number, and one dividend in sixteen
+// a zero of either sign.  Counts the pairs whose results differ in any bit (the sign of a zero
+// included).
 __device__ __forceinline__ unsigned long long splitmix64(unsigned long long& s) {
   unsigned long long z = (s += 0x9E3779B97F4A7C15ull);
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -1307,6 +1315,7 @@ __global__ void k_check_division(unsigned long long n, unsigned long long seed, 
     const double b = make_double(r2, -110, 110, (r3 & 7) == 0);
     double a = make_double(r1, -920, 920, false);
     if (((r3 >> 3) & 3) == 0) a = __dmul_rn(make_double(r1, -700, 700, false), b);
+    if (((r3 >> 5) & 15) == 0) a = ((r3 >> 9) & 1) ? -0.0 : 0.0;  // signed zero dividends
     const double y = __ddiv_rn(1.0, b);
     const double q1 = div_cr(a, b, y), q2 = __ddiv_rn(a, b);
     if (__double_as_longlong(q1) != __double_as_longlong(q2)) local++;
