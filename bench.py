@@ -45,16 +45,16 @@ BYTES_PER_CELL = {
 # DRAM bytes per launch measured by ncu on this workload, FP64 path (dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch of the fourteenth time step, cold cache); None where no
 # capture was taken
-TRAFFIC = {"assemble": 20982016 + 512, "sweep_loop": 18983680 + 13568, "flux_diff": 9731840}
+TRAFFIC = {"assemble": 21020160 + 256, "sweep_loop": 18984448 + 25088, "flux_diff": 9726464}
 
 # FP64 instructions per cell of the FP64 path's kernels (per cell and sweep for the sweep loop),
 # counted by ncu on this workload (smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on
 # of one launch divided by its 1203 x 123 cells and, for the sweep loop, by its 8 sweeps).  The
 # kernels are bound by the FP64 unit, so their roofline is this work at the device's measured
 # FP64 rates (sts_fp64_rates) against the measured launch time.
-FP64_OPS = {"assemble": {"add": 104.24, "mul": 134.77, "fma": 371.65},
+FP64_OPS = {"assemble": {"add": 106.17, "mul": 115.10, "fma": 62.58},
             "sweep_loop": {"add": 22.75, "mul": 16.55, "fma": 19.22},
-            "flux_diff": {"add": 23.58, "mul": 65.25, "fma": 63.57}}
+            "flux_diff": {"add": 23.58, "mul": 65.23, "fma": 63.32}}
 
 
 def parse():
