@@ -46,6 +46,16 @@ constexpr int kProfileKinds = 8;
 
 }  // namespace
 
+// The temperature-jump wall values read T, the cell density and static data; the slip walls
+// and the velocity boundary phases write only u and v, and the pressure-begin phase writes p and
+// the cell density on the inlet/outlet columns, and only with the ratio-corrected pressure
+// condition (never in an x-periodic domain).  Unless that can meet a local-Kn jump (which reads
+// the cell density), the jump values need nothing of those kernels and run beside them.
+static bool tjump_beside_walls(uint64_t bits) {
+  if (bits & F_PERIODIC) return true;
+  return !((bits & F_KN_LOCAL) && (bits & F_PRESSURE_BC) && (bits & F_RATIO_CORRECT));
+}
+
 struct sts_ctx {
   Case hc;
   Geo g{};
@@ -309,8 +319,12 @@ int sts_ctx::build_graph() {
   if (int r = add_kernel(&n_bnd, b_outer, {n_walls}, k_boundary, dim3(1), dim3(1024), g,
                          (unsigned)(PH_VEL | PH_PBEGIN), (unsigned long long)0, 0))
     return r;
-  if (int r = add_kernel(&n_tj, b_outer, {n_bnd}, k_bnd_tjump, tjump_grid(), dim3(256), g)) return r;
-  if (int r = add_kernel(&n_fd, b_outer, {n_tj}, flux_kernel(), grid, block, g,
+  if (tjump_beside_walls(g.bits)) {
+    if (int r = add_kernel(&n_tj, b_outer, {n_cor}, k_bnd_tjump, tjump_grid(), dim3(256), g)) return r;
+  } else if (int r = add_kernel(&n_tj, b_outer, {n_bnd}, k_bnd_tjump, tjump_grid(), dim3(256), g)) {
+    return r;
+  }
+  if (int r = add_kernel(&n_fd, b_outer, {n_bnd, n_tj}, flux_kernel(), grid, block, g,
                          (unsigned)(PH_TEMP | PH_PRES)))
     return r;
   CU(cudaGraphInstantiate(&exec, graph, 0));
@@ -1746,8 +1760,10 @@ int sts_batch::build_graph() {
   if (int r = add_kernel(&n[6], b, {n[5]}, kb_boundary, dim3(1, 1, ncases), dim3(1024), G,
                          (unsigned)(PH_VEL | PH_PBEGIN), (unsigned long long)0, 0))
     return r;
-  if (int r = add_kernel(&n[7], b, {n[6]}, kb_bnd_tjump, tjump_grid, dim3(256), G)) return r;
-  if (int r = add_kernel(&n[8], b, {n[7]}, precision == 3 ? kb_flux_diff_df : (fast() ? kb_flux_diff_fast : kb_flux_diff),
+  bool beside = true;
+  for (const sts_ctx* c : cases) beside = beside && tjump_beside_walls(c->g.bits);
+  if (int r = add_kernel(&n[7], b, {beside ? n[3] : n[6]}, kb_bnd_tjump, tjump_grid, dim3(256), G)) return r;
+  if (int r = add_kernel(&n[8], b, {n[6], n[7]}, precision == 3 ? kb_flux_diff_df : (fast() ? kb_flux_diff_fast : kb_flux_diff),
                          cell_grid, blk, G,
                          (unsigned)(PH_TEMP | PH_PRES)))
     return r;
