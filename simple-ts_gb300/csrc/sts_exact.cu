@@ -281,7 +281,34 @@ __global__ void kb_warm_apply(const Geo* gs) {
 // momentum coefficients (u: SIMPLE_TS_MPI.cpp:3269-3344 bc, :3478-3545 nch;
 // v: :3373-3450 bc, :3561-3630 nch) and the energy source ScT1 (:3655-3756)
 // ---------------------------------------------------------------------------
+// The interior form's corner term of ScT1 at cell (i, j) (s0 below): it belongs to the mesh
+// vertex at the cell's lower-left corner, and s1, s2, s3 of a cell are s0 of its east, north and
+// north-east neighbours whenever those neighbours are the plain i+1 / j+1 cells (same operands,
+// same operations, so the same bits).
+__device__ __forceinline__ double corner_s0(const Geo& g, int i, int j) {
+  const Nb d = neighbours(i, j, g.Nx, g.Ny, g.bits & F_PERIODIC);
+  const int jm = j - (0 < j ? 1 : 0);
+  return div_cr(g.u[d.ij] - g.u[d.ij_1], g.hy[jm] + g.hy[j], g.ryy_m[j]) +
+         div_cr(g.v[d.ij] - g.v[d.i_1j], g.hx[d.i_1] + g.hx[i], g.rxx_m[i]);
+}
+
+constexpr int kAsmCorners = 400;  // corners of the largest block shape the tuner uses (128x2 + 1)
+
 __device__ __forceinline__ void assemble_body(const Geo& g, unsigned long long h_sweep, int in_graph) {
+  // corner terms of the block's cells and of one more column and row, computed once each by
+  // the block's threads in turn
+  __shared__ double corner[kAsmCorners];
+  const int W1 = blockDim.x + 1, ncorner = W1 * (blockDim.y + 1);
+  const bool shared_corners = ncorner <= kAsmCorners;
+  if (shared_corners) {
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x, nthr = blockDim.x * blockDim.y;
+    const int i0 = blockIdx.x * blockDim.x, j0 = blockIdx.y * blockDim.y;
+    for (int q = tid; q < ncorner; q += nthr) {
+      const int py = q / W1, px = q - py * W1, ci = i0 + px, cj = j0 + py;
+      corner[q] = (ci < g.Nx && cj < g.Ny) ? corner_s0(g, ci, cj) : 0.0;
+    }
+    __syncthreads();
+  }
   Cell c = cell(g);
   Ctl* ctl = g.ctl;
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
@@ -416,10 +443,19 @@ __device__ __forceinline__ void assemble_body(const Geo& g, unsigned long long h
       const double rym = g.ryy_m[j], ryp = g.ryy_p[j], rxm = g.rxx_m[i], rxp = g.rxx_p[i];
       dudx = div_cr(u[d.i1j] - u[d.ij], hx[i], g.rhx[i]);
       dvdy = div_cr(v[d.ij1] - v[d.ij], hy[j], g.rhy[j]);
-      s0 = div_cr(u[d.ij] - u[d.ij_1], hy[jm] + hy[j], rym) + div_cr(v[d.ij] - v[d.i_1j], hx[d.i_1] + hx[i], rxm);
-      s1 = div_cr(u[d.i1j] - u[d.i1j_1], hy[jm] + hy[j], rym) + div_cr(v[d.i1j] - v[d.ij], hx[i] + hx[d.i1], rxp);
-      s2 = div_cr(u[d.ij1] - u[d.ij], hy[j] + hy[jp], ryp) + div_cr(v[d.ij1] - v[d.i_1j1], hx[d.i_1] + hx[i], rxm);
-      s3 = div_cr(u[d.i1j1] - u[d.i1j], hy[j] + hy[jp], ryp) + div_cr(v[d.i1j1] - v[d.ij1], hx[i] + hx[d.i1], rxp);
+      // east: d.i1 is i + 1 (no clamp or wrap); north: d.ij1 is one row up and jp = j + 1
+      const bool east = shared_corners && d.i1 == i + 1, north = shared_corners && j + 1 < g.Ny && j < Nx - 1;
+      const int q = threadIdx.x + threadIdx.y * W1;
+      s0 = shared_corners ? corner[q]
+                          : div_cr(u[d.ij] - u[d.ij_1], hy[jm] + hy[j], rym) +
+                                div_cr(v[d.ij] - v[d.i_1j], hx[d.i_1] + hx[i], rxm);
+      s1 = east ? corner[q + 1]
+                : div_cr(u[d.i1j] - u[d.i1j_1], hy[jm] + hy[j], rym) + div_cr(v[d.i1j] - v[d.ij], hx[i] + hx[d.i1], rxp);
+      s2 = north ? corner[q + W1]
+                 : div_cr(u[d.ij1] - u[d.ij], hy[j] + hy[jp], ryp) + div_cr(v[d.ij1] - v[d.i_1j1], hx[d.i_1] + hx[i], rxm);
+      s3 = (east && north)
+               ? corner[q + W1 + 1]
+               : div_cr(u[d.i1j1] - u[d.i1j], hy[j] + hy[jp], ryp) + div_cr(v[d.i1j1] - v[d.ij1], hx[i] + hx[d.i1], rxp);
     }
     g.ScT1[d.ij] = ht * sT[d.ij] * g.cT2 * hx[i] * hy[j] *
                        (2.0 * (dudx * dudx + dvdy * dvdy) + s0 * s0 + s1 * s1 + s2 * s2 + s3 * s3 -
