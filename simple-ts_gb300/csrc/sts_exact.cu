@@ -721,7 +721,25 @@ __global__ void kb_face_rho(const Geo* gs) {
 
 // SolveFluxes (SIMPLE_TS_MPI.cpp:10440-10454) and SolveDiffisionTerms (:10457-10618)
 
-__device__ __forceinline__ void flux_diff_cell(const Geo& g, const Cell& c) {
+// The linear interpolations of sqrt(T) behind Gamma_yf and Gamma_xf (LiY, LiX below) belong to
+// cell faces: a cell's west interpolation in y is its west neighbour's own one, and its south
+// interpolation in x is its south neighbour's own one, whenever those neighbours are the plain
+// i-1 / j-1 cells.  A 32x8 block computes each once (with one more column on the west and one
+// more row on the south) in shared memory; the operands and operations are those of the per-cell
+// form, so the values are the same bits.
+__device__ __forceinline__ double li_y_at(const Geo& g, int i, int j) {
+  const Nb d = neighbours(i, j, g.Nx, g.Ny, g.bits & F_PERIODIC);
+  const int jm = j - (0 < j ? 1 : 0);
+  return div_cr(g.sqrt_T[d.ij_1] * g.hy[j] + g.sqrt_T[d.ij] * g.hy[jm], g.hy[jm] + g.hy[j], g.ryy_m[j]);
+}
+__device__ __forceinline__ double li_x_at(const Geo& g, int i, int j) {
+  const Nb d = neighbours(i, j, g.Nx, g.Ny, g.bits & F_PERIODIC);
+  return div_cr(g.sqrt_T[d.i_1j] * g.hx[i] + g.sqrt_T[d.ij] * g.hx[d.i_1], g.hx[d.i_1] + g.hx[i], g.rxx_m[i]);
+}
+constexpr int kFluxLy = 33 * 8, kFluxLx = 32 * 9;
+
+// ly, lx: the block's staged interpolations (null when the block is not 32x8)
+__device__ __forceinline__ void flux_diff_cell(const Geo& g, const Cell& c, const double* ly, const double* lx) {
   const int i = c.i, j = c.j;
   const Nb d = neighbours(i, j, g.Nx, g.Ny, g.bits & F_PERIODIC);
   const double* __restrict__ hx = g.hx;
@@ -741,13 +759,19 @@ __device__ __forceinline__ void flux_diff_cell(const Geo& g, const Cell& c) {
   auto LiY = [&](double f1, double f2) { return div_cr(f1 * hy[j] + f2 * hy[jm], hy[jm] + hy[j], ry); };
   auto LiX = [&](double f1, double f2) { return div_cr(f1 * hx[i] + f2 * hx[d.i_1], hx[d.i_1] + hx[i], rx); };
   auto rsum = [](bool a, bool b, double r_both, double r_a, double r_b) { return a ? (b ? r_both : r_a) : r_b; };
+  const int x = threadIdx.x, y = threadIdx.y;
+  const bool west = ly && d.i_1 == i - 1, south = lx && j > 0;
+  auto ly_west = [&]() { return west ? ly[x + 33 * y] : LiY(sT[d.i_1j_1], sT[d.i_1j]); };
+  auto ly_own = [&]() { return ly ? ly[x + 1 + 33 * y] : LiY(sT[d.ij_1], sT[d.ij]); };
+  auto lx_south = [&]() { return south ? lx[x + 32 * y] : LiX(sT[d.i_1j_1], sT[d.ij_1]); };
+  auto lx_own = [&]() { return lx ? lx[x + 32 * (y + 1)] : LiX(sT[d.i_1j], sT[d.ij]); };
   double Gy = g.Gamma_yf[d.ij], Gx = g.Gamma_xf[d.ij];
   if (b_ws && b_s && b_w && b_p) {
-    Gy = 0.5 * (LiY(sT[d.i_1j_1], sT[d.i_1j]) + LiY(sT[d.ij_1], sT[d.ij]));
+    Gy = 0.5 * (ly_west() + ly_own());
   } else if (b_ws || b_s || b_w || b_p) {
-    Gy = 0.5 * ((double)(b_ws && b_w) * LiY(sT[d.i_1j_1], sT[d.i_1j]) +
+    Gy = 0.5 * ((double)(b_ws && b_w) * ly_west() +
                 (double)(b_ws != b_w) * sqrt(Tw_v[d.i_1j]) +
-                (double)(b_s && b_p) * LiY(sT[d.ij_1], sT[d.ij]) + (double)(b_s != b_p) * sqrt(Tw_v[d.ij]) +
+                (double)(b_s && b_p) * ly_own() + (double)(b_s != b_p) * sqrt(Tw_v[d.ij]) +
                 (double)((!(b_ws && b_w)) || (!(b_s && b_p))) * LiY(sqrt(Tw_u[d.ij_1]), sqrt(Tw_u[d.ij])));
   }
   g.Gamma_yf[d.ij] = Gy;
@@ -758,11 +782,11 @@ __device__ __forceinline__ void flux_diff_cell(const Geo& g, const Cell& c) {
   else
     g.D_uy[d.ij] = 0;
   if (b_ws && b_s && b_w && b_p) {
-    Gx = 0.5 * (LiX(sT[d.i_1j_1], sT[d.ij_1]) + LiX(sT[d.i_1j], sT[d.ij]));
+    Gx = 0.5 * (lx_south() + lx_own());
   } else if (b_ws || b_s || b_w || b_p) {
-    Gx = 0.5 * ((double)(b_ws && b_s) * LiX(sT[d.i_1j_1], sT[d.ij_1]) +
+    Gx = 0.5 * ((double)(b_ws && b_s) * lx_south() +
                 (double)(b_ws != b_s) * sqrt(Tw_u[d.ij_1]) +
-                (double)(b_w && b_p) * LiX(sT[d.i_1j], sT[d.ij]) + (double)(b_w != b_p) * sqrt(Tw_u[d.ij]) +
+                (double)(b_w && b_p) * lx_own() + (double)(b_w != b_p) * sqrt(Tw_u[d.ij]) +
                 (double)((!(b_ws && b_s)) || (!(b_w && b_p))) * LiX(sqrt(Tw_v[d.i_1j]), sqrt(Tw_v[d.ij])));
   }
   g.Gamma_xf[d.ij] = Gx;
@@ -792,8 +816,22 @@ __device__ __forceinline__ void flux_diff_cell(const Geo& g, const Cell& c) {
 // The zero-gradient temperature and pressure copies (phases `tail`) touch only ghost cells of p
 // and T, which the fluxes and diffusion terms do not read, so the first CTA does them too.
 __device__ __forceinline__ void flux_diff_body(const Geo& g, unsigned tail) {
+  __shared__ double ly[kFluxLy], lx[kFluxLx];
+  const bool staged = blockDim.x == 32 && blockDim.y == 8;
+  if (staged) {
+    const int tid = threadIdx.x + 32 * threadIdx.y, i0 = blockIdx.x * 32, j0 = blockIdx.y * 8;
+    for (int q = tid; q < kFluxLy; q += 256) {  // faces of columns i0-1 .. i0+31
+      const int py = q / 33, ci = i0 - 1 + (q - 33 * py), cj = j0 + py;
+      ly[q] = (ci >= 0 && ci < g.Nx && cj < g.Ny) ? li_y_at(g, ci, cj) : 0.0;
+    }
+    for (int q = tid; q < kFluxLx; q += 256) {  // faces of rows j0-1 .. j0+7
+      const int ci = i0 + (q & 31), cj = j0 - 1 + (q >> 5);
+      lx[q] = (ci < g.Nx && cj >= 0 && cj < g.Ny) ? li_x_at(g, ci, cj) : 0.0;
+    }
+    __syncthreads();
+  }
   Cell c = cell(g);
-  if (c.ok) flux_diff_cell(g, c);
+  if (c.ok) flux_diff_cell(g, c, staged ? ly : nullptr, staged ? lx : nullptr);
   if (tail && blockIdx.x == 0 && blockIdx.y == 0) {
     const int tid = threadIdx.x + threadIdx.y * blockDim.x, nt = blockDim.x * blockDim.y;
     const unsigned cur = g.ctl->cur;
