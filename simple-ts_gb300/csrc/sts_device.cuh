@@ -24,6 +24,15 @@ __device__ __forceinline__ unsigned long long as_b(double d) { return (unsigned 
 // being evaluated (predicated) beside every fast division.
 __device__ __noinline__ double div_ieee(double a, double b) { return __ddiv_rn(a, b); }
 
+// The IEEE quotient a / b, with zero dividends answered directly: for every b that is neither
+// zero nor NaN, 0 / b is the zero whose sign is sign(a) xor sign(b), which a * copysign(1, b)
+// gives exactly; every other pair takes the division.  Zero dividends are common in the fields
+// (v vanishes over much of a channel) and slow for the IEEE division.
+__device__ __forceinline__ double div_z(double a, double b) {
+  if (a == 0.0 && (b > 0.0 || b < 0.0)) return __dmul_rn(a, copysign(1.0, b));
+  return __ddiv_rn(a, b);
+}
+
 // Correctly rounded a / b from y = RN(1/b), the division by a correctly rounded reciprocal of
 // P. Markstein (IBM J. Res. Develop. 34(1), 1990; Muller et al., Handbook of Floating-Point
 // Arithmetic, 2nd ed., sec. 4.9): q0 = RN(a y) is within two units in the last place of a/b;

@@ -367,9 +367,9 @@ __device__ __forceinline__ void assemble_body(const Geo& g, unsigned long long h
                        Spu + div_cr((rho[d.i_1j] * hx[d.i_1] + rho[d.ij] * hx[i]) * hy[j] * 0.5, ht, g.rht);
     double up;
     if (cu == CLS_BC)
-      up = (au1 * B(d.i1j) * u[d.i_1j] + au2 * B(d.i_2j) * u[d.i1j] + au3 * u[d.ij_1] + au4 * u[d.ij1] + bu3) / au0;
+      up = div_z(au1 * B(d.i1j) * u[d.i_1j] + au2 * B(d.i_2j) * u[d.i1j] + au3 * u[d.ij_1] + au4 * u[d.ij1] + bu3, au0);
     else
-      up = (au1 * u[d.i_1j] + au2 * u[d.i1j] + au3 * u[d.ij_1] + au4 * u[d.ij1] + bu3) / au0;
+      up = div_z(au1 * u[d.i_1j] + au2 * u[d.i1j] + au3 * u[d.ij_1] + au4 * u[d.ij1] + bu3, au0);
     const double dpc = cPch * hy[j] / au0;
     const double hr = hy[j] * g.rho_u[d.ij];
     g.u_pseudo[d.ij] = up;
@@ -411,9 +411,9 @@ __device__ __forceinline__ void assemble_body(const Geo& g, unsigned long long h
                        Spv + div_cr((rho[d.ij_1] * hy[j - 1] + rho[d.ij] * hy[j]) * hx[i] * 0.5, ht, g.rht);
     double vp;
     if (cv == CLS_BC)
-      vp = (av1 * v[d.i_1j] + av2 * v[d.i1j] + av3 * B(far) * v[d.ij_1] + av4 * B(d.ij1) * v[d.ij1] + bv3) / av0;
+      vp = div_z(av1 * v[d.i_1j] + av2 * v[d.i1j] + av3 * B(far) * v[d.ij_1] + av4 * B(d.ij1) * v[d.ij1] + bv3, av0);
     else
-      vp = (av1 * v[d.i_1j] + av2 * v[d.i1j] + av3 * v[d.ij_1] + av4 * v[d.ij1] + bv3) / av0;
+      vp = div_z(av1 * v[d.i_1j] + av2 * v[d.i1j] + av3 * v[d.ij_1] + av4 * v[d.ij1] + bv3, av0);
     const double dpc = cPch * hx[i] / av0;
     const double hr = hx[i] * g.rho_v[d.ij];
     g.v_pseudo[d.ij] = vp;
@@ -429,14 +429,14 @@ __device__ __forceinline__ void assemble_body(const Geo& g, unsigned long long h
     if (co == CLS_BC) {
       dudx = div_cr(B(d.i1j) * u[d.i1j] - B(d.i_1j) * u[d.ij], hx[i], g.rhx[i]);
       dvdy = div_cr(B(d.ij1) * v[d.ij1] - B(d.ij_1) * v[d.ij], hy[j], g.rhy[j]);
-      s0 = ((u[d.ij] - u[d.ij_1]) / ((double)(BB(d.i_1j_1) && BB(d.ij_1)) * hy[jm] + hy[j])) +
-           ((v[d.ij] - v[d.i_1j]) / ((double)(BB(d.i_1j_1) && BB(d.i_1j)) * hx[d.i_1] + hx[i]));
-      s1 = ((u[d.i1j] - u[d.i1j_1]) / ((double)(BB(d.ij_1) && BB(d.i1j_1)) * hy[jm] + hy[j])) +
-           ((v[d.i1j] - v[d.ij]) / (hx[i] + (double)(BB(d.i1j_1) && BB(d.i1j)) * hx[d.i1]));
-      s2 = ((u[d.ij1] - u[d.ij]) / (hy[j] + (double)(BB(d.i_1j1) && BB(d.ij1)) * hy[jp])) +
-           ((v[d.ij1] - v[d.i_1j1]) / ((double)(BB(d.i_1j) && BB(d.i_1j1)) * hx[d.i_1] + hx[i]));
-      s3 = ((u[d.i1j1] - u[d.i1j]) / (hy[j] + (double)(BB(d.ij1) && BB(d.i1j1)) * hy[jp])) +
-           ((v[d.i1j1] - v[d.ij1]) / (hx[i] + (double)(BB(d.i1j) && BB(d.i1j1)) * hx[d.i1]));
+      s0 = div_z(u[d.ij] - u[d.ij_1], (double)(BB(d.i_1j_1) && BB(d.ij_1)) * hy[jm] + hy[j]) +
+           div_z(v[d.ij] - v[d.i_1j], (double)(BB(d.i_1j_1) && BB(d.i_1j)) * hx[d.i_1] + hx[i]);
+      s1 = div_z(u[d.i1j] - u[d.i1j_1], (double)(BB(d.ij_1) && BB(d.i1j_1)) * hy[jm] + hy[j]) +
+           div_z(v[d.i1j] - v[d.ij], hx[i] + (double)(BB(d.i1j_1) && BB(d.i1j)) * hx[d.i1]);
+      s2 = div_z(u[d.ij1] - u[d.ij], hy[j] + (double)(BB(d.i_1j1) && BB(d.ij1)) * hy[jp]) +
+           div_z(v[d.ij1] - v[d.i_1j1], (double)(BB(d.i_1j) && BB(d.i_1j1)) * hx[d.i_1] + hx[i]);
+      s3 = div_z(u[d.i1j1] - u[d.i1j], hy[j] + (double)(BB(d.ij1) && BB(d.i1j1)) * hy[jp]) +
+           div_z(v[d.i1j1] - v[d.ij1], hx[i] + (double)(BB(d.i1j) && BB(d.i1j1)) * hx[d.i1]);
     } else {
       // the interior cells' sums hy[jm] + hy[j], hy[j] + hy[jp] and their x counterparts have
       // correctly rounded reciprocal tables (jp as here, clamped to the mesh for the table)
@@ -932,14 +932,14 @@ __device__ void do_slip_u(const Geo& g, int k) {
     const int jm = j - (0 < j ? 1 : 0);
     const double a_ij = kl ? FK / (g.rho_u[d.ij_1] * 0.5 * g.hy[jm]) : FK / (0.5 * g.hy[jm]);
     const double a_i1j = kl ? FK / (g.rho_u[d.i1j_1] * 0.5 * g.hy[jm]) : FK / (0.5 * g.hy[jm]);
-    if ((fin & 1) && fl(d.i_1j_1)) u[d.ij] = (u[d.ij_1] * a_ij + Bd.u) / (1.0 + a_ij);
-    if ((fin & 2) && fl(d.i1j_1)) u[d.i1j] = (u[d.i1j_1] * a_i1j + Bd.u) / (1.0 + a_i1j);
+    if ((fin & 1) && fl(d.i_1j_1)) u[d.ij] = div_z(u[d.ij_1] * a_ij + Bd.u, 1.0 + a_ij);
+    if ((fin & 2) && fl(d.i1j_1)) u[d.i1j] = div_z(u[d.i1j_1] * a_i1j + Bd.u, 1.0 + a_i1j);
   } else {
     const int jp = j + (j < (Ny - 1) ? 1 : 0);
     const double a_ij = kl ? FK / (g.rho_u[d.ij1] * 0.5 * g.hy[jp]) : FK / (0.5 * g.hy[jp]);
     const double a_i1j = kl ? FK / (g.rho_u[d.i1j1] * 0.5 * g.hy[jp]) : FK / (0.5 * g.hy[jp]);
-    if ((fin & 1) && fl(d.i_1j1)) u[d.ij] = (u[d.ij1] * a_ij + Bd.u) / (1.0 + a_ij);
-    if ((fin & 2) && fl(d.i1j1)) u[d.i1j] = (u[d.i1j1] * a_i1j + Bd.u) / (1.0 + a_i1j);
+    if ((fin & 1) && fl(d.i_1j1)) u[d.ij] = div_z(u[d.ij1] * a_ij + Bd.u, 1.0 + a_ij);
+    if ((fin & 2) && fl(d.i1j1)) u[d.i1j] = div_z(u[d.i1j1] * a_i1j + Bd.u, 1.0 + a_i1j);
   }
 }
 
@@ -961,13 +961,13 @@ __device__ void do_slip_v(const Geo& g, int k) {
   if (g.vol_id[d.i_1j] == 0) {
     const double a_ij = kl ? FK / (g.rho_v[d.i_1j] * 0.5 * g.hx[d.i_1]) : FK / (0.5 * g.hx[d.i_1]);
     const double a_ij1 = kl ? FK / (g.rho_v[d.i_1j1] * 0.5 * g.hx[d.i_1]) : FK / (0.5 * g.hx[d.i_1]);
-    if ((fin & 1) && fl(d.i_1j_1)) v[d.ij] = (v[d.i_1j] * a_ij + Bd.v) / (1.0 + a_ij);
-    if ((fin & 2) && fl(d.i_1j1)) v[d.ij1] = (v[d.i_1j1] * a_ij1 + Bd.v) / (1.0 + a_ij1);
+    if ((fin & 1) && fl(d.i_1j_1)) v[d.ij] = div_z(v[d.i_1j] * a_ij + Bd.v, 1.0 + a_ij);
+    if ((fin & 2) && fl(d.i_1j1)) v[d.ij1] = div_z(v[d.i_1j1] * a_ij1 + Bd.v, 1.0 + a_ij1);
   } else {
     const double a_ij = kl ? FK / (g.rho_v[d.i1j] * 0.5 * g.hx[d.i1]) : FK / (0.5 * g.hx[d.i1]);
     const double a_ij1 = kl ? FK / (g.rho_v[d.i1j1] * 0.5 * g.hx[d.i1]) : FK / (0.5 * g.hx[d.i1]);
-    if ((fin & 1) && fl(d.i1j_1)) v[d.ij] = (v[d.i1j] * a_ij + Bd.v) / (1.0 + a_ij);
-    if ((fin & 2) && fl(d.i1j1)) v[d.ij1] = (v[d.i1j1] * a_ij1 + Bd.v) / (1.0 + a_ij1);
+    if ((fin & 1) && fl(d.i1j_1)) v[d.ij] = div_z(v[d.i1j] * a_ij + Bd.v, 1.0 + a_ij);
+    if ((fin & 2) && fl(d.i1j1)) v[d.ij1] = div_z(v[d.i1j1] * a_ij1 + Bd.v, 1.0 + a_ij1);
   }
 }
 
@@ -1086,7 +1086,7 @@ __device__ __forceinline__ void boundary_body(const Geo& g, unsigned phases, uns
     if (bits & F_DURHODX0_XB) {
       for (int j = tid; j < Ny; j += nt) {
         const int n = g.Nx_u0 - 1 + j * Nx;
-        if (fl(n)) u[n] = (g.rho_u[n + 1] * u[n + 1]) / g.rho_u[n];
+        if (fl(n)) u[n] = div_z(g.rho_u[n + 1] * u[n + 1], g.rho_u[n]);
       }
       __syncthreads();
     }
@@ -1113,7 +1113,7 @@ __device__ __forceinline__ void boundary_body(const Geo& g, unsigned phases, uns
     if (bits & F_DURHODX0_XE) {
       for (int j = tid; j < Ny; j += nt) {
         const int n = g.Nx_u1 - 1 + j * Nx;
-        if (fl(n)) u[n + 1] = (g.rho_u[n] * u[n]) / g.rho_u[n + 1];
+        if (fl(n)) u[n + 1] = div_z(g.rho_u[n] * u[n], g.rho_u[n + 1]);
       }
       __syncthreads();
     }
