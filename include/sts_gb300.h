@@ -118,10 +118,12 @@ int sts_get_field(sts_ctx* ctx, const char* name, double* host_out);
 int sts_set_field(sts_ctx* ctx, const char* name, const double* host_in);
 
 /* The state the reference dumps -- u, v, p, T (Nx*Ny doubles each) -- to or from host memory in
- * one call: the four copies are queued together and the call returns once they are done (one
- * synchronisation instead of four).  For callers that exchange the whole state every step; host
- * buffers in pinned memory copy fastest.  sts_set_state has sts_set_field's effect on each field
- * (a warm start's history starts over). */
+ * one call that returns once the data has moved (one synchronisation instead of four).  For
+ * callers that exchange the whole state every step.  Host buffers the device can address
+ * (pinned by cudaHostAlloc / cudaMallocHost, or registered with cudaHostRegister) are read or
+ * written by one kernel that moves all four fields at once; other host memory goes through four
+ * copies.  sts_set_state has sts_set_field's effect on each field (a warm start's history
+ * starts over). */
 int sts_set_state(sts_ctx* ctx, const double* u_in, const double* v_in, const double* p_in, const double* T_in);
 int sts_get_state(sts_ctx* ctx, double* u_out, double* v_out, double* p_out, double* T_out);
 
@@ -216,10 +218,12 @@ int sts_pt_sweeps_noalloc(const sts_sweep_fields* f, int max_sweeps, int fixed_s
                           void* stream, int* sweeps_done, double* res_p, double* res_T);
 
 /* Self-check of the library's division through correctly rounded reciprocals (used by the FP64
- * kernels for divisors fixed by the mesh or by the outer iteration; Markstein's method) against
- * IEEE division on `device`: n pseudo-random operand pairs from `seed`, *mismatches receives the
- * number of results that differ in any bit (0 is the only passing answer).  No counterpart in
- * the reference, which divides with the host's IEEE division. */
+ * kernels for divisors fixed by the mesh or by the outer iteration; Markstein's method) and of
+ * its IEEE division with zero dividends answered directly, against IEEE division on `device`:
+ * n pseudo-random operand pairs from `seed` (zero dividends and zero, infinite and NaN divisors
+ * among them), *mismatches receives the number of results that differ in any bit (0 is the only
+ * passing answer).  No counterpart in the reference, which divides with the host's IEEE
+ * division. */
 int sts_check_division(unsigned long long n, unsigned long long seed, int device, unsigned long long* mismatches);
 
 /* FP64 throughput of `device`, measured: gops[0..2] receive the rates (10^9 operations per

@@ -12,6 +12,7 @@
 // block of each sweep (SIMPLE_TS_MPI.cpp:4099-4107), which also drives the CUDA
 // graph's conditional WHILE node.
 #include <cuda_runtime.h>
+#include <math_constants.h>
 
 #include "sts_common.cuh"
 #include "sts_kernels.h"
@@ -1363,8 +1364,10 @@ namespace sts {
 // some pairs take the IEEE fallback), divisor exponents over 2^-110..2^110, one divisor in eight
 // with an all-ones significand, every fourth dividend formed as a rounded product q*b so that
 // the quotient is exact or within an ulp of a representable number, and one dividend in sixteen
-// a zero of either sign.  Counts the pairs whose results differ in any bit (the sign of a zero
-// included).
+// a zero of either sign.  Each pair also checks div_z (the IEEE division with zero dividends
+// answered directly) against the IEEE quotient, one divisor in eight then replaced by a zero
+// of either sign, an infinity or NaN.  Counts the results that differ in any bit (the sign of
+// a zero included).
 __device__ __forceinline__ unsigned long long splitmix64(unsigned long long& s) {
   unsigned long long z = (s += 0x9E3779B97F4A7C15ull);
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -1393,9 +1396,29 @@ __global__ void k_check_division(unsigned long long n, unsigned long long seed, 
     const double y = __ddiv_rn(1.0, b);
     const double q1 = div_cr(a, b, y), q2 = __ddiv_rn(a, b);
     if (__double_as_longlong(q1) != __double_as_longlong(q2)) local++;
+    // div_z, also with zero, infinite and NaN divisors
+    double bz = b;
+    const unsigned sp = (unsigned)(r3 >> 12) & 31u;
+    if (sp == 1) bz = ((r3 >> 17) & 1) ? -0.0 : 0.0;
+    if (sp == 2) bz = ((r3 >> 17) & 1) ? -CUDART_INF : CUDART_INF;
+    if (sp == 3) bz = CUDART_NAN;
+    if (__double_as_longlong(div_z(a, bz)) != __double_as_longlong(__ddiv_rn(a, bz))) local++;
   }
   for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
   if ((threadIdx.x & 31) == 0 && local) atomicAdd(bad, local);
+}
+
+// The state exchange with host buffers the device can address (pinned or registered memory):
+// one grid-stride pass moves all four fields, so the four transfers share the host link at
+// once instead of queueing on the copy engines one after another.
+__global__ void k_move4(const double* __restrict__ a0, const double* __restrict__ a1, const double* __restrict__ a2,
+                        const double* __restrict__ a3, double* b0, double* b1, double* b2, double* b3, int n) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    b0[k] = a0[k];
+    b1[k] = a1[k];
+    b2[k] = a2[k];
+    b3[k] = a3[k];
+  }
 }
 
 // FP64 throughput of the device: every thread advances 8 independent chains `iters` times with

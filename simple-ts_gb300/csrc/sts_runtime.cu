@@ -1218,6 +1218,24 @@ int sts_set_field(sts_ctx* ctx, const char* name, const double* in) {
   return STS_OK;
 }
 
+// Device addresses of host buffers the device can read and write directly (memory pinned by
+// cudaHostAlloc / cudaMallocHost or registered with cudaHostRegister); false for any other
+// memory, which then goes through the copy engines.
+static bool mapped_host(const void* const* ptrs, void** dev, int n) {
+  for (int k = 0; k < n; k++) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, ptrs[k]) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return false;
+    dev[k] = a.devicePointer;
+  }
+  return true;
+}
+
+static int move_grid(int n) { return std::max(1, std::min((n + 255) / 256, 4 * 152)); }
+
 int sts_set_state(sts_ctx* ctx, const double* u_in, const double* v_in, const double* p_in, const double* T_in) {
   if (!ctx || !u_in || !v_in || !p_in || !T_in) return fail(STS_ERR_ARG, "null argument");
   CU(cudaSetDevice(ctx->opt.device));
@@ -1226,10 +1244,18 @@ int sts_set_state(sts_ctx* ctx, const double* u_in, const double* v_in, const do
   const Geo& g = ctx->g;
   const unsigned cur = ctx->h_ctl->cur;
   const size_t bytes = sizeof(double) * g.Na;
-  CU(cudaMemcpyAsync(g.u, u_in, bytes, cudaMemcpyHostToDevice, ctx->s));
-  CU(cudaMemcpyAsync(g.v, v_in, bytes, cudaMemcpyHostToDevice, ctx->s));
-  CU(cudaMemcpyAsync(g.p[cur], p_in, bytes, cudaMemcpyHostToDevice, ctx->s));
-  CU(cudaMemcpyAsync(g.T[cur], T_in, bytes, cudaMemcpyHostToDevice, ctx->s));
+  const void* hp[4] = {u_in, v_in, p_in, T_in};
+  void* dp[4];
+  if (mapped_host(hp, dp, 4)) {
+    k_move4<<<move_grid(g.Na), 256, 0, ctx->s>>>((const double*)dp[0], (const double*)dp[1], (const double*)dp[2],
+                                                 (const double*)dp[3], g.u, g.v, g.p[cur], g.T[cur], g.Na);
+    CU(cudaGetLastError());
+  } else {
+    CU(cudaMemcpyAsync(g.u, u_in, bytes, cudaMemcpyHostToDevice, ctx->s));
+    CU(cudaMemcpyAsync(g.v, v_in, bytes, cudaMemcpyHostToDevice, ctx->s));
+    CU(cudaMemcpyAsync(g.p[cur], p_in, bytes, cudaMemcpyHostToDevice, ctx->s));
+    CU(cudaMemcpyAsync(g.T[cur], T_in, bytes, cudaMemcpyHostToDevice, ctx->s));
+  }
   if (g.warm_start) {
     static const unsigned zero = 0;
     CU(cudaMemcpyAsync(&g.ctl->warm_ready, &zero, sizeof(unsigned), cudaMemcpyHostToDevice, ctx->s));
@@ -1246,10 +1272,18 @@ int sts_get_state(sts_ctx* ctx, double* u_out, double* v_out, double* p_out, dou
   const Geo& g = ctx->g;
   const unsigned cur = ctx->h_ctl->cur;
   const size_t bytes = sizeof(double) * g.Na;
-  CU(cudaMemcpyAsync(u_out, g.u, bytes, cudaMemcpyDeviceToHost, ctx->s));
-  CU(cudaMemcpyAsync(v_out, g.v, bytes, cudaMemcpyDeviceToHost, ctx->s));
-  CU(cudaMemcpyAsync(p_out, g.p[cur], bytes, cudaMemcpyDeviceToHost, ctx->s));
-  CU(cudaMemcpyAsync(T_out, g.T[cur], bytes, cudaMemcpyDeviceToHost, ctx->s));
+  const void* hp[4] = {u_out, v_out, p_out, T_out};
+  void* dp[4];
+  if (mapped_host(hp, dp, 4)) {
+    k_move4<<<move_grid(g.Na), 256, 0, ctx->s>>>(g.u, g.v, g.p[cur], g.T[cur], (double*)dp[0], (double*)dp[1],
+                                                 (double*)dp[2], (double*)dp[3], g.Na);
+    CU(cudaGetLastError());
+  } else {
+    CU(cudaMemcpyAsync(u_out, g.u, bytes, cudaMemcpyDeviceToHost, ctx->s));
+    CU(cudaMemcpyAsync(v_out, g.v, bytes, cudaMemcpyDeviceToHost, ctx->s));
+    CU(cudaMemcpyAsync(p_out, g.p[cur], bytes, cudaMemcpyDeviceToHost, ctx->s));
+    CU(cudaMemcpyAsync(T_out, g.T[cur], bytes, cudaMemcpyDeviceToHost, ctx->s));
+  }
   CU(cudaStreamSynchronize(ctx->s));
   return STS_OK;
 }

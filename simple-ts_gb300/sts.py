@@ -298,7 +298,8 @@ def pt_sweeps_noalloc(fields: SweepFields, max_sweeps: int, fixed_sweeps: bool, 
 
 
 def check_division(n: int, seed: int = 1, device: int = 0) -> int:
-    """Pairs (of n) where the library's reciprocal-based division differs from IEEE division."""
+    """Results (of n pairs) where the library's reciprocal-based division, or its IEEE division
+    with zero dividends answered directly, differs from IEEE division in any bit."""
     lib = load()
     lib.sts_check_division.argtypes = [C.c_ulonglong, C.c_ulonglong, C.c_int, C.POINTER(C.c_ulonglong)]
     out = C.c_ulonglong()

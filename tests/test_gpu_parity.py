@@ -139,9 +139,11 @@ def test_nonfinite_residual_is_reported(lib_built):
         assert e.value.code == sts.STS_ERR_NONFINITE
 
 
-def test_state_exchange_equals_field_calls(lib_built):
+@pytest.mark.parametrize("memory", ["pageable", "pinned"])
+def test_state_exchange_equals_field_calls(memory, lib_built):
     """sts_get_state / sts_set_state move the same bytes as four get/set_field calls, and a run
-    continued from a state set either way is the same run."""
+    continued from a state set either way is the same run.  Pinned host buffers take the
+    library's direct kernel path, ordinary ones the copy engines."""
     import sts
     case = sc.channel_case("c", 80, 10, 0.3, 0.002, 1e-3, 40)
     with tempfile.TemporaryDirectory() as d:
@@ -149,7 +151,12 @@ def test_state_exchange_equals_field_calls(lib_built):
         a = sts.Solver(d, fixed_sweeps=False)
         b = sts.Solver(d, fixed_sweeps=False)
         assert a.step(12) == b.step(12) == 12
-        bufs = [np.empty((a.Ny, a.Nx)) for _ in range(4)]
+        if memory == "pinned":
+            torch = pytest.importorskip("torch")
+            pins = [torch.empty((a.Ny, a.Nx), dtype=torch.float64).pin_memory() for _ in range(4)]
+            bufs = [t.numpy() for t in pins]
+        else:
+            bufs = [np.empty((a.Ny, a.Nx)) for _ in range(4)]
         a.get_state_ptr(*[x.ctypes.data for x in bufs])
         for f, x in zip(("u", "v", "p", "T"), bufs):
             np.testing.assert_array_equal(x, a.field(f), err_msg=f)
