@@ -124,6 +124,26 @@ def test_large_meshes_match_oracle(which, steps, lib_built, oracle_built):
         g.close()
 
 
+@pytest.mark.parametrize("nx,ny", [(12, 40), (30, 29)])
+def test_tall_periodic_box_matches_oracle(nx, ny, lib_built, oracle_built):
+    """Domains taller than wide: the energy source's upper neighbour row is chosen by comparing
+    the row with Nx (the reference's own test), so cells from row Nx - 1 up use their own row
+    there; the shared-corner form of the assembly must hand those cells to the per-cell form.
+    A periodic box also exercises the wrap in x."""
+    import ora
+    import sts
+    case = sc.rayleigh_benard_case("rb_tall", nx, ny, Kn=0.01, ht=1e-3, Nt=12)
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        o = ora.Oracle(d, fixed_sweeps=False)
+        g = sts.Solver(d, fixed_sweeps=False)
+        assert g.step(12) == o.step(12) == 12
+        for f in ("u", "v", "p", "T", "rho"):
+            np.testing.assert_array_equal(g.field(f), o.field(f), err_msg=f)
+        np.testing.assert_array_equal(g.sweep_history(), o.sweeps())
+        g.close()
+
+
 def test_nonfinite_residual_is_reported(lib_built):
     import sts
     case = sc.channel_case("c", 40, 6, 0.3, 0.002, 1e-3, 10)
