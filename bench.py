@@ -68,6 +68,10 @@ def parse():
     ap.add_argument("--warm-lead", type=int, default=40,
                     help="untimed steps before the timed ones for warm-started variants (the learned "
                          "predictors fit on the run's own history, which fills in the first 10 steps)")
+    ap.add_argument("--variant-set", default="all", choices=["all", "warm"],
+                    help="which variants to time: all of them, or only the warm-start comparison "
+                         "(plain FP64 against the extrapolated and learned starts) without the "
+                         "checkpoint and untuned-shape lines")
     ap.add_argument("--no-variants", dest="variants", action="store_false",
                     help="skip the FP64-fast and FP32-correction runs of the same workload")
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2, 3],
@@ -531,11 +535,14 @@ def main():
                 ref.close()
             return base[n]
 
-        for name, prec, warm in (("fp64_fast", sts.FAST_FP64, 0), ("fp32_corrections", sts.MIXED, 0),
-                                 ("fp32_corrections_df", sts.MIXED_DF, 0), ("fp32_corrections_df_warm2", sts.MIXED_DF, 2),
-                                 ("fp64_exact_warm2", sts.EXACT, 2), ("fp32_corrections_warm2", sts.MIXED, 2),
-                                 ("fp32_corrections_learned", sts.MIXED, 3), ("fp64_exact_conv", sts.EXACT, 4),
-                                 ("fp32_corrections_conv", sts.MIXED, 4), ("fp32_corrections_df_conv", sts.MIXED_DF, 4)):
+        chosen = (("fp64_fast", sts.FAST_FP64, 0), ("fp32_corrections", sts.MIXED, 0),
+                  ("fp32_corrections_df", sts.MIXED_DF, 0), ("fp32_corrections_df_warm2", sts.MIXED_DF, 2),
+                  ("fp64_exact_warm2", sts.EXACT, 2), ("fp32_corrections_warm2", sts.MIXED, 2),
+                  ("fp32_corrections_learned", sts.MIXED, 3), ("fp64_exact_conv", sts.EXACT, 4),
+                  ("fp32_corrections_conv", sts.MIXED, 4), ("fp32_corrections_df_conv", sts.MIXED_DF, 4))
+        if args.variant_set == "warm":
+            chosen = tuple(x for x in chosen if x[2] in (2, 4))
+        for name, prec, warm in chosen:
             v = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=prec, warm_start=warm)
             lead = lead_w if warm else w
             vd, vms, vsw = timed_steps(v, args.steps, lead, flush, barrier)
@@ -553,12 +560,13 @@ def main():
                 "kernel_ms_per_step": {k: round(x / max(vpn, 1), 5) for k, x in vkms.items() if x > 0}}
             v.close()
 
-    ckpt = checkpoint_bench(d, local, barrier) if args.variants else None
+    full = args.variants and args.variant_set == "all"
+    ckpt = checkpoint_bench(d, local, barrier) if full else None
 
     # the FP64 bit-exact path with the default launch shapes (no autotuning), beside the headline,
     # which uses the shapes the autotuner chose on the run's first steps (the shapes change no result)
     tuned = None
-    if args.variants:
+    if full:
         t = sts.Solver(d, fixed_sweeps=False, use_graph=True, device=local, precision=sts.EXACT, autotune=False)
         td, tms, tsw = timed_steps(t, args.steps, args.warmup, flush, barrier)
         tuned = {"value": Na * td * world / (tms / 1e3), "ms_per_step": tms / max(td, 1),

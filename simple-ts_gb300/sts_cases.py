@@ -462,6 +462,9 @@ def config_case(which: str, scale: float = 1.0, Nt: Optional[int] = None,
     if which == "channel_2048":
         return channel_case("channel_2048", s(2048), s(256), 0.5, 0.003, 1.25e-4,
                             Nt if Nt is not None else 1000, tol=tol)
+    if which.startswith("channel_2048_ma"):  # the 2048x256 channel at another Mach number
+        mach = float(which[len("channel_2048_ma"):])
+        return channel_case(which, s(2048), s(256), mach, 0.003, 1.25e-4, Nt if Nt is not None else 1000, tol=tol)
     raise KeyError(which)
 
 
