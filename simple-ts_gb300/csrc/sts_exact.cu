@@ -739,6 +739,14 @@ __device__ __forceinline__ double li_x_at(const Geo& g, int i, int j) {
 }
 constexpr int kFluxLy = 33 * 8, kFluxLx = 32 * 9;
 
+// The reference's masked sum m_wall * sqrt(tw) + m_cell * h when the masks switch the wall term
+// off (m_wall = 0, m_cell = 1): h itself whenever tw is a finite non-negative number (then
+// 0 * sqrt(tw) is a zero) and h is not a zero (a zero added to h leaves it); any other operands
+// take the sum as written.  It saves the square root where both cells of a face are fluid.
+__device__ __forceinline__ double wall_term_off(double tw, double h) {
+  return (tw >= 0.0 && tw < CUDART_INF && h != 0.0) ? h : 0.0 * sqrt(tw) + 1.0 * h;
+}
+
 // ly, lx: the block's staged interpolations (null when the block is not 32x8)
 __device__ __forceinline__ void flux_diff_cell(const Geo& g, const Cell& c, const double* ly, const double* lx) {
   const int i = c.i, j = c.j;
@@ -777,7 +785,11 @@ __device__ __forceinline__ void flux_diff_cell(const Geo& g, const Cell& c, cons
   }
   g.Gamma_yf[d.ij] = Gy;
   g.D_ux[d.ij] = cT * sT[d.i_1j] * div_cr(hy[j], hx[d.i_1], g.rhx[d.i_1]);
-  if ((b_p && b_w) || (b_s && b_ws))
+  // where every mask is 1 the masked sums are the plain sums (1 * x = x exactly)
+  const bool all4 = b_ws && b_s && b_w && b_p;
+  if (all4)
+    g.D_uy[d.ij] = cT * Gy * div_cr(hx[i] + hx[d.i_1], hy[j] + hy[jm], ry);
+  else if ((b_p && b_w) || (b_s && b_ws))
     g.D_uy[d.ij] = cT * Gy * div_cr(hx[i] + hx[d.i_1], (double)(b_p * b_w) * hy[j] + (double)(b_s * b_ws) * hy[jm],
                                     rsum(b_p && b_w, b_s && b_ws, ry, g.rhy[j], g.rhy[jm]));
   else
@@ -791,21 +803,29 @@ __device__ __forceinline__ void flux_diff_cell(const Geo& g, const Cell& c, cons
                 (double)((!(b_ws && b_s)) || (!(b_w && b_p))) * LiX(sqrt(Tw_v[d.i_1j]), sqrt(Tw_v[d.ij])));
   }
   g.Gamma_xf[d.ij] = Gx;
-  if ((b_p && b_s) || (b_w && b_ws))
+  if (all4)
+    g.D_vx[d.ij] = cT * Gx * div_cr(hy[j] + hy[jm], hx[i] + hx[d.i_1], rx);
+  else if ((b_p && b_s) || (b_w && b_ws))
     g.D_vx[d.ij] = cT * Gx * div_cr(hy[j] + hy[jm], (double)(b_p * b_s) * hx[i] + (double)(b_w * b_ws) * hx[d.i_1],
                                     rsum(b_p && b_s, b_w && b_ws, rx, g.rhx[i], g.rhx[d.i_1]));
   else
     g.D_vx[d.ij] = 0;
   g.D_vy[d.ij] = cT * sT[d.ij_1] * div_cr(hx[i], hy[jm], g.rhy[jm]);
   // 1 / (0.5 s) = 2 (1 / s) exactly
-  if (b_p || b_w)
+  if (b_p && b_w)
+    g.DTx[d.ij] = cT1 * div_cr(hy[j], 0.5 * (hx[i] + hx[d.i_1]), 2.0 * rx) *
+                  wall_term_off(Tw_u[d.ij], Hi(sT[d.i_1j], sT[d.ij], hx[d.i_1], hx[i]));
+  else if (b_p || b_w)
     g.DTx[d.ij] = cT1 * div_cr(hy[j], 0.5 * ((double)b_p * hx[i] + (double)b_w * hx[d.i_1]),
                                2.0 * rsum(b_p, b_w, rx, g.rhx[i], g.rhx[d.i_1])) *
                   ((double)((!b_p) || (!b_w)) * sqrt(Tw_u[d.ij]) +
                    (double)(b_p * b_w) * Hi(sT[d.i_1j], sT[d.ij], hx[d.i_1], hx[i]));
   else
     g.DTx[d.ij] = 0;
-  if (b_p || b_s)
+  if (b_p && b_s)
+    g.DTy[d.ij] = cT1 * div_cr(hx[i], 0.5 * (hy[j] + hy[jm]), 2.0 * ry) *
+                  wall_term_off(Tw_v[d.ij], Hi(sT[d.ij_1], sT[d.ij], hy[jm], hy[j]));
+  else if (b_p || b_s)
     g.DTy[d.ij] = cT1 * div_cr(hx[i], 0.5 * ((double)b_p * hy[j] + (double)b_s * hy[jm]),
                                2.0 * rsum(b_p, b_s, ry, g.rhy[j], g.rhy[jm])) *
                   ((double)((!b_p) || (!b_s)) * sqrt(Tw_v[d.ij]) +
