@@ -45,7 +45,7 @@ BYTES_PER_CELL = {
 # DRAM bytes per launch measured by ncu on this workload, FP64 path (dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch of the fourteenth time step, cold cache); None where no
 # capture was taken
-TRAFFIC = {"assemble": 21062144 + 768, "sweep_loop": 18985472 + 22528, "flux_diff": 9750528}
+TRAFFIC = {"assemble": 21066240 + 768, "sweep_loop": 18984704 + 27392, "flux_diff": 9751808}
 
 # FP64 instructions per cell of the FP64 path's kernels (per cell and sweep for the sweep loop),
 # counted by ncu on this workload (smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on
@@ -54,7 +54,7 @@ TRAFFIC = {"assemble": 21062144 + 768, "sweep_loop": 18985472 + 22528, "flux_dif
 # FP64 rates (sts_fp64_rates) against the measured launch time.
 FP64_OPS = {"assemble": {"add": 97.59, "mul": 108.00, "fma": 29.74},
             "sweep_loop": {"add": 22.75, "mul": 16.55, "fma": 19.22},
-            "flux_diff": {"add": 22.05, "mul": 59.96, "fma": 56.28}}
+            "flux_diff": {"add": 20.12, "mul": 50.32, "fma": 56.28}}
 
 
 def parse():
