@@ -157,6 +157,11 @@ struct Geo {
   const int *slip_u, *slip_v, *tjump;
   const uint8_t *slip_u_fin, *slip_v_fin, *tjump_fin, *tjump_wr_fin;
   int n_slip_u, n_slip_v, n_tjump;
+  // the cells the p-T sweeps solve (p/T class set) and the other cells, row-major, each packed
+  // as i | j << 16: a single case's FP64 sweep loops split the solved cells evenly over their
+  // CTAs, and copy the others through in the first sweep of a loop only
+  const unsigned *pt_cells, *pt_copy;
+  int n_pt_cells, n_pt_copy;
   // fields
   double *u, *v, *u_pr, *v_pr, *p[2], *T[2], *p_pr, *T_pr, *rho, *rho_pr, *sqrt_T, *rho_u, *rho_v;
   double *Fx, *Fy, *D_ux, *D_uy, *D_vx, *D_vy, *DTx, *DTy, *Gamma_xf, *Gamma_yf;

@@ -358,9 +358,50 @@ __device__ __forceinline__ void pt_loop_rounds(const Geo& g0, const Geo* __restr
     sc[c] = s;
   }
   __syncthreads();
+  // Ops::kCellList, one case: each CTA takes an equal slice of the solved cells instead of
+  // 32x8 tiles (tiles leave most SMs with four full tiles while the mean is lower: walls, bodies
+  // and the last tile row); the unsolved cells are copied through in the first sweep only, after
+  // which both iterate buffers hold the same values there.
+  const bool by_list = Ops::kCellList && SINGLE && g0.pt_cells != nullptr;
   for (unsigned round = 0;; round++) {
     const unsigned slot = round % 3;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    if (by_list) {
+      const LoopCase s = sc[0];
+      if (s.phase != PS_DONE) {
+        unsigned* st = &g0.ctl->status;
+        unsigned long long bp = 0, bT = 0;
+        const int per = (g0.n_pt_cells + (int)gridDim.x - 1) / (int)gridDim.x;
+        const int k0 = (int)blockIdx.x * per, k1 = min(g0.n_pt_cells, k0 + per);
+        for (int k = k0 + tid; k < k1; k += nthr) {
+          const unsigned e = g0.pt_cells[k];
+          Cell cl;
+          cl.i = (int)(e & 0xffffu);
+          cl.j = (int)(e >> 16);
+          cl.ok = true;
+          cl.ij = cl.i + cl.j * g0.Nx;
+          double a = 0, b = 0;
+          Ops::pass(g0, cl, s, a, b);
+          bp = umax64(bp, res_bits(a, st));
+          bT = umax64(bT, res_bits(b, st));
+        }
+        if (s.phase == PS_FIRST) {
+          const int perc = (g0.n_pt_copy + (int)gridDim.x - 1) / (int)gridDim.x;
+          const int c0 = (int)blockIdx.x * perc, c1 = min(g0.n_pt_copy, c0 + perc);
+          for (int k = c0 + tid; k < c1; k += nthr) {
+            const unsigned e = g0.pt_copy[k];
+            Cell cl;
+            cl.i = (int)(e & 0xffffu);
+            cl.j = (int)(e >> 16);
+            cl.ok = true;
+            cl.ij = cl.i + cl.j * g0.Nx;
+            double a = 0, b = 0;
+            Ops::pass(g0, cl, s, a, b);  // an unsolved cell: copied through, no residual
+          }
+        }
+        block_max2_bits(bp, bT, &g0.ctl->rb_p[slot], &g0.ctl->rb_T[slot]);
+      }
+    }
+    for (int t = by_list ? ntiles : (int)blockIdx.x; t < ntiles; t += gridDim.x) {
       const int c = SINGLE ? 0 : tile_case[t];
       const LoopCase s = sc[c];
       if (s.phase == PS_DONE) continue;  // uniform over the CTA

@@ -632,6 +632,7 @@ __global__ void k_sweep(Geo g, unsigned long long h_sweep, int in_graph) { sweep
 // launch: the same cell arithmetic as k_sweep_first / k_sweep (so the same bits), one sweep per
 // round of pt_loop_rounds.
 struct ExactOps {
+  static constexpr bool kCellList = true;  // a single case's sweeps split the solved cells evenly
   static __device__ __forceinline__ void pass(const Geo& g, const Cell& c, const LoopCase& s, double& rp, double& rT) {
     const double* P = g.p[s.cur];
     const double* TT = g.T[s.cur];

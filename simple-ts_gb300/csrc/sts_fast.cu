@@ -317,6 +317,7 @@ __device__ __forceinline__ bool sweep_cell_fast(const Geo& g, const Cell& c, con
 
 // The sweep loop of mode 1 (see k_pt_loop).
 struct FastOps {
+  static constexpr bool kCellList = true;
   static __device__ __forceinline__ void pass(const Geo& g, const Cell& c, const LoopCase& s, double& rp, double& rT) {
     const double* P = g.p[s.cur];
     const double* TT = g.T[s.cur];
@@ -401,6 +402,7 @@ __device__ __forceinline__ void sweep32_cell(const Geo& g, const Cell& c, unsign
 // R: the arithmetic of the FP64 sweeps (FP64, or double-float in precision mode 3).
 template <class R>
 struct MixedOpsT {
+  static constexpr bool kCellList = false;  // its materialise pass covers every cell
   static __device__ __forceinline__ void pass(const Geo& g, const Cell& c, const LoopCase& s, double& rp, double& rT) {
     const int ij = c.ij;
     const unsigned base = s.base;

@@ -891,6 +891,21 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
   g.n_slip_u = (int)h.slip_u.size();
   g.n_slip_v = (int)h.slip_v.size();
   g.n_tjump = (int)h.tjump.size();
+  {
+    std::vector<unsigned> solved, other;
+    for (int j = 0; j < h.Ny; j++)
+      for (int i = 0; i < h.Nx; i++)
+        ((h.cls[i + j * h.Nx] & 0x30u) ? solved : other).push_back((unsigned)i | ((unsigned)j << 16));
+    unsigned *dsol = nullptr, *doth = nullptr;
+    if (int r = c->alloc(&dsol, solved.size())) return r;
+    if (int r = c->alloc(&doth, other.size())) return r;
+    if (int r = c->upload(dsol, solved)) return r;
+    if (int r = c->upload(doth, other)) return r;
+    g.pt_cells = dsol;
+    g.pt_copy = doth;
+    g.n_pt_cells = (int)solved.size();
+    g.n_pt_copy = (int)other.size();
+  }
 
   // fields
   double** fields[] = {&g.u, &g.v, &g.u_pr, &g.v_pr, &g.p[0], &g.p[1], &g.T[0], &g.T[1], &g.p_pr, &g.T_pr, &g.rho,
