@@ -163,6 +163,17 @@ __device__ __forceinline__ void block_max2(double a, double b, unsigned long lon
   block_max2_bits(res_bits(a, status), res_bits(b, status), ga, gb);
 }
 
+// Bit pattern of an FP32 residual for the maximum, with block_max2_f's rule: NaN and +inf set the
+// status bit, NaN counts as 0.
+__device__ __forceinline__ unsigned res_bits_f(float x, unsigned int* status) {
+  unsigned m = __float_as_uint(x) & 0x7fffffffu;
+  if (m >= 0x7f800000u) {
+    atomicOr(status, 1u);
+    if (m > 0x7f800000u) m = 0u;
+  }
+  return m;
+}
+
 // The same for FP32 residuals: reduced as 32-bit patterns, folded in as doubles (exact widening).
 __device__ void block_max2_f(float a, float b, unsigned long long* ga, unsigned long long* gb, unsigned int* status) {
   __shared__ unsigned sa[32], sb[32];
@@ -360,27 +371,39 @@ __device__ __forceinline__ void pt_loop_rounds(const Geo& g0, const Geo* __restr
   __syncthreads();
   // Ops::kCellList, one case: each CTA takes an equal slice of the solved cells instead of
   // 32x8 tiles (tiles leave most SMs with four full tiles while the mean is lower: walls, bodies
-  // and the last tile row); the unsolved cells are copied through in the first sweep only, after
-  // which both iterate buffers hold the same values there.
+  // and the last tile row); the unsolved cells are passed in the first pass only (copied, and
+  // their correction terms zeroed), after which both iterate buffers hold the same values there
+  // and every later pass would only copy them onto themselves.
   const bool by_list = Ops::kCellList && SINGLE && g0.pt_cells != nullptr;
   for (unsigned round = 0;; round++) {
     const unsigned slot = round % 3;
     if (by_list) {
       const LoopCase s = sc[0];
-      if (s.phase != PS_DONE) {
-        unsigned* st = &g0.ctl->status;
-        unsigned long long bp = 0, bT = 0;
-        const int per = (g0.n_pt_cells + (int)gridDim.x - 1) / (int)gridDim.x;
-        const int k0 = (int)blockIdx.x * per, k1 = min(g0.n_pt_cells, k0 + per);
+      const int per = (g0.n_pt_cells + (int)gridDim.x - 1) / (int)gridDim.x;
+      const int k0 = (int)blockIdx.x * per, k1 = min(g0.n_pt_cells, k0 + per);
+      auto list_cell = [&](unsigned e) {
+        Cell cl;
+        cl.i = (int)(e & 0xffffu);
+        cl.j = (int)(e >> 16);
+        cl.ok = true;
+        cl.ij = cl.i + cl.j * g0.Nx;
+        return cl;
+      };
+      unsigned* st = &g0.ctl->status;
+      if (s.phase == PS_SWEEP32) {  // FP32 residuals: the thread's maximum, then the block's
+        unsigned fp = 0, fT = 0;
         for (int k = k0 + tid; k < k1; k += nthr) {
-          const unsigned e = g0.pt_cells[k];
-          Cell cl;
-          cl.i = (int)(e & 0xffffu);
-          cl.j = (int)(e >> 16);
-          cl.ok = true;
-          cl.ij = cl.i + cl.j * g0.Nx;
+          float a = 0.f, b = 0.f;
+          Ops::pass32(g0, list_cell(g0.pt_cells[k]), s, a, b);
+          fp = max(fp, res_bits_f(a, st));
+          fT = max(fT, res_bits_f(b, st));
+        }
+        block_max2_f(__uint_as_float(fp), __uint_as_float(fT), &g0.ctl->rb_p[slot], &g0.ctl->rb_T[slot], st);
+      } else if (s.phase != PS_DONE) {
+        unsigned long long bp = 0, bT = 0;
+        for (int k = k0 + tid; k < k1; k += nthr) {
           double a = 0, b = 0;
-          Ops::pass(g0, cl, s, a, b);
+          Ops::pass(g0, list_cell(g0.pt_cells[k]), s, a, b);
           bp = umax64(bp, res_bits(a, st));
           bT = umax64(bT, res_bits(b, st));
         }
@@ -388,17 +411,11 @@ __device__ __forceinline__ void pt_loop_rounds(const Geo& g0, const Geo* __restr
           const int perc = (g0.n_pt_copy + (int)gridDim.x - 1) / (int)gridDim.x;
           const int c0 = (int)blockIdx.x * perc, c1 = min(g0.n_pt_copy, c0 + perc);
           for (int k = c0 + tid; k < c1; k += nthr) {
-            const unsigned e = g0.pt_copy[k];
-            Cell cl;
-            cl.i = (int)(e & 0xffffu);
-            cl.j = (int)(e >> 16);
-            cl.ok = true;
-            cl.ij = cl.i + cl.j * g0.Nx;
             double a = 0, b = 0;
-            Ops::pass(g0, cl, s, a, b);  // an unsolved cell: copied through, no residual
+            Ops::pass(g0, list_cell(g0.pt_copy[k]), s, a, b);  // an unsolved cell: copied, no residual
           }
         }
-        block_max2_bits(bp, bT, &g0.ctl->rb_p[slot], &g0.ctl->rb_T[slot]);
+        if (s.phase != PS_MATERIALIZE) block_max2_bits(bp, bT, &g0.ctl->rb_p[slot], &g0.ctl->rb_T[slot]);
       }
     }
     for (int t = by_list ? ntiles : (int)blockIdx.x; t < ntiles; t += gridDim.x) {

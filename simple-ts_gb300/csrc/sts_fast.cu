@@ -402,7 +402,7 @@ __device__ __forceinline__ void sweep32_cell(const Geo& g, const Cell& c, unsign
 // R: the arithmetic of the FP64 sweeps (FP64, or double-float in precision mode 3).
 template <class R>
 struct MixedOpsT {
-  static constexpr bool kCellList = false;  // its materialise pass covers every cell
+  static constexpr bool kCellList = false;  // measured slower with the cell list
   static __device__ __forceinline__ void pass(const Geo& g, const Cell& c, const LoopCase& s, double& rp, double& rT) {
     const int ij = c.ij;
     const unsigned base = s.base;
