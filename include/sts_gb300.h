@@ -76,7 +76,7 @@ typedef struct sts_options {
   int async_save;
   /* 1: the first steps of the run choose the launch shapes -- the sweep loop's CTAs per SM and the
    *    assembly kernel's block shape -- by timing each candidate on real steps launched kernel by
-   *    kernel (1 + 2 x max(CTAs per SM that fit, 3) steps); results do not depend on launch shapes,
+   *    kernel (1 + 3 x max(CTAs per SM that fit, 3) steps); results do not depend on launch shapes,
    *    so the run is the same bit for bit; the graph is built with the chosen shapes (default);
    * 0: the largest number of CTAs that fit and 32x8 blocks. */
   int autotune;

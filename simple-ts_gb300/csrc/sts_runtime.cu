@@ -168,11 +168,12 @@ struct sts_ctx {
   // by the autotuner from the run's first steps
   dim3 asm_block{32, 8, 1};
   int sms = 0, pt_per_sm_max = 0, pt_per_sm = 0;  // pt_per_sm 0: as many as fit
+  // per candidate: the fastest sample (per assembly launch, per sweep or sweep round), the most
+  // robust of the samples against a step disturbed by something else
   struct TuneStat {
-    double ms = 0, sweeps = 0;
-    int n = 0;
+    double best = 1e30;
   };
-  static constexpr int kTuneRounds = 2;
+  static constexpr int kTuneRounds = 3;
   int tune_left = 0, tune_idx = 0;
   std::vector<TuneStat> tune_pt, tune_asm;
   static dim3 asm_shape(int k) {
@@ -429,11 +430,8 @@ int sts_ctx::tune_step(int* done) {
   }
   for (cudaEvent_t e : ev) cudaEventDestroy(e);
   if (record) {
-    tune_asm[ac].ms += t_asm;
-    tune_asm[ac].n += outer;
-    tune_pt[pc].ms += t_pt;
-    tune_pt[pc].sweeps += h_ctl->step_sweeps;
-    tune_pt[pc].n += 1;
+    if (outer > 0) tune_asm[ac].best = std::min(tune_asm[ac].best, t_asm / outer);
+    if (h_ctl->step_sweeps > 0) tune_pt[pc].best = std::min(tune_pt[pc].best, t_pt / h_ctl->step_sweeps);
   }
   tune_idx++;
   if (--tune_left == 0) tune_choose();
@@ -446,10 +444,9 @@ int sts_ctx::tune_step(int* done) {
 void sts_ctx::tune_choose() {
   int best_a = 0, best_p = (int)tune_pt.size() - 1;
   for (int k = 0; k < (int)tune_asm.size(); k++)
-    if (tune_asm[k].n && tune_asm[k].ms / tune_asm[k].n < tune_asm[best_a].ms / std::max(tune_asm[best_a].n, 1)) best_a = k;
-  auto per_sweep = [&](int k) { return tune_pt[k].sweeps > 0 ? tune_pt[k].ms / tune_pt[k].sweeps : 1e30; };
+    if (tune_asm[k].best < tune_asm[best_a].best) best_a = k;
   for (int k = 0; k < (int)tune_pt.size(); k++)
-    if (per_sweep(k) < per_sweep(best_p)) best_p = k;
+    if (tune_pt[k].best < tune_pt[best_p].best) best_p = k;
   asm_block = asm_shape(best_a);
   pt_per_sm = best_p + 1;
   size_pt_grid();
@@ -1744,20 +1741,16 @@ int sts_batch::tune_step() {
     rounds = std::max(rounds, c->h_ctl->step_sweeps);
   }
   if (record) {
-    tune_asm[ac].ms += ta;
-    tune_asm[ac].n += 1;
-    tune_pt[pc].ms += tp;
-    tune_pt[pc].sweeps += rounds;
-    tune_pt[pc].n += 1;
+    tune_asm[ac].best = std::min(tune_asm[ac].best, (double)ta);
+    if (rounds > 0) tune_pt[pc].best = std::min(tune_pt[pc].best, (double)tp / rounds);
   }
   tune_idx++;
   if (--tune_left == 0) {
     int best_a = 0, best_p = npt - 1;
     for (int k = 0; k < nasm; k++)
-      if (tune_asm[k].n && tune_asm[k].ms / tune_asm[k].n < tune_asm[best_a].ms / std::max(tune_asm[best_a].n, 1)) best_a = k;
-    auto per_round = [&](int k) { return tune_pt[k].sweeps > 0 ? tune_pt[k].ms / tune_pt[k].sweeps : 1e30; };
+      if (tune_asm[k].best < tune_asm[best_a].best) best_a = k;
     for (int k = 0; k < npt; k++)
-      if (per_round(k) < per_round(best_p)) best_p = k;
+      if (tune_pt[k].best < tune_pt[best_p].best) best_p = k;
     asm_block = sts_ctx::asm_shape(best_a);
     per_sm = best_p + 1;
     size_pt();
