@@ -42,7 +42,7 @@ BYTES_PER_CELL = {
     "step_begin": 10 * 8,
 }
 
-# DRAM bytes per launch measured by ncu on this workload, FP64 path (dram__bytes_read.sum +
+# DRAM bytes per launch measured by ncu on the default workload (the 1200x120 channel), FP64 path (dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch of the fourteenth time step, cold cache); None where no
 # capture was taken
 TRAFFIC = {"assemble": 21061120, "sweep_loop": 19600128 + 20480, "flux_diff": 9751296}
@@ -510,7 +510,7 @@ def main():
         bpc *= float(sum(int(x) for x in psweeps)) / max(kcnt[dom], 1)
     achieved = bpc * Na / avg_s / 1e9 if bpc else None
     roof = {"bound": "hbm", "kernel": "k_" + dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": (achieved / peak) if achieved else None, "traffic": TRAFFIC.get(dom),
+            "frac": (achieved / peak) if achieved else None, "traffic": TRAFFIC.get(dom) if args.workload == WORKLOAD else None,
             "peak_source": peak_kind, "bytes_per_cell": bpc, "avg_launch_us": avg_s * 1e6,
             "kernel_share": {k: round(v / max(sum(kms.values()), 1e-30), 4) for k, v in kms.items()},
             "fp64_pipe": fp64_roof(dom, kms, kcnt, psweeps, Na, local)}
