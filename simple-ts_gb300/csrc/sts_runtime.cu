@@ -1246,7 +1246,8 @@ static bool mapped_host(const void* const* ptrs, void** dev, int n) {
   return true;
 }
 
-static int move_grid(int n) { return std::max(1, std::min((n + 255) / 256, 4 * 152)); }
+// 256-thread CTAs, at most four per multiprocessor (a grid-stride pass covers the rest)
+static int move_grid(int n, int sms) { return std::max(1, std::min((n + 255) / 256, 4 * std::max(sms, 1))); }
 
 int sts_set_state(sts_ctx* ctx, const double* u_in, const double* v_in, const double* p_in, const double* T_in) {
   if (!ctx || !u_in || !v_in || !p_in || !T_in) return fail(STS_ERR_ARG, "null argument");
@@ -1259,7 +1260,7 @@ int sts_set_state(sts_ctx* ctx, const double* u_in, const double* v_in, const do
   const void* hp[4] = {u_in, v_in, p_in, T_in};
   void* dp[4];
   if (mapped_host(hp, dp, 4)) {
-    k_move4<<<move_grid(g.Na), 256, 0, ctx->s>>>((const double*)dp[0], (const double*)dp[1], (const double*)dp[2],
+    k_move4<<<move_grid(g.Na, ctx->sms), 256, 0, ctx->s>>>((const double*)dp[0], (const double*)dp[1], (const double*)dp[2],
                                                  (const double*)dp[3], g.u, g.v, g.p[cur], g.T[cur], g.Na);
     CU(cudaGetLastError());
   } else {
@@ -1287,7 +1288,7 @@ int sts_get_state(sts_ctx* ctx, double* u_out, double* v_out, double* p_out, dou
   const void* hp[4] = {u_out, v_out, p_out, T_out};
   void* dp[4];
   if (mapped_host(hp, dp, 4)) {
-    k_move4<<<move_grid(g.Na), 256, 0, ctx->s>>>(g.u, g.v, g.p[cur], g.T[cur], (double*)dp[0], (double*)dp[1],
+    k_move4<<<move_grid(g.Na, ctx->sms), 256, 0, ctx->s>>>(g.u, g.v, g.p[cur], g.T[cur], (double*)dp[0], (double*)dp[1],
                                                  (double*)dp[2], (double*)dp[3], g.Na);
     CU(cudaGetLastError());
   } else {
