@@ -367,11 +367,14 @@ constexpr float kFloor32 = 8.0f / 16777216.0f;  // 8 units in the last place of 
 template <class R>
 __device__ __forceinline__ void set_base(const Geo& g, const Cell& c, R T0, R p0, R T1, R p1, R sa) {
   const int ij = c.ij;
-  const R hT = num<R>(g.hx[c.i]) * num<R>(g.hy[c.j]) / T1;
-  g.T1[ij] = to_float(T1);
-  g.hT[ij] = to_float(hT);
+  // the FP32 sweeps' coefficients are formed in FP32 (they only steer the corrections; the
+  // FP64 passes decide the converged iterate), which keeps an FP64 division off this pass
+  const float T1f = to_float(T1);
+  const float hT = ((float)g.hx[c.i] * (float)g.hy[c.j]) / T1f;
+  g.T1[ij] = T1f;
+  g.hT[ij] = hT;
   g.q1[ij] = to_float(p1);
-  g.den1[ij] = to_float(sa + hT);
+  g.den1[ij] = to_float(sa) + hT;
   const float dT = to_float(T1 - T0), dp = to_float(p1 - p0);
   g.dT[ij] = dT;
   g.dp[ij] = dp;
@@ -420,16 +423,16 @@ struct MixedOpsT {
         rp = to_double(dabs(pnew - P0));
         rT = to_double(dabs(Tnew - T0));
         const Nb d = neighbours(c.i, c.j, g.Nx, g.Ny, g.bits & F_PERIODIC);
-        const R ht = num<R>(g.ht), r = ht * num<R>(g.inv[5][ij]);
+        // the FP32 sweeps' coefficients, products formed in FP32
+        const float ht = (float)g.ht, r = ht * (float)g.inv[5][ij];
         const int nb[4] = {d.i_1j, d.i1j, d.ij_1, d.ij1};
         for (int k = 0; k < 4; k++)  // a wall neighbour's term is a constant and sits in the defect
-          g.c32[k][ij] =
-              (cls_o(g.cls[ij]) == CLS_NCH || cls_fluid(g.cls[nb[k]])) ? to_float(r * num<R>(g.inv[k][ij])) : 0.0f;
-        g.c32[4][ij] = to_float(r * num<R>(1.0 - g.gamma1) * num<R>(g.inv[4][ij]));
-        g.a32[0][ij] = to_float(ht * num<R>(g.apx[ij]));
-        g.a32[1][ij] = to_float(ht * num<R>(g.apx[d.i1j]));
-        g.a32[2][ij] = to_float(ht * num<R>(g.apy[ij]));
-        g.a32[3][ij] = to_float(ht * num<R>(g.apy[d.ij1]));
+          g.c32[k][ij] = (cls_o(g.cls[ij]) == CLS_NCH || cls_fluid(g.cls[nb[k]])) ? r * (float)g.inv[k][ij] : 0.0f;
+        g.c32[4][ij] = r * (float)(1.0 - g.gamma1) * (float)g.inv[4][ij];
+        g.a32[0][ij] = ht * (float)g.apx[ij];
+        g.a32[1][ij] = ht * (float)g.apx[d.i1j];
+        g.a32[2][ij] = ht * (float)g.apy[ij];
+        g.a32[3][ij] = ht * (float)g.apy[d.ij1];
         set_base<R>(g, c, T0, P0, Tnew, pnew, sa);
         return;
       }
