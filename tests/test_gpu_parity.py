@@ -68,6 +68,62 @@ def test_every_array_matches_oracle_step_by_step(name, lib_built, oracle_built):
         g.close()
 
 
+def ratio_corrected_example(steps, **entered):
+    """The shipped example with Pressure_ratio_correct = 1, the inflow pressure corrected
+    towards the given mean inflow velocity (p_BC_xb_correction_method = 2) and temperature-jump
+    walls.  With the pressure boundary, the ratio correction and the local Kn all on, the
+    temperature-jump walls read the pressure that the boundary kernel has just corrected, so the
+    jump kernel runs after the boundary kernel instead of beside the wall kernels (the one graph
+    order no other case takes)."""
+    case = sc.shipped_example(steps)
+    case.entered.update(Pressure_ratio_correct=1, p_BC_xb_correction_method=2)
+    case.entered.update(entered)
+    for body in case.polygons:
+        body.jump = 1
+    return case
+
+
+@pytest.mark.parametrize("use_graph", [True, False], ids=["graph", "launches"])
+def test_ratio_corrected_jump_walls_match_oracle(use_graph, lib_built, oracle_built):
+    import ora
+    import sts
+    with tempfile.TemporaryDirectory() as d:
+        ratio_corrected_example(8).write(d)
+        o = ora.Oracle(d, fixed_sweeps=False)
+        g = sts.Solver(d, fixed_sweeps=False, use_graph=use_graph)
+        for k in range(4):
+            assert g.step(2) == o.step(2) == 2
+            for f in ALL_FIELDS:
+                np.testing.assert_array_equal(g.field(f), o.field(f), err_msg=f"step {2 * k + 2} {f}")
+            np.testing.assert_array_equal(g.stats(), o.stats())
+        np.testing.assert_array_equal(g.sweep_history(), o.sweeps())
+        g.close()
+
+
+def test_ratio_corrected_jump_walls_in_a_batch(lib_built, oracle_built):
+    """The batched graph takes the same order when one of its cases needs it."""
+    import ora
+    import sts
+    cases = [ratio_corrected_example(6), ratio_corrected_example(6, Kn=0.02, p_correction_auto=1),
+             ratio_corrected_example(6, correct_p_BC_xb=0, p_BC_xb_correction_method=1),
+             sc.channel_case("c", 60, 8, 0.3, 0.002, 1e-3, 6)]
+    with tempfile.TemporaryDirectory() as root:
+        dirs = []
+        for k, c in enumerate(cases):
+            dirs.append(os.path.join(root, f"c{k}"))
+            os.makedirs(dirs[-1])
+            c.write(dirs[-1])
+        b = sts.Batch(dirs, fixed_sweeps=False)
+        assert b.step(6) == 6
+        for k, d in enumerate(dirs):
+            o = ora.Oracle(d, fixed_sweeps=False)
+            assert o.step(6) == 6
+            for f in ("u", "v", "p", "T", "rho"):
+                np.testing.assert_array_equal(b.cases[k].field(f), o.field(f), err_msg=f"case {k} {f}")
+            np.testing.assert_array_equal(b.cases[k].sweep_history(), o.sweeps())
+        b.close()
+
+
 def test_graph_and_launch_modes_agree(lib_built):
     import sts
     case = sc.channel_case("c", 100, 10, 0.3, 0.002, 1e-3, 40)
