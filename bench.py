@@ -45,14 +45,14 @@ BYTES_PER_CELL = {
 # DRAM bytes per launch measured by ncu on the default workload (the 1200x120 channel), FP64 path (dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch of the fourteenth time step, cold cache); None where no
 # capture was taken
-TRAFFIC = {"assemble": 21061120, "sweep_loop": 19600128 + 20480, "flux_diff": 9751296}
+TRAFFIC = {"assemble": 21101056, "sweep_loop": 19600128 + 20480, "flux_diff": 9751296}
 
 # FP64 instructions per cell of the FP64 path's kernels (per cell and sweep for the sweep loop),
 # counted by ncu on this workload (smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on
 # of one launch divided by its 1203 x 123 cells and, for the sweep loop, by its 8 sweeps).  The
 # kernels are bound by the FP64 unit, so their roofline is this work at the device's measured
 # FP64 rates (sts_fp64_rates) against the measured launch time.
-FP64_OPS = {"assemble": {"add": 97.59, "mul": 108.00, "fma": 29.74},
+FP64_OPS = {"assemble": {"add": 94.24, "mul": 104.97, "fma": 29.69},
             "sweep_loop": {"add": 20.64, "mul": 16.55, "fma": 19.22},
             "flux_diff": {"add": 20.12, "mul": 50.32, "fma": 56.28}}
 

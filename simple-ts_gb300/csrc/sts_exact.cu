@@ -286,19 +286,30 @@ __global__ void kb_warm_apply(const Geo* gs) {
 // vertex at the cell's lower-left corner, and s1, s2, s3 of a cell are s0 of its east, north and
 // north-east neighbours whenever those neighbours are the plain i+1 / j+1 cells (same operands,
 // same operations, so the same bits).
-__device__ __forceinline__ double corner_s0(const Geo& g, int i, int j) {
-  const Nb d = neighbours(i, j, g.Nx, g.Ny, g.bits & F_PERIODIC);
-  const int jm = j - (0 < j ? 1 : 0);
+__device__ __forceinline__ double corner_s0(const Geo& g, const Nb& d) {
+  const int i = d.i, j = d.j, jm = j - (0 < j ? 1 : 0);
   return div_cr(g.u[d.ij] - g.u[d.ij_1], g.hy[jm] + g.hy[j], g.ryy_m[j]) +
          div_cr(g.v[d.ij] - g.v[d.i_1j], g.hx[d.i_1] + g.hx[i], g.rxx_m[i]);
+}
+
+// Two more shared terms of the interior forms.  The u part of cell (i, j) takes
+// sT·(v_N - v)·2/3 at (i, j) and at (i-1, j): staged at (i, j) is the west one, and the east
+// neighbour's staged term is the cell's own whenever that neighbour is the plain i+1 cell.  The
+// v part takes sT·(u_E - u)·2/3 at (i, j) and at (i, j-1): staged at (i, j) is the south one,
+// and the north neighbour's staged term is the cell's own whenever that neighbour exists.
+__device__ __forceinline__ double west_term_v(const Geo& g, const Nb& d) {
+  return div_cr(g.sqrt_T[d.i_1j] * (g.v[d.i_1j1] - g.v[d.i_1j]) * 2.0, 3.0, g.r3);
+}
+__device__ __forceinline__ double south_term_u(const Geo& g, const Nb& d) {
+  return div_cr(g.sqrt_T[d.ij_1] * (g.u[d.i1j_1] - g.u[d.ij_1]) * 2.0, 3.0, g.r3);
 }
 
 constexpr int kAsmCorners = 400;  // corners of the largest block shape the tuner uses (128x2 + 1)
 
 __device__ __forceinline__ void assemble_body(const Geo& g, unsigned long long h_sweep, int in_graph) {
-  // corner terms of the block's cells and of one more column and row, computed once each by
+  // shared terms of the block's cells and of one more column and row, computed once each by
   // the block's threads in turn
-  __shared__ double corner[kAsmCorners];
+  __shared__ double corner[kAsmCorners], west_v[kAsmCorners], south_u[kAsmCorners];
   const int W1 = blockDim.x + 1, ncorner = W1 * (blockDim.y + 1);
   const bool shared_corners = ncorner <= kAsmCorners;
   if (shared_corners) {
@@ -306,7 +317,16 @@ __device__ __forceinline__ void assemble_body(const Geo& g, unsigned long long h
     const int i0 = blockIdx.x * blockDim.x, j0 = blockIdx.y * blockDim.y;
     for (int q = tid; q < ncorner; q += nthr) {
       const int py = q / W1, px = q - py * W1, ci = i0 + px, cj = j0 + py;
-      corner[q] = (ci < g.Nx && cj < g.Ny) ? corner_s0(g, ci, cj) : 0.0;
+      double s = 0.0, w = 0.0, z = 0.0;
+      if (ci < g.Nx && cj < g.Ny) {
+        const Nb e = neighbours(ci, cj, g.Nx, g.Ny, g.bits & F_PERIODIC);
+        s = corner_s0(g, e);
+        w = west_term_v(g, e);
+        z = south_term_u(g, e);
+      }
+      corner[q] = s;
+      west_v[q] = w;
+      south_u[q] = z;
     }
     __syncthreads();
   }
@@ -326,6 +346,9 @@ __device__ __forceinline__ void assemble_body(const Geo& g, unsigned long long h
   if (!(cl & 0x3F)) return;
   const int i = c.i, j = c.j, Nx = g.Nx;
   const Nb d = neighbours(i, j, g.Nx, g.Ny, g.bits & F_PERIODIC);
+  // east: d.i1 is i + 1 (no clamp or wrap); north: the cell above exists
+  const int q = threadIdx.x + threadIdx.y * W1;
+  const bool east = shared_corners && d.i1 == i + 1, north = shared_corners && j + 1 < g.Ny;
   const double cT = ctl->cT, cPch = ctl->cPch, ht = g.ht;
   const double* __restrict__ hx = g.hx;
   const double* __restrict__ hy = g.hy;
@@ -352,11 +375,11 @@ __device__ __forceinline__ void assemble_body(const Geo& g, unsigned long long h
                   div_cr(sT[d.ij] * (v[d.ij1] * B(d.ij1) - v[d.ij] * B(d.ij_1)) * 2.0, 3.0, g.r3) +
                   div_cr(sT[d.i_1j] * (v[d.i_1j1] * B(d.i_1j1) - v[d.i_1j] * B(d.i_1j_1)) * 2.0, 3.0, g.r3));
     } else {
+      const double wE = east ? west_v[q + 1] : div_cr(sT[d.ij] * (v[d.ij1] - v[d.ij]) * 2.0, 3.0, g.r3);
+      const double wW = shared_corners ? west_v[q] : west_term_v(g, d);
       Scu = cT * (div_cr(u[d.i1j] * sT[d.ij] * hy[j], hx[i] * 3.0, g.r3x[i]) +
                   div_cr(u[d.i_1j] * sT[d.i_1j] * hy[j], hx[d.i_1] * 3.0, g.r3x[d.i_1]) +
-                  g.Gamma_yf[d.ij1] * (v[d.ij1] - v[d.i_1j1]) - g.Gamma_yf[d.ij] * (v[d.ij] - v[d.i_1j]) -
-                  div_cr(sT[d.ij] * (v[d.ij1] - v[d.ij]) * 2.0, 3.0, g.r3) +
-                  div_cr(sT[d.i_1j] * (v[d.i_1j1] - v[d.i_1j]) * 2.0, 3.0, g.r3));
+                  g.Gamma_yf[d.ij1] * (v[d.ij1] - v[d.i_1j1]) - g.Gamma_yf[d.ij] * (v[d.ij] - v[d.i_1j]) - wE + wW);
     }
     const double Spu = div_cr(-(g.D_ux[d.ij] + g.D_ux[d.i1j]), 3.0, g.r3);
     const double au1 = dmax0(0, F_xu1) + g.D_ux[d.ij];
@@ -395,11 +418,11 @@ __device__ __forceinline__ void assemble_body(const Geo& g, unsigned long long h
                   div_cr(sT[d.ij_1] * (u[d.i1j_1] * B(d.i1j_1) - u[d.ij_1] * B(d.i_1j_1)) * 2.0, 3.0, g.r3)) -
             g.c_Fr_v * (rho[d.ij_1] * hx[i] * 0.5 * hy[jm] + rho[d.ij] * hx[i] * 0.5 * hy[j]);
     } else {
+      const double zN = north ? south_u[q + W1] : div_cr(sT[d.ij] * (u[d.i1j] - u[d.ij]) * 2.0, 3.0, g.r3);
+      const double zS = shared_corners ? south_u[q] : south_term_u(g, d);
       Scv = cT * (div_cr(v[d.ij1] * sT[d.ij] * hx[i], hy[j] * 3.0, g.r3y[j]) +
                   div_cr(v[d.ij_1] * sT[d.ij_1] * hx[i], hy[j - 1] * 3.0, g.r3y[j - 1]) +
-                  g.Gamma_xf[d.i1j] * (u[d.i1j] - u[d.i1j_1]) - g.Gamma_xf[d.ij] * (u[d.ij] - u[d.ij_1]) -
-                  div_cr(sT[d.ij] * (u[d.i1j] - u[d.ij]) * 2.0, 3.0, g.r3) +
-                  div_cr(sT[d.ij_1] * (u[d.i1j_1] - u[d.ij_1]) * 2.0, 3.0, g.r3)) -
+                  g.Gamma_xf[d.i1j] * (u[d.i1j] - u[d.i1j_1]) - g.Gamma_xf[d.ij] * (u[d.ij] - u[d.ij_1]) - zN + zS) -
             g.c_Fr_v * (rho[d.ij_1] * hx[i] * 0.5 * hy[j - 1] + rho[d.ij] * hx[i] * 0.5 * hy[j]);
     }
     const double Spv = div_cr(-(g.D_vy[d.ij] + g.D_vy[d.ij1]), 3.0, g.r3);
@@ -444,17 +467,16 @@ __device__ __forceinline__ void assemble_body(const Geo& g, unsigned long long h
       const double rym = g.ryy_m[j], ryp = g.ryy_p[j], rxm = g.rxx_m[i], rxp = g.rxx_p[i];
       dudx = div_cr(u[d.i1j] - u[d.ij], hx[i], g.rhx[i]);
       dvdy = div_cr(v[d.ij1] - v[d.ij], hy[j], g.rhy[j]);
-      // east: d.i1 is i + 1 (no clamp or wrap); north: d.ij1 is one row up and jp = j + 1
-      const bool east = shared_corners && d.i1 == i + 1, north = shared_corners && j + 1 < g.Ny && j < Nx - 1;
-      const int q = threadIdx.x + threadIdx.y * W1;
+      // north corners also need jp = j + 1
+      const bool north_c = north && j < Nx - 1;
       s0 = shared_corners ? corner[q]
                           : div_cr(u[d.ij] - u[d.ij_1], hy[jm] + hy[j], rym) +
                                 div_cr(v[d.ij] - v[d.i_1j], hx[d.i_1] + hx[i], rxm);
       s1 = east ? corner[q + 1]
                 : div_cr(u[d.i1j] - u[d.i1j_1], hy[jm] + hy[j], rym) + div_cr(v[d.i1j] - v[d.ij], hx[i] + hx[d.i1], rxp);
-      s2 = north ? corner[q + W1]
+      s2 = north_c ? corner[q + W1]
                  : div_cr(u[d.ij1] - u[d.ij], hy[j] + hy[jp], ryp) + div_cr(v[d.ij1] - v[d.i_1j1], hx[d.i_1] + hx[i], rxm);
-      s3 = (east && north)
+      s3 = (east && north_c)
                ? corner[q + W1 + 1]
                : div_cr(u[d.i1j1] - u[d.i1j], hy[j] + hy[jp], ryp) + div_cr(v[d.i1j1] - v[d.ij1], hx[i] + hx[d.i1], rxp);
     }
