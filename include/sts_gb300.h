@@ -28,6 +28,8 @@ extern "C" {
 #define STS_ERR_INPUT (-2)     /* missing or malformed case file */
 #define STS_ERR_CUDA (-3)      /* CUDA runtime error (no device, launch failure, ...) */
 #define STS_ERR_NONFINITE (-4) /* a residual went NaN/Inf during the steps just taken */
+#define STS_ERR_TIMEOUT (-5)   /* a bounded device-side wait (the sweep loop's grid barrier) gave up;
+                                  the context's state is no longer consistent and it stops stepping */
 
 typedef struct sts_ctx sts_ctx;
 
@@ -209,9 +211,10 @@ int sts_pt_sweeps(const sts_sweep_fields* f, int max_sweeps, int fixed_sweeps, d
  * Inputs and outputs are the caller's device arrays, as for sts_pt_sweeps.  The scratch lives
  * in one fixed device array inside the library, sized for STS_NOALLOC_MAX_CELLS cells (about
  * 2.6 MB, held on every GPU that loads the library until the process exits); larger meshes are
- * rejected with STS_ERR_ARG.  The first call on a device looks up that array's device address
- * (cudaGetSymbolAddress) with the device current; make that first call before any stream
- * capture.  All calls share the one array and it keeps the last call's contents (each call
+ * rejected with STS_ERR_ARG.  Every call looks up that array's device address on the current
+ * device (cudaGetSymbolAddress), so a device reset between calls leaves no stale address; the
+ * first call on a device may also load the library's device code there, so make that first call
+ * before any stream capture.  All calls share the one array and it keeps the last call's contents (each call
  * clears the counters it needs), so calls whose work overlaps on the GPU -- from several
  * threads or streams at once -- race and must be serialised by the caller. */
 int sts_pt_sweeps_noalloc(const sts_sweep_fields* f, int max_sweeps, int fixed_sweeps, double tol_p, double tol_T,
@@ -225,6 +228,15 @@ int sts_pt_sweeps_noalloc(const sts_sweep_fields* f, int max_sweeps, int fixed_s
  * passing answer).  No counterpart in the reference, which divides with the host's IEEE
  * division. */
 int sts_check_division(unsigned long long n, unsigned long long seed, int device, unsigned long long* mismatches);
+
+/* Self-check of the bounded wait of the sweep loop's grid barrier on `device`: one cooperative
+ * launch of one CTA per multiprocessor meets `rounds` grid barriers, each wait limited to
+ * spin_limit polls (about 0.1-1 us each).  CTA skip_cta (none when negative) leaves without
+ * arriving, so the others' first wait runs out; they record the timeout and end, the device stays
+ * usable.  Returns STS_OK when every barrier completed, STS_ERR_TIMEOUT when a wait gave up.  The
+ * same bounded wait guards every grid barrier of the sweep loops (about a second there), which
+ * then end the step with STS_ERR_TIMEOUT instead of hanging.  No counterpart in the reference. */
+int sts_check_barrier_timeout(int device, int skip_cta, unsigned spin_limit, int rounds);
 
 /* FP64 throughput of `device`, measured: gops[0..2] receive the rates (10^9 operations per
  * second) of dependent-free FP64 adds, multiplies and fused multiply-adds in a loop that keeps

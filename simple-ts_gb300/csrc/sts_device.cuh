@@ -265,10 +265,10 @@ __device__ __forceinline__ void st_relaxed(unsigned* p, unsigned v) {
 // last arriver has acquired every earlier arrival; it resets the counter and publishes the next
 // generation with a release store, which the others acquire before their CTA barrier releases
 // their threads (acquire/release pairs instead of full fences: about 0.5 us less per barrier
-// with 608 CTAs).  A CTA that waits longer than kSpinLimit polls sets ST_BARRIER_TIMEOUT and
+// with 608 CTAs).  A CTA that waits longer than spin_limit polls sets ST_BARRIER_TIMEOUT and
 // returns false, so a launch whose CTAs are not all resident ends with an error status instead
 // of hanging.
-__device__ bool grid_barrier(LoopCtl* lc) {
+__device__ bool grid_barrier(LoopCtl* lc, unsigned spin_limit = kSpinLimit) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0 && threadIdx.y == 0) {
@@ -280,7 +280,7 @@ __device__ bool grid_barrier(LoopCtl* lc) {
     } else {
       unsigned spins = 0;
       while (ld_acquire(&lc->bar_gen) == g0) {
-        if (++spins > kSpinLimit) {
+        if (++spins > spin_limit) {
           atomicOr(&lc->status, ST_BARRIER_TIMEOUT);
           good = 0;
           break;

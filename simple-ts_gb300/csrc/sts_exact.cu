@@ -1426,6 +1426,15 @@ __device__ __forceinline__ double make_double(unsigned long long bits, int exp_l
   return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 1023) << 52) | mant));
 }
 
+// Self-check of the grid barrier's bounded wait: CTA `skip` (none when skip < 0) returns without
+// arriving; every other CTA meets `rounds` barriers, each wait limited to spin_limit polls, and
+// leaves at the first one that gives up (ST_BARRIER_TIMEOUT in lc->status).  Every CTA ends.
+__global__ void k_barrier_probe(LoopCtl* lc, int skip, unsigned spin_limit, int rounds) {
+  if ((int)blockIdx.x == skip) return;
+  for (int r = 0; r < rounds; r++)
+    if (!grid_barrier(lc, spin_limit)) return;
+}
+
 __global__ void k_check_division(unsigned long long n, unsigned long long seed, unsigned long long* bad) {
   unsigned long long local = 0;
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;

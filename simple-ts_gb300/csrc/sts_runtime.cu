@@ -1125,7 +1125,7 @@ int sts_step(sts_ctx* ctx, int nsteps, int* steps_done) {
     if (!ctx->h_ctl->continue_step) ctx->finished = true;
     if (ctx->h_ctl->status & ST_BARRIER_TIMEOUT) {
       ctx->finished = true;  // the device state is no longer consistent
-      return fail(STS_ERR_CUDA, "a grid barrier of the sweep loop timed out");
+      return fail(STS_ERR_TIMEOUT, "a grid barrier of the sweep loop timed out");
     }
     if (ctx->h_ctl->status & ~status_before & ST_NONFINITE) {
       if (steps_done) *steps_done = done;
@@ -1168,7 +1168,7 @@ int sts_profile_steps(sts_ctx* ctx, int nsteps, double* kernel_ms, int* kernel_l
   }
   if (ctx->h_ctl->status & ST_BARRIER_TIMEOUT) {
     ctx->finished = true;
-    return fail(STS_ERR_CUDA, "a grid barrier of the sweep loop timed out");
+    return fail(STS_ERR_TIMEOUT, "a grid barrier of the sweep loop timed out");
   }
   if (!ctx->h_ctl->continue_step) ctx->finished = true;
   if (steps_done) *steps_done = done;
@@ -1371,9 +1371,17 @@ int sts_run_case(const char* case_dir, const sts_options* opt) {
   if (opt) o = *opt;
   sts_ctx* ctx = nullptr;
   g_err.clear();
+  const time_t time_solve_start = time(nullptr);  // SIMPLE_TS_MPI.cpp:1799
   if (int r = open_impl(case_dir, &o, &ctx)) return r;
   std::unique_ptr<sts_ctx> guard(ctx);
   const Config& cf = ctx->hc.cfg;
+  // The reference's wall-clock limit: the run ends after the first step that ends at or after
+  // time_solve_stop = start + max_time_for_solve hours (SIMPLE_TS_MPI.cpp:2010, :4443).  The host
+  // checks it between chunks of steps; a chunk is cut to the steps that fit in the time left
+  // (one step once the limit is closer than a step), so the run stops at the reference's step up
+  // to the resolution of time(NULL).
+  const double time_solve_stop = (double)time_solve_start + cf.d("max_time_for_solve") * 3600.0;
+  double s_per_step = 0;  // wall seconds per step, from the last chunk
   const long save_every = cf.n("Nt_save_solved_data") > 0 ? cf.n("Nt_save_solved_data") : 1;
   const long log_every = cf.n("Nt_save_temp_data") > 0 ? cf.n("Nt_save_temp_data") : 1;
   const long drag_every = cf.n("Nt_save_DragCoefficient") > 0 ? cf.n("Nt_save_DragCoefficient") : 1;
@@ -1385,9 +1393,16 @@ int sts_run_case(const char* case_dir, const sts_options* opt) {
   while (!ctx->finished) {
     long chunk = std::min(save_every - save_c, std::min(log_every - log_c, drag_every - drag_c));
     if (cont_each_step) chunk = 1;
+    {
+      const double left = time_solve_stop - (double)time(nullptr);
+      if (left <= 0 || s_per_step <= 0) chunk = 1;
+      else chunk = std::max(1L, std::min(chunk, (long)(left / s_per_step)));
+    }
     int done = 0;
+    const auto c0 = std::chrono::steady_clock::now();
     const int r = sts_step(ctx, (int)chunk, &done);
     if (r && r != STS_ERR_NONFINITE) return r;
+    if (done > 0) s_per_step = std::chrono::duration<double>(std::chrono::steady_clock::now() - c0).count() / done;
     save_c += done;
     log_c += done;
     drag_c += done;
@@ -1409,6 +1424,7 @@ int sts_run_case(const char* case_dir, const sts_options* opt) {
       log_c = 0;
     }
     if (done == 0) break;
+    if ((double)time(nullptr) >= time_solve_stop) break;  // SIMPLE_TS_MPI.cpp:4443
   }
   // after the loop (SIMPLE_TS_MPI.cpp:4695-4714)
   const double hours = std::chrono::duration<double>(std::chrono::steady_clock::now() - ctx->t0).count() / 3600.0;
@@ -1443,22 +1459,14 @@ namespace {
 constexpr size_t kNoAllocBytes = sizeof(Ctl) + 256 + 10 * (size_t)STS_NOALLOC_MAX_CELLS * sizeof(double);
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-// Device address of g_noalloc_scratch on each device, looked up once with that device current
-// (in host code the array's name only stands in for the symbol; it is not a device address).
-std::mutex g_noalloc_mutex;
-std::vector<char*> g_noalloc_addr;
-
+// Device address of g_noalloc_scratch on the current device.  In host code the array's name only
+// stands in for the symbol; it is not a device address.  The address is looked up on every call
+// (cudaGetSymbolAddress is cheap) so that a device reset or another context never leaves a stale
+// pointer behind.
 int noalloc_scratch(char** out) {
-  int dev = 0;
-  CU(cudaGetDevice(&dev));
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if ((int)g_noalloc_addr.size() <= dev) g_noalloc_addr.resize(dev + 1, nullptr);
-  if (!g_noalloc_addr[dev]) {
-    void* p = nullptr;
-    CU(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_noalloc_addr[dev] = (char*)p;
-  }
-  *out = g_noalloc_addr[dev];
+  void* p = nullptr;
+  CU(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+  *out = (char*)p;
   return STS_OK;
 }
 
@@ -1540,6 +1548,27 @@ int sts_check_division(unsigned long long n, unsigned long long seed, int device
   if (e == cudaSuccess) e = cudaMemcpy(mismatches, d, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
   cudaFree(d);
   if (e != cudaSuccess) return fail(STS_ERR_CUDA, std::string("sts_check_division: ") + cudaGetErrorString(e));
+  return STS_OK;
+}
+
+int sts_check_barrier_timeout(int device, int skip_cta, unsigned spin_limit, int rounds) {
+  if (rounds < 1 || spin_limit < 1) return fail(STS_ERR_ARG, "bad argument");
+  CU(cudaSetDevice(device));
+  int sms = 0;
+  CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  if (skip_cta >= sms) return fail(STS_ERR_ARG, "skip_cta beyond the grid (one CTA per multiprocessor)");
+  LoopCtl* lc = nullptr;
+  CU(cudaMalloc(&lc, sizeof(LoopCtl)));
+  LoopCtl h{};
+  cudaError_t e = cudaMemset(lc, 0, sizeof(LoopCtl));
+  if (e == cudaSuccess) {
+    void* args[] = {(void*)&lc, (void*)&skip_cta, (void*)&spin_limit, (void*)&rounds};
+    e = cudaLaunchCooperativeKernel((const void*)k_barrier_probe, dim3(sms), dim3(32, 8), args, 0, nullptr);
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(&h, lc, sizeof(LoopCtl), cudaMemcpyDeviceToHost);
+  cudaFree(lc);
+  if (e != cudaSuccess) return fail(STS_ERR_CUDA, std::string("sts_check_barrier_timeout: ") + cudaGetErrorString(e));
+  if (h.status & ST_BARRIER_TIMEOUT) return fail(STS_ERR_TIMEOUT, "a grid barrier timed out");
   return STS_OK;
 }
 
@@ -1942,7 +1971,7 @@ int sts_batch_step(sts_batch* b, int nsteps, int* steps_done) {
       if (int r = c->read_ctl()) return r;
       done = std::max(done, (int)(c->h_ctl->it_counter - before[k]));
       if (!c->h_ctl->continue_step) c->finished = true;
-      if (c->h_ctl->status & ST_BARRIER_TIMEOUT) return fail(STS_ERR_CUDA, "a grid barrier of the sweep loop timed out");
+      if (c->h_ctl->status & ST_BARRIER_TIMEOUT) return fail(STS_ERR_TIMEOUT, "a grid barrier of the sweep loop timed out");
       if (c->h_ctl->status & ~status_before[k] & ST_NONFINITE) nonfinite = true;
     }
     if (nonfinite) {

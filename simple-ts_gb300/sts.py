@@ -21,6 +21,7 @@ STS_ERR_ARG = -1
 STS_ERR_INPUT = -2
 STS_ERR_CUDA = -3
 STS_ERR_NONFINITE = -4
+STS_ERR_TIMEOUT = -5
 
 # every symbol include/sts_gb300.h declares
 EXPORTS = [
@@ -305,6 +306,17 @@ def check_division(n: int, seed: int = 1, device: int = 0) -> int:
     out = C.c_ulonglong()
     _check(lib.sts_check_division(int(n), int(seed), int(device), C.byref(out)))
     return out.value
+
+
+def check_barrier_timeout(skip_cta: int, spin_limit: int, rounds: int = 1, device: int = 0) -> int:
+    """The grid barrier's bounded wait: STS_OK when all `rounds` barriers completed, STS_ERR_TIMEOUT
+    when a wait gave up (skip_cta >= 0 leaves one CTA out of the barrier)."""
+    lib = load()
+    lib.sts_check_barrier_timeout.argtypes = [C.c_int, C.c_int, C.c_uint, C.c_int]
+    r = lib.sts_check_barrier_timeout(int(device), int(skip_cta), int(spin_limit), int(rounds))
+    if r not in (STS_OK, STS_ERR_TIMEOUT):
+        _check(r)
+    return r
 
 
 def fp64_rates(device: int = 0):

@@ -1,0 +1,115 @@
+"""The configured workloads for their whole length against the reference binary's own runs.
+
+Fixtures (tests/golden/make_golden_long.py): the reference solver run on
+  * the 400x40 Mach 0.1 channel for 1000 steps,
+  * the 1200x120 Mach 2.43 channel for 4000 steps,
+  * the 512x256 Rayleigh-Benard box for its steps (long_rayleigh_benard.json),
+  * an 80x8 channel with the time-dependent inflow ramp (SIMPLE_TS_MPI.cpp:8102-8144),
+each saving ten times into files of its own and logging every step.  The FP64 drop-in run must
+write every one of those files byte for byte (the time loop SIMPLE_TS_MPI.cpp:3230-4691 for
+the whole run).  The FP32-correction paths (precision 2 and 3) are then run for the same steps
+and their per-field relative L2 distance from the FP64 fields is printed and bounded.
+"""
+import json
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+import sts_cases as sc
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+LONG = ["channel_inflow_ramp", "channel_ma0.1", "channel_ma2.43", "rayleigh_benard"]
+FIELDS = ("u", "v", "p", "T", "rho")
+
+
+def record(name):
+    with open(os.path.join(GOLDEN, f"long_{name}.json")) as f:
+        rec = json.load(f)
+    arrays = dict(np.load(os.path.join(GOLDEN, f"long_{name}.npz")))
+    return rec, arrays
+
+
+def case_of(rec):
+    from make_golden_long import long_case
+    return long_case(rec["name"], rec["steps"])
+
+
+def rel_l2(a, b, mask):
+    d = np.linalg.norm((a - b)[mask])
+    n = np.linalg.norm(b[mask])
+    return float(d / n) if n > 0 else float(d)
+
+
+@pytest.mark.parametrize("name", LONG)
+def test_full_length_dropin_matches_reference(name, lib_built):
+    """Every dump of every save, Tmp.txt and Iterations_in_loops.txt equal the reference's."""
+    import sts
+    from make_golden_long import file_digest
+    rec, arrays = record(name)
+    case = case_of(rec)
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        sts.run_case(d, fixed_sweeps=False)
+        lines = open(os.path.join(d, "Iterations_in_loops.txt")).read().split("\n")
+        sweeps = np.array([int(l.split()[-1]) for l in lines if l.strip() and not l.startswith("it")])
+        np.testing.assert_array_equal(sweeps, arrays["sweeps"], err_msg="sweep count per step")
+        s = rec["stride"]
+        for f in ("u", "v", "p", "Temper"):
+            a = sc.read_field(d, f, rec["Nx"], rec["Ny"])[::s, ::s]
+            np.testing.assert_array_equal(a, arrays[f], err_msg=f)
+        bad = [f for f, h in rec["files"].items()
+               if not os.path.exists(os.path.join(d, f)) or file_digest(os.path.join(d, f)) != h]
+        assert not bad, f"files that differ from the reference's: {bad}"
+
+
+def run_fields(case, rec, precision):
+    """Steps the case in a fresh directory with the fixture's save cadence (a save applies the
+    reference's output-time wall-temperature overwrite to the live state, so the saves are part
+    of the trajectory); returns the final fields and the fluid mask."""
+    import sts
+    steps, every = rec["steps"], rec["save_every"]
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        fluid = sc.read_field(d, "vol_inf_fb", rec["Nx"], rec["Ny"]) == 0
+        with sts.Solver(d, fixed_sweeps=False, precision=precision) as g:
+            done = 0
+            while done < steps:
+                n = g.step(min(every, steps - done))
+                assert n > 0
+                done += n
+                if done % every == 0:
+                    g.write_outputs()
+            return {f: g.field(f) for f in FIELDS}, fluid
+
+
+# bounds of the FP32-correction paths' relative L2 distance from the FP64 fields after the whole
+# run; the Rayleigh-Benard box is convectively unstable, so differences at the tolerance level
+# grow with the instability there
+BOUNDS = {"channel_ma2.43": 1e-6, "rayleigh_benard": 1e-2}
+
+
+@pytest.mark.parametrize("name", ["channel_ma2.43", "rayleigh_benard"])
+def test_full_length_fp32_corrections_error(name, lib_built):
+    """Per-field relative L2 of precision 2 (FP32 sweeps on corrections, FP64 base fields,
+    FP64 stopping residuals) and precision 3 (the same with double-float FP64 parts) against
+    the FP64 path, which equals the reference on the sampled cells, after the whole run."""
+    rec, arrays = record(name)
+    case = case_of(rec)
+    ref, fluid = run_fields(case, rec, 0)
+    s = rec["stride"]
+    sampled_fluid = arrays["vol_inf_fb"] == 0
+    for f, g in (("u", "u"), ("v", "v"), ("p", "p"), ("T", "Temper")):
+        # compared on fluid cells: the dump's wall cells hold the output-time overwrite
+        np.testing.assert_array_equal(ref[f][::s, ::s][sampled_fluid], arrays[g][sampled_fluid], err_msg=f)
+    out = {}
+    for prec in (2, 3):
+        got, _ = run_fields(case, rec, prec)
+        out[prec] = {f: rel_l2(got[f], ref[f], fluid) for f in FIELDS}
+    print(f"\nFP32_CORRECTIONS_ERROR {name} steps={rec['steps']} " + json.dumps(out))
+    for prec, errs in out.items():
+        for f, e in errs.items():
+            assert e <= BOUNDS[name], (prec, f, e)

@@ -15,14 +15,49 @@ from test_gpu_sweeps import device_fields, sweep_inputs
 pytestmark = pytest.mark.gpu
 
 
+def _cudart():
+    """The CUDA runtime of the toolkit, for the device's memory counters."""
+    import ctypes
+    import glob
+    for path in sorted(glob.glob("/usr/local/cuda/lib64/libcudart.so*")):
+        try:
+            return ctypes.CDLL(path)
+        except OSError:
+            pass
+    pytest.skip("no CUDA runtime library to read the device memory counters")
+
+
+def _memory_state(rt, reset_high=False):
+    """(free device bytes, bytes the default stream-ordered pool has reserved, the pool's
+    high-water mark of bytes in use): what any cudaMalloc or cudaMallocAsync would change."""
+    import ctypes
+    free, total = ctypes.c_size_t(), ctypes.c_size_t()
+    assert rt.cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) == 0
+    pool = ctypes.c_void_p()
+    assert rt.cudaDeviceGetDefaultMemPool(ctypes.byref(pool), 0) == 0
+    reserved, used_high = ctypes.c_uint64(), ctypes.c_uint64()
+    if reset_high:  # cudaMemPoolAttrUsedMemHigh = 8: setting it to 0 restarts the high-water mark
+        assert rt.cudaMemPoolSetAttribute(pool, 8, ctypes.byref(ctypes.c_uint64(0))) == 0
+    assert rt.cudaMemPoolGetAttribute(pool, 5, ctypes.byref(reserved)) == 0  # ReservedMemCurrent
+    assert rt.cudaMemPoolGetAttribute(pool, 8, ctypes.byref(used_high)) == 0  # UsedMemHigh
+    return free.value, reserved.value, used_high.value
+
+
 def _run(meta, f, p0, T0, max_sweeps, fixed, noalloc):
     import sts
     import torch
     F, pt, Tt, keep = device_fields(meta, f, p0, T0)
     fn = sts.pt_sweeps_noalloc if noalloc else sts.pt_sweeps
+    mem = None
+    if noalloc:
+        rt = _cudart()
+        torch.cuda.synchronize()
+        before = _memory_state(rt, reset_high=True)
     n, rp, rT = fn(F, max_sweeps, fixed, 1e-10, 1e-10)
     torch.cuda.synchronize()
-    return n, rp, rT, pt.cpu().numpy(), Tt.cpu().numpy()
+    if noalloc:
+        mem = (before, _memory_state(rt))
+    return n, rp, rT, pt.cpu().numpy(), Tt.cpu().numpy(), mem
 
 
 def test_noalloc_matches_allocating_entry_point_twice(lib_built):
@@ -32,6 +67,7 @@ def test_noalloc_matches_allocating_entry_point_twice(lib_built):
     rng = np.random.default_rng(11)
     runs = [(sc.channel_case("c", 60, 10, 2.43, 0.00283, 2.5e-4, 100), False, 40),
             (sc.rayleigh_benard_case("rb", 24, 12, Nt=100), True, 5)]
+    calls = 0
     for case, fixed, nmax in runs:
         meta, f, p, T = sweep_inputs(case)
         assert meta["Nx"] * meta["Ny"] <= 32768
@@ -42,6 +78,15 @@ def test_noalloc_matches_allocating_entry_point_twice(lib_built):
         assert got[:3] == want[:3]
         np.testing.assert_array_equal(got[3], want[3])
         np.testing.assert_array_equal(got[4], want[4])
+        # nothing was allocated: the stream-ordered pool saw no allocation during the call and
+        # holds what it held, and the device's free memory is unchanged (checked from the second
+        # call on: the first call in a process may load the library's device code, which the
+        # CUDA runtime places in device memory)
+        (free0, reserved0, _), (free1, reserved1, used_high) = got[5]
+        assert reserved1 == reserved0 and used_high == 0
+        if calls:
+            assert free1 == free0
+        calls += 1
 
 
 def test_noalloc_rejects_meshes_beyond_its_limit(lib_built):
