@@ -31,8 +31,8 @@ UNIT = "cell-steps/s"
 WORKLOAD = "channel_ma2.43"
 L2_BYTES = 129 * 2 ** 20
 
-# algorithmic bytes per cell and launch of each kernel (stated in the design doc): arrays the
-# kernel must read once and write once for one cell, 8 bytes each, plus the 1-byte class
+# algorithmic bytes per cell and launch of each kernel: arrays the kernel must read once and
+# write once for one cell, 8 bytes each, plus the 1-byte class
 BYTES_PER_CELL = {
     "sweep_loop": 32,     # per sweep: read p, T of the iterate, write p, T (times sweeps per launch)
     "assemble": 27 * 8 + 1,
@@ -72,6 +72,10 @@ def parse():
                     help="which variants to time: all of them, or only the warm-start comparison "
                          "(plain FP64 against the extrapolated and learned starts) without the "
                          "checkpoint and untuned-shape lines")
+    ap.add_argument("--c5-steps", type=int, default=20,
+                    help="timed steps per path of the 2048x256 metric-configuration runs (0: skip them)")
+    ap.add_argument("--c5-lead", type=int, default=30,
+                    help="untimed steps before the timed ones for the warm-started paths of those runs")
     ap.add_argument("--no-variants", dest="variants", action="store_false",
                     help="skip the FP64-fast and FP32-correction runs of the same workload")
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2, 3],
@@ -218,49 +222,94 @@ def make_case(workload):
     return case, d
 
 
-def cpu_baseline(case_dir, seconds, start_steps=0):
-    """The oracle (serial C++ restatement of the reference) on this host: bounded sample."""
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def _replica_worker(case_dir, warm_steps, steps, seconds, start, q):
+    """One oracle replica on one host core: set-up and warm-up steps, then (after every replica is
+    ready) timed steps -- `steps` of them, or as many as fit in `seconds` when steps is 0."""
+    import sys
+    sys.path[:0] = [os.path.join(ROOT, "simple-ts_gb300"), os.path.join(ROOT, "oracle")]
     import ora
-    from build_oracle import build_oracle
-    build_oracle()
     o = ora.Oracle(case_dir, fixed_sweeps=False)
-    if start_steps:
-        o.step(start_steps)
+    if warm_steps:
+        o.step(warm_steps)
+    start.wait()
     n, t0 = 0, time.perf_counter()
     while True:
-        o.step(1)
-        n += 1
+        n += o.step(1)
         dt = time.perf_counter() - t0
-        if (dt >= seconds and n >= 2) or n >= 10000:
+        if (steps and n >= steps) or (not steps and ((dt >= seconds and n >= 2) or n >= 10000)):
             break
-    cells = o.Nx * o.Ny
-    return {"value": cells * n / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{n} time steps (steps {start_steps + 1}-{start_steps + n}) of the same case, serial oracle"}
+    q.put((o.Nx * o.Ny, n, dt))
+
+
+def cpu_replicas(case_dir, procs, warm_steps=0, steps=0, seconds=0.0):
+    """The oracle (serial C++ restatement of the reference) on `procs` host cores at once: one
+    independent replica of the case per core, started together after their set-up.  Returns the
+    host's aggregate cell-steps/s (the sum over replicas) and the per-replica samples.  The pool is
+    started with spawn, so it never inherits a CUDA context."""
+    import multiprocessing as mpr
+    from build_oracle import build_oracle
+    build_oracle()
+    ctx = mpr.get_context("spawn")
+    start = ctx.Barrier(procs)
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_replica_worker, args=(case_dir, warm_steps, steps, seconds, start, q))
+          for _ in range(procs)]
+    for p in ps:
+        p.start()
+    res = [q.get() for _ in ps]
+    for p in ps:
+        p.join()
+    return sum(c * n / dt for c, n, dt in res), res
+
+
+def cpu_baseline(case_dir, seconds, start_steps=0):
+    """The oracle (serial C++ restatement of the reference, bit-identical with the reference binary)
+    on this host: one replica of the case per host core, all timed together for a bounded time;
+    `value` is the host's aggregate cell-steps/s.  The reference solver is serial without MPI, so
+    independent replicas are how it uses every core.  The one-core rate is reported beside it."""
+    procs = host_cores()
+    agg, res = cpu_replicas(case_dir, procs, warm_steps=start_steps, seconds=seconds)
+    one, one_res = cpu_replicas(case_dir, 1, warm_steps=start_steps, seconds=min(seconds, 5.0))
+    steps = [n for _, n, _ in res]
+    return {"value": agg, "unit": UNIT, "cores": procs, "kind": "port",
+            "sample": f"{procs} concurrent replicas of the same case, one per host core, each timed for "
+                      f"about {seconds:.0f} s ({min(steps)}-{max(steps)} time steps each) after {start_steps} "
+                      "untimed steps; serial oracle, bit-identical with the reference binary",
+            "single_core": {"value": one, "cores": 1, "steps": one_res[0][1]}}
 
 
 def reference_arm(args):
+    """The reference's CPU path (the oracle port: the reference tree is not on the GPU host) on
+    every host core: one replica of the case per core, W warm-up steps, then K timed steps each;
+    the line's value is the host's aggregate cell-steps/s.  Rank 0 only."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     case, d = make_case(args.workload)
-    import ora
-    from build_oracle import build_oracle
-    build_oracle()
-    o = ora.Oracle(d, fixed_sweeps=False)
-    o.step(args.warmup)
+    procs = host_cores()
     t0 = time.perf_counter()
-    n = o.step(args.steps)
-    dt = time.perf_counter() - t0
-    cells = o.Nx * o.Ny
-    v = cells * n / dt
-    cfg = config(case, o.Nx, o.Ny)
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": n, "warmup": args.warmup, "ms_per_step": dt / n * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-                             "sample": f"{n} time steps after {args.warmup} warm-up steps, serial oracle "
+    agg, res = cpu_replicas(d, procs, warm_steps=args.warmup, steps=args.steps)
+    wall = time.perf_counter() - t0
+    cells, n, dt = res[0]
+    Nx, Ny = case.Nx, case.Ny
+    cfg = config(case, Nx, Ny)
+    line = {"impl": "reference", "metric": METRIC, "value": agg, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": max(x[2] / x[1] for x in res) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": cfg,
+            "cpu_baseline": {"value": agg, "unit": UNIT, "cores": procs, "kind": "port",
+                             "sample": f"{procs} concurrent replicas of the case, one per host core, each "
+                                       f"{args.warmup} warm-up + {args.steps} timed time steps; serial oracle "
                                        "(the reference solver is serial without MPI)"},
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": agg, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": round(wall, 2)}
     print(json.dumps(line), flush=True)
 
 
@@ -310,13 +359,28 @@ def launches_per_step(kcnt, pn):
     return sum(kcnt.values()) / max(pn, 1)
 
 
-def batch_dirs():
-    """Case directories of the 64-case batch (seed 20261204)."""
+def partition_cases(cells, world):
+    """Shards independent cases over `world` ranks: largest case first, each to the rank with the
+    fewest cells so far (ties to the lower rank).  Returns one sorted list of case indices per
+    rank; every case is in exactly one list.  Deterministic, so every rank computes the same."""
+    load = [0] * world
+    parts = [[] for _ in range(world)]
+    for k in sorted(range(len(cells)), key=lambda k: (-cells[k], k)):
+        r = min(range(world), key=lambda r: (load[r], r))
+        parts[r].append(k)
+        load[r] += cells[k]
+    return [sorted(p) for p in parts]
+
+
+def batch_dirs(indices=None):
+    """Case directories of the 64-case batch (seed 20261204), or of the cases `indices` of it."""
     import sts_cases as sc
     cases = sc.batch_cases(n=64, Nt=10 ** 7)
     root = tempfile.mkdtemp(prefix="sts_batch_")
     dirs = []
     for k, c in enumerate(cases):
+        if indices is not None and k not in indices:
+            continue
         d = os.path.join(root, f"c{k:02d}")
         os.makedirs(d)
         c.write(d)
@@ -324,24 +388,49 @@ def batch_dirs():
     return dirs
 
 
+def batch_cells():
+    import sts_cases as sc
+    return [c.Nx * c.Ny for c in sc.batch_cases(n=64, Nt=10 ** 7)]
+
+
 def batch_bench(args):
     """The 64-case batch (nx ~ U{200..800}, ny = nx/10, Mach, Kn and square position drawn
-    with seed 20261204): all cases advance together, one launch per kernel and step.  Prints a
-    JSON line of the same shape as the main bench (no e2e, no CPU baseline)."""
+    with seed 20261204): all cases advance together, one launch per kernel and step.  With
+    N > 1 ranks the cases are sharded over the GPUs (partition_cases; no collective on the data
+    path): every rank advances its share as one batch, the job's time is the slowest rank's and
+    the value counts every case's cells.  Prints a JSON line of the same shape as the main bench
+    (no e2e, no CPU baseline)."""
     import numpy as np
     import torch
     import sts
     import build as stsbuild
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     stsbuild.build()
-    dirs = batch_dirs()
+    all_cells = batch_cells()
+    mine = partition_cases(all_cells, world)[rank]
+    dirs = batch_dirs(set(mine))
     flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
     out = {}
     base = None
-    for name, prec, warm in (("fp64_exact", sts.EXACT, 0), ("fp64_fast", sts.FAST_FP64, 0),
-                             ("fp32_corrections", sts.MIXED, 0), ("fp32_corrections_warm2", sts.MIXED, 2),
-                             ("fp32_corrections_df", sts.MIXED_DF, 0), ("fp32_corrections_df_warm2", sts.MIXED_DF, 2),
-                             ("fp32_corrections_learned", sts.MIXED, 3), ("fp32_corrections_conv", sts.MIXED, 4),
-                             ("fp32_corrections_df_conv", sts.MIXED_DF, 4)):
+    variants = (("fp64_exact", sts.EXACT, 0), ("fp64_fast", sts.FAST_FP64, 0),
+                ("fp32_corrections", sts.MIXED, 0), ("fp32_corrections_warm2", sts.MIXED, 2),
+                ("fp32_corrections_df", sts.MIXED_DF, 0), ("fp32_corrections_df_warm2", sts.MIXED_DF, 2),
+                ("fp32_corrections_learned", sts.MIXED, 3), ("fp32_corrections_conv", sts.MIXED, 4),
+                ("fp32_corrections_df_conv", sts.MIXED_DF, 4))
+    if not args.variants:
+        variants = variants[:1]
+    for name, prec, warm in variants:
         b = sts.Batch(dirs, fixed_sweeps=False, precision=prec, warm_start=warm)
         cells = sum(c.Nx * c.Ny for c in b.cases)
         w = max(args.warmup, 3)
@@ -349,17 +438,20 @@ def batch_bench(args):
         lead += b.autotune_result()["steps_left"]  # the autotuner's steps come before the warm-up
         for _ in range(lead):
             b.step(1)
+        barrier()
         total, done = 0.0, 0
-        with Clocks(0) as clk:
+        with Clocks(local) as clk:
             for _ in range(args.steps):
                 flush.fill_(1.0)
                 torch.cuda.synchronize()
                 n, ms = b.step_timed(1)
                 total += ms
                 done += n
+        barrier()
+        total = slowest(total, world)
         fields = {f: np.concatenate([c.field(f).ravel() for c in b.cases]) for f in ("u", "v", "p", "T", "rho")}
         sweeps = np.concatenate([c.sweep_history()[-done:] for c in b.cases])
-        r = {"value": cells * done / (total / 1e3), "ms_per_step": total / max(done, 1),
+        r = {"value": sum(all_cells) * done / (total / 1e3), "ms_per_step": total / max(done, 1),
              "sweeps_per_step": float(np.mean(sweeps)), "clocks": clk.summary()}
         r["untimed_steps"] = lead
         r["launch_shapes"] = b.autotune_result()
@@ -379,15 +471,19 @@ def batch_bench(args):
         out[name] = r
         b.close()
     head = out["fp64_exact"]
-    line = {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+    line = {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": head["ms_per_step"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "scaling": "strong" if world > 1 else "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "batch of 64 channel cases, nx ~ U{200..800}, ny = nx/10, seed 20261204",
-                       "cells_per_step": cells, "residual_tolerance": 1e-8,
+                       "cells_per_step": sum(all_cells), "residual_tolerance": 1e-8,
+                       "sharding": f"{world} rank(s), cases per rank {[len(p) for p in partition_cases(all_cells, world)]}",
                        "l2": "flushed before every timed step (256 MiB write)"},
             "clocks": head["clocks"], "variants": {k: v for k, v in out.items() if k != "fp64_exact"},
             "sweeps_per_step": head["sweeps_per_step"]}
-    print(json.dumps(line), flush=True)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
 
 
 def checkpoint_bench(d, local, barrier, every=10, saves=10):
@@ -419,6 +515,66 @@ def checkpoint_bench(d, local, barrier, every=10, saves=10):
     return {"every_steps": every, "saves": saves, "bytes_per_save": Na * (4 * 8 + 4),
             "ms_per_step": {k: round(v, 5) for k, v in ms.items()},
             "save_cost_hidden": round(1.0 - cost_async / cost_sync, 3) if cost_sync > 0 else None}
+
+
+# The metric's own configuration: the 2048x256 channel with the square at four Mach numbers
+# (Kn 0.003, dt 1.25e-4, tolerance 1e-8); each path from the same initial state
+C5_MACHS = (0.1, 0.5, 1.0, 2.43)
+
+
+def metric_config_bench(args, local, flush, barrier):
+    """Plain GPU Jacobi (FP64 bit-exact, cold start) against the warm starts on the 2048x256
+    channel at each Mach number: FP32 corrections with double-float FP64 parts from a cold start,
+    from quadratic extrapolation and from the learned convolutional predictor, and the learned
+    predictor on the FP64 path.  Per path: cell-steps/s (device time, L2 flushed before every
+    timed step), sweeps per step and the largest per-field relative L2 distance from the plain
+    path after the same steps; per Mach: the learned start against plain Jacobi and against the
+    same precision without it."""
+    import numpy as np
+    import sts
+    import sts_cases as sc
+    EX, DF = sts.EXACT, sts.MIXED_DF
+    paths = (("plain_fp64", EX, 0), ("fp64_learned", EX, 4), ("fp32df_cold", DF, 0),
+             ("fp32df_quadratic", DF, 2), ("fp32df_learned", DF, 4))
+    out = {}
+    for mach in C5_MACHS:
+        case = sc.config_case(f"channel_2048_ma{mach}", Nt=10 ** 7)
+        d = tempfile.mkdtemp(prefix="sts_c5_")
+        case.write(d)
+        base = {}
+
+        def base_at(n):
+            if n not in base:
+                ref = sts.Solver(d, fixed_sweeps=False, device=local, precision=EX, autotune=False)
+                ref.step(n)
+                base[n] = {f: ref.field(f) for f in ("u", "v", "p", "T", "rho")}
+                ref.close()
+            return base[n]
+
+        row = {}
+        for name, prec, warm in paths:
+            v = sts.Solver(d, fixed_sweeps=False, device=local, precision=prec, warm_start=warm)
+            lead = max(args.c5_lead, 3) if warm else max(args.warmup, 3)
+            vd, vms, vsw = timed_steps(v, args.c5_steps, lead, flush, barrier)
+            ref = base_at(v.steps_before_timing + vd)
+            err = max(float(np.linalg.norm(v.field(f) - ref[f]) / np.linalg.norm(ref[f])) for f in ref)
+            row[name] = {"value": v.Nx * v.Ny * vd / (vms / 1e3), "ms_per_step": vms / max(vd, 1),
+                         "sweeps_per_step": float(np.mean(vsw)) if len(vsw) else 0.0,
+                         "max_rel_l2_vs_plain": err, "untimed_steps": v.steps_before_timing}
+            cells = v.Nx * v.Ny
+            v.close()
+        plain, learned = row["plain_fp64"], row["fp32df_learned"]
+
+        def gain(a, b):
+            return {"speedup": row[a]["value"] / row[b]["value"],
+                    "sweep_ratio": row[b]["sweeps_per_step"] / max(row[a]["sweeps_per_step"], 1e-30)}
+        out[f"ma{mach}"] = {"cells": cells, "paths": row,
+                            "learned_vs_plain": gain("fp32df_learned", "plain_fp64"),
+                            "learned_vs_same_precision_cold": gain("fp32df_learned", "fp32df_cold"),
+                            "learned_vs_quadratic": gain("fp32df_learned", "fp32df_quadratic"),
+                            "fp64_learned_vs_plain": gain("fp64_learned", "plain_fp64")}
+    return {"workload": "channel 2048x256 with the square, Kn 0.003, dt 1.25e-4, tolerance 1e-8",
+            "timed_steps": args.c5_steps, "untimed_steps_warm": args.c5_lead, "by_mach": out}
 
 
 def warm_summary(plain_value, plain_sweeps, variants):
@@ -562,6 +718,7 @@ def main():
 
     full = args.variants and args.variant_set == "all"
     ckpt = checkpoint_bench(d, local, barrier) if full else None
+    c5 = metric_config_bench(args, local, flush, barrier) if full and args.c5_steps > 0 else None
 
     # the FP64 bit-exact path with the default launch shapes (no autotuning), beside the headline,
     # which uses the shapes the autotuner chose on the run's first steps (the shapes change no result)
@@ -585,7 +742,8 @@ def main():
                                     "max": int(max(sweeps)) if len(sweeps) else 0},
                 "variants": variants,
                 "warm_start_vs_plain": warm_summary(value, sweeps, variants),
-                "checkpoint": ckpt, "untuned_fp64": tuned, "launch_shapes": launch_shapes}
+                "checkpoint": ckpt, "untuned_fp64": tuned, "launch_shapes": launch_shapes,
+                "metric_config": c5}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

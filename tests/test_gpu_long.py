@@ -89,7 +89,7 @@ def run_fields(case, rec, precision):
 # bounds of the FP32-correction paths' relative L2 distance from the FP64 fields after the whole
 # run; the Rayleigh-Benard box is convectively unstable, so differences at the tolerance level
 # grow with the instability there
-BOUNDS = {"channel_ma2.43": 1e-6, "rayleigh_benard": 1e-2}
+BOUNDS = {"channel_ma2.43": 1e-8, "rayleigh_benard": 1e-2}
 
 
 @pytest.mark.parametrize("name", ["channel_ma2.43", "rayleigh_benard"])

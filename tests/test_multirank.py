@@ -69,3 +69,63 @@ def test_reference_arm_runs_on_rank_zero_only(capsys, monkeypatch):
         gpus = 2
     assert bench.reference_arm(Args()) is None
     assert capsys.readouterr().out == ""
+
+
+def test_partition_covers_every_case_once():
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    cells = bench.batch_cells()
+    assert len(cells) == 64
+    for world in (1, 2, 3, 4, 8):
+        parts = bench.partition_cases(cells, world)
+        flat = sorted(k for p in parts for k in p)
+        assert flat == list(range(64))
+        loads = [sum(cells[k] for k in p) for p in parts]
+        assert max(loads) - min(loads) <= max(cells)  # greedy largest-first balance
+        assert parts == bench.partition_cases(cells, world)  # every rank computes the same
+
+
+def shard_worker(rank, world, port, out_dir):
+    import sys
+    sys.path[:0] = [ROOT, os.path.join(ROOT, "simple-ts_gb300"), os.path.join(ROOT, "oracle")]
+    import torch.distributed as dist
+    import bench
+    import ora
+    import sts_cases as sc
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    cases = sc.batch_cases(n=6, Nt=10, nx_range=(30, 60))
+    mine = bench.partition_cases([c.Nx * c.Ny for c in cases], world)[rank]
+    for k in mine:  # each rank advances only its own cases
+        d = tempfile.mkdtemp()
+        cases[k].write(d)
+        o = ora.Oracle(d, fixed_sweeps=False)
+        o.step(3)
+        np.save(os.path.join(out_dir, f"case{k}_rank{rank}.npy"), np.stack([o.field(f) for f in ("u", "v", "p", "T")]))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_rank_case_sharding_equals_single_process(oracle_built):
+    """Sharded over two gloo ranks, every case is advanced by exactly one rank, and its fields
+    equal those of the same case advanced in a single process."""
+    import sys
+    sys.path[:0] = [os.path.join(ROOT, "simple-ts_gb300"), os.path.join(ROOT, "oracle")]
+    import ora
+    import sts_cases as sc
+    port = free_port()
+    with tempfile.TemporaryDirectory() as out:
+        mp.start_processes(shard_worker, args=(2, port, out), nprocs=2, join=True, start_method="spawn")
+        files = sorted(os.listdir(out))
+        owners = {}
+        for f in files:
+            k = int(f.split("_")[0][4:])
+            owners.setdefault(k, []).append(f)
+        assert sorted(owners) == list(range(6)) and all(len(v) == 1 for v in owners.values())
+        for k, c in enumerate(sc.batch_cases(n=6, Nt=10, nx_range=(30, 60))):
+            with tempfile.TemporaryDirectory() as d:
+                c.write(d)
+                o = ora.Oracle(d, fixed_sweeps=False)
+                o.step(3)
+                want = np.stack([o.field(f) for f in ("u", "v", "p", "T")])
+            np.testing.assert_array_equal(np.load(os.path.join(out, owners[k][0])), want)
