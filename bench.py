@@ -256,16 +256,25 @@ def cpu_replicas(case_dir, procs, warm_steps=0, steps=0, seconds=0.0):
     import multiprocessing as mpr
     from build_oracle import build_oracle
     build_oracle()
+    import queue
     ctx = mpr.get_context("spawn")
-    start = ctx.Barrier(procs)
+    start = ctx.Barrier(procs, timeout=600)
     q = ctx.Queue()
-    ps = [ctx.Process(target=_replica_worker, args=(case_dir, warm_steps, steps, seconds, start, q))
+    ps = [ctx.Process(target=_replica_worker, args=(case_dir, warm_steps, steps, seconds, start, q), daemon=True)
           for _ in range(procs)]
     for p in ps:
         p.start()
-    res = [q.get() for _ in ps]
-    for p in ps:
-        p.join()
+    res = []
+    try:
+        for _ in ps:
+            res.append(q.get(timeout=900))
+    except queue.Empty:
+        raise RuntimeError(f"CPU baseline: {len(res)} of {procs} oracle replicas reported")
+    finally:
+        for p in ps:
+            p.join(timeout=5)
+            if p.is_alive():
+                p.terminate()
     return sum(c * n / dt for c, n, dt in res), res
 
 

@@ -129,6 +129,16 @@ int sts_set_field(sts_ctx* ctx, const char* name, const double* host_in);
 int sts_set_state(sts_ctx* ctx, const double* u_in, const double* v_in, const double* p_in, const double* T_in);
 int sts_get_state(sts_ctx* ctx, double* u_out, double* v_out, double* p_out, double* T_out);
 
+/* Global conservation sums of the current state over the fluid cells, in FP64 on the device in a
+ * fixed order (each row in chunks of 64 cells in x order, the chunks of a row in order, the rows in
+ * y order), so the same state always gives the same bits: out5[0] mass sum rho A, [1] and [2]
+ * momentum sums rho A u_c and rho A v_c, [3] internal energy sum rho A T / (gamma - 1), [4] kinetic
+ * energy sum rho A (u_c^2 + v_c^2); A = hx hy, u_c and v_c the means of a cell's two face
+ * velocities (energies in units of rho0 R T0 per unit area, velocities being in units of
+ * sqrt(2 R T0)).  No counterpart in the reference, whose SolveContinuityEquation
+ * (SIMPLE_TS_MPI.cpp:10621-10714) gives the local continuity residual. */
+int sts_conservation(sts_ctx* ctx, double* out5);
+
 /* Mesh size. */
 int sts_dims(sts_ctx* ctx, int* Nx, int* Ny);
 
@@ -228,6 +238,38 @@ int sts_pt_sweeps_noalloc(const sts_sweep_fields* f, int max_sweeps, int fixed_s
  * passing answer).  No counterpart in the reference, which divides with the host's IEEE
  * division. */
 int sts_check_division(unsigned long long n, unsigned long long seed, int device, unsigned long long* mismatches);
+
+/* Self-check of the BF16 tensor-core GEMM of the learned warm start's network (tcgen05 MMAs fed by
+ * TMA, FP32 accumulation in tensor memory) on `device`: D[M x N] = A[M x K] * B[N x K]^T (+ bias[n],
+ * then max(., 0) if relu), A and B row-major BF16 bit patterns on the host (K a multiple of 8),
+ * D row-major FP32 on the host; bias may be NULL.  STS_ERR_TIMEOUT if a pipeline wait gave up.
+ * No counterpart in the reference. */
+int sts_tc_gemm(const unsigned short* A, const unsigned short* B, int M, int N, int K, int relu, const float* bias,
+                float* D, int device);
+
+/* The convolutional network of the learned warm start, on host arrays: a U-Net (levels L, base
+ * channels C0, C_l = C0 2^l; two 3x3 convolutions with ReLU per level, 2x2 average pooling down,
+ * nearest-neighbour upsampling and concatenation with the encoder output up, a 1x1 head) with BF16
+ * weights and activations and FP32 accumulation; every convolution is a tcgen05 tensor-core GEMM
+ * (sts_tc_gemm).  Images are batches of B crops of H x W pixels, NHWC (channels contiguous), FP32
+ * on the host.  in_ch, out_ch <= 8; C0 a multiple of 8; H, W multiples of 2^(L-1).  Parameters
+ * (FP32 master copy) in layer order: per convolution Wt[(3 (dy+1) + (dx+1)) C_in + c][C_out] then
+ * the bias [C_out]; the head's Wt [C0][8] then its bias [8] (outputs beyond out_ch held at 0).
+ * No counterpart in the reference, which starts every step's sweeps from the previous step. */
+typedef struct sts_net sts_net;
+int sts_net_create(int in_ch, int out_ch, int base_ch, int levels, int max_batch, int H, int W, unsigned long long seed,
+                   int device, sts_net** out);
+long long sts_net_param_count(sts_net* net);
+int sts_net_get_params(sts_net* net, float* out);
+int sts_net_set_params(sts_net* net, const float* in);
+/* y [B][H][W][out_ch] = net(x [B][H][W][in_ch]). */
+int sts_net_forward(sts_net* net, const float* x, int B, float* y);
+/* After sts_net_forward with the same B: the parameter gradients of sum(gy * y) into grads. */
+int sts_net_backward(sts_net* net, const float* gy, int B, float* grads);
+/* One Adam step (learning rate lr) on the mean squared error against target [B][H][W][out_ch];
+ * *loss receives the loss before the step. */
+int sts_net_train_step(sts_net* net, const float* x, const float* target, int B, float lr, float* loss);
+void sts_net_destroy(sts_net* net);
 
 /* Self-check of the bounded wait of the sweep loop's grid barrier on `device`: one cooperative
  * launch of one CTA per multiprocessor meets `rounds` grid barriers, each wait limited to

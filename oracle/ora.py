@@ -39,6 +39,7 @@ def load():
         lib.ora_stats.argtypes = [P, C.POINTER(C.c_double)]
         lib.ora_set_warm_start.argtypes = [P, C.c_int]
         lib.ora_set_guess.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        lib.ora_conservation.argtypes = [P, C.POINTER(C.c_double)]
         _lib = lib
     return _lib
 
@@ -91,6 +92,13 @@ class Oracle:
     def stats(self):
         out = np.zeros(9)
         load().ora_stats(self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out
+
+    def conservation(self):
+        """[mass, x momentum, y momentum, internal energy, kinetic energy] sums of the current
+        state over the fluid cells, in the GB300 library's fixed summation order."""
+        out = np.zeros(5)
+        load().ora_conservation(self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
         return out
 
     def finish(self):

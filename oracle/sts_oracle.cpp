@@ -2604,6 +2604,41 @@ int ora_pt_sweeps(int Nx, int Ny, int periodic, int given_xb, int given_xe, int 
   return 0;
 }
 
+// Global conservation sums of the current state (the GB300 library's sts_conservation, which has
+// no counterpart in the reference): per fluid cell, A = hx hy, u_c = (u_ij + u_i+1,j) / 2,
+// v_c = (v_ij + v_i,j+1) / 2 (neighbour clamped at the last column or row); mass rho A, momentum
+// rho A u_c and rho A v_c, internal energy rho A T / (gamma - 1), kinetic energy
+// rho A (u_c^2 + v_c^2).  Summed in the library's fixed order: chunks of 64 cells of a row in x
+// order, the chunks of a row in order, the rows in y order.
+int ora_conservation(ora_handle* h, double* out) {
+  Oracle& o = h->o;
+  const int Nx = (int)o.Nx, Ny = (int)o.Ny, CH = 64, nch = (Nx + CH - 1) / CH;
+  double tot[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int j = 0; j < Ny; j++) {
+    double row[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int k = 0; k < nch; k++) {
+      double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+      for (int i = k * CH; i < std::min(Nx, (k + 1) * CH); i++) {
+        const int n = i + j * Nx;
+        if (!o.vol[n]) continue;
+        const int ne = (i + 1 < Nx) ? n + 1 : n, nn = (j + 1 < Ny) ? n + Nx : n;
+        const double A = o.hx[i] * o.hy[j];
+        const double uc = 0.5 * (o.u[n] + o.u[ne]), vc = 0.5 * (o.v[n] + o.v[nn]);
+        const double m = o.rho[n] * A;
+        s[0] = s[0] + m;
+        s[1] = s[1] + m * uc;
+        s[2] = s[2] + m * vc;
+        s[3] = s[3] + (m * o.Temper[n]) / (o.gamma1 - 1.0);
+        s[4] = s[4] + m * (uc * uc + vc * vc);
+      }
+      for (int q = 0; q < 5; q++) row[q] = row[q] + s[q];
+    }
+    for (int q = 0; q < 5; q++) tot[q] = tot[q] + row[q];
+  }
+  for (int q = 0; q < 5; q++) out[q] = tot[q];
+  return 0;
+}
+
 // Per-step sweep counts (sum over outer iterations), oldest first; returns how many were copied.
 int ora_sweeps(ora_handle* h, unsigned int* out, int cap) {
   int n = (int)h->o.sweeps_per_step.size();

@@ -21,6 +21,8 @@ UNITS = [
     ("sts_exact.cu", ["--fmad=false"]),
     ("sts_fast.cu", []),
     ("sts_learn.cu", ["--fmad=false"]),
+    ("sts_net.cu", []),
+    ("sts_unet.cu", []),
     ("sts_runtime.cu", []),
     ("sts_host.cpp", []),
     ("sts_checkpoint.cpp", []),

@@ -1426,6 +1426,53 @@ __device__ __forceinline__ double make_double(unsigned long long bits, int exp_l
   return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 1023) << 52) | mant));
 }
 
+// Global conservation sums of the current state (no counterpart in the reference; its
+// SolveContinuityEquation, SIMPLE_TS_MPI.cpp:10621-10714, gives the local continuity residual).
+// Per fluid cell (i, j), area A = hx_i hy_j, cell-centre velocities u_c = (u_ij + u_i+1,j) / 2,
+// v_c = (v_ij + v_i,j+1) / 2 (the neighbour index clamped at the last column or row):
+//   mass rho A, momentum rho A u_c and rho A v_c, internal energy rho A T / (gamma - 1),
+//   kinetic energy rho A (u_c^2 + v_c^2)
+// (energies per unit depth in units of rho0 R T0 L^2: velocities are in units of sqrt(2 R T0)).
+// FP64 in a fixed order: each thread sums kConsChunk cells of a row in x order, then
+// k_cons_final sums each row's chunks in order and the rows in y order.
+__global__ void k_cons_partial(Geo g, unsigned cur, double* part, int nch) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (k >= nch || j >= g.Ny) return;
+  const int Nx = g.Nx, Ny = g.Ny;
+  const double* T = g.T[cur];
+  double s[kConsQ] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  const int i1 = min(Nx, (k + 1) * kConsChunk);
+  for (int i = k * kConsChunk; i < i1; i++) {
+    const int n = i + j * Nx;
+    if (!cls_fluid(g.cls[n])) continue;
+    const int ne = (i + 1 < Nx) ? n + 1 : n, nn = (j + 1 < Ny) ? n + Nx : n;
+    const double A = g.hx[i] * g.hy[j];
+    const double uc = 0.5 * (g.u[n] + g.u[ne]), vc = 0.5 * (g.v[n] + g.v[nn]);
+    const double m = g.rho[n] * A;
+    s[0] = s[0] + m;
+    s[1] = s[1] + m * uc;
+    s[2] = s[2] + m * vc;
+    s[3] = s[3] + (m * T[n]) / (g.gamma1 - 1.0);
+    s[4] = s[4] + m * (uc * uc + vc * vc);
+  }
+  for (int q = 0; q < kConsQ; q++) part[((size_t)j * nch + k) * kConsQ + q] = s[q];
+}
+
+__global__ void k_cons_final(int Ny, int nch, const double* part, double* rows, double* out) {
+  for (int j = threadIdx.x; j < Ny; j += blockDim.x)
+    for (int q = 0; q < kConsQ; q++) {
+      double s = 0.0;
+      for (int k = 0; k < nch; k++) s = s + part[((size_t)j * nch + k) * kConsQ + q];
+      rows[(size_t)j * kConsQ + q] = s;
+    }
+  __syncthreads();
+  if (threadIdx.x < kConsQ) {
+    double s = 0.0;
+    for (int j = 0; j < Ny; j++) s = s + rows[(size_t)j * kConsQ + threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+}
+
 // Self-check of the grid barrier's bounded wait: CTA `skip` (none when skip < 0) returns without
 // arriving; every other CTA meets `rounds` barriers, each wait limited to spin_limit polls, and
 // leaves at the first one that gives up (ST_BARRIER_TIMEOUT in lc->status).  Every CTA ends.

@@ -80,6 +80,9 @@ __global__ void k_continuity(Geo g, double* st, double* ce);
 // self-check of the correctly rounded division by a reciprocal against IEEE division
 __global__ void k_check_division(unsigned long long n, unsigned long long seed, unsigned long long* bad);
 __global__ void k_barrier_probe(LoopCtl* lc, int skip, unsigned spin_limit, int rounds);
+constexpr int kConsQ = 5, kConsChunk = 64;
+__global__ void k_cons_partial(Geo g, unsigned cur, double* part, int nch);
+__global__ void k_cons_final(int Ny, int nch, const double* part, double* rows, double* out);
 __global__ void k_fp64_rate(int op, int iters, double c_mul, double c_add, double* out);
 __global__ void k_move4(const double* a0, const double* a1, const double* a2, const double* a3, double* b0,
                         double* b1, double* b2, double* b3, int n);

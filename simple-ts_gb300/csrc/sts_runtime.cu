@@ -83,6 +83,8 @@ struct sts_ctx {
   int* d_drag_first = nullptr;
   double* d_drag_out = nullptr;
   double *d_cont_st = nullptr, *d_cont = nullptr;
+  // global conservation sums (made at the first sts_conservation call)
+  double *d_cons_part = nullptr, *d_cons_rows = nullptr, *d_cons_out = nullptr;
   bool cd_fresh = true, pu_fresh = true;
   // checkpoint dumps (made at the first save)
   std::unique_ptr<Checkpointer> saver;
@@ -1486,6 +1488,24 @@ int sts_pt_sweeps_noalloc(const sts_sweep_fields* f, int max_sweeps, int fixed_s
   if (int r = noalloc_scratch(&scratch)) return r;
   return pt_sweeps_on(f, max_sweeps, fixed_sweeps, tol_p, tol_T, (cudaStream_t)stream, scratch, sweeps_done, res_p,
                       res_T);
+}
+
+int sts_conservation(sts_ctx* ctx, double* out5) {
+  if (!ctx || !out5) return fail(STS_ERR_ARG, "null argument");
+  CU(cudaSetDevice(ctx->opt.device));
+  const Geo& g = ctx->g;
+  const int nch = (g.Nx + kConsChunk - 1) / kConsChunk;
+  if (!ctx->d_cons_part) {
+    if (int r = ctx->alloc(&ctx->d_cons_part, (size_t)g.Ny * nch * kConsQ)) return r;
+    if (int r = ctx->alloc(&ctx->d_cons_rows, (size_t)g.Ny * kConsQ)) return r;
+    if (int r = ctx->alloc(&ctx->d_cons_out, (size_t)kConsQ)) return r;
+  }
+  k_cons_partial<<<dim3((nch + 31) / 32, g.Ny), 32, 0, ctx->s>>>(g, ctx->h_ctl->cur, ctx->d_cons_part, nch);
+  k_cons_final<<<1, 256, 0, ctx->s>>>(g.Ny, nch, ctx->d_cons_part, ctx->d_cons_rows, ctx->d_cons_out);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(out5, ctx->d_cons_out, sizeof(double) * kConsQ, cudaMemcpyDeviceToHost, ctx->s));
+  CU(cudaStreamSynchronize(ctx->s));
+  return STS_OK;
 }
 
 int sts_sync(sts_ctx* ctx) {

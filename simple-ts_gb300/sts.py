@@ -183,6 +183,13 @@ class Solver:
         _check(load().sts_stats(self._h, _dptr(out)))
         return out
 
+    def conservation(self) -> np.ndarray:
+        """[mass, x momentum, y momentum, internal energy, kinetic energy] sums of the current state
+        over the fluid cells (FP64, fixed order, on the device)."""
+        out = np.zeros(5)
+        _check(load().sts_conservation(self._h, _dptr(out)))
+        return out
+
     def sweep_history(self, cap: int = 4096) -> np.ndarray:
         out = np.zeros(cap, dtype=np.uint32)
         n = C.c_int()

@@ -1,0 +1,165 @@
+"""The learned warm start's U-Net (BF16 weights and activations, FP32 accumulation, tcgen05 GEMMs)
+against an FP32 restatement of the same network in PyTorch on the CPU: forward outputs, parameter
+gradients of the backward pass, and an Adam training run whose loss falls."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+class Net:
+    def __init__(self, in_ch, out_ch, base, levels, B, H, W, seed=1):
+        import sts
+        self.lib = lib = sts.load()
+        lib.sts_net_create.argtypes = [C.c_int] * 7 + [C.c_ulonglong, C.c_int, C.POINTER(C.c_void_p)]
+        lib.sts_net_param_count.restype = C.c_longlong
+        lib.sts_net_param_count.argtypes = [C.c_void_p]
+        for f in ("sts_net_get_params", "sts_net_set_params"):
+            getattr(lib, f).argtypes = [C.c_void_p, C.c_void_p]
+        lib.sts_net_forward.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+        lib.sts_net_backward.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+        lib.sts_net_train_step.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_void_p]
+        lib.sts_net_destroy.argtypes = [C.c_void_p]
+        self.h = C.c_void_p()
+        assert lib.sts_net_create(in_ch, out_ch, base, levels, B, H, W, seed, 0, C.byref(self.h)) == 0
+        self.shape = (in_ch, out_ch, base, levels, H, W)
+        self.n = lib.sts_net_param_count(self.h)
+
+    def params(self):
+        p = np.zeros(self.n, np.float32)
+        assert self.lib.sts_net_get_params(self.h, p.ctypes.data) == 0
+        return p
+
+    def forward(self, x):
+        B = x.shape[0]
+        y = np.zeros(x.shape[:3] + (self.shape[1],), np.float32)
+        x = np.ascontiguousarray(x, np.float32)
+        assert self.lib.sts_net_forward(self.h, x.ctypes.data, B, y.ctypes.data) == 0
+        return y
+
+    def backward(self, gy):
+        g = np.zeros(self.n, np.float32)
+        gy = np.ascontiguousarray(gy, np.float32)
+        assert self.lib.sts_net_backward(self.h, gy.ctypes.data, gy.shape[0], g.ctypes.data) == 0
+        return g
+
+    def train_step(self, x, t, lr):
+        loss = C.c_float()
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        assert self.lib.sts_net_train_step(self.h, x.ctypes.data, t.ctypes.data, x.shape[0], lr, C.byref(loss)) == 0
+        return loss.value
+
+    def close(self):
+        self.lib.sts_net_destroy(self.h)
+
+
+def torch_net(params, in_ch, out_ch, base, levels):
+    """The same network in PyTorch (FP32), weights from the flat parameter vector; activations are
+    rounded to BF16 after every layer as on the GPU.  Returns (forward function, parameter tensors)."""
+    import torch
+    import torch.nn.functional as F
+    bf = lambda t: t.to(torch.bfloat16).to(torch.float32)  # noqa: E731
+    off = [0]
+    tensors = []
+
+    def take(cin, cout, k):
+        n = k * k * cin * cout
+        wt = torch.tensor(params[off[0]:off[0] + n]).reshape(k, k, cin, cout)
+        b = torch.tensor(params[off[0] + n:off[0] + n + cout])
+        off[0] += n + cout
+        w = bf(wt.permute(3, 2, 0, 1).contiguous()).requires_grad_(True)
+        b = b.clone().requires_grad_(True)
+        tensors.append((w, b))
+        return w, b
+
+    ch = [base << l for l in range(levels)]
+    enc = [(take(8, ch[0], 3), take(ch[0], ch[0], 3))]
+    for l in range(1, levels):
+        enc.append((take(ch[l - 1], ch[l], 3), take(ch[l], ch[l], 3)))
+    dec = {}
+    for l in range(levels - 2, -1, -1):
+        dec[l] = (take(ch[l + 1] + ch[l], ch[l], 3), take(ch[l], ch[l], 3))
+    head = take(ch[0], 8, 1)
+
+    def conv(x, wb, relu=True):
+        y = F.conv2d(x, wb[0], wb[1], padding=wb[0].shape[-1] // 2)
+        return bf(F.relu(y)) if relu else y
+
+    def fwd(x):
+        x = bf(F.pad(x, (0, 0, 0, 0, 0, 8 - in_ch)) if x.shape[1] < 8 else bf(x))
+        skips = []
+        h = x
+        for l in range(levels):
+            if l > 0:
+                h = bf(F.avg_pool2d(h, 2))
+            h = conv(conv(h, enc[l][0]), enc[l][1])
+            skips.append(h)
+        for l in range(levels - 2, -1, -1):
+            h = torch.cat([F.interpolate(h, scale_factor=2, mode="nearest"), skips[l]], dim=1)
+            h = conv(conv(h, dec[l][0]), dec[l][1])
+        return conv(h, head, relu=False)[:, :out_ch]
+
+    return fwd, tensors
+
+
+def flat_grads(tensors, params):
+    """Gradients of the torch tensors in the library's parameter layout."""
+    out = []
+    for w, b in tensors:
+        out.append(w.grad.permute(2, 3, 1, 0).reshape(-1).numpy())
+        out.append(b.grad.numpy())
+    return np.concatenate(out)
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.mark.parametrize("levels,base,H,W", [(1, 16, 16, 16), (2, 16, 32, 16), (4, 32, 32, 64)])
+def test_unet_forward_and_gradients_match_torch(levels, base, H, W, lib_built):
+    import torch
+    in_ch, out_ch, B = 8, 2, 2
+    net = Net(in_ch, out_ch, base, levels, B, H, W, seed=7)
+    p = net.params()
+    rng = np.random.default_rng(levels)
+    x = rng.standard_normal((B, H, W, in_ch)).astype(np.float32)
+    y = net.forward(x)
+    fwd, tensors = torch_net(p, in_ch, out_ch, base, levels)
+    xt = torch.tensor(x).permute(0, 3, 1, 2)
+    yt = fwd(xt)
+    want = yt.detach().permute(0, 2, 3, 1).numpy()
+    assert rel(y, want) < 3e-2, rel(y, want)
+    # gradients of sum(gy * y)
+    gy = rng.standard_normal(y.shape).astype(np.float32)
+    g = net.backward(gy)
+    (yt * torch.tensor(gy).permute(0, 3, 1, 2)).sum().backward()
+    gw = flat_grads(tensors, p)
+    assert g.shape == gw.shape
+    off = 0
+    for w, b in tensors:  # per layer: weights and biases
+        nw, nb = w.numel(), b.numel()
+        live = np.abs(gw[off:off + nw]).sum() > 0
+        if live:
+            assert rel(g[off:off + nw], gw[off:off + nw]) < 6e-2, ("weights", off, rel(g[off:off + nw], gw[off:off + nw]))
+        assert rel(g[off + nw:off + nw + nb], gw[off + nw:off + nw + nb]) < 6e-2 or np.abs(gw[off + nw:off + nw + nb]).sum() == 0
+        off += nw + nb
+    net.close()
+
+
+def test_unet_training_reduces_loss(lib_built):
+    """Adam on a smooth regression (the output a fixed blur of two input channels): the loss falls
+    by an order of magnitude."""
+    B, H, W = 4, 32, 32
+    net = Net(8, 2, 16, 3, B, H, W, seed=3)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((B, H, W, 8)).astype(np.float32)
+    k = np.array([0.25, 0.5, 0.25], np.float32)
+    t = x[..., :2].copy()
+    for ax in (1, 2):
+        t = k[0] * np.roll(t, 1, axis=ax) + k[1] * t + k[2] * np.roll(t, -1, axis=ax)
+    losses = [net.train_step(x, t, 3e-3) for _ in range(300)]
+    assert losses[-1] < 0.1 * losses[0], (losses[0], losses[-1])
+    net.close()

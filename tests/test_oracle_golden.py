@@ -64,3 +64,32 @@ def test_oracle_library_matches_cli(oracle_built, golden_records):
         assert list(o.sweeps()) == rec["sweeps"]
         assert sha(o.field("u")) == rec["sha256_u"]
         assert sha(o.field("p")) == rec["sha256_p"]
+
+
+def test_oracle_conservation_sums_definition(oracle_built):
+    """The oracle's conservation sums of a restart state equal the same sums taken with numpy
+    (to rounding: numpy sums in another order)."""
+    import tempfile
+    import numpy as np
+    import ora
+    import sts_cases as sc
+    case = sc.rayleigh_benard_case("rb", 40, 20, Nt=5)
+    rng = np.random.default_rng(3)
+    Ny, Nx = case.restart["u"].shape
+    case.restart["u"] = 0.01 * rng.standard_normal((Ny, Nx))
+    case.restart["v"] = 0.01 * rng.standard_normal((Ny, Nx))
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        o = ora.Oracle(d, fixed_sweeps=False)
+        got = o.conservation()
+        u, v, T, rho = o.field("u"), o.field("v"), o.field("T"), o.field("rho")
+        hx, hy = o.field("hx"), o.field("hy")
+        fluid = case.restart["vol_inf_fb"] == 0
+        A = hy[:, None] * hx[None, :]
+        ue = np.concatenate([u[:, 1:], u[:, -1:]], axis=1)
+        vn = np.concatenate([v[1:, :], v[-1:, :]], axis=0)
+        uc, vc = 0.5 * (u + ue), 0.5 * (v + vn)
+        m = rho * A
+        want = [m, m * uc, m * vc, m * T / (5.0 / 3.0 - 1.0), m * (uc ** 2 + vc ** 2)]
+        want = np.array([x[fluid].sum() for x in want])
+        np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-15)
