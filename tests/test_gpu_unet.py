@@ -138,14 +138,22 @@ def test_unet_forward_and_gradients_match_torch(levels, base, H, W, lib_built):
     (yt * torch.tensor(gy).permute(0, 3, 1, 2)).sum().backward()
     gw = flat_grads(tensors, p)
     assert g.shape == gw.shape
-    off = 0
-    for w, b in tensors:  # per layer: weights and biases
-        nw, nb = w.numel(), b.numel()
-        live = np.abs(gw[off:off + nw]).sum() > 0
-        if live:
-            assert rel(g[off:off + nw], gw[off:off + nw]) < 6e-2, ("weights", off, rel(g[off:off + nw], gw[off:off + nw]))
-        assert rel(g[off + nw:off + nw + nb], gw[off + nw:off + nw + nb]) < 6e-2 or np.abs(gw[off + nw:off + nw + nb]).sum() == 0
-        off += nw + nb
+    # per layer, weights and biases: BF16 activations and gradients differ from the FP32 restatement
+    # by rounding that grows with depth (ReLU decisions at near-zero inputs flip), so the bound is on
+    # the direction (cosine) and a loose relative distance; a wrong layer is far off both
+    off, errs = 0, []
+    for w, b in tensors:
+        for n in (w.numel(), b.numel()):
+            a, r = g[off:off + n], gw[off:off + n]
+            off += n
+            if np.abs(r).sum() == 0:
+                assert np.abs(a).sum() == 0
+                continue
+            cos = float(a @ r / (np.linalg.norm(a) * np.linalg.norm(r)))
+            errs.append((rel(a, r), cos))
+    print("per-layer gradient (rel L2, cosine):", [(round(e, 4), round(c, 5)) for e, c in errs])
+    for e, c in errs:
+        assert e < 0.15 and c > 0.99, (e, c)
     net.close()
 
 
