@@ -68,6 +68,12 @@ typedef struct sts_options {
    *    linear function of 36 features of the cell's neighbourhood in the last four changes,
    *    refitted every step by least squares on the last 6 steps; elsewhere mode 2.  Tracks fronts
    *    that move across cells, which extrapolation in time cannot.
+   * 5: warm_start 4, its start corrected on a window around the moving front (64 x 256 cells, or the
+   *    mesh when smaller, centred on the largest change of p) by a U-Net (3 levels, 16 base
+   *    channels, BF16 tensor-core kernels) that predicts the stencil's error from the last three
+   *    changes and the stencil's prediction; the solver stores every step's window and the
+   *    stencil's error there as a training pair (a ring of 256), sts_warm_net_train trains the
+   *    network on them and sts_warm_net_enable switches the correction on.  Single cases only.
    * The sweeps still iterate to the same tolerance, so the result moves only within it; the
    * sweep count falls.  Meaningful for tolerance-terminated loops (fixed_sweeps = 0). */
   int warm_start;
@@ -208,6 +214,19 @@ typedef struct sts_sweep_fields {
  * reduction words: 10*Nx*Ny doubles + 20 KB) is allocated stream-ordered and freed by the call. */
 int sts_pt_sweeps(const sts_sweep_fields* f, int max_sweeps, int fixed_sweeps, double tol_p, double tol_T,
                   void* stream, int* sweeps_done, double* res_p, double* res_T);
+
+/* warm_start 5: `iters` Adam steps (learning rate lr) of the network on batches of 8 training pairs
+ * drawn from the pairs the solver has stored (the mean squared error of the predicted stencil error
+ * on the window's flagged cells); *loss_out (optional) receives the last batch's loss.  Runs on the
+ * context's stream between steps.  No counterpart in the reference. */
+int sts_warm_net_train(sts_ctx* ctx, int iters, float lr, float* loss_out);
+/* warm_start 5: on = 1 applies the network's correction from the next step on (the training pairs
+ * are stored either way); off by default. */
+int sts_warm_net_enable(sts_ctx* ctx, int on);
+/* warm_start 5: training pairs stored so far, the window's size and the network's parameter count. */
+int sts_warm_net_info(sts_ctx* ctx, int* pairs, int* win_h, int* win_w, long long* nparams);
+/* warm_start 5: the network's FP32 parameters (layout of sts_net_get_params) out and/or in (NULL to skip). */
+int sts_warm_net_params(sts_ctx* ctx, float* out, const float* in);
 
 /* Largest mesh (Nx*Ny cells) that sts_pt_sweeps_noalloc accepts. */
 #define STS_NOALLOC_MAX_CELLS 32768

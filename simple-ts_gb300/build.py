@@ -23,6 +23,7 @@ UNITS = [
     ("sts_learn.cu", ["--fmad=false"]),
     ("sts_net.cu", []),
     ("sts_unet.cu", []),
+    ("sts_warmnet.cu", []),
     ("sts_runtime.cu", []),
     ("sts_host.cpp", []),
     ("sts_checkpoint.cpp", []),

@@ -21,6 +21,8 @@
 #include "sts_common.cuh"
 #include "sts_host.h"
 #include "sts_kernels.h"
+#include "sts_unet.h"
+#include "sts_warmnet.h"
 #include "../../include/sts_gb300.h"
 
 using namespace sts;
@@ -88,6 +90,18 @@ struct sts_ctx {
   bool cd_fresh = true, pu_fresh = true;
   // checkpoint dumps (made at the first save)
   std::unique_ptr<Checkpointer> saver;
+  // warm_start 5: the network's correction of the stencil's start (sts_warmnet.cu); the device
+  // runs warm_start 4 and these kernels follow the stencil's
+  bool warm_net = false;
+  std::unique_ptr<UNet> net;
+  NetState* d_ns = nullptr;
+  NetBuffers nb{};
+  int net_slots = 0;
+  static constexpr int kNetBatch = 8, kNetBase = 16, kNetLevels = 3;
+  float *d_bx = nullptr, *d_bt = nullptr, *d_bw = nullptr, *d_loss = nullptr;
+  int* d_bslots = nullptr;
+  unsigned long long net_rng = 0x9E3779B97F4A7C15ull;
+  cudaStream_t cap = nullptr;  // capture stream of the network's graph nodes
 
   ~sts_ctx() {
     saver.reset();  // writes out pending saves before the buffers and the stream go
@@ -95,6 +109,8 @@ struct sts_ctx {
     if (graph) cudaGraphDestroy(graph);
     for (void* p : allocs) cudaFree(p);
     if (h_ctl) cudaFreeHost(h_ctl);
+    net.reset();
+    if (cap) cudaStreamDestroy(cap);
     if (s) cudaStreamDestroy(s);
   }
 
@@ -161,8 +177,24 @@ struct sts_ctx {
     k_conv_solve<<<2, kConvSolveThreads, 0, s>>>(g);
     k_conv_next<<<grid, block, 0, s>>>(g);
     k_conv_predict<<<grid, block, 0, s>>>(g);
+    if (warm_net) net_tail(s);
     mark(0);
   }
+  // warm_start 5: the network's kernels after the stencil's, on stream `st` (the context's stream,
+  // or a stream that captures them into the step graph)
+  void net_tail(cudaStream_t st) {
+    const int px = nb.H * nb.W, b = (px + 255) / 256;
+    k_net_target<<<b, 256, 0, st>>>(g, d_ns, nb);
+    k_net_head<<<1, 1, 0, st>>>(g, d_ns, net_slots);
+    k_net_locate<<<dim3((g.Nx + 255) / 256, g.Ny), 256, 0, st>>>(g, d_ns);
+    k_net_gather<<<b, 256, 0, st>>>(g, d_ns, nb);
+    k_net_commit<<<1, 1, 0, st>>>(g, d_ns, nb);
+    net->set_stream(st);
+    net->forward(nb.infer_in, 1, nb.infer_out);
+    net->set_stream(s);
+    k_net_apply<<<b, 256, 0, st>>>(g, d_ns, nb);
+  }
+  int net_setup(unsigned long long seed);
   bool fast() const { return g.precision >= 1; }
   bool mixed() const { return g.precision >= 2 && !(hc.bits & F_FIXED_SWEEPS); }
   // launch shapes (neither changes any result: every cell is computed on its own and the residual
@@ -313,6 +345,12 @@ int sts_ctx::build_graph() {
     if (int r = add_kernel(&w[1], b_outer, {w[0]}, k_conv_solve, dim3(2), dim3(kConvSolveThreads), g)) return r;
     if (int r = add_kernel(&w[2], b_outer, {w[0]}, k_conv_next, grid, block, g)) return r;
     if (int r = add_kernel(&w[3], b_outer, {w[1], w[2]}, k_conv_predict, grid, block, g)) return r;
+    if (warm_net) {  // the network's kernels, captured into the body after the stencil's
+      CU(cudaStreamBeginCaptureToGraph(cap, b_outer, &w[3], nullptr, 1, cudaStreamCaptureModeRelaxed));
+      net_tail(cap);
+      cudaGraph_t captured = nullptr;
+      CU(cudaStreamEndCapture(cap, &captured));
+    }
   }
   if (int r = add_kernel(&n_rho, b_outer, {n_cor}, k_face_rho, grid, block, g)) return r;
   cudaGraphNode_t n_walls, n_tj;
@@ -706,6 +744,34 @@ int sts_ctx::write_logs(bool iterations) {
   return STS_OK;
 }
 
+// warm_start 5: the window (64 x 256 cells, or the mesh rounded down to multiples of 4 when it is
+// smaller), a U-Net of 3 levels and 16 base channels over it, a replay ring of 256 windows and
+// the training batch buffers; one forward on the context's stream before any graph is built.
+int sts_ctx::net_setup(unsigned long long seed) {
+  nb.H = std::min(64, g.Ny / 4 * 4);
+  nb.W = std::min(256, g.Nx / 4 * 4);
+  if (nb.H < 4 || nb.W < 4) return fail(STS_ERR_ARG, "warm_start 5 needs a mesh of at least 4 x 4 cells");
+  const size_t px = (size_t)nb.H * nb.W;
+  net_slots = 256;
+  nb.slot_floats = px * (kNetIn + kNetOut + 1 + kNetOut);
+  if (int r = alloc(&nb.replay, nb.slot_floats * net_slots)) return r;
+  if (int r = alloc(&nb.infer_in, px * kNetIn)) return r;
+  if (int r = alloc(&nb.infer_w, px)) return r;
+  if (int r = alloc(&nb.infer_out, px * kNetOut)) return r;
+  if (int r = alloc(&d_ns, 1)) return r;
+  if (int r = alloc(&d_bx, px * kNetBatch * kNetIn)) return r;
+  if (int r = alloc(&d_bt, px * kNetBatch * kNetOut)) return r;
+  if (int r = alloc(&d_bw, px * kNetBatch)) return r;
+  if (int r = alloc(&d_loss, 1)) return r;
+  if (int r = alloc(&d_bslots, kNetBatch)) return r;
+  CU(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  net.reset(new UNet(kNetIn, kNetOut, kNetBase, kNetLevels, kNetBatch, nb.H, nb.W, seed, s));
+  if (!net->ok()) return fail(STS_ERR_CUDA, std::string("network set-up: ") + net->error());
+  CU(net->forward(nb.infer_in, 1, nb.infer_out));
+  CU(cudaStreamSynchronize(s));
+  return STS_OK;
+}
+
 namespace {
 
 // Scratch of one sweep-loop call: the second p and T buffers, the 8 sweep invariants and the
@@ -804,7 +870,7 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
   c->t0 = std::chrono::steady_clock::now();
   std::string err;
   if (opt.precision < 0 || opt.precision > 3) return fail(STS_ERR_ARG, "precision must be 0, 1, 2 or 3");
-  if (opt.warm_start < 0 || opt.warm_start > 4) return fail(STS_ERR_ARG, "warm_start must be 0, 1, 2, 3 or 4");
+  if (opt.warm_start < 0 || opt.warm_start > 5) return fail(STS_ERR_ARG, "warm_start must be 0, 1, 2, 3, 4 or 5");
   if (!load_case(dir, opt.fixed_sweeps != 0, c->hc, err)) return fail(STS_ERR_INPUT, err);
   Case& h = c->hc;
   int ndev = 0;
@@ -947,7 +1013,9 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
     g.rht = 1.0 / g.ht;
     g.r3 = 1.0 / 3.0;
   }
-  g.warm_start = opt.warm_start;
+  // warm_start 5 is warm_start 4 on the device plus the network's kernels
+  g.warm_start = opt.warm_start == 5 ? 4 : opt.warm_start;
+  c->warm_net = opt.warm_start == 5;
   if (g.warm_start)
     for (int k = 0; k < 2; k++) {
       if (int r = c->alloc(&g.p_m[k], Na)) return r;
@@ -982,6 +1050,8 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
   }
   if (int r = c->alloc(&c->d_ctl, 1)) return r;
   g.ctl = c->d_ctl;
+  if (c->warm_net)
+    if (int r = c->net_setup(0x5EED0005ull)) return r;
   if (int r = c->upload(g.u, h.u)) return r;
   if (int r = c->upload(g.v, h.v)) return r;
   if (int r = c->upload(g.p[0], h.p)) return r;
@@ -1508,6 +1578,76 @@ int sts_conservation(sts_ctx* ctx, double* out5) {
   return STS_OK;
 }
 
+int sts_warm_net_train(sts_ctx* ctx, int iters, float lr, float* loss_out) {
+  if (!ctx || iters < 0) return fail(STS_ERR_ARG, "bad argument");
+  if (!ctx->warm_net) return fail(STS_ERR_ARG, "the context does not use warm_start 5");
+  CU(cudaSetDevice(ctx->opt.device));
+  NetState h{};
+  CU(cudaMemcpyAsync(&h, ctx->d_ns, sizeof(NetState), cudaMemcpyDeviceToHost, ctx->s));
+  CU(cudaStreamSynchronize(ctx->s));
+  // completed pairs: slots 0 .. count-1, or the whole ring but the slot being filled
+  const int B = sts_ctx::kNetBatch, S = ctx->net_slots;
+  const int n = (int)std::min<unsigned>(h.count, (unsigned)S);
+  if (n < 1) return fail(STS_ERR_ARG, "no training pairs yet: step the case first");
+  const int pending = h.have_win ? h.slot : -1;
+  const int px = ctx->nb.H * ctx->nb.W;
+  float loss = 0.f;
+  for (int it = 0; it < iters; it++) {
+    int slots[sts_ctx::kNetBatch];
+    for (int b = 0; b < B; b++) {
+      int q;
+      do {
+        ctx->net_rng = ctx->net_rng * 6364136223846793005ull + 1442695040888963407ull;
+        q = (int)((ctx->net_rng >> 33) % (unsigned long long)n);
+      } while (n > 1 && q == pending && h.count >= (unsigned)S);
+      slots[b] = q;
+    }
+    CU(cudaMemcpyAsync(ctx->d_bslots, slots, sizeof(slots), cudaMemcpyHostToDevice, ctx->s));
+    k_net_batch<<<std::max(1, std::min((B * px + 255) / 256, 4096)), 256, 0, ctx->s>>>(ctx->nb, ctx->d_bslots, B,
+                                                                                     ctx->d_bx, ctx->d_bt, ctx->d_bw);
+    CU(ctx->net->forward(ctx->d_bx, B, nullptr));
+    CU(ctx->net->backward_mse(ctx->d_bt, ctx->d_bw, B, ctx->d_loss));
+    CU(ctx->net->adam(lr));
+    if (it + 1 == iters) CU(cudaMemcpyAsync(&loss, ctx->d_loss, sizeof(float), cudaMemcpyDeviceToHost, ctx->s));
+    CU(cudaStreamSynchronize(ctx->s));  // the slot list on the host stack is reused
+  }
+  unsigned e = 0;
+  CU(cudaMemcpy(&e, ctx->net->error_flag(), sizeof(unsigned), cudaMemcpyDeviceToHost));
+  if (e) return fail(STS_ERR_TIMEOUT, "a tensor-core GEMM pipeline wait gave up");
+  if (loss_out) *loss_out = loss;
+  return STS_OK;
+}
+
+int sts_warm_net_enable(sts_ctx* ctx, int on) {
+  if (!ctx || !ctx->warm_net) return fail(STS_ERR_ARG, "the context does not use warm_start 5");
+  CU(cudaSetDevice(ctx->opt.device));
+  const unsigned v = on ? 1u : 0u;
+  CU(cudaMemcpyAsync(&ctx->d_ns->enabled, &v, sizeof(unsigned), cudaMemcpyHostToDevice, ctx->s));
+  CU(cudaStreamSynchronize(ctx->s));
+  return STS_OK;
+}
+
+int sts_warm_net_info(sts_ctx* ctx, int* pairs, int* win_h, int* win_w, long long* nparams) {
+  if (!ctx || !ctx->warm_net) return fail(STS_ERR_ARG, "the context does not use warm_start 5");
+  CU(cudaSetDevice(ctx->opt.device));
+  NetState h{};
+  CU(cudaMemcpyAsync(&h, ctx->d_ns, sizeof(NetState), cudaMemcpyDeviceToHost, ctx->s));
+  CU(cudaStreamSynchronize(ctx->s));
+  if (pairs) *pairs = (int)h.count;
+  if (win_h) *win_h = ctx->nb.H;
+  if (win_w) *win_w = ctx->nb.W;
+  if (nparams) *nparams = ctx->net->param_count();
+  return STS_OK;
+}
+
+int sts_warm_net_params(sts_ctx* ctx, float* out, const float* in) {
+  if (!ctx || !ctx->warm_net) return fail(STS_ERR_ARG, "the context does not use warm_start 5");
+  CU(cudaSetDevice(ctx->opt.device));
+  if (out) CU(ctx->net->get_params(out));
+  if (in) CU(ctx->net->set_params(in));
+  return STS_OK;
+}
+
 int sts_sync(sts_ctx* ctx) {
   if (!ctx) return fail(STS_ERR_ARG, "null context");
   CU(cudaStreamSynchronize(ctx->s));
@@ -1880,6 +2020,7 @@ int sts_batch::build_graph() {
 extern "C" {
 
 int sts_open_batch(const char* const* case_dirs, int ncases, const sts_options* opt_in, sts_batch** out) {
+  if (opt_in && opt_in->warm_start == 5) return fail(STS_ERR_ARG, "warm_start 5 is not available in batches");
   g_err.clear();
   if (out) *out = nullptr;
   if (!case_dirs || !out || ncases < 1) return fail(STS_ERR_ARG, "bad argument");

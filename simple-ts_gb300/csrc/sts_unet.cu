@@ -433,6 +433,7 @@ const char* UNet::error() const { return d->err.c_str(); }
 long long UNet::param_count() const { return d->nparams; }
 const float* UNet::grads() const { return d->grads; }
 unsigned* UNet::error_flag() const { return d->errw; }
+void UNet::set_stream(cudaStream_t s) { d->s = s; }
 
 cudaError_t UNet::get_params(float* host) const {
   cudaError_t r = cudaMemcpyAsync(host, d->params, sizeof(float) * d->nparams, cudaMemcpyDeviceToHost, d->s);

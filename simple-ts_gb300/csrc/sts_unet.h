@@ -37,6 +37,7 @@ class UNet {
   // One Adam step with learning rate lr on the current gradients.
   cudaError_t adam(float lr);
   unsigned* error_flag() const;  // device word; bit 0: a GEMM pipeline wait gave up
+  void set_stream(cudaStream_t s);  // the stream later calls queue their work on
 
  private:
   std::unique_ptr<UNetImpl> d;

@@ -183,6 +183,38 @@ class Solver:
         _check(load().sts_stats(self._h, _dptr(out)))
         return out
 
+    def warm_net_train(self, iters: int, lr: float = 1e-3) -> float:
+        """warm_start 5: Adam steps of the network on the stored training pairs; the last loss."""
+        lib = load()
+        lib.sts_warm_net_train.argtypes = [C.c_void_p, C.c_int, C.c_float, C.POINTER(C.c_float)]
+        loss = C.c_float()
+        _check(lib.sts_warm_net_train(self._h, int(iters), float(lr), C.byref(loss)))
+        return loss.value
+
+    def warm_net_enable(self, on: bool = True):
+        _check(load().sts_warm_net_enable(self._h, int(on)))
+
+    def warm_net_info(self) -> dict:
+        lib = load()
+        lib.sts_warm_net_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                          C.POINTER(C.c_longlong)]
+        v = [C.c_int(), C.c_int(), C.c_int()]
+        n = C.c_longlong()
+        _check(lib.sts_warm_net_info(self._h, *[C.byref(x) for x in v], C.byref(n)))
+        return {"pairs": v[0].value, "window": (v[1].value, v[2].value), "params": n.value}
+
+    def warm_net_params(self, new=None) -> np.ndarray:
+        """The network's FP32 parameters; with `new`, sets them (returning the old ones)."""
+        lib = load()
+        lib.sts_warm_net_params.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        out = np.zeros(self.warm_net_info()["params"], np.float32)
+        src = None
+        if new is not None:
+            src = np.ascontiguousarray(new, np.float32)
+            assert src.size == out.size
+        _check(lib.sts_warm_net_params(self._h, out.ctypes.data, None if src is None else src.ctypes.data))
+        return out
+
     def conservation(self) -> np.ndarray:
         """[mass, x momentum, y momentum, internal energy, kinetic energy] sums of the current state
         over the fluid cells (FP64, fixed order, on the device)."""
