@@ -220,6 +220,9 @@ int sts_pt_sweeps(const sts_sweep_fields* f, int max_sweeps, int fixed_sweeps, d
  * on the window's flagged cells); *loss_out (optional) receives the last batch's loss.  Runs on the
  * context's stream between steps.  No counterpart in the reference. */
 int sts_warm_net_train(sts_ctx* ctx, int iters, float lr, float* loss_out);
+/* warm_start 5: the network's mean loss over every stored training pair, and the loss of a zero
+ * correction (the stencil alone) on the same pairs. */
+int sts_warm_net_eval(sts_ctx* ctx, float* loss_net, float* loss_zero);
 /* warm_start 5: on = 1 applies the network's correction from the next step on (the training pairs
  * are stored either way); off by default. */
 int sts_warm_net_enable(sts_ctx* ctx, int on);

@@ -2,7 +2,7 @@
 //
 // D[M x N] = epilogue(A[M x K] * B[N x K]^T): A and B row-major BF16 with K contiguous (both
 // operands K-major), FP32 accumulation in tensor memory.  One CTA of 128 threads per 128 x BN tile
-// of D: warp 0 (one thread) streams 128 x 64 tiles of A and BN x 64 tiles of B into a 4-stage
+// of D: warp 0 (one thread) streams 128 x 64 tiles of A and BN x 64 tiles of B into a 3- or 4-stage
 // shared-memory ring with TMA (128-byte swizzle, zero fill past the edges); warp 1 (one thread)
 // issues four 128 x BN x 16 tcgen05 MMAs per stage and releases the stage with tcgen05.commit;
 // then all four warps read the accumulator rows of their tensor-memory lanes (warp w holds rows
@@ -23,20 +23,24 @@
 namespace sts {
 namespace {
 
-constexpr int kBM = 128, kBK = 64, kStages = 4;
+constexpr int kBM = 128, kBK = 64;
 constexpr uint32_t kWaitLimit = 1u << 22;  // polls of a pipeline barrier before the CTA gives up
 
+// Pipeline depth: 4 stages for 256-wide tiles (one CTA per SM), 3 for narrower ones so that two or
+// three CTAs fit on an SM and one's epilogue overlaps another's main loop.
 template <int BN>
 struct GemmSmem {
+  static constexpr int kStages = BN >= 256 ? 4 : 3;
   static constexpr uint32_t kA = kBM * kBK * 2, kB = BN * kBK * 2;
   static constexpr uint32_t kBytes = kStages * (kA + kB) + 1024 + 256;
 };
 
 template <int BN>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(128)
     k_gemm_tn(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, int M, int N, int K,
               GemmEpilogue e, unsigned* err) {
   using L = GemmSmem<BN>;
+  constexpr int kStages = L::kStages;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* sa = smem;

@@ -1618,6 +1618,45 @@ int sts_warm_net_train(sts_ctx* ctx, int iters, float lr, float* loss_out) {
   return STS_OK;
 }
 
+int sts_warm_net_eval(sts_ctx* ctx, float* loss_net, float* loss_zero) {
+  if (!ctx || !ctx->warm_net) return fail(STS_ERR_ARG, "the context does not use warm_start 5");
+  CU(cudaSetDevice(ctx->opt.device));
+  NetState h{};
+  CU(cudaMemcpyAsync(&h, ctx->d_ns, sizeof(NetState), cudaMemcpyDeviceToHost, ctx->s));
+  CU(cudaStreamSynchronize(ctx->s));
+  const int B = sts_ctx::kNetBatch, S = ctx->net_slots;
+  const int n = (int)std::min<unsigned>(h.count, (unsigned)S);
+  const int pending = (h.have_win && h.count >= (unsigned)S) ? h.slot : -1;
+  const int px = ctx->nb.H * ctx->nb.W;
+  double sn = 0, sz = 0;
+  int batches = 0;
+  for (int q0 = 0; q0 < n; q0 += B) {
+    int slots[sts_ctx::kNetBatch];
+    int m = 0;
+    for (int q = q0; q < n && m < B; q++)
+      if (q != pending) slots[m++] = q;
+    if (m == 0) continue;
+    for (int b = m; b < B; b++) slots[b] = slots[b % m];  // a short last batch repeats its pairs
+    CU(cudaMemcpyAsync(ctx->d_bslots, slots, sizeof(slots), cudaMemcpyHostToDevice, ctx->s));
+    k_net_batch<<<std::max(1, std::min((B * px + 255) / 256, 4096)), 256, 0, ctx->s>>>(ctx->nb, ctx->d_bslots, B,
+                                                                                     ctx->d_bx, ctx->d_bt, ctx->d_bw);
+    float l[2] = {0.f, 0.f};
+    CU(ctx->net->forward(ctx->d_bx, B, nullptr));
+    CU(ctx->net->loss(ctx->d_bt, ctx->d_bw, B, ctx->d_loss, false));
+    CU(cudaMemcpyAsync(&l[0], ctx->d_loss, sizeof(float), cudaMemcpyDeviceToHost, ctx->s));
+    CU(ctx->net->loss(ctx->d_bt, ctx->d_bw, B, ctx->d_loss, true));
+    CU(cudaMemcpyAsync(&l[1], ctx->d_loss, sizeof(float), cudaMemcpyDeviceToHost, ctx->s));
+    CU(cudaStreamSynchronize(ctx->s));
+    sn += l[0];
+    sz += l[1];
+    batches++;
+  }
+  if (!batches) return fail(STS_ERR_ARG, "no training pairs yet: step the case first");
+  if (loss_net) *loss_net = (float)(sn / batches);
+  if (loss_zero) *loss_zero = (float)(sz / batches);
+  return STS_OK;
+}
+
 int sts_warm_net_enable(sts_ctx* ctx, int on) {
   if (!ctx || !ctx->warm_net) return fail(STS_ERR_ARG, "the context does not use warm_start 5");
   CU(cudaSetDevice(ctx->opt.device));

@@ -494,6 +494,16 @@ cudaError_t UNet::backward_mse(const float* target, const float* weight, int B, 
   return backward(nullptr, B);
 }
 
+cudaError_t UNet::loss(const float* target, const float* weight, int B, float* loss_dev, bool zero_prediction) {
+  UNetImpl& u = *d;
+  const long long P0 = u.P(0, B);
+  if (zero_prediction) cudaMemsetAsync(u.head_out, 0, sizeof(float) * P0 * 8, u.s);
+  cudaMemsetAsync(loss_dev, 0, sizeof(float), u.s);
+  k_mse<<<grid_for(P0 * 8), 256, 0, u.s>>>(u.head_out, 8, target, weight, u.g_head, P0, u.out_ch,
+                                           1.0f / (float)(P0 * u.out_ch), loss_dev);
+  return cudaGetLastError();
+}
+
 cudaError_t UNet::backward(const float* gy, int B) {
   UNetImpl& u = *d;
   if (!ok() || B < 1 || B > u.maxB) return cudaErrorInvalidValue;

@@ -31,6 +31,9 @@ class UNet {
   // After forward: the loss against target [B][H][W][out_ch] with per-pixel weights (NULL: 1),
   // backward into the gradient buffer (*loss_dev receives the loss, device FP32).
   cudaError_t backward_mse(const float* target, const float* weight, int B, float* loss_dev);
+  // After forward: only the loss (as backward_mse computes it), of the forward's output or, with
+  // zero_prediction, of an output of zeros (the forward's output is then overwritten).
+  cudaError_t loss(const float* target, const float* weight, int B, float* loss_dev, bool zero_prediction);
   // Backward from a given output gradient gy [B][H][W][out_ch] (device FP32).
   cudaError_t backward(const float* gy, int B);
   const float* grads() const;  // device, param_count() values in the layout of get_params

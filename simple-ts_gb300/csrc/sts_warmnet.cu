@@ -38,13 +38,17 @@ __global__ void k_net_target(Geo g, NetState* ns, NetBuffers nb) {
   if (k < H * W) {
     const int i = ns->i0 + k % W, j = ns->j0 + k / W, n = i + j * g.Nx;
     float* tgt = nb.replay + (size_t)ns->slot * nb.slot_floats + (size_t)H * W * kNetIn;
-    const float w = tgt[(size_t)H * W * kNetOut + k];
+    float* wp = tgt + (size_t)H * W * kNetOut + k;
     const float* S = tgt + (size_t)H * W * (kNetOut + 1);
+    bool outlier = false;
     for (int f = 0; f < kNetOut; f++) {
-      const float err = w > 0.f ? g.cD[f][r % kConvRing][n] - S[(size_t)k * kNetOut + f] : 0.f;
-      tgt[(size_t)k * kNetOut + f] = err / ns->s[f];
+      const float err = *wp > 0.f ? g.cD[f][r % kConvRing][n] - S[(size_t)k * kNetOut + f] : 0.f;
+      const float t = err / ns->s[f];
+      outlier = outlier || !(fabsf(t) <= kNetTargetClip);
+      tgt[(size_t)k * kNetOut + f] = fminf(fmaxf(t, -kNetTargetClip), kNetTargetClip);
       e[f] = fabsf(err);
     }
+    if (outlier) *wp = 0.f;  // a pixel far outside the window's scale is left out of training
   }
   for (int f = 0; f < kNetOut; f++) {
     unsigned v = __float_as_uint(e[f]);
@@ -55,7 +59,8 @@ __global__ void k_net_target(Geo g, NetState* ns, NetBuffers nb) {
 
 // One thread: the pending window's pair is complete; the coming window takes the next slot, its
 // inputs are scaled by the step change's maximum and its target by the stencil's largest error on
-// the completed window (never below 1e-6 of the change).
+// the completed window (never below kNetScaleFloor of the change, so that the windows before the
+// stencil acts do not get a vanishing scale).
 __global__ void k_net_head(Geo g, NetState* ns, int slots) {
   const unsigned r = g.ctl->warm_ready;
   if (ns->have_win) ns->count++;
@@ -63,7 +68,7 @@ __global__ void k_net_head(Geo g, NetState* ns, int slots) {
     const float m = __uint_as_float(g.ctl->conv_max[r & 1][f]);
     ns->m[f] = m > 0.f ? m : 1.f;
     const float e = ns->have_win ? __uint_as_float(ns->err_bits[f]) : 0.f;
-    ns->s[f] = fmaxf(e, 1e-6f * ns->m[f]);
+    ns->s[f] = fmaxf(e, kNetScaleFloor * ns->m[f]);
     ns->err_bits[f] = 0u;
   }
   ns->argmax = 0xffffffffu;
@@ -133,7 +138,10 @@ __global__ void k_net_apply(Geo g, NetState* ns, NetBuffers nb) {
   const int i = ns->i0 + k % W, j = ns->j0 + k / W, n = i + j * g.Nx;
   const uint8_t b = g.cact[r & 1][n];
   for (int f = 0; f < kNetOut; f++)
-    if ((b >> (2 + f)) & 1u) g.cnext[f][n] += (double)(ns->s[f] * nb.infer_out[(size_t)k * kNetOut + f]);
+    if ((b >> (2 + f)) & 1u) {
+      const float o = fminf(fmaxf(nb.infer_out[(size_t)k * kNetOut + f], -kNetTargetClip), kNetTargetClip);
+      g.cnext[f][n] += (double)(ns->s[f] * o);
+    }
 }
 
 // Training batch: the listed slots' inputs, targets and weights side by side.

@@ -5,6 +5,8 @@
 namespace sts {
 
 constexpr int kNetIn = 8, kNetOut = 2;
+constexpr float kNetScaleFloor = 1e-4f;  // smallest target scale, relative to the step change's maximum
+constexpr float kNetTargetClip = 8.f;    // targets (and outputs) beyond this many scales are clipped
 
 // Device-side bookkeeping of the window and the replay ring.
 struct NetState {

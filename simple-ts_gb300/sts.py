@@ -191,6 +191,14 @@ class Solver:
         _check(lib.sts_warm_net_train(self._h, int(iters), float(lr), C.byref(loss)))
         return loss.value
 
+    def warm_net_eval(self):
+        """(network loss, zero-correction loss) over every stored training pair."""
+        lib = load()
+        lib.sts_warm_net_eval.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        a, b = C.c_float(), C.c_float()
+        _check(lib.sts_warm_net_eval(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def warm_net_enable(self, on: bool = True):
         _check(load().sts_warm_net_enable(self._h, int(on)))
 
