@@ -76,6 +76,8 @@ def parse():
                     help="timed steps per path of the 2048x256 metric-configuration runs (0: skip them)")
     ap.add_argument("--c5-lead", type=int, default=30,
                     help="untimed steps before the timed ones for the warm-started paths of those runs")
+    ap.add_argument("--no-network", dest="network", action="store_false",
+                    help="skip the network warm start (warm_start 5) runs")
     ap.add_argument("--no-variants", dest="variants", action="store_false",
                     help="skip the FP64-fast and FP32-correction runs of the same workload")
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2, 3],
@@ -526,6 +528,34 @@ def checkpoint_bench(d, local, barrier, every=10, saves=10):
             "save_cost_hidden": round(1.0 - cost_async / cost_sync, 3) if cost_sync > 0 else None}
 
 
+def network_run(d, local, steps, flush, barrier, lead=60, train_iters=300, lr=3e-4, warmup=10):
+    """warm_start 5 on FP32 corrections with double-float FP64 parts: `lead` steps that store the
+    network's training pairs (the stencil's start is used unchanged meanwhile), `train_iters` Adam
+    steps of the U-Net on the GPU, the correction switched on, `warmup` more steps, then `steps`
+    timed steps (device time, L2 flushed before each).  Returns the path's numbers and the training
+    losses (network against a zero correction, on the stored pairs)."""
+    import numpy as np
+    import sts
+    v = sts.Solver(d, fixed_sweeps=False, device=local, precision=sts.MIXED_DF, warm_start=5)
+    v.step(lead)
+    t0 = time.perf_counter()
+    v.warm_net_train(train_iters, lr)
+    train_s = time.perf_counter() - t0
+    loss_net, loss_zero = v.warm_net_eval()
+    v.warm_net_enable(True)
+    vd, vms, vsw = timed_steps(v, steps, warmup, flush, barrier)
+    info = v.warm_net_info()
+    out = {"value": v.Nx * v.Ny * vd / (vms / 1e3), "ms_per_step": vms / max(vd, 1),
+           "sweeps_per_step": float(np.mean(vsw)) if len(vsw) else 0.0,
+           "untimed_steps": lead + v.steps_before_timing, "training": {
+               "pairs": min(info["pairs"], 256), "window": info["window"], "params": info["params"],
+               "iters": train_iters, "seconds": round(train_s, 3), "loss_network": loss_net,
+               "loss_zero_correction": loss_zero}}
+    fields = {f: v.field(f) for f in ("u", "v", "p", "T", "rho")}
+    v.close()
+    return out, fields
+
+
 # The metric's own configuration: the 2048x256 channel with the square at four Mach numbers
 # (Kn 0.003, dt 1.25e-4, tolerance 1e-8); each path from the same initial state
 C5_MACHS = (0.1, 0.5, 1.0, 2.43)
@@ -572,6 +602,11 @@ def metric_config_bench(args, local, flush, barrier):
                          "max_rel_l2_vs_plain": err, "untimed_steps": v.steps_before_timing}
             cells = v.Nx * v.Ny
             v.close()
+        if args.network:
+            nr, nf = network_run(d, local, args.c5_steps, flush, barrier, lead=args.c5_lead + 30)
+            ref = base_at(nr["untimed_steps"] + args.c5_steps)
+            nr["max_rel_l2_vs_plain"] = max(float(np.linalg.norm(nf[f] - ref[f]) / np.linalg.norm(ref[f])) for f in ref)
+            row["fp32df_network"] = nr
         plain, learned = row["plain_fp64"], row["fp32df_learned"]
 
         def gain(a, b):
@@ -582,6 +617,8 @@ def metric_config_bench(args, local, flush, barrier):
                             "learned_vs_same_precision_cold": gain("fp32df_learned", "fp32df_cold"),
                             "learned_vs_quadratic": gain("fp32df_learned", "fp32df_quadratic"),
                             "fp64_learned_vs_plain": gain("fp64_learned", "plain_fp64")}
+        if "fp32df_network" in row:
+            out[f"ma{mach}"]["network_vs_stencil"] = gain("fp32df_network", "fp32df_learned")
     return {"workload": "channel 2048x256 with the square, Kn 0.003, dt 1.25e-4, tolerance 1e-8",
             "timed_steps": args.c5_steps, "untimed_steps_warm": args.c5_lead, "by_mach": out}
 
@@ -601,7 +638,7 @@ def warm_summary(plain_value, plain_sweeps, variants):
                 "speedup": v["value"] / plain_value, "sweep_ratio": ps / max(v["sweeps_per_step"], 1e-30)}
 
     out = {"plain_gpu_jacobi": {"path": "FP64 bit-exact, cold start", "value": plain_value, "sweeps_per_step": ps}}
-    learned = [k for k in warm if warm[k]["warm_start"] in (3, 4)]
+    learned = [k for k in warm if warm[k]["warm_start"] in (3, 4, 5)]
     if learned:
         out["learned"] = entry(max(learned, key=lambda k: warm[k]["value"]))
     out["fastest"] = entry(max(warm, key=lambda k: warm[k]["value"]))
@@ -724,6 +761,14 @@ def main():
                 "gpu_launches": int(round(launches_per_step(vkcnt, vpn) * vd)),
                 "kernel_ms_per_step": {k: round(x / max(vpn, 1), 5) for k, x in vkms.items() if x > 0}}
             v.close()
+
+        if args.network:
+            nr, nf = network_run(d, local, args.steps, flush, barrier)
+            ref_f = base_at(nr["untimed_steps"] + args.steps)
+            nr["rel_l2_vs_fp64"] = {f: float(np.linalg.norm(nf[f] - ref_f[f]) / np.linalg.norm(ref_f[f])) for f in ref_f}
+            nr["precision_mode"], nr["warm_start"] = 3, 5
+            nr["speedup_vs_fp64"] = nr["value"] / value
+            variants["fp32_corrections_df_network"] = nr
 
     full = args.variants and args.variant_set == "all"
     ckpt = checkpoint_bench(d, local, barrier) if full else None
