@@ -215,6 +215,17 @@ typedef struct sts_sweep_fields {
 int sts_pt_sweeps(const sts_sweep_fields* f, int max_sweeps, int fixed_sweeps, double tol_p, double tol_T,
                   void* stream, int* sweeps_done, double* res_p, double* res_T);
 
+/* Sweeps per tile load of the FP32 correction sweeps (precision 2 and 3, tolerance-terminated loops,
+ * single cases): k = 2 runs two sweeps per round of the persistent loop -- each CTA loads its tile
+ * of the corrections with a margin of two cells by TMA and sweeps it twice, halving the grid-wide
+ * barriers -- and the loop still stops at the same sweep with the same iterate (the residuals of
+ * both sweeps are kept and the stop rule is applied after each); k = 1 one sweep per round; k = 0
+ * the autotuner's choice (it times both on the run's first steps).  The results are the same bits
+ * either way.  The reference sweeps one sweep at a time (SIMPLE_TS_MPI.cpp:3788-4131). */
+int sts_set_sweep_blocking(sts_ctx* ctx, int k);
+/* The sweeps per tile load in use (1 or 2). */
+int sts_get_sweep_blocking(sts_ctx* ctx, int* k);
+
 /* warm_start 5: `iters` Adam steps (learning rate lr) of the network on batches of 8 training pairs
  * drawn from the pairs the solver has stored (the mean squared error of the predicted stencil error
  * on the window's flagged cells); *loss_out (optional) receives the last batch's loss.  Runs on the

@@ -14,6 +14,8 @@
 #define STS_HD inline
 #endif
 
+#include <cuda.h>  // CUtensorMap
+
 namespace sts {
 
 // Per-cell class byte.
@@ -102,6 +104,8 @@ struct Ctl {
   // persistent sweep loop: per-sweep residual maxima (three slots used in rotation; all zero
   // between launches)
   unsigned long long rb_p[3], rb_T[3];
+  // the second sweep of a temporally blocked FP32 round (two sweeps per round), same rotation
+  unsigned long long rb2_p[3], rb2_T[3];
   unsigned int running;       // the case takes part in the current step (batches; 1 otherwise)
   unsigned int warm_ready;    // steps of history the warm start has
   // mode 3: per step, the normal-equation terms of its newest target (6 Gram entries and 3
@@ -131,6 +135,12 @@ constexpr int kMaxBatchCases = 256;
 // Grid barrier and exit ticket of one persistent sweep-loop launch (one per context or batch).
 struct LoopCtl {
   unsigned int bar_count, bar_gen, status, block_count;
+};
+
+// TMA tensor maps of the three FP32 correction buffers of e_T and e_p (the temporally blocked
+// FP32 sweeps load their tiles with them); a kernel parameter.
+struct alignas(64) EMaps {
+  CUtensorMap eT[3], ep[3];
 };
 
 // Bits of Ctl::status.
@@ -175,9 +185,11 @@ struct Geo {
   // --- precision modes 1 and 2 ---
   // FP32 correction sweeps: coefficients c[0..4] of the T correction, a[0..3] of the p
   // numerator, the base-sweep values T1, H/T1, p1, Den and the defects dT, dp; e_p/e_T are the
-  // double-buffered corrections
+  // corrections in three buffers used in rotation, rows of Nxe floats (Nx rounded up to a multiple
+  // of 4, so that a row starts on a 16-byte boundary for TMA)
   float *c32[5], *a32[4], *T1, *hT, *q1, *den1, *dT, *dp;
-  float *ep[2], *eT[2];
+  float *ep[3], *eT[3];
+  int Nxe;
   int precision;  // 0 bit-exact FP64, 1 FP64 with reciprocal/FMA arithmetic, 2 = 1 + FP32 correction sweeps
   // warm start of the sweeps: 0 none (the reference), 1 linear and 2 quadratic extrapolation in
   // time of p and T on the solved cells, 3 the fitted linear predictor, 4 the fitted 3x3 stencil

@@ -342,14 +342,21 @@ struct LoopCase {
   unsigned cur;   // FP64 buffer with the latest iterate
   unsigned base;  // FP64 buffer with the base of the FP32 corrections
   unsigned I;     // outer iteration (row of the residual records)
-  unsigned char phase, ec, active, pad;  // ec: correction buffer with the latest FP32 iterate
+  unsigned char phase, ec, active, eprev;  // ec: correction buffer with the latest FP32 iterate,
+                                          // eprev: the one with the iterate before it
 };
 
 // SINGLE: one case whose Geo g0 is a kernel parameter (gs, tile_case, tile_first unused).
-template <class Ops, bool SINGLE>
+// TB (single cases of the FP32-correction loop): a round of FP32 sweeps takes two sweeps per tile
+// load (Ops::pass32_pair, tiles staged by TMA through `maps`, shared memory at tb_smem); the round's
+// second residual pair goes to the rb2 slots, and the state advances sweep by sweep from them, so
+// the loop stops at the same sweep with the same iterate as with one sweep per round.
+template <class Ops, bool SINGLE, bool TB = false>
 __device__ __forceinline__ void pt_loop_rounds(const Geo& g0, const Geo* __restrict__ gs,
                                                const int* __restrict__ tile_case, const int* __restrict__ tile_first,
-                                               int ncases, int ntiles, LoopCtl* lc) {
+                                               int ncases, int ntiles, LoopCtl* lc, const EMaps* maps = nullptr,
+                                               void* tb_smem = nullptr) {
+  unsigned tphase = 0;  // parity of the TMA barrier's next completion (TB)
   auto G = [&](int c) -> const Geo& { return SINGLE ? g0 : gs[c]; };
   __shared__ LoopCase sc[kMaxBatchCases];
   __shared__ bool last;
@@ -365,7 +372,7 @@ __device__ __forceinline__ void pt_loop_rounds(const Geo& g0, const Geo* __restr
     s.ec = 0;
     s.active = ctl->running ? 1 : 0;
     s.phase = s.active ? PS_FIRST : PS_DONE;
-    s.pad = 0;
+    s.eprev = 0;
     sc[c] = s;
   }
   __syncthreads();
@@ -418,7 +425,15 @@ __device__ __forceinline__ void pt_loop_rounds(const Geo& g0, const Geo* __restr
         if (s.phase != PS_MATERIALIZE) block_max2_bits(bp, bT, &g0.ctl->rb_p[slot], &g0.ctl->rb_T[slot]);
       }
     }
-    for (int t = by_list ? ntiles : (int)blockIdx.x; t < ntiles; t += gridDim.x) {
+    bool pair_round = false;
+    if constexpr (TB) {
+      if (sc[0].phase == PS_SWEEP32) {  // two FP32 sweeps per tile load
+        pair_round = true;
+        for (int t = (int)blockIdx.x; t < ntiles; t += gridDim.x)
+          if (!Ops::pass32_pair(g0, t, sc[0], maps, tb_smem, tphase, slot)) break;
+      }
+    }
+    for (int t = (by_list || pair_round) ? ntiles : (int)blockIdx.x; t < ntiles; t += gridDim.x) {
       const int c = SINGLE ? 0 : tile_case[t];
       const LoopCase s = sc[c];
       if (s.phase == PS_DONE) continue;  // uniform over the CTA
@@ -439,6 +454,10 @@ __device__ __forceinline__ void pt_loop_rounds(const Geo& g0, const Geo* __restr
       for (int c = tid; c < ncases; c += nthr) {
         G(c).ctl->rb_p[(round + 1) % 3] = 0ull;
         G(c).ctl->rb_T[(round + 1) % 3] = 0ull;
+        if (TB) {
+          G(c).ctl->rb2_p[(round + 1) % 3] = 0ull;
+          G(c).ctl->rb2_T[(round + 1) % 3] = 0ull;
+        }
       }
     if (!grid_barrier(lc)) break;
     int any = 0;
@@ -451,6 +470,8 @@ __device__ __forceinline__ void pt_loop_rounds(const Geo& g0, const Geo* __restr
         res_T = ld_res(&G(c).ctl->rb_T[slot]);
       }
       Ops::advance(G(c), lead, s, res_p, res_T);
+      if (TB && pair_round && s.phase == PS_SWEEP32)  // the round's second sweep
+        Ops::advance(G(c), lead, s, ld_res(&G(c).ctl->rb2_p[slot]), ld_res(&G(c).ctl->rb2_T[slot]));
       sc[c] = s;
       any |= (s.phase != PS_DONE);
     }
@@ -479,6 +500,8 @@ __device__ __forceinline__ void pt_loop_rounds(const Geo& g0, const Geo* __restr
     for (int k = 0; k < 3; k++) {
       ctl->rb_p[k] = 0ull;
       ctl->rb_T[k] = 0ull;
+      ctl->rb2_p[k] = 0ull;
+      ctl->rb2_T[k] = 0ull;
     }
   }
 }

@@ -12,6 +12,7 @@
 #include "sts_device.cuh"
 #include "sts_df.cuh"
 #include "sts_kernels.h"
+#include "sts_tc.cuh"
 
 namespace sts {
 
@@ -362,11 +363,14 @@ __global__ void __launch_bounds__(256, 4) kb_pt_loop_fast(const Geo* gs, const i
 // ---------------------------------------------------------------------------
 constexpr float kFloor32 = 8.0f / 16777216.0f;  // 8 units in the last place of an FP32 number
 
+// Index of cell (i, j) in the FP32 correction buffers (rows of g.Nxe floats).
+__device__ __forceinline__ int eix(const Geo& g, int i, int j) { return i + j * g.Nxe; }
+
 // Base values of the FP32 corrections taken from an FP64 sweep x -> x1 of a solved cell
 // (x, x1 in FP64 or double-float).
 template <class R>
 __device__ __forceinline__ void set_base(const Geo& g, const Cell& c, R T0, R p0, R T1, R p1, R sa) {
-  const int ij = c.ij;
+  const int ij = c.ij, e = eix(g, c.i, c.j);
   // the FP32 sweeps' coefficients are formed in FP32 (they only steer the corrections; the
   // FP64 passes decide the converged iterate), which keeps an FP64 division off this pass
   const float T1f = to_float(T1);
@@ -378,28 +382,145 @@ __device__ __forceinline__ void set_base(const Geo& g, const Cell& c, R T0, R p0
   const float dT = to_float(T1 - T0), dp = to_float(p1 - p0);
   g.dT[ij] = dT;
   g.dp[ij] = dp;
-  g.eT[0][ij] = dT;
-  g.ep[0][ij] = dp;
+  g.eT[0][e] = dT;
+  g.ep[0][e] = dp;
 }
 
-// One FP32 correction sweep of a solved cell: e (buffer src) -> e' (buffer src ^ 1).
-__device__ __forceinline__ void sweep32_cell(const Geo& g, const Cell& c, unsigned src, float& rp, float& rT) {
-  const int ij = c.ij;
-  const Nb d = neighbours(c.i, c.j, g.Nx, g.Ny, g.bits & F_PERIODIC);
-  const float* __restrict__ ep = g.ep[src];
-  const float* __restrict__ eT = g.eT[src];
-  const float dT = g.c32[0][ij] * eT[d.i_1j] + g.c32[1][ij] * eT[d.i1j] + g.c32[2][ij] * eT[d.ij_1] +
-                   g.c32[3][ij] * eT[d.ij1] + g.c32[4][ij] * ep[ij];
-  const float eTnew = g.dT[ij] + dT;
+// One FP32 correction update of solved cell ij from its corrections (centre P and neighbours W, E,
+// S, N of e_T and e_p); both the one-sweep pass and the two-sweep tile pass use it, so their
+// arithmetic is the same expression.
+__device__ __forceinline__ void sweep32_math(const Geo& g, int ij, float TW, float TE, float TS, float TN, float pP,
+                                             float pW, float pE, float pS, float pN, float TP, float& eTnew,
+                                             float& epnew, float& rp, float& rT) {
+  const float dT = g.c32[0][ij] * TW + g.c32[1][ij] * TE + g.c32[2][ij] * TS + g.c32[3][ij] * TN + g.c32[4][ij] * pP;
+  eTnew = g.dT[ij] + dT;
   const float q = g.hT[ij] * dT / (g.T1[ij] + dT);
-  const float num = g.a32[0][ij] * ep[d.i_1j] + g.a32[1][ij] * ep[d.i1j] + g.a32[2][ij] * ep[d.ij_1] +
-                    g.a32[3][ij] * ep[d.ij1];
-  const float epnew = g.dp[ij] + (num + g.q1[ij] * q) / (g.den1[ij] - q);
-  g.eT[src ^ 1][ij] = eTnew;
-  g.ep[src ^ 1][ij] = epnew;
-  const float aT = fabsf(eTnew - eT[ij]), ap = fabsf(epnew - ep[ij]);
+  const float num = g.a32[0][ij] * pW + g.a32[1][ij] * pE + g.a32[2][ij] * pS + g.a32[3][ij] * pN;
+  epnew = g.dp[ij] + (num + g.q1[ij] * q) / (g.den1[ij] - q);
+  const float aT = fabsf(eTnew - TP), ap = fabsf(epnew - pP);
   rT = aT <= kFloor32 * fabsf(eTnew) ? 0.0f : aT;
   rp = ap <= kFloor32 * fabsf(epnew) ? 0.0f : ap;
+}
+
+// One FP32 correction sweep of a solved cell: e (buffer src) -> e' (buffer dst).
+__device__ __forceinline__ void sweep32_cell(const Geo& g, const Cell& c, unsigned src, unsigned dst, float& rp,
+                                             float& rT) {
+  const Nb d = neighbours(c.i, c.j, g.Nx, g.Ny, g.bits & F_PERIODIC);
+  const int jm = c.j > 0 ? c.j - 1 : c.j, jp = c.j < g.Ny - 1 ? c.j + 1 : c.j;
+  const int P = eix(g, c.i, c.j), W = eix(g, d.i_1, c.j), E = eix(g, d.i1, c.j), S = eix(g, c.i, jm),
+            N = eix(g, c.i, jp);
+  const float* __restrict__ ep = g.ep[src];
+  const float* __restrict__ eT = g.eT[src];
+  float eTnew, epnew;
+  sweep32_math(g, c.ij, eT[W], eT[E], eT[S], eT[N], ep[P], ep[W], ep[E], ep[S], ep[N], eT[P], eTnew, epnew, rp, rT);
+  g.eT[dst][P] = eTnew;
+  g.ep[dst][P] = epnew;
+}
+
+__device__ __forceinline__ unsigned next_buf(unsigned b) { return b == 2u ? 0u : b + 1u; }
+
+// Shared memory of the two-sweep tile pass: the corrections of the tile and a margin of two cells
+// (one TMA box of 40 x 12 floats per field, x starting 4 cells left of the tile so that the start
+// is a multiple of 16 bytes), the first sweep's values of the tile and a margin of one cell, and the
+// TMA completion barrier.
+struct Tile2Smem {
+  alignas(128) float E0[2][12][40];
+  float E1[2][10][34];
+  alignas(8) uint64_t bar;
+};
+
+// Two FP32 correction sweeps of the 32x8 tile t in one round (temporal blocking).  The first sweep
+// updates the tile and a margin of one cell in shared memory, the second the tile, each cell with
+// sweep32_math and the neighbours of neighbours() (x wraps on periodic meshes, indices clamp at the
+// mesh edges), so every value is the one the one-sweep passes would compute; the tile's values of
+// both sweeps go to the next two buffers and both sweeps' residual maxima to the round's two slot
+// pairs.  Returns false if the TMA load did not complete in time (status flagged).
+__device__ bool sweep32_pair_tile(const Geo& g, int t, const LoopCase& s, const EMaps* maps, Tile2Smem& sm,
+                                  unsigned& tphase, unsigned slot) {
+  const int tx = (g.Nx + 31) / 32, tyi = t / tx;
+  const int i0 = (t - tyi * tx) * 32, j0 = tyi * 8;
+  const int tid = threadIdx.x + 32 * threadIdx.y;
+  const unsigned src = s.ec, d1 = next_buf(src), d2 = next_buf(d1);
+  const bool per = g.bits & F_PERIODIC;
+  const int Nx = g.Nx, Ny = g.Ny;
+  __syncthreads();  // the previous tile's readers of the shared arrays are done
+  if (tid == 0) {
+    tc::mbar_arrive_expect_tx(&sm.bar, 2u * 12u * 40u * 4u);
+    tc::tma_load_2d(&sm.E0[0][0][0], &maps->eT[src], i0 - 4, j0 - 2, &sm.bar);
+    tc::tma_load_2d(&sm.E0[1][0][0], &maps->ep[src], i0 - 4, j0 - 2, &sm.bar);
+  }
+  const bool got = tc::mbar_wait(&sm.bar, tphase, 1u << 22);
+  tphase ^= 1u;
+  if (!__syncthreads_and(got)) {
+    if (tid == 0) atomicOr(&g.ctl->status, ST_BARRIER_TIMEOUT);
+    return false;
+  }
+  if (per) {  // the margin columns outside [0, Nx) hold the wrapped cells
+    for (int k = tid; k < 12 * 40; k += 256) {
+      const int yy = k / 40, xx = k - yy * 40, i = i0 - 4 + xx, j = j0 - 2 + yy;
+      if ((i < 0 || i >= Nx) && j >= 0 && j < Ny) {
+        const int wi = ((i % Nx) + Nx) % Nx;
+        sm.E0[0][yy][xx] = g.eT[src][eix(g, wi, j)];
+        sm.E0[1][yy][xx] = g.ep[src][eix(g, wi, j)];
+      }
+    }
+    __syncthreads();
+  }
+  unsigned* st = &g.ctl->status;
+  unsigned r1p = 0u, r1T = 0u;  // residual maxima as bit patterns (NaN counts as 0 and is flagged)
+  float r2p = 0.f, r2T = 0.f;
+  // first sweep: the tile and a margin of one cell (cells outside the mesh and unsolved cells keep
+  // their values)
+  for (int k = tid; k < 10 * 34; k += 256) {
+    const int yy = k / 34, xx = k - yy * 34, i = i0 - 1 + xx, j = j0 - 1 + yy;
+    const int cx = xx + 3, cy = yy + 1;  // the cell in E0
+    float vT = sm.E0[0][cy][cx], vp = sm.E0[1][cy][cx];
+    if (j >= 0 && j < Ny && (per || (i >= 0 && i < Nx))) {
+      const int gi = ((i % Nx) + Nx) % Nx, ij = gi + j * Nx;
+      if (cls_o(g.cls[ij])) {
+        const int xw = (per || gi > 0) ? cx - 1 : cx, xe = (per || gi < Nx - 1) ? cx + 1 : cx;
+        const int ys = j > 0 ? cy - 1 : cy, yn = j < Ny - 1 ? cy + 1 : cy;
+        const float(*T)[40] = sm.E0[0];
+        const float(*p)[40] = sm.E0[1];
+        float eTn, epn, rp, rT;
+        sweep32_math(g, ij, T[cy][xw], T[cy][xe], T[ys][cx], T[yn][cx], p[cy][cx], p[cy][xw], p[cy][xe], p[ys][cx],
+                     p[yn][cx], T[cy][cx], eTn, epn, rp, rT);
+        vT = eTn;
+        vp = epn;
+        if (i >= i0 && i < i0 + 32 && i < Nx && j >= j0 && j < j0 + 8) {  // a cell of the tile: value, residual
+          g.eT[d1][eix(g, gi, j)] = eTn;
+          g.ep[d1][eix(g, gi, j)] = epn;
+          r1p = max(r1p, res_bits_f(rp, st));
+          r1T = max(r1T, res_bits_f(rT, st));
+        }
+      }
+    }
+    sm.E1[0][yy][xx] = vT;
+    sm.E1[1][yy][xx] = vp;
+  }
+  __syncthreads();
+  // second sweep: the tile's cells, one per thread
+  {
+    const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+    if (i < Nx && j < Ny) {
+      const int ij = i + j * Nx;
+      if (cls_o(g.cls[ij])) {
+        const int cx = threadIdx.x + 1, cy = threadIdx.y + 1;  // the cell in E1
+        const int xw = (per || i > 0) ? cx - 1 : cx, xe = (per || i < Nx - 1) ? cx + 1 : cx;
+        const int ys = j > 0 ? cy - 1 : cy, yn = j < Ny - 1 ? cy + 1 : cy;
+        const float(*T)[34] = sm.E1[0];
+        const float(*p)[34] = sm.E1[1];
+        float eTn, epn;
+        sweep32_math(g, ij, T[cy][xw], T[cy][xe], T[ys][cx], T[yn][cx], p[cy][cx], p[cy][xw], p[cy][xe], p[ys][cx],
+                     p[yn][cx], T[cy][cx], eTn, epn, r2p, r2T);
+        g.eT[d2][eix(g, i, j)] = eTn;
+        g.ep[d2][eix(g, i, j)] = epn;
+      }
+    }
+  }
+  block_max2_f(__uint_as_float(r1p), __uint_as_float(r1T), &g.ctl->rb_p[slot], &g.ctl->rb_T[slot], st);
+  block_max2_f(r2p, r2T, &g.ctl->rb2_p[slot], &g.ctl->rb2_T[slot], st);
+  return true;
 }
 
 // R: the arithmetic of the FP64 sweeps (FP64, or double-float in precision mode 3).
@@ -416,7 +537,11 @@ struct MixedOpsT {
         R Tnew, pnew, sa;
         if (!sweep_cell_t<true, R>(g, c, P, TT, g.p[base ^ 1], g.T[base ^ 1], Tnew, pnew, sa)) {
           g.dT[ij] = 0.0f; g.dp[ij] = 0.0f;
-          g.eT[0][ij] = 0.0f; g.ep[0][ij] = 0.0f; g.eT[1][ij] = 0.0f; g.ep[1][ij] = 0.0f;
+          const int e = eix(g, c.i, c.j);
+          for (int b = 0; b < 3; b++) {
+            g.eT[b][e] = 0.0f;
+            g.ep[b][e] = 0.0f;
+          }
           return;
         }
         const R P0 = num<R>(P[ij]), T0 = num<R>(TT[ij]);
@@ -437,8 +562,8 @@ struct MixedOpsT {
         return;
       }
       case PS_MATERIALIZE:  // the iterate of the sweep before the last FP32 one, in FP64
-        g.p[base ^ 1][ij] = g.p[base][ij] + widen(g.ep[s.ec ^ 1][ij]);
-        g.T[base ^ 1][ij] = g.T[base][ij] + widen(g.eT[s.ec ^ 1][ij]);
+        g.p[base ^ 1][ij] = g.p[base][ij] + widen(g.ep[s.eprev][eix(g, c.i, c.j)]);
+        g.T[base ^ 1][ij] = g.T[base][ij] + widen(g.eT[s.eprev][eix(g, c.i, c.j)]);
         return;
       case PS_CONFIRM: {  // that sweep again in FP64 into the base buffer; exports for a re-basing
         const double* P = g.p[base ^ 1];
@@ -456,7 +581,11 @@ struct MixedOpsT {
     }
   }
   static __device__ __forceinline__ void pass32(const Geo& g, const Cell& c, const LoopCase& s, float& rp, float& rT) {
-    if (cls_o(g.cls[c.ij])) sweep32_cell(g, c, s.ec, rp, rT);
+    if (cls_o(g.cls[c.ij])) sweep32_cell(g, c, s.ec, next_buf(s.ec), rp, rT);
+  }
+  static __device__ __forceinline__ bool pass32_pair(const Geo& g, int t, const LoopCase& s, const EMaps* maps,
+                                                     void* smem, unsigned& tphase, unsigned slot) {
+    return sweep32_pair_tile(g, t, s, maps, *(Tile2Smem*)smem, tphase, slot);
   }
   static __device__ __forceinline__ void advance(const Geo& g, bool lead, LoopCase& s, double res_p, double res_T) {
     Ctl* ctl = g.ctl;
@@ -466,11 +595,13 @@ struct MixedOpsT {
         if (lead) record_residual(ctl, s.n, s.I, res_p, res_T);
         s.cur = s.base ^ 1;
         s.ec = 0;
+        s.eprev = 0;
         s.phase = (s.n >= (unsigned)g.N_I_p_c) ? PS_DONE : PS_SWEEP32;  // a single sweep: x1 is the result
         break;
       case PS_SWEEP32:
         s.n++;
-        s.ec ^= 1;
+        s.eprev = s.ec;
+        s.ec = next_buf(s.ec);
         if (lead) ctl->sweeps32++;
         s.phase = ((s.n < (unsigned)g.N_I_p_c) && ((g.MaxError_p_c < res_p) || (g.MaxError_T < res_T)))
                       ? PS_SWEEP32 : PS_MATERIALIZE;
@@ -501,6 +632,21 @@ struct MixedOpsT {
 
 __global__ void __launch_bounds__(256, 4) k_pt_loop_mixed(Geo g, int ntiles, LoopCtl* lc) {
   pt_loop_rounds<MixedOpsT<double>, true>(g, nullptr, nullptr, nullptr, 1, ntiles, lc);
+}
+
+// The same loop with two FP32 sweeps per tile load (temporal blocking, tiles staged by TMA).
+__device__ __forceinline__ void init_tile2(Tile2Smem& sm) {
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    tc::mbar_init(&sm.bar, 1);
+    tc::fence_barrier_init();
+  }
+  __syncthreads();
+}
+__global__ void __launch_bounds__(256, 4) k_pt_loop_mixed_tb(Geo g, int ntiles, LoopCtl* lc,
+                                                             const __grid_constant__ EMaps maps) {
+  __shared__ Tile2Smem sm;
+  init_tile2(sm);
+  pt_loop_rounds<MixedOpsT<double>, true, true>(g, nullptr, nullptr, nullptr, 1, ntiles, lc, &maps, &sm);
 }
 __global__ void __launch_bounds__(256, 4) kb_pt_loop_mixed(const Geo* gs, const int* tile_case, const int* tile_first,
                                                           int ncases, int ntiles, LoopCtl* lc) {
@@ -567,6 +713,12 @@ __global__ void __launch_bounds__(256, 4) kb_flux_diff_df(const Geo* gs, unsigne
 }
 __global__ void __launch_bounds__(256, 4) k_pt_loop_mixed_df(Geo g, int ntiles, LoopCtl* lc) {
   pt_loop_rounds<MixedOpsT<df>, true>(g, nullptr, nullptr, nullptr, 1, ntiles, lc);
+}
+__global__ void __launch_bounds__(256, 4) k_pt_loop_mixed_df_tb(Geo g, int ntiles, LoopCtl* lc,
+                                                                const __grid_constant__ EMaps maps) {
+  __shared__ Tile2Smem sm;
+  init_tile2(sm);
+  pt_loop_rounds<MixedOpsT<df>, true, true>(g, nullptr, nullptr, nullptr, 1, ntiles, lc, &maps, &sm);
 }
 __global__ void __launch_bounds__(256, 4) kb_pt_loop_mixed_df(const Geo* gs, const int* tile_case,
                                                              const int* tile_first, int ncases, int ntiles,

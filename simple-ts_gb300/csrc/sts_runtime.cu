@@ -1,5 +1,7 @@
 // Device context, set-up sequence, step orchestration (CUDA graph with
 // conditional WHILE nodes) and the C ABI of libsts_gb300.so.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -229,16 +231,25 @@ struct sts_ctx {
   }
   // the persistent sweep-loop kernel of this context and its grid (CTAs that fit at once)
   using PtKernel = void (*)(Geo, int, LoopCtl*);
+  using PtKernelTB = void (*)(Geo, int, LoopCtl*, EMaps);
   PtKernel pt_kernel() const {
     if (mixed()) return g.precision == 3 ? k_pt_loop_mixed_df : k_pt_loop_mixed;
     return fast() ? k_pt_loop_fast : k_pt_loop;
   }
+  // temporal blocking of the FP32-correction loop: pt_tb 2 runs two FP32 sweeps per tile load
+  // (single cases); pt_tb_forced (sts_set_sweep_blocking) overrides the autotuner's choice
+  EMaps emaps{};
+  int pt_tb = 0, pt_tb_forced = 0;
+  bool tb_available() const { return mixed() && !in_batch && g.eT[0] != nullptr; }
+  bool tb_on() const { return pt_tb == 2 && tb_available(); }
+  PtKernelTB pt_kernel_tb() const { return g.precision == 3 ? k_pt_loop_mixed_df_tb : k_pt_loop_mixed_tb; }
+  const void* pt_func() const { return tb_on() ? (const void*)pt_kernel_tb() : (const void*)pt_kernel(); }
   dim3 pt_grid;
   int size_pt_grid() {
     int dev = 0, per_sm = 0;
     CU(cudaGetDevice(&dev));
     CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pt_kernel(), 256, 0));
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pt_func(), 256, 0));
     if (per_sm < 1) return fail(STS_ERR_CUDA, "the sweep-loop kernel does not fit on a multiprocessor");
     pt_per_sm_max = per_sm;
     const int use = (pt_per_sm > 0 && pt_per_sm <= per_sm) ? pt_per_sm : per_sm;
@@ -247,10 +258,11 @@ struct sts_ctx {
   }
   // the sweep loop of one outer iteration outside the graph: one cooperative launch
   int pt_loop() {
-    void* args[] = {(void*)&g, (void*)&ntiles, (void*)&d_lc};
-    CU(cudaLaunchCooperativeKernel((const void*)pt_kernel(), pt_grid, dim3(32, 8), args, 0, s));
+    void* args[] = {(void*)&g, (void*)&ntiles, (void*)&d_lc, (void*)&emaps};
+    CU(cudaLaunchCooperativeKernel(pt_func(), pt_grid, dim3(32, 8), args, 0, s));
     return STS_OK;
   }
+  int make_emaps();
   int build_graph();
   int write_mesh();
   int write_drag();
@@ -332,7 +344,12 @@ int sts_ctx::build_graph() {
   // warm_start 4: the predictor's kernels (first outer iteration only) beside the assembly
   std::vector<cudaGraphNode_t> before_sweeps{n_asm};
 
-  if (int r = add_kernel(&n_sw, b_outer, before_sweeps, pt_kernel(), pt_grid, dim3(32, 8), g, ntiles, d_lc)) return r;
+  if (tb_on()) {
+    if (int r = add_kernel(&n_sw, b_outer, before_sweeps, pt_kernel_tb(), pt_grid, dim3(32, 8), g, ntiles, d_lc, emaps))
+      return r;
+  } else if (int r = add_kernel(&n_sw, b_outer, before_sweeps, pt_kernel(), pt_grid, dim3(32, 8), g, ntiles, d_lc)) {
+    return r;
+  }
   {
     cudaLaunchAttributeValue v{};
     v.cooperative = 1;
@@ -427,7 +444,8 @@ int sts_ctx::tune_step(int* done) {
   const bool record = tune_idx >= 0;  // index -1: one warm-up step, not recorded
   const int pc = record ? tune_idx % npt : npt - 1, ac = record ? tune_idx % nasm : 0;
   asm_block = asm_shape(ac);
-  pt_per_sm = pc + 1;
+  pt_per_sm = pc % pt_per_sm_max + 1;
+  pt_tb = pt_tb_forced ? pt_tb_forced : (pc >= pt_per_sm_max ? 2 : 1);
   if (int r = size_pt_grid()) return r;
   std::vector<cudaEvent_t> ev;
   auto mark = [&]() {
@@ -488,8 +506,32 @@ void sts_ctx::tune_choose() {
   for (int k = 0; k < (int)tune_pt.size(); k++)
     if (tune_pt[k].best < tune_pt[best_p].best) best_p = k;
   asm_block = asm_shape(best_a);
-  pt_per_sm = best_p + 1;
+  pt_per_sm = best_p % pt_per_sm_max + 1;
+  pt_tb = pt_tb_forced ? pt_tb_forced : (best_p >= pt_per_sm_max ? 2 : 1);
   size_pt_grid();
+}
+
+// The TMA tensor maps of the FP32 correction buffers: 2D FP32, rows of Nxe floats, boxes of 40 x 12
+// (the tile of 32 x 8 cells with a margin of two, x from 4 cells left of the tile).
+int sts_ctx::make_emaps() {
+  void* fp = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  CU(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fp, 12000, cudaEnableDefault, &q));
+  if (q != cudaDriverEntryPointSuccess || !fp) return fail(STS_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  auto enc = (PFN_cuTensorMapEncodeTiled_v12000)fp;
+  cuuint64_t dims[2] = {(cuuint64_t)g.Nxe, (cuuint64_t)g.Ny};
+  cuuint64_t strides[1] = {(cuuint64_t)g.Nxe * sizeof(float)};
+  cuuint32_t box[2] = {40, 12}, es[2] = {1, 1};
+  for (int b = 0; b < 3; b++)
+    for (int f = 0; f < 2; f++) {
+      CUtensorMap* m = f ? &emaps.ep[b] : &emaps.eT[b];
+      float* base = f ? g.ep[b] : g.eT[b];
+      if (enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return fail(STS_ERR_CUDA, "cuTensorMapEncodeTiled failed for a correction buffer");
+    }
+  return STS_OK;
 }
 
 // The launch loop with a CUDA event pair around every kernel: per-kernel device time.
@@ -1044,9 +1086,15 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
   }
   if (g.precision >= 2) {
     float** f32[] = {&g.c32[0], &g.c32[1], &g.c32[2], &g.c32[3], &g.c32[4], &g.a32[0], &g.a32[1], &g.a32[2], &g.a32[3],
-                     &g.T1, &g.hT, &g.q1, &g.den1, &g.dT, &g.dp, &g.ep[0], &g.ep[1], &g.eT[0], &g.eT[1]};
+                     &g.T1, &g.hT, &g.q1, &g.den1, &g.dT, &g.dp};
     for (float** f : f32)
       if (int r = c->alloc(f, Na)) return r;
+    g.Nxe = (h.Nx + 3) / 4 * 4;
+    for (int b = 0; b < 3; b++) {
+      if (int r = c->alloc(&g.ep[b], (size_t)g.Nxe * h.Ny)) return r;
+      if (int r = c->alloc(&g.eT[b], (size_t)g.Nxe * h.Ny)) return r;
+    }
+    if (int r = c->make_emaps()) return r;
   }
   if (int r = c->alloc(&c->d_ctl, 1)) return r;
   g.ctl = c->d_ctl;
@@ -1109,10 +1157,11 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
   }
   if (int r = c->size_pt_grid()) return r;
   if (opt.autotune) {
-    c->tune_pt.assign(c->pt_per_sm_max, sts_ctx::TuneStat{});
+    // candidates of the sweep loop: CTAs per SM, times one or two FP32 sweeps per tile load
+    c->tune_pt.assign(c->pt_per_sm_max * (c->mixed() ? 2 : 1), sts_ctx::TuneStat{});
     c->tune_asm.assign(3, sts_ctx::TuneStat{});
     c->tune_idx = -1;  // one warm-up step first
-    c->tune_left = 1 + sts_ctx::kTuneRounds * std::max(c->pt_per_sm_max, 3);
+    c->tune_left = 1 + sts_ctx::kTuneRounds * std::max((int)c->tune_pt.size(), 3);
   }
   const dim3 G = c->grid, B = c->block;
   cudaStream_t s = c->s;
@@ -1575,6 +1624,32 @@ int sts_conservation(sts_ctx* ctx, double* out5) {
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(out5, ctx->d_cons_out, sizeof(double) * kConsQ, cudaMemcpyDeviceToHost, ctx->s));
   CU(cudaStreamSynchronize(ctx->s));
+  return STS_OK;
+}
+
+int sts_set_sweep_blocking(sts_ctx* ctx, int k) {
+  if (!ctx || k < 0 || k > 2) return fail(STS_ERR_ARG, "k must be 0, 1 or 2");
+  if (k == 2 && !ctx->tb_available())
+    return fail(STS_ERR_ARG, "two sweeps per tile load need a single case with FP32 correction sweeps");
+  CU(cudaSetDevice(ctx->opt.device));
+  CU(cudaStreamSynchronize(ctx->s));
+  ctx->pt_tb_forced = k;
+  if (k) ctx->pt_tb = k;
+  if (int r = ctx->size_pt_grid()) return r;
+  if (ctx->exec) {  // the graph is rebuilt with the new sweep-loop kernel at the next step
+    cudaGraphExecDestroy(ctx->exec);
+    ctx->exec = nullptr;
+  }
+  if (ctx->graph) {
+    cudaGraphDestroy(ctx->graph);
+    ctx->graph = nullptr;
+  }
+  return STS_OK;
+}
+
+int sts_get_sweep_blocking(sts_ctx* ctx, int* k) {
+  if (!ctx || !k) return fail(STS_ERR_ARG, "null argument");
+  *k = ctx->tb_on() ? 2 : 1;
   return STS_OK;
 }
 

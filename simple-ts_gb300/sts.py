@@ -183,6 +183,15 @@ class Solver:
         _check(load().sts_stats(self._h, _dptr(out)))
         return out
 
+    def set_sweep_blocking(self, k: int):
+        """FP32 correction sweeps per tile load: 1, 2, or 0 for the autotuner's choice."""
+        _check(load().sts_set_sweep_blocking(self._h, int(k)))
+
+    def sweep_blocking(self) -> int:
+        k = C.c_int()
+        _check(load().sts_get_sweep_blocking(self._h, C.byref(k)))
+        return k.value
+
     def warm_net_train(self, iters: int, lr: float = 1e-3) -> float:
         """warm_start 5: Adam steps of the network on the stored training pairs; the last loss."""
         lib = load()
