@@ -84,6 +84,8 @@ def parse():
                     help="precision mode of the --profile-target run")
     ap.add_argument("--warm-start", type=int, default=0, choices=[0, 1, 2, 3, 4],
                     help="warm start of the --profile-target run")
+    ap.add_argument("--sweep-blocking", type=int, default=0, choices=[0, 1, 2],
+                    help="FP32 correction sweeps per tile load for the --profile-target run (0: autotuner)")
     ap.add_argument("--profile-target", type=int, default=0,
                     help="only run this many steps kernel by kernel (a small target for ncu), then exit")
     return ap.parse_args()
@@ -102,7 +104,10 @@ def profile_target(args):
         b.close()
         return
     _, d = make_case(args.workload)
-    s = sts.Solver(d, fixed_sweeps=False, use_graph=False, precision=args.precision, warm_start=args.warm_start)
+    s = sts.Solver(d, fixed_sweeps=False, use_graph=False, precision=args.precision, warm_start=args.warm_start,
+                   autotune=args.sweep_blocking == 0)
+    if args.sweep_blocking:
+        s.set_sweep_blocking(args.sweep_blocking)
     s.step(args.profile_target)
     s.sync()
     print(f"profile target: {args.workload}, {args.profile_target} steps, sweeps {list(s.sweep_history())}")
@@ -528,6 +533,31 @@ def checkpoint_bench(d, local, barrier, every=10, saves=10):
             "save_cost_hidden": round(1.0 - cost_async / cost_sync, 3) if cost_sync > 0 else None}
 
 
+def blocking_ab(d, local, steps, flush, barrier, lead):
+    """One against two FP32 correction sweeps per tile load (the results are the same bits), on the
+    FP32-correction path with double-float FP64 parts from a cold start and with the learned stencil:
+    cell-steps/s, sweeps per step and the sweep loop's device time per step (kernel-by-kernel
+    profile of further steps).  The autotuner still picks the assembly block and CTAs per SM."""
+    import numpy as np
+    import sts
+    out = {}
+    for name, warm in (("fp32df_cold", 0), ("fp32df_learned", 4)):
+        row = {}
+        for k in (1, 2):
+            v = sts.Solver(d, fixed_sweeps=False, device=local, precision=sts.MIXED_DF, warm_start=warm)
+            v.set_sweep_blocking(k)
+            vd, vms, vsw = timed_steps(v, steps, lead if warm else 3, flush, barrier)
+            pn, kms, kcnt = v.profile(max(3, min(steps, 10)))
+            row[f"k{k}"] = {"value": v.Nx * v.Ny * vd / (vms / 1e3), "ms_per_step": vms / max(vd, 1),
+                            "sweeps_per_step": float(np.mean(vsw)) if len(vsw) else 0.0,
+                            "sweep_loop_ms_per_step": kms["sweep_loop"] / max(pn, 1),
+                            "blocking_in_use": v.sweep_blocking()}
+            v.close()
+        row["speedup_k2_over_k1"] = row["k2"]["value"] / row["k1"]["value"]
+        out[name] = row
+    return out
+
+
 def network_run(d, local, steps, flush, barrier, lead=60, train_iters=300, lr=3e-4, warmup=10):
     """warm_start 5 on FP32 corrections with double-float FP64 parts: `lead` steps that store the
     network's training pairs (the stencil's start is used unchanged meanwhile), `train_iters` Adam
@@ -773,6 +803,7 @@ def main():
     full = args.variants and args.variant_set == "all"
     ckpt = checkpoint_bench(d, local, barrier) if full else None
     c5 = metric_config_bench(args, local, flush, barrier) if full and args.c5_steps > 0 else None
+    tb = blocking_ab(d, local, args.steps, flush, barrier, args.warm_lead) if full else None
 
     # the FP64 bit-exact path with the default launch shapes (no autotuning), beside the headline,
     # which uses the shapes the autotuner chose on the run's first steps (the shapes change no result)
@@ -797,7 +828,7 @@ def main():
                 "variants": variants,
                 "warm_start_vs_plain": warm_summary(value, sweeps, variants),
                 "checkpoint": ckpt, "untuned_fp64": tuned, "launch_shapes": launch_shapes,
-                "metric_config": c5}
+                "metric_config": c5, "sweep_blocking_ab": tb}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
