@@ -86,6 +86,9 @@ def parse():
                     help="warm start of the --profile-target run")
     ap.add_argument("--sweep-blocking", type=int, default=0, choices=[0, 1, 2],
                     help="FP32 correction sweeps per tile load for the --profile-target run (0: autotuner)")
+    ap.add_argument("--gemm-target", type=int, nargs=3, default=None, metavar=("M", "N", "K"),
+                    help="only run the network's tensor-core GEMM self-check twice on seeded BF16 data of "
+                         "this shape (a small target for ncu), then exit")
     ap.add_argument("--profile-target", type=int, default=0,
                     help="only run this many steps kernel by kernel (a small target for ncu), then exit")
     return ap.parse_args()
@@ -112,6 +115,32 @@ def profile_target(args):
     s.sync()
     print(f"profile target: {args.workload}, {args.profile_target} steps, sweeps {list(s.sweep_history())}")
     s.close()
+
+
+def gemm_target(M, N, K):
+    """The BF16 tensor-core GEMM (sts_tc_gemm) twice on seeded data: D = A B^T, A [M x K], B [N x K]."""
+    import ctypes as C
+    import numpy as np
+    import sts
+    import build as stsbuild
+    stsbuild.build()
+    lib = sts.load()
+    lib.sts_tc_gemm.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                C.c_int]
+    rng = np.random.default_rng(0)
+
+    def bf16(x):
+        u = x.astype(np.float32).view(np.uint32)
+        return ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+
+    A = bf16(rng.standard_normal((M, K)) * 0.1)
+    B = bf16(rng.standard_normal((N, K)) * 0.1)
+    D = np.zeros((M, N), np.float32)
+    for _ in range(2):
+        r = lib.sts_tc_gemm(A.ctypes.data, B.ctypes.data, M, N, K, 0, None, D.ctypes.data, 0)
+        if r != 0:
+            raise RuntimeError(f"sts_tc_gemm returned {r}")
+    print(f"gemm target: {M} x {N} x {K}")
 
 
 def dist_env():
@@ -679,6 +708,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.gemm_target:
+        return gemm_target(*args.gemm_target)
     if args.profile_target:
         return profile_target(args)
     if args.workload == "batch64":
