@@ -87,9 +87,9 @@ def run_fields(case, rec, precision):
 
 
 # bounds of the FP32-correction paths' relative L2 distance from the FP64 fields after the whole
-# run; the Rayleigh-Benard box is convectively unstable, so differences at the tolerance level
-# grow with the instability there
-BOUNDS = {"channel_ma2.43": 1e-8, "rayleigh_benard": 1e-2}
+# run (measured on GB300: at most 4.4e-10 on the channel after 4000 steps, 6.5e-8 on the box after
+# 20000 steps, where u is about 1e-5 of v)
+BOUNDS = {"channel_ma2.43": 1e-8, "rayleigh_benard": 1e-6}
 
 
 @pytest.mark.parametrize("name", ["channel_ma2.43", "rayleigh_benard"])
