@@ -4,11 +4,15 @@ the reference solver itself on the configured workloads for their whole length.
 Cases (FP64, the reference's tolerance-terminated sweep loop at 1e-8, cold start):
   * channel_ma0.1   -- 400x40 channel past a square, Mach 0.1, Kn 0.00194, dt 1e-3, 1000 steps;
   * channel_ma2.43  -- 1200x120 supersonic channel, Mach 2.43, Kn 0.00283, dt 2.5e-4, 4000 steps;
-  * rayleigh_benard -- 512x256 periodic Rayleigh-Benard box, Kn 0.01, g = 1, dt 1e-3, seeded
+  * rayleigh_benard -- 512x256 periodic Rayleigh-Benard box, Kn 0.01, g = 1, dt 5e-5, seeded
                        noise; as many steps as given on the command line (20000 by default).
   * channel_inflow_ramp -- an 80x8 channel whose inflow speed follows the reference's
                        time-dependent inflow (use_interpolation_for_u_BC_by_time,
-                       SIMPLE_TS_MPI.cpp:8102-8144), 40 steps, dumps in full.
+                       SIMPLE_TS_MPI.cpp:8102-8144), 40 steps, dumps in full;
+  * channel_2048_ma<M> -- the 2048x256 channel with the square at Mach M (Kn 0.003, dt 1.25e-4),
+                       1000 steps by default;
+  * batch64_<k>     -- case k of the 64-case batch (seed 20261204) for its 2000 steps, the final
+                       dumps only (one save at the end).
 
 Every case saves ten times during the run into files of their own
 (ToWriteSolvedDataToNewFiles, SIMPLE_TS_MPI.cpp:5607-5631) and writes a log line every step,
@@ -20,6 +24,8 @@ reference binary is built by oracle/build_oracle.py from the reference sources.
 Run from the repository root, one case per process (they are independent):
   python tests/golden/make_golden_long.py channel_ma0.1
   python tests/golden/make_golden_long.py rayleigh_benard 20000
+  python tests/golden/make_golden_long.py batch64_17          (then: ... make_golden_long.py --merge-batch)
+The 64 batch cases are merged into long_batch64.json / long_batch64.npz by --merge-batch.
 """
 import hashlib
 import json
@@ -43,6 +49,11 @@ STRIDE = 8  # sampled cells: every STRIDE-th in x and in y
 
 def long_case(name, steps=None):
     """The Case of a long fixture, with its save cadence set (ten saves, a log line every step)."""
+    if name.startswith("batch64_"):  # one case of the 64-case batch (seed 20261204), final dumps only
+        k = int(name[len("batch64_"):])
+        c = sc.batch_cases(n=64, Nt=steps or 2000)[k]
+        c.entered.update(Nt_save_solved_data=int(c.entered["Nt"]), Nt_save_temp_data=1)
+        return c
     if name == "channel_inflow_ramp":
         c = sc.channel_case("c", 80, 8, 0.3, 0.002, 1e-3, steps or 40)
         c.entered.update(use_interpolation_for_u_BC_by_time=1, t_BC_b=0.005, t_BC_e=0.025,
@@ -66,7 +77,27 @@ def file_digest(path):
     return hashlib.sha256(data).hexdigest()
 
 
+def merge_batch():
+    """long_batch64_<k>.{json,npz} (k = 0..63) into long_batch64.json (records by case) and
+    long_batch64.npz (arrays named <k>_<field>); the per-case files are removed."""
+    recs, arrays = [], {}
+    for k in range(64):
+        base = os.path.join(OUT, f"long_batch64_{k}")
+        with open(base + ".json") as f:
+            recs.append(json.load(f))
+        for key, a in np.load(base + ".npz").items():
+            arrays[f"{k}_{key}"] = a
+    with open(os.path.join(OUT, "long_batch64.json"), "w") as f:
+        json.dump(recs, f, indent=1)
+    np.savez_compressed(os.path.join(OUT, "long_batch64.npz"), **arrays)
+    for k in range(64):
+        for ext in (".json", ".npz"):
+            os.remove(os.path.join(OUT, f"long_batch64_{k}{ext}"))
+
+
 def main():
+    if sys.argv[1] == "--merge-batch":
+        return merge_batch()
     name = sys.argv[1]
     steps = int(sys.argv[2]) if len(sys.argv) > 2 else None
     exes = build_reference()

@@ -5,10 +5,13 @@ Fixtures (tests/golden/make_golden_long.py): the reference solver run on
   * the 1200x120 Mach 2.43 channel for 4000 steps,
   * the 512x256 Rayleigh-Benard box for its steps (long_rayleigh_benard.json),
   * an 80x8 channel with the time-dependent inflow ramp (SIMPLE_TS_MPI.cpp:8102-8144),
+  * the 2048x256 channel with the square at Mach 0.1, 0.5, 1.0 and 2.43 for 1000 steps,
 each saving ten times into files of its own and logging every step.  The FP64 drop-in run must
 write every one of those files byte for byte (the time loop SIMPLE_TS_MPI.cpp:3230-4691 for
 the whole run).  The FP32-correction paths (precision 2 and 3) are then run for the same steps
-and their per-field relative L2 distance from the FP64 fields is printed and bounded.
+and their per-field relative L2 distance from the FP64 fields is printed and bounded.  The
+64-case batch (config 4) runs its 2000 steps as one batch against the reference's run of every
+case alone.
 """
 import json
 import os
@@ -22,7 +25,8 @@ from conftest import GOLDEN
 
 pytestmark = pytest.mark.gpu
 
-LONG = ["channel_inflow_ramp", "channel_ma0.1", "channel_ma2.43", "rayleigh_benard"]
+LONG = ["channel_inflow_ramp", "channel_ma0.1", "channel_ma2.43", "rayleigh_benard", "channel_2048_ma0.1",
+        "channel_2048_ma0.5", "channel_2048_ma1.0", "channel_2048_ma2.43"]
 FIELDS = ("u", "v", "p", "T", "rho")
 
 
@@ -113,3 +117,34 @@ def test_full_length_fp32_corrections_error(name, lib_built):
     for prec, errs in out.items():
         for f, e in errs.items():
             assert e <= BOUNDS[name], (prec, f, e)
+
+
+def test_batch64_full_length_matches_reference(lib_built):
+    """The 64 cases of config 4 advanced together for their 2000 steps: every case's sweep count of
+    every step and its final dumps equal the reference's run of that case alone (the reference
+    saves at its last step and again after the loop, so the batch case saves twice)."""
+    import sts
+    from make_golden_long import file_digest, long_case
+    with open(os.path.join(GOLDEN, "long_batch64.json")) as f:
+        recs = json.load(f)
+    arrays = np.load(os.path.join(GOLDEN, "long_batch64.npz"))
+    with tempfile.TemporaryDirectory() as root:
+        dirs = []
+        for k in range(64):
+            d = os.path.join(root, f"c{k:02d}")
+            os.makedirs(d)
+            long_case(f"batch64_{k}", recs[k]["steps"]).write(d)
+            dirs.append(d)
+        b = sts.Batch(dirs, fixed_sweeps=False)
+        steps = recs[0]["steps"]
+        assert b.step(steps) == steps
+        bad = []
+        for k, c in enumerate(b.cases):
+            np.testing.assert_array_equal(c.sweep_history()[-steps:], arrays[f"{k}_sweeps"], err_msg=f"case {k}")
+            c.write_outputs()
+            c.write_outputs()
+            for f in ("u.bin", "v.bin", "p.bin", "Temper.bin"):
+                if file_digest(os.path.join(dirs[k], f)) != recs[k]["files"][f]:
+                    bad.append((k, f))
+        b.close()
+        assert not bad, f"dumps that differ from the reference's: {bad}"
