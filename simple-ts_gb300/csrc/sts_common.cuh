@@ -117,6 +117,7 @@ struct Ctl {
   unsigned int conv_max[2][2];
   float conv_w[2][36];
   unsigned int conv_ok[2];
+  unsigned int conv_nlist;  // tiles in the list of tiles with active cells (Geo::clist) of this step
 };
 
 // Learned warm start: differences kept, and steps of the least-squares window.
@@ -139,7 +140,7 @@ struct LoopCtl {
 
 // TMA tensor maps of the three FP32 correction buffers of e_T and e_p (the temporally blocked
 // FP32 sweeps load their tiles with them); a kernel parameter.
-struct alignas(64) EMaps {
+struct EMaps {  // aligned as CUtensorMap (128 bytes)
   CUtensorMap eT[3], ep[3];
 };
 
@@ -208,6 +209,7 @@ struct Geo {
   double* cnext[2];  // the stencil's start for the next step, on the cells flagged for it
   float* cpart;
   int* crows;
+  int* clist;  // tiles with active cells, listed by k_conv_gram for k_conv_gram_list (any order)
   float* cgram;
 };
 
