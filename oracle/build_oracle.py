@@ -75,6 +75,42 @@ def build_reference(force=False):
     return out
 
 
+def build_reference_mpi(force=False):
+    """The reference solver's own MPI build (COMPILE_MPI kept, residual-terminated sweeps) against the
+    minimal shared-memory MPI of oracle/mpishim, and its launcher: oracle/_ref/simple_ts_mpi_resid
+    and oracle/_ref/mpishim_run, when the reference sources are present (returns paths or None).
+    Run as `mpishim_run N simple_ts_mpi_resid` in a case directory whose EnteredData.txt asks for N
+    subdomains.  Compiled as C++98: the reference's global `rank` clashes with std::rank of C++11."""
+    main = os.path.join(REFERENCE, "SIMPLE_TS_MPI.cpp")
+    if not os.path.exists(main):
+        return None
+    rdir = os.path.join(HERE, "_ref")
+    shim = os.path.join(HERE, "mpishim")
+    os.makedirs(rdir, exist_ok=True)
+    others = [os.path.join(REFERENCE, f) for f in
+              ("Circles_Objects.cpp", "Polyhedrons_Objects.cpp", "Objects_for_Solving.cpp", "DomainDecomposition2D.cpp")]
+    shim_src = [os.path.join(shim, f) for f in ("mpi.h", "mpishim.c", "mpishim_seg.h", "mpishim_run.c")]
+    exe = os.path.join(rdir, "simple_ts_mpi_resid")
+    run = os.path.join(rdir, "mpishim_run")
+    procs = []
+    if force or not _newer(exe, [main] + others + shim_src):
+        obj = os.path.join(rdir, "mpishim.o")
+        cmd = (f"gcc -O2 -c {os.path.join(shim, 'mpishim.c')} -o {obj} && "
+               f"sed -e 's|^#define FIXED_NUMBER_OF_ITERATIONS_LOOP_3\r*$|/* residual-terminated */|' {main} | "
+               f"g++ -std=gnu++98 -O3 -msse2 -ffp-contract=off -w -I{shim} -I{REFERENCE} -x c++ - -x none {' '.join(others)} "
+               f"{obj} -o {exe} -lpthread -lrt")
+        if os.uname().machine not in ("x86_64", "i686"):
+            cmd = cmd.replace("-msse2 ", "")
+        procs.append(subprocess.Popen(["bash", "-c", cmd]))
+    if force or not _newer(run, shim_src):
+        procs.append(subprocess.Popen(["gcc", "-O2", os.path.join(shim, "mpishim_run.c"), "-o", run, "-lpthread", "-lrt"]))
+    for p in procs:
+        if p.wait() != 0:
+            raise RuntimeError("reference MPI build failed")
+    return {"simple_ts_mpi_resid": exe, "mpishim_run": run}
+
+
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
     print(build_reference(force="--force" in sys.argv))
+    print(build_reference_mpi(force="--force" in sys.argv))

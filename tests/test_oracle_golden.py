@@ -93,3 +93,25 @@ def test_oracle_conservation_sums_definition(oracle_built):
         want = [m, m * uc, m * vc, m * T / (5.0 / 3.0 - 1.0), m * (uc ** 2 + vc ** 2)]
         want = np.array([x[fluid].sum() for x in want])
         np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-15)
+
+
+@pytest.mark.parametrize("ranks", [2, 4])
+def test_reference_mpi_build_equals_serial(ranks, oracle_built, golden_records):
+    """The reference's own MPI build, run on the minimal shared-memory MPI (oracle/mpishim) with one
+    strip of the mesh per rank, writes the serial reference's dumps and logs byte for byte: the
+    multi-core CPU baseline is the reference itself."""
+    import tempfile
+    import sts_cases as sc
+    from build_oracle import build_reference_mpi
+    from make_golden import digest
+    if build_reference_mpi() is None:
+        pytest.skip("the reference sources are not present")
+    import reference_mpi
+    rec = golden_records["channel_ma2.43_60x12_resid"]
+    case, _ = golden_case("channel_ma2.43_60x12_resid")
+    case.entered["Nt_save_temp_data"] = 1
+    with tempfile.TemporaryDirectory() as d:
+        reference_mpi.run(case, d, ranks, timeout=300)
+        for f in ("u", "v", "p", "Temper"):
+            assert digest(sc.read_field(d, f, rec["Nx"], rec["Ny"])) == rec["sha256_" + f], f
+        assert open(os.path.join(d, "Tmp.txt")).read() == rec["tmp_txt"]
