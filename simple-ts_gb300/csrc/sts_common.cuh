@@ -117,7 +117,6 @@ struct Ctl {
   unsigned int conv_max[2][2];
   float conv_w[2][36];
   unsigned int conv_ok[2];
-  unsigned int conv_nlist;  // tiles in the list of tiles with active cells (Geo::clist) of this step
 };
 
 // Learned warm start: differences kept, and steps of the least-squares window.
@@ -209,7 +208,6 @@ struct Geo {
   double* cnext[2];  // the stencil's start for the next step, on the cells flagged for it
   float* cpart;
   int* crows;
-  int* clist;  // tiles with active cells, listed by k_conv_gram for k_conv_gram_list (any order)
   float* cgram;
 };
 

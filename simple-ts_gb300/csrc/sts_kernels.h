@@ -43,14 +43,11 @@ __global__ void kb_warm_diff(const Geo* gs);
 __global__ void kb_warm_fit(const Geo* gs);
 __global__ void kb_warm_apply(const Geo* gs);
 // convolutional warm start (warm_start 4), sts_learn.cu (k_step_begin stores the differences and
-// takes the prepared start): at the end of a step k_conv_gram -> {k_conv_gram_list -> k_conv_solve,
-// k_conv_next} -> k_conv_predict; k_conv_gram, k_conv_next and k_conv_predict on the 32x8 cell
-// tiles, k_conv_gram_list with kConvGramListCTAs CTAs of kConvGramThreads (32 x 32) over the listed
-// active tiles, k_conv_solve with one CTA of kConvSolveThreads per field
-constexpr int kConvSolveThreads = 1024, kConvGramThreads = 1024, kConvGramListCTAs = 128;
+// takes the prepared start): at the end of a step k_conv_gram -> {k_conv_solve, k_conv_next} ->
+// k_conv_predict; k_conv_gram, k_conv_next and k_conv_predict on the 32x8 cell tiles,
+// k_conv_solve with one CTA of kConvSolveThreads per field
+constexpr int kConvSolveThreads = 1024;
 __global__ void k_conv_gram(Geo g);
-__global__ void k_conv_gram_list(Geo g);
-__global__ void kb_conv_gram_list(const Geo* gs);
 __global__ void k_conv_solve(Geo g);
 __global__ void k_conv_next(Geo g);
 __global__ void k_conv_predict(Geo g);

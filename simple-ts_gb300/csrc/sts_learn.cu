@@ -126,65 +126,45 @@ __device__ __forceinline__ void neumaier(float& s, float& c, float x) {
   s = t;
 }
 
-// The training pair formed at the end of a step (after the sweeps): its target is the coming
-// difference D_{h+1} = x_{n+1} - x_n -- the step's final iterate less the start-of-step value,
-// rounded to FP32 exactly as the next step's start stores it -- and its features are those of the
-// newest stored difference D_h on its active cells.  (It is the pair the next step would form;
-// forming it now lets the fit run beside the step's last kernels instead of on the next step's
-// path.)  Two kernels: conv_gram_body, one CTA of 32x8 threads per tile, finds the tiles with
-// active cells, records the others as empty and lists the active ones; conv_gram_tile, run for
-// each listed tile by a CTA of kConvGramThreads, sums the normal-equation terms in FP32 over each
-// strip's rows (32x2 cells, cell order), then over the tile's strips with rows in strip order
-// (compensated).  Which CTA handles a tile changes no bit: its sums are the tile's alone.
+// One CTA per tile of 32x8 cells, i.e. four strips of 32x2 cells, at the end of a step (after the
+// sweeps): the normal-equation terms of the training pair whose target is the coming difference
+// D_{h+1} = x_{n+1} - x_n -- the step's final iterate less the start-of-step value, rounded to
+// FP32 exactly as the next step's start stores it -- and whose features are those of the newest
+// stored difference D_h on its active cells; summed in FP32 over each strip's rows in cell order,
+// then over the tile's strips with rows in strip order (compensated).  A tile without active
+// cells only records that.  (The pair is the one the next step would form; forming it now lets
+// the fit run beside the step's last kernels instead of on the next step's path.)
 __device__ __forceinline__ void conv_gram_body(const Geo& g) {
-  Ctl* ctl = g.ctl;
-  const unsigned r = ctl->warm_ready;
+  const Ctl* ctl = g.ctl;
+  const unsigned r = ctl->warm_ready, cur = ctl->cur;
   // conv_next folds the coming difference's maximum once this kernel is done (with several
   // outer iterations, only the last one's counts)
-  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < 2 && threadIdx.y == 0) ctl->conv_max[r & 1][threadIdx.x] = 0u;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < 2 && threadIdx.y == 0)
+    const_cast<Ctl*>(ctl)->conv_max[r & 1][threadIdx.x] = 0u;
   if (r < 4) return;  // the features need four stored differences
   const unsigned h = r - 1;
   const int Nx = g.Nx, Ny = g.Ny;
-  constexpr int TX = 32, TY = 8;
+  constexpr int TX = 32, TY = 8, NS = TY / kConvStripY, SR = kConvStripX * kConvStripY;
   const int ntx = (Nx + TX - 1) / TX, nty = (Ny + TY - 1) / TY, ntiles = ntx * nty;
   if ((int)blockIdx.x >= ntx || (int)blockIdx.y >= nty) return;
   const int tile = blockIdx.x + blockIdx.y * ntx;
-  const int tid = threadIdx.x + TX * threadIdx.y;
-  const int i = blockIdx.x * TX + threadIdx.x, j = blockIdx.y * TY + threadIdx.y;
-  const unsigned bits = (i < Nx && j < Ny) ? g.cact[h & 1][i + j * Nx] : 0u;
+  const int tid = threadIdx.x + TX * threadIdx.y, lane = threadIdx.x;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+  const bool in = i < Nx && j < Ny;
+  const int n = i + j * Nx;
+  const unsigned bits = in ? g.cact[h & 1][n] : 0u;
   if (!__syncthreads_or(bits != 0u)) {
     if (tid < 2) g.crows[tid * ntiles + tile] = 0;
     return;
   }
-  if (tid == 0) g.clist[atomicAdd(&ctl->conv_nlist, 1u)] = tile;
-}
-
-// The terms of one listed tile; blockDim (32, kConvGramThreads / 32): the first 8 rows of threads
-// hold the tile's cells, every thread takes part in the term sums (kConvGramThreads / 4 per strip).
-__device__ __forceinline__ void conv_gram_tile(const Geo& g, int tile) {
-  const Ctl* ctl = g.ctl;
-  const unsigned r = ctl->warm_ready, cur = ctl->cur;
-  const unsigned h = r - 1;
-  const int Nx = g.Nx, Ny = g.Ny;
-  constexpr int TX = 32, TY = 8, NS = TY / kConvStripY, SR = kConvStripX * kConvStripY;
-  constexpr int NT = kConvGramThreads, TPS = NT / NS;
-  const int ntx = (Nx + TX - 1) / TX, nty = (Ny + TY - 1) / TY, ntiles = ntx * nty;
-  const int tyi = tile / ntx;
-  const int i0 = (tile - tyi * ntx) * TX, j0 = tyi * TY;
-  const int tid = threadIdx.x + TX * threadIdx.y, lane = threadIdx.x;
-  const bool cellt = threadIdx.y < TY;
-  const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
-  const bool in = cellt && i < Nx && j < Ny;
-  const int n = i + j * Nx;
-  const unsigned bits = in ? g.cact[h & 1][n] : 0u;
   __shared__ float Df[4][TY + 2][TX + 2];          // D_{h..h-3} of one field, margin one (clamped)
   __shared__ float F[NS][SR][kConvFeat + 1];       // per strip: active rows' features and target
   __shared__ int wcount[TY];
   float* P = &F[0][0][0];                          // the strips' terms, after F is used: [NS][kConvTerms]
-  const int s = threadIdx.y / kConvStripY;         // a cell thread's strip
-  const int sT = tid / TPS, tT = tid - sT * TPS;   // strip and index of a term-summing thread
+  const int s = threadIdx.y / kConvStripY, t64 = threadIdx.x + TX * (threadIdx.y % kConvStripY);
   for (int f = 0; f < 2; f++) {
-    stage<4 * (TY + 2) * (TX + 2), NT>(&Df[0][0][0], tid, [&](int k) {
+    stage<4 * (TY + 2) * (TX + 2), TX * TY>(&Df[0][0][0], tid, [&](int k) {
       const int t = k / ((TY + 2) * (TX + 2)), rem = k - t * ((TY + 2) * (TX + 2));
       const int yy = rem / (TX + 2), xx = rem - yy * (TX + 2);
       const int jj = min(max(j0 - 1 + yy, 0), Ny - 1), ii = min(max(i0 - 1 + xx, 0), Nx - 1);
@@ -193,40 +173,40 @@ __device__ __forceinline__ void conv_gram_tile(const Geo& g, int tile) {
     const bool act = (bits >> f) & 1u;  // active cells are solved cells
     const float target = act ? (float)((f ? g.T[cur][n] : g.p[cur][n]) - (f ? g.T_m[0][n] : g.p_m[0][n])) : 0.f;
     const unsigned bal = __ballot_sync(0xffffffffu, act);
-    if (lane == 0 && cellt) wcount[threadIdx.y] = __popc(bal);
+    if (lane == 0) wcount[threadIdx.y] = __popc(bal);
     __syncthreads();
     int nr[NS];
     for (int q = 0; q < NS; q++) nr[q] = wcount[kConvStripY * q] + wcount[kConvStripY * q + 1];
+    const int pos = ((threadIdx.y % kConvStripY) ? wcount[threadIdx.y - 1] : 0) + __popc(bal & ((1u << lane) - 1u));
     if (act) {
-      const int pos = ((threadIdx.y % kConvStripY) ? wcount[threadIdx.y - 1] : 0) + __popc(bal & ((1u << lane) - 1u));
       const int x0 = threadIdx.x + 1, y0 = threadIdx.y + 1;
       conv_features_from([&](int k, int dj, int di) { return Df[k][y0 + dj][x0 + di]; }, F[s][pos]);
       F[s][pos][kConvFeat] = target;
     }
     __syncthreads();
-    // each strip's TPS threads: terms e = tT + TPS k accumulate side by side, every term over the
+    // each strip's 64 threads: terms e = t64 + 64 k accumulate side by side, every term over the
     // strip's rows in order
-    constexpr int kPerT = (kConvTerms + TPS - 1) / TPS;
+    constexpr int kPerT = (kConvTerms + SR - 1) / SR;
     float acc[kPerT];
     for (int k = 0; k < kPerT; k++) acc[k] = 0.f;
-    if (nr[sT] > 0) {
+    if (nr[s] > 0) {
       int ta[kPerT], tb[kPerT];
       for (int k = 0; k < kPerT; k++) {
-        const int e = tT + k * TPS;
+        const int e = t64 + k * SR;
         if (e < kConvTerms) conv_term(e, ta[k], tb[k]);
         else ta[k] = tb[k] = 0;
       }
-      for (int q = 0; q < nr[sT]; q++)
+      for (int q = 0; q < nr[s]; q++)
 #pragma unroll
-        for (int k = 0; k < kPerT; k++) acc[k] = acc[k] + F[sT][q][ta[k]] * F[sT][q][tb[k]];
+        for (int k = 0; k < kPerT; k++) acc[k] = acc[k] + F[s][q][ta[k]] * F[s][q][tb[k]];
     }
     __syncthreads();  // F is read no more: its space takes the strips' terms
     for (int k = 0; k < kPerT; k++) {
-      const int e = tT + k * TPS;
-      if (e < kConvTerms) P[sT * kConvTerms + e] = acc[k];
+      const int e = t64 + k * SR;
+      if (e < kConvTerms) P[s * kConvTerms + e] = acc[k];
     }
     __syncthreads();
-    for (int e = tid; e < kConvTerms; e += NT) {
+    for (int e = tid; e < kConvTerms; e += TX * TY) {
       float sum = 0.f, cmp = 0.f;
       for (int q = 0; q < NS; q++)
         if (nr[q] > 0) neumaier(sum, cmp, P[q * kConvTerms + e]);
@@ -235,12 +215,6 @@ __device__ __forceinline__ void conv_gram_tile(const Geo& g, int tile) {
     if (tid == 0) g.crows[f * ntiles + tile] = nr[0] + nr[1] + nr[2] + nr[3];
     __syncthreads();
   }
-}
-
-__device__ __forceinline__ void conv_gram_list_body(const Geo& g) {
-  if (g.ctl->warm_ready < 4) return;
-  const int n = (int)*(volatile unsigned*)&g.ctl->conv_nlist;
-  for (int q = blockIdx.x; q < n; q += gridDim.x) conv_gram_tile(g, g.clist[q]);
 }
 
 // One CTA of kConvSolveThreads (1024) threads per field, after conv_gram: the pair's total over the
@@ -315,7 +289,6 @@ __device__ __forceinline__ void conv_solve_body(const Geo& g) {
     __syncthreads();
   }
   if (e < kConvTerms) g.cgram[((size_t)(pair % kConvWin) * 2 + f) * kConvTerms + e] = sum + cmp;
-  if (f == 0 && tid == 0) ctl->conv_nlist = 0u;  // the list of active tiles, read by conv_gram_tile before
   __syncthreads();
   if (pair + 1 < (unsigned)kConvWin) {
     if (tid == 0) ctl->conv_ok[f] = 0u;
@@ -476,7 +449,6 @@ __device__ __forceinline__ void conv_predict_body(const Geo& g) {
 }  // namespace
 
 __global__ void k_conv_gram(Geo g) { conv_gram_body(g); }
-__global__ void __launch_bounds__(kConvGramThreads) k_conv_gram_list(Geo g) { conv_gram_list_body(g); }
 __global__ void __launch_bounds__(kConvSolveThreads) k_conv_solve(Geo g) { conv_solve_body(g); }
 __global__ void k_conv_next(Geo g) { conv_next_body(g); }
 __global__ void k_conv_predict(Geo g) { conv_predict_body(g); }
@@ -484,11 +456,6 @@ __global__ void kb_conv_gram(const Geo* gs) {
   __shared__ Geo sg;
   if (!stage_geo(sg, gs)) return;
   conv_gram_body(sg);
-}
-__global__ void __launch_bounds__(kConvGramThreads) kb_conv_gram_list(const Geo* gs) {
-  __shared__ Geo sg;
-  if (!stage_geo(sg, gs)) return;
-  conv_gram_list_body(sg);
 }
 __global__ void __launch_bounds__(kConvSolveThreads) kb_conv_solve(const Geo* gs) {
   __shared__ Geo sg;

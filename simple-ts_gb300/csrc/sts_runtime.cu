@@ -176,7 +176,6 @@ struct sts_ctx {
     if (g.warm_start != 4) return;
     mark(-1);
     k_conv_gram<<<grid, block, 0, s>>>(g);
-    k_conv_gram_list<<<kConvGramListCTAs, dim3(32, kConvGramThreads / 32), 0, s>>>(g);
     k_conv_solve<<<2, kConvSolveThreads, 0, s>>>(g);
     k_conv_next<<<grid, block, 0, s>>>(g);
     k_conv_predict<<<grid, block, 0, s>>>(g);
@@ -358,12 +357,9 @@ int sts_ctx::build_graph() {
   }
   if (int r = add_kernel(&n_cor, b_outer, {n_sw}, k_correct, grid, block, g)) return r;
   if (g.warm_start == 4) {  // the fit and the next step's start, beside the step's last kernels
-    cudaGraphNode_t w[5];
+    cudaGraphNode_t w[4];
     if (int r = add_kernel(&w[0], b_outer, {n_sw}, k_conv_gram, grid, block, g)) return r;
-    if (int r = add_kernel(&w[4], b_outer, {w[0]}, k_conv_gram_list, dim3(kConvGramListCTAs),
-                           dim3(32, kConvGramThreads / 32), g))
-      return r;
-    if (int r = add_kernel(&w[1], b_outer, {w[4]}, k_conv_solve, dim3(2), dim3(kConvSolveThreads), g)) return r;
+    if (int r = add_kernel(&w[1], b_outer, {w[0]}, k_conv_solve, dim3(2), dim3(kConvSolveThreads), g)) return r;
     if (int r = add_kernel(&w[2], b_outer, {w[0]}, k_conv_next, grid, block, g)) return r;
     if (int r = add_kernel(&w[3], b_outer, {w[1], w[2]}, k_conv_predict, grid, block, g)) return r;
     if (warm_net) {  // the network's kernels, captured into the body after the stencil's
@@ -1086,7 +1082,6 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
     const size_t nt = (size_t)((h.Nx + 31) / 32) * ((h.Ny + 7) / 8);
     if (int r = c->alloc(&g.cpart, nt * 2 * kConvTerms)) return r;
     if (int r = c->alloc(&g.crows, nt * 2)) return r;
-    if (int r = c->alloc(&g.clist, nt)) return r;
     if (int r = c->alloc(&g.cgram, (size_t)kConvWin * 2 * kConvTerms)) return r;
   }
   if (g.precision >= 2) {
@@ -1980,7 +1975,6 @@ int sts_batch::step_host(int n) {
     else kb_flux_diff<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
     if (warm4) {
       kb_conv_gram<<<cell_grid, blk, 0, s>>>(G);
-      kb_conv_gram_list<<<dim3(kConvGramListCTAs, 1, ncases), dim3(32, kConvGramThreads / 32), 0, s>>>(G);
       kb_conv_solve<<<dim3(2, 1, ncases), kConvSolveThreads, 0, s>>>(G);
       kb_conv_next<<<cell_grid, blk, 0, s>>>(G);
       kb_conv_predict<<<cell_grid, blk, 0, s>>>(G);
@@ -2034,7 +2028,6 @@ int sts_batch::tune_step() {
   else kb_flux_diff<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
   if (warm4) {
     kb_conv_gram<<<cell_grid, blk, 0, s>>>(G);
-    kb_conv_gram_list<<<dim3(kConvGramListCTAs, 1, ncases), dim3(32, kConvGramThreads / 32), 0, s>>>(G);
     kb_conv_solve<<<dim3(2, 1, ncases), kConvSolveThreads, 0, s>>>(G);
     kb_conv_next<<<cell_grid, blk, 0, s>>>(G);
     kb_conv_predict<<<cell_grid, blk, 0, s>>>(G);
@@ -2122,12 +2115,9 @@ int sts_batch::build_graph() {
     return r;
   std::vector<cudaGraphNode_t> before_end{n[8]};
   if (warm4) {  // the fit and the next step's start, beside the step's last kernels
-    cudaGraphNode_t w[5];
+    cudaGraphNode_t w[4];
     if (int r = add_kernel(&w[0], b, {n[2]}, kb_conv_gram, cell_grid, blk, G)) return r;
-    if (int r = add_kernel(&w[4], b, {w[0]}, kb_conv_gram_list, dim3(kConvGramListCTAs, 1, ncases),
-                           dim3(32, kConvGramThreads / 32), G))
-      return r;
-    if (int r = add_kernel(&w[1], b, {w[4]}, kb_conv_solve, dim3(2, 1, ncases), dim3(kConvSolveThreads), G)) return r;
+    if (int r = add_kernel(&w[1], b, {w[0]}, kb_conv_solve, dim3(2, 1, ncases), dim3(kConvSolveThreads), G)) return r;
     if (int r = add_kernel(&w[2], b, {w[0]}, kb_conv_next, cell_grid, blk, G)) return r;
     if (int r = add_kernel(&w[3], b, {w[1], w[2]}, kb_conv_predict, cell_grid, blk, G)) return r;
     before_end.push_back(w[3]);
