@@ -623,8 +623,8 @@ C5_MACHS = (0.1, 0.5, 1.0, 2.43)
 def metric_config_bench(args, local, flush, barrier):
     """Plain GPU Jacobi (FP64 bit-exact, cold start) against the warm starts on the 2048x256
     channel at each Mach number: FP32 corrections with double-float FP64 parts from a cold start,
-    from quadratic extrapolation and from the learned convolutional predictor, and the learned
-    predictor on the FP64 path.  Per path: cell-steps/s (device time, L2 flushed before every
+    from quadratic extrapolation and from the learned convolutional predictor, and quadratic
+    extrapolation and the learned predictor on the FP64 path.  Per path: cell-steps/s (device time, L2 flushed before every
     timed step), sweeps per step and the largest per-field relative L2 distance from the plain
     path after the same steps; per Mach: the learned start against plain Jacobi and against the
     same precision without it."""
@@ -632,7 +632,7 @@ def metric_config_bench(args, local, flush, barrier):
     import sts
     import sts_cases as sc
     EX, DF = sts.EXACT, sts.MIXED_DF
-    paths = (("plain_fp64", EX, 0), ("fp64_learned", EX, 4), ("fp32df_cold", DF, 0),
+    paths = (("plain_fp64", EX, 0), ("fp64_quadratic", EX, 2), ("fp64_learned", EX, 4), ("fp32df_cold", DF, 0),
              ("fp32df_quadratic", DF, 2), ("fp32df_learned", DF, 4))
     out = {}
     for mach in C5_MACHS:
@@ -675,7 +675,8 @@ def metric_config_bench(args, local, flush, barrier):
                             "learned_vs_plain": gain("fp32df_learned", "plain_fp64"),
                             "learned_vs_same_precision_cold": gain("fp32df_learned", "fp32df_cold"),
                             "learned_vs_quadratic": gain("fp32df_learned", "fp32df_quadratic"),
-                            "fp64_learned_vs_plain": gain("fp64_learned", "plain_fp64")}
+                            "fp64_learned_vs_plain": gain("fp64_learned", "plain_fp64"),
+                            "fp64_learned_vs_fp64_quadratic": gain("fp64_learned", "fp64_quadratic")}
         if "fp32df_network" in row:
             out[f"ma{mach}"]["network_vs_stencil"] = gain("fp32df_network", "fp32df_learned")
     return {"workload": "channel 2048x256 with the square, Kn 0.003, dt 1.25e-4, tolerance 1e-8",
