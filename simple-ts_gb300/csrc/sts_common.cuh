@@ -93,6 +93,7 @@ struct Ctl {
   unsigned int continue_iter, continue_step;
   unsigned int steps_left; // multi-step graph launches count down here
   unsigned int block_count;  // last-block detection
+  unsigned int bnd_count;    // last-CTA detection of the fused boundary kernel
   unsigned int status;     // ST_* bits
   unsigned int step_sweeps;  // sum of sweeps in the current step
   // per-step record (ring of the last 4096 steps)

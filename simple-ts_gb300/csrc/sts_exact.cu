@@ -924,8 +924,9 @@ __global__ void k_sqrt_rho(Geo g, int do_rho) {
 
 // ---------------------------------------------------------------------------
 // Boundary work, in the reference's order.  The wall lists are O(perimeter) but carry FP64
-// divisions, so they run over the whole grid (k_bnd_walls, k_bnd_tjump); the short column
-// and row copies run in one CTA (k_boundary) or in the first CTA of k_flux_diff.
+// divisions, so they run one entry per thread over a grid (k_bnd_fused); the short column and
+// row copies run in one CTA (the last of k_bnd_fused, k_boundary before the time loop) or in the
+// first CTA of k_flux_diff.
 // ---------------------------------------------------------------------------
 // loop control after the velocity correction: SIMPLE_TS_MPI.cpp:4347-4361 (coefficients), :4406-4450
 __device__ void do_control(const Geo& g, unsigned long long h_outer, int in_graph) {
@@ -1323,40 +1324,56 @@ __device__ __forceinline__ void boundary_body(const Geo& g, unsigned phases, uns
   if (phases & PH_PRES) phase_pres(g, p, tid, nt);
 }
 __global__ void __launch_bounds__(1024) k_boundary(Geo g, unsigned phases, unsigned long long h_outer, int in_graph) { boundary_body(g, phases, h_outer, in_graph); }
-__global__ void __launch_bounds__(1024) kb_boundary(const Geo* gs, unsigned phases, unsigned long long h_outer, int in_graph) {
-  __shared__ Geo sg;
-  if (!stage_geo(sg, gs)) return;
-  boundary_body(sg, phases, h_outer, in_graph);
+
+// The boundary work of one outer iteration in one launch.  Over the whole grid, one entry per
+// thread: the loop control (first thread), the slip-wall entries of u and of v (independent:
+// they write u and v respectively, each entry only the writes that survive in the reference's
+// sequential order) and, when they need nothing of the velocity and pressure phases
+// (jump_beside), the temperature-jump entries.  The last CTA to finish then runs the column and
+// row phases (PH_VEL | PH_PBEGIN), which read the slip walls' u and v and the control's
+// residuals, and after them the jump entries when those read the inlet density that PH_PBEGIN
+// writes: the reference's order (control, slip u, slip v, velocities, pressure begin) with the
+// jump values wherever they see the same inputs.
+__device__ __forceinline__ bool last_cta(unsigned* counter) {
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();  // this CTA's writes before its ticket
+    const unsigned t = atomicAdd(counter, 1u);
+    last = (t == gridDim.x * gridDim.y - 1);
+    if (last) {
+      *counter = 0;
+      __threadfence();  // every other CTA's writes before the reads that follow
+    }
+  }
+  __syncthreads();
+  return last;
 }
 
-// Wall lists over the whole grid: loop control (one thread), slip u and slip v (independent:
-// they write u and v respectively).
-__device__ __forceinline__ void bnd_walls_body(const Geo& g, unsigned phases, unsigned long long h_outer, int in_graph) {
+__device__ __forceinline__ void bnd_fused_body(const Geo& g, unsigned long long h_outer, int in_graph, int jump_beside) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
-  if ((phases & PH_CONTROL) && t == 0) do_control(g, h_outer, in_graph);
-  if (phases & PH_SLIP_U)
-    for (int k = t; k < g.n_slip_u; k += nt) do_slip_u(g, k);
-  if (phases & PH_SLIP_V)
-    for (int k = t; k < g.n_slip_v; k += nt) do_slip_v(g, k);
-}
-__global__ void k_bnd_walls(Geo g, unsigned phases, unsigned long long h_outer, int in_graph) { bnd_walls_body(g, phases, h_outer, in_graph); }
-__global__ void kb_bnd_walls(const Geo* gs, unsigned phases, unsigned long long h_outer, int in_graph) {
-  __shared__ Geo sg;
-  if (!stage_geo(sg, gs)) return;
-  bnd_walls_body(sg, phases, h_outer, in_graph);
-}
-
-// Temperature-jump wall values over the whole grid.
-__device__ __forceinline__ void bnd_tjump_body(const Geo& g) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+  if (t == 0) do_control(g, h_outer, in_graph);
+  const int nu = g.n_slip_u, nuv = nu + g.n_slip_v, n = nuv + (jump_beside ? g.n_tjump : 0);
   const double* T = g.T[g.ctl->cur];
-  for (int k = t; k < g.n_tjump; k += nt) do_tjump(g, T, k);
+  for (int k = t; k < n; k += nt) {
+    if (k < nu) do_slip_u(g, k);
+    else if (k < nuv) do_slip_v(g, k - nu);
+    else do_tjump(g, T, k - nuv);
+  }
+  if (!last_cta(&g.ctl->bnd_count)) return;
+  boundary_body(g, PH_VEL | PH_PBEGIN, 0ull, 0);
+  if (!jump_beside) {
+    __syncthreads();
+    for (int k = threadIdx.x; k < g.n_tjump; k += blockDim.x) do_tjump(g, T, k);
+  }
 }
-__global__ void k_bnd_tjump(Geo g) { bnd_tjump_body(g); }
-__global__ void kb_bnd_tjump(const Geo* gs) {
+__global__ void k_bnd_fused(Geo g, unsigned long long h_outer, int in_graph, int jump_beside) {
+  bnd_fused_body(g, h_outer, in_graph, jump_beside);
+}
+__global__ void kb_bnd_fused(const Geo* gs, unsigned long long h_outer, int in_graph, int jump_beside) {
   __shared__ Geo sg;
   if (!stage_geo(sg, gs)) return;
-  bnd_tjump_body(sg);
+  bnd_fused_body(sg, h_outer, in_graph, jump_beside);
 }
 
 // End of a time step: time-dependent inflow (SIMPLE_TS_MPI.cpp:8102-8144), per-step
@@ -1512,7 +1529,45 @@ __global__ void k_check_division(unsigned long long n, unsigned long long seed, 
 // once instead of queueing on the copy engines one after another.
 __global__ void k_move4(const double* __restrict__ a0, const double* __restrict__ a1, const double* __restrict__ a2,
                         const double* __restrict__ a3, double* b0, double* b1, double* b2, double* b3, int n) {
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+  // every pointer 16-byte aligned: pairs of doubles, two pairs of each array in flight per thread
+  // (the host link needs many bytes in flight); otherwise one double at a time
+  const bool vec = ((reinterpret_cast<uintptr_t>(a0) | reinterpret_cast<uintptr_t>(a1) |
+                     reinterpret_cast<uintptr_t>(a2) | reinterpret_cast<uintptr_t>(a3) |
+                     reinterpret_cast<uintptr_t>(b0) | reinterpret_cast<uintptr_t>(b1) |
+                     reinterpret_cast<uintptr_t>(b2) | reinterpret_cast<uintptr_t>(b3)) & 15u) == 0;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+  int done = 0;
+  if (vec) {
+    const int n2 = n / 2;
+    const double2 *c0 = reinterpret_cast<const double2*>(a0), *c1 = reinterpret_cast<const double2*>(a1),
+                  *c2 = reinterpret_cast<const double2*>(a2), *c3 = reinterpret_cast<const double2*>(a3);
+    double2 *d0 = reinterpret_cast<double2*>(b0), *d1 = reinterpret_cast<double2*>(b1),
+            *d2 = reinterpret_cast<double2*>(b2), *d3 = reinterpret_cast<double2*>(b3);
+    for (int k = t; k < n2; k += 2 * nt) {
+      const int k2 = k + nt;
+      const bool two = k2 < n2;
+      const double2 x0 = c0[k], x1 = c1[k], x2 = c2[k], x3 = c3[k];
+      double2 y0 = x0, y1 = x1, y2 = x2, y3 = x3;
+      if (two) {
+        y0 = c0[k2];
+        y1 = c1[k2];
+        y2 = c2[k2];
+        y3 = c3[k2];
+      }
+      d0[k] = x0;
+      d1[k] = x1;
+      d2[k] = x2;
+      d3[k] = x3;
+      if (two) {
+        d0[k2] = y0;
+        d1[k2] = y1;
+        d2[k2] = y2;
+        d3[k2] = y3;
+      }
+    }
+    done = 2 * n2;
+  }
+  for (int k = done + t; k < n; k += nt) {
     b0[k] = a0[k];
     b1[k] = a1[k];
     b2[k] = a2[k];

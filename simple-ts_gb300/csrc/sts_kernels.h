@@ -31,8 +31,7 @@ __global__ void k_sweep(Geo g, unsigned long long h_sweep, int in_graph);
 __global__ void k_correct(Geo g);
 __global__ void k_face_rho(Geo g);
 __global__ void k_flux_diff(Geo g, unsigned tail);
-__global__ void k_bnd_walls(Geo g, unsigned phases, unsigned long long h_outer, int in_graph);
-__global__ void k_bnd_tjump(Geo g);
+__global__ void k_bnd_fused(Geo g, unsigned long long h_outer, int in_graph, int jump_beside);
 __global__ void k_sqrt_rho(Geo g, int do_rho);
 __global__ void k_boundary(Geo g, unsigned phases, unsigned long long h_outer, int in_graph);
 __global__ void k_step_end(Geo g, unsigned long long h_step, int in_graph);
@@ -62,9 +61,7 @@ __global__ void kb_assemble(const Geo* gs, unsigned long long h_sweep, int in_gr
 __global__ void kb_correct(const Geo* gs);
 __global__ void kb_face_rho(const Geo* gs);
 __global__ void kb_flux_diff(const Geo* gs, unsigned tail);
-__global__ void kb_bnd_walls(const Geo* gs, unsigned phases, unsigned long long h_outer, int in_graph);
-__global__ void kb_bnd_tjump(const Geo* gs);
-__global__ void kb_boundary(const Geo* gs, unsigned phases, unsigned long long h_outer, int in_graph);
+__global__ void kb_bnd_fused(const Geo* gs, unsigned long long h_outer, int in_graph, int jump_beside);
 __global__ void kb_step_end(const Geo* gs, unsigned long long h_step, int in_graph);
 // The whole sweep loop of an outer iteration in one cooperative launch (grid <= resident CTAs):
 // k_ for one case (ntiles 32x8 tiles), kb_ for ncases cases, where tile_case[t] is the case of

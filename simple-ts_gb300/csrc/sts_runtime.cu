@@ -141,19 +141,19 @@ struct sts_ctx {
   }
   // launches
   void boundary(unsigned ph) { k_boundary<<<1, 1024, 0, s>>>(g, ph, 0, 0); }
-  dim3 walls_grid() const {
-    const int n = g.n_slip_u + g.n_slip_v;
+  // the fused boundary kernel: one thread per slip-wall entry (and per jump entry when those
+  // run beside the velocity and pressure phases)
+  bool jump_beside() const { return tjump_beside_walls(g.bits); }
+  dim3 bnd_grid() const {
+    const int n = g.n_slip_u + g.n_slip_v + (jump_beside() ? g.n_tjump : 0);
     return dim3((unsigned)std::max(1, std::min((n + 255) / 256, 1024)));
   }
-  dim3 tjump_grid() const { return dim3((unsigned)std::max(1, std::min((g.n_tjump + 255) / 256, 1024))); }
   // boundary work and fluxes/diffusion of one outer iteration outside the graph; `mark`
   // (optional) brackets the launches for the per-kernel profile
   template <class M>
   void boundary_step(M mark) {
     mark(-1);
-    k_bnd_walls<<<walls_grid(), 256, 0, s>>>(g, PH_CONTROL | PH_SLIP_U | PH_SLIP_V, 0, 0);
-    k_boundary<<<1, 1024, 0, s>>>(g, PH_VEL | PH_PBEGIN, 0, 0);
-    k_bnd_tjump<<<tjump_grid(), 256, 0, s>>>(g);
+    k_bnd_fused<<<bnd_grid(), 256, 0, s>>>(g, 0ull, 0, jump_beside() ? 1 : 0);
     mark(5);
     mark(-1);
     flux_kernel()<<<grid, block, 0, s>>>(g, PH_TEMP | PH_PRES);
@@ -370,19 +370,10 @@ int sts_ctx::build_graph() {
     }
   }
   if (int r = add_kernel(&n_rho, b_outer, {n_cor}, k_face_rho, grid, block, g)) return r;
-  cudaGraphNode_t n_walls, n_tj;
-  if (int r = add_kernel(&n_walls, b_outer, {n_rho}, k_bnd_walls, walls_grid(), dim3(256), g,
-                         (unsigned)(PH_CONTROL | PH_SLIP_U | PH_SLIP_V), (unsigned long long)ho, 1))
+  if (int r = add_kernel(&n_bnd, b_outer, {n_rho}, k_bnd_fused, bnd_grid(), dim3(256), g, (unsigned long long)ho, 1,
+                         jump_beside() ? 1 : 0))
     return r;
-  if (int r = add_kernel(&n_bnd, b_outer, {n_walls}, k_boundary, dim3(1), dim3(1024), g,
-                         (unsigned)(PH_VEL | PH_PBEGIN), (unsigned long long)0, 0))
-    return r;
-  if (tjump_beside_walls(g.bits)) {
-    if (int r = add_kernel(&n_tj, b_outer, {n_cor}, k_bnd_tjump, tjump_grid(), dim3(256), g)) return r;
-  } else if (int r = add_kernel(&n_tj, b_outer, {n_bnd}, k_bnd_tjump, tjump_grid(), dim3(256), g)) {
-    return r;
-  }
-  if (int r = add_kernel(&n_fd, b_outer, {n_bnd, n_tj}, flux_kernel(), grid, block, g,
+  if (int r = add_kernel(&n_fd, b_outer, {n_bnd}, flux_kernel(), grid, block, g,
                          (unsigned)(PH_TEMP | PH_PRES)))
     return r;
   CU(cudaGraphInstantiate(&exec, graph, 0));
@@ -1894,7 +1885,8 @@ struct sts_batch {
   LoopCtl* d_lc = nullptr;
   int ncases = 0, ntiles = 0, precision = 0;
   bool fixed = true;
-  dim3 cell_grid, walls_grid, tjump_grid, pt_grid;
+  dim3 cell_grid, bnd_grid, pt_grid;
+  int jump_beside = 1;  // every case's jump entries run beside its velocity and pressure phases
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<unsigned> counter_before;
@@ -1967,9 +1959,7 @@ int sts_batch::step_host(int n) {
     CU(cudaLaunchCooperativeKernel((const void*)pt_kernel(), pt_grid, blk, args, 0, s));
     kb_correct<<<cell_grid, blk, 0, s>>>(G);
     kb_face_rho<<<cell_grid, blk, 0, s>>>(G);
-    kb_bnd_walls<<<walls_grid, 256, 0, s>>>(G, PH_CONTROL | PH_SLIP_U | PH_SLIP_V, 0ull, 0);
-    kb_boundary<<<dim3(1, 1, ncases), 1024, 0, s>>>(G, PH_VEL | PH_PBEGIN, 0ull, 0);
-    kb_bnd_tjump<<<tjump_grid, 256, 0, s>>>(G);
+    kb_bnd_fused<<<bnd_grid, 256, 0, s>>>(G, 0ull, 0, jump_beside);
     if (precision == 3) kb_flux_diff_df<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
     else if (fast()) kb_flux_diff_fast<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
     else kb_flux_diff<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
@@ -2020,9 +2010,7 @@ int sts_batch::tune_step() {
   CU(cudaEventRecord(ev[2], s));
   kb_correct<<<cell_grid, blk, 0, s>>>(G);
   kb_face_rho<<<cell_grid, blk, 0, s>>>(G);
-  kb_bnd_walls<<<walls_grid, 256, 0, s>>>(G, PH_CONTROL | PH_SLIP_U | PH_SLIP_V, 0ull, 0);
-  kb_boundary<<<dim3(1, 1, ncases), 1024, 0, s>>>(G, PH_VEL | PH_PBEGIN, 0ull, 0);
-  kb_bnd_tjump<<<tjump_grid, 256, 0, s>>>(G);
+  kb_bnd_fused<<<bnd_grid, 256, 0, s>>>(G, 0ull, 0, jump_beside);
   if (precision == 3) kb_flux_diff_df<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
   else if (fast()) kb_flux_diff_fast<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
   else kb_flux_diff<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
@@ -2100,16 +2088,10 @@ int sts_batch::build_graph() {
   }
   if (int r = add_kernel(&n[3], b, {n[2]}, kb_correct, cell_grid, blk, G)) return r;
   if (int r = add_kernel(&n[4], b, {n[3]}, kb_face_rho, cell_grid, blk, G)) return r;
-  if (int r = add_kernel(&n[5], b, {n[4]}, kb_bnd_walls, walls_grid, dim3(256), G,
-                         (unsigned)(PH_CONTROL | PH_SLIP_U | PH_SLIP_V), (unsigned long long)0, 0))
+  if (int r = add_kernel(&n[6], b, {n[4]}, kb_bnd_fused, bnd_grid, dim3(256), G, (unsigned long long)0, 0,
+                         jump_beside))
     return r;
-  if (int r = add_kernel(&n[6], b, {n[5]}, kb_boundary, dim3(1, 1, ncases), dim3(1024), G,
-                         (unsigned)(PH_VEL | PH_PBEGIN), (unsigned long long)0, 0))
-    return r;
-  bool beside = true;
-  for (const sts_ctx* c : cases) beside = beside && tjump_beside_walls(c->g.bits);
-  if (int r = add_kernel(&n[7], b, {beside ? n[3] : n[6]}, kb_bnd_tjump, tjump_grid, dim3(256), G)) return r;
-  if (int r = add_kernel(&n[8], b, {n[6], n[7]}, precision == 3 ? kb_flux_diff_df : (fast() ? kb_flux_diff_fast : kb_flux_diff),
+  if (int r = add_kernel(&n[8], b, {n[6]}, precision == 3 ? kb_flux_diff_df : (fast() ? kb_flux_diff_fast : kb_flux_diff),
                          cell_grid, blk, G,
                          (unsigned)(PH_TEMP | PH_PRES)))
     return r;
@@ -2162,7 +2144,7 @@ int sts_open_batch(const char* const* case_dirs, int ncases, const sts_options* 
   b->ncases = ncases;
   std::vector<Geo> geos;
   std::vector<int> tile_case, tile_first;
-  unsigned gx = 1, gy = 1, wx = 1, tx = 1;
+  unsigned gx = 1, gy = 1, wx = 1;
   for (int k = 0; k < ncases; k++) {
     sts_ctx* c = b->cases[k];
     geos.push_back(c->g);
@@ -2172,8 +2154,8 @@ int sts_open_batch(const char* const* case_dirs, int ncases, const sts_options* 
     gy = std::max(gy, c->grid.y);
     b->max_nx = std::max(b->max_nx, c->g.Nx);
     b->max_ny = std::max(b->max_ny, c->g.Ny);
-    wx = std::max(wx, c->walls_grid().x);
-    tx = std::max(tx, c->tjump_grid().x);
+    wx = std::max(wx, c->bnd_grid().x);
+    if (!c->jump_beside()) b->jump_beside = 0;
   }
   b->ntiles = (int)tile_case.size();
   b->warm3 = opt.warm_start == 3;
@@ -2187,8 +2169,7 @@ int sts_open_batch(const char* const* case_dirs, int ncases, const sts_options* 
   CU(cudaMemcpy(b->d_tile_first, tile_first.data(), sizeof(int) * tile_first.size(), cudaMemcpyHostToDevice));
   CU(cudaMemset(b->d_lc, 0, sizeof(LoopCtl)));
   b->cell_grid = dim3(gx, gy, (unsigned)ncases);
-  b->walls_grid = dim3(wx, 1, (unsigned)ncases);
-  b->tjump_grid = dim3(tx, 1, (unsigned)ncases);
+  b->bnd_grid = dim3(wx, 1, (unsigned)ncases);
   int sms = 0, per_sm = 0;
   CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, opt.device));
   CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b->pt_kernel(), 256, 0));
