@@ -183,6 +183,10 @@ struct Geo {
   // 1/(hx[i-1]+hx[i]), 1/(hx[i]+hx[i+1]), the same in y, 1/(3 hx), 1/(3 hy), 1/ht and 1/3
   const double *rhx, *rhy, *rxx_m, *rxx_p, *ryy_m, *ryy_p, *r3x, *r3y;
   double rht, r3;
+  // the quotients of mesh widths that the diffusion coefficients take per cell (static: widths
+  // and fluid masks), computed once by k_flux_quotients with the divisions of the per-step
+  // form: [0] D_ux, [1] D_uy, [2] D_vx, [3] D_vy, [4] DTx, [5] DTy
+  const double* fq[6];
   // --- precision modes 1 and 2 ---
   // FP32 correction sweeps: coefficients c[0..4] of the T correction, a[0..3] of the p
   // numerator, the base-sweep values T1, H/T1, p1, Den and the defects dT, dp; e_p/e_T are the

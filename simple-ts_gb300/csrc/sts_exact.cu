@@ -770,6 +770,62 @@ __device__ __forceinline__ double wall_term_off(double tw, double h) {
   return (tw >= 0.0 && tw < CUDART_INF && h != 0.0) ? h : 0.0 * sqrt(tw) + 1.0 * h;
 }
 
+// The diffusion coefficients' quotients of mesh widths at cell (i, j): divisions by mesh sums
+// through their correctly rounded reciprocals (same bits as IEEE); a divisor (m1 h1 + m2 h2) with
+// fluid masks m is h1, h2 or the rounded sum.  They depend on the mesh and the cell classes
+// only, so k_flux_quotients evaluates them once per run into g.fq and the per-step kernel reads
+// them (the same operands and operations, so the same bits); entries whose term is a plain zero
+// hold 0.
+__device__ __forceinline__ void flux_quotients(const Geo& g, int i, int j, double q[6]) {
+  const Nb d = neighbours(i, j, g.Nx, g.Ny, g.bits & F_PERIODIC);
+  const double* __restrict__ hx = g.hx;
+  const double* __restrict__ hy = g.hy;
+  const bool b_ws = cls_fluid(g.cls[d.i_1j_1]), b_s = cls_fluid(g.cls[d.ij_1]), b_w = cls_fluid(g.cls[d.i_1j]),
+             b_p = cls_fluid(g.cls[d.ij]);
+  const int jm = j - (0 < j ? 1 : 0);
+  const double ry = g.ryy_m[j], rx = g.rxx_m[i];
+  auto rsum = [](bool a, bool b, double r_both, double r_a, double r_b) { return a ? (b ? r_both : r_a) : r_b; };
+  const bool all4 = b_ws && b_s && b_w && b_p;
+  q[0] = div_cr(hy[j], hx[d.i_1], g.rhx[d.i_1]);
+  if (all4)
+    q[1] = div_cr(hx[i] + hx[d.i_1], hy[j] + hy[jm], ry);
+  else if ((b_p && b_w) || (b_s && b_ws))
+    q[1] = div_cr(hx[i] + hx[d.i_1], (double)(b_p * b_w) * hy[j] + (double)(b_s * b_ws) * hy[jm],
+                  rsum(b_p && b_w, b_s && b_ws, ry, g.rhy[j], g.rhy[jm]));
+  else
+    q[1] = 0.0;
+  if (all4)
+    q[2] = div_cr(hy[j] + hy[jm], hx[i] + hx[d.i_1], rx);
+  else if ((b_p && b_s) || (b_w && b_ws))
+    q[2] = div_cr(hy[j] + hy[jm], (double)(b_p * b_s) * hx[i] + (double)(b_w * b_ws) * hx[d.i_1],
+                  rsum(b_p && b_s, b_w && b_ws, rx, g.rhx[i], g.rhx[d.i_1]));
+  else
+    q[2] = 0.0;
+  q[3] = div_cr(hx[i], hy[jm], g.rhy[jm]);
+  // 1 / (0.5 s) = 2 (1 / s) exactly
+  if (b_p && b_w)
+    q[4] = div_cr(hy[j], 0.5 * (hx[i] + hx[d.i_1]), 2.0 * rx);
+  else if (b_p || b_w)
+    q[4] = div_cr(hy[j], 0.5 * ((double)b_p * hx[i] + (double)b_w * hx[d.i_1]),
+                  2.0 * rsum(b_p, b_w, rx, g.rhx[i], g.rhx[d.i_1]));
+  else
+    q[4] = 0.0;
+  if (b_p && b_s)
+    q[5] = div_cr(hx[i], 0.5 * (hy[j] + hy[jm]), 2.0 * ry);
+  else if (b_p || b_s)
+    q[5] = div_cr(hx[i], 0.5 * ((double)b_p * hy[j] + (double)b_s * hy[jm]),
+                  2.0 * rsum(b_p, b_s, ry, g.rhy[j], g.rhy[jm]));
+  else
+    q[5] = 0.0;
+}
+__global__ void k_flux_quotients(Geo g) {
+  const Cell c = cell(g);
+  if (!c.ok) return;
+  double q[6];
+  flux_quotients(g, c.i, c.j, q);
+  for (int k = 0; k < 6; k++) const_cast<double*>(g.fq[k])[c.ij] = q[k];
+}
+
 // ly, lx: the block's staged interpolations (null when the block is not 32x8)
 __device__ __forceinline__ void flux_diff_cell(const Geo& g, const Cell& c, const double* ly, const double* lx) {
   const int i = c.i, j = c.j;
@@ -785,12 +841,9 @@ __device__ __forceinline__ void flux_diff_cell(const Geo& g, const Cell& c, cons
   const bool b_ws = cls_fluid(g.cls[d.i_1j_1]), b_s = cls_fluid(g.cls[d.ij_1]), b_w = cls_fluid(g.cls[d.i_1j]),
              b_p = cls_fluid(g.cls[d.ij]);
   const int jm = j - (0 < j ? 1 : 0);
-  // divisions by mesh sums through their correctly rounded reciprocals (same bits as IEEE):
-  // a divisor (m1 h1 + m2 h2) with masks m is h1, h2 or the rounded sum
   const double ry = g.ryy_m[j], rx = g.rxx_m[i];
   auto LiY = [&](double f1, double f2) { return div_cr(f1 * hy[j] + f2 * hy[jm], hy[jm] + hy[j], ry); };
   auto LiX = [&](double f1, double f2) { return div_cr(f1 * hx[i] + f2 * hx[d.i_1], hx[d.i_1] + hx[i], rx); };
-  auto rsum = [](bool a, bool b, double r_both, double r_a, double r_b) { return a ? (b ? r_both : r_a) : r_b; };
   const int x = threadIdx.x, y = threadIdx.y;
   const bool west = ly && d.i_1 == i - 1, south = lx && j > 0;
   auto ly_west = [&]() { return west ? ly[x + 33 * y] : LiY(sT[d.i_1j_1], sT[d.i_1j]); };
@@ -807,14 +860,10 @@ __device__ __forceinline__ void flux_diff_cell(const Geo& g, const Cell& c, cons
                 (double)((!(b_ws && b_w)) || (!(b_s && b_p))) * LiY(sqrt(Tw_u[d.ij_1]), sqrt(Tw_u[d.ij])));
   }
   g.Gamma_yf[d.ij] = Gy;
-  g.D_ux[d.ij] = cT * sT[d.i_1j] * div_cr(hy[j], hx[d.i_1], g.rhx[d.i_1]);
+  g.D_ux[d.ij] = cT * sT[d.i_1j] * g.fq[0][d.ij];
   // where every mask is 1 the masked sums are the plain sums (1 * x = x exactly)
-  const bool all4 = b_ws && b_s && b_w && b_p;
-  if (all4)
-    g.D_uy[d.ij] = cT * Gy * div_cr(hx[i] + hx[d.i_1], hy[j] + hy[jm], ry);
-  else if ((b_p && b_w) || (b_s && b_ws))
-    g.D_uy[d.ij] = cT * Gy * div_cr(hx[i] + hx[d.i_1], (double)(b_p * b_w) * hy[j] + (double)(b_s * b_ws) * hy[jm],
-                                    rsum(b_p && b_w, b_s && b_ws, ry, g.rhy[j], g.rhy[jm]));
+  if ((b_p && b_w) || (b_s && b_ws))
+    g.D_uy[d.ij] = cT * Gy * g.fq[1][d.ij];
   else
     g.D_uy[d.ij] = 0;
   if (b_ws && b_s && b_w && b_p) {
@@ -826,31 +875,23 @@ __device__ __forceinline__ void flux_diff_cell(const Geo& g, const Cell& c, cons
                 (double)((!(b_ws && b_s)) || (!(b_w && b_p))) * LiX(sqrt(Tw_v[d.i_1j]), sqrt(Tw_v[d.ij])));
   }
   g.Gamma_xf[d.ij] = Gx;
-  if (all4)
-    g.D_vx[d.ij] = cT * Gx * div_cr(hy[j] + hy[jm], hx[i] + hx[d.i_1], rx);
-  else if ((b_p && b_s) || (b_w && b_ws))
-    g.D_vx[d.ij] = cT * Gx * div_cr(hy[j] + hy[jm], (double)(b_p * b_s) * hx[i] + (double)(b_w * b_ws) * hx[d.i_1],
-                                    rsum(b_p && b_s, b_w && b_ws, rx, g.rhx[i], g.rhx[d.i_1]));
+  if ((b_p && b_s) || (b_w && b_ws))
+    g.D_vx[d.ij] = cT * Gx * g.fq[2][d.ij];
   else
     g.D_vx[d.ij] = 0;
-  g.D_vy[d.ij] = cT * sT[d.ij_1] * div_cr(hx[i], hy[jm], g.rhy[jm]);
-  // 1 / (0.5 s) = 2 (1 / s) exactly
+  g.D_vy[d.ij] = cT * sT[d.ij_1] * g.fq[3][d.ij];
   if (b_p && b_w)
-    g.DTx[d.ij] = cT1 * div_cr(hy[j], 0.5 * (hx[i] + hx[d.i_1]), 2.0 * rx) *
-                  wall_term_off(Tw_u[d.ij], Hi(sT[d.i_1j], sT[d.ij], hx[d.i_1], hx[i]));
+    g.DTx[d.ij] = cT1 * g.fq[4][d.ij] * wall_term_off(Tw_u[d.ij], Hi(sT[d.i_1j], sT[d.ij], hx[d.i_1], hx[i]));
   else if (b_p || b_w)
-    g.DTx[d.ij] = cT1 * div_cr(hy[j], 0.5 * ((double)b_p * hx[i] + (double)b_w * hx[d.i_1]),
-                               2.0 * rsum(b_p, b_w, rx, g.rhx[i], g.rhx[d.i_1])) *
+    g.DTx[d.ij] = cT1 * g.fq[4][d.ij] *
                   ((double)((!b_p) || (!b_w)) * sqrt(Tw_u[d.ij]) +
                    (double)(b_p * b_w) * Hi(sT[d.i_1j], sT[d.ij], hx[d.i_1], hx[i]));
   else
     g.DTx[d.ij] = 0;
   if (b_p && b_s)
-    g.DTy[d.ij] = cT1 * div_cr(hx[i], 0.5 * (hy[j] + hy[jm]), 2.0 * ry) *
-                  wall_term_off(Tw_v[d.ij], Hi(sT[d.ij_1], sT[d.ij], hy[jm], hy[j]));
+    g.DTy[d.ij] = cT1 * g.fq[5][d.ij] * wall_term_off(Tw_v[d.ij], Hi(sT[d.ij_1], sT[d.ij], hy[jm], hy[j]));
   else if (b_p || b_s)
-    g.DTy[d.ij] = cT1 * div_cr(hx[i], 0.5 * ((double)b_p * hy[j] + (double)b_s * hy[jm]),
-                               2.0 * rsum(b_p, b_s, ry, g.rhy[j], g.rhy[jm])) *
+    g.DTy[d.ij] = cT1 * g.fq[5][d.ij] *
                   ((double)((!b_p) || (!b_s)) * sqrt(Tw_v[d.ij]) +
                    (double)(b_p * b_s) * Hi(sT[d.ij_1], sT[d.ij], hy[jm], hy[j]));
   else

@@ -31,6 +31,7 @@ __global__ void k_sweep(Geo g, unsigned long long h_sweep, int in_graph);
 __global__ void k_correct(Geo g);
 __global__ void k_face_rho(Geo g);
 __global__ void k_flux_diff(Geo g, unsigned tail);
+__global__ void k_flux_quotients(Geo g);
 __global__ void k_bnd_fused(Geo g, unsigned long long h_outer, int in_graph, int jump_beside);
 __global__ void k_sqrt_rho(Geo g, int do_rho);
 __global__ void k_boundary(Geo g, unsigned phases, unsigned long long h_outer, int in_graph);

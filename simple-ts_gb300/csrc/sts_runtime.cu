@@ -1045,6 +1045,11 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
     g.r3x = t[6]; g.r3y = t[7];
     g.rht = 1.0 / g.ht;
     g.r3 = 1.0 / 3.0;
+    for (int k = 0; k < 6; k++) {  // filled by k_flux_quotients before the first flux kernel
+      double* q = nullptr;
+      if (int r = c->alloc(&q, Na)) return r;
+      g.fq[k] = q;
+    }
   }
   // warm_start 5 is warm_start 4 on the device plus the network's kernels
   g.warm_start = opt.warm_start == 5 ? 4 : opt.warm_start;
@@ -1156,6 +1161,7 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
   }
   const dim3 G = c->grid, B = c->block;
   cudaStream_t s = c->s;
+  k_flux_quotients<<<G, B, 0, s>>>(g);
 
   // the rest of main() before the time loop (SIMPLE_TS_MPI.cpp:2833-3227), on the device
   if (!h.restart) {
