@@ -36,7 +36,7 @@ L2_BYTES = 129 * 2 ** 20
 BYTES_PER_CELL = {
     "sweep_loop": 32,     # per sweep: read p, T of the iterate, write p, T (times sweeps per launch)
     "assemble": 27 * 8 + 1,
-    "flux_diff": 15 * 8 + 1,
+    "flux_diff": 21 * 8 + 1,  # with the six static quotient tables
     "correct": 10 * 8 + 1,
     "face_rho": 5 * 8 + 1,
     "step_begin": 10 * 8,
@@ -45,7 +45,7 @@ BYTES_PER_CELL = {
 # DRAM bytes per launch measured by ncu on the default workload (the 1200x120 channel), FP64 path (dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch of the fourteenth time step, cold cache); None where no
 # capture was taken
-TRAFFIC = {"assemble": 21101056, "sweep_loop": 19600128 + 20480, "flux_diff": 9751296}
+TRAFFIC = {"assemble": 21101056, "sweep_loop": 19600128 + 20480, "flux_diff": 16722432}
 
 # FP64 instructions per cell of the FP64 path's kernels (per cell and sweep for the sweep loop),
 # counted by ncu on this workload (smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on
@@ -54,7 +54,7 @@ TRAFFIC = {"assemble": 21101056, "sweep_loop": 19600128 + 20480, "flux_diff": 97
 # FP64 rates (sts_fp64_rates) against the measured launch time.
 FP64_OPS = {"assemble": {"add": 94.24, "mul": 104.97, "fma": 29.69},
             "sweep_loop": {"add": 20.64, "mul": 16.55, "fma": 19.22},
-            "flux_diff": {"add": 20.12, "mul": 50.32, "fma": 56.28}}
+            "flux_diff": {"add": 14.28, "mul": 42.42, "fma": 32.74}}
 
 
 def parse():
@@ -651,7 +651,7 @@ def metric_config_bench(args, local, flush, barrier):
 
         row = {}
         for name, prec, warm in paths:
-            v = sts.Solver(d, fixed_sweeps=False, device=local, precision=prec, warm_start=warm)
+            v = sts.Solver(d, fixed_sweeps=False, device=local, precision=sts.MIXED_DF, warm_start=warm)
             lead = max(args.c5_lead, 3) if warm else max(args.warmup, 3)
             vd, vms, vsw = timed_steps(v, args.c5_steps, lead, flush, barrier)
             ref = base_at(v.steps_before_timing + vd)
