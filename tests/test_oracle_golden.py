@@ -52,7 +52,7 @@ def test_oracle_matches_reference_dumps(name, oracle_built, golden_records):
 
 
 def test_oracle_library_matches_cli(oracle_built, golden_records):
-    """The in-process oracle (used on the GPU machine) steps exactly like its CLI."""
+    """The in-process oracle (the checker of the GPU tests) steps exactly like its CLI."""
     import ora
     rec = golden_records["channel_ma2.43_60x12_resid"]
     case, fixed = golden_case(rec["name"])
