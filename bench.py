@@ -651,7 +651,7 @@ def metric_config_bench(args, local, flush, barrier):
 
         row = {}
         for name, prec, warm in paths:
-            v = sts.Solver(d, fixed_sweeps=False, device=local, precision=sts.MIXED_DF, warm_start=warm)
+            v = sts.Solver(d, fixed_sweeps=False, device=local, precision=prec, warm_start=warm)
             lead = max(args.c5_lead, 3) if warm else max(args.warmup, 3)
             vd, vms, vsw = timed_steps(v, args.c5_steps, lead, flush, barrier)
             ref = base_at(v.steps_before_timing + vd)
