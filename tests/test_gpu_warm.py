@@ -35,6 +35,27 @@ def test_warm_start_matches_oracle(name, warm, lib_built, oracle_built):
             g.close()
 
 
+@pytest.mark.parametrize("warm", [2, 4])
+def test_warm_start_with_outer_iterations(warm, lib_built, oracle_built):
+    """Three outer iterations per step: the warm start belongs to the step's first one; the step
+    graph and the launch-by-launch loop both equal to the oracle bit for bit."""
+    import ora
+    import sts
+    case = sc.channel_case("c", 60, 12, 2.43, 0.00283, 2.5e-4, 100)
+    case.entered["N_I"] = 3
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        o = ora.Oracle(d, fixed_sweeps=False, warm_start=warm)
+        assert o.step(30) == 30
+        for use_graph in (True, False):
+            g = sts.Solver(d, fixed_sweeps=False, use_graph=use_graph, warm_start=warm)
+            assert g.step(30) == 30
+            for f in FIELDS:
+                np.testing.assert_array_equal(g.field(f), o.field(f), err_msg=f"{f} graph={use_graph}")
+            np.testing.assert_array_equal(g.sweep_history(), o.sweeps())
+            g.close()
+
+
 def test_warm_start_cuts_sweeps_within_tolerance(lib_built, oracle_built):
     import ora
     import sts
