@@ -745,8 +745,9 @@ def main():
     value = job_rate(Na * done, world, total_ms / 1e3)
 
     # e2e through the C ABI with host buffers: per step the state u, v, p, T goes host->device
-    # from pinned memory (sts_set_state), one step runs, and the new state comes back
-    # device->host (sts_get_state).
+    # from pinned memory, one step runs, and the new state comes back device->host into the same
+    # buffers, in one call (sts_step_exchange: the set-state, step and get-state calls' work with
+    # one synchronisation)
     pins = {f: torch.empty(Na, dtype=torch.float64).pin_memory() for f in ("u", "v", "p", "T")}
     ptrs = [pins[f].data_ptr() for f in ("u", "v", "p", "T")]
     s.get_state_ptr(*ptrs)
@@ -754,13 +755,20 @@ def main():
     e2e_steps = max(1, min(args.steps, 20))
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
+        s.step_exchange_ptr(1, ptrs, ptrs)
+    barrier()
+    e2e_s = slowest(time.perf_counter() - t0, world)
+    # the same exchange as three calls (set state, one step, get state: three synchronisations)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
         s.set_state_ptr(*ptrs)
         s.step(1)
         s.get_state_ptr(*ptrs)
     barrier()
-    e2e_s = slowest(time.perf_counter() - t0, world)
+    three_s = slowest(time.perf_counter() - t0, world)
     e2e = {"value": job_rate(Na * e2e_steps, world, e2e_s), "unit": UNIT, "h2d_bytes_per_step": 4 * Na * 8,
-           "d2h_bytes_per_step": 4 * Na * 8}
+           "d2h_bytes_per_step": 4 * Na * 8, "call": "sts_step_exchange",
+           "three_calls_value": job_rate(Na * e2e_steps, world, three_s)}
 
     # per-kernel device time over a few more real steps (the roofline's dominant kernel)
     pn, kms, kcnt = s.profile(max(3, min(args.steps, 10)))

@@ -135,6 +135,18 @@ int sts_set_field(sts_ctx* ctx, const char* name, const double* host_in);
 int sts_set_state(sts_ctx* ctx, const double* u_in, const double* v_in, const double* p_in, const double* T_in);
 int sts_get_state(sts_ctx* ctx, double* u_out, double* v_out, double* p_out, double* T_out);
 
+/* sts_set_state, sts_step and sts_get_state in one call, for a host loop that hands the library
+ * the state, advances it and takes it back every time (the three calls' results, bit for bit):
+ * the input move, the steps and the output move are queued on the context's stream and the call
+ * synchronises once, at the end, instead of three times.  The outputs take the direct kernel path
+ * when they are device-addressable host memory and the steps run as the step graph; otherwise
+ * (steps of the autotuner, use_graph 0, other host memory) the state is fetched after the steps as
+ * sts_get_state does.  Input and output buffers may be the same.  Returns sts_step's status; after
+ * STS_OK or STS_ERR_NONFINITE the outputs hold the state at the end of the steps taken. */
+int sts_step_exchange(sts_ctx* ctx, int nsteps, const double* u_in, const double* v_in, const double* p_in,
+                      const double* T_in, double* u_out, double* v_out, double* p_out, double* T_out,
+                      int* steps_done);
+
 /* Global conservation sums of the current state over the fluid cells, in FP64 on the device in a
  * fixed order (each row in chunks of 64 cells in x order, the chunks of a row in order, the rows in
  * y order), so the same state always gives the same bits: out5[0] mass sum rho A, [1] and [2]

@@ -1568,8 +1568,9 @@ __global__ void k_check_division(unsigned long long n, unsigned long long seed, 
 // The state exchange with host buffers the device can address (pinned or registered memory):
 // one grid-stride pass moves all four fields, so the four transfers share the host link at
 // once instead of queueing on the copy engines one after another.
-__global__ void k_move4(const double* __restrict__ a0, const double* __restrict__ a1, const double* __restrict__ a2,
-                        const double* __restrict__ a3, double* b0, double* b1, double* b2, double* b3, int n) {
+__device__ __forceinline__ void move4_body(const double* __restrict__ a0, const double* __restrict__ a1,
+                                           const double* __restrict__ a2, const double* __restrict__ a3, double* b0,
+                                           double* b1, double* b2, double* b3, int n) {
   // every pointer 16-byte aligned: pairs of doubles, two pairs of each array in flight per thread
   // (the host link needs many bytes in flight); otherwise one double at a time
   const bool vec = ((reinterpret_cast<uintptr_t>(a0) | reinterpret_cast<uintptr_t>(a1) |
@@ -1614,6 +1615,16 @@ __global__ void k_move4(const double* __restrict__ a0, const double* __restrict_
     b2[k] = a2[k];
     b3[k] = a3[k];
   }
+}
+__global__ void k_move4(const double* __restrict__ a0, const double* __restrict__ a1, const double* __restrict__ a2,
+                        const double* __restrict__ a3, double* b0, double* b1, double* b2, double* b3, int n) {
+  move4_body(a0, a1, a2, a3, b0, b1, b2, b3, n);
+}
+// The state u, v, p, T out to host buffers at the end of steps queued before it: the buffer with
+// the latest p-T iterate is the one the device recorded (the host has not read it yet).
+__global__ void k_move4_state_out(Geo g, double* b0, double* b1, double* b2, double* b3) {
+  const unsigned cur = *(volatile const unsigned*)&g.ctl->cur;
+  move4_body(g.u, g.v, g.p[cur], g.T[cur], b0, b1, b2, b3, g.Na);
 }
 
 // FP64 throughput of the device: every thread advances 8 independent chains `iters` times with

@@ -84,6 +84,7 @@ __global__ void k_cons_final(int Ny, int nch, const double* part, double* rows, 
 __global__ void k_fp64_rate(int op, int iters, double c_mul, double c_add, double* out);
 __global__ void k_move4(const double* a0, const double* a1, const double* a2, const double* a3, double* b0,
                         double* b1, double* b2, double* b3, int n);
+__global__ void k_move4_state_out(Geo g, double* b0, double* b1, double* b2, double* b3);
 // precision modes 1 and 2
 __global__ void k_assemble_fast(Geo g, unsigned long long h_sweep, int in_graph);
 __global__ void k_flux_diff_fast(Geo g, unsigned tail);

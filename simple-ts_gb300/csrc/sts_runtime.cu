@@ -268,7 +268,7 @@ struct sts_ctx {
   int write_drag();
   int continuity();
   int step_host(int n, int* done);
-  int step_graph(int n, int* done);
+  int step_graph(int n, int* done, double* const* state_out = nullptr);
   int write_outputs(bool wait_files);
   int wait_outputs();
   int write_logs(bool iterations = true);
@@ -382,13 +382,18 @@ int sts_ctx::build_graph() {
   return STS_OK;
 }
 
-int sts_ctx::step_graph(int n, int* done) {
+int sts_ctx::step_graph(int n, int* done, double* const* state_out) {
   if (!exec)
     if (int r = build_graph()) return r;
   const unsigned before = h_ctl->it_counter;
   unsigned left = (unsigned)n;
   CU(cudaMemcpyAsync(&d_ctl->steps_left, &left, sizeof(unsigned), cudaMemcpyHostToDevice, s));
   CU(cudaGraphLaunch(exec, s));
+  if (state_out) {  // the new state straight to device-addressable host buffers, before the one sync
+    k_move4_state_out<<<std::max(1, std::min((g.Na + 255) / 256, 4 * std::max(sms, 1))), 256, 0, s>>>(
+        g, state_out[0], state_out[1], state_out[2], state_out[3]);
+    CU(cudaGetLastError());
+  }
   if (int r = read_ctl()) return r;
   *done = (int)(h_ctl->it_counter - before);
   return STS_OK;
@@ -1219,9 +1224,12 @@ int sts_open_case(const char* case_dir, const sts_options* opt, sts_ctx** out) {
   return open_impl(case_dir, &o, out);
 }
 
-int sts_step(sts_ctx* ctx, int nsteps, int* steps_done) {
-  if (!ctx || nsteps < 0) return fail(STS_ERR_ARG, "bad argument");
-  if (ctx->in_batch) return fail(STS_ERR_ARG, "the case belongs to a batch: step it with sts_batch_step");
+// sts_step; with state_out (device addresses of host buffers), the graph launch is followed by the
+// move of the new state into those buffers before its synchronisation, and *moved says whether
+// that happened (the autotuner's steps, launched one by one, or a run that had ended, leave it to
+// the caller).
+static int step_impl(sts_ctx* ctx, int nsteps, int* steps_done, double* const* state_out, bool* moved) {
+  if (moved) *moved = false;
   int done = 0;
   if (!ctx->finished && nsteps > 0) {
     CU(cudaSetDevice(ctx->opt.device));
@@ -1236,8 +1244,9 @@ int sts_step(sts_ctx* ctx, int nsteps, int* steps_done) {
     }
     if (done < nsteps && !ctx->finished && !(ctx->h_ctl->status & ~status_before & (ST_BARRIER_TIMEOUT | ST_NONFINITE))) {
       int d = 0;
-      int r = ctx->opt.use_graph ? ctx->step_graph(nsteps - done, &d) : ctx->step_host(nsteps - done, &d);
+      int r = ctx->opt.use_graph ? ctx->step_graph(nsteps - done, &d, state_out) : ctx->step_host(nsteps - done, &d);
       if (r) return r;
+      if (ctx->opt.use_graph && state_out && moved) *moved = true;
       done += d;
     }
     if (!ctx->h_ctl->continue_step) ctx->finished = true;
@@ -1252,6 +1261,12 @@ int sts_step(sts_ctx* ctx, int nsteps, int* steps_done) {
   }
   if (steps_done) *steps_done = done;
   return STS_OK;
+}
+
+int sts_step(sts_ctx* ctx, int nsteps, int* steps_done) {
+  if (!ctx || nsteps < 0) return fail(STS_ERR_ARG, "bad argument");
+  if (ctx->in_batch) return fail(STS_ERR_ARG, "the case belongs to a batch: step it with sts_batch_step");
+  return step_impl(ctx, nsteps, steps_done, nullptr, nullptr);
 }
 
 int sts_step_timed(sts_ctx* ctx, int nsteps, int* steps_done, double* device_ms) {
@@ -1367,11 +1382,9 @@ static bool mapped_host(const void* const* ptrs, void** dev, int n) {
 // 256-thread CTAs, at most four per multiprocessor (a grid-stride pass covers the rest)
 static int move_grid(int n, int sms) { return std::max(1, std::min((n + 255) / 256, 4 * std::max(sms, 1))); }
 
-int sts_set_state(sts_ctx* ctx, const double* u_in, const double* v_in, const double* p_in, const double* T_in) {
-  if (!ctx || !u_in || !v_in || !p_in || !T_in) return fail(STS_ERR_ARG, "null argument");
-  CU(cudaSetDevice(ctx->opt.device));
-  if (ctx->in_batch)
-    if (int r = ctx->read_ctl()) return r;
+// sts_set_state's work queued on the context's stream, without its synchronisation.
+static int set_state_queue(sts_ctx* ctx, const double* u_in, const double* v_in, const double* p_in,
+                           const double* T_in) {
   const Geo& g = ctx->g;
   const unsigned cur = ctx->h_ctl->cur;
   const size_t bytes = sizeof(double) * g.Na;
@@ -1391,6 +1404,15 @@ int sts_set_state(sts_ctx* ctx, const double* u_in, const double* v_in, const do
     static const unsigned zero = 0;
     CU(cudaMemcpyAsync(&g.ctl->warm_ready, &zero, sizeof(unsigned), cudaMemcpyHostToDevice, ctx->s));
   }
+  return STS_OK;
+}
+
+int sts_set_state(sts_ctx* ctx, const double* u_in, const double* v_in, const double* p_in, const double* T_in) {
+  if (!ctx || !u_in || !v_in || !p_in || !T_in) return fail(STS_ERR_ARG, "null argument");
+  CU(cudaSetDevice(ctx->opt.device));
+  if (ctx->in_batch)
+    if (int r = ctx->read_ctl()) return r;
+  if (int r = set_state_queue(ctx, u_in, v_in, p_in, T_in)) return r;
   CU(cudaStreamSynchronize(ctx->s));
   return STS_OK;
 }
@@ -1417,6 +1439,28 @@ int sts_get_state(sts_ctx* ctx, double* u_out, double* v_out, double* p_out, dou
   }
   CU(cudaStreamSynchronize(ctx->s));
   return STS_OK;
+}
+
+int sts_step_exchange(sts_ctx* ctx, int nsteps, const double* u_in, const double* v_in, const double* p_in,
+                      const double* T_in, double* u_out, double* v_out, double* p_out, double* T_out,
+                      int* steps_done) {
+  if (!ctx || nsteps < 0 || !u_in || !v_in || !p_in || !T_in || !u_out || !v_out || !p_out || !T_out)
+    return fail(STS_ERR_ARG, "bad argument");
+  if (ctx->in_batch) return fail(STS_ERR_ARG, "the case belongs to a batch: step it with sts_batch_step");
+  if (steps_done) *steps_done = 0;
+  CU(cudaSetDevice(ctx->opt.device));
+  const void* hout[4] = {u_out, v_out, p_out, T_out};
+  void* dout[4];
+  const bool direct = mapped_host(hout, dout, 4);
+  if (int r = set_state_queue(ctx, u_in, v_in, p_in, T_in)) return r;
+  bool moved = false;
+  const int r = step_impl(ctx, nsteps, steps_done, direct ? (double* const*)dout : nullptr, &moved);
+  if (r != STS_OK && r != STS_ERR_NONFINITE) return r;
+  if (!moved) {
+    CU(cudaStreamSynchronize(ctx->s));  // the inputs are read (a run that had ended takes no step)
+    if (int q = sts_get_state(ctx, u_out, v_out, p_out, T_out)) return q;
+  }
+  return r;
 }
 
 int sts_dims(sts_ctx* ctx, int* Nx, int* Ny) {

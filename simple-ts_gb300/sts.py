@@ -31,6 +31,7 @@ EXPORTS = [
     "sts_pt_sweeps_noalloc", "sts_check_division", "sts_fp64_rates", "sts_open_batch", "sts_batch_step", "sts_batch_step_timed",
     "sts_batch_case", "sts_batch_destroy", "sts_check_double_float", "sts_write_outputs_async",
     "sts_wait_outputs", "sts_autotune_result", "sts_set_state", "sts_get_state", "sts_batch_autotune_result",
+    "sts_step_exchange",
 ]
 
 KERNELS = ["step_begin", "assemble", "sweep_loop", "correct", "face_rho", "boundary", "flux_diff", "step_end"]
@@ -85,6 +86,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     lib.sts_autotune_result.argtypes = [P, ip, ip, ip, ip]
     lib.sts_set_state.argtypes = [P, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.sts_get_state.argtypes = [P, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.sts_step_exchange.argtypes = [P, C.c_int] + [C.c_void_p] * 8 + [C.POINTER(C.c_int)]
     lib.sts_run_case.argtypes = [C.c_char_p, C.POINTER(Options)]
     lib.sts_sync.argtypes = [P]
     lib.sts_destroy.argtypes = [P]
@@ -264,6 +266,13 @@ class Solver:
     def get_state_ptr(self, u, v, p, T):
         """u, v, p, T to raw host pointers (Nx*Ny doubles each) in one call."""
         _check(load().sts_get_state(self._h, u, v, p, T))
+
+    def step_exchange_ptr(self, n: int, ins, outs) -> int:
+        """u, v, p, T in from raw host pointers, n steps, u, v, p, T out to raw host pointers, with
+        one synchronisation (sts_step_exchange); returns the steps taken."""
+        done = C.c_int()
+        _check(load().sts_step_exchange(self._h, int(n), *ins, *outs, C.byref(done)))
+        return done.value
 
     def autotune_result(self) -> dict:
         """Launch shapes in use: tuning steps still to come, sweep-loop CTAs per SM, assembly block."""

@@ -216,6 +216,51 @@ def test_nonfinite_residual_is_reported(lib_built):
 
 
 @pytest.mark.parametrize("memory", ["pageable", "pinned"])
+@pytest.mark.parametrize("autotune", [False, True], ids=["fixed_shapes", "autotuned"])
+def test_step_exchange_equals_three_calls(memory, autotune, lib_built):
+    """sts_step_exchange gives the bits of sts_set_state + sts_step + sts_get_state: over several
+    calls, with separate and with the same input and output buffers, from the autotuner's first
+    steps (launched one by one) on, and with no steps at all."""
+    import sts
+    case = sc.channel_case("c", 80, 10, 0.3, 0.002, 1e-3, 80)
+    keep = []
+
+    def bufs(ny, nx):
+        if memory == "pinned":
+            torch = pytest.importorskip("torch")
+            ts = [torch.empty((ny, nx), dtype=torch.float64).pin_memory() for _ in range(4)]
+            keep.append(ts)
+            return [t.numpy() for t in ts]
+        return [np.empty((ny, nx)) for _ in range(4)]
+
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        a = sts.Solver(d, fixed_sweeps=False, autotune=autotune)
+        b = sts.Solver(d, fixed_sweeps=False, autotune=autotune)
+        assert a.step(2) == b.step(2) == 2
+        ins, outs = bufs(a.Ny, a.Nx), bufs(a.Ny, a.Nx)
+        a.get_state_ptr(*[x.ctypes.data for x in ins])
+        for rnd, n in enumerate((3, 4, 0, 5, 4)):
+            ins[2] *= 1.0 + 1e-7  # a slightly different state goes in every time
+            b_in = [x.copy() for x in ins]
+            b_out = [np.empty_like(x) for x in ins]
+            b.set_state_ptr(*[x.ctypes.data for x in b_in])
+            assert b.step(n) == n
+            b.get_state_ptr(*[x.ctypes.data for x in b_out])
+            o = ins if rnd % 2 else outs
+            assert a.step_exchange_ptr(n, [x.ctypes.data for x in ins], [x.ctypes.data for x in o]) == n
+            for f, x, y in zip(("u", "v", "p", "T"), o, b_out):
+                np.testing.assert_array_equal(x, y, err_msg=f"{f} round {rnd}")
+            for f in ("u", "v", "p", "T", "rho"):
+                np.testing.assert_array_equal(a.field(f), b.field(f), err_msg=f"{f} round {rnd}")
+            if o is outs:
+                for x, y in zip(ins, outs):
+                    x[...] = y
+        a.close()
+        b.close()
+
+
+@pytest.mark.parametrize("memory", ["pageable", "pinned"])
 def test_state_exchange_equals_field_calls(memory, lib_built):
     """sts_get_state / sts_set_state move the same bytes as four get/set_field calls, and a run
     continued from a state set either way is the same run.  Pinned host buffers take the
