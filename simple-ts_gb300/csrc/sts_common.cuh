@@ -187,6 +187,9 @@ struct Geo {
   // and fluid masks), computed once by k_flux_quotients with the divisions of the per-step
   // form: [0] D_ux, [1] D_uy, [2] D_vx, [3] D_vy, [4] DTx, [5] DTy
   const double* fq[6];
+  // hx[i] hy[j] per cell (static; the product the sweeps would form, the same bits), also filled
+  // by k_flux_quotients
+  const double* hxy;
   // --- precision modes 1 and 2 ---
   // FP32 correction sweeps: coefficients c[0..4] of the T correction, a[0..3] of the p
   // numerator, the base-sweep values T1, H/T1, p1, Den and the defects dT, dp; e_p/e_T are the

@@ -504,8 +504,9 @@ __global__ void kb_assemble(const Geo* gs, unsigned long long h_sweep, int in_gr
 // Invariants: a_k = aT_k, or aT_k * T_wall for a wall neighbour (the bc form multiplies the
 // wall temperature by aT_k and adds exact zeros), divu, the T denominator, the p_pr/T_pr
 // term and ht * (sum of the p coefficients).
-// RCP: the first sweep also stores RN(1/den_T) in inv[8] and later sweeps divide by den_T through
-// it (div_cr, the same bits as the IEEE quotient).
+// RCP (the persistent loop): the first sweep also stores RN(1/den_T) in inv[8] and later sweeps
+// divide by den_T through it (div_cr, the same bits as the IEEE quotient) and read hx hy from the
+// per-cell table instead of multiplying.
 template <bool FIRST, bool RCP = false>
 __device__ __forceinline__ void sweep_cell(const Geo& g, const Cell& c, const double* __restrict__ P,
                                            const double* __restrict__ TT, double* __restrict__ pn,
@@ -598,7 +599,8 @@ __device__ __forceinline__ void sweep_cell(const Geo& g, const Cell& c, const do
       const double gxe = ((g.bits & F_GIVEN_U_XE) && i == g.Nx_o1 - 1) ? 1.0 : 0.0;
       num = num + gxb * Fx[d.ij] - gxe * Fx[d.i1j];
     }
-    pnew = (ht * num + g.inv[6][ij]) / (g.inv[7][ij] + hx[i] * hy[j] / (Tnew));
+    const double H = RCP ? g.hxy[ij] : hx[i] * hy[j];  // the persistent loop reads the stored product
+    pnew = (ht * num + g.inv[6][ij]) / (g.inv[7][ij] + H / (Tnew));
   }
   Tn[ij] = Tnew;
   pn[ij] = pnew;
@@ -824,6 +826,7 @@ __global__ void k_flux_quotients(Geo g) {
   double q[6];
   flux_quotients(g, c.i, c.j, q);
   for (int k = 0; k < 6; k++) const_cast<double*>(g.fq[k])[c.ij] = q[k];
+  const_cast<double*>(g.hxy)[c.ij] = g.hx[c.i] * g.hy[c.j];
 }
 
 // ly, lx: the block's staged interpolations (null when the block is not 32x8)

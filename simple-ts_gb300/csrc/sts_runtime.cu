@@ -1050,10 +1050,11 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
     g.r3x = t[6]; g.r3y = t[7];
     g.rht = 1.0 / g.ht;
     g.r3 = 1.0 / 3.0;
-    for (int k = 0; k < 6; k++) {  // filled by k_flux_quotients before the first flux kernel
+    for (int k = 0; k < 7; k++) {  // filled by k_flux_quotients before the first flux kernel
       double* q = nullptr;
       if (int r = c->alloc(&q, Na)) return r;
-      g.fq[k] = q;
+      if (k < 6) g.fq[k] = q;
+      else g.hxy = q;
     }
   }
   // warm_start 5 is warm_start 4 on the device plus the network's kernels
