@@ -602,16 +602,29 @@ def network_run(d, local, steps, flush, barrier, lead=60, train_iters=300, lr=3e
     train_s = time.perf_counter() - t0
     loss_net, loss_zero = v.warm_net_eval()
     v.warm_net_enable(True)
+    gate0 = v.warm_net_gate()
     vd, vms, vsw = timed_steps(v, steps, warmup, flush, barrier)
     info = v.warm_net_info()
+    gate1 = v.warm_net_gate()
     out = {"value": v.Nx * v.Ny * vd / (vms / 1e3), "ms_per_step": vms / max(vd, 1),
            "sweeps_per_step": float(np.mean(vsw)) if len(vsw) else 0.0,
-           "untimed_steps": lead + v.steps_before_timing, "training": {
+           "untimed_steps": lead + v.steps_before_timing,
+           "steps_with_correction": {f: gate1[f] - gate0[f] for f in ("p", "T")},  # of the warm-up and timed steps
+           "steps_gated": v.steps_before_timing + vd,
+           "training": {
                "pairs": min(info["pairs"], 256), "window": info["window"], "params": info["params"],
                "iters": train_iters, "seconds": round(train_s, 3), "loss_network": loss_net,
                "loss_zero_correction": loss_zero}}
     fields = {f: v.field(f) for f in ("u", "v", "p", "T", "rho")}
+    total = lead + v.steps_before_timing + vd
     v.close()
+    # the stencil alone (warm_start 4: the same run with the network switched off) over the same
+    # steps, for the sweeps the network's correction saves or adds
+    ref = sts.Solver(d, fixed_sweeps=False, device=local, precision=sts.MIXED_DF, warm_start=4)
+    ref.step(total)
+    rsw = ref.sweep_history()[-vd:] if vd else []
+    ref.close()
+    out["stencil_sweeps_same_steps"] = float(np.mean(rsw)) if len(rsw) else 0.0
     return out, fields
 
 
@@ -679,6 +692,8 @@ def metric_config_bench(args, local, flush, barrier):
                             "fp64_learned_vs_fp64_quadratic": gain("fp64_learned", "fp64_quadratic")}
         if "fp32df_network" in row:
             out[f"ma{mach}"]["network_vs_stencil"] = gain("fp32df_network", "fp32df_learned")
+            out[f"ma{mach}"]["network_vs_stencil"]["sweep_ratio_same_steps"] = (
+                row["fp32df_network"]["stencil_sweeps_same_steps"] / max(row["fp32df_network"]["sweeps_per_step"], 1e-30))
     return {"workload": "channel 2048x256 with the square, Kn 0.003, dt 1.25e-4, tolerance 1e-8",
             "timed_steps": args.c5_steps, "untimed_steps_warm": args.c5_lead, "by_mach": out}
 

@@ -251,6 +251,11 @@ int sts_warm_net_eval(sts_ctx* ctx, float* loss_net, float* loss_zero);
 int sts_warm_net_enable(sts_ctx* ctx, int on);
 /* warm_start 5: training pairs stored so far, the window's size and the network's parameter count. */
 int sts_warm_net_info(sts_ctx* ctx, int* pairs, int* win_h, int* win_w, long long* nparams);
+/* warm_start 5: steps whose window took the network's correction of p and of T so far.  The
+ * correction of p is applied on a step's window only if, on the window completed at that step, it
+ * had left a smaller largest error than the stencil's own start (the sweep count follows the
+ * largest error of the start); the correction of T is not applied. */
+int sts_warm_net_gate(sts_ctx* ctx, int* steps_on_p, int* steps_on_T);
 /* warm_start 5: the network's FP32 parameters (layout of sts_net_get_params) out and/or in (NULL to skip). */
 int sts_warm_net_params(sts_ctx* ctx, float* out, const float* in);
 

@@ -1796,6 +1796,17 @@ int sts_warm_net_info(sts_ctx* ctx, int* pairs, int* win_h, int* win_w, long lon
   return STS_OK;
 }
 
+int sts_warm_net_gate(sts_ctx* ctx, int* steps_on_p, int* steps_on_T) {
+  if (!ctx || !ctx->warm_net) return fail(STS_ERR_ARG, "the context does not use warm_start 5");
+  CU(cudaSetDevice(ctx->opt.device));
+  NetState h{};
+  CU(cudaMemcpyAsync(&h, ctx->d_ns, sizeof(NetState), cudaMemcpyDeviceToHost, ctx->s));
+  CU(cudaStreamSynchronize(ctx->s));
+  if (steps_on_p) *steps_on_p = (int)h.steps_on[0];
+  if (steps_on_T) *steps_on_T = (int)h.steps_on[1];
+  return STS_OK;
+}
+
 int sts_warm_net_params(sts_ctx* ctx, float* out, const float* in) {
   if (!ctx || !ctx->warm_net) return fail(STS_ERR_ARG, "the context does not use warm_start 5");
   CU(cudaSetDevice(ctx->opt.device));

@@ -18,7 +18,12 @@
 //     predicted change S over the same), S and the flags, into the inference buffer and the slot;
 //   k_net_commit (one thread): the window's origin;
 //   the U-Net forward on the inference buffer (a child graph);
-//   k_net_apply: where the network is enabled, cnext += s * output on the window's flagged cells.
+//   k_net_apply: where the network is enabled, cnext += s * output on the window's flagged cells,
+//     field by field, if on the window completed this step the network's correction had left a
+//     smaller largest error than the stencil's own (the gate: the sweep count follows the largest
+//     error of the start, and consecutive windows of a front are alike; T's gate stays shut, see
+//     kNetGateMarginT).  k_net_target measures both on that window from its target and the output
+//     still held from its forward pass.
 // Training (sts_warm_net_train) draws batches of completed slots from the ring between steps.
 #include <cuda_runtime.h>
 
@@ -34,26 +39,40 @@ __global__ void k_net_target(Geo g, NetState* ns, NetBuffers nb) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (!ns->have_win) return;
   const unsigned r = g.ctl->warm_ready;
-  float e[kNetOut] = {0.f, 0.f};
+  float e[kNetOut] = {0.f, 0.f}, es[kNetOut] = {0.f, 0.f}, en[kNetOut] = {0.f, 0.f};
   if (k < H * W) {
     const int i = ns->i0 + k % W, j = ns->j0 + k / W, n = i + j * g.Nx;
     float* tgt = nb.replay + (size_t)ns->slot * nb.slot_floats + (size_t)H * W * kNetIn;
     float* wp = tgt + (size_t)H * W * kNetOut + k;
     const float* S = tgt + (size_t)H * W * (kNetOut + 1);
+    const bool flagged = *wp > 0.f;
     bool outlier = false;
     for (int f = 0; f < kNetOut; f++) {
-      const float err = *wp > 0.f ? g.cD[f][r % kConvRing][n] - S[(size_t)k * kNetOut + f] : 0.f;
+      const float err = flagged ? g.cD[f][r % kConvRing][n] - S[(size_t)k * kNetOut + f] : 0.f;
       const float t = err / ns->s[f];
       outlier = outlier || !(fabsf(t) <= kNetTargetClip);
       tgt[(size_t)k * kNetOut + f] = fminf(fmaxf(t, -kNetTargetClip), kNetTargetClip);
       e[f] = fabsf(err);
+      if (flagged) {  // the gate's errors: the network's output for this window is still in infer_out
+        const float o = fminf(fmaxf(nb.infer_out[(size_t)k * kNetOut + f], -kNetTargetClip), kNetTargetClip);
+        es[f] = fabsf(t);
+        en[f] = fabsf(t - o);
+      }
     }
     if (outlier) *wp = 0.f;  // a pixel far outside the window's scale is left out of training
   }
   for (int f = 0; f < kNetOut; f++) {
-    unsigned v = __float_as_uint(e[f]);
-    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if ((threadIdx.x & 31) == 0 && v) atomicMax(&ns->err_bits[f], v);
+    unsigned v = __float_as_uint(e[f]), a = __float_as_uint(es[f]), b = __float_as_uint(en[f]);
+    for (int o = 16; o > 0; o >>= 1) {
+      v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+      a = max(a, __shfl_xor_sync(0xffffffffu, a, o));
+      b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      if (v) atomicMax(&ns->err_bits[f], v);
+      if (a) atomicMax(&ns->gate_es[f], a);
+      if (b) atomicMax(&ns->gate_en[f], b);
+    }
   }
 }
 
@@ -70,6 +89,12 @@ __global__ void k_net_head(Geo g, NetState* ns, int slots) {
     const float e = ns->have_win ? __uint_as_float(ns->err_bits[f]) : 0.f;
     ns->s[f] = fmaxf(e, kNetScaleFloor * ns->m[f]);
     ns->err_bits[f] = 0u;
+    // the gate (non-negative floats order like their bit patterns; NaN never passes)
+    const unsigned a = ns->gate_es[f], b = ns->gate_en[f];
+    ns->gate[f] = (ns->have_win && a != 0u && a < 0x7f800000u && b < 0x7f800000u &&
+                   __uint_as_float(b) < (f ? kNetGateMarginT : kNetGateMarginP) * __uint_as_float(a)) ? 1u : 0u;
+    ns->gate_es[f] = 0u;
+    ns->gate_en[f] = 0u;
   }
   ns->argmax = 0xffffffffu;
   ns->slot = (int)(ns->count % (unsigned)slots);
@@ -133,12 +158,14 @@ __global__ void k_net_commit(Geo g, NetState* ns, NetBuffers nb) {
 __global__ void k_net_apply(Geo g, NetState* ns, NetBuffers nb) {
   const int H = nb.H, W = nb.W;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k == 0 && ns->enabled)
+    for (int f = 0; f < kNetOut; f++) ns->steps_on[f] += ns->gate[f];
   if (k >= H * W || !ns->enabled || !(nb.infer_w[k] > 0.f)) return;
   const unsigned r = g.ctl->warm_ready;
   const int i = ns->i0 + k % W, j = ns->j0 + k / W, n = i + j * g.Nx;
   const uint8_t b = g.cact[r & 1][n];
   for (int f = 0; f < kNetOut; f++)
-    if ((b >> (2 + f)) & 1u) {
+    if (((b >> (2 + f)) & 1u) && ns->gate[f]) {
       const float o = fminf(fmaxf(nb.infer_out[(size_t)k * kNetOut + f], -kNetTargetClip), kNetTargetClip);
       g.cnext[f][n] += (double)(ns->s[f] * o);
     }

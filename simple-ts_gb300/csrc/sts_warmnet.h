@@ -7,6 +7,10 @@ namespace sts {
 constexpr int kNetIn = 8, kNetOut = 2;
 constexpr float kNetScaleFloor = 1e-4f;  // smallest target scale, relative to the step change's maximum
 constexpr float kNetTargetClip = 8.f;    // targets (and outputs) beyond this many scales are clipped
+// the gate opens for p (T) when the network left less than this fraction of the stencil's
+// largest error on the window completed last; T's stays shut (on the 2048x256 and 1200x120
+// channels its correction added sweeps wherever it opened)
+constexpr float kNetGateMarginP = 1.0f, kNetGateMarginT = 0.0f;
 
 // Device-side bookkeeping of the window and the replay ring.
 struct NetState {
@@ -19,6 +23,12 @@ struct NetState {
   float m[kNetOut];           // input scale of the window: max |D_r| per field
   float s[kNetOut];           // target and output scale of the window
   unsigned enabled;           // apply the network's correction
+  // the gate: on the completed window, the largest stencil error |t| and the largest error left
+  // after the network's correction |t - o| over its flagged cells (scaled, float bits); the
+  // coming window takes field f's correction only if the latter was the smaller
+  unsigned gate_es[kNetOut], gate_en[kNetOut];
+  unsigned gate[kNetOut];
+  unsigned steps_on[kNetOut];  // steps whose window took field f's correction
 };
 
 // Buffers: the replay ring of `slots` records of slot_floats floats each (per window pixel: 8

@@ -31,7 +31,7 @@ EXPORTS = [
     "sts_pt_sweeps_noalloc", "sts_check_division", "sts_fp64_rates", "sts_open_batch", "sts_batch_step", "sts_batch_step_timed",
     "sts_batch_case", "sts_batch_destroy", "sts_check_double_float", "sts_write_outputs_async",
     "sts_wait_outputs", "sts_autotune_result", "sts_set_state", "sts_get_state", "sts_batch_autotune_result",
-    "sts_step_exchange",
+    "sts_step_exchange", "sts_warm_net_gate",
 ]
 
 KERNELS = ["step_begin", "assemble", "sweep_loop", "correct", "face_rho", "boundary", "flux_diff", "step_end"]
@@ -221,6 +221,14 @@ class Solver:
         n = C.c_longlong()
         _check(lib.sts_warm_net_info(self._h, *[C.byref(x) for x in v], C.byref(n)))
         return {"pairs": v[0].value, "window": (v[1].value, v[2].value), "params": n.value}
+
+    def warm_net_gate(self) -> dict:
+        """Steps whose window took the network's correction of p and of T (sts_warm_net_gate)."""
+        lib = load()
+        lib.sts_warm_net_gate.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        a, b = C.c_int(), C.c_int()
+        _check(lib.sts_warm_net_gate(self._h, C.byref(a), C.byref(b)))
+        return {"p": a.value, "T": b.value}
 
     def warm_net_params(self, new=None) -> np.ndarray:
         """The network's FP32 parameters; with `new`, sets them (returning the old ones)."""

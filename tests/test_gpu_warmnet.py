@@ -6,7 +6,9 @@
 * Trained on the supersonic channel's own pairs, the network's loss falls; switched on, the run
   still converges to the same tolerance (fields within the tolerance-level distance of the cold
   start), and the sweep counts of the stencil alone and of the stencil with the network are
-  printed side by side over the same steps.
+  printed side by side over the same steps.  The correction of p is gated (applied on a step's
+  window only where, on the window completed last, it had lowered the stencil's largest error),
+  so it adds sweeps rarely; T's correction is not applied.
 """
 import tempfile
 
@@ -61,6 +63,10 @@ def test_network_trains_on_solver_pairs_and_keeps_tolerance(lib_built, oracle_bu
               f"sweeps per step over steps 81-120: "
               f"stencil {s4.mean():.3f}, stencil + network {s5.mean():.3f}, cold {cold.sweeps()[80:120].mean():.3f}")
         assert after < before and after < zero
+        gate = net.warm_net_gate()  # the steps whose window took the correction (p only)
+        print(f"steps with the network's correction of p: {gate['p']} of 40")
+        assert 0 <= gate["p"] <= 40 and gate["T"] == 0
+        assert s5.mean() <= s4.mean() + 0.25  # the gate keeps corrections that add sweeps rare
         for f in ("p", "T"):
             e = np.linalg.norm(net.field(f) - cold.field(f)) / np.linalg.norm(cold.field(f))
             assert e < 1e-6, (f, e)
