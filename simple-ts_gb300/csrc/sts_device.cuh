@@ -20,6 +20,12 @@ __device__ __forceinline__ double Hi(double f1, double f2, double h1, double h2)
 __device__ __forceinline__ double as_d(unsigned long long b) { return __longlong_as_double((long long)b); }
 __device__ __forceinline__ unsigned long long as_b(double d) { return (unsigned long long)__double_as_longlong(d); }
 
+// Kernels that the step graph launches before their predecessor has completed (a programmatic
+// dependency: launched once every CTA of the predecessor has finished) wait here, before their
+// first access to memory, until the predecessor has completed and its writes are visible.
+// Launched any other way the wait returns at once.
+__device__ __forceinline__ void wait_for_predecessor() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // The IEEE quotient, out of line: the rare operands div_cr cannot take branch here instead of
 // being evaluated (predicated) beside every fast division.
 __device__ __noinline__ double div_ieee(double a, double b) { return __ddiv_rn(a, b); }

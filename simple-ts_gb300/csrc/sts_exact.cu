@@ -714,7 +714,10 @@ __device__ __forceinline__ void correct_body(const Geo& g) {
   }
   block_max2(ru, rv, &ctl->res_bits_u, &ctl->res_bits_v, &ctl->status);
 }
-__global__ void k_correct(Geo g) { correct_body(g); }
+__global__ void k_correct(Geo g) {
+  wait_for_predecessor();
+  correct_body(g);
+}
 __global__ void kb_correct(const Geo* gs) {
   __shared__ Geo sg;
   if (!stage_geo(sg, gs)) return;
@@ -738,7 +741,10 @@ __device__ __forceinline__ void face_rho_body(const Geo& g) {
   g.rho_u[d.ij] = ru;
   g.rho_v[d.ij] = rv;
 }
-__global__ void k_face_rho(Geo g) { face_rho_body(g); }
+__global__ void k_face_rho(Geo g) {
+  wait_for_predecessor();
+  face_rho_body(g);
+}
 __global__ void kb_face_rho(const Geo* gs) {
   __shared__ Geo sg;
   if (!stage_geo(sg, gs)) return;
@@ -928,7 +934,10 @@ __device__ __forceinline__ void flux_diff_body(const Geo& g, unsigned tail) {
     if (tail & PH_PRES) phase_pres(g, g.p[cur], tid, nt);
   }
 }
-__global__ void k_flux_diff(Geo g, unsigned tail) { flux_diff_body(g, tail); }
+__global__ void k_flux_diff(Geo g, unsigned tail) {
+  wait_for_predecessor();
+  flux_diff_body(g, tail);
+}
 __global__ void kb_flux_diff(const Geo* gs, unsigned tail) {
   __shared__ Geo sg;
   if (!stage_geo(sg, gs)) return;
@@ -1412,6 +1421,7 @@ __device__ __forceinline__ void bnd_fused_body(const Geo& g, unsigned long long 
   }
 }
 __global__ void k_bnd_fused(Geo g, unsigned long long h_outer, int in_graph, int jump_beside) {
+  wait_for_predecessor();
   bnd_fused_body(g, h_outer, in_graph, jump_beside);
 }
 __global__ void kb_bnd_fused(const Geo* gs, unsigned long long h_outer, int in_graph, int jump_beside) {

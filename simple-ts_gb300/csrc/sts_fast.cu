@@ -224,7 +224,10 @@ __device__ __forceinline__ void flux_diff_t(const Geo& g, unsigned tail) {
   }
 }
 __device__ __forceinline__ void flux_diff_fast_body(const Geo& g, unsigned tail) { flux_diff_t<double>(g, tail); }
-__global__ void k_flux_diff_fast(Geo g, unsigned tail) { flux_diff_fast_body(g, tail); }
+__global__ void k_flux_diff_fast(Geo g, unsigned tail) {
+  wait_for_predecessor();
+  flux_diff_fast_body(g, tail);
+}
 __global__ void kb_flux_diff_fast(const Geo* gs, unsigned tail) {
   __shared__ Geo sg;
   if (!stage_geo(sg, gs)) return;
@@ -705,7 +708,10 @@ __global__ void __launch_bounds__(256, 3) kb_assemble_df(const Geo* gs, unsigned
   if (!stage_geo(sg, gs, blockIdx.z / 3)) return;
   assemble_df_part(sg, h_sweep, in_graph, blockIdx.z % 3);
 }
-__global__ void __launch_bounds__(256, 4) k_flux_diff_df(Geo g, unsigned tail) { flux_diff_t<df>(g, tail); }
+__global__ void __launch_bounds__(256, 4) k_flux_diff_df(Geo g, unsigned tail) {
+  wait_for_predecessor();
+  flux_diff_t<df>(g, tail);
+}
 __global__ void __launch_bounds__(256, 4) kb_flux_diff_df(const Geo* gs, unsigned tail) {
   __shared__ Geo sg;
   if (!stage_geo(sg, gs)) return;

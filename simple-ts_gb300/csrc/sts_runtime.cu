@@ -297,6 +297,21 @@ int add_kernel(cudaGraphNode_t* node, cudaGraph_t graph, const std::vector<cudaG
   return STS_OK;
 }
 
+// A programmatic edge between two kernel nodes: `to` is launched as soon as every CTA of `from`
+// has finished, and its kernel waits (wait_for_predecessor) for `from` to complete, writes
+// visible, before it touches memory, so the launch of `to` overlaps the completion of `from`.
+// (Launching `to` once every CTA of `from` has begun, cudaGraphKernelNodePortLaunchCompletion,
+// measured slower: its waiting CTAs hold resources the predictor's kernels beside them need.)
+constexpr unsigned char kPdlPort = cudaGraphKernelNodePortProgrammatic;
+int add_pdl_edge(cudaGraph_t graph, cudaGraphNode_t from, cudaGraphNode_t to) {
+  cudaGraphEdgeData e{};
+  e.from_port = kPdlPort;
+  e.to_port = 0;
+  e.type = cudaGraphDependencyTypeProgrammatic;
+  CU(cudaGraphAddDependencies(graph, &from, &to, &e, 1));
+  return STS_OK;
+}
+
 int add_while(cudaGraphNode_t* node, cudaGraph_t graph, const std::vector<cudaGraphNode_t>& deps,
               cudaGraphConditionalHandle h, cudaGraph_t* body) {
   cudaGraphNodeParams cp{};
@@ -355,7 +370,10 @@ int sts_ctx::build_graph() {
     v.cooperative = 1;
     CU(cudaGraphKernelNodeSetAttribute(n_sw, cudaLaunchAttributeCooperative, &v));
   }
-  if (int r = add_kernel(&n_cor, b_outer, {n_sw}, k_correct, grid, block, g)) return r;
+  // correct -> face_rho -> boundary -> flux_diff, each launched as soon as its predecessor's CTAs
+  // have all finished (programmatic edges; every one of these kernels waits before touching memory)
+  if (int r = add_kernel(&n_cor, b_outer, {}, k_correct, grid, block, g)) return r;
+  if (int r = add_pdl_edge(b_outer, n_sw, n_cor)) return r;
   if (g.warm_start == 4) {  // the fit and the next step's start, beside the step's last kernels
     cudaGraphNode_t w[4];
     if (int r = add_kernel(&w[0], b_outer, {n_sw}, k_conv_gram, grid, block, g)) return r;
@@ -369,13 +387,14 @@ int sts_ctx::build_graph() {
       CU(cudaStreamEndCapture(cap, &captured));
     }
   }
-  if (int r = add_kernel(&n_rho, b_outer, {n_cor}, k_face_rho, grid, block, g)) return r;
-  if (int r = add_kernel(&n_bnd, b_outer, {n_rho}, k_bnd_fused, bnd_grid(), dim3(256), g, (unsigned long long)ho, 1,
+  if (int r = add_kernel(&n_rho, b_outer, {}, k_face_rho, grid, block, g)) return r;
+  if (int r = add_pdl_edge(b_outer, n_cor, n_rho)) return r;
+  if (int r = add_kernel(&n_bnd, b_outer, {}, k_bnd_fused, bnd_grid(), dim3(256), g, (unsigned long long)ho, 1,
                          jump_beside() ? 1 : 0))
     return r;
-  if (int r = add_kernel(&n_fd, b_outer, {n_bnd}, flux_kernel(), grid, block, g,
-                         (unsigned)(PH_TEMP | PH_PRES)))
-    return r;
+  if (int r = add_pdl_edge(b_outer, n_rho, n_bnd)) return r;
+  if (int r = add_kernel(&n_fd, b_outer, {}, flux_kernel(), grid, block, g, (unsigned)(PH_TEMP | PH_PRES))) return r;
+  if (int r = add_pdl_edge(b_outer, n_bnd, n_fd)) return r;
   CU(cudaGraphInstantiate(&exec, graph, 0));
   h_step = hs;
   h_outer = ho;
