@@ -708,6 +708,49 @@ __global__ void __launch_bounds__(256, 3) kb_assemble_df(const Geo* gs, unsigned
   if (!stage_geo(sg, gs, blockIdx.z / 3)) return;
   assemble_df_part(sg, h_sweep, in_graph, blockIdx.z % 3);
 }
+// The velocity correction, sqrt(T) and the cell density of k_correct (SIMPLE_TS_MPI.cpp:4171-4330)
+// for precision mode 3: the same formulas with their FP64 arithmetic in double-float -- the
+// division p / T and the square root are what bind k_correct to GB300's FP64 unit -- and the
+// fields FP64 in memory.  The residuals |u_new - u| are taken between the stored FP64 values.
+__device__ __forceinline__ void correct_df_body(const Geo& g) {
+  Cell c = cell(g);
+  Ctl* ctl = g.ctl;
+  const unsigned cur = ctl->cur;
+  const double* __restrict__ p = g.p[cur];
+  const double* __restrict__ T = g.T[cur];
+  double ru = 0, rv = 0;
+  if (c.ok) {
+    const uint8_t cl = g.cls[c.ij];
+    const int n = c.ij;
+    const df pn = to_df(p[n]);
+    if (cls_u(cl)) {
+      const int w = (cls_u(cl) == CLS_BC && (g.bits & F_PERIODIC) && c.i == 0) ? n + g.Nx - 1 : n - 1;
+      const double t = g.u[n];
+      const double un = to_double(to_df(g.u_pseudo[n]) - (pn - to_df(p[w])) * to_df(g.d12[n]));
+      g.u[n] = un;
+      ru = fabs(un - t);
+    }
+    if (cls_v(cl)) {
+      const double t = g.v[n];
+      const double vn = to_double(to_df(g.v_pseudo[n]) - (pn - to_df(p[n - g.Nx])) * to_df(g.d34[n]));
+      g.v[n] = vn;
+      rv = fabs(vn - t);
+    }
+    const df Tn = to_df(T[n]);
+    g.sqrt_T[n] = to_double(dsqrt(Tn));
+    g.rho[n] = cls_fluid(cl) ? to_double(pn / Tn) : 0.0;
+  }
+  block_max2(ru, rv, &ctl->res_bits_u, &ctl->res_bits_v, &ctl->status);
+}
+__global__ void k_correct_df(Geo g) {
+  wait_for_predecessor();
+  correct_df_body(g);
+}
+__global__ void kb_correct_df(const Geo* gs) {
+  __shared__ Geo sg;
+  if (!stage_geo(sg, gs)) return;
+  correct_df_body(sg);
+}
 __global__ void __launch_bounds__(256, 4) k_flux_diff_df(Geo g, unsigned tail) {
   wait_for_predecessor();
   flux_diff_t<df>(g, tail);

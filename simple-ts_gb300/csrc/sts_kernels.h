@@ -102,6 +102,8 @@ __global__ void k_assemble_df(Geo g, unsigned long long h_sweep, int in_graph);
 __global__ void kb_assemble_df(const Geo* gs, unsigned long long h_sweep, int in_graph);
 __global__ void k_flux_diff_df(Geo g, unsigned tail);
 __global__ void kb_flux_diff_df(const Geo* gs, unsigned tail);
+__global__ void k_correct_df(Geo g);
+__global__ void kb_correct_df(const Geo* gs);
 __global__ void k_pt_loop_mixed_df(Geo g, int ntiles, LoopCtl* lc);
 // the FP32-correction loops with two FP32 sweeps per tile load (temporal blocking, TMA-staged tiles)
 __global__ void k_pt_loop_mixed_tb(Geo g, int ntiles, LoopCtl* lc, const __grid_constant__ EMaps maps);

@@ -229,6 +229,8 @@ struct sts_ctx {
   FluxKernel flux_kernel() const {
     return g.precision == 3 ? k_flux_diff_df : (fast() ? k_flux_diff_fast : k_flux_diff);
   }
+  using CorrectKernel = void (*)(Geo);
+  CorrectKernel correct_kernel() const { return g.precision == 3 ? k_correct_df : k_correct; }
   // the persistent sweep-loop kernel of this context and its grid (CTAs that fit at once)
   using PtKernel = void (*)(Geo, int, LoopCtl*);
   using PtKernelTB = void (*)(Geo, int, LoopCtl*, EMaps);
@@ -372,7 +374,7 @@ int sts_ctx::build_graph() {
   }
   // correct -> face_rho -> boundary -> flux_diff, each launched as soon as its predecessor's CTAs
   // have all finished (programmatic edges; every one of these kernels waits before touching memory)
-  if (int r = add_kernel(&n_cor, b_outer, {}, k_correct, grid, block, g)) return r;
+  if (int r = add_kernel(&n_cor, b_outer, {}, correct_kernel(), grid, block, g)) return r;
   if (int r = add_pdl_edge(b_outer, n_sw, n_cor)) return r;
   if (g.warm_start == 4) {  // the fit and the next step's start, beside the step's last kernels
     cudaGraphNode_t w[4];
@@ -429,7 +431,7 @@ int sts_ctx::step_host(int n, int* done) {
     for (int outer = 0; outer < NI; outer++) {
       asm_kernel()<<<asm_grid(), asm_block, 0, s>>>(g, 0, 0);
       if (int r = pt_loop()) return r;
-      k_correct<<<grid, block, 0, s>>>(g);
+      correct_kernel()<<<grid, block, 0, s>>>(g);
       k_face_rho<<<grid, block, 0, s>>>(g);
       boundary_step([](int) {});
       if (NI > 1) {
@@ -478,7 +480,7 @@ int sts_ctx::tune_step(int* done) {
     mark();
     if (int r = pt_loop()) return r;
     mark();
-    k_correct<<<grid, block, 0, s>>>(g);
+    correct_kernel()<<<grid, block, 0, s>>>(g);
     k_face_rho<<<grid, block, 0, s>>>(g);
     boundary_step([](int) {});
     if (NI > 1) {
@@ -575,7 +577,7 @@ int sts_ctx::profile(int n, double* ms, int* cnt, int* done) {
       mark(-1);
       if (int r = pt_loop()) return r;
       mark(2);
-      mark(-1); k_correct<<<grid, block, 0, s>>>(g); mark(3);
+      mark(-1); correct_kernel()<<<grid, block, 0, s>>>(g); mark(3);
       mark(-1); k_face_rho<<<grid, block, 0, s>>>(g); mark(4);
       boundary_step(mark);
       if (NI > 1) {
@@ -2038,7 +2040,7 @@ int sts_batch::step_host(int n) {
     const int* tf = d_tile_first;
     void* args[] = {(void*)&G, (void*)&tc, (void*)&tf, (void*)&ncases, (void*)&ntiles, (void*)&d_lc};
     CU(cudaLaunchCooperativeKernel((const void*)pt_kernel(), pt_grid, blk, args, 0, s));
-    kb_correct<<<cell_grid, blk, 0, s>>>(G);
+    (precision == 3 ? kb_correct_df : kb_correct)<<<cell_grid, blk, 0, s>>>(G);
     kb_face_rho<<<cell_grid, blk, 0, s>>>(G);
     kb_bnd_fused<<<bnd_grid, 256, 0, s>>>(G, 0ull, 0, jump_beside);
     if (precision == 3) kb_flux_diff_df<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
@@ -2089,7 +2091,7 @@ int sts_batch::tune_step() {
   void* args[] = {(void*)&G, (void*)&tc, (void*)&tf, (void*)&ncases, (void*)&ntiles, (void*)&d_lc};
   CU(cudaLaunchCooperativeKernel((const void*)pt_kernel(), pt_grid, blk, args, 0, s));
   CU(cudaEventRecord(ev[2], s));
-  kb_correct<<<cell_grid, blk, 0, s>>>(G);
+  (precision == 3 ? kb_correct_df : kb_correct)<<<cell_grid, blk, 0, s>>>(G);
   kb_face_rho<<<cell_grid, blk, 0, s>>>(G);
   kb_bnd_fused<<<bnd_grid, 256, 0, s>>>(G, 0ull, 0, jump_beside);
   if (precision == 3) kb_flux_diff_df<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
@@ -2167,7 +2169,7 @@ int sts_batch::build_graph() {
     v.cooperative = 1;
     CU(cudaGraphKernelNodeSetAttribute(n[2], cudaLaunchAttributeCooperative, &v));
   }
-  if (int r = add_kernel(&n[3], b, {n[2]}, kb_correct, cell_grid, blk, G)) return r;
+  if (int r = add_kernel(&n[3], b, {n[2]}, precision == 3 ? kb_correct_df : kb_correct, cell_grid, blk, G)) return r;
   if (int r = add_kernel(&n[4], b, {n[3]}, kb_face_rho, cell_grid, blk, G)) return r;
   if (int r = add_kernel(&n[6], b, {n[4]}, kb_bnd_fused, bnd_grid, dim3(256), G, (unsigned long long)0, 0,
                          jump_beside))
