@@ -8,8 +8,14 @@ namespace sts {
 namespace {
 
 __device__ __forceinline__ double dmax0(double a, double b) { return a > b ? a : b; }
+// Face density upwind of velocity v1 (the mean when v1 is zero).  The two tests of v1 are made
+// on its bit pattern (the integer pipes; GB300's FP64 unit is the scarce one): zero of either
+// sign -> the mean; positive and not NaN (+inf included) -> r0; anything else -> r1, as the
+// comparisons v1 == 0 and v1 > 0 decide.
 __device__ __forceinline__ double upwind_rho(double r0, double r1, double v1) {
-  return (v1 == 0) ? (0.5 * (r0 + r1)) : ((v1 > 0) ? r0 : r1);
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v1), mag = b & 0x7fffffffffffffffull;
+  if (mag == 0ull) return 0.5 * (r0 + r1);
+  return ((b >> 63) == 0ull && mag <= 0x7ff0000000000000ull) ? r0 : r1;
 }
 __device__ __forceinline__ double Li(double f1, double f2, double h1, double h2) {
   return (f1 * h2 + f2 * h1) / (h1 + h2);

@@ -47,6 +47,9 @@ int fail(int code, const std::string& msg) {
 
 // kernel kinds reported by sts_profile_steps
 constexpr int kProfileKinds = 8;
+// threads per CTA of the fused boundary kernel (32, 64 and 128 measured slower: the wall entries
+// gain nothing from more CTAs, and the last CTA's column and row phases run on fewer threads)
+constexpr int kBndThreads = 256;
 
 }  // namespace
 
@@ -146,14 +149,14 @@ struct sts_ctx {
   bool jump_beside() const { return tjump_beside_walls(g.bits); }
   dim3 bnd_grid() const {
     const int n = g.n_slip_u + g.n_slip_v + (jump_beside() ? g.n_tjump : 0);
-    return dim3((unsigned)std::max(1, std::min((n + 255) / 256, 1024)));
+    return dim3((unsigned)std::max(1, std::min((n + kBndThreads - 1) / kBndThreads, 4096)));
   }
   // boundary work and fluxes/diffusion of one outer iteration outside the graph; `mark`
   // (optional) brackets the launches for the per-kernel profile
   template <class M>
   void boundary_step(M mark) {
     mark(-1);
-    k_bnd_fused<<<bnd_grid(), 256, 0, s>>>(g, 0ull, 0, jump_beside() ? 1 : 0);
+    k_bnd_fused<<<bnd_grid(), kBndThreads, 0, s>>>(g, 0ull, 0, jump_beside() ? 1 : 0);
     mark(5);
     mark(-1);
     flux_kernel()<<<grid, block, 0, s>>>(g, PH_TEMP | PH_PRES);
@@ -391,7 +394,7 @@ int sts_ctx::build_graph() {
   }
   if (int r = add_kernel(&n_rho, b_outer, {}, k_face_rho, grid, block, g)) return r;
   if (int r = add_pdl_edge(b_outer, n_cor, n_rho)) return r;
-  if (int r = add_kernel(&n_bnd, b_outer, {}, k_bnd_fused, bnd_grid(), dim3(256), g, (unsigned long long)ho, 1,
+  if (int r = add_kernel(&n_bnd, b_outer, {}, k_bnd_fused, bnd_grid(), dim3(kBndThreads), g, (unsigned long long)ho, 1,
                          jump_beside() ? 1 : 0))
     return r;
   if (int r = add_pdl_edge(b_outer, n_rho, n_bnd)) return r;
@@ -2042,7 +2045,7 @@ int sts_batch::step_host(int n) {
     CU(cudaLaunchCooperativeKernel((const void*)pt_kernel(), pt_grid, blk, args, 0, s));
     (precision == 3 ? kb_correct_df : kb_correct)<<<cell_grid, blk, 0, s>>>(G);
     kb_face_rho<<<cell_grid, blk, 0, s>>>(G);
-    kb_bnd_fused<<<bnd_grid, 256, 0, s>>>(G, 0ull, 0, jump_beside);
+    kb_bnd_fused<<<bnd_grid, kBndThreads, 0, s>>>(G, 0ull, 0, jump_beside);
     if (precision == 3) kb_flux_diff_df<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
     else if (fast()) kb_flux_diff_fast<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
     else kb_flux_diff<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
@@ -2093,7 +2096,7 @@ int sts_batch::tune_step() {
   CU(cudaEventRecord(ev[2], s));
   (precision == 3 ? kb_correct_df : kb_correct)<<<cell_grid, blk, 0, s>>>(G);
   kb_face_rho<<<cell_grid, blk, 0, s>>>(G);
-  kb_bnd_fused<<<bnd_grid, 256, 0, s>>>(G, 0ull, 0, jump_beside);
+  kb_bnd_fused<<<bnd_grid, kBndThreads, 0, s>>>(G, 0ull, 0, jump_beside);
   if (precision == 3) kb_flux_diff_df<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
   else if (fast()) kb_flux_diff_fast<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
   else kb_flux_diff<<<cell_grid, blk, 0, s>>>(G, PH_TEMP | PH_PRES);
@@ -2171,7 +2174,7 @@ int sts_batch::build_graph() {
   }
   if (int r = add_kernel(&n[3], b, {n[2]}, precision == 3 ? kb_correct_df : kb_correct, cell_grid, blk, G)) return r;
   if (int r = add_kernel(&n[4], b, {n[3]}, kb_face_rho, cell_grid, blk, G)) return r;
-  if (int r = add_kernel(&n[6], b, {n[4]}, kb_bnd_fused, bnd_grid, dim3(256), G, (unsigned long long)0, 0,
+  if (int r = add_kernel(&n[6], b, {n[4]}, kb_bnd_fused, bnd_grid, dim3(kBndThreads), G, (unsigned long long)0, 0,
                          jump_beside))
     return r;
   if (int r = add_kernel(&n[8], b, {n[6]}, precision == 3 ? kb_flux_diff_df : (fast() ? kb_flux_diff_fast : kb_flux_diff),
