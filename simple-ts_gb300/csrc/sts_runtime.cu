@@ -342,10 +342,15 @@ int sts_ctx::build_graph() {
   cudaGraphNode_t n_step;
   cudaGraph_t b_step;
   if (int r = add_while(&n_step, graph, {}, hs, &b_step)) return r;
-  cudaGraphConditionalHandle ho;
-  CU(cudaGraphConditionalHandleCreate(&ho, b_step, 1, cudaGraphCondAssignDefault));
-  cudaGraphNode_t n_begin, n_outer, n_end;
-  if (int r = add_kernel(&n_begin, b_step, {}, k_step_begin, grid, block, g, 1, (unsigned long long)ho, 1)) return r;
+  // one outer iteration per step (N_I = 1): its kernels go straight into the step's body, without
+  // the conditional WHILE node that repeats them (the network's captured kernels keep the node)
+  const bool one_outer = hc.cfg.n("N_I") == 1 && !warm_net;
+  cudaGraphConditionalHandle ho = 0;
+  if (!one_outer) CU(cudaGraphConditionalHandleCreate(&ho, b_step, 1, cudaGraphCondAssignDefault));
+  const int outer_cond = one_outer ? 0 : 1;  // the kernels that set the outer node's condition
+  cudaGraphNode_t n_begin, n_outer = nullptr, n_end;
+  if (int r = add_kernel(&n_begin, b_step, {}, k_step_begin, grid, block, g, 1, (unsigned long long)ho, outer_cond))
+    return r;
   if (g.warm_start == 3) {
     cudaGraphNode_t w[3];
     if (int r = add_kernel(&w[0], b_step, {n_begin}, k_warm_diff, grid, block, g)) return r;
@@ -353,13 +358,12 @@ int sts_ctx::build_graph() {
     if (int r = add_kernel(&w[2], b_step, {w[1]}, k_warm_apply, grid, block, g)) return r;
     n_begin = w[2];
   }
-  cudaGraph_t b_outer;
-  if (int r = add_while(&n_outer, b_step, {n_begin}, ho, &b_outer)) return r;
-  if (int r = add_kernel(&n_end, b_step, {n_outer}, k_step_end, dim3(1), dim3(1024), g, (unsigned long long)hs, 1))
-    return r;
-  cudaGraphNode_t n_asm, n_sw, n_cor, n_rho, n_bnd, n_fd;
-  if (int r = add_kernel(&n_asm, b_outer, {}, asm_kernel(), asm_grid(), asm_block, g,
-                         (unsigned long long)0, 0))
+  cudaGraph_t b_outer = b_step;
+  if (!one_outer)
+    if (int r = add_while(&n_outer, b_step, {n_begin}, ho, &b_outer)) return r;
+  cudaGraphNode_t n_asm, n_sw, n_cor, n_rho, n_bnd, n_fd, n_pred = nullptr;
+  if (int r = add_kernel(&n_asm, b_outer, one_outer ? std::vector<cudaGraphNode_t>{n_begin} : std::vector<cudaGraphNode_t>{},
+                         asm_kernel(), asm_grid(), asm_block, g, (unsigned long long)0, 0))
     return r;
   // warm_start 4: the predictor's kernels (first outer iteration only) beside the assembly
   std::vector<cudaGraphNode_t> before_sweeps{n_asm};
@@ -385,6 +389,7 @@ int sts_ctx::build_graph() {
     if (int r = add_kernel(&w[1], b_outer, {w[0]}, k_conv_solve, dim3(2), dim3(kConvSolveThreads), g)) return r;
     if (int r = add_kernel(&w[2], b_outer, {w[0]}, k_conv_next, grid, block, g)) return r;
     if (int r = add_kernel(&w[3], b_outer, {w[1], w[2]}, k_conv_predict, grid, block, g)) return r;
+    n_pred = w[3];
     if (warm_net) {  // the network's kernels, captured into the body after the stencil's
       CU(cudaStreamBeginCaptureToGraph(cap, b_outer, &w[3], nullptr, 1, cudaStreamCaptureModeRelaxed));
       net_tail(cap);
@@ -394,12 +399,19 @@ int sts_ctx::build_graph() {
   }
   if (int r = add_kernel(&n_rho, b_outer, {}, k_face_rho, grid, block, g)) return r;
   if (int r = add_pdl_edge(b_outer, n_cor, n_rho)) return r;
-  if (int r = add_kernel(&n_bnd, b_outer, {}, k_bnd_fused, bnd_grid(), dim3(kBndThreads), g, (unsigned long long)ho, 1,
-                         jump_beside() ? 1 : 0))
+  if (int r = add_kernel(&n_bnd, b_outer, {}, k_bnd_fused, bnd_grid(), dim3(kBndThreads), g, (unsigned long long)ho,
+                         outer_cond, jump_beside() ? 1 : 0))
     return r;
   if (int r = add_pdl_edge(b_outer, n_rho, n_bnd)) return r;
   if (int r = add_kernel(&n_fd, b_outer, {}, flux_kernel(), grid, block, g, (unsigned)(PH_TEMP | PH_PRES))) return r;
   if (int r = add_pdl_edge(b_outer, n_bnd, n_fd)) return r;
+  std::vector<cudaGraphNode_t> before_end{n_outer};
+  if (one_outer) {  // every last node of the outer iteration's kernels
+    before_end = {n_fd};
+    if (n_pred) before_end.push_back(n_pred);
+  }
+  if (int r = add_kernel(&n_end, b_step, before_end, k_step_end, dim3(1), dim3(1024), g, (unsigned long long)hs, 1))
+    return r;
   CU(cudaGraphInstantiate(&exec, graph, 0));
   h_step = hs;
   h_outer = ho;
