@@ -76,6 +76,9 @@ struct sts_ctx {
   // graph
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  // the same step without the WHILE node over steps, for launches of one step
+  cudaGraph_t graph1 = nullptr;
+  cudaGraphExec_t exec1 = nullptr;
   unsigned long long h_step = 0, h_outer = 0;
   // the sweep loop's grid barrier and the case's 32x8 tiles
   LoopCtl* d_lc = nullptr;
@@ -110,8 +113,7 @@ struct sts_ctx {
 
   ~sts_ctx() {
     saver.reset();  // writes out pending saves before the buffers and the stream go
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
+    drop_graphs();
     for (void* p : allocs) cudaFree(p);
     if (h_ctl) cudaFreeHost(h_ctl);
     net.reset();
@@ -268,7 +270,16 @@ struct sts_ctx {
     return STS_OK;
   }
   int make_emaps();
-  int build_graph();
+  int build_graph(bool loop);
+  // the step graphs are rebuilt at the next graph step
+  void drop_graphs() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (exec1) cudaGraphExecDestroy(exec1);
+    if (graph1) cudaGraphDestroy(graph1);
+    exec = exec1 = nullptr;
+    graph = graph1 = nullptr;
+  }
   int write_mesh();
   int write_drag();
   int continuity();
@@ -335,13 +346,19 @@ int add_while(cudaGraphNode_t* node, cudaGraph_t graph, const std::vector<cudaGr
 //   WHILE(step) { step_begin -> WHILE(outer) { assemble -> sweep loop (one cooperative kernel) ->
 //                 correct -> face_rho -> walls -> boundary -> T-jump -> flux_diff } -> step_end }
 // Every decision (sweep count, outer iterations, end of run) is taken on the device.
-int sts_ctx::build_graph() {
-  CU(cudaGraphCreate(&graph, 0));
-  cudaGraphConditionalHandle hs;
-  CU(cudaGraphConditionalHandleCreate(&hs, graph, 1, cudaGraphCondAssignDefault));
-  cudaGraphNode_t n_step;
-  cudaGraph_t b_step;
-  if (int r = add_while(&n_step, graph, {}, hs, &b_step)) return r;
+// loop: the steps in a WHILE node (any number of steps per launch, each ended by the device's
+// decision); otherwise one step, its kernels at the top level of the graph (launches of one step:
+// a conditional node costs several microseconds per step).
+int sts_ctx::build_graph(bool loop) {
+  cudaGraph_t& top = loop ? graph : graph1;
+  CU(cudaGraphCreate(&top, 0));
+  cudaGraphConditionalHandle hs = 0;
+  cudaGraph_t b_step = top;
+  if (loop) {
+    CU(cudaGraphConditionalHandleCreate(&hs, top, 1, cudaGraphCondAssignDefault));
+    cudaGraphNode_t n_step;
+    if (int r = add_while(&n_step, top, {}, hs, &b_step)) return r;
+  }
   // one outer iteration per step (N_I = 1): its kernels go straight into the step's body, without
   // the conditional WHILE node that repeats them (the network's captured kernels keep the node)
   const bool one_outer = hc.cfg.n("N_I") == 1 && !warm_net;
@@ -410,21 +427,23 @@ int sts_ctx::build_graph() {
     before_end = {n_fd};
     if (n_pred) before_end.push_back(n_pred);
   }
-  if (int r = add_kernel(&n_end, b_step, before_end, k_step_end, dim3(1), dim3(1024), g, (unsigned long long)hs, 1))
+  if (int r = add_kernel(&n_end, b_step, before_end, k_step_end, dim3(1), dim3(1024), g, (unsigned long long)hs,
+                         loop ? 1 : 0))
     return r;
-  CU(cudaGraphInstantiate(&exec, graph, 0));
-  h_step = hs;
+  CU(cudaGraphInstantiate(loop ? &exec : &exec1, top, 0));
+  if (loop) h_step = hs;
   h_outer = ho;
   return STS_OK;
 }
 
 int sts_ctx::step_graph(int n, int* done, double* const* state_out) {
-  if (!exec)
-    if (int r = build_graph()) return r;
+  const bool loop = n != 1;
+  if (!(loop ? exec : exec1))
+    if (int r = build_graph(loop)) return r;
   const unsigned before = h_ctl->it_counter;
   unsigned left = (unsigned)n;
   CU(cudaMemcpyAsync(&d_ctl->steps_left, &left, sizeof(unsigned), cudaMemcpyHostToDevice, s));
-  CU(cudaGraphLaunch(exec, s));
+  CU(cudaGraphLaunch(loop ? exec : exec1, s));
   if (state_out) {  // the new state straight to device-addressable host buffers, before the one sync
     k_move4_state_out<<<std::max(1, std::min((g.Na + 255) / 256, 4 * std::max(sms, 1))), 256, 0, s>>>(
         g, state_out[0], state_out[1], state_out[2], state_out[3]);
@@ -1714,14 +1733,7 @@ int sts_set_sweep_blocking(sts_ctx* ctx, int k) {
   ctx->pt_tb_forced = k;
   if (k) ctx->pt_tb = k;
   if (int r = ctx->size_pt_grid()) return r;
-  if (ctx->exec) {  // the graph is rebuilt with the new sweep-loop kernel at the next step
-    cudaGraphExecDestroy(ctx->exec);
-    ctx->exec = nullptr;
-  }
-  if (ctx->graph) {
-    cudaGraphDestroy(ctx->graph);
-    ctx->graph = nullptr;
-  }
+  ctx->drop_graphs();  // the graphs are rebuilt with the new sweep-loop kernel at the next step
   return STS_OK;
 }
 
