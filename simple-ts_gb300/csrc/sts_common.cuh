@@ -217,6 +217,7 @@ struct Geo {
   float* cpart;
   int* crows;
   float* cgram;
+  unsigned* ctmax;  // [field][tile]: largest |D| of the coming difference per 32x8 tile (FP32 bits)
 };
 
 // Neighbour indices of one cell: ij_function / ij_function_PeriodicBC (SIMPLE_TS_MPI.cpp:140-232).

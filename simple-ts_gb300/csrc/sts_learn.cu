@@ -349,9 +349,10 @@ __device__ __forceinline__ void conv_solve_body(const Geo& g) {
   }
 }
 
-// End of a step, all cells: the coming difference D_r = x_{n+1} - x_n (FP32; 0 off the solved
-// cells) into its ring slot -- the value the next step's start stores there again -- and its
-// per-field maximum (cleared by conv_gram) for the active flags.
+// End of a step, all cells, one CTA per 32x8 tile: the coming difference D_r = x_{n+1} - x_n
+// (FP32; 0 off the solved cells) into its ring slot -- the value the next step's start stores
+// there again -- its per-field maximum over the tile, and over the mesh (cleared by conv_gram), for
+// the active flags.
 __device__ __forceinline__ void conv_next_body(const Geo& g) {
   Cell c = cell(g);
   const Ctl* ctl = g.ctl;
@@ -380,6 +381,8 @@ __device__ __forceinline__ void conv_next_body(const Geo& g) {
   if (tid < 2) {
     unsigned v = 0;
     for (int w = 0; w < nw; w++) v = max(v, wm[tid][w]);
+    const int ntx = (g.Nx + 31) / 32, nty = (g.Ny + 7) / 8;
+    if ((int)blockIdx.x < ntx && (int)blockIdx.y < nty) g.ctmax[tid * ntx * nty + blockIdx.x + blockIdx.y * ntx] = v;
     if (v) atomicMax(&g.ctl->conv_max[r & 1][tid], v);
   }
 }
@@ -388,6 +391,9 @@ __device__ __forceinline__ void conv_next_body(const Geo& g) {
 // kConvReach steps of a source, |D_r| > kConvAlpha max |D_r|; x wrapped on periodic meshes), and
 // on the active cells, with the weights just fitted, the stencil's start for the next step,
 // x_{n+1} + sum_k w_k feature_k, kept in cnext and flagged for k_step_begin (bits 2 and 3).
+// A tile none of whose 3x3 neighbouring tiles holds a source (their maxima from conv_next; the
+// reach is shorter than a tile) has no active cell and only clears its flags; the front covers a
+// few percent of the tiles.  Tiles whose reach wraps around a periodic mesh take the per-cell test.
 __device__ __forceinline__ void conv_predict_body(const Geo& g) {
   const Ctl* ctl = g.ctl;
   const unsigned r = ctl->warm_ready, cur = ctl->cur;
@@ -400,6 +406,21 @@ __device__ __forceinline__ void conv_predict_body(const Geo& g) {
   const bool in = i < Nx && j < Ny;
   const int n = i + j * Nx;
   const bool per = g.bits & F_PERIODIC;
+  const float thr0 = kConvAlpha * __uint_as_float(ctl->conv_max[r & 1][0]);
+  const float thr1 = kConvAlpha * __uint_as_float(ctl->conv_max[r & 1][1]);
+  {
+    const int ntx = (Nx + TX - 1) / TX, nty = (Ny + TY - 1) / TY;
+    bool near = per && (i0 - R < 0 || i0 + TX - 1 + R >= Nx);
+    if (tid < 18) {
+      const int f = tid / 9, q = tid - 9 * f, tx = (int)blockIdx.x + q % 3 - 1, ty = (int)blockIdx.y + q / 3 - 1;
+      if (tx >= 0 && tx < ntx && ty >= 0 && ty < nty)
+        near = near || __uint_as_float(g.ctmax[f * ntx * nty + tx + ty * ntx]) > (f ? thr1 : thr0);
+    }
+    if (!__syncthreads_or(near)) {
+      if (in) g.cact[r & 1][n] = 0;
+      return;
+    }
+  }
   __shared__ float Dh[2][HY][HX];
   stage<2 * HY * HX, TX * TY>(&Dh[0][0][0], tid, [&](int k) {
     const int f = k / (HY * HX), rem = k - f * (HY * HX);
@@ -411,8 +432,6 @@ __device__ __forceinline__ void conv_predict_body(const Geo& g) {
   __syncthreads();
   unsigned bits = 0;
   if (in && solved_cell(g, n)) {
-    const float thr0 = kConvAlpha * __uint_as_float(ctl->conv_max[r & 1][0]);
-    const float thr1 = kConvAlpha * __uint_as_float(ctl->conv_max[r & 1][1]);
     for (int dj = -R; dj <= R; dj++) {
       const int rx = R - (dj < 0 ? -dj : dj);
       for (int di = -rx; di <= rx; di++) {

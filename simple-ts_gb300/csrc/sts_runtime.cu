@@ -1139,6 +1139,7 @@ int open_impl(const char* dir, const sts_options* opt_in, sts_ctx** out) {
     const size_t nt = (size_t)((h.Nx + 31) / 32) * ((h.Ny + 7) / 8);
     if (int r = c->alloc(&g.cpart, nt * 2 * kConvTerms)) return r;
     if (int r = c->alloc(&g.crows, nt * 2)) return r;
+    if (int r = c->alloc(&g.ctmax, nt * 2)) return r;
     if (int r = c->alloc(&g.cgram, (size_t)kConvWin * 2 * kConvTerms)) return r;
   }
   if (g.precision >= 2) {
