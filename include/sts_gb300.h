@@ -141,7 +141,9 @@ int sts_get_state(sts_ctx* ctx, double* u_out, double* v_out, double* p_out, dou
  * synchronises once, at the end, instead of three times.  The outputs take the direct kernel path
  * when they are device-addressable host memory and the steps run as the step graph; otherwise
  * (steps of the autotuner, use_graph 0, other host memory) the state is fetched after the steps as
- * sts_get_state does.  Input and output buffers may be the same.  Returns sts_step's status; after
+ * sts_get_state does.  For one step with device-addressable inputs and outputs, the state is read
+ * from the inputs inside the step's first kernel and written to the outputs while the step's last
+ * kernels run.  Input and output buffers may be the same.  Returns sts_step's status; after
  * STS_OK or STS_ERR_NONFINITE the outputs hold the state at the end of the steps taken. */
 int sts_step_exchange(sts_ctx* ctx, int nsteps, const double* u_in, const double* v_in, const double* p_in,
                       const double* T_in, double* u_out, double* v_out, double* p_out, double* T_out,

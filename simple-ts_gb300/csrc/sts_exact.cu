@@ -85,6 +85,21 @@ __device__ __forceinline__ void k_step_begin_body(const Geo& g, int counters, un
 __global__ void k_step_begin(Geo g, int counters, unsigned long long h_outer, int in_graph) {
   k_step_begin_body(g, counters, h_outer, in_graph);
 }
+// The same, with the state u, v, p, T first read from device-addressable host buffers (when
+// given): every thread stores its cell's values before the step's copies read them back.
+__global__ void k_step_begin_in(Geo g, unsigned long long h_outer, int in_graph, const double* u_in,
+                                const double* v_in, const double* p_in, const double* T_in) {
+  const Cell c = cell(g);
+  if (u_in && c.ok) {
+    const unsigned cur = g.ctl->cur;
+    const double u = u_in[c.ij], v = v_in[c.ij], p = p_in[c.ij], T = T_in[c.ij];
+    g.u[c.ij] = u;
+    g.v[c.ij] = v;
+    g.p[cur][c.ij] = p;
+    g.T[cur][c.ij] = T;
+  }
+  k_step_begin_body(g, 1, h_outer, in_graph);
+}
 
 // Batched start of a step: a case takes part while its run goes on and steps are left; cases
 // that stopped skip every kernel of the step (stage_geo reads the flag).
@@ -1403,7 +1418,10 @@ __device__ __forceinline__ bool last_cta(unsigned* counter) {
   return last;
 }
 
-__device__ __forceinline__ void bnd_fused_body(const Geo& g, unsigned long long h_outer, int in_graph, int jump_beside) {
+// tail: the zero-gradient temperature and pressure copies (PH_TEMP, PH_PRES) after the jump walls,
+// in the last CTA, where the flux kernel does not do them.
+__device__ __forceinline__ void bnd_fused_body(const Geo& g, unsigned long long h_outer, int in_graph, int jump_beside,
+                                               unsigned tail) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
   if (t == 0) do_control(g, h_outer, in_graph);
   const int nu = g.n_slip_u, nuv = nu + g.n_slip_v, n = nuv + (jump_beside ? g.n_tjump : 0);
@@ -1419,15 +1437,22 @@ __device__ __forceinline__ void bnd_fused_body(const Geo& g, unsigned long long 
     __syncthreads();
     for (int k = threadIdx.x; k < g.n_tjump; k += blockDim.x) do_tjump(g, T, k);
   }
+  if (tail) {
+    const unsigned cur = g.ctl->cur;
+    __syncthreads();
+    if (tail & PH_TEMP) phase_temp(g, g.T[cur], threadIdx.x, blockDim.x);
+    __syncthreads();
+    if (tail & PH_PRES) phase_pres(g, g.p[cur], threadIdx.x, blockDim.x);
+  }
 }
-__global__ void k_bnd_fused(Geo g, unsigned long long h_outer, int in_graph, int jump_beside) {
+__global__ void k_bnd_fused(Geo g, unsigned long long h_outer, int in_graph, int jump_beside, unsigned tail) {
   wait_for_predecessor();
-  bnd_fused_body(g, h_outer, in_graph, jump_beside);
+  bnd_fused_body(g, h_outer, in_graph, jump_beside, tail);
 }
 __global__ void kb_bnd_fused(const Geo* gs, unsigned long long h_outer, int in_graph, int jump_beside) {
   __shared__ Geo sg;
   if (!stage_geo(sg, gs)) return;
-  bnd_fused_body(sg, h_outer, in_graph, jump_beside);
+  bnd_fused_body(sg, h_outer, in_graph, jump_beside, 0u);
 }
 
 // End of a time step: time-dependent inflow (SIMPLE_TS_MPI.cpp:8102-8144), per-step

@@ -24,6 +24,8 @@ enum : unsigned {
 // Per-case kernels.  Each k_X takes the case's Geo by value; its batched form kb_X takes the
 // device array of the batch's Geos and runs case blockIdx.z (cases outside the step return).
 __global__ void k_step_begin(Geo g, int counters, unsigned long long h_outer, int in_graph);
+__global__ void k_step_begin_in(Geo g, unsigned long long h_outer, int in_graph, const double* u_in,
+                                const double* v_in, const double* p_in, const double* T_in);
 __global__ void k_apply_bodies(Geo g);
 __global__ void k_assemble(Geo g, unsigned long long h_sweep, int in_graph);
 __global__ void k_sweep_first(Geo g, unsigned long long h_sweep, int in_graph);
@@ -32,7 +34,7 @@ __global__ void k_correct(Geo g);
 __global__ void k_face_rho(Geo g);
 __global__ void k_flux_diff(Geo g, unsigned tail);
 __global__ void k_flux_quotients(Geo g);
-__global__ void k_bnd_fused(Geo g, unsigned long long h_outer, int in_graph, int jump_beside);
+__global__ void k_bnd_fused(Geo g, unsigned long long h_outer, int in_graph, int jump_beside, unsigned tail);
 __global__ void k_sqrt_rho(Geo g, int do_rho);
 __global__ void k_boundary(Geo g, unsigned phases, unsigned long long h_outer, int in_graph);
 __global__ void k_step_end(Geo g, unsigned long long h_step, int in_graph);

@@ -79,6 +79,12 @@ struct sts_ctx {
   // the same step without the WHILE node over steps, for launches of one step
   cudaGraph_t graph1 = nullptr;
   cudaGraphExec_t exec1 = nullptr;
+  // the one-step graph of sts_step_exchange: the state comes in from host buffers in the first
+  // kernel (node n_xin) and goes out to host buffers beside the flux kernel (node n_xout); their
+  // buffers are set before every launch
+  cudaGraph_t graph1x = nullptr;
+  cudaGraphExec_t exec1x = nullptr;
+  cudaGraphNode_t n_xin = nullptr, n_xout = nullptr;
   unsigned long long h_step = 0, h_outer = 0;
   // the sweep loop's grid barrier and the case's 32x8 tiles
   LoopCtl* d_lc = nullptr;
@@ -158,7 +164,7 @@ struct sts_ctx {
   template <class M>
   void boundary_step(M mark) {
     mark(-1);
-    k_bnd_fused<<<bnd_grid(), kBndThreads, 0, s>>>(g, 0ull, 0, jump_beside() ? 1 : 0);
+    k_bnd_fused<<<bnd_grid(), kBndThreads, 0, s>>>(g, 0ull, 0, jump_beside() ? 1 : 0, 0u);
     mark(5);
     mark(-1);
     flux_kernel()<<<grid, block, 0, s>>>(g, PH_TEMP | PH_PRES);
@@ -270,21 +276,30 @@ struct sts_ctx {
     return STS_OK;
   }
   int make_emaps();
-  int build_graph(bool loop);
+  int build_graph(bool loop, bool xout = false);
   // the step graphs are rebuilt at the next graph step
   void drop_graphs() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     if (exec1) cudaGraphExecDestroy(exec1);
     if (graph1) cudaGraphDestroy(graph1);
-    exec = exec1 = nullptr;
-    graph = graph1 = nullptr;
+    if (exec1x) cudaGraphExecDestroy(exec1x);
+    if (graph1x) cudaGraphDestroy(graph1x);
+    exec = exec1 = exec1x = nullptr;
+    graph = graph1 = graph1x = nullptr;
+    n_xin = n_xout = nullptr;
+  }
+  // The state is final once the boundary kernel is done (the flux kernel and the end of the step
+  // read it; only a time-dependent inflow writes u at the end of the step), so the state can go
+  // out beside the flux kernel when the step's kernels sit at the top level of the graph.
+  bool xout_in_graph() {
+    return hc.cfg.n("N_I") == 1 && !warm_net && !(g.bits & F_U_BY_TIME);
   }
   int write_mesh();
   int write_drag();
   int continuity();
   int step_host(int n, int* done);
-  int step_graph(int n, int* done, double* const* state_out = nullptr);
+  int step_graph(int n, int* done, double* const* state_out = nullptr, const double* const* state_in = nullptr);
   int write_outputs(bool wait_files);
   int wait_outputs();
   int write_logs(bool iterations = true);
@@ -310,6 +325,25 @@ int add_kernel(cudaGraphNode_t* node, cudaGraph_t graph, const std::vector<cudaG
   p.sharedMemBytes = 0;
   p.kernelParams = argv;
   CU(cudaGraphAddKernelNode(node, graph, deps.data(), deps.size(), &p));
+  return STS_OK;
+}
+
+// Sets the arguments of a kernel node of an instantiated graph (for its next launches).
+template <class... P, class... A>
+int set_kernel_args(cudaGraphExec_t exec, cudaGraphNode_t node, void (*f)(P...), dim3 grid, dim3 block, A... args) {
+  std::tuple<P...> vals(args...);
+  void* argv[sizeof...(P)];
+  std::apply([&](auto&... x) {
+    int k = 0;
+    ((argv[k++] = (void*)&x), ...);
+  }, vals);
+  cudaKernelNodeParams p{};
+  p.func = (void*)f;
+  p.gridDim = grid;
+  p.blockDim = block;
+  p.sharedMemBytes = 0;
+  p.kernelParams = argv;
+  CU(cudaGraphExecKernelNodeSetParams(exec, node, &p));
   return STS_OK;
 }
 
@@ -348,9 +382,16 @@ int add_while(cudaGraphNode_t* node, cudaGraph_t graph, const std::vector<cudaGr
 // Every decision (sweep count, outer iterations, end of run) is taken on the device.
 // loop: the steps in a WHILE node (any number of steps per launch, each ended by the device's
 // decision); otherwise one step, its kernels at the top level of the graph (launches of one step:
-// a conditional node costs several microseconds per step).
-int sts_ctx::build_graph(bool loop) {
-  cudaGraph_t& top = loop ? graph : graph1;
+// a conditional node costs several microseconds per step).  xout (one step, xout_in_graph()): the
+// state goes out to host buffers beside the flux kernel, the zero-gradient copies of p and T
+// moving from the flux kernel to the end of the boundary kernel.
+// One small CTA per SM for the state's way out: it fits beside the flux kernel's resident CTAs
+// (their registers leave about 4k per SM), and 64 threads a CTA still keep enough bytes in flight
+// to fill the host link.
+constexpr int kXoutThreads = 64;
+
+int sts_ctx::build_graph(bool loop, bool xout) {
+  cudaGraph_t& top = loop ? graph : (xout ? graph1x : graph1);
   CU(cudaGraphCreate(&top, 0));
   cudaGraphConditionalHandle hs = 0;
   cudaGraph_t b_step = top;
@@ -366,8 +407,15 @@ int sts_ctx::build_graph(bool loop) {
   if (!one_outer) CU(cudaGraphConditionalHandleCreate(&ho, b_step, 1, cudaGraphCondAssignDefault));
   const int outer_cond = one_outer ? 0 : 1;  // the kernels that set the outer node's condition
   cudaGraphNode_t n_begin, n_outer = nullptr, n_end;
-  if (int r = add_kernel(&n_begin, b_step, {}, k_step_begin, grid, block, g, 1, (unsigned long long)ho, outer_cond))
+  if (xout) {  // one_outer holds: no outer node
+    const double* none = nullptr;
+    if (int r = add_kernel(&n_begin, b_step, {}, k_step_begin_in, grid, block, g, 0ull, 0, none, none, none, none))
+      return r;
+    n_xin = n_begin;
+  } else if (int r = add_kernel(&n_begin, b_step, {}, k_step_begin, grid, block, g, 1, (unsigned long long)ho,
+                                outer_cond)) {
     return r;
+  }
   if (g.warm_start == 3) {
     cudaGraphNode_t w[3];
     if (int r = add_kernel(&w[0], b_step, {n_begin}, k_warm_diff, grid, block, g)) return r;
@@ -416,12 +464,17 @@ int sts_ctx::build_graph(bool loop) {
   }
   if (int r = add_kernel(&n_rho, b_outer, {}, k_face_rho, grid, block, g)) return r;
   if (int r = add_pdl_edge(b_outer, n_cor, n_rho)) return r;
+  const unsigned tail = PH_TEMP | PH_PRES;
   if (int r = add_kernel(&n_bnd, b_outer, {}, k_bnd_fused, bnd_grid(), dim3(kBndThreads), g, (unsigned long long)ho,
-                         outer_cond, jump_beside() ? 1 : 0))
+                         outer_cond, jump_beside() ? 1 : 0, xout ? tail : 0u))
     return r;
   if (int r = add_pdl_edge(b_outer, n_rho, n_bnd)) return r;
-  if (int r = add_kernel(&n_fd, b_outer, {}, flux_kernel(), grid, block, g, (unsigned)(PH_TEMP | PH_PRES))) return r;
+  if (int r = add_kernel(&n_fd, b_outer, {}, flux_kernel(), grid, block, g, xout ? 0u : tail)) return r;
   if (int r = add_pdl_edge(b_outer, n_bnd, n_fd)) return r;
+  if (xout)  // the buffers are set before every launch
+    if (int r = add_kernel(&n_xout, b_outer, {n_bnd}, k_move4_state_out, dim3(std::max(1, sms)), dim3(kXoutThreads), g,
+                           (double*)nullptr, (double*)nullptr, (double*)nullptr, (double*)nullptr))
+      return r;
   std::vector<cudaGraphNode_t> before_end{n_outer};
   if (one_outer) {  // every last node of the outer iteration's kernels
     before_end = {n_fd};
@@ -430,21 +483,32 @@ int sts_ctx::build_graph(bool loop) {
   if (int r = add_kernel(&n_end, b_step, before_end, k_step_end, dim3(1), dim3(1024), g, (unsigned long long)hs,
                          loop ? 1 : 0))
     return r;
-  CU(cudaGraphInstantiate(loop ? &exec : &exec1, top, 0));
+  CU(cudaGraphInstantiate(loop ? &exec : (xout ? &exec1x : &exec1), top, 0));
   if (loop) h_step = hs;
   h_outer = ho;
   return STS_OK;
 }
 
-int sts_ctx::step_graph(int n, int* done, double* const* state_out) {
+int sts_ctx::step_graph(int n, int* done, double* const* state_out, const double* const* state_in) {
   const bool loop = n != 1;
-  if (!(loop ? exec : exec1))
-    if (int r = build_graph(loop)) return r;
+  const bool xout = !loop && state_out && xout_in_graph();
+  cudaGraphExec_t& ex = loop ? exec : (xout ? exec1x : exec1);
+  if (!ex)
+    if (int r = build_graph(loop, xout)) return r;
   const unsigned before = h_ctl->it_counter;
   unsigned left = (unsigned)n;
   CU(cudaMemcpyAsync(&d_ctl->steps_left, &left, sizeof(unsigned), cudaMemcpyHostToDevice, s));
-  CU(cudaGraphLaunch(loop ? exec : exec1, s));
-  if (state_out) {  // the new state straight to device-addressable host buffers, before the one sync
+  if (xout) {
+    const double* none[4] = {nullptr, nullptr, nullptr, nullptr};
+    const double* const* in = state_in ? state_in : none;
+    if (int r = set_kernel_args(ex, n_xin, k_step_begin_in, grid, block, g, 0ull, 0, in[0], in[1], in[2], in[3]))
+      return r;
+    if (int r = set_kernel_args(ex, n_xout, k_move4_state_out, dim3(std::max(1, sms)), dim3(kXoutThreads), g, state_out[0],
+                                state_out[1], state_out[2], state_out[3]))
+      return r;
+  }
+  CU(cudaGraphLaunch(ex, s));
+  if (state_out && !xout) {  // the new state straight to device-addressable host buffers, before the one sync
     k_move4_state_out<<<std::max(1, std::min((g.Na + 255) / 256, 4 * std::max(sms, 1))), 256, 0, s>>>(
         g, state_out[0], state_out[1], state_out[2], state_out[3]);
     CU(cudaGetLastError());
@@ -1285,7 +1349,10 @@ int sts_open_case(const char* case_dir, const sts_options* opt, sts_ctx** out) {
 // move of the new state into those buffers before its synchronisation, and *moved says whether
 // that happened (the autotuner's steps, launched one by one, or a run that had ended, leave it to
 // the caller).
-static int step_impl(sts_ctx* ctx, int nsteps, int* steps_done, double* const* state_out, bool* moved) {
+// state_in (with state_out, one step in the graph): the state is read from those buffers in the step's
+// first kernel; *moved tells whether the step's graph ran with the buffers.
+static int step_impl(sts_ctx* ctx, int nsteps, int* steps_done, double* const* state_out, bool* moved,
+                     const double* const* state_in = nullptr) {
   if (moved) *moved = false;
   int done = 0;
   if (!ctx->finished && nsteps > 0) {
@@ -1301,7 +1368,7 @@ static int step_impl(sts_ctx* ctx, int nsteps, int* steps_done, double* const* s
     }
     if (done < nsteps && !ctx->finished && !(ctx->h_ctl->status & ~status_before & (ST_BARRIER_TIMEOUT | ST_NONFINITE))) {
       int d = 0;
-      int r = ctx->opt.use_graph ? ctx->step_graph(nsteps - done, &d, state_out) : ctx->step_host(nsteps - done, &d);
+      int r = ctx->opt.use_graph ? ctx->step_graph(nsteps - done, &d, state_out, state_in) : ctx->step_host(nsteps - done, &d);
       if (r) return r;
       if (ctx->opt.use_graph && state_out && moved) *moved = true;
       done += d;
@@ -1507,13 +1574,28 @@ int sts_step_exchange(sts_ctx* ctx, int nsteps, const double* u_in, const double
   if (steps_done) *steps_done = 0;
   CU(cudaSetDevice(ctx->opt.device));
   const void* hout[4] = {u_out, v_out, p_out, T_out};
-  void* dout[4];
+  const void* hin[4] = {u_in, v_in, p_in, T_in};
+  void *dout[4], *din[4];
   const bool direct = mapped_host(hout, dout, 4);
-  if (int r = set_state_queue(ctx, u_in, v_in, p_in, T_in)) return r;
+  // one step in the exchange graph, both sides device-addressable: the state comes in in the
+  // step's first kernel, otherwise ahead of the step
+  const bool fused_in = direct && nsteps == 1 && ctx->opt.use_graph && ctx->tune_left == 0 && !ctx->finished &&
+                        ctx->xout_in_graph() && mapped_host(hin, din, 4);
+  if (fused_in) {
+    if (ctx->g.warm_start) {  // as sts_set_state: the warm start's history begins again
+      static const unsigned zero = 0;
+      CU(cudaMemcpyAsync(&ctx->g.ctl->warm_ready, &zero, sizeof(unsigned), cudaMemcpyHostToDevice, ctx->s));
+    }
+  } else if (int r = set_state_queue(ctx, u_in, v_in, p_in, T_in)) {
+    return r;
+  }
   bool moved = false;
-  const int r = step_impl(ctx, nsteps, steps_done, direct ? (double* const*)dout : nullptr, &moved);
+  const int r = step_impl(ctx, nsteps, steps_done, direct ? (double* const*)dout : nullptr, &moved,
+                          fused_in ? (const double* const*)din : nullptr);
   if (r != STS_OK && r != STS_ERR_NONFINITE) return r;
   if (!moved) {
+    if (fused_in)  // no step ran: the state still goes in
+      if (int q = set_state_queue(ctx, u_in, v_in, p_in, T_in)) return q;
     CU(cudaStreamSynchronize(ctx->s));  // the inputs are read (a run that had ended takes no step)
     if (int q = sts_get_state(ctx, u_out, v_out, p_out, T_out)) return q;
   }

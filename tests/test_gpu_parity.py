@@ -219,8 +219,8 @@ def test_nonfinite_residual_is_reported(lib_built):
 @pytest.mark.parametrize("autotune", [False, True], ids=["fixed_shapes", "autotuned"])
 def test_step_exchange_equals_three_calls(memory, autotune, lib_built):
     """sts_step_exchange gives the bits of sts_set_state + sts_step + sts_get_state: over several
-    calls, with separate and with the same input and output buffers, from the autotuner's first
-    steps (launched one by one) on, and with no steps at all."""
+    calls of one and of several steps, with separate and with the same input and output buffers,
+    from the autotuner's first steps (launched one by one) on, and with no steps at all."""
     import sts
     case = sc.channel_case("c", 80, 10, 0.3, 0.002, 1e-3, 80)
     keep = []
@@ -240,7 +240,7 @@ def test_step_exchange_equals_three_calls(memory, autotune, lib_built):
         assert a.step(2) == b.step(2) == 2
         ins, outs = bufs(a.Ny, a.Nx), bufs(a.Ny, a.Nx)
         a.get_state_ptr(*[x.ctypes.data for x in ins])
-        for rnd, n in enumerate((3, 4, 0, 5, 4)):
+        for rnd, n in enumerate((3, 1, 4, 0, 1, 5, 1, 4)):
             ins[2] *= 1.0 + 1e-7  # a slightly different state goes in every time
             b_in = [x.copy() for x in ins]
             b_out = [np.empty_like(x) for x in ins]
@@ -251,13 +251,50 @@ def test_step_exchange_equals_three_calls(memory, autotune, lib_built):
             assert a.step_exchange_ptr(n, [x.ctypes.data for x in ins], [x.ctypes.data for x in o]) == n
             for f, x, y in zip(("u", "v", "p", "T"), o, b_out):
                 np.testing.assert_array_equal(x, y, err_msg=f"{f} round {rnd}")
-            for f in ("u", "v", "p", "T", "rho"):
+            for f in ALL_FIELDS:
                 np.testing.assert_array_equal(a.field(f), b.field(f), err_msg=f"{f} round {rnd}")
             if o is outs:
                 for x, y in zip(ins, outs):
                     x[...] = y
         a.close()
         b.close()
+
+
+@pytest.mark.parametrize("which", ["channel", "jump_walls", "periodic_box"])
+def test_one_step_exchanges_match_oracle(which, lib_built, oracle_built):
+    """One step per sts_step_exchange call with pinned buffers: the new state goes out to the host
+    beside the flux kernel and the zero-gradient copies of p and T move into the boundary kernel.
+    Every array after every step, the statistics and the sweep counts equal the oracle's, and the
+    state that comes out is the library's state (the ratio-corrected jump walls write p and T on
+    the walls; the periodic box wraps)."""
+    torch = pytest.importorskip("torch")
+    import ora
+    import sts
+    if which == "channel":
+        case = sc.channel_case("c", 120, 12, 0.5, 0.002, 1e-3, 20)
+    elif which == "jump_walls":
+        case = ratio_corrected_example(20)
+    else:
+        case = sc.config_case("rayleigh_benard", scale=0.125, Nt=20)
+    with tempfile.TemporaryDirectory() as d:
+        case.write(d)
+        o = ora.Oracle(d, fixed_sweeps=False)
+        g = sts.Solver(d, fixed_sweeps=False, autotune=False)  # every step in the graph
+        assert g.step(2) == o.step(2) == 2
+        ts = [torch.empty((g.Ny, g.Nx), dtype=torch.float64).pin_memory() for _ in range(8)]
+        ins, outs = [t.numpy() for t in ts[:4]], [t.numpy() for t in ts[4:]]
+        g.get_state_ptr(*[x.ctypes.data for x in ins])
+        for k in range(6):
+            assert g.step_exchange_ptr(1, [x.ctypes.data for x in ins], [x.ctypes.data for x in outs]) == 1
+            assert o.step(1) == 1
+            for f in ALL_FIELDS:
+                np.testing.assert_array_equal(g.field(f), o.field(f), err_msg=f"step {k + 3} {f}")
+            for f, x in zip(("u", "v", "p", "T"), outs):
+                np.testing.assert_array_equal(x, o.field(f), err_msg=f"state out, step {k + 3} {f}")
+            np.testing.assert_array_equal(g.stats(), o.stats())
+            ins, outs = outs, ins
+        np.testing.assert_array_equal(g.sweep_history(), o.sweeps())
+        g.close()
 
 
 @pytest.mark.parametrize("memory", ["pageable", "pinned"])
