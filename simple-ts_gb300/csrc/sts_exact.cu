@@ -1039,20 +1039,25 @@ __device__ void do_slip_u(const Geo& g, int k) {
   const uint8_t fin = g.slip_u_fin[k];
   const int j = node / Nx, i = node - j * Nx;
   const Nb d = neighbours(i, j, Nx, Ny, per);
-  const Body& Bd = g.bodies[g.vol_id[d.ij] - 1];
+  // the static operands of both sides (below / above) loaded together, before the choice, so
+  // that the entry's loads do not wait on one another; u keeps its place in the reference's order
+  const int vid = g.vol_id[d.ij], vid_s = g.vol_id[d.ij_1];
+  const int jm = j - (0 < j ? 1 : 0), jp = j + (j < (Ny - 1) ? 1 : 0);
+  const double hym = g.hy[jm], hyp = g.hy[jp];
+  const double ru_s0 = g.rho_u[d.ij_1], ru_s1 = g.rho_u[d.i1j_1], ru_n0 = g.rho_u[d.ij1], ru_n1 = g.rho_u[d.i1j1];
+  const bool f_s0 = fl(d.i_1j_1), f_s1 = fl(d.i1j_1), f_n0 = fl(d.i_1j1), f_n1 = fl(d.i1j1);
+  const Body& Bd = g.bodies[vid - 1];
   const double FK = Bd.F_slip * g.Kn;
-  if (g.vol_id[d.ij_1] == 0) {
-    const int jm = j - (0 < j ? 1 : 0);
-    const double a_ij = kl ? FK / (g.rho_u[d.ij_1] * 0.5 * g.hy[jm]) : FK / (0.5 * g.hy[jm]);
-    const double a_i1j = kl ? FK / (g.rho_u[d.i1j_1] * 0.5 * g.hy[jm]) : FK / (0.5 * g.hy[jm]);
-    if ((fin & 1) && fl(d.i_1j_1)) u[d.ij] = div_z(u[d.ij_1] * a_ij + Bd.u, 1.0 + a_ij);
-    if ((fin & 2) && fl(d.i1j_1)) u[d.i1j] = div_z(u[d.i1j_1] * a_i1j + Bd.u, 1.0 + a_i1j);
+  if (vid_s == 0) {
+    const double a_ij = kl ? FK / (ru_s0 * 0.5 * hym) : FK / (0.5 * hym);
+    const double a_i1j = kl ? FK / (ru_s1 * 0.5 * hym) : FK / (0.5 * hym);
+    if ((fin & 1) && f_s0) u[d.ij] = div_z(u[d.ij_1] * a_ij + Bd.u, 1.0 + a_ij);
+    if ((fin & 2) && f_s1) u[d.i1j] = div_z(u[d.i1j_1] * a_i1j + Bd.u, 1.0 + a_i1j);
   } else {
-    const int jp = j + (j < (Ny - 1) ? 1 : 0);
-    const double a_ij = kl ? FK / (g.rho_u[d.ij1] * 0.5 * g.hy[jp]) : FK / (0.5 * g.hy[jp]);
-    const double a_i1j = kl ? FK / (g.rho_u[d.i1j1] * 0.5 * g.hy[jp]) : FK / (0.5 * g.hy[jp]);
-    if ((fin & 1) && fl(d.i_1j1)) u[d.ij] = div_z(u[d.ij1] * a_ij + Bd.u, 1.0 + a_ij);
-    if ((fin & 2) && fl(d.i1j1)) u[d.i1j] = div_z(u[d.i1j1] * a_i1j + Bd.u, 1.0 + a_i1j);
+    const double a_ij = kl ? FK / (ru_n0 * 0.5 * hyp) : FK / (0.5 * hyp);
+    const double a_i1j = kl ? FK / (ru_n1 * 0.5 * hyp) : FK / (0.5 * hyp);
+    if ((fin & 1) && f_n0) u[d.ij] = div_z(u[d.ij1] * a_ij + Bd.u, 1.0 + a_ij);
+    if ((fin & 2) && f_n1) u[d.i1j] = div_z(u[d.i1j1] * a_i1j + Bd.u, 1.0 + a_i1j);
   }
 }
 
@@ -1069,18 +1074,23 @@ __device__ void do_slip_v(const Geo& g, int k) {
   const uint8_t fin = g.slip_v_fin[k];
   const int j = node / Nx, i = node - j * Nx;
   const Nb d = neighbours(i, j, Nx, Ny, per);
-  const Body& Bd = g.bodies[g.vol_id[d.ij] - 1];
+  // as in do_slip_u: both sides' static operands (left / right) loaded together
+  const int vid = g.vol_id[d.ij], vid_w = g.vol_id[d.i_1j];
+  const double hxw = g.hx[d.i_1], hxe = g.hx[d.i1];
+  const double rv_w0 = g.rho_v[d.i_1j], rv_w1 = g.rho_v[d.i_1j1], rv_e0 = g.rho_v[d.i1j], rv_e1 = g.rho_v[d.i1j1];
+  const bool f_w0 = fl(d.i_1j_1), f_w1 = fl(d.i_1j1), f_e0 = fl(d.i1j_1), f_e1 = fl(d.i1j1);
+  const Body& Bd = g.bodies[vid - 1];
   const double FK = Bd.F_slip * g.Kn;
-  if (g.vol_id[d.i_1j] == 0) {
-    const double a_ij = kl ? FK / (g.rho_v[d.i_1j] * 0.5 * g.hx[d.i_1]) : FK / (0.5 * g.hx[d.i_1]);
-    const double a_ij1 = kl ? FK / (g.rho_v[d.i_1j1] * 0.5 * g.hx[d.i_1]) : FK / (0.5 * g.hx[d.i_1]);
-    if ((fin & 1) && fl(d.i_1j_1)) v[d.ij] = div_z(v[d.i_1j] * a_ij + Bd.v, 1.0 + a_ij);
-    if ((fin & 2) && fl(d.i_1j1)) v[d.ij1] = div_z(v[d.i_1j1] * a_ij1 + Bd.v, 1.0 + a_ij1);
+  if (vid_w == 0) {
+    const double a_ij = kl ? FK / (rv_w0 * 0.5 * hxw) : FK / (0.5 * hxw);
+    const double a_ij1 = kl ? FK / (rv_w1 * 0.5 * hxw) : FK / (0.5 * hxw);
+    if ((fin & 1) && f_w0) v[d.ij] = div_z(v[d.i_1j] * a_ij + Bd.v, 1.0 + a_ij);
+    if ((fin & 2) && f_w1) v[d.ij1] = div_z(v[d.i_1j1] * a_ij1 + Bd.v, 1.0 + a_ij1);
   } else {
-    const double a_ij = kl ? FK / (g.rho_v[d.i1j] * 0.5 * g.hx[d.i1]) : FK / (0.5 * g.hx[d.i1]);
-    const double a_ij1 = kl ? FK / (g.rho_v[d.i1j1] * 0.5 * g.hx[d.i1]) : FK / (0.5 * g.hx[d.i1]);
-    if ((fin & 1) && fl(d.i1j_1)) v[d.ij] = div_z(v[d.i1j] * a_ij + Bd.v, 1.0 + a_ij);
-    if ((fin & 2) && fl(d.i1j1)) v[d.ij1] = div_z(v[d.i1j1] * a_ij1 + Bd.v, 1.0 + a_ij1);
+    const double a_ij = kl ? FK / (rv_e0 * 0.5 * hxe) : FK / (0.5 * hxe);
+    const double a_ij1 = kl ? FK / (rv_e1 * 0.5 * hxe) : FK / (0.5 * hxe);
+    if ((fin & 1) && f_e0) v[d.ij] = div_z(v[d.i1j] * a_ij + Bd.v, 1.0 + a_ij);
+    if ((fin & 2) && f_e1) v[d.ij1] = div_z(v[d.i1j1] * a_ij1 + Bd.v, 1.0 + a_ij1);
   }
 }
 
@@ -1098,17 +1108,26 @@ __device__ void do_tjump(const Geo& g, const double* __restrict__ T, int k) {
   const Nb d = neighbours(i, j, Nx, Ny, per);
   const int nb[4] = {d.i_1j, d.i1j, d.ij_1, d.ij1};
   const int dst[4] = {d.ij, d.i1j, d.ij, d.ij1};
+  // every operand of the four sides loaded together (T and rho are not written here), so that the
+  // sides do not wait on one another's loads
+  bool fluid[4];
+  int vid[4];
   for (int q = 0; q < 4; q++) {
-    if (fl(nb[q]) || !(fin & (1 << q))) continue;
-    const Body& Bd = g.bodies[g.vol_id[nb[q]] - 1];
+    fluid[q] = fl(nb[q]);
+    vid[q] = g.vol_id[nb[q]];
+  }
+  const double Tc = T[d.ij], rc = g.rho[d.ij], hxi = g.hx[i], hyj = g.hy[j];
+  for (int q = 0; q < 4; q++) {
+    if (fluid[q] || !(fin & (1 << q))) continue;
+    const Body& Bd = g.bodies[vid[q] - 1];
     double* out = (q < 2) ? g.Tw_u : g.Tw_v;
     double val;
     if (Bd.jump) {
-      const double FK = kl ? (Bd.F_jump * g.Kn) / g.rho[d.ij] : Bd.F_jump * g.Kn;
-      const double a = FK / (0.5 * ((q < 2) ? g.hx[i] : g.hy[j]));
-      val = (a * T[d.ij] + Bd.T) / (1.0 + a);
+      const double FK = kl ? (Bd.F_jump * g.Kn) / rc : Bd.F_jump * g.Kn;
+      const double a = FK / (0.5 * ((q < 2) ? hxi : hyj));
+      val = (a * Tc + Bd.T) / (1.0 + a);
     } else if (Bd.dTdn0 != 0) {
-      val = T[d.ij];
+      val = Tc;
     } else {
       val = Bd.T;
     }
