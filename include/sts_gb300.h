@@ -51,9 +51,9 @@ typedef struct sts_options {
    * 2: as 1, and the p-T sweeps of the tolerance-terminated loop run in FP32 on correction
    *    fields over FP64 base fields; the sweep that meets the tolerance is recomputed in FP64,
    *    so the stopping residual is an FP64 update.  Fixed sweep counts run as mode 1.
-   * 3: as 2, with the FP64 arithmetic of the assembly, the flux/diffusion kernel and the FP64
-   *    sweeps done in double-float (pairs of FP32 numbers, about 47 significant bits) on the FP32
-   *    pipes; fields stay FP64 in memory. */
+   * 3: as 2, with the FP64 arithmetic of the assembly, the velocity correction, the
+   *    flux/diffusion kernel and the FP64 sweeps done in double-float (pairs of FP32 numbers,
+   *    about 47 significant bits) on the FP32 pipes; fields stay FP64 in memory. */
   int precision;
   /* Initial iterate of every step's p-T sweeps (no counterpart in the reference, which starts from
    * the previous step's p and T):
