@@ -132,3 +132,15 @@ def test_entered_data_roundtrip():
         back = sc.read_entered_data(p)
         for k, v in e.items():
             assert back[k] == pytest.approx(float(v)), k
+
+
+def test_missing_library_fails_loudly(lib_built):
+    """The Python binding has no fallback: without the compiled library it raises at load."""
+    import sts
+    saved = sts._lib
+    try:
+        sts._lib = None
+        with pytest.raises(FileNotFoundError, match="no fallback"):
+            sts.load(os.path.join(tempfile.gettempdir(), "no_such_dir", "libsts_gb300.so"))
+    finally:
+        sts._lib = saved
